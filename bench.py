@@ -1,0 +1,394 @@
+"""BVH traversal benchmark: Mrays/s closest-hit + any-hit on one GB300 (per GPU under torchrun).
+
+Workload (the traversal microbenchmark scene, FP32):
+  scene   1024 x 1024-cell fBm heightfield (2,097,152 triangles, amplitude 0.2, 6 octaves, seed 1)
+          + 200,000 random triangles (centres U([-1,1]x[0,0.5]x[-1,1]), vertex offsets N(0, 0.01^2))
+          = 2,297,152 triangles; binned SAH (32 bins, leaves <= 3) collapsed to 8-wide nodes.
+  rays    16,777,216 per step: 8,388,608 primary (4096 x 2048 pinhole at (0,1.5,-2.5) aimed at the
+          origin, 30 degree vertical FOV), 4,194,304 cosine-hemisphere bounce rays from primary hits,
+          4,194,304 any-hit shadow rays to uniform points on a 0.5 x 0.5 quad at y = 2
+          (tmax = distance - 1e-4).
+A step = the three launches over the resident batch (closest primary, closest bounce, any shadow).
+The ray batch (604 MB in, 196 MB out per step) is larger than L2, so no extra flush is done.
+
+--impl reference times the reference's CPU traversal instead (the reference's own code from
+oracle/_ref where it was compiled for this machine, else the oracle's restatement of it) on all
+host cores over a bounded sample of the same batch.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "hiprt-path-tracer_gb300"))
+
+METRIC = "Mrays/s closest-hit (BVH traversal, 16M-ray batch: 8M primary + 4M bounce closest-hit, 4M shadow any-hit)"
+UNIT = "Mrays/s"
+WIDTH, HEIGHT, VFOV = 4096, 2048, 30.0
+N_BOUNCE = 4 * 1024 * 1024
+N_SHADOW = 4 * 1024 * 1024
+RAY_IN_BYTES = 36  # origin+tmin, direction+tmax, last_prim
+CLOSEST_OUT_BYTES = 16
+ANY_OUT_BYTES = 1
+NODE_BYTES = 80
+TRI_BYTES = 36  # algorithmic: three float3 vertex records
+
+
+def workload_config(n_tris):
+    return {"workload": "bvh-traversal-microbench", "triangles": n_tris, "rays_per_step": 8388608 + N_BOUNCE + N_SHADOW,
+            "primary": f"{WIDTH}x{HEIGHT} pinhole, vfov {VFOV} deg", "bounce": N_BOUNCE, "shadow_any_hit": N_SHADOW,
+            "bvh": "binned SAH 32 bins, leaf<=3, 8-wide quantised (80 B nodes)",
+            "l2": "inputs larger than L2 (604 MB of rays per step); no flush"}
+
+
+def build_workload(seed=1, log=print):
+    """Scene + 16M-ray batch (numpy). Bounce/shadow rays need primary hits: traced on the GPU when
+    a BVH is given, else (reference arm) on a CPU structure."""
+    from gbpt import scenes
+    t0 = time.time()
+    mesh = scenes.traversal_scene(cells=1024, n_random=200_000, seed=seed)
+    log(f"scene: {mesh.n_triangles} triangles in {time.time() - t0:.1f}s")
+    primary = scenes.pinhole_rays(WIDTH, HEIGHT, vfov_deg=VFOV)
+    return mesh, primary
+
+
+def secondary_rays(mesh, primary, primary_hits, seed=1):
+    from gbpt import scenes
+    pts, nrm, prim = scenes.hit_points_normals(mesh, primary, primary_hits)
+    hit_idx = np.nonzero(prim >= 0)[0]
+    rng = np.random.Generator(np.random.PCG64(seed + 100))
+    pick_b = rng.choice(hit_idx, N_BOUNCE, replace=len(hit_idx) < N_BOUNCE)
+    pick_s = rng.choice(hit_idx, N_SHADOW, replace=len(hit_idx) < N_SHADOW)
+    bounce = scenes.bounce_rays(pts[pick_b], nrm[pick_b], prim[pick_b], seed=seed + 2)
+    shadow, _ = scenes.shadow_rays(pts[pick_s], prim[pick_s], seed=seed + 3)
+    return bounce, shadow
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        rows = [l.split(", ") for (t, l) in self.lines if t0 <= t <= t1 + 0.15]
+        rows = [r for r in rows if len(r) >= 10]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[6 + k].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[4]) for r in rows if r[4].replace(".", "").isdigit()) if rows else None}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per closest-hit ray from the committed ncu summary, if present."""
+    path = os.path.join(REPO, "profiles", "trace_closest_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_ray="):
+                return float(line.split("=")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline_sample(mesh, primary, bounce, shadow, frac, log=print):
+    """Times the reference CPU traversal on a strided sample of each ray class (all host cores)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    soup = mesh.triangle_soup()
+    kind = "port"
+    cores = os.cpu_count() or 1
+    impl = None
+    if pyoracle.ref_available():
+        try:
+            ref = pyoracle.RefBVH(soup)
+            impl = (lambda r: ref.closest(r), lambda r: ref.shadow_occluded(
+                r, (r.dir_tmax[:, 3] + np.float32(1e-4)).astype(np.float32)))
+            kind = "reference"
+        except OSError:
+            impl = None
+    if impl is None:
+        orc = pyoracle.Oracle()
+        t0 = time.time()
+        oc = orc.octree(soup)
+        log(f"oracle octree build {time.time() - t0:.1f}s ({oc.node_count} nodes)")
+        impl = (lambda r: oc.closest(r, nthreads=cores), lambda r: oc.occluded(r, nthreads=cores))
+    step = max(1, int(round(1.0 / frac)))
+    samples = [primary.slice(slice(0, None, step)), bounce.slice(slice(0, None, step)),
+               shadow.slice(slice(0, None, step))]
+    n = sum(len(s) for s in samples)
+    t0 = time.perf_counter()
+    impl[0](samples[0])
+    impl[0](samples[1])
+    impl[1](samples[2])
+    dt = time.perf_counter() - t0
+    return {"value": n / dt / 1e6, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"every {step}th ray of each class ({n} rays: {len(samples[0])} primary, {len(samples[1])} bounce, "
+                      f"{len(samples[2])} shadow), {dt:.2f}s"}, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    mesh, primary = build_workload(log=lambda *a: print(*a, file=sys.stderr))
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    # primary hits for the secondary rays come from the CPU structure itself on this arm
+    orc = pyoracle.Oracle()
+    oc = orc.octree(mesh.triangle_soup())
+    step = 8
+    prim_hits = np.zeros((len(primary), 4), np.float32)
+    prim_hits[:, 3] = np.int32(-1).view(np.float32)
+    sl = slice(0, None, step)
+    prim_hits[sl] = oc.closest(primary.slice(sl))
+    bounce, shadow = secondary_rays(mesh, primary.slice(sl), prim_hits[sl])
+    frac = args.ref_fraction
+    for _ in range(args.warmup):
+        cpu_baseline_sample(mesh, primary, bounce, shadow, frac / 4, log=lambda *a: None)
+    vals, times = [], []
+    base = None
+    for _ in range(args.steps):
+        base, dt = cpu_baseline_sample(mesh, primary, bounce, shadow, frac, log=lambda *a: None)
+        vals.append(base["value"])
+        times.append(dt)
+    value = statistics.median(vals)
+    base["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * statistics.median(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene and rays)",
+            "config": workload_config(mesh.n_triangles), "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-fraction", type=float, default=0.5)
+    ap.add_argument("--ref-fraction", type=float, default=1.0 / 256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import gbpt
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    def log(*a):
+        if rank == 0:
+            print(*a, file=sys.stderr)
+
+    gbpt.load()
+    mesh, primary = build_workload(log=log)
+    t0 = time.time()
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    st = bvh.stats()
+    log(f"bvh: {st['n_nodes']} nodes, depth {st['wide_depth']}, build {st['build_seconds']:.2f}s "
+        f"(wall {time.time() - t0:.2f}s)")
+
+    def to_dev(r):
+        return (torch.from_numpy(r.origin_tmin).to(dev), torch.from_numpy(r.dir_tmax).to(dev),
+                torch.from_numpy(r.last_prim).to(dev))
+
+    P = to_dev(primary)
+    hits_p = bvh.closest(*P)
+    torch.cuda.synchronize()
+    bounce, shadow = secondary_rays(mesh, primary, hits_p.cpu().numpy())
+    B, S = to_dev(bounce), to_dev(shadow)
+    hits_b = torch.empty((len(bounce), 4), dtype=torch.float32, device=dev)
+    occ_s = torch.empty((len(shadow),), dtype=torch.uint8, device=dev)
+    n_rays = len(primary) + len(bounce) + len(shadow)
+    hit_frac = float((gbpt.hit_prim(hits_p) >= 0).float().mean())
+
+    # traversal statistics (counting build of the same kernels on the same batch)
+    cp = bvh.count(*P)
+    cb = bvh.count(*B)
+    cs = bvh.count(*S, any_hit=True)
+    alg_closest = (len(primary) + len(bounce)) * (RAY_IN_BYTES + CLOSEST_OUT_BYTES) + \
+        (cp[0] + cb[0]) * NODE_BYTES + (cp[1] + cb[1]) * TRI_BYTES
+    alg_any = len(shadow) * (RAY_IN_BYTES + ANY_OUT_BYTES) + cs[0] * NODE_BYTES + cs[1] * TRI_BYTES
+
+    stream = torch.cuda.current_stream()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+
+    def step(e=None):
+        if e is not None:
+            e[0].record(stream)
+        bvh.closest(*P, out=hits_p)
+        if e is not None:
+            e[1].record(stream)
+        bvh.closest(*B, out=hits_b)
+        if e is not None:
+            e[2].record(stream)
+        bvh.occluded(*S, out=occ_s)
+        if e is not None:
+            e[3].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(1.0)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for k in range(args.steps):
+        step(ev[k])
+    end.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    t_wall1 = time.time()
+    time.sleep(0.3)
+    sampler.stop()
+    total_ms = start.elapsed_time(end)
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    closest_ms = sum(e[0].elapsed_time(e[2]) for e in ev) / args.steps
+    primary_ms = sum(e[0].elapsed_time(e[1]) for e in ev) / args.steps
+    bounce_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / args.steps
+    any_ms = sum(e[2].elapsed_time(e[3]) for e in ev) / args.steps
+    value = world * n_rays / (ms_step * 1e-3) / 1e6
+    clocks = sampler.summary(t_wall0, t_wall1)
+
+    # end to end through the host-buffer C entry points (pinned host memory, copies in the call)
+    hp = [torch.from_numpy(x).pin_memory() for x in (primary.origin_tmin, primary.dir_tmax, primary.last_prim)]
+    hb = [torch.from_numpy(x).pin_memory() for x in (bounce.origin_tmin, bounce.dir_tmax, bounce.last_prim)]
+    hs = [torch.from_numpy(x).pin_memory() for x in (shadow.origin_tmin, shadow.dir_tmax, shadow.last_prim)]
+    out_p = torch.empty((len(primary), 4), dtype=torch.float32).pin_memory()
+    out_b = torch.empty((len(bounce), 4), dtype=torch.float32).pin_memory()
+    out_s = torch.empty((len(shadow),), dtype=torch.uint8).pin_memory()
+
+    def e2e_step():
+        bvh.closest_host(*hp, out=out_p.numpy())
+        bvh.closest_host(*hb, out=out_b.numpy())
+        bvh.occluded_host(*hs, out=out_s.numpy())
+
+    for _ in range(2):
+        e2e_step()
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    assert np.array_equal(out_p.numpy().view(np.uint32), hits_p.cpu().numpy().view(np.uint32))
+
+    peak, peak_kind = measured_peaks()
+    achieved = alg_closest / (closest_ms * 1e-3) / 1e9
+    traffic_per_ray = ncu_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded procedural scene and rays)", "config": workload_config(mesh.n_triangles),
+        "breakdown": {"primary_mrays_s": len(primary) / primary_ms / 1e3, "bounce_mrays_s": len(bounce) / bounce_ms / 1e3,
+                      "shadow_mrays_s": len(shadow) / any_ms / 1e3, "primary_hit_fraction": hit_frac,
+                      "nodes_per_ray": {"primary": cp[0] / len(primary), "bounce": cb[0] / len(bounce),
+                                        "shadow": cs[0] / len(shadow)},
+                      "tris_per_ray": {"primary": cp[1] / len(primary), "bounce": cb[1] / len(bounce),
+                                       "shadow": cs[1] / len(shadow)},
+                      "bvh_build_s": st["build_seconds"], "bvh_nodes": st["n_nodes"], "bvh_depth": st["wide_depth"]},
+        "roofline": {"bound": "hbm", "kernel": "trace_kernel<closest> (primary + bounce launches)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_launch": alg_closest / 2,
+                     "traffic": (traffic_per_ray * (len(primary) + len(bounce)) / 2) if traffic_per_ray else None},
+        "e2e": {"value": world * n_rays / e2e_s / 1e6, "unit": UNIT,
+                "h2d_bytes_per_step": n_rays * RAY_IN_BYTES,
+                "d2h_bytes_per_step": (len(primary) + len(bounce)) * CLOSEST_OUT_BYTES + len(shadow) * ANY_OUT_BYTES},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        base, _ = cpu_baseline_sample(mesh, primary, bounce, shadow, args.cpu_fraction, log=log)
+        line["cpu_baseline"] = base
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,242 @@
+// C ABI of libgbpt: handles, status codes, argument checks and launches (declared in include/gbpt.h).
+//
+// Replaces the reference's host-side launch layer for the intersection path: HIPRTGeometry
+// (src/HIPRT-Orochi/HIPRTScene.h:87-202) and the traversal calls made from
+// src/Device/includes/Intersect.h. Every failure is returned as a gbpt_status with a
+// thread-local message; nothing exits, aborts or traps.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/gbpt.h"
+#include "bvh.h"
+#include "trace_kernels.h"
+
+struct gbpt_bvh
+{
+    gbpt::DeviceBVH dev;
+    gbpt_bvh_stats stats;
+    int device = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gbpt_status fail(gbpt_status s, const std::string& msg)
+{
+    g_last_error = msg;
+    return s;
+}
+
+gbpt_status cuda_fail(cudaError_t e, const char* what)
+{
+    gbpt_status s = (e == cudaErrorMemoryAllocation) ? GBPT_ERROR_OOM : GBPT_ERROR_CUDA;
+    return fail(s, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+gbpt_status check_rays(const gbpt_bvh* bvh, const float* o, const float* d, int64_t n)
+{
+    if (!bvh) return fail(GBPT_ERROR_INVALID_ARG, "bvh is NULL");
+    if (n < 0) return fail(GBPT_ERROR_INVALID_ARG, "n_rays is negative");
+    if (n > 0 && (!o || !d)) return fail(GBPT_ERROR_INVALID_ARG, "ray buffers are NULL");
+    if (!aligned16(o) || !aligned16(d)) return fail(GBPT_ERROR_INVALID_ARG, "ray buffers must be 16-byte aligned");
+    if (n > (int64_t)0x7FFFFFFF * 128) return fail(GBPT_ERROR_INVALID_ARG, "n_rays too large for one launch");
+    return GBPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbpt_status_string(gbpt_status s)
+{
+    switch (s)
+    {
+    case GBPT_OK: return "ok";
+    case GBPT_ERROR_INVALID_ARG: return "invalid argument";
+    case GBPT_ERROR_OOM: return "out of memory";
+    case GBPT_ERROR_CUDA: return "CUDA error";
+    case GBPT_ERROR_TIMEOUT: return "timeout";
+    case GBPT_ERROR_NAN: return "NaN detected";
+    case GBPT_ERROR_UNSUPPORTED: return "unsupported";
+    case GBPT_ERROR_BVH_TOO_DEEP: return "BVH too deep";
+    }
+    return "unknown status";
+}
+
+const char* gbpt_last_error(void) { return g_last_error.c_str(); }
+
+int32_t gbpt_version(void) { return 1; }
+
+gbpt_status gbpt_bvh_build(const int32_t* indices, const float* positions, int64_t n_vertices, int64_t n_triangles,
+                           const gbpt_bvh_params* params, gbpt_bvh** out)
+{
+    if (!out) return fail(GBPT_ERROR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (n_triangles < 0 || n_vertices < 0) return fail(GBPT_ERROR_INVALID_ARG, "negative sizes");
+    if (n_triangles > 0 && (!indices || !positions)) return fail(GBPT_ERROR_INVALID_ARG, "geometry buffers are NULL");
+
+    gbpt::BuildParams bp;
+    if (params)
+    {
+        if (params->sah_bins) bp.sah_bins = params->sah_bins;
+        if (params->max_leaf_size) bp.max_leaf = params->max_leaf_size;
+        bp.threads = params->num_threads;
+    }
+    gbpt::HostBVH host;
+    bool too_deep = false;
+    std::string err;
+    try
+    {
+        err = gbpt::build_wide_bvh(indices, positions, n_vertices, n_triangles, bp, host, too_deep);
+    }
+    catch (const std::bad_alloc&)
+    {
+        return fail(GBPT_ERROR_OOM, "host allocation failed during the BVH build");
+    }
+    if (!err.empty()) return fail(too_deep ? GBPT_ERROR_BVH_TOO_DEEP : GBPT_ERROR_INVALID_ARG, err);
+
+    auto t0 = std::chrono::steady_clock::now();
+    gbpt_bvh* b = new (std::nothrow) gbpt_bvh();
+    if (!b) return fail(GBPT_ERROR_OOM, "host allocation failed");
+    cudaGetDevice(&b->device);
+    const size_t node_bytes = host.nodes.size() * sizeof(gbpt::WideNode);
+    const size_t tri_bytes = std::max<size_t>(16, host.tris.size() * sizeof(float));
+    void* dn = nullptr;
+    void* dt = nullptr;
+    cudaError_t e = cudaMalloc(&dn, node_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&dt, tri_bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(dn, host.nodes.data(), node_bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !host.tris.empty())
+        e = cudaMemcpy(dt, host.tris.data(), host.tris.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+    {
+        cudaFree(dn);
+        cudaFree(dt);
+        delete b;
+        return cuda_fail(e, "BVH upload");
+    }
+    b->dev.nodes = dn;
+    b->dev.tris = dt;
+    b->dev.n_nodes = (int64_t)host.nodes.size();
+    b->dev.n_tris = (int64_t)(host.tris.size() / 12);
+    std::memset(&b->stats, 0, sizeof(b->stats));
+    b->stats.n_triangles = n_triangles;
+    b->stats.n_bvh_triangles = b->dev.n_tris;
+    b->stats.n_nodes = b->dev.n_nodes;
+    b->stats.n_binary_nodes = host.n_binary_nodes;
+    b->stats.wide_depth = host.wide_depth;
+    b->stats.node_bytes = (int32_t)sizeof(gbpt::WideNode);
+    b->stats.triangle_bytes = 48;
+    b->stats.device_bytes = (int64_t)(node_bytes + tri_bytes);
+    b->stats.build_seconds = host.build_seconds;
+    b->stats.upload_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    *out = b;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_bvh_get_stats(const gbpt_bvh* bvh, gbpt_bvh_stats* out)
+{
+    if (!bvh || !out) return fail(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    *out = bvh->stats;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_bvh_destroy(gbpt_bvh* bvh)
+{
+    if (!bvh) return GBPT_OK;
+    cudaError_t e1 = cudaFree(const_cast<void*>(bvh->dev.nodes));
+    cudaError_t e2 = cudaFree(const_cast<void*>(bvh->dev.tris));
+    delete bvh;
+    if (e1 != cudaSuccess) return cuda_fail(e1, "BVH free");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "BVH free");
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_trace_closest(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                               const int32_t* last_prim, int64_t n_rays, float* hits, void* stream)
+{
+    gbpt_status s = check_rays(bvh, origin_tmin, dir_tmax, n_rays);
+    if (s != GBPT_OK) return s;
+    if (n_rays > 0 && !hits) return fail(GBPT_ERROR_INVALID_ARG, "hits is NULL");
+    if (!aligned16(hits)) return fail(GBPT_ERROR_INVALID_ARG, "hits must be 16-byte aligned");
+    cudaError_t e = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, hits, nullptr, false, nullptr,
+                                       (cudaStream_t)stream);
+    return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "closest-hit launch");
+}
+
+gbpt_status gbpt_trace_any(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                           const int32_t* last_prim, int64_t n_rays, uint8_t* occluded, void* stream)
+{
+    gbpt_status s = check_rays(bvh, origin_tmin, dir_tmax, n_rays);
+    if (s != GBPT_OK) return s;
+    if (n_rays > 0 && !occluded) return fail(GBPT_ERROR_INVALID_ARG, "occluded is NULL");
+    cudaError_t e = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, nullptr, occluded, true,
+                                       nullptr, (cudaStream_t)stream);
+    return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "any-hit launch");
+}
+
+gbpt_status gbpt_trace_count(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                             const int32_t* last_prim, int64_t n_rays, int32_t any_hit, unsigned long long* counters,
+                             void* stream)
+{
+    gbpt_status s = check_rays(bvh, origin_tmin, dir_tmax, n_rays);
+    if (s != GBPT_OK) return s;
+    if (!counters) return fail(GBPT_ERROR_INVALID_ARG, "counters is NULL");
+    cudaError_t e = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, nullptr, nullptr, any_hit != 0,
+                                       counters, (cudaStream_t)stream);
+    return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "counting launch");
+}
+
+static gbpt_status trace_host(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                              const int32_t* last_prim, int64_t n, void* out, bool any_hit, cudaStream_t st)
+{
+    gbpt_status s = check_rays(bvh, origin_tmin, dir_tmax, n);
+    if (s != GBPT_OK) return s;
+    if (n > 0 && !out) return fail(GBPT_ERROR_INVALID_ARG, "output is NULL");
+    if (n == 0) return GBPT_OK;
+    const size_t ray_bytes = (size_t)n * 16;
+    const size_t out_bytes = any_hit ? (size_t)n : (size_t)n * 16;
+    char* buf = nullptr;
+    const size_t lp_off = 2 * ray_bytes;
+    const size_t out_off = lp_off + (((size_t)n * 4 + 255) & ~(size_t)255);
+    cudaError_t e = cudaMallocAsync((void**)&buf, out_off + out_bytes, st);
+    if (e != cudaSuccess) return cuda_fail(e, "scratch allocation");
+    float* d_o = (float*)buf;
+    float* d_d = (float*)(buf + ray_bytes);
+    int32_t* d_lp = last_prim ? (int32_t*)(buf + lp_off) : nullptr;
+    void* d_out = buf + out_off;
+    e = cudaMemcpyAsync(d_o, origin_tmin, ray_bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_d, dir_tmax, ray_bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && d_lp) e = cudaMemcpyAsync(d_lp, last_prim, (size_t)n * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = gbpt::launch_trace(bvh->dev, d_o, d_d, d_lp, n, any_hit ? nullptr : (float*)d_out,
+                               any_hit ? (uint8_t*)d_out : nullptr, any_hit, nullptr, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, st);
+    cudaError_t ef = cudaFreeAsync(buf, st);
+    if (e == cudaSuccess) e = ef;
+    cudaError_t es = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = es;
+    return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "host-buffer trace");
+}
+
+gbpt_status gbpt_trace_closest_host(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                    const int32_t* last_prim, int64_t n_rays, float* hits, void* stream)
+{
+    return trace_host(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits, false, (cudaStream_t)stream);
+}
+
+gbpt_status gbpt_trace_any_host(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                const int32_t* last_prim, int64_t n_rays, uint8_t* occluded, void* stream)
+{
+    return trace_host(bvh, origin_tmin, dir_tmax, last_prim, n_rays, occluded, true, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,444 @@
+// Host BVH builder: binned SAH binary tree, collapsed to 8-wide quantised nodes.
+//
+// Replaces the reference's GPU BVH build through HIPRT (hiprtBuildGeometry in
+// src/HIPRT-Orochi/HIPRTScene.h:87-150 of the reference, whose algorithm lives in the absent HIPRT
+// submodule). The layout follows the compressed wide BVH of Ylitie, Karras and Laine,
+// "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs" (HPG 2017):
+// 8 children per node, 8-bit child boxes relative to a per-node origin and power-of-two scale,
+// children placed in slots by ray octant so that traversal order is near-first.
+#include "bvh.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+
+namespace gbpt {
+namespace {
+
+struct Box
+{
+    float lo[3] = {INFINITY, INFINITY, INFINITY};
+    float hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    void grow(const float* l, const float* h)
+    {
+        for (int a = 0; a < 3; a++)
+        {
+            lo[a] = std::min(lo[a], l[a]);
+            hi[a] = std::max(hi[a], h[a]);
+        }
+    }
+    void grow(const Box& b) { grow(b.lo, b.hi); }
+    float half_area() const
+    {
+        float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        if (!(dx >= 0.0f)) return 0.0f;
+        return dx * dy + dy * dz + dz * dx;
+    }
+};
+
+struct BNode
+{
+    Box box;
+    int32_t left = -1;  // right child = left + 1; -1 marks a leaf
+    int32_t begin = 0;
+    int32_t count = 0;
+};
+
+struct Builder
+{
+    const BuildParams& params;
+    std::vector<float> plo, phi, pc;  // per primitive: box lo/hi and centroid, 3 floats each
+    std::vector<int32_t> idx;         // primitive order (leaves index into it)
+    std::vector<BNode> nodes;
+    std::atomic<int32_t> next_node{1};
+    std::atomic<int> live_threads{0};
+    int max_threads = 1;
+
+    explicit Builder(const BuildParams& p) : params(p) {}
+
+    int32_t alloc_pair() { return next_node.fetch_add(2); }
+
+    void build(int32_t ni, int32_t begin, int32_t end)
+    {
+        BNode& node = nodes[ni];
+        Box box, cbox;
+        for (int32_t i = begin; i < end; i++)
+        {
+            int32_t p = idx[i];
+            box.grow(&plo[3 * p], &phi[3 * p]);
+            cbox.grow(&pc[3 * p], &pc[3 * p]);
+        }
+        node.box = box;
+        const int32_t count = end - begin;
+        if (count <= params.max_leaf)
+        {
+            node.begin = begin;
+            node.count = count;
+            node.left = -1;
+            return;
+        }
+
+        const int B = params.sah_bins;
+        int best_axis = -1, best_split = -1;
+        float best_cost = INFINITY;
+        std::vector<Box> bin_box(B);
+        std::vector<int32_t> bin_cnt(B);
+        std::vector<float> left_area(B), left_cnt(B);
+        for (int a = 0; a < 3; a++)
+        {
+            float ext = cbox.hi[a] - cbox.lo[a];
+            if (!(ext > 0.0f)) continue;
+            float k = B / ext;
+            std::fill(bin_box.begin(), bin_box.end(), Box());
+            std::fill(bin_cnt.begin(), bin_cnt.end(), 0);
+            for (int32_t i = begin; i < end; i++)
+            {
+                int32_t p = idx[i];
+                int b = std::min(B - 1, std::max(0, (int)((pc[3 * p + a] - cbox.lo[a]) * k)));
+                bin_box[b].grow(&plo[3 * p], &phi[3 * p]);
+                bin_cnt[b]++;
+            }
+            Box acc;
+            int32_t n = 0;
+            for (int b = 0; b < B - 1; b++)
+            {
+                acc.grow(bin_box[b]);
+                n += bin_cnt[b];
+                left_area[b] = acc.half_area();
+                left_cnt[b] = (float)n;
+            }
+            acc = Box();
+            n = 0;
+            for (int b = B - 1; b >= 1; b--)
+            {
+                acc.grow(bin_box[b]);
+                n += bin_cnt[b];
+                float lc = left_cnt[b - 1];
+                if (lc <= 0.0f || n == 0) continue;
+                float cost = left_area[b - 1] * lc + acc.half_area() * (float)n;
+                if (cost < best_cost)
+                {
+                    best_cost = cost;
+                    best_axis = a;
+                    best_split = b;
+                }
+            }
+        }
+
+        int32_t mid;
+        if (best_axis < 0)
+        {
+            mid = begin + count / 2;  // all centroids coincide: split the range in half
+        }
+        else
+        {
+            const int a = best_axis;
+            const float k = B / (cbox.hi[a] - cbox.lo[a]);
+            const float lo = cbox.lo[a];
+            auto it = std::partition(idx.begin() + begin, idx.begin() + end, [&](int32_t p) {
+                int b = std::min(B - 1, std::max(0, (int)((pc[3 * p + a] - lo) * k)));
+                return b < best_split;
+            });
+            mid = (int32_t)(it - idx.begin());
+            if (mid == begin || mid == end)
+            {
+                mid = begin + count / 2;
+                std::nth_element(idx.begin() + begin, idx.begin() + mid, idx.begin() + end,
+                                 [&](int32_t x, int32_t y) { return pc[3 * x + a] < pc[3 * y + a]; });
+            }
+        }
+
+        int32_t l = alloc_pair();
+        node.left = l;
+        node.count = 0;
+        if (count > 65536 && live_threads.load() < max_threads)
+        {
+            live_threads++;
+            std::thread t([this, l, begin, mid]() {
+                build(l, begin, mid);
+                live_threads--;
+            });
+            build(l + 1, mid, end);
+            t.join();
+        }
+        else
+        {
+            build(l, begin, mid);
+            build(l + 1, mid, end);
+        }
+    }
+};
+
+struct Child
+{
+    int32_t bnode;
+    bool leaf;
+};
+
+// 2^e as a float, e in [-126, 127].
+float pow2f(int e)
+{
+    uint32_t bits = (uint32_t)(e + 127) << 23;
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+}
+
+}  // namespace
+
+std::string build_wide_bvh(const int32_t* indices, const float* positions, int64_t n_vertices, int64_t n_tris,
+                           const BuildParams& params, HostBVH& out, bool& too_deep)
+{
+    too_deep = false;
+    auto t0 = std::chrono::steady_clock::now();
+    if (n_tris < 0 || n_vertices < 0) return "negative sizes";
+    if (n_tris > (int64_t)std::numeric_limits<int32_t>::max() / 4) return "too many triangles";
+    if (params.max_leaf < 1 || params.max_leaf > kMaxLeafTriangles) return "max_leaf_size must be in 1..3";
+    if (params.sah_bins < 2 || params.sah_bins > 256) return "sah_bins must be in 2..256";
+
+    Builder b(params);
+    b.max_threads = params.threads > 0 ? params.threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    b.plo.resize(3 * n_tris);
+    b.phi.resize(3 * n_tris);
+    b.pc.resize(3 * n_tris);
+    b.idx.reserve(n_tris);
+    for (int64_t t = 0; t < n_tris; t++)
+    {
+        const float* v[3];
+        bool ok = true;
+        for (int k = 0; k < 3; k++)
+        {
+            int32_t vi = indices[3 * t + k];
+            if (vi < 0 || vi >= n_vertices) return "triangle " + std::to_string(t) + " has an out-of-range vertex index";
+            v[k] = positions + 3 * (int64_t)vi;
+            for (int a = 0; a < 3; a++) ok = ok && std::isfinite(v[k][a]);
+        }
+        if (!ok) continue;  // Moller-Trumbore never reports a hit on a non-finite triangle
+        for (int a = 0; a < 3; a++)
+        {
+            float lo = std::min(v[0][a], std::min(v[1][a], v[2][a]));
+            float hi = std::max(v[0][a], std::max(v[1][a], v[2][a]));
+            b.plo[3 * t + a] = lo;
+            b.phi[3 * t + a] = hi;
+            b.pc[3 * t + a] = 0.5f * (lo + hi);
+        }
+        b.idx.push_back((int32_t)t);
+    }
+    const int32_t n_valid = (int32_t)b.idx.size();
+
+    out = HostBVH();
+    out.n_input_triangles = n_tris;
+
+    if (n_valid == 0)
+    {
+        // Empty structure: one node with no children; every ray misses.
+        WideNode root;
+        std::memset(&root, 0, sizeof(root));
+        root.ex = root.ey = root.ez = 127;
+        out.nodes.push_back(root);
+        out.wide_depth = 1;
+        out.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return "";
+    }
+
+    b.nodes.resize(std::max<int64_t>(1, 2 * (int64_t)n_valid));
+    b.build(0, 0, n_valid);
+    out.n_binary_nodes = b.next_node.load();
+
+    // ---- collapse to 8-wide, breadth first ----
+    struct Pending
+    {
+        int32_t wide;
+        int32_t bnode;
+        int depth;
+    };
+    std::vector<Pending> queue;
+    out.nodes.reserve(out.n_binary_nodes / 4 + 16);
+    out.nodes.emplace_back();
+    queue.push_back({0, 0, 1});
+    int max_depth = 1;
+    std::vector<int32_t> order_tris;
+    order_tris.reserve(n_valid);
+
+    for (size_t qi = 0; qi < queue.size(); qi++)
+    {
+        const Pending pend = queue[qi];
+        max_depth = std::max(max_depth, pend.depth);
+        const BNode& bn = b.nodes[pend.bnode];
+
+        Child kids[8];
+        int nk = 0;
+        if (bn.left < 0)
+        {
+            kids[nk++] = {pend.bnode, true};
+        }
+        else
+        {
+            kids[nk++] = {bn.left, b.nodes[bn.left].left < 0};
+            kids[nk++] = {bn.left + 1, b.nodes[bn.left + 1].left < 0};
+            while (nk < 8)
+            {
+                int best = -1;
+                float best_area = -1.0f;
+                for (int i = 0; i < nk; i++)
+                {
+                    if (kids[i].leaf) continue;
+                    float area = b.nodes[kids[i].bnode].box.half_area();
+                    if (area > best_area)
+                    {
+                        best_area = area;
+                        best = i;
+                    }
+                }
+                if (best < 0) break;
+                int32_t l = b.nodes[kids[best].bnode].left;
+                kids[best] = {l, b.nodes[l].left < 0};
+                kids[nk++] = {l + 1, b.nodes[l + 1].left < 0};
+            }
+        }
+
+        // Union box and octant slot assignment (greedy on the offset of each child's centre).
+        Box ub;
+        for (int i = 0; i < nk; i++) ub.grow(b.nodes[kids[i].bnode].box);
+        double cen[3];
+        for (int a = 0; a < 3; a++) cen[a] = 0.5 * ((double)ub.lo[a] + (double)ub.hi[a]);
+        struct Score
+        {
+            double s;
+            int child, slot;
+        };
+        Score scores[64];
+        int ns = 0;
+        for (int i = 0; i < nk; i++)
+        {
+            const Box& cb = b.nodes[kids[i].bnode].box;
+            double off[3];
+            for (int a = 0; a < 3; a++) off[a] = 0.5 * ((double)cb.lo[a] + (double)cb.hi[a]) - cen[a];
+            for (int s = 0; s < 8; s++)
+            {
+                double d = ((s & 4) ? off[0] : -off[0]) + ((s & 2) ? off[1] : -off[1]) + ((s & 1) ? off[2] : -off[2]);
+                scores[ns++] = {d, i, s};
+            }
+        }
+        std::sort(scores, scores + ns, [](const Score& x, const Score& y) {
+            if (x.s != y.s) return x.s > y.s;
+            if (x.child != y.child) return x.child < y.child;
+            return x.slot < y.slot;
+        });
+        int slot_of[8], child_in_slot[8];
+        for (int i = 0; i < 8; i++) { slot_of[i] = -1; child_in_slot[i] = -1; }
+        for (int k = 0; k < ns; k++)
+        {
+            const Score& sc = scores[k];
+            if (slot_of[sc.child] >= 0 || child_in_slot[sc.slot] >= 0) continue;
+            slot_of[sc.child] = sc.slot;
+            child_in_slot[sc.slot] = sc.child;
+        }
+
+        WideNode wn;
+        std::memset(&wn, 0, sizeof(wn));
+
+        // Quantisation frame: origin rounded down below the (slightly padded) union box, per-axis
+        // power-of-two scale with room for a one-step outward margin on every child bound.
+        float p[3];
+        float scale[3];
+        for (int a = 0; a < 3; a++)
+        {
+            double L = ub.lo[a], H = ub.hi[a];
+            double mag = std::max(std::max(std::fabs(L), std::fabs(H)), H - L);
+            double pad = std::max(mag * std::ldexp(1.0, -22), 1e-30);
+            float pf = (float)(L - pad);
+            if ((double)pf > L - pad) pf = std::nextafter(pf, -INFINITY);
+            double ext = (H + pad) - (double)pf;
+            int e = (ext > 0.0) ? (int)std::ceil(std::log2(ext / 253.0)) : -100;
+            while (std::ldexp(253.0, e) < ext) e++;
+            e = std::max(-100, std::min(100, e));
+            p[a] = pf;
+            scale[a] = pow2f(e);
+            (&wn.ex)[a] = (uint8_t)(e + 127);
+        }
+        wn.px = p[0];
+        wn.py = p[1];
+        wn.pz = p[2];
+
+        uint8_t* qlo[3] = {wn.qlo_x, wn.qlo_y, wn.qlo_z};
+        uint8_t* qhi[3] = {wn.qhi_x, wn.qhi_y, wn.qhi_z};
+        wn.child_base = (uint32_t)out.nodes.size();
+        wn.tri_base = (uint32_t)order_tris.size();
+        uint32_t tri_off = 0;
+        uint8_t imask = 0;
+        for (int s = 0; s < 8; s++)
+        {
+            int ci = child_in_slot[s];
+            if (ci < 0) continue;
+            const BNode& cn = b.nodes[kids[ci].bnode];
+            for (int a = 0; a < 3; a++)
+            {
+                double lo = std::floor(((double)cn.box.lo[a] - (double)p[a]) / (double)scale[a]) - 1.0;
+                double hi = std::ceil(((double)cn.box.hi[a] - (double)p[a]) / (double)scale[a]) + 1.0;
+                qlo[a][s] = (uint8_t)std::max(0.0, std::min(255.0, lo));
+                qhi[a][s] = (uint8_t)std::max(0.0, std::min(255.0, hi));
+            }
+            if (kids[ci].leaf)
+            {
+                uint32_t cnt = (uint32_t)cn.count;
+                static const uint8_t unary[4] = {0, 1, 3, 7};
+                wn.meta[s] = (uint8_t)((unary[cnt] << 5) | tri_off);
+                for (int32_t k = 0; k < cn.count; k++) order_tris.push_back(b.idx[cn.begin + k]);
+                tri_off += cnt;
+            }
+            else
+            {
+                wn.meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
+                imask |= (uint8_t)(1u << s);
+                int32_t wi = (int32_t)out.nodes.size();
+                out.nodes.emplace_back();
+                queue.push_back({wi, kids[ci].bnode, pend.depth + 1});
+            }
+        }
+        wn.imask = imask;
+        out.nodes[pend.wide] = wn;
+    }
+
+    out.wide_depth = max_depth;
+    if (max_depth >= kTraversalStack)
+    {
+        too_deep = true;
+        return "8-wide BVH depth " + std::to_string(max_depth) + " exceeds the traversal stack (" +
+               std::to_string(kTraversalStack) + ")";
+    }
+
+    // ---- triangle records in leaf order ----
+    out.tris.resize(order_tris.size() * 12);
+    for (size_t k = 0; k < order_tris.size(); k++)
+    {
+        int32_t t = order_tris[k];
+        const float* va = positions + 3 * (int64_t)indices[3 * t + 0];
+        const float* vb = positions + 3 * (int64_t)indices[3 * t + 1];
+        const float* vc = positions + 3 * (int64_t)indices[3 * t + 2];
+        float* r = &out.tris[12 * k];
+        r[0] = va[0];
+        r[1] = va[1];
+        r[2] = va[2];
+        std::memcpy(&r[3], &t, 4);
+        // volatile stores keep the compiler from contracting or reassociating the edge subtraction
+        volatile float e;
+        for (int a = 0; a < 3; a++)
+        {
+            e = vb[a] - va[a];
+            r[4 + a] = e;
+            e = vc[a] - va[a];
+            r[8 + a] = e;
+        }
+        r[7] = 0.0f;
+        r[11] = 0.0f;
+    }
+    out.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return "";
+}
+
+}  // namespace gbpt

@@ -1,0 +1,223 @@
+// Traversal core of the 8-wide compressed BVH, shared by the CUDA kernels (trace.cu) and the
+// host-compiled test harness that checks the builder and traversal logic on machines without a GPU
+// (tests/native/traverse_emu.cpp). Under nvcc it compiles to device code; under a host compiler the
+// rounding intrinsics map to plain IEEE float operations (the host build uses -ffp-contract=off).
+//
+// Replaces hiprtGeomTraversalClosest / hiprtGeomTraversalAnyHit and the filter function of the
+// reference (src/Device/includes/Intersect.h:22-69,200-324, src/Device/functions/FilterFunction.h:
+// 22-75; GB300 has no RT cores, so traversal is software). Traversal order follows Ylitie et al.
+// (HPG 2017): node groups (child base + 8 hit bits + internal-child mask) on a per-thread stack,
+// children visited nearest-first through the octant slot order, triangle hits from a 24-bit mask.
+//
+// The triangle test is the reference's Moller-Trumbore (src/Renderer/Triangle.h:20-63) written
+// with explicitly rounded operations (__fmul_rn/__fadd_rn/__fsub_rn/__fdiv_rn), which the compiler
+// never contracts into FMAs, so t/u/v match the reference's CPU results bit for bit. Box tests use
+// FMAs and a small relative slack: they only prune, so their rounding cannot change a result as
+// long as they stay conservative.
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "bvh.h"
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#define GBPT_HD __device__ __forceinline__
+#define GBPT_LDG(p) __ldg(p)
+#else
+#include <cmath>
+#include <cstring>
+#define GBPT_HD inline
+#define GBPT_LDG(p) (*(p))
+struct uint2 { uint32_t x, y; };
+struct uint4 { uint32_t x, y, z, w; };
+struct float4 { float x, y, z, w; };
+inline uint2 make_uint2(uint32_t x, uint32_t y) { return uint2{x, y}; }
+inline float4 make_float4(float x, float y, float z, float w) { return float4{x, y, z, w}; }
+inline float __fmul_rn(float a, float b) { return a * b; }
+inline float __fadd_rn(float a, float b) { return a + b; }
+inline float __fsub_rn(float a, float b) { return a - b; }
+inline float __fdiv_rn(float a, float b) { return a / b; }
+inline float __frcp_rn(float a) { return 1.0f / a; }
+inline float __uint_as_float(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline float __int_as_float(int32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline int32_t __float_as_int(float f) { int32_t u; std::memcpy(&u, &f, 4); return u; }
+inline uint32_t __clz(uint32_t x) { return x ? (uint32_t)__builtin_clz(x) : 32u; }
+inline uint32_t __popc(uint32_t x) { return (uint32_t)__builtin_popcount(x); }
+inline int __ffs(uint32_t x) { return __builtin_ffs((int)x); }
+using ::copysignf;
+using ::fabsf;
+using ::fmaf;
+using ::fmaxf;
+using ::fminf;
+#endif
+
+namespace gbpt {
+namespace core {
+
+constexpr float kMtEps = 0.0000001f;     // EPSILON of src/Renderer/Triangle.h:24
+constexpr float kBoxSlack = 1.0f / 131072.0f;  // relative widening of box slab intervals (2^-17)
+
+GBPT_HD float dot_rn(float ax, float ay, float az, float bx, float by, float bz)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+GBPT_HD void cross_rn(float ax, float ay, float az, float bx, float by, float bz, float& cx, float& cy,
+                                         float& cz)
+{
+    cx = __fsub_rn(__fmul_rn(ay, bz), __fmul_rn(az, by));
+    cy = __fsub_rn(__fmul_rn(az, bx), __fmul_rn(ax, bz));
+    cz = __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
+}
+
+// Moller-Trumbore in the reference's operation order. Returns true with t/u/v on a hit.
+GBPT_HD bool mt_test(const float4 a, const float4 e1, const float4 e2, float ox, float oy, float oz,
+                                        float dx, float dy, float dz, float& t, float& u, float& v)
+{
+    float hx, hy, hz;
+    cross_rn(dx, dy, dz, e2.x, e2.y, e2.z, hx, hy, hz);
+    const float det = dot_rn(e1.x, e1.y, e1.z, hx, hy, hz);
+    if (det > -kMtEps && det < kMtEps) return false;
+    const float f = __fdiv_rn(1.0f, det);
+    const float sx = __fsub_rn(ox, a.x), sy = __fsub_rn(oy, a.y), sz = __fsub_rn(oz, a.z);
+    u = __fmul_rn(f, dot_rn(sx, sy, sz, hx, hy, hz));
+    if (u < 0.0f || u > 1.0f) return false;
+    float qx, qy, qz;
+    cross_rn(sx, sy, sz, e1.x, e1.y, e1.z, qx, qy, qz);
+    v = __fmul_rn(f, dot_rn(dx, dy, dz, qx, qy, qz));
+    if (v < 0.0f || __fadd_rn(u, v) > 1.0f) return false;
+    t = __fmul_rn(f, dot_rn(e2.x, e2.y, e2.z, qx, qy, qz));
+    return t > kMtEps;
+}
+
+GBPT_HD float safe_rcp(float d)
+{
+    const float tiny = 1e-20f;
+    return __frcp_rn(fabsf(d) < tiny ? copysignf(tiny, d) : d);
+}
+
+GBPT_HD uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
+
+// Intersects the 8 children of one node; returns the hit mask (bits 24-31: internal children by
+// octant-ordered slot, bits 0-23: triangles relative to the node's triangle base).
+GBPT_HD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 w2, const uint4 w3,
+                                                       const uint4 w4, float ox, float oy, float oz, float idx,
+                                                       float idy, float idz, float tmin, float tmax, uint32_t oct_inv)
+{
+    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    const float sx = __uint_as_float((w0.w & 0xFFu) << 23) * idx;
+    const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * idy;
+    const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * idz;
+    const float ax = (px - ox) * idx, ay = (py - oy) * idy, az = (pz - oz) * idz;
+
+    // near/far planes per axis by ray sign: words hold 4 children's bytes each
+    uint32_t nx0 = w2.x, nx1 = w2.y, fx0 = w3.z, fx1 = w3.w;
+    uint32_t ny0 = w2.z, ny1 = w2.w, fy0 = w4.x, fy1 = w4.y;
+    uint32_t nz0 = w3.x, nz1 = w3.y, fz0 = w4.z, fz1 = w4.w;
+    if (idx < 0.0f) { uint32_t t0 = nx0, t1 = nx1; nx0 = fx0; nx1 = fx1; fx0 = t0; fx1 = t1; }
+    if (idy < 0.0f) { uint32_t t0 = ny0, t1 = ny1; ny0 = fy0; ny1 = fy1; fy0 = t0; fy1 = t1; }
+    if (idz < 0.0f) { uint32_t t0 = nz0, t1 = nz1; nz0 = fz0; nz1 = fz1; fz0 = t0; fz1 = t1; }
+
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+    {
+        const uint32_t meta = byte_of(i < 4 ? w1.z : w1.w, i & 3);
+        const uint32_t qnx = byte_of(i < 4 ? nx0 : nx1, i & 3), qfx = byte_of(i < 4 ? fx0 : fx1, i & 3);
+        const uint32_t qny = byte_of(i < 4 ? ny0 : ny1, i & 3), qfy = byte_of(i < 4 ? fy0 : fy1, i & 3);
+        const uint32_t qnz = byte_of(i < 4 ? nz0 : nz1, i & 3), qfz = byte_of(i < 4 ? fz0 : fz1, i & 3);
+        const float tx0 = fmaf((float)qnx, sx, ax), tx1 = fmaf((float)qfx, sx, ax);
+        const float ty0 = fmaf((float)qny, sy, ay), ty1 = fmaf((float)qfy, sy, ay);
+        const float tz0 = fmaf((float)qnz, sz, az), tz1 = fmaf((float)qfz, sz, az);
+        float t_enter = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, tmin));
+        float t_exit = fminf(fminf(tx1, ty1), fminf(tz1, tmax));
+        t_enter -= fabsf(t_enter) * kBoxSlack;
+        t_exit += fabsf(t_exit) * kBoxSlack;
+        const bool inner = (meta & 0x18u) == 0x18u;
+        const uint32_t bit_index = inner ? ((meta & 0x1Fu) ^ oct_inv) : (meta & 0x1Fu);
+        const uint32_t child_bits = meta >> 5;
+        if (t_enter <= t_exit) hitmask |= child_bits << bit_index;
+    }
+    return hitmask;
+}
+
+// Traces one ray. Closest hit: returns the hit as (t, u, v, prim bits), prim = -1 and t = -1 on a
+// miss. Any hit: returns prim >= 0 iff some accepted hit has t < tmax. Counts visited nodes and
+// tested triangles when COUNT is set.
+template <bool ANY_HIT, bool COUNT>
+GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const float4 ot,
+                         const float4 dt, const int32_t skip_prim, uint32_t& n_nodes, uint32_t& n_tris)
+{
+    const float ox = ot.x, oy = ot.y, oz = ot.z, ray_tmin = ot.w;
+    const float dx = dt.x, dy = dt.y, dz = dt.z;
+    const float idx = safe_rcp(dx), idy = safe_rcp(dy), idz = safe_rcp(dz);
+    const uint32_t oct_inv = (dx >= 0.0f ? 4u : 0u) | (dy >= 0.0f ? 2u : 0u) | (dz >= 0.0f ? 1u : 0u);
+
+    float t_best = dt.w;  // hits must satisfy t < tmax
+    float u_best = 0.0f, v_best = 0.0f;
+    int32_t prim_best = -1;
+
+    uint2 stack[kTraversalStack];
+    int sp = 0;
+    uint2 ngroup = make_uint2(0u, 0x80000000u);
+    uint2 tgroup = make_uint2(0u, 0u);
+
+    for (;;)
+    {
+        if (ngroup.y & 0xFF000000u)
+        {
+            const uint32_t hits_imask = ngroup.y;
+            const uint32_t bit = 31u - __clz(hits_imask & 0xFF000000u);
+            ngroup.y &= ~(1u << bit);
+            if (ngroup.y & 0xFF000000u) stack[sp++] = ngroup;
+            const uint32_t slot = (bit - 24u) ^ oct_inv;
+            const uint32_t rel = __popc(hits_imask & ~(0xFFFFFFFFu << slot));
+            const uint32_t ni = ngroup.x + rel;
+            const uint4* np = nodes + 5 * (size_t)ni;
+            const uint4 w0 = GBPT_LDG(np + 0), w1 = GBPT_LDG(np + 1), w2 = GBPT_LDG(np + 2), w3 = GBPT_LDG(np + 3),
+                        w4 = GBPT_LDG(np + 4);
+            if (COUNT) n_nodes++;
+            const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, ox, oy, oz, idx, idy, idz, ray_tmin,
+                                                   ANY_HIT ? dt.w : t_best, oct_inv);
+            ngroup = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
+            tgroup = make_uint2(w1.y, hm & 0x00FFFFFFu);
+        }
+
+        while (tgroup.y != 0u)
+        {
+            const int b = __ffs(tgroup.y) - 1;
+            tgroup.y &= tgroup.y - 1u;
+            const size_t ti = (size_t)(tgroup.x + (uint32_t)b);
+            const float4 a = GBPT_LDG(tris + 3 * ti), e1 = GBPT_LDG(tris + 3 * ti + 1), e2 = GBPT_LDG(tris + 3 * ti + 2);
+            if (COUNT) n_tris++;
+            float t, u, v;
+            if (!mt_test(a, e1, e2, ox, oy, oz, dx, dy, dz, t, u, v)) continue;
+            const int32_t prim = __float_as_int(a.w);
+            if (t < ray_tmin || prim == skip_prim) continue;
+            if (ANY_HIT)
+            {
+                if (t < dt.w) return make_float4(t, u, v, __int_as_float(prim));
+            }
+            else if (t < t_best || (t == t_best && prim < prim_best))
+            {
+                t_best = t;
+                u_best = u;
+                v_best = v;
+                prim_best = prim;
+            }
+        }
+
+        if (!(ngroup.y & 0xFF000000u))
+        {
+            if (sp == 0) break;
+            ngroup = stack[--sp];
+        }
+    }
+    return prim_best >= 0 ? make_float4(t_best, u_best, v_best, __int_as_float(prim_best))
+                          : make_float4(-1.0f, 0.0f, 0.0f, __int_as_float(-1));
+}
+
+}  // namespace core
+}  // namespace gbpt

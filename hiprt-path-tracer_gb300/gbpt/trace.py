@@ -1,0 +1,133 @@
+"""Acceleration structure and ray queries (host-side mirror of the reference's traversal API).
+
+Mirrors, over the C ABI:
+  * ``BVH(indices, positions)``           <- HIPRTGeometry::build_bvh (src/HIPRT-Orochi/HIPRTScene.h:87-150)
+  * ``BVH.closest(rays)``                 <- trace_main_path_ray's traversal (src/Device/includes/Intersect.h:200)
+  * ``BVH.occluded(rays)``                <- evaluate_shadow_ray_occluded (src/Device/includes/Intersect.h:276)
+
+Device buffers are torch CUDA tensors (torch is used for device memory and streams only; every
+computation runs in libgbpt's CUDA kernels). Rays are SoA queues: origin_tmin (N,4) float32,
+dir_tmax (N,4) float32, last_prim (N,) int32. Closest hits are (N,4) float32 records
+(t, u, v, prim as int32 bits); ``hit_prim(hits)`` reinterprets the last column.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+def _stream_handle(stream) -> int:
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream)
+
+
+def _ptr(t) -> int:
+    return int(t.data_ptr()) if t is not None else 0
+
+
+def hit_prim(hits):
+    """Primitive indices of closest-hit records (int32 view of column 3)."""
+    if isinstance(hits, np.ndarray):
+        return hits[:, 3].view(np.int32)
+    import torch
+    return hits[:, 3].contiguous().view(torch.int32)
+
+
+class BVH:
+    """8-wide compressed BVH over a triangle mesh, resident on the current CUDA device."""
+
+    def __init__(self, indices: np.ndarray, positions: np.ndarray, sah_bins: int = 32, max_leaf_size: int = 3,
+                 num_threads: int = 0):
+        lib = _lib.load()
+        idx = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1, 3)
+        pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+        params = _lib.BvhParams(sah_bins, max_leaf_size, num_threads)
+        handle = ctypes.c_void_p()
+        _lib.check(lib.gbpt_bvh_build(idx.ctypes.data_as(_lib.c_i32), pos.ctypes.data_as(_lib.c_f), pos.shape[0],
+                                      idx.shape[0], ctypes.byref(params), ctypes.byref(handle)))
+        self._h = handle
+        self._lib = lib
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        if not self._h:
+            raise RuntimeError("BVH has been destroyed")
+        return self._h
+
+    def stats(self) -> dict:
+        s = _lib.BvhStats()
+        _lib.check(self._lib.gbpt_bvh_get_stats(self.handle, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_ if f != "reserved"}
+
+    def destroy(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.check(self._lib.gbpt_bvh_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    # ---- device-resident queues -------------------------------------------------------------
+    def closest(self, origin_tmin, dir_tmax, last_prim=None, out=None, stream=None):
+        import torch
+        n = origin_tmin.shape[0]
+        if out is None:
+            out = torch.empty((n, 4), dtype=torch.float32, device=origin_tmin.device)
+        _lib.check(self._lib.gbpt_trace_closest(self.handle, _ptr(origin_tmin), _ptr(dir_tmax), _ptr(last_prim), n,
+                                                _ptr(out), _stream_handle(stream)))
+        return out
+
+    def occluded(self, origin_tmin, dir_tmax, last_prim=None, out=None, stream=None):
+        import torch
+        n = origin_tmin.shape[0]
+        if out is None:
+            out = torch.empty((n,), dtype=torch.uint8, device=origin_tmin.device)
+        _lib.check(self._lib.gbpt_trace_any(self.handle, _ptr(origin_tmin), _ptr(dir_tmax), _ptr(last_prim), n,
+                                            _ptr(out), _stream_handle(stream)))
+        return out
+
+    def count(self, origin_tmin, dir_tmax, last_prim=None, any_hit: bool = False, stream=None):
+        """(nodes visited, triangles tested) summed over the batch, from the counting kernels."""
+        import torch
+        n = origin_tmin.shape[0]
+        counters = torch.zeros(2, dtype=torch.int64, device=origin_tmin.device)
+        _lib.check(self._lib.gbpt_trace_count(self.handle, _ptr(origin_tmin), _ptr(dir_tmax), _ptr(last_prim), n,
+                                              1 if any_hit else 0, _ptr(counters), _stream_handle(stream)))
+        c = counters.cpu().numpy()
+        return int(c[0]), int(c[1])
+
+    # ---- host buffers (end-to-end: copies inside the call) ------------------------------------
+    def closest_host(self, origin_tmin, dir_tmax, last_prim=None, out=None, stream=None):
+        """Host arrays or (pinned) CPU tensors in, host results out; synchronous."""
+        n = origin_tmin.shape[0]
+        if out is None:
+            out = np.empty((n, 4), np.float32)
+        _lib.check(self._lib.gbpt_trace_closest_host(self.handle, _host_ptr(origin_tmin), _host_ptr(dir_tmax),
+                                                     _host_ptr(last_prim), n, _host_ptr(out), _stream_handle(stream)))
+        return out
+
+    def occluded_host(self, origin_tmin, dir_tmax, last_prim=None, out=None, stream=None):
+        n = origin_tmin.shape[0]
+        if out is None:
+            out = np.empty((n,), np.uint8)
+        _lib.check(self._lib.gbpt_trace_any_host(self.handle, _host_ptr(origin_tmin), _host_ptr(dir_tmax),
+                                                 _host_ptr(last_prim), n, _host_ptr(out), _stream_handle(stream)))
+        return out
+
+
+def _host_ptr(a) -> int:
+    if a is None:
+        return 0
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return int(a.ctypes.data)
+    assert a.is_contiguous() and a.device.type == "cpu"
+    return int(a.data_ptr())

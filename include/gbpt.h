@@ -1,0 +1,121 @@
+/*
+ * gbpt — GB300-native (sm_103a) render path: C ABI.
+ *
+ * Plain C types only (pointers, sizes, PODs): no CUDA, C++ or torch types cross this boundary.
+ * Device pointers are CUdeviceptr-compatible addresses passed as void* / typed pointers; every
+ * stream argument is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ * Every entry point returns a gbpt_status and never exits or traps; gbpt_last_error() returns a
+ * thread-local message for the last failure on the calling thread.
+ *
+ * Each declaration cites the reference interface it replaces (file:line in
+ * TomClabault/HIPRT-Path-Tracer).
+ */
+#ifndef GBPT_H
+#define GBPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBPT_API __attribute__((visibility("default")))
+
+/* Replaces the reference's abort-on-error macros OROCHI_CHECK_ERROR / HIPRT_CHECK_ERROR
+ * (src/HIPRT-Orochi/HIPRTOrochiUtils.cpp:15-48), which log and exit(EXIT_FAILURE). */
+typedef enum gbpt_status {
+    GBPT_OK = 0,
+    GBPT_ERROR_INVALID_ARG = 1,
+    GBPT_ERROR_OOM = 2,
+    GBPT_ERROR_CUDA = 3,
+    GBPT_ERROR_TIMEOUT = 4,
+    GBPT_ERROR_NAN = 5,
+    GBPT_ERROR_UNSUPPORTED = 6,
+    GBPT_ERROR_BVH_TOO_DEEP = 7
+} gbpt_status;
+
+GBPT_API const char* gbpt_status_string(gbpt_status s);
+GBPT_API const char* gbpt_last_error(void);
+GBPT_API int32_t gbpt_version(void);
+
+/* ------------------------------------------------------------------------------------------
+ * Acceleration structure.
+ * Replaces HIPRTGeometry::build_bvh (src/HIPRT-Orochi/HIPRTScene.h:87-150), i.e.
+ * hiprtCreateGeometry + hiprtBuildGeometry over a hiprtTriangleMeshPrimitive
+ * {indices, vertices} (src/HIPRT-Orochi/HIPRTScene.h:152-155), and its OOM retry path
+ * (:118-139) which here becomes GBPT_ERROR_OOM.
+ * Build: binned SAH (sah_bins bins, leaves of at most max_leaf_size <= 3 triangles), collapsed
+ * to 8-wide nodes with 8-bit quantised child boxes (80 B per node), uploaded to the device.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct gbpt_bvh gbpt_bvh;
+
+typedef struct gbpt_bvh_params {
+    int32_t sah_bins;      /* 0 -> 32 */
+    int32_t max_leaf_size; /* 0 -> 3; 1..3 */
+    int32_t num_threads;   /* host build threads; 0 -> hardware concurrency */
+} gbpt_bvh_params;
+
+typedef struct gbpt_bvh_stats {
+    int64_t n_triangles;     /* triangles given */
+    int64_t n_bvh_triangles; /* triangles referenced by leaves (non-finite ones are left out) */
+    int64_t n_nodes;         /* 8-wide nodes */
+    int64_t n_binary_nodes;  /* nodes of the binned-SAH binary tree before collapsing */
+    int32_t wide_depth;      /* levels of 8-wide nodes (traversal stack bound) */
+    int32_t node_bytes;      /* bytes per 8-wide node (80) */
+    int32_t triangle_bytes;  /* bytes per stored triangle record (48) */
+    int32_t reserved;
+    int64_t device_bytes;    /* device memory held by the structure */
+    double build_seconds;    /* host build time (binning + collapse + encode) */
+    double upload_seconds;   /* host-to-device upload time */
+} gbpt_bvh_stats;
+
+/* indices: 3*n_triangles int32 (host); positions: 3*n_vertices float (host). */
+GBPT_API gbpt_status gbpt_bvh_build(const int32_t* indices, const float* positions, int64_t n_vertices,
+                                    int64_t n_triangles, const gbpt_bvh_params* params, gbpt_bvh** out);
+GBPT_API gbpt_status gbpt_bvh_get_stats(const gbpt_bvh* bvh, gbpt_bvh_stats* out);
+GBPT_API gbpt_status gbpt_bvh_destroy(gbpt_bvh* bvh);
+
+/* ------------------------------------------------------------------------------------------
+ * Ray queries over SoA ray queues (device memory, 16-byte aligned):
+ *   origin_tmin[4*i..]  = origin.xyz, tmin   (hiprtRay.origin / .minT)
+ *   dir_tmax[4*i..]     = direction.xyz, tmax (hiprtRay.direction / .maxT; a hit counts iff t < tmax)
+ *   last_prim[i]        = primitive to ignore (self-hit filter; -1 = none)
+ * Closest-hit output hits[4*i..] = t, u, v (float), prim (int32 bits); prim = -1 and t = -1 on a miss.
+ *
+ * gbpt_trace_closest replaces hiprtGeomTraversalClosest + the filter function as called by
+ *   trace_main_path_ray (src/Device/includes/Intersect.h:200-270, traversal macros :22-69,
+ *   filter src/Device/functions/FilterFunction.h:22-75 with alpha testing off) and, on the CPU,
+ *   BVH::intersect (src/Renderer/BVH.h:132-223).
+ * gbpt_trace_any replaces hiprtGeomTraversalAnyHit as called by evaluate_shadow_ray_occluded
+ *   (src/Device/includes/Intersect.h:276-324): occluded[i] = 1 iff some accepted hit has t < tmax.
+ *   Callers pass tmax = t_max - 1e-4f as the reference does.
+ * The triangle test is Moller-Trumbore with the reference's operation order and epsilon
+ * (src/Renderer/Triangle.h:20-63), evaluated without FMA contraction, so t/u/v are bit-identical
+ * to the reference's CPU results; ties on t resolve to the lowest primitive index.
+ * ---------------------------------------------------------------------------------------- */
+GBPT_API gbpt_status gbpt_trace_closest(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                        const int32_t* last_prim, int64_t n_rays, float* hits, void* stream);
+GBPT_API gbpt_status gbpt_trace_any(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                    const int32_t* last_prim, int64_t n_rays, uint8_t* occluded, void* stream);
+
+/* Host-buffer variants (the end-to-end entry points): copy the rays host->device, trace, copy
+ * the results device->host, and synchronise the stream before returning. Host buffers should be
+ * pinned for full copy bandwidth. Scratch device buffers are allocated stream-ordered. */
+GBPT_API gbpt_status gbpt_trace_closest_host(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                             const int32_t* last_prim, int64_t n_rays, float* hits, void* stream);
+GBPT_API gbpt_status gbpt_trace_any_host(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                         const int32_t* last_prim, int64_t n_rays, uint8_t* occluded, void* stream);
+
+/* Instrumented traversal (same kernels, counting build): adds to counters[0] the 8-wide nodes
+ * visited and to counters[1] the triangles tested over the batch (device int64[2]). Used to
+ * compute algorithmic bytes per ray for the roofline. any_hit selects the shadow-ray kernel. */
+GBPT_API gbpt_status gbpt_trace_count(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                      const int32_t* last_prim, int64_t n_rays, int32_t any_hit,
+                                      unsigned long long* counters, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPT_H */

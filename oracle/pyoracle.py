@@ -1,0 +1,163 @@
+"""TEST INFRASTRUCTURE ONLY — ctypes bindings for the CPU oracle libraries.
+
+* ``liboracle.so``: this project's C++ restatement of the reference's CPU intersection path
+  (trace_oracle.cpp). Built anywhere by ``make -C oracle``.
+* ``_ref/libref.so``: the reference's own CPU code compiled behind clean-room shims
+  (ref_trace.cpp). Built only where the reference tree is present (``make -C oracle ref``).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref.so")
+
+_c_f = ctypes.POINTER(ctypes.c_float)
+_c_i = ctypes.POINTER(ctypes.c_int32)
+_c_u8 = ctypes.POINTER(ctypes.c_uint8)
+_i64 = ctypes.c_int64
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the restatement (always) and the reference build (when its sources exist)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    ref_root = os.environ.get("GBPT_REFERENCE_ROOT", "/root/reference")
+    if ref is None:
+        ref = os.path.isdir(os.path.join(ref_root, "src", "Renderer"))
+    if ref:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={ref_root}"])
+
+
+def _ptr(a: np.ndarray, t):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(t)
+
+
+def _rays(rays):
+    o = np.ascontiguousarray(rays.origin_tmin, np.float32)
+    d = np.ascontiguousarray(rays.dir_tmax, np.float32)
+    lp = np.ascontiguousarray(rays.last_prim, np.int32)
+    return o, d, lp
+
+
+class Oracle:
+    """The restatement oracle (octree + k-DOP + Moller-Trumbore, reference semantics)."""
+
+    def __init__(self):
+        if not os.path.exists(ORACLE_SO):
+            build(ref=False)
+        lib = ctypes.CDLL(ORACLE_SO)
+        lib.orc_octree_build.restype = ctypes.c_void_p
+        lib.orc_octree_build.argtypes = [_c_f, _i64, ctypes.c_int, ctypes.c_int]
+        lib.orc_octree_free.argtypes = [ctypes.c_void_p]
+        lib.orc_octree_node_count.restype = _i64
+        lib.orc_octree_node_count.argtypes = [ctypes.c_void_p]
+        lib.orc_octree_closest.argtypes = [ctypes.c_void_p, _c_f, _c_f, _c_i, _i64, _c_f, ctypes.c_int]
+        lib.orc_octree_occluded.argtypes = [ctypes.c_void_p, _c_f, _c_f, _c_i, _i64, _c_u8, ctypes.c_int]
+        lib.orc_brute_closest.argtypes = [_c_f, _i64, _c_f, _c_f, _c_i, _i64, _c_f, ctypes.c_int]
+        lib.orc_mt_intersect.restype = ctypes.c_int
+        lib.orc_mt_intersect.argtypes = [_c_f, _c_f, _c_f, _c_f]
+        self.lib = lib
+
+    def octree(self, soup: np.ndarray, max_depth: int = 32, leaf_max: int = 8) -> "OracleOctree":
+        return OracleOctree(self, soup, max_depth, leaf_max)
+
+    def brute_closest(self, soup: np.ndarray, rays, nthreads: int = 0) -> np.ndarray:
+        soup = np.ascontiguousarray(soup, np.float32)
+        o, d, lp = _rays(rays)
+        hits = np.zeros((len(o), 4), np.float32)
+        self.lib.orc_brute_closest(_ptr(soup, _c_f), soup.shape[0], _ptr(o, _c_f), _ptr(d, _c_f), _ptr(lp, _c_i),
+                                   len(o), _ptr(hits, _c_f), nthreads)
+        return hits
+
+    def mt(self, tri9: np.ndarray, origin3, dir3):
+        tri9 = np.ascontiguousarray(tri9, np.float32).reshape(9)
+        o = np.ascontiguousarray(origin3, np.float32).reshape(3)
+        d = np.ascontiguousarray(dir3, np.float32).reshape(3)
+        out = np.zeros(3, np.float32)
+        ok = self.lib.orc_mt_intersect(_ptr(tri9, _c_f), _ptr(o, _c_f), _ptr(d, _c_f), _ptr(out, _c_f))
+        return bool(ok), out
+
+
+class OracleOctree:
+    def __init__(self, orc: Oracle, soup: np.ndarray, max_depth: int, leaf_max: int):
+        self.orc = orc
+        self.soup = np.ascontiguousarray(soup, np.float32)
+        self.h = orc.lib.orc_octree_build(_ptr(self.soup, _c_f), self.soup.shape[0], max_depth, leaf_max)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.orc.lib.orc_octree_free(self.h)
+            self.h = None
+
+    @property
+    def node_count(self) -> int:
+        return int(self.orc.lib.orc_octree_node_count(self.h))
+
+    def closest(self, rays, nthreads: int = 0) -> np.ndarray:
+        o, d, lp = _rays(rays)
+        hits = np.zeros((len(o), 4), np.float32)
+        self.orc.lib.orc_octree_closest(self.h, _ptr(o, _c_f), _ptr(d, _c_f), _ptr(lp, _c_i), len(o),
+                                        _ptr(hits, _c_f), nthreads)
+        return hits
+
+    def occluded(self, rays, nthreads: int = 0) -> np.ndarray:
+        o, d, lp = _rays(rays)
+        occ = np.zeros(len(o), np.uint8)
+        self.orc.lib.orc_octree_occluded(self.h, _ptr(o, _c_f), _ptr(d, _c_f), _ptr(lp, _c_i), len(o),
+                                         _ptr(occ, _c_u8), nthreads)
+        return occ
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+class RefBVH:
+    """The reference's own CPU BVH (src/Renderer/BVH.*), compiled behind shims."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            lib = ctypes.CDLL(REF_SO)
+            lib.ref_bvh_build.restype = ctypes.c_void_p
+            lib.ref_bvh_build.argtypes = [_c_f, _i64]
+            lib.ref_bvh_free.argtypes = [ctypes.c_void_p]
+            lib.ref_bvh_closest.argtypes = [ctypes.c_void_p, _c_f, _c_f, _c_i, _i64, _c_f]
+            lib.ref_shadow_occluded.argtypes = [ctypes.c_void_p, _c_f, _c_f, _c_i, _c_f, _i64, _c_u8]
+            cls._lib = lib
+        return cls._lib
+
+    def __init__(self, soup: np.ndarray):
+        self.soup = np.ascontiguousarray(soup, np.float32)
+        self.h = self.lib().ref_bvh_build(_ptr(self.soup, _c_f), self.soup.shape[0])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib().ref_bvh_free(self.h)
+            self.h = None
+
+    def closest(self, rays) -> np.ndarray:
+        o, d, lp = _rays(rays)
+        hits = np.zeros((len(o), 4), np.float32)
+        self.lib().ref_bvh_closest(self.h, _ptr(o, _c_f), _ptr(d, _c_f), _ptr(lp, _c_i), len(o), _ptr(hits, _c_f))
+        return hits
+
+    def shadow_occluded(self, rays, light_dist: np.ndarray) -> np.ndarray:
+        o, d, lp = _rays(rays)
+        ld = np.ascontiguousarray(light_dist, np.float32)
+        occ = np.zeros(len(o), np.uint8)
+        self.lib().ref_shadow_occluded(self.h, _ptr(o, _c_f), _ptr(d, _c_f), _ptr(lp, _c_i), _ptr(ld, _c_f), len(o),
+                                       _ptr(occ, _c_u8))
+        return occ

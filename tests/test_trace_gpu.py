@@ -1,0 +1,123 @@
+"""GPU: the CUDA traversal kernels through the C ABI against the oracle and the reference's
+golden vectors. Closest-hit records must be bit-identical (t, u, v, prim) except for exact ties
+on t, which resolve to the lowest primitive index; shadow decisions must be identical."""
+import numpy as np
+import pytest
+import torch
+
+import gbpt
+from gbpt import scenes
+from helpers import classify_mismatches, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(rays, device):
+    return (torch.from_numpy(np.ascontiguousarray(rays.origin_tmin)).to(device),
+            torch.from_numpy(np.ascontiguousarray(rays.dir_tmax)).to(device),
+            torch.from_numpy(np.ascontiguousarray(rays.last_prim)).to(device))
+
+
+def _closest(bvh, rays, device):
+    o, d, lp = _dev(rays, device)
+    h = bvh.closest(o, d, lp)
+    torch.cuda.synchronize()
+    return h.cpu().numpy()
+
+
+def _occluded(bvh, rays, device):
+    o, d, lp = _dev(rays, device)
+    r = bvh.occluded(o, d, lp)
+    torch.cuda.synchronize()
+    return r.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ["cornell", "terrain"])
+def test_golden_closest_and_shadow(cuda, oracle, name):
+    mesh, closest, c_hits, shadow, _, s_occ = load_golden(name)
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    got = _closest(bvh, closest, cuda)
+    n, ties, other = classify_mismatches(oracle, mesh, closest, got, c_hits)
+    assert other == 0, f"{other} non-tie mismatches of {n}"
+    assert np.array_equal(_occluded(bvh, shadow, cuda), s_occ)
+
+
+def test_random_scene_against_oracle(cuda, oracle):
+    mesh = scenes.traversal_scene(cells=128, n_random=8000, seed=21)
+    oc = oracle.octree(mesh.triangle_soup())
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    rays = scenes.pinhole_rays(256, 128, vfov_deg=30)
+    want = oc.closest(rays)
+    got = _closest(bvh, rays, cuda)
+    n, ties, other = classify_mismatches(oracle, mesh, rays, got, want)
+    assert other == 0, f"{other} non-tie mismatches of {n}"
+    pts, nrm, prim = scenes.hit_points_normals(mesh, rays, want)
+    m = prim >= 0
+    b = scenes.bounce_rays(pts[m], nrm[m], prim[m], seed=5)
+    n, ties, other = classify_mismatches(oracle, mesh, b, _closest(bvh, b, cuda), oc.closest(b))
+    assert other == 0
+    s, _ = scenes.shadow_rays(pts[m], prim[m], seed=6)
+    assert np.array_equal(_occluded(bvh, s, cuda), oc.occluded(s))
+
+
+def test_matches_host_emulation_bits(cuda):
+    """The CUDA build and the host build of the same traversal source agree bit for bit."""
+    from native.emu import EmuBVH
+    mesh = scenes.traversal_scene(cells=96, n_random=4000, seed=8)
+    rays = scenes.pinhole_rays(192, 96, vfov_deg=35)
+    got = _closest(gbpt.BVH(mesh.indices, mesh.positions), rays, cuda)
+    want, _ = EmuBVH(mesh).trace(rays)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_host_buffer_entry_points_match_device(cuda):
+    mesh, closest, c_hits, shadow, _, s_occ = load_golden("terrain")
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    dev = _closest(bvh, closest, cuda)
+    host = bvh.closest_host(np.ascontiguousarray(closest.origin_tmin), np.ascontiguousarray(closest.dir_tmax),
+                            np.ascontiguousarray(closest.last_prim))
+    assert np.array_equal(dev.view(np.uint32), host.view(np.uint32))
+    occ = bvh.occluded_host(np.ascontiguousarray(shadow.origin_tmin), np.ascontiguousarray(shadow.dir_tmax),
+                            np.ascontiguousarray(shadow.last_prim))
+    assert np.array_equal(occ, s_occ)
+
+
+def test_count_kernel_matches_emulation(cuda):
+    from native.emu import EmuBVH
+    mesh = scenes.traversal_scene(cells=64, n_random=2000, seed=4)
+    rays = scenes.pinhole_rays(128, 64, vfov_deg=30)
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    o, d, lp = _dev(rays, cuda)
+    nodes, tris = bvh.count(o, d, lp)
+    _, cnt = EmuBVH(mesh).trace(rays)
+    assert (nodes, tris) == (int(cnt[0]), int(cnt[1]))
+
+
+def test_empty_and_zero_rays(cuda):
+    bvh = gbpt.BVH(np.zeros((0, 3), np.int32), np.zeros((0, 3), np.float32))
+    rays = scenes.pinhole_rays(16, 8)
+    got = _closest(bvh, rays, cuda)
+    assert (got[:, 3].view(np.int32) == -1).all()
+    o, d, lp = _dev(rays.slice(slice(0, 0)), cuda)
+    assert bvh.closest(o, d, lp).shape == (0, 4)
+
+
+def test_full_size_scene_sampled(cuda, oracle):
+    """The benchmark scene at full size (2,297,152 triangles): a strided sample of primary rays
+    against the oracle, plus size-independent properties over the whole batch."""
+    mesh = scenes.traversal_scene()
+    assert mesh.n_triangles == 2_297_152
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    st = bvh.stats()
+    assert st["n_bvh_triangles"] == mesh.n_triangles and st["wide_depth"] < 48
+    rays = scenes.pinhole_rays(1024, 512, vfov_deg=30)
+    got = _closest(bvh, rays, cuda)
+    sample = rays.slice(slice(0, None, 97))
+    oc = oracle.octree(mesh.triangle_soup())
+    n, ties, other = classify_mismatches(oracle, mesh, sample, got[::97], oc.closest(sample))
+    assert other == 0, f"{other} non-tie mismatches of {n}"
+    prim = got[:, 3].view(np.int32)
+    hit = prim >= 0
+    assert (got[hit, 0] > 0).all() and (prim < mesh.n_triangles).all()
+    # determinism: a second launch returns identical bits
+    assert np.array_equal(got.view(np.uint32), _closest(bvh, rays, cuda).view(np.uint32))
