@@ -44,10 +44,10 @@ TRI_BYTES = 36  # algorithmic: three float3 vertex records
 
 
 def workload_config(n_tris):
-    return {"workload": "bvh-traversal-microbench", "triangles": n_tris, "rays_per_step": 8388608 + N_BOUNCE + N_SHADOW,
+    return {"workload": "bvh-traversal-microbench", "triangles": n_tris, "rays_per_step": WIDTH * HEIGHT + N_BOUNCE + N_SHADOW,
             "primary": f"{WIDTH}x{HEIGHT} pinhole, vfov {VFOV} deg", "bounce": N_BOUNCE, "shadow_any_hit": N_SHADOW,
             "bvh": "binned SAH 32 bins, leaf<=3, 8-wide quantised (80 B nodes)",
-            "l2": "inputs larger than L2 (604 MB of rays per step); no flush"}
+            "l2": f"inputs larger than L2 ({(WIDTH * HEIGHT + N_BOUNCE + N_SHADOW) * RAY_IN_BYTES / 1e6:.0f} MB of rays per step); no flush"}
 
 
 def build_workload(seed=1, log=print):
@@ -142,36 +142,40 @@ def ncu_traffic():
     return None
 
 
-def cpu_baseline_sample(mesh, primary, bounce, shadow, frac, log=print):
-    """Times the reference CPU traversal on a strided sample of each ray class (all host cores)."""
+def make_cpu_impl(mesh, log=print):
+    """The reference CPU traversal over all host cores: the reference's own code (oracle/_ref) where
+    it was compiled for this machine, else the oracle's restatement. Returns (closest, occluded, kind)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
     soup = mesh.triangle_soup()
-    kind = "port"
     cores = os.cpu_count() or 1
-    impl = None
     if pyoracle.ref_available():
         try:
             ref = pyoracle.RefBVH(soup)
-            impl = (lambda r: ref.closest(r), lambda r: ref.shadow_occluded(
-                r, (r.dir_tmax[:, 3] + np.float32(1e-4)).astype(np.float32)))
-            kind = "reference"
+            # the reference's shadow test subtracts 1e-4 from the light distance itself
+            return (lambda r: ref.closest(r),
+                    lambda r: ref.shadow_occluded(r, (r.dir_tmax[:, 3] + np.float32(1e-4)).astype(np.float32)),
+                    "reference", cores)
         except OSError:
-            impl = None
-    if impl is None:
-        orc = pyoracle.Oracle()
-        t0 = time.time()
-        oc = orc.octree(soup)
-        log(f"oracle octree build {time.time() - t0:.1f}s ({oc.node_count} nodes)")
-        impl = (lambda r: oc.closest(r, nthreads=cores), lambda r: oc.occluded(r, nthreads=cores))
+            pass
+    orc = pyoracle.Oracle()
+    t0 = time.time()
+    oc = orc.octree(soup)
+    log(f"oracle octree build {time.time() - t0:.1f}s ({oc.node_count} nodes)")
+    return (lambda r: oc.closest(r, nthreads=cores), lambda r: oc.occluded(r, nthreads=cores), "port", cores)
+
+
+def cpu_baseline_sample(impl, primary, bounce, shadow, frac):
+    """Times the CPU traversal on a strided sample of each ray class."""
+    closest, occluded, kind, cores = impl
     step = max(1, int(round(1.0 / frac)))
     samples = [primary.slice(slice(0, None, step)), bounce.slice(slice(0, None, step)),
                shadow.slice(slice(0, None, step))]
     n = sum(len(s) for s in samples)
     t0 = time.perf_counter()
-    impl[0](samples[0])
-    impl[0](samples[1])
-    impl[1](samples[2])
+    closest(samples[0])
+    closest(samples[1])
+    occluded(samples[2])
     dt = time.perf_counter() - t0
     return {"value": n / dt / 1e6, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"every {step}th ray of each class ({n} rays: {len(samples[0])} primary, {len(samples[1])} bounce, "
@@ -182,24 +186,18 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     mesh, primary = build_workload(log=lambda *a: print(*a, file=sys.stderr))
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import pyoracle
+    impl = make_cpu_impl(mesh, log=lambda *a: print(*a, file=sys.stderr))
     # primary hits for the secondary rays come from the CPU structure itself on this arm
-    orc = pyoracle.Oracle()
-    oc = orc.octree(mesh.triangle_soup())
-    step = 8
-    prim_hits = np.zeros((len(primary), 4), np.float32)
-    prim_hits[:, 3] = np.int32(-1).view(np.float32)
-    sl = slice(0, None, step)
-    prim_hits[sl] = oc.closest(primary.slice(sl))
-    bounce, shadow = secondary_rays(mesh, primary.slice(sl), prim_hits[sl])
+    sl = slice(0, None, 8)
+    sub = primary.slice(sl)
+    bounce, shadow = secondary_rays(mesh, sub, impl[0](sub))
     frac = args.ref_fraction
     for _ in range(args.warmup):
-        cpu_baseline_sample(mesh, primary, bounce, shadow, frac / 4, log=lambda *a: None)
+        cpu_baseline_sample(impl, primary, bounce, shadow, frac / 4)
     vals, times = [], []
     base = None
     for _ in range(args.steps):
-        base, dt = cpu_baseline_sample(mesh, primary, bounce, shadow, frac, log=lambda *a: None)
+        base, dt = cpu_baseline_sample(impl, primary, bounce, shadow, frac)
         vals.append(base["value"])
         times.append(dt)
     value = statistics.median(vals)
@@ -222,9 +220,16 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=0.5)
     ap.add_argument("--ref-fraction", type=float, default=1.0 / 256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: 2048x1024 primary + 1M bounce + 1M shadow rays, no e2e/CPU legs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global WIDTH, HEIGHT, N_BOUNCE, N_SHADOW
+    if args.small:
+        WIDTH, HEIGHT, N_BOUNCE, N_SHADOW = 2048, 1024, 1024 * 1024, 1024 * 1024
+        args.no_cpu_baseline = True
+        args.e2e_steps = 0
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -342,19 +347,22 @@ def main():
         bvh.closest_host(*hb, out=out_b.numpy())
         bvh.occluded_host(*hs, out=out_s.numpy())
 
-    for _ in range(2):
-        e2e_step()
-    if dist is not None:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        e2e_step()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_s = float("nan")
+    if args.e2e_steps > 0:
+        for _ in range(2):
+            e2e_step()
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     if dist is not None:
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    assert np.array_equal(out_p.numpy().view(np.uint32), hits_p.cpu().numpy().view(np.uint32))
+    if args.e2e_steps > 0:
+        assert np.array_equal(out_p.numpy().view(np.uint32), hits_p.cpu().numpy().view(np.uint32))
 
     peak, peak_kind = measured_peaks()
     achieved = alg_closest / (closest_ms * 1e-3) / 1e9
@@ -382,7 +390,8 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        base, _ = cpu_baseline_sample(mesh, primary, bounce, shadow, args.cpu_fraction, log=log)
+        del P, B, S
+        base, _ = cpu_baseline_sample(make_cpu_impl(mesh, log=log), primary, bounce, shadow, args.cpu_fraction)
         line["cpu_baseline"] = base
     if rank == 0:
         print(json.dumps(line))
