@@ -14,30 +14,31 @@
 
 #include "../../include/gbpt.h"
 #include "bvh.h"
+#include "handles.h"
 #include "trace_kernels.h"
 
-struct gbpt_bvh
-{
-    gbpt::DeviceBVH dev;
-    gbpt_bvh_stats stats;
-    int device = 0;
-};
-
 namespace {
-
 thread_local std::string g_last_error;
+}
 
-gbpt_status fail(gbpt_status s, const std::string& msg)
+namespace gbpt {
+gbpt_status set_error(gbpt_status s, const std::string& msg)
 {
     g_last_error = msg;
     return s;
 }
 
-gbpt_status cuda_fail(cudaError_t e, const char* what)
+gbpt_status cuda_error(cudaError_t e, const char* what)
 {
     gbpt_status s = (e == cudaErrorMemoryAllocation) ? GBPT_ERROR_OOM : GBPT_ERROR_CUDA;
-    return fail(s, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+    return set_error(s, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
 }
+}  // namespace gbpt
+
+namespace {
+
+gbpt_status fail(gbpt_status s, const std::string& msg) { return gbpt::set_error(s, msg); }
+gbpt_status cuda_fail(cudaError_t e, const char* what) { return gbpt::cuda_error(e, what); }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 

@@ -1,0 +1,565 @@
+// Wavefront path tracer kernels (sm_103a): camera rays, per-bounce shading with next-event
+// estimation + BSDF MIS, resolve, accumulation, and the emissive power alias table build.
+//
+// One launch traces samples_per_launch samples of every pixel as one wavefront. Each bounce runs
+//   extend (closest hit on the active queue) -> shade -> shadow (any hit) + BSDF-light (closest hit)
+//   -> resolve,
+// with the active paths compacted into the next queue by warp-aggregated appends. Path state is
+// SoA indexed by a fixed slot (pixel + W*H*sample), so accumulation is deterministic.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "render_common.h"
+#include "render_kernels.h"
+#include "trace_core.h"
+
+namespace gbpt {
+namespace {
+
+// Appends one entry per calling thread with 'want' set; returns the slot index (or -1).
+// Warp-aggregated: one atomicAdd per warp (ballot + popc prefix).
+__device__ __forceinline__ int warp_append(int32_t* counter, bool want)
+{
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, want);
+    if (!want) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void warp_count(unsigned long long* counter, bool c)
+{
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, c);
+    if ((threadIdx.x & 31) == __ffs(active) - 1 && mask) atomicAdd(counter, (unsigned long long)__popc(mask));
+}
+
+__device__ __forceinline__ void store_rng(uint64_t* p, const Pcg32& r) { *p = r.state; }
+
+// ---------------------------------------------------------------------------------------------
+// camera rays (CameraRays, src/Device/kernels/CameraRays.h:155-176; HIPRTCamera::get_camera_ray,
+// src/HostDeviceCommon/HIPRTCamera.h:31-52)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers pb, Queue q, int32_t iteration_base,
+                                                     unsigned long long* stats)
+{
+    const int64_t n_pix = (int64_t)rc.width * rc.height;
+    const int64_t n = n_pix * rc.spp;
+    for (int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; slot < n; slot += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int pixel = (int)(slot % n_pix);
+        const int s = (int)(slot / n_pix);
+        const int x = pixel % rc.width, y = pixel / rc.width;
+        Pcg32 rng = pcg_seed((uint32_t)pixel, (uint32_t)(iteration_base + s), rc.seed);
+        float px = x + 0.5f, py = y + 0.5f;
+        if (rc.do_jittering)
+        {
+            px += rng.next() - 0.5f;
+            py += rng.next() - 0.5f;
+        }
+        const float xn = px / rc.width * 2.0f - 1.0f;
+        const float yn = py / rc.height * 2.0f - 1.0f;
+        const V3 origin = mat_x_point(rc.inverse_view, v3(0.0f, 0.0f, 0.0f));
+        const V3 p_vs = mat_x_point(rc.inverse_projection, v3(xn, yn, -1.0f));
+        const V3 p_ws = mat_x_point(rc.inverse_view, p_vs);
+        const V3 dir = normalize(p_ws - origin);
+        q.origin_tmin[slot] = f4(origin, 0.0f);
+        q.dir_tmax[slot] = f4(dir, INFINITY);
+        q.last_prim[slot] = -1;
+        q.slot[slot] = (int32_t)slot;
+        pb.throughput[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        pb.radiance[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        store_rng(pb.rng + slot, rng);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        *q.count = (int32_t)n;
+        atomicAdd(stats + 0, (unsigned long long)n);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// traversal over a device-counted queue (grid-stride, count read from device memory)
+// ---------------------------------------------------------------------------------------------
+template <bool ANY_HIT>
+__global__ void __launch_bounds__(128) trace_queue_kernel(const uint4* __restrict__ nodes,
+                                                          const float4* __restrict__ tris, Queue q)
+{
+    const int n = *q.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        uint32_t cn = 0, ct = 0;
+        const float4 h = core::trace_ray<ANY_HIT, false>(nodes, tris, q.origin_tmin[i], q.dir_tmax[i], q.last_prim[i], cn, ct);
+        if (ANY_HIT)
+            q.occluded[i] = __float_as_int(h.w) >= 0 ? 1 : 0;
+        else
+            q.hits[i] = h;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Lambertian BSDF (src/Device/includes/BSDFs/Lambertian.h:14-58)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ V3 lambert_eval(V3 albedo, float NoL, float& pdf)
+{
+    pdf = 0.0f;
+    if (NoL <= 0.0f) return v3(0.0f, 0.0f, 0.0f);
+    pdf = NoL * kInvPi;
+    return albedo * kInvPi;
+}
+
+// fix_backfacing_normals (src/Device/includes/Intersect.h:142-176)
+__device__ __forceinline__ void fix_backfacing(V3 view, V3& ng, V3& ns)
+{
+    if (dot(view, ng) < 0.0f)
+    {
+        ng = -ng;
+        ns = -ns;
+    }
+    if (dot(view, ns) < 0.0f) ns = -ns;
+    V3 refl = 2.0f * dot(view, ns) * ns - view;
+    if (dot(refl, ng) <= 0.0f)
+    {
+        refl = refl - normalize((dot(refl, ng) - 0.01f) * ng);
+        ns = normalize(view + refl);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// shade: one path vertex per active path
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue next,
+                                                    Queue shadow, Queue bsdfq, int bounce, unsigned long long* stats)
+{
+    const int n = *in.count;
+    // iterate in whole warps so that the warp-aggregated appends see converged lanes
+    const int n_round = (n + 31) & ~31;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += gridDim.x * blockDim.x)
+    {
+        const bool valid = i < n;
+        int slot = 0;
+        int prim = -1;
+        float4 hit = make_float4(0, 0, 0, 0);
+        if (valid)
+        {
+            slot = in.slot[i];
+            hit = in.hits[i];
+            prim = __float_as_int(hit.w);
+            pb.shadow_entry[slot] = -1;
+            pb.bsdf_entry[slot] = -1;
+        }
+        const bool alive = valid && prim >= 0;
+
+        bool want_shadow = false, want_bsdf = false, want_next = false;
+        float4 sh_o, sh_d, bs_d, nx_d;
+        V3 P = v3(0, 0, 0), tp = v3(0, 0, 0);
+        V3 light_contrib = v3(0, 0, 0);
+        float4 bsdf_pending = make_float4(0, 0, 0, 0);
+        Pcg32 rng;
+        rng.inc = pcg_inc(rc.seed);
+        rng.state = 0;
+        if (alive)
+        {
+            rng.state = pb.rng[slot];
+            const float4 o4 = in.origin_tmin[i], d4 = in.dir_tmax[i];
+            const V3 o = xyz(o4), d = xyz(d4);
+            P = o + hit.x * d;
+            V3 a, b, c;
+            load_triangle(s, prim, a, b, c);
+            V3 ng = normalize(cross(b - a, c - a));
+            V3 ns = ng;
+            const V3 view = -d;
+            fix_backfacing(view, ng, ns);
+            const DeviceMaterial m = s.materials[__ldg(s.material_of + prim)];
+            const V3 albedo = xyz(m.base_color);
+            tp = xyz(pb.throughput[slot]);
+            V3 L = v3(0, 0, 0);
+            if (bounce == 0) L = xyz(m.emission);
+
+            // ---- next-event estimation: light sample (sample_one_light_MIS, Lights.h:123-185) ----
+            if (s.n_emissive > 0)
+            {
+                int e;
+                if (rc.light_sampling == GBPT_LIGHT_POWER)
+                {
+                    e = rng.index(s.n_emissive);
+                    if (rng.next() > __ldg(s.alias_prob + e)) e = __ldg(s.alias_index + e);
+                }
+                else
+                    e = rng.index(s.n_emissive);
+                const int lt = __ldg(s.emissive + e);
+                float r1 = rng.next(), r2 = rng.next();
+                square_to_triangle(r1, r2);
+                V3 la, lb, lc;
+                load_triangle(s, lt, la, lb, lc);
+                const V3 ab = lb - la, ac = lc - la;
+                const V3 nrm = cross(ab, ac);
+                const float len = length(nrm);
+                const V3 lp = la + ab * r1 + ac * r2;
+                const V3 ln = nrm / len;
+                const float area = 0.5f * len;
+                const V3 Le = xyz(s.materials[__ldg(s.material_of + lt)].emission);
+                float pdf_area = 1.0f / area;
+                if (rc.light_sampling == GBPT_LIGHT_POWER)
+                    pdf_area *= (luminance(Le) * area) / s.power_sum;
+                else
+                    pdf_area /= (float)s.n_emissive;
+                if (pdf_area > 0.0f)
+                {
+                    const V3 to_l = lp - P;
+                    const float dist = length(to_l);
+                    const V3 wi = to_l / dist;
+                    float bsdf_pdf;
+                    const V3 f = lambert_eval(albedo, dot(ns, wi), bsdf_pdf);
+                    if (bsdf_pdf > 0.0f)
+                    {
+                        const float cos_l = fmaxf(0.0f, dot(ln, -wi));
+                        if (cos_l > 1.0e-5f)
+                        {
+                            const float light_pdf = area_to_solid_angle_pdf(pdf_area, dist, cos_l);
+                            const float mis = balance_heuristic(light_pdf, bsdf_pdf);
+                            const float cosine = fabsf(dot(ns, wi));
+                            light_contrib = tp * (f * cosine * Le * mis / light_pdf);
+                            if (!is_black(light_contrib))
+                            {
+                                want_shadow = true;
+                                sh_o = f4(P, 0.0f);
+                                sh_d = f4(wi, dist - 1.0e-4f);
+                            }
+                        }
+                    }
+                }
+            }
+
+            // ---- next-event estimation: BSDF sample (Lights.h:187-226) ----
+            {
+                const float r1 = rng.next(), r2 = rng.next();
+                const V3 wi = cosine_sample(ns, r1, r2);
+                float pdf;
+                const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
+                if (pdf > 0.0f && s.n_emissive > 0)
+                {
+                    const float cosine = fabsf(dot(ns, wi));
+                    const V3 w = tp * (f * cosine / pdf);
+                    want_bsdf = true;
+                    bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                    bsdf_pending = f4(w, pdf);
+                }
+            }
+
+            // ---- continuation (PathTracing.h:81-101, RussianRoulette.h:20-55) ----
+            if (bounce < rc.nb_bounces)
+            {
+                const float r1 = rng.next(), r2 = rng.next();
+                const V3 wi = cosine_sample(ns, r1, r2);
+                float pdf;
+                const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
+                if (pdf > 0.0f)
+                {
+                    const V3 atten = f * fabsf(dot(wi, ns)) / pdf;
+                    bool survive = true;
+                    V3 t2 = tp;
+                    if (rc.do_rr && bounce >= rc.rr_min_depth)
+                    {
+                        const float p = fminf(max_comp(t2), 1.0f);
+                        if (rng.next() > p)
+                            survive = false;
+                        else
+                        {
+                            float scale = 1.0f / p;
+                            if (rc.rr_clamp > 0.0f) scale = fminf(scale, rc.rr_clamp);
+                            t2 = t2 * scale;
+                        }
+                    }
+                    if (survive)
+                    {
+                        t2 = t2 * atten;
+                        t2 = v3(fmaxf(t2.x, 1.0e-5f), fmaxf(t2.y, 1.0e-5f), fmaxf(t2.z, 1.0e-5f));
+                        tp = t2;
+                        want_next = true;
+                        nx_d = f4(wi, INFINITY);
+                    }
+                }
+            }
+            if (!is_black(L))
+            {
+                float4 r = pb.radiance[slot];
+                pb.radiance[slot] = make_float4(r.x + L.x, r.y + L.y, r.z + L.z, 0.0f);
+            }
+            store_rng(pb.rng + slot, rng);
+        }
+
+        const int si = warp_append(shadow.count, want_shadow);
+        if (want_shadow)
+        {
+            shadow.origin_tmin[si] = sh_o;
+            shadow.dir_tmax[si] = sh_d;
+            shadow.last_prim[si] = prim;
+            shadow.slot[si] = slot;
+            pb.shadow_entry[slot] = si;
+            pb.pending_light[slot] = f4(light_contrib, 0.0f);
+        }
+        const int bi = warp_append(bsdfq.count, want_bsdf);
+        if (want_bsdf)
+        {
+            bsdfq.origin_tmin[bi] = f4(P, 0.0f);
+            bsdfq.dir_tmax[bi] = bs_d;
+            bsdfq.last_prim[bi] = prim;
+            bsdfq.slot[bi] = slot;
+            pb.bsdf_entry[slot] = bi;
+            pb.pending_bsdf[slot] = bsdf_pending;
+        }
+        const int ni = warp_append(next.count, want_next);
+        if (want_next)
+        {
+            next.origin_tmin[ni] = f4(P, 0.0f);
+            next.dir_tmax[ni] = nx_d;
+            next.last_prim[ni] = prim;
+            next.slot[ni] = slot;
+            pb.throughput[slot] = f4(tp, 0.0f);
+        }
+        warp_count(stats + 1, want_shadow);
+        warp_count(stats + 2, want_bsdf);
+        warp_count(stats + 0, want_next);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// resolve: add the light-sample and BSDF-sample contributions of this bounce, in a fixed order
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue shadow,
+                                                      Queue bsdfq)
+{
+    const int n = *in.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const int slot = in.slot[i];
+        const int se = pb.shadow_entry[slot];
+        const int be = pb.bsdf_entry[slot];
+        if (se < 0 && be < 0) continue;
+        V3 add = v3(0, 0, 0);
+        if (se >= 0 && !shadow.occluded[se]) add = add + xyz(pb.pending_light[slot]);
+        if (be >= 0)
+        {
+            const float4 h = bsdfq.hits[be];
+            const int lprim = __float_as_int(h.w);
+            if (lprim >= 0)
+            {
+                const V3 Le = xyz(s.materials[__ldg(s.material_of + lprim)].emission);
+                if (!is_black(Le))
+                {
+                    V3 a, b, c;
+                    load_triangle(s, lprim, a, b, c);
+                    const V3 nrm = cross(b - a, c - a);
+                    const float len = length(nrm);
+                    const V3 ln = nrm / len;
+                    const V3 wi = xyz(bsdfq.dir_tmax[be]);
+                    const float cos_l = fmaxf(0.0f, dot(ln, -wi));
+                    if (cos_l > 0.0f)
+                    {
+                        const float area = 0.5f * len;
+                        float pdf_area = 1.0f / area;
+                        if (rc.light_sampling == GBPT_LIGHT_POWER)
+                            pdf_area *= (luminance(Le) * area) / s.power_sum;
+                        else
+                            pdf_area /= (float)s.n_emissive;
+                        const float light_pdf = area_to_solid_angle_pdf(pdf_area, h.x, cos_l);
+                        const float4 pend = pb.pending_bsdf[slot];
+                        const float mis = balance_heuristic(pend.w, light_pdf);
+                        add = add + xyz(pend) * Le * mis;
+                    }
+                }
+            }
+        }
+        const float4 r = pb.radiance[slot];
+        pb.radiance[slot] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// accumulate: per pixel, samples of this launch in sample order (FP32 and FP64 sums)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) accumulate_kernel(RenderConst rc, PathBuffers pb, float* __restrict__ acc32,
+                                                         double* __restrict__ acc64)
+{
+    const int n_pix = rc.width * rc.height;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_pix; p += gridDim.x * blockDim.x)
+    {
+        float r = acc32[3 * p], g = acc32[3 * p + 1], b = acc32[3 * p + 2];
+        double R = acc64[3 * p], G = acc64[3 * p + 1], B = acc64[3 * p + 2];
+        for (int k = 0; k < rc.spp; k++)
+        {
+            const float4 v = pb.radiance[(int64_t)k * n_pix + p];
+            r += v.x;
+            g += v.y;
+            b += v.z;
+            R += v.x;
+            G += v.y;
+            B += v.z;
+        }
+        acc32[3 * p] = r;
+        acc32[3 * p + 1] = g;
+        acc32[3 * p + 2] = b;
+        acc64[3 * p] = R;
+        acc64[3 * p + 1] = G;
+        acc64[3 * p + 2] = B;
+    }
+}
+
+__global__ void reset_counts_kernel(int32_t* a, int32_t* b, int32_t* c)
+{
+    if (a) *a = 0;
+    if (b) *b = 0;
+    if (c) *c = 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// emissive power alias table
+// ---------------------------------------------------------------------------------------------
+__global__ void light_power_kernel(SceneView s, float* __restrict__ power)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < s.n_emissive; e += gridDim.x * blockDim.x)
+    {
+        const int t = s.emissive[e];
+        V3 a, b, c;
+        load_triangle(s, t, a, b, c);
+        const float area = 0.5f * length(cross(b - a, c - a));
+        const V3 Le = xyz(s.materials[s.material_of[t]].emission);
+        power[e] = luminance(Le) * area;
+    }
+}
+
+// Deterministic FP64 sum: fixed-shape tree per block, then one block over the partials.
+constexpr int kSumThreads = 256;
+__global__ void __launch_bounds__(kSumThreads) sum_f64_kernel(const float* __restrict__ x, int n,
+                                                              double* __restrict__ partial)
+{
+    __shared__ double sh[kSumThreads];
+    double acc = 0.0;
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+    for (int i = lo + threadIdx.x; i < hi; i += kSumThreads) acc += (double)x[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kSumThreads / 2; w > 0; w >>= 1)
+    {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(kSumThreads) sum_partials_kernel(const double* __restrict__ partial, int n,
+                                                                   double* __restrict__ out)
+{
+    __shared__ double sh[kSumThreads];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += kSumThreads) acc += partial[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kSumThreads / 2; w > 0; w >>= 1)
+    {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+__global__ void normalize_f64_kernel(const float* __restrict__ power, int n, const double* __restrict__ sum,
+                                     double* __restrict__ q)
+{
+    const double s = *sum;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        q[i] = (double)power[i] / s * (double)n;
+}
+
+// Vose's alias method with the reference's queue discipline (src/Utils/Utils.cpp:63-131):
+// smalls/larges are FIFO queues filled in index order; a large that falls to <= 1 moves to the
+// smalls. Runs on one thread (O(n)); the queues are ring buffers of n entries each.
+__global__ void alias_vose_kernel(double* __restrict__ q, int n, float* __restrict__ prob, int32_t* __restrict__ alias,
+                                  int32_t* __restrict__ smalls, int32_t* __restrict__ larges)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int s_head = 0, s_tail = 0, l_head = 0, l_tail = 0;  // tail - head = size; indices mod n
+    for (int i = 0; i < n; i++)
+    {
+        alias[i] = i;
+        if (q[i] < 1.0)
+            smalls[(s_tail++) % n] = i;
+        else
+            larges[(l_tail++) % n] = i;
+    }
+    while (s_tail > s_head && l_tail > l_head)
+    {
+        const int si = smalls[(s_head++) % n];
+        const int li = larges[(l_head++) % n];
+        prob[si] = (float)q[si];
+        alias[si] = li;
+        q[li] = (q[li] + q[si]) - 1.0;
+        if (q[li] > 1.0)
+            larges[(l_tail++) % n] = li;
+        else
+            smalls[(s_tail++) % n] = li;
+    }
+    while (l_tail > l_head) prob[larges[(l_head++) % n]] = 1.0f;
+    while (s_tail > s_head) prob[smalls[(s_head++) % n]] = 1.0f;
+}
+
+inline int grid_for(int64_t n, int threads, int max_blocks)
+{
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > max_blocks) b = max_blocks;
+    return (int)b;
+}
+
+}  // namespace
+
+cudaError_t launch_light_table(const SceneView& s, float* power, double* partial, int n_partial, double* sum64,
+                               double* q, float* prob, int32_t* alias, int32_t* smalls, int32_t* larges,
+                               cudaStream_t st)
+{
+    const int n = s.n_emissive;
+    if (n <= 0) return cudaSuccess;
+    light_power_kernel<<<grid_for(n, 256, 4096), 256, 0, st>>>(s, power);
+    sum_f64_kernel<<<n_partial, kSumThreads, 0, st>>>(power, n, partial);
+    sum_partials_kernel<<<1, kSumThreads, 0, st>>>(partial, n_partial, sum64);
+    normalize_f64_kernel<<<grid_for(n, 256, 4096), 256, 0, st>>>(power, n, sum64, q);
+    alias_vose_kernel<<<1, 1, 0, st>>>(q, n, prob, alias, smalls, larges);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Queue& q, int32_t iteration_base,
+                          unsigned long long* stats, int n_sm, cudaStream_t st)
+{
+    const int64_t n = (int64_t)rc.width * rc.height * rc.spp;
+    camera_kernel<<<grid_for(n, 256, n_sm * 8), 256, 0, st>>>(rc, pb, q, iteration_base, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bounce(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
+                          const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
+                          unsigned long long* stats, int n_sm, cudaStream_t st)
+{
+    const int tgrid = grid_for(capacity, 128, n_sm * 16);
+    reset_counts_kernel<<<1, 1, 0, st>>>(next.count, shadow.count, bsdfq.count);
+    trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, in);
+    shade_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats);
+    trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, shadow);
+    trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, bsdfq);
+    resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate(const RenderConst& rc, const PathBuffers& pb, float* acc32, double* acc64, int n_sm,
+                              cudaStream_t st)
+{
+    accumulate_kernel<<<grid_for((int64_t)rc.width * rc.height, 256, n_sm * 8), 256, 0, st>>>(rc, pb, acc32, acc64);
+    return cudaGetLastError();
+}
+
+}  // namespace gbpt

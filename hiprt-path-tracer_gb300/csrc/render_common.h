@@ -1,0 +1,216 @@
+// Device-side data layout and math shared by the wavefront path-tracing kernels.
+//
+// Restates, for sm_103a, the reference's per-vertex estimator of the megakernel path
+// (src/Device/kernels/Megakernel.h:23-144) with direct lighting by 'sample_one_light_MIS'
+// (src/Device/includes/LightSampling/Lights.h:123-226): one light sample with a shadow ray and one
+// separate BSDF sample with its own ray, combined by the balance heuristic
+// (src/Device/includes/Sampling.h:103-116); emission added at the camera hit only
+// (Lights.h:384-389); continuation by a second BSDF sample with Russian roulette
+// (src/Device/includes/PathTracing.h:44-101, src/Device/includes/RussianRoulette.h:20-55).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbpt_render.h"
+
+namespace gbpt {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.31830988618379067154f;
+constexpr float kTwoPi = 6.28318530717958647693f;
+
+// ---------------------------------------------------------------------------------------------
+// scene view and per-path buffers (all device pointers)
+// ---------------------------------------------------------------------------------------------
+struct DeviceMaterial
+{
+    float4 base_color;  // rgb, w unused
+    float4 emission;    // rgb = emission colour * strength, w unused
+};
+
+struct SceneView
+{
+    const float4* vertices;       // xyz per vertex
+    const int32_t* indices;       // 3 per triangle
+    const int32_t* material_of;   // per triangle
+    const DeviceMaterial* materials;
+    const int32_t* emissive;      // emissive triangle indices
+    const float* alias_prob;      // power alias table (per emissive triangle)
+    const int32_t* alias_index;
+    float power_sum;              // sum of luminance(emission) * area over emissive triangles
+    int32_t n_emissive;
+    const uint4* bvh_nodes;
+    const float4* bvh_tris;
+};
+
+struct Queue
+{
+    float4* origin_tmin;
+    float4* dir_tmax;
+    int32_t* last_prim;
+    int32_t* slot;
+    float4* hits;       // closest-hit output (extension and BSDF-light rays)
+    uint8_t* occluded;  // any-hit output (shadow rays)
+    int32_t* count;     // device counter
+};
+
+struct PathBuffers
+{
+    float4* throughput;     // rgb
+    float4* radiance;       // rgb accumulated over the path
+    uint64_t* rng;          // PCG state
+    float4* pending_light;  // light-sample contribution waiting on its shadow ray
+    float4* pending_bsdf;   // rgb = throughput * f * cos / pdf, w = BSDF pdf
+    int32_t* shadow_entry;  // queue index of the slot's shadow ray this bounce, -1 if none
+    int32_t* bsdf_entry;    // queue index of the slot's BSDF-light ray this bounce, -1 if none
+};
+
+#ifdef __CUDACC__
+// ---------------------------------------------------------------------------------------------
+// small vector helpers
+// ---------------------------------------------------------------------------------------------
+struct V3
+{
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 operator/(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b)
+{
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float length(V3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ V3 normalize(V3 a) { return a / sqrtf(dot(a, a)); }
+__device__ __forceinline__ float max_comp(V3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+__device__ __forceinline__ bool is_black(V3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+__device__ __forceinline__ float luminance(V3 c) { return 0.3086f * c.x + 0.6094f * c.y + 0.0820f * c.z; }
+__device__ __forceinline__ V3 xyz(float4 f) { return v3(f.x, f.y, f.z); }
+__device__ __forceinline__ float4 f4(V3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// ---------------------------------------------------------------------------------------------
+// PCG32 (O'Neill 2014): one 64-bit state per path, stream selected by the render seed.
+// ---------------------------------------------------------------------------------------------
+struct Pcg32
+{
+    uint64_t state;
+    uint64_t inc;
+
+    __device__ __forceinline__ uint32_t next_u32()
+    {
+        const uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = (uint32_t)(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
+    }
+    // uniform float in [0, 1)
+    __device__ __forceinline__ float next() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+    __device__ __forceinline__ int index(int n)
+    {
+        int i = (int)(next() * (float)n);
+        return i < n - 1 ? i : n - 1;
+    }
+};
+
+__device__ __forceinline__ uint64_t pcg_inc(uint32_t seed) { return ((uint64_t)seed << 1u) | 1u; }
+
+// splitmix64 finaliser: decorrelates (pixel, iteration) into an initial PCG state
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ Pcg32 pcg_seed(uint32_t pixel, uint32_t iteration, uint32_t seed)
+{
+    Pcg32 r;
+    r.state = 0;
+    r.inc = pcg_inc(seed);
+    r.next_u32();
+    r.state += mix64(((uint64_t)iteration << 32) | pixel);
+    r.next_u32();
+    return r;
+}
+
+// Row-major 4x4 times point (w = 1) with perspective divide, as the reference's matrix_X_point
+// (src/HostDeviceCommon/Math.h:617-640).
+__device__ __forceinline__ V3 mat_x_point(const float* m, V3 p)
+{
+    float x = m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3];
+    float y = m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7];
+    float z = m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11];
+    float w = m[12] * p.x + m[13] * p.y + m[14] * p.z + m[15];
+    float inv_w = 1.0f;
+    if (!(w < 1.0e-10f && w > -1.0e-10f)) inv_w = 1.0f / w;
+    return v3(x * inv_w, y * inv_w, z * inv_w);
+}
+
+// ---------------------------------------------------------------------------------------------
+// sampling helpers
+// ---------------------------------------------------------------------------------------------
+
+// Cosine-weighted direction around n: normalize(n + uniform point on the unit sphere)
+// (the construction of src/Device/includes/Sampling.h:180-201).
+__device__ __forceinline__ V3 cosine_sample(V3 n, float r1, float r2u)
+{
+    float r2 = 2.0f * r2u - 1.0f;
+    if (r1 < 1.0e-8f && r2 < -0.999999f && n.z > 0.999999f)
+    {
+        r1 += 1.0e-7f;
+        r2 += 1.0e-7f;
+    }
+    const float theta = kTwoPi * r1;
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - r2 * r2));
+    float st, ct;
+    sincosf(theta, &st, &ct);
+    return normalize(n + v3(s * ct, s * st, r2));
+}
+
+// Heitz 2019 square-to-triangle map (src/Device/includes/LightSampling/LightUtils.h:150-164).
+__device__ __forceinline__ void square_to_triangle(float& x, float& y)
+{
+    if (y > x)
+    {
+        x *= 0.5f;
+        y -= x;
+    }
+    else
+    {
+        y *= 0.5f;
+        x -= y;
+    }
+}
+
+__device__ __forceinline__ float balance_heuristic(float pdf_a, float pdf_b)
+{
+    if (pdf_a == 0.0f) return 0.0f;
+    return pdf_a / (pdf_a + pdf_b);
+}
+
+__device__ __forceinline__ float area_to_solid_angle_pdf(float area_pdf, float dist, float cos_light)
+{
+    if (cos_light < 1.0e-8f) return 0.0f;
+    return area_pdf * dist * dist / cos_light;
+}
+
+__device__ __forceinline__ void load_triangle(const SceneView& s, int prim, V3& a, V3& b, V3& c)
+{
+    const int i0 = __ldg(s.indices + 3 * prim), i1 = __ldg(s.indices + 3 * prim + 1), i2 = __ldg(s.indices + 3 * prim + 2);
+    a = xyz(__ldg(s.vertices + i0));
+    b = xyz(__ldg(s.vertices + i1));
+    c = xyz(__ldg(s.vertices + i2));
+}
+
+#endif  // __CUDACC__
+
+}  // namespace gbpt

@@ -1,0 +1,243 @@
+"""Scene, light table and wavefront renderer (host-side mirror of the reference's renderer API).
+
+  * ``Scene(mesh, material_of_triangle, albedo, emission)`` <- GPURenderer::set_scene
+    (src/Renderer/GPURenderer.cpp:952-958): BVH, emissive list, power alias table on the device.
+  * ``Renderer(scene, settings)``                          <- GPURenderer + its render passes
+  * ``Renderer.render(n)``                                 <- GPURendererThread::render_path_tracing
+  * ``Renderer.pass_camera_rays / pass_bounce / pass_accumulate`` <- CameraRays / MegaKernel bounce /
+    path_tracing_accumulate_color, for callers that schedule passes themselves.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import c_vp, i32, i64
+
+LIGHT_UNIFORM = 0
+LIGHT_POWER = 1
+BSDF_LAMBERTIAN = 1
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("base_color", ctypes.c_float * 3), ("emission", ctypes.c_float * 3)]
+
+
+class SceneDesc(ctypes.Structure):
+    _fields_ = [("positions", c_vp), ("n_vertices", i64), ("indices", c_vp), ("n_triangles", i64),
+                ("material_indices", c_vp), ("materials", c_vp), ("n_materials", i32)]
+
+
+class RenderSettingsC(ctypes.Structure):
+    _fields_ = [("width", i32), ("height", i32), ("samples_per_launch", i32), ("nb_bounces", i32),
+                ("do_russian_roulette", i32), ("russian_roulette_min_depth", i32),
+                ("russian_roulette_throughput_clamp", ctypes.c_float), ("light_sampling", i32), ("bsdf", i32),
+                ("seed", ctypes.c_uint32), ("do_jittering", i32), ("reserved", i32),
+                ("inverse_view", ctypes.c_float * 16), ("inverse_projection", ctypes.c_float * 16)]
+
+
+class RenderStatsC(ctypes.Structure):
+    _fields_ = [("samples", i64), ("extension_rays", i64), ("shadow_rays", i64), ("bsdf_light_rays", i64)]
+
+
+RENDER_SIGNATURES = [
+    ("gbpt_scene_create", ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(_lib.BvhParams),
+                                         ctypes.POINTER(c_vp), c_vp]),
+    ("gbpt_scene_destroy", ctypes.c_int, [c_vp]),
+    ("gbpt_scene_get_bvh", ctypes.c_int, [c_vp, ctypes.POINTER(c_vp)]),
+    ("gbpt_scene_get_light_table", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    ("gbpt_renderer_create", ctypes.c_int, [c_vp, ctypes.POINTER(RenderSettingsC), ctypes.POINTER(c_vp)]),
+    ("gbpt_renderer_destroy", ctypes.c_int, [c_vp]),
+    ("gbpt_renderer_reset", ctypes.c_int, [c_vp, c_vp]),
+    ("gbpt_render", ctypes.c_int, [c_vp, i32, c_vp]),
+    ("gbpt_pass_camera_rays", ctypes.c_int, [c_vp, c_vp]),
+    ("gbpt_pass_bounce", ctypes.c_int, [c_vp, i32, c_vp]),
+    ("gbpt_pass_accumulate", ctypes.c_int, [c_vp, c_vp]),
+    ("gbpt_renderer_get_image", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp]),
+    ("gbpt_renderer_get_stats", ctypes.c_int, [c_vp, ctypes.POINTER(RenderStatsC), c_vp]),
+]
+
+
+def _stream(stream) -> int:
+    import torch
+    if stream is None:
+        return int(torch.cuda.current_stream().cuda_stream)
+    return int(stream.cuda_stream)
+
+
+def look_at_camera(eye, target, up=(0.0, 1.0, 0.0), vfov_deg=40.0, aspect=1.0, near=0.1, far=100.0):
+    """(inverse_view, inverse_projection), row-major float32 4x4, points multiplied on the right.
+    View space looks down -z (OpenGL convention); NDC (x, y, -1) maps to the near plane."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, np.asarray(up, np.float64))
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    inv_view = np.eye(4)
+    inv_view[:3, 0], inv_view[:3, 1], inv_view[:3, 2], inv_view[:3, 3] = s, u, -f, eye
+    t = np.tan(np.radians(vfov_deg) / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0] = 1 / (aspect * t)
+    proj[1, 1] = 1 / t
+    proj[2, 2] = -(far + near) / (far - near)
+    proj[2, 3] = -2 * far * near / (far - near)
+    proj[3, 2] = -1
+    return inv_view.astype(np.float32), np.linalg.inv(proj).astype(np.float32)
+
+
+@dataclass
+class RenderSettings:
+    width: int = 256
+    height: int = 256
+    samples_per_launch: int = 1
+    nb_bounces: int = 4
+    do_russian_roulette: bool = True
+    russian_roulette_min_depth: int = 3
+    russian_roulette_throughput_clamp: float = 0.0
+    light_sampling: int = LIGHT_UNIFORM
+    bsdf: int = BSDF_LAMBERTIAN
+    seed: int = 1
+    do_jittering: bool = True
+    inverse_view: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
+    inverse_projection: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
+
+    def to_c(self) -> RenderSettingsC:
+        c = RenderSettingsC()
+        for k in ("width", "height", "samples_per_launch", "nb_bounces", "russian_roulette_min_depth",
+                  "light_sampling", "bsdf", "seed"):
+            setattr(c, k, int(getattr(self, k)))
+        c.do_russian_roulette = 1 if self.do_russian_roulette else 0
+        c.do_jittering = 1 if self.do_jittering else 0
+        c.russian_roulette_throughput_clamp = float(self.russian_roulette_throughput_clamp)
+        c.inverse_view[:] = [float(v) for v in np.asarray(self.inverse_view, np.float32).reshape(16)]
+        c.inverse_projection[:] = [float(v) for v in np.asarray(self.inverse_projection, np.float32).reshape(16)]
+        return c
+
+
+def _load():
+    lib = _lib.load()
+    if not getattr(lib, "_render_sigs", False):
+        for name, res, args in RENDER_SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        lib._render_sigs = True
+    return lib
+
+
+class Scene:
+    def __init__(self, positions, indices, material_of_triangle, albedo, emission, stream=None, sah_bins=32,
+                 max_leaf_size=3):
+        lib = _load()
+        self._pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        self._idx = np.ascontiguousarray(indices, np.int32).reshape(-1, 3)
+        self._mat_of = np.ascontiguousarray(material_of_triangle, np.int32).reshape(-1)
+        alb = np.asarray(albedo, np.float32).reshape(-1, 3)
+        emi = np.asarray(emission, np.float32).reshape(-1, 3)
+        self._mats = (Material * len(alb))()
+        for k in range(len(alb)):
+            self._mats[k].base_color[:] = [float(v) for v in alb[k]]
+            self._mats[k].emission[:] = [float(v) for v in emi[k]]
+        desc = SceneDesc(self._pos.ctypes.data, self._pos.shape[0], self._idx.ctypes.data, self._idx.shape[0],
+                         self._mat_of.ctypes.data, ctypes.addressof(self._mats), len(alb))
+        params = _lib.BvhParams(sah_bins, max_leaf_size, 0)
+        h = c_vp()
+        _lib.check(lib.gbpt_scene_create(ctypes.byref(desc), ctypes.byref(params), ctypes.byref(h), _stream(stream)))
+        self._h = h
+        self._lib = lib
+
+    @classmethod
+    def from_cornell(cls, cb, **kw):
+        return cls(cb.mesh.positions, cb.mesh.indices, cb.material_of_triangle, cb.albedo, cb.emission, **kw)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def light_table(self):
+        n = ctypes.c_int32()
+        _lib.check(self._lib.gbpt_scene_get_light_table(self._h, ctypes.addressof(n), None, None, None, None, None))
+        e = np.zeros(n.value, np.int32)
+        p = np.zeros(n.value, np.float32)
+        a = np.zeros(n.value, np.int32)
+        s32 = ctypes.c_float()
+        s64 = ctypes.c_double()
+        _lib.check(self._lib.gbpt_scene_get_light_table(self._h, None, e.ctypes.data, p.ctypes.data, a.ctypes.data,
+                                                        ctypes.addressof(s32), ctypes.addressof(s64)))
+        return {"emissive": e, "probas": p, "alias": a, "power_sum": s32.value, "power_sum64": s64.value}
+
+    def destroy(self):
+        if getattr(self, "_h", None):
+            _lib.check(self._lib.gbpt_scene_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Renderer:
+    def __init__(self, scene: Scene, settings: RenderSettings):
+        lib = _load()
+        self.scene = scene  # keeps the scene alive
+        self.settings = settings
+        h = c_vp()
+        c = settings.to_c()
+        _lib.check(lib.gbpt_renderer_create(scene.handle, ctypes.byref(c), ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def render(self, n_launches: int = 1, stream=None):
+        _lib.check(self._lib.gbpt_render(self._h, n_launches, _stream(stream)))
+
+    def reset(self, stream=None):
+        _lib.check(self._lib.gbpt_renderer_reset(self._h, _stream(stream)))
+
+    def pass_camera_rays(self, stream=None):
+        _lib.check(self._lib.gbpt_pass_camera_rays(self._h, _stream(stream)))
+
+    def pass_bounce(self, bounce: int, stream=None):
+        _lib.check(self._lib.gbpt_pass_bounce(self._h, bounce, _stream(stream)))
+
+    def pass_accumulate(self, stream=None):
+        _lib.check(self._lib.gbpt_pass_accumulate(self._h, _stream(stream)))
+
+    def image_sums(self, stream=None):
+        """(FP32 sums, FP64 sums) as (H, W, 3) arrays; row 0 is the bottom row."""
+        w, h = self.settings.width, self.settings.height
+        a32 = np.zeros((h, w, 3), np.float32)
+        a64 = np.zeros((h, w, 3), np.float64)
+        _lib.check(self._lib.gbpt_renderer_get_image(self._h, a32.ctypes.data, a64.ctypes.data, _stream(stream)))
+        return a32, a64
+
+    def stats(self, stream=None) -> dict:
+        s = RenderStatsC()
+        _lib.check(self._lib.gbpt_renderer_get_stats(self._h, ctypes.byref(s), _stream(stream)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def destroy(self):
+        if getattr(self, "_h", None):
+            _lib.check(self._lib.gbpt_renderer_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def cornell_settings(width=256, height=256, **kw) -> RenderSettings:
+    """The Cornell-box configuration: camera at (2.75, 2.75, -8) looking +z, 40 degree vertical
+    FOV, 4 bounces, Russian roulette from bounce 3, uniform light sampling, Lambertian BSDF."""
+    iv, ip = look_at_camera((2.75, 2.75, -8.0), (2.75, 2.75, 0.0), vfov_deg=40.0, aspect=width / height)
+    s = RenderSettings(width=width, height=height, inverse_view=iv, inverse_projection=ip)
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s

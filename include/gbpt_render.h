@@ -1,0 +1,120 @@
+/*
+ * gbpt — render path C ABI: scene upload, emissive power alias table, wavefront path tracer.
+ *
+ * Mirrors the reference's render-data / render-settings surface for the parts this path uses
+ * (HIPRTRenderData src/HostDeviceCommon/RenderData.h:93-129, HIPRTRenderSettings
+ * src/HostDeviceCommon/RenderSettings.h:24-278, HIPRTCamera src/HostDeviceCommon/HIPRTCamera.h:16-53)
+ * and its per-pass kernel entry points (CameraRays src/Device/kernels/CameraRays.h:83,
+ * MegaKernel src/Device/kernels/Megakernel.h:23). Plain C types only; see gbpt.h for the status codes.
+ */
+#ifndef GBPT_RENDER_H
+#define GBPT_RENDER_H
+
+#include "gbpt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbpt_scene gbpt_scene;
+typedef struct gbpt_renderer gbpt_renderer;
+
+/* Material subset of the reference's CPUMaterial (src/HostDeviceCommon/Material/MaterialUnpacked.h):
+ * base colour and emission (= emission colour * emission_strength * global_emissive_factor). */
+typedef struct gbpt_material {
+    float base_color[3];
+    float emission[3];
+} gbpt_material;
+
+/* Mirrors the reference's Scene (src/Scene/SceneParser.h:109-170): flat triangle soup with a
+ * material index per triangle. Host pointers. */
+typedef struct gbpt_scene_desc {
+    const float* positions;          /* 3 per vertex */
+    int64_t n_vertices;
+    const int32_t* indices;          /* 3 per triangle */
+    int64_t n_triangles;
+    const int32_t* material_indices; /* 1 per triangle */
+    const gbpt_material* materials;
+    int32_t n_materials;
+} gbpt_scene_desc;
+
+/* Uploads the scene, builds its BVH (gbpt_bvh_build), the emissive-triangle list (triangles
+ * whose material has non-black emission, in triangle order, as the reference's scene parser
+ * collects them) and the power alias table on the device.
+ * Replaces GPURenderer::set_scene (src/Renderer/GPURenderer.cpp:952-958) and
+ * compute_emissives_power_alias_table (src/Renderer/GPURenderer.cpp:173,221-295 with
+ * Utils::compute_alias_table src/Utils/Utils.cpp:63-131). Power = luminance(emission) * area in
+ * float as the reference computes it; the sum and the normalisation run in FP64 on the device
+ * (the reference sums in float), then the Vose partition with the reference's queue order. */
+GBPT_API gbpt_status gbpt_scene_create(const gbpt_scene_desc* desc, const gbpt_bvh_params* bvh_params,
+                                       gbpt_scene** out, void* stream);
+GBPT_API gbpt_status gbpt_scene_destroy(gbpt_scene* scene);
+/* Borrowed pointer to the scene's BVH (owned by the scene). */
+GBPT_API gbpt_status gbpt_scene_get_bvh(const gbpt_scene* scene, const gbpt_bvh** out);
+/* Copies the emissive list and power alias table to host arrays of n_emissive entries each
+ * (DeviceAliasTable src/Device/includes/AliasTable.h:11-29). Any pointer may be NULL. */
+GBPT_API gbpt_status gbpt_scene_get_light_table(const gbpt_scene* scene, int32_t* n_emissive, int32_t* emissive,
+                                                float* probas, int32_t* alias, float* power_sum, double* power_sum64);
+
+enum {
+    GBPT_LIGHT_UNIFORM = 0, /* LSS_BASE_UNIFORM */
+    GBPT_LIGHT_POWER = 1    /* LSS_BASE_POWER */
+};
+enum {
+    GBPT_BSDF_LAMBERTIAN = 1 /* BSDFOverride = BSDF_LAMBERTIAN (src/Device/includes/Dispatcher.h:21-82) */
+};
+
+/* Subset of HIPRTRenderSettings + HIPRTCamera used by the render path. */
+typedef struct gbpt_render_settings {
+    int32_t width, height;
+    int32_t samples_per_launch;      /* spp traced together in one wavefront (>= 1) */
+    int32_t nb_bounces;              /* render_settings.nb_bounces */
+    int32_t do_russian_roulette;     /* render_settings.do_russian_roulette */
+    int32_t russian_roulette_min_depth;
+    float russian_roulette_throughput_clamp; /* 0 = no clamp */
+    int32_t light_sampling;          /* GBPT_LIGHT_* */
+    int32_t bsdf;                    /* GBPT_BSDF_* */
+    uint32_t seed;
+    int32_t do_jittering;            /* HIPRTCamera::do_jittering */
+    int32_t reserved;
+    float inverse_view[16];          /* row-major, points multiplied on the right */
+    float inverse_projection[16];
+} gbpt_render_settings;
+
+typedef struct gbpt_render_stats {
+    int64_t samples;         /* path samples accumulated since the last reset */
+    int64_t extension_rays;  /* closest-hit rays traced (camera + bounce) */
+    int64_t shadow_rays;     /* any-hit rays traced */
+    int64_t bsdf_light_rays; /* closest-hit rays traced for the MIS BSDF sample */
+} gbpt_render_stats;
+
+GBPT_API gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_settings* settings,
+                                          gbpt_renderer** out);
+GBPT_API gbpt_status gbpt_renderer_destroy(gbpt_renderer* r);
+GBPT_API gbpt_status gbpt_renderer_reset(gbpt_renderer* r, void* stream);
+
+/* Full frame: n_launches x (camera rays + nb_bounces+1 wavefront bounces + accumulate), each
+ * launch adding samples_per_launch samples per pixel. Replaces the render loop of
+ * GPURendererThread::render_path_tracing (src/Renderer/GPURendererThread.cpp:311-330) over the
+ * FillGBuffer and MegaKernel passes. */
+GBPT_API gbpt_status gbpt_render(gbpt_renderer* r, int32_t n_launches, void* stream);
+
+/* The same passes one by one (for callers that schedule passes themselves):
+ * camera rays   <- CameraRays (src/Device/kernels/CameraRays.h:83)
+ * bounce k      <- one iteration of MegaKernel's bounce loop (src/Device/kernels/Megakernel.h:88-131)
+ * accumulate    <- path_tracing_accumulate_color (src/Device/includes/PathTracing.h:176-217) */
+GBPT_API gbpt_status gbpt_pass_camera_rays(gbpt_renderer* r, void* stream);
+GBPT_API gbpt_status gbpt_pass_bounce(gbpt_renderer* r, int32_t bounce, void* stream);
+GBPT_API gbpt_status gbpt_pass_accumulate(gbpt_renderer* r, void* stream);
+
+/* Copies the accumulated sums (not divided by the sample count) to host memory:
+ * rgb32 = FP32 sums (W*H*3), rgb64 = FP64 sums (W*H*3); either may be NULL. Pixel (x, y) is at
+ * index x + y*W with y = 0 the bottom row (the reference's NDC convention). Synchronous. */
+GBPT_API gbpt_status gbpt_renderer_get_image(gbpt_renderer* r, float* rgb32, double* rgb64, void* stream);
+GBPT_API gbpt_status gbpt_renderer_get_stats(gbpt_renderer* r, gbpt_render_stats* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPT_RENDER_H */

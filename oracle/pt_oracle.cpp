@@ -1,0 +1,417 @@
+/*
+ * TEST INFRASTRUCTURE ONLY — CPU oracle of the path-tracing estimator and of the power alias table.
+ *
+ * Only tests/ and __graft_entry__.smoke() call this, as a checker. It restates, in plain C++ with
+ * -ffp-contract=off, the reference's per-pixel estimator for a Lambertian scene:
+ *   - camera ray with jitter: CameraRays (src/Device/kernels/CameraRays.h:162-172) and
+ *     HIPRTCamera::get_camera_ray (src/HostDeviceCommon/HIPRTCamera.h:31-52, matrix_X_point
+ *     src/HostDeviceCommon/Math.h:617-640);
+ *   - bounce loop of MegaKernel (src/Device/kernels/Megakernel.h:88-131): emission at bounce 0
+ *     (src/Device/includes/LightSampling/Lights.h:384-389), direct lighting by
+ *     sample_one_light_MIS (Lights.h:123-226) = one light sample (uniform or power alias,
+ *     LightUtils.h:248-309, Heitz square-to-triangle LightUtils.h:150-199, area->solid angle
+ *     PDFConversion.h:32-38, one-sided lights PDFConversion.h:19-30) + one BSDF sample with its
+ *     own closest-hit ray (Intersect.h:544-643), balance heuristic (Sampling.h:103-116);
+ *   - continuation: Lambertian sample (Lambertian.h:14-58, Sampling.h:180-201), throughput update
+ *     and Russian roulette (PathTracing.h:44-101, RussianRoulette.h:20-55), 1e-5 throughput floor;
+ *   - fix_backfacing_normals (Intersect.h:142-176);
+ *   - closest hit by exhaustive Moller-Trumbore (Triangle.h:20-63) with the self-hit filter.
+ * Random numbers come from PCG32 in the same order as the GPU kernels draw them (camera jitter 2,
+ * then per vertex: light index 1 [+1 for the alias test], light point 2, MIS BSDF sample 2,
+ * continuation 2, Russian roulette 1), so GPU and oracle images agree sample by sample up to
+ * floating-point contraction.
+ *
+ * orc_vose_alias restates Utils::compute_alias_table (src/Utils/Utils.cpp:63-131).
+ */
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct V { float x, y, z; };
+inline V mk(float x, float y, float z) { return V{x, y, z}; }
+inline V operator+(V a, V b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V operator-(V a, V b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V operator*(V a, V b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline V operator*(V a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+inline V operator/(V a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+inline V neg(V a) { return mk(-a.x, -a.y, -a.z); }
+inline float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V cross(V a, V b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline float len(V a) { return std::sqrt(dot(a, a)); }
+inline V nrm(V a) { return a / std::sqrt(dot(a, a)); }
+inline bool black(V a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+inline float lum(V c) { return 0.3086f * c.x + 0.6094f * c.y + 0.0820f * c.z; }
+
+struct Pcg
+{
+    uint64_t state, inc;
+    uint32_t u32()
+    {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    }
+    float next() { return (float)(u32() >> 8) * (1.0f / 16777216.0f); }
+    int index(int n)
+    {
+        int i = (int)(next() * (float)n);
+        return i < n - 1 ? i : n - 1;
+    }
+};
+
+uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+Pcg pcg_seed(uint32_t pixel, uint32_t iteration, uint32_t seed)
+{
+    Pcg r;
+    r.state = 0;
+    r.inc = ((uint64_t)seed << 1u) | 1u;
+    r.u32();
+    r.state += mix64(((uint64_t)iteration << 32) | pixel);
+    r.u32();
+    return r;
+}
+
+V mat_point(const float* m, V p)
+{
+    float x = m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3];
+    float y = m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7];
+    float z = m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11];
+    float w = m[12] * p.x + m[13] * p.y + m[14] * p.z + m[15];
+    float iw = 1.0f;
+    if (!(w < 1.0e-10f && w > -1.0e-10f)) iw = 1.0f / w;
+    return mk(x * iw, y * iw, z * iw);
+}
+
+struct Scene
+{
+    const float* tv;
+    int nt;
+    const int* mat_of;
+    const float* albedo;
+    const float* emission;
+    const int* emissive;
+    int ne;
+    const float* alias_prob;
+    const int* alias_idx;
+    float power_sum;
+    V a(int t) const { return mk(tv[9 * t], tv[9 * t + 1], tv[9 * t + 2]); }
+    V b(int t) const { return mk(tv[9 * t + 3], tv[9 * t + 4], tv[9 * t + 5]); }
+    V c(int t) const { return mk(tv[9 * t + 6], tv[9 * t + 7], tv[9 * t + 8]); }
+    V alb(int t) const { int m = mat_of[t]; return mk(albedo[3 * m], albedo[3 * m + 1], albedo[3 * m + 2]); }
+    V emi(int t) const { int m = mat_of[t]; return mk(emission[3 * m], emission[3 * m + 1], emission[3 * m + 2]); }
+};
+
+bool mt(V A, V B, V C, V o, V d, float& t)
+{
+    const float EPS = 0.0000001f;
+    V e1 = B - A, e2 = C - A;
+    V h = cross(d, e2);
+    float a = dot(e1, h);
+    if (a > -EPS && a < EPS) return false;
+    float f = 1.0f / a;
+    V s = o - A;
+    float u = f * dot(s, h);
+    if (u < 0.0f || u > 1.0f) return false;
+    V q = cross(s, e1);
+    float v = f * dot(d, q);
+    if (v < 0.0f || u + v > 1.0f) return false;
+    t = f * dot(e2, q);
+    return t > EPS;
+}
+
+// closest hit with the self-hit filter; returns prim or -1 (lowest index on exact ties)
+int closest(const Scene& s, V o, V d, int skip, float& t_out)
+{
+    int best = -1;
+    float bt = 0.0f;
+    for (int k = 0; k < s.nt; k++)
+    {
+        float t;
+        if (k == skip || !mt(s.a(k), s.b(k), s.c(k), o, d, t)) continue;
+        if (best < 0 || t < bt)
+        {
+            best = k;
+            bt = t;
+        }
+    }
+    t_out = bt;
+    return best;
+}
+
+bool occluded(const Scene& s, V o, V d, int skip, float tmax)
+{
+    float t;
+    int p = closest(s, o, d, skip, t);
+    return p >= 0 && t < tmax;
+}
+
+V cosine_sample(V n, float r1, float r2u)
+{
+    float r2 = 2.0f * r2u - 1.0f;
+    if (r1 < 1.0e-8f && r2 < -0.999999f && n.z > 0.999999f)
+    {
+        r1 += 1.0e-7f;
+        r2 += 1.0e-7f;
+    }
+    float theta = 6.28318530717958647693f * r1;
+    float sn = std::sqrt(std::max(0.0f, 1.0f - r2 * r2));
+    return nrm(n + mk(sn * std::cos(theta), sn * std::sin(theta), r2));
+}
+
+V lambert(V albedo, float NoL, float& pdf)
+{
+    pdf = 0.0f;
+    if (NoL <= 0.0f) return mk(0, 0, 0);
+    pdf = NoL * 0.31830988618379067154f;
+    return albedo * 0.31830988618379067154f;
+}
+
+float light_pdf_area(const Scene& s, int lt, float area, V Le, int strategy)
+{
+    float p = 1.0f / area;
+    if (strategy == 1)
+        p *= (lum(Le) * area) / s.power_sum;
+    else
+        p /= (float)s.ne;
+    return p;
+}
+
+float balance(float a, float b) { return a == 0.0f ? 0.0f : a / (a + b); }
+
+float a2s(float area_pdf, float dist, float cosl) { return cosl < 1.0e-8f ? 0.0f : area_pdf * dist * dist / cosl; }
+
+struct Settings
+{
+    int width, height, nb_bounces, do_rr, rr_min, light, seed, jitter, spp, iteration_base;
+    float rr_clamp;
+    const float* iv;
+    const float* ip;
+};
+
+V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
+{
+    const int x = pixel % st.width, y = pixel / st.width;
+    Pcg rng = pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
+    float px = x + 0.5f, py = y + 0.5f;
+    if (st.jitter)
+    {
+        px += rng.next() - 0.5f;
+        py += rng.next() - 0.5f;
+    }
+    float xn = px / st.width * 2.0f - 1.0f, yn = py / st.height * 2.0f - 1.0f;
+    V o = mat_point(st.iv, mk(0, 0, 0));
+    V pv = mat_point(st.ip, mk(xn, yn, -1.0f));
+    V pw = mat_point(st.iv, pv);
+    V d = nrm(pw - o);
+    int skip = -1;
+    V tp = mk(1, 1, 1), L = mk(0, 0, 0);
+    for (int bounce = 0; bounce <= st.nb_bounces; bounce++)
+    {
+        float t;
+        int prim = closest(s, o, d, skip, t);
+        if (prim < 0) break;
+        V P = o + d * t;
+        V ng = nrm(cross(s.b(prim) - s.a(prim), s.c(prim) - s.a(prim)));
+        V ns = ng;
+        V view = neg(d);
+        if (dot(view, ng) < 0.0f) { ng = neg(ng); ns = neg(ns); }
+        if (dot(view, ns) < 0.0f) ns = neg(ns);
+        V refl = ns * (2.0f * dot(view, ns)) - view;
+        if (dot(refl, ng) <= 0.0f)
+        {
+            refl = refl - nrm(ng * (dot(refl, ng) - 0.01f));
+            ns = nrm(view + refl);
+        }
+        V albedo = s.alb(prim);
+        if (bounce == 0) L = L + s.emi(prim);
+        if (s.ne > 0)
+        {
+            int e;
+            if (st.light == 1)
+            {
+                e = rng.index(s.ne);
+                if (rng.next() > s.alias_prob[e]) e = s.alias_idx[e];
+            }
+            else
+                e = rng.index(s.ne);
+            int lt = s.emissive[e];
+            float r1 = rng.next(), r2 = rng.next();
+            if (r2 > r1) { r1 *= 0.5f; r2 -= r1; }
+            else { r2 *= 0.5f; r1 -= r2; }
+            V la = s.a(lt), ab = s.b(lt) - la, ac = s.c(lt) - la;
+            V n = cross(ab, ac);
+            float ln = len(n);
+            V lp = la + ab * r1 + ac * r2;
+            V lnrm = n / ln;
+            float area = 0.5f * ln;
+            V Le = s.emi(lt);
+            float pa = light_pdf_area(s, lt, area, Le, st.light);
+            if (pa > 0.0f)
+            {
+                V tl = lp - P;
+                float dist = len(tl);
+                V wi = tl / dist;
+                float bp;
+                V f = lambert(albedo, dot(ns, wi), bp);
+                if (bp > 0.0f)
+                {
+                    float cl = std::max(0.0f, dot(lnrm, neg(wi)));
+                    if (cl > 1.0e-5f)
+                    {
+                        float lpdf = a2s(pa, dist, cl);
+                        float mis = balance(lpdf, bp);
+                        V c = tp * (f * std::fabs(dot(ns, wi)) * Le * mis / lpdf);
+                        if (!black(c) && !occluded(s, P, wi, prim, dist - 1.0e-4f)) L = L + c;
+                    }
+                }
+            }
+        }
+        {
+            float r1 = rng.next(), r2 = rng.next();
+            V wi = cosine_sample(ns, r1, r2);
+            float pdf;
+            V f = lambert(albedo, dot(ns, wi), pdf);
+            if (pdf > 0.0f && s.ne > 0)
+            {
+                V w = tp * (f * std::fabs(dot(ns, wi)) / pdf);
+                float th;
+                int lp = closest(s, P, wi, prim, th);
+                if (lp >= 0 && th < 1.0e35f - 1.0e-4f)
+                {
+                    V Le = s.emi(lp);
+                    if (!black(Le))
+                    {
+                        V n = cross(s.b(lp) - s.a(lp), s.c(lp) - s.a(lp));
+                        float ln = len(n);
+                        float cl = std::max(0.0f, dot(n / ln, neg(wi)));
+                        if (cl > 0.0f)
+                        {
+                            float lpdf = a2s(light_pdf_area(s, lp, 0.5f * ln, Le, st.light), th, cl);
+                            L = L + w * Le * balance(pdf, lpdf);
+                        }
+                    }
+                }
+            }
+        }
+        if (bounce == st.nb_bounces) break;
+        float r1 = rng.next(), r2 = rng.next();
+        V wi = cosine_sample(ns, r1, r2);
+        float pdf;
+        V f = lambert(albedo, dot(ns, wi), pdf);
+        if (pdf <= 0.0f) break;
+        V att = f * std::fabs(dot(wi, ns)) / pdf;
+        if (st.do_rr && bounce >= st.rr_min)
+        {
+            float p = std::min(std::max(tp.x, std::max(tp.y, tp.z)), 1.0f);
+            if (rng.next() > p) break;
+            float sc = 1.0f / p;
+            if (st.rr_clamp > 0.0f) sc = std::min(sc, st.rr_clamp);
+            tp = tp * sc;
+        }
+        tp = tp * att;
+        tp = mk(std::max(tp.x, 1.0e-5f), std::max(tp.y, 1.0e-5f), std::max(tp.z, 1.0e-5f));
+        o = P;
+        d = wi;
+        skip = prim;
+    }
+    return L;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* settings_i: width, height, nb_bounces, do_rr, rr_min_depth, light_sampling (0 uniform, 1 power),
+ * seed, do_jittering, spp, iteration_base. Adds the samples of iterations
+ * [iteration_base, iteration_base + spp) to out_rgb (W*H*3 doubles). */
+void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const float* albedo, const float* emission,
+                   const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx, float power_sum,
+                   const int* settings_i, float rr_clamp, const float* inv_view, const float* inv_proj, double* out_rgb,
+                   int nthreads)
+{
+    Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
+    Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
+                settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj};
+    const int npix = st.width * st.height;
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int w = 0; w < nthreads; w++)
+        pool.emplace_back([&]() {
+            for (;;)
+            {
+                int p = next.fetch_add(1);
+                if (p >= npix) break;
+                double r = 0, g = 0, b = 0;
+                for (int k = 0; k < st.spp; k++)
+                {
+                    V c = trace_path(s, st, p, st.iteration_base + k);
+                    r += c.x;
+                    g += c.y;
+                    b += c.z;
+                }
+                out_rgb[3 * p] += r;
+                out_rgb[3 * p + 1] += g;
+                out_rgb[3 * p + 2] += b;
+            }
+        });
+    for (auto& t : pool) t.join();
+}
+
+/* Vose alias table exactly as src/Utils/Utils.cpp:63-131: elements normalised in double by
+ * 'total_sum' (as given) and scaled by n; FIFO small/large queues in index order. */
+void orc_vose_alias(const float* input, int n, double total_sum, float* out_prob, int* out_alias)
+{
+    std::vector<double> q(n);
+    for (int i = 0; i < n; i++) q[i] = (double)input[i] / total_sum * n;
+    std::deque<int> smalls, larges;
+    for (int i = 0; i < n; i++)
+    {
+        out_alias[i] = i;
+        if (q[i] < 1.0f)
+            smalls.push_back(i);
+        else
+            larges.push_back(i);
+    }
+    while (!smalls.empty() && !larges.empty())
+    {
+        int si = smalls.front(), li = larges.front();
+        smalls.pop_front();
+        larges.pop_front();
+        out_prob[si] = (float)q[si];
+        out_alias[si] = li;
+        q[li] = (q[li] + q[si]) - 1.0f;
+        if (q[li] > 1.0f)
+            larges.push_back(li);
+        else
+            smalls.push_back(li);
+    }
+    while (!larges.empty())
+    {
+        out_prob[larges.front()] = 1.0f;
+        larges.pop_front();
+    }
+    while (!smalls.empty())
+    {
+        out_prob[smalls.front()] = 1.0f;
+        smalls.pop_front();
+    }
+}
+
+} // extern "C"

@@ -161,3 +161,58 @@ class RefBVH:
         self.lib().ref_shadow_occluded(self.h, _ptr(o, _c_f), _ptr(d, _c_f), _ptr(lp, _c_i), _ptr(ld, _c_f), len(o),
                                        _ptr(occ, _c_u8))
         return occ
+
+
+def _pt_lib():
+    orc = Oracle()
+    lib = orc.lib
+    if not getattr(lib, "_pt_sigs", False):
+        lib.orc_pt_render.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, _c_f, _c_i, ctypes.c_int, _c_f, _c_i,
+                                      ctypes.c_float, _c_i, ctypes.c_float, _c_f, _c_f,
+                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        lib.orc_vose_alias.argtypes = [_c_f, ctypes.c_int, ctypes.c_double, _c_f, _c_i]
+        lib._pt_sigs = True
+    return lib
+
+
+def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_idx, power_sum, settings, spp,
+              iteration_base=0, nthreads=0):
+    """Path-tracing oracle (Lambertian scenes). Returns the FP64 per-pixel sums (H, W, 3) of
+    'spp' samples per pixel, drawn with the same PCG sequence as the GPU kernels."""
+    lib = _pt_lib()
+    soup = np.ascontiguousarray(soup, np.float32)
+    mo = np.ascontiguousarray(material_of, np.int32)
+    al = np.ascontiguousarray(albedo, np.float32)
+    em = np.ascontiguousarray(emission, np.float32)
+    ei = np.ascontiguousarray(emissive, np.int32)
+    ap = np.ascontiguousarray(alias_prob if alias_prob is not None else np.ones(len(ei)), np.float32)
+    ai = np.ascontiguousarray(alias_idx if alias_idx is not None else np.arange(len(ei)), np.int32)
+    s = settings
+    si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0, s.russian_roulette_min_depth,
+                   s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base], np.int32)
+    iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
+    ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
+    out = np.zeros((s.height, s.width, 3), np.float64)
+    lib.orc_pt_render(_ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(al, _c_f), _ptr(em, _c_f), _ptr(ei, _c_i),
+                      len(ei), _ptr(ap, _c_f), _ptr(ai, _c_i), float(power_sum), _ptr(si, _c_i),
+                      float(s.russian_roulette_throughput_clamp), _ptr(iv, _c_f), _ptr(ip, _c_f),
+                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads)
+    return out
+
+
+def vose_alias(power: np.ndarray, total_sum: float):
+    """Utils::compute_alias_table restated (src/Utils/Utils.cpp:63-131)."""
+    lib = _pt_lib()
+    p = np.ascontiguousarray(power, np.float32)
+    prob = np.zeros(len(p), np.float32)
+    alias = np.zeros(len(p), np.int32)
+    lib.orc_vose_alias(_ptr(p, _c_f), len(p), float(total_sum), _ptr(prob, _c_f), _ptr(alias, _c_i))
+    return prob, alias
+
+
+def alias_distribution(prob: np.ndarray, alias: np.ndarray) -> np.ndarray:
+    """Probability of each index under the alias sampler (pick uniform i, keep it with prob[i])."""
+    n = len(prob)
+    d = prob.astype(np.float64).copy()
+    np.add.at(d, alias, 1.0 - prob.astype(np.float64))
+    return d / n

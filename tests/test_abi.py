@@ -9,12 +9,16 @@ import pytest
 import gbpt
 from gbpt import _lib
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "gbpt.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
 
 
 def declared_symbols():
-    text = open(HEADER).read()
-    return sorted(set(re.findall(r"GBPT_API\s+[^;]*?\b(gbpt_\w+)\s*\(", text, re.S)))
+    names = set()
+    for h in sorted(os.listdir(INCLUDE)):
+        if h.endswith(".h"):
+            text = open(os.path.join(INCLUDE, h)).read()
+            names |= set(re.findall(r"GBPT_API\s+[^;]*?\b(gbpt_\w+)\s*\(", text, re.S))
+    return sorted(names)
 
 
 def test_library_exports_every_declared_symbol():
@@ -23,7 +27,9 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 10
     for n in names:
         assert hasattr(lib, n), n
-    assert {n for n, _, _ in _lib.SIGNATURES} == set(names)
+    from gbpt import render
+    bound = {n for n, _, _ in _lib.SIGNATURES} | {n for n, _, _ in render.RENDER_SIGNATURES}
+    assert bound == set(names)
 
 
 def test_status_strings_and_version():
