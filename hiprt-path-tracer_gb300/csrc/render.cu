@@ -420,6 +420,10 @@ __global__ void reset_counts_kernel(int32_t* a, int32_t* b, int32_t* c)
 // ---------------------------------------------------------------------------------------------
 // emissive power alias table
 // ---------------------------------------------------------------------------------------------
+// Power of one emissive triangle = luminance(emission) * area, with every float operation rounded
+// separately in the reference's order (GPURenderer::compute_emissives_power_alias_table,
+// src/Renderer/GPURenderer.cpp:256-275, computed on the host without FMA contraction), so the
+// power list is bit-identical to the reference's.
 __global__ void light_power_kernel(SceneView s, float* __restrict__ power)
 {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < s.n_emissive; e += gridDim.x * blockDim.x)
@@ -427,9 +431,16 @@ __global__ void light_power_kernel(SceneView s, float* __restrict__ power)
         const int t = s.emissive[e];
         V3 a, b, c;
         load_triangle(s, t, a, b, c);
-        const float area = 0.5f * length(cross(b - a, c - a));
+        const V3 ab = v3(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z));
+        const V3 ac = v3(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z));
+        const V3 n = v3(__fsub_rn(__fmul_rn(ab.y, ac.z), __fmul_rn(ab.z, ac.y)),
+                        __fsub_rn(__fmul_rn(ab.z, ac.x), __fmul_rn(ab.x, ac.z)),
+                        __fsub_rn(__fmul_rn(ab.x, ac.y), __fmul_rn(ab.y, ac.x)));
+        const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(n.x, n.x), __fmul_rn(n.y, n.y)), __fmul_rn(n.z, n.z)));
+        const float area = __fmul_rn(0.5f, len);
         const V3 Le = xyz(s.materials[s.material_of[t]].emission);
-        power[e] = luminance(Le) * area;
+        const float lum = __fadd_rn(__fadd_rn(__fmul_rn(0.3086f, Le.x), __fmul_rn(0.6094f, Le.y)), __fmul_rn(0.0820f, Le.z));
+        power[e] = __fmul_rn(lum, area);
     }
 }
 

@@ -374,6 +374,24 @@ void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const 
     for (auto& t : pool) t.join();
 }
 
+/* Emissive power list exactly as GPURenderer::compute_emissives_power_alias_table
+ * (src/Renderer/GPURenderer.cpp:256-275): luminance(emission) * area in float, operations rounded
+ * one by one (this file is compiled with -ffp-contract=off). tri_verts = 9 floats per triangle,
+ * emission = 3 floats per material (colour * strength * global factor). */
+void orc_emissive_power(const float* tri_verts, const int* mat_of, const float* emission, const int* emissive,
+                        int n_emissive, float* out_power)
+{
+    for (int i = 0; i < n_emissive; i++)
+    {
+        const float* t = tri_verts + 9 * (size_t)emissive[i];
+        V a = mk(t[0], t[1], t[2]), b = mk(t[3], t[4], t[5]), c = mk(t[6], t[7], t[8]);
+        V n = cross(b - a, c - a);
+        float area = 0.5f * len(n);
+        const float* e = emission + 3 * mat_of[emissive[i]];
+        out_power[i] = lum(mk(e[0], e[1], e[2])) * area;
+    }
+}
+
 /* Vose alias table exactly as src/Utils/Utils.cpp:63-131: elements normalised in double by
  * 'total_sum' (as given) and scaled by n; FIFO small/large queues in index order. */
 void orc_vose_alias(const float* input, int n, double total_sum, float* out_prob, int* out_alias)

@@ -171,6 +171,7 @@ def _pt_lib():
                                       ctypes.c_float, _c_i, ctypes.c_float, _c_f, _c_f,
                                       ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         lib.orc_vose_alias.argtypes = [_c_f, ctypes.c_int, ctypes.c_double, _c_f, _c_i]
+        lib.orc_emissive_power.argtypes = [_c_f, _c_i, _c_f, _c_i, ctypes.c_int, _c_f]
         lib._pt_sigs = True
     return lib
 
@@ -197,6 +198,19 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
                       len(ei), _ptr(ap, _c_f), _ptr(ai, _c_i), float(power_sum), _ptr(si, _c_i),
                       float(s.russian_roulette_throughput_clamp), _ptr(iv, _c_f), _ptr(ip, _c_f),
                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads)
+    return out
+
+
+def emissive_power(soup, material_of, emission, emissive) -> np.ndarray:
+    """Float power list of the emissive triangles, as the reference computes it
+    (src/Renderer/GPURenderer.cpp:256-275)."""
+    lib = _pt_lib()
+    soup = np.ascontiguousarray(soup, np.float32)
+    mo = np.ascontiguousarray(material_of, np.int32)
+    em = np.ascontiguousarray(emission, np.float32)
+    ei = np.ascontiguousarray(emissive, np.int32)
+    out = np.zeros(len(ei), np.float32)
+    lib.orc_emissive_power(_ptr(soup, _c_f), _ptr(mo, _c_i), _ptr(em, _c_f), _ptr(ei, _c_i), len(ei), _ptr(out, _c_f))
     return out
 
 

@@ -78,15 +78,17 @@ def test_light_table_matches_vose_restatement(cuda):
     mesh, mat_of, albedo, emission = _emitter_scene(n_emit=500, seed=5)
     scene = gbpt.Scene(mesh.positions, mesh.indices, mat_of, albedo, emission)
     lt = scene.light_table()
-    soup = mesh.triangle_soup().reshape(-1, 3, 3)[lt["emissive"]]
-    area = 0.5 * np.linalg.norm(np.cross(soup[:, 1] - soup[:, 0], soup[:, 2] - soup[:, 0]), axis=1)
-    e = emission[mat_of[lt["emissive"]]]
-    power = (0.3086 * e[:, 0] + 0.6094 * e[:, 1] + 0.0820 * e[:, 2]) * area
-    assert np.allclose(lt["power_sum64"], power.astype(np.float64).sum(), rtol=1e-5)
-    # same table as Utils::compute_alias_table restated, given the device's power list and FP64 sum
-    p32 = power.astype(np.float32)
+    # emissive list in triangle order, power list in the reference's float order (bit-exact)
+    want_emissive = np.nonzero(np.any(emission[mat_of] != 0, axis=1))[0]
+    assert np.array_equal(lt["emissive"], want_emissive)
+    p32 = pyoracle.emissive_power(mesh.triangle_soup(), mat_of, emission, lt["emissive"])
+    exact64 = p32.astype(np.float64).sum()
+    assert abs(lt["power_sum64"] - exact64) <= 1e-12 * exact64
+    assert lt["power_sum"] == np.float32(lt["power_sum64"])
+    # same table as Utils::compute_alias_table restated, given the same power list and FP64 sum
     prob, alias = pyoracle.vose_alias(p32, lt["power_sum64"])
-    assert np.array_equal(prob, lt["probas"]) or np.allclose(prob, lt["probas"], rtol=1e-6)
+    assert np.array_equal(prob, lt["probas"])
+    assert np.array_equal(alias, lt["alias"])
     dist = pyoracle.alias_distribution(lt["probas"], lt["alias"])
     assert np.allclose(dist, p32 / p32.astype(np.float64).sum(), rtol=1e-5, atol=1e-9)
 
