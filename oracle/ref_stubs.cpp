@@ -1,9 +1,17 @@
 /*
- * TEST INFRASTRUCTURE ONLY — link stubs for reference symbols that the intersection harness
- * references but never calls. Image8Bit::sample_rgba32f is only reached by alpha testing
- * (src/Device/includes/Texture.h:57 of the reference), which the harness switches off; the full
- * Image.cpp needs the absent ImGui, so it is not compiled here.
+ * TEST INFRASTRUCTURE ONLY — link stubs for reference symbols that the harnesses reference but
+ * never call.
+ *  - Image8Bit::sample_rgba32f is only reached by alpha testing (src/Device/includes/Texture.h:57
+ *    of the reference), which the intersection harness switches off.
+ *  - Image32Bit::sample_rgba32f is only reached by the energy-compensation and sheen lookup
+ *    tables, which the BSDF harness compiles out (energy compensation off) or never reaches
+ *    (sheen weight 0).
+ *  - Utils::debugbreak is only reached by the CPU NaN sanity check after a failed check.
+ * The full Image.cpp / Utils.cpp need the absent ImGui and OIDN, so they are not compiled here.
  */
 #include "Image/Image.h"
+#include "Utils/Utils.h"
 
 ColorRGBA32F Image8Bit::sample_rgba32f(float2) const { return ColorRGBA32F(1.0f); }
+ColorRGBA32F Image32Bit::sample_rgba32f(float2) const { return ColorRGBA32F(1.0f); }
+void Utils::debugbreak() {}

@@ -15,6 +15,22 @@
 #include <algorithm>
 #include <atomic>
 
+// Device compilers (HIP, CUDA) declare float overloads of the math functions in the global
+// namespace, so the reference's device code computes cos(float), sqrt(float), pow(float, float)
+// in float on the GPU. A plain host build would pick the C double versions instead; these
+// using-declarations make the host build compute in float like the reference's GPU path.
+using std::acos;
+using std::asin;
+using std::atan2;
+using std::cos;
+using std::exp;
+using std::fabs;
+using std::log;
+using std::pow;
+using std::sin;
+using std::sqrt;
+using std::tan;
+
 #ifndef HIPRT_HOST_DEVICE
 #define HIPRT_HOST_DEVICE
 #define HIPRT_DEVICE

@@ -1,5 +1,5 @@
-"""CPU: libgbpt builds, loads and exports every entry point declared in include/gbpt.h; argument
-checks answer without touching the GPU."""
+"""CPU: libgbpt builds, loads and exports every entry point declared in include/*.h; argument
+checks answer without touching the GPU; the material record layout matches the C struct."""
 import ctypes
 import os
 import re
@@ -27,8 +27,9 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 10
     for n in names:
         assert hasattr(lib, n), n
-    from gbpt import render
-    bound = {n for n, _, _ in _lib.SIGNATURES} | {n for n, _, _ in render.RENDER_SIGNATURES}
+    from gbpt import bsdf, render
+    bound = ({n for n, _, _ in _lib.SIGNATURES} | {n for n, _, _ in render.RENDER_SIGNATURES}
+             | {n for n, _, _ in bsdf.BSDF_SIGNATURES})
     assert bound == set(names)
 
 
@@ -49,3 +50,28 @@ def test_invalid_arguments_are_reported_not_fatal():
     assert lib.gbpt_bvh_build(None, None, 0, 5, None, ctypes.byref(h)) == 1
     with pytest.raises(gbpt.GbptError):
         _lib.check(1)
+
+
+def test_material_record_layout_matches_header():
+    """gbpt.materials word offsets agree with gbpt_principled_material in include/gbpt_bsdf.h."""
+    from gbpt import materials as M
+    text = open(os.path.join(INCLUDE, "gbpt_bsdf.h")).read()
+    body = text[text.index("typedef struct gbpt_principled_material {"):text.index("} gbpt_principled_material;")]
+    off = 0
+    seen = {}
+    for m in re.finditer(r"(float|int32_t)\s+(\w+)(?:\[(\d+)\])?;", body):
+        name, cnt = m.group(2), int(m.group(3) or 1)
+        seen[name] = (off, cnt)
+        off += cnt
+    assert off == M.WORDS
+    for name, (o, c) in M.OFFSETS.items():
+        assert seen[name] == (o, c), name
+
+
+def test_bsdf_entry_points_reject_bad_arguments():
+    from gbpt import bsdf
+    lib = bsdf._load()
+    assert lib.gbpt_bsdf_eval(None, 0, None, None, -1, None, None, None) == 1
+    assert lib.gbpt_bsdf_eval(None, 0, None, None, 0, None, None, None) == 0
+    assert lib.gbpt_bsdf_sample(None, 0, None, None, None, 5, None, None, None, None, None) == 1
+    assert b"device pointers" in lib.gbpt_last_error()
