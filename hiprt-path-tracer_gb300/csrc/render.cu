@@ -544,6 +544,17 @@ cudaError_t launch_light_table(const SceneView& s, float* power, double* partial
     return cudaGetLastError();
 }
 
+cudaError_t launch_alias_table(const float* power, int n, double* partial, int n_partial, double* sum64, double* q,
+                               float* prob, int32_t* alias, int32_t* smalls, int32_t* larges, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    sum_f64_kernel<<<n_partial, kSumThreads, 0, st>>>(power, n, partial);
+    sum_partials_kernel<<<1, kSumThreads, 0, st>>>(partial, n_partial, sum64);
+    normalize_f64_kernel<<<grid_for(n, 256, 4096), 256, 0, st>>>(power, n, sum64, q);
+    alias_vose_kernel<<<1, 1, 0, st>>>(q, n, prob, alias, smalls, larges);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Queue& q, int32_t iteration_base,
                           unsigned long long* stats, int n_sm, cudaStream_t st)
 {

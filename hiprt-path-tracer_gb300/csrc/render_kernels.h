@@ -28,6 +28,10 @@ struct RenderConst
 cudaError_t launch_light_table(const SceneView& s, float* power, double* partial, int n_partial, double* sum64,
                                double* q, float* prob, int32_t* alias, int32_t* smalls, int32_t* larges,
                                cudaStream_t st);
+// The FP64 sum, normalisation and Vose partition of launch_light_table over a power list that
+// the caller already holds on the device (power list -> prob/alias, sum into *sum64).
+cudaError_t launch_alias_table(const float* power, int n, double* partial, int n_partial, double* sum64, double* q,
+                               float* prob, int32_t* alias, int32_t* smalls, int32_t* larges, cudaStream_t st);
 cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Queue& q, int32_t iteration_base,
                           unsigned long long* stats, int n_sm, cudaStream_t st);
 cudaError_t launch_bounce(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,

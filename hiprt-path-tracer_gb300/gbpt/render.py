@@ -20,6 +20,7 @@ from ._lib import c_vp, i32, i64
 LIGHT_UNIFORM = 0
 LIGHT_POWER = 1
 BSDF_LAMBERTIAN = 1
+GBPT_ALIAS_NOALLOC_MAX_EMITTERS = 131072  # include/gbpt_render.h
 
 
 class Material(ctypes.Structure):
@@ -58,6 +59,7 @@ RENDER_SIGNATURES = [
     ("gbpt_pass_accumulate", ctypes.c_int, [c_vp, c_vp]),
     ("gbpt_renderer_get_image", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp]),
     ("gbpt_renderer_get_stats", ctypes.c_int, [c_vp, ctypes.POINTER(RenderStatsC), c_vp]),
+    ("gbpt_alias_table_build_noalloc", ctypes.c_int, [c_vp, i32, c_vp, c_vp, c_vp, c_vp]),
 ]
 
 

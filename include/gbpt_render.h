@@ -56,6 +56,26 @@ GBPT_API gbpt_status gbpt_scene_get_bvh(const gbpt_scene* scene, const gbpt_bvh*
 GBPT_API gbpt_status gbpt_scene_get_light_table(const gbpt_scene* scene, int32_t* n_emissive, int32_t* emissive,
                                                 float* probas, int32_t* alias, float* power_sum, double* power_sum64);
 
+/* Largest emitter count gbpt_alias_table_build_noalloc accepts. */
+#define GBPT_ALIAS_NOALLOC_MAX_EMITTERS 131072
+
+/* No counterpart in the reference: an extra entry point of this library for callers that cannot
+ * allocate device memory. An interactive render loop that rebuilds the light table after an
+ * emission edit cannot afford cudaMalloc/cudaFree (they can synchronise the whole device and stall
+ * the frame), and a host application that hands the library a fixed device-memory budget up front
+ * cannot let it allocate later. This call allocates nothing: it takes a device power list
+ * (luminance(emission) * area per emitter, n entries) and writes the same table as the light-table
+ * build of gbpt_scene_create — FP64 sum into *power_sum64, then probas[n] and alias[n] — all three
+ * device pointers owned by the caller.
+ * Limits: n <= GBPT_ALIAS_NOALLOC_MAX_EMITTERS, else GBPT_ERROR_INVALID_ARG. Its scratch is one
+ * fixed 2 MiB device array inside libgbpt that every device which loads the library holds until
+ * exit. The first call on a device looks up that array's device address (with the device current);
+ * make that first call before any stream capture. All calls share the one array: two calls that
+ * overlap on the GPU (different streams, or different host threads) race and must be serialised
+ * by the caller. Asynchronous on 'stream'. */
+GBPT_API gbpt_status gbpt_alias_table_build_noalloc(const float* power, int32_t n, float* probas, int32_t* alias,
+                                                    double* power_sum64, void* stream);
+
 enum {
     GBPT_LIGHT_UNIFORM = 0, /* LSS_BASE_UNIFORM */
     GBPT_LIGHT_POWER = 1    /* LSS_BASE_POWER */
