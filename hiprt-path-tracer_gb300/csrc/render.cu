@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "render_common.h"
+#include "principled.h"
 #include "render_kernels.h"
 #include "trace_core.h"
 
@@ -73,6 +74,7 @@ __global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers
         q.slot[slot] = (int32_t)slot;
         pb.throughput[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         pb.radiance[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (pb.medium) pb.medium[slot] = -1;
         store_rng(pb.rng + slot, rng);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -130,8 +132,71 @@ __device__ __forceinline__ void fix_backfacing(V3 view, V3& ng, V3& ns)
 }
 
 // ---------------------------------------------------------------------------------------------
-// shade: one path vertex per active path
+// light sample on an emissive triangle (sample_one_emissive_triangle_uniform / _power,
+// src/Device/includes/LightSampling/LightUtils.h:248-309; Heitz 2019 point, :150-199)
 // ---------------------------------------------------------------------------------------------
+struct LightSample
+{
+    V3 point, normal, emission;
+    float pdf_area;
+};
+
+__device__ __forceinline__ LightSample sample_light(const SceneView& s, const RenderConst& rc, Pcg32& rng)
+{
+    int e;
+    if (rc.light_sampling == GBPT_LIGHT_POWER)
+    {
+        e = rng.index(s.n_emissive);
+        if (rng.next() > __ldg(s.alias_prob + e)) e = __ldg(s.alias_index + e);
+    }
+    else
+        e = rng.index(s.n_emissive);
+    const int lt = __ldg(s.emissive + e);
+    float r1 = rng.next(), r2 = rng.next();
+    square_to_triangle(r1, r2);
+    V3 la, lb, lc;
+    load_triangle(s, lt, la, lb, lc);
+    const V3 ab = lb - la, ac = lc - la;
+    const V3 nrm = cross(ab, ac);
+    const float len = length(nrm);
+    LightSample ls;
+    ls.point = la + ab * r1 + ac * r2;
+    ls.normal = nrm / len;
+    const float area = 0.5f * len;
+    ls.emission = xyz(s.materials[__ldg(s.material_of + lt)].emission);
+    ls.pdf_area = 1.0f / area;
+    if (rc.light_sampling == GBPT_LIGHT_POWER)
+        ls.pdf_area *= (luminance(ls.emission) * area) / s.power_sum;
+    else
+        ls.pdf_area /= (float)s.n_emissive;
+    return ls;
+}
+
+// A BSDF sample draws its random numbers from a Xorshift32 generator (the reference's generator,
+// src/HostDeviceCommon/Xorshift.h) seeded by the path's PCG stream, so the same numbers can be
+// replayed through the reference's own BSDF.
+__device__ __forceinline__ bsdf::Xorshift32 bsdf_rng(Pcg32& rng)
+{
+    uint32_t seed = rng.next_u32();
+    return bsdf::Xorshift32{seed != 0u ? seed : 0x9E3779B9u};
+}
+
+// MaterialUtils::can_do_light_sampling (MaterialUtils.h:71-93): a material whose every lobe is a
+// delta distribution skips light sampling (and its random numbers).
+__device__ __forceinline__ bool can_light_sample(const bsdf::Material& m)
+{
+    const bool smooth_base = bsdf::is_smooth(m.roughness) && (m.metallic == 1.0f || m.transmission == 1.0f);
+    const bool smooth_coat = m.coat == 0.0f || bsdf::is_smooth(m.coat_roughness);
+    const bool smooth_second = bsdf::is_smooth(m.second_roughness) || m.second_weight == 0.0f;
+    return !(smooth_base && smooth_coat && smooth_second);
+}
+
+// ---------------------------------------------------------------------------------------------
+// shade: one path vertex per active path. PRINCIPLED selects the layered principled BSDF with
+// volume tracking (a path refracting into a non-thin transmissive material is inside it until it
+// refracts out), else the Lambertian BSDF override.
+// ---------------------------------------------------------------------------------------------
+template <bool PRINCIPLED>
 __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue next,
                                                     Queue shadow, Queue bsdfq, int bounce, unsigned long long* stats)
 {
@@ -159,6 +224,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
         V3 P = v3(0, 0, 0), tp = v3(0, 0, 0);
         V3 light_contrib = v3(0, 0, 0);
         float4 bsdf_pending = make_float4(0, 0, 0, 0);
+        int next_medium = -1;
         Pcg32 rng;
         rng.inc = pcg_inc(rc.seed);
         rng.state = 0;
@@ -170,118 +236,202 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
             P = o + hit.x * d;
             V3 a, b, c;
             load_triangle(s, prim, a, b, c);
-            V3 ng = normalize(cross(b - a, c - a));
+            const V3 ng_raw = normalize(cross(b - a, c - a));
+            V3 ng = ng_raw;
             V3 ns = ng;
             const V3 view = -d;
             fix_backfacing(view, ng, ns);
-            const DeviceMaterial m = s.materials[__ldg(s.material_of + prim)];
-            const V3 albedo = xyz(m.base_color);
+            const int mat = __ldg(s.material_of + prim);
             tp = xyz(pb.throughput[slot]);
             V3 L = v3(0, 0, 0);
-            if (bounce == 0) L = xyz(m.emission);
+            if (bounce == 0) L = xyz(s.materials[mat].emission);
 
-            // ---- next-event estimation: light sample (sample_one_light_MIS, Lights.h:123-185) ----
-            if (s.n_emissive > 0)
+            if constexpr (!PRINCIPLED)
             {
-                int e;
-                if (rc.light_sampling == GBPT_LIGHT_POWER)
+                const V3 albedo = xyz(s.materials[mat].base_color);
+                // ---- next-event estimation: light sample (sample_one_light_MIS, Lights.h:123-185) ----
+                if (s.n_emissive > 0)
                 {
-                    e = rng.index(s.n_emissive);
-                    if (rng.next() > __ldg(s.alias_prob + e)) e = __ldg(s.alias_index + e);
-                }
-                else
-                    e = rng.index(s.n_emissive);
-                const int lt = __ldg(s.emissive + e);
-                float r1 = rng.next(), r2 = rng.next();
-                square_to_triangle(r1, r2);
-                V3 la, lb, lc;
-                load_triangle(s, lt, la, lb, lc);
-                const V3 ab = lb - la, ac = lc - la;
-                const V3 nrm = cross(ab, ac);
-                const float len = length(nrm);
-                const V3 lp = la + ab * r1 + ac * r2;
-                const V3 ln = nrm / len;
-                const float area = 0.5f * len;
-                const V3 Le = xyz(s.materials[__ldg(s.material_of + lt)].emission);
-                float pdf_area = 1.0f / area;
-                if (rc.light_sampling == GBPT_LIGHT_POWER)
-                    pdf_area *= (luminance(Le) * area) / s.power_sum;
-                else
-                    pdf_area /= (float)s.n_emissive;
-                if (pdf_area > 0.0f)
-                {
-                    const V3 to_l = lp - P;
-                    const float dist = length(to_l);
-                    const V3 wi = to_l / dist;
-                    float bsdf_pdf;
-                    const V3 f = lambert_eval(albedo, dot(ns, wi), bsdf_pdf);
-                    if (bsdf_pdf > 0.0f)
+                    const LightSample ls = sample_light(s, rc, rng);
+                    if (ls.pdf_area > 0.0f)
                     {
-                        const float cos_l = fmaxf(0.0f, dot(ln, -wi));
-                        if (cos_l > 1.0e-5f)
+                        const V3 to_l = ls.point - P;
+                        const float dist = length(to_l);
+                        const V3 wi = to_l / dist;
+                        float bsdf_pdf;
+                        const V3 f = lambert_eval(albedo, dot(ns, wi), bsdf_pdf);
+                        if (bsdf_pdf > 0.0f)
                         {
-                            const float light_pdf = area_to_solid_angle_pdf(pdf_area, dist, cos_l);
-                            const float mis = balance_heuristic(light_pdf, bsdf_pdf);
-                            const float cosine = fabsf(dot(ns, wi));
-                            light_contrib = tp * (f * cosine * Le * mis / light_pdf);
-                            if (!is_black(light_contrib))
+                            const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
+                            if (cos_l > 1.0e-5f)
                             {
-                                want_shadow = true;
-                                sh_o = f4(P, 0.0f);
-                                sh_d = f4(wi, dist - 1.0e-4f);
+                                const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
+                                const float mis = balance_heuristic(light_pdf, bsdf_pdf);
+                                const float cosine = fabsf(dot(ns, wi));
+                                light_contrib = tp * (f * cosine * ls.emission * mis / light_pdf);
+                                if (!is_black(light_contrib))
+                                {
+                                    want_shadow = true;
+                                    sh_o = f4(P, 0.0f);
+                                    sh_d = f4(wi, dist - 1.0e-4f);
+                                }
                             }
                         }
                     }
                 }
-            }
 
-            // ---- next-event estimation: BSDF sample (Lights.h:187-226) ----
-            {
-                const float r1 = rng.next(), r2 = rng.next();
-                const V3 wi = cosine_sample(ns, r1, r2);
-                float pdf;
-                const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
-                if (pdf > 0.0f && s.n_emissive > 0)
+                // ---- next-event estimation: BSDF sample (Lights.h:187-226) ----
                 {
-                    const float cosine = fabsf(dot(ns, wi));
-                    const V3 w = tp * (f * cosine / pdf);
-                    want_bsdf = true;
-                    bs_d = f4(wi, 1.0e35f - 1.0e-4f);
-                    bsdf_pending = f4(w, pdf);
-                }
-            }
-
-            // ---- continuation (PathTracing.h:81-101, RussianRoulette.h:20-55) ----
-            if (bounce < rc.nb_bounces)
-            {
-                const float r1 = rng.next(), r2 = rng.next();
-                const V3 wi = cosine_sample(ns, r1, r2);
-                float pdf;
-                const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
-                if (pdf > 0.0f)
-                {
-                    const V3 atten = f * fabsf(dot(wi, ns)) / pdf;
-                    bool survive = true;
-                    V3 t2 = tp;
-                    if (rc.do_rr && bounce >= rc.rr_min_depth)
+                    const float r1 = rng.next(), r2 = rng.next();
+                    const V3 wi = cosine_sample(ns, r1, r2);
+                    float pdf;
+                    const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
+                    if (pdf > 0.0f && s.n_emissive > 0)
                     {
-                        const float p = fminf(max_comp(t2), 1.0f);
-                        if (rng.next() > p)
-                            survive = false;
-                        else
+                        const float cosine = fabsf(dot(ns, wi));
+                        const V3 w = tp * (f * cosine / pdf);
+                        want_bsdf = true;
+                        bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                        bsdf_pending = f4(w, pdf);
+                    }
+                }
+
+                // ---- continuation (PathTracing.h:81-101, RussianRoulette.h:20-55) ----
+                if (bounce < rc.nb_bounces)
+                {
+                    const float r1 = rng.next(), r2 = rng.next();
+                    const V3 wi = cosine_sample(ns, r1, r2);
+                    float pdf;
+                    const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
+                    if (pdf > 0.0f)
+                    {
+                        const V3 atten = f * fabsf(dot(wi, ns)) / pdf;
+                        bool survive = true;
+                        V3 t2 = tp;
+                        if (rc.do_rr && bounce >= rc.rr_min_depth)
                         {
-                            float scale = 1.0f / p;
-                            if (rc.rr_clamp > 0.0f) scale = fminf(scale, rc.rr_clamp);
-                            t2 = t2 * scale;
+                            const float p = fminf(max_comp(t2), 1.0f);
+                            if (rng.next() > p)
+                                survive = false;
+                            else
+                            {
+                                float scale = 1.0f / p;
+                                if (rc.rr_clamp > 0.0f) scale = fminf(scale, rc.rr_clamp);
+                                t2 = t2 * scale;
+                            }
+                        }
+                        if (survive)
+                        {
+                            t2 = t2 * atten;
+                            t2 = v3(fmaxf(t2.x, 1.0e-5f), fmaxf(t2.y, 1.0e-5f), fmaxf(t2.z, 1.0e-5f));
+                            tp = t2;
+                            want_next = true;
+                            nx_d = f4(wi, INFINITY);
                         }
                     }
-                    if (survive)
+                }
+            }
+            else
+            {
+                const bsdf::Material m = bsdf::load_material(s.pmats[mat]);
+                const bool hc = rc.ggx_height_correlated != 0;
+                // volume state: inside a transmissive (non thin-walled) object when its back face is
+                // hit; the incident medium is then the object, else the volume the path is in
+                const int cur_medium = pb.medium[slot];
+                const bool transmissive = (m.transmission > 0.0f || m.diffuse_transmission > 0.0f) && !m.thin_walled;
+                bsdf::Medium md;
+                md.inside = transmissive && dot(view, ng_raw) < 0.0f;
+                md.eta_incident = md.inside ? m.ior : (cur_medium >= 0 ? s.pmats[cur_medium].ior : 1.0f);
+                md.eta_outgoing = md.inside ? 1.0f : m.ior;
+                next_medium = cur_medium;
+
+                // ---- next-event estimation: light sample ----
+                if (s.n_emissive > 0 && can_light_sample(m))
+                {
+                    const LightSample ls = sample_light(s, rc, rng);
+                    if (ls.pdf_area > 0.0f)
                     {
-                        t2 = t2 * atten;
-                        t2 = v3(fmaxf(t2.x, 1.0e-5f), fmaxf(t2.y, 1.0e-5f), fmaxf(t2.z, 1.0e-5f));
-                        tp = t2;
-                        want_next = true;
-                        nx_d = f4(wi, INFINITY);
+                        const V3 to_l = ls.point - P;
+                        const float dist = length(to_l);
+                        const V3 wi = to_l / dist;
+                        bsdf::Query q;
+                        q.view = view;
+                        q.ns = ns;
+                        q.ng = ng;
+                        q.light = wi;
+                        float bsdf_pdf;
+                        const V3 f = bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
+                        if (bsdf_pdf > 0.0f)
+                        {
+                            const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
+                            if (cos_l > 1.0e-5f)
+                            {
+                                const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
+                                const float mis = balance_heuristic(light_pdf, bsdf_pdf);
+                                const float cosine = fabsf(dot(ns, wi));
+                                light_contrib = tp * (f * cosine * ls.emission * mis / light_pdf);
+                                if (!is_black(light_contrib))
+                                {
+                                    want_shadow = true;
+                                    sh_o = f4(P, 0.0f);
+                                    sh_d = f4(wi, dist - 1.0e-4f);
+                                }
+                            }
+                        }
+                    }
+                }
+
+                // ---- next-event estimation: BSDF sample ----
+                {
+                    bsdf::Xorshift32 xr = bsdf_rng(rng);
+                    V3 wi;
+                    int lobe;
+                    float pdf;
+                    const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                    if (pdf > 0.0f && s.n_emissive > 0)
+                    {
+                        const V3 w = tp * (f * fabsf(dot(ns, wi)) / pdf);
+                        want_bsdf = true;
+                        bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                        bsdf_pending = f4(w, pdf);
+                    }
+                }
+
+                // ---- continuation ----
+                if (bounce < rc.nb_bounces)
+                {
+                    bsdf::Xorshift32 xr = bsdf_rng(rng);
+                    V3 wi;
+                    int lobe;
+                    float pdf;
+                    const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                    if (pdf > 0.0f)
+                    {
+                        const V3 atten = f * fabsf(dot(wi, ns)) / pdf;
+                        bool survive = true;
+                        V3 t2 = tp;
+                        if (rc.do_rr && bounce >= rc.rr_min_depth)
+                        {
+                            const float p = fminf(max_comp(t2), 1.0f);
+                            if (rng.next() > p)
+                                survive = false;
+                            else
+                            {
+                                float scale = 1.0f / p;
+                                if (rc.rr_clamp > 0.0f) scale = fminf(scale, rc.rr_clamp);
+                                t2 = t2 * scale;
+                            }
+                        }
+                        if (survive)
+                        {
+                            t2 = t2 * atten;
+                            t2 = v3(fmaxf(t2.x, 1.0e-5f), fmaxf(t2.y, 1.0e-5f), fmaxf(t2.z, 1.0e-5f));
+                            tp = t2;
+                            want_next = true;
+                            nx_d = f4(wi, INFINITY);
+                            if (transmissive && (lobe == GBPT_LOBE_GLASS_REFRACT || lobe == GBPT_LOBE_DIFFUSE_TRANSMISSION))
+                                next_medium = md.inside ? -1 : mat;
+                        }
                     }
                 }
             }
@@ -321,6 +471,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
             next.last_prim[ni] = prim;
             next.slot[ni] = slot;
             pb.throughput[slot] = f4(tp, 0.0f);
+            if (PRINCIPLED) pb.medium[slot] = next_medium;
         }
         warp_count(stats + 1, want_shadow);
         warp_count(stats + 2, want_bsdf);
@@ -570,7 +721,10 @@ cudaError_t launch_bounce(const SceneView& s, const RenderConst& rc, const PathB
     const int tgrid = grid_for(capacity, 128, n_sm * 16);
     reset_counts_kernel<<<1, 1, 0, st>>>(next.count, shadow.count, bsdfq.count);
     trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, in);
-    shade_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats);
+    if (rc.bsdf == GBPT_BSDF_PRINCIPLED)
+        shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats);
+    else
+        shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats);
     trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, shadow);
     trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, bsdfq);
     resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq);

@@ -7,6 +7,7 @@
 // (src/Renderer/GPURendererThread.cpp:311-330).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -59,6 +60,7 @@ int sm_count()
 struct gbpt_scene
 {
     gbpt_bvh* bvh = nullptr;
+    bool principled = false;
     DevMem mem;
     gbpt::SceneView view;
     int32_t n_emissive = 0;
@@ -100,6 +102,34 @@ gbpt::Queue make_queue(DevMem& m, int64_t cap, bool closest_out, bool any_out)
 
 bool is_emissive(const gbpt_material& m) { return m.emission[0] > 0.0f || m.emission[1] > 0.0f || m.emission[2] > 0.0f; }
 
+float lerpf(float a, float b, float t) { return (1.0f - t) * a + t * b; }
+float pow4f(float x)
+{
+    const float x2 = x * x;
+    return x2 * x2;
+}
+
+// Coat roughening of the base and second metal roughness, as the reference's material fetch
+// applies it (src/Device/includes/Material.h:122-146; OpenPBR coat roughening), done once here.
+gbpt_principled_material effective_material(gbpt_principled_material m)
+{
+    const float coat = m.coat, roughening = m.coat_roughening;
+    if (coat > 0.0f && roughening > 0.0f)
+    {
+        const float cr4 = pow4f(m.coat_roughness);
+        const float base = m.roughness;
+        const float target = sqrtf(sqrtf(std::min(1.0f, pow4f(base) + 2.0f * cr4)));
+        m.roughness = lerpf(base, lerpf(base, target, coat), roughening);
+        if (m.second_roughness_weight > 0.0f)
+        {
+            const float second = m.second_roughness;
+            const float target2 = sqrtf(sqrtf(std::min(1.0f, pow4f(second) + 2.0f * cr4)));
+            m.second_roughness = lerpf(second, lerpf(second, target2, coat), roughening);
+        }
+    }
+    return m;
+}
+
 }  // namespace
 
 extern "C" {
@@ -114,13 +144,39 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
         return set_error(GBPT_ERROR_INVALID_ARG, "negative sizes");
     if (d->n_triangles > 0 && (!d->indices || !d->positions || !d->material_indices))
         return set_error(GBPT_ERROR_INVALID_ARG, "geometry buffers are NULL");
-    if (d->n_materials > 0 && !d->materials) return set_error(GBPT_ERROR_INVALID_ARG, "materials is NULL");
+    if (d->n_materials > 0 && !d->materials && !d->principled_materials)
+        return set_error(GBPT_ERROR_INVALID_ARG, "materials and principled_materials are both NULL");
+    // the emission/base colour view used by light sampling: the plain materials, else the
+    // principled ones
+    std::vector<gbpt_material> plain;
+    if (d->principled_materials)
+    {
+        for (int32_t m = 0; m < d->n_materials; m++)
+        {
+            const gbpt_principled_material& pm = d->principled_materials[m];
+            if (pm.sheen != 0.0f)
+                return set_error(GBPT_ERROR_UNSUPPORTED, "material " + std::to_string(m) + ": the sheen lobe is not built (sheen must be 0)");
+            if (!(pm.ior > 0.0f) || !(pm.coat_ior > 0.0f))
+                return set_error(GBPT_ERROR_INVALID_ARG, "material " + std::to_string(m) + " has a non-positive IOR");
+        }
+        if (!d->materials)
+        {
+            plain.resize(d->n_materials);
+            for (int32_t m = 0; m < d->n_materials; m++)
+                for (int k = 0; k < 3; k++)
+                {
+                    plain[m].base_color[k] = d->principled_materials[m].base_color[k];
+                    plain[m].emission[k] = d->principled_materials[m].emission[k];
+                }
+        }
+    }
+    const gbpt_material* materials = d->materials ? d->materials : plain.data();
     for (int64_t t = 0; t < d->n_triangles; t++)
         if (d->material_indices[t] < 0 || d->material_indices[t] >= d->n_materials)
             return set_error(GBPT_ERROR_INVALID_ARG, "triangle " + std::to_string(t) + " has an out-of-range material index");
     for (int32_t m = 0; m < d->n_materials; m++)
         for (int k = 0; k < 3; k++)
-            if (!std::isfinite(d->materials[m].emission[k]) || d->materials[m].emission[k] < 0.0f)
+            if (!std::isfinite(materials[m].emission[k]) || materials[m].emission[k] < 0.0f)
                 return set_error(GBPT_ERROR_INVALID_ARG, "material " + std::to_string(m) + " has an invalid emission");
 
     gbpt_scene* s = new (std::nothrow) gbpt_scene();
@@ -139,13 +195,13 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     std::vector<gbpt::DeviceMaterial> mats(d->n_materials);
     for (int32_t m = 0; m < d->n_materials; m++)
     {
-        const gbpt_material& src = d->materials[m];
+        const gbpt_material& src = materials[m];
         mats[m].base_color = make_float4(src.base_color[0], src.base_color[1], src.base_color[2], 0.0f);
         mats[m].emission = make_float4(src.emission[0], src.emission[1], src.emission[2], 0.0f);
     }
     std::vector<int32_t> emissive;
     for (int64_t t = 0; t < d->n_triangles; t++)
-        if (is_emissive(d->materials[d->material_indices[t]])) emissive.push_back((int32_t)t);
+        if (is_emissive(materials[d->material_indices[t]])) emissive.push_back((int32_t)t);
     const int32_t ne = (int32_t)emissive.size();
 
     DevMem& M = s->mem;
@@ -163,7 +219,16 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     double* dq = M.alloc<double>(ne);
     int32_t* dsmall = M.alloc<int32_t>(ne);
     int32_t* dlarge = M.alloc<int32_t>(ne);
+    gbpt_principled_material* dpm = nullptr;
+    std::vector<gbpt_principled_material> pmats;
+    if (d->principled_materials)
+    {
+        for (int32_t m = 0; m < d->n_materials; m++) pmats.push_back(effective_material(d->principled_materials[m]));
+        dpm = M.alloc<gbpt_principled_material>(pmats.size());
+    }
     cudaError_t e = M.err;
+    if (e == cudaSuccess && dpm)
+        e = cudaMemcpyAsync(dpm, pmats.data(), pmats.size() * sizeof(gbpt_principled_material), cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dv, verts.data(), verts.size() * sizeof(float4), cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(di, d->indices, 3 * d->n_triangles * sizeof(int32_t), cudaMemcpyHostToDevice, cs);
@@ -186,6 +251,8 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     v.n_emissive = ne;
     v.bvh_nodes = static_cast<const uint4*>(s->bvh->dev.nodes);
     v.bvh_tris = static_cast<const float4*>(s->bvh->dev.tris);
+    v.pmats = dpm;
+    s->principled = dpm != nullptr;
     s->n_emissive = ne;
     if (e == cudaSuccess) e = gbpt::launch_light_table(v, dpower, dpartial, n_partial, dsum, dq, dprob, dalias, dsmall, dlarge, cs);
     if (e == cudaSuccess && ne > 0) e = cudaMemcpyAsync(&s->power_sum64, dsum, sizeof(double), cudaMemcpyDeviceToHost, cs);
@@ -243,7 +310,10 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
     if (st->nb_bounces < 0 || st->nb_bounces > 64) return set_error(GBPT_ERROR_INVALID_ARG, "nb_bounces must be in 0..64");
     if (st->light_sampling != GBPT_LIGHT_UNIFORM && st->light_sampling != GBPT_LIGHT_POWER)
         return set_error(GBPT_ERROR_INVALID_ARG, "unknown light_sampling");
-    if (st->bsdf != GBPT_BSDF_LAMBERTIAN) return set_error(GBPT_ERROR_UNSUPPORTED, "only GBPT_BSDF_LAMBERTIAN is available");
+    if (st->bsdf != GBPT_BSDF_LAMBERTIAN && st->bsdf != GBPT_BSDF_PRINCIPLED)
+        return set_error(GBPT_ERROR_UNSUPPORTED, "bsdf must be GBPT_BSDF_LAMBERTIAN or GBPT_BSDF_PRINCIPLED");
+    if (st->bsdf == GBPT_BSDF_PRINCIPLED && !scene->principled)
+        return set_error(GBPT_ERROR_INVALID_ARG, "GBPT_BSDF_PRINCIPLED needs a scene created with principled_materials");
     const int64_t cap = (int64_t)st->width * st->height * st->samples_per_launch;
     if (cap > (int64_t)1 << 30) return set_error(GBPT_ERROR_INVALID_ARG, "width*height*samples_per_launch exceeds 2^30 paths");
 
@@ -265,6 +335,7 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
     rc.bsdf = st->bsdf;
     rc.seed = st->seed;
     rc.do_jittering = st->do_jittering;
+    rc.ggx_height_correlated = st->ggx_height_correlated;
     std::memcpy(rc.inverse_view, st->inverse_view, sizeof(rc.inverse_view));
     std::memcpy(rc.inverse_projection, st->inverse_projection, sizeof(rc.inverse_projection));
 
@@ -276,6 +347,7 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
     r->pb.pending_bsdf = M.alloc<float4>(cap);
     r->pb.shadow_entry = M.alloc<int32_t>(cap);
     r->pb.bsdf_entry = M.alloc<int32_t>(cap);
+    r->pb.medium = st->bsdf == GBPT_BSDF_PRINCIPLED ? M.alloc<int32_t>(cap) : nullptr;
     r->q[0] = make_queue(M, cap, true, false);
     r->q[1] = make_queue(M, cap, true, false);
     r->shadow = make_queue(M, cap, false, true);

@@ -12,13 +12,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/gbpt_bsdf.h"
 #include "../../include/gbpt_render.h"
+#include "hd_math.h"
 
 namespace gbpt {
 
-constexpr float kPi = 3.14159265358979323846f;
-constexpr float kInvPi = 0.31830988618379067154f;
-constexpr float kTwoPi = 6.28318530717958647693f;
+using namespace hd;
 
 // ---------------------------------------------------------------------------------------------
 // scene view and per-path buffers (all device pointers)
@@ -42,6 +42,7 @@ struct SceneView
     int32_t n_emissive;
     const uint4* bvh_nodes;
     const float4* bvh_tris;
+    const gbpt_principled_material* pmats;  // effective principled materials (NULL: Lambertian scene)
 };
 
 struct Queue
@@ -64,34 +65,13 @@ struct PathBuffers
     float4* pending_bsdf;   // rgb = throughput * f * cos / pdf, w = BSDF pdf
     int32_t* shadow_entry;  // queue index of the slot's shadow ray this bounce, -1 if none
     int32_t* bsdf_entry;    // queue index of the slot's BSDF-light ray this bounce, -1 if none
+    int32_t* medium;        // material index of the volume the path travels in, -1 = air
 };
 
 #ifdef __CUDACC__
 // ---------------------------------------------------------------------------------------------
-// small vector helpers
+// small vector helpers (the float3 type and operators shared with the BSDF live in hd_math.h)
 // ---------------------------------------------------------------------------------------------
-struct V3
-{
-    float x, y, z;
-};
-__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
-__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
-__device__ __forceinline__ V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ V3 operator*(float s, V3 a) { return v3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ V3 operator/(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
-__device__ __forceinline__ V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
-__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V3 cross(V3 a, V3 b)
-{
-    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ float length(V3 a) { return sqrtf(dot(a, a)); }
-__device__ __forceinline__ V3 normalize(V3 a) { return a / sqrtf(dot(a, a)); }
-__device__ __forceinline__ float max_comp(V3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
-__device__ __forceinline__ bool is_black(V3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
-__device__ __forceinline__ float luminance(V3 c) { return 0.3086f * c.x + 0.6094f * c.y + 0.0820f * c.z; }
 __device__ __forceinline__ V3 xyz(float4 f) { return v3(f.x, f.y, f.z); }
 __device__ __forceinline__ float4 f4(V3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
 
@@ -113,6 +93,7 @@ struct Pcg32
     }
     // uniform float in [0, 1)
     __device__ __forceinline__ float next() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+    __device__ __forceinline__ float operator()() { return next(); }
     __device__ __forceinline__ int index(int n)
     {
         int i = (int)(next() * (float)n);

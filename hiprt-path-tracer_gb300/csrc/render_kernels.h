@@ -21,6 +21,7 @@ struct RenderConst
     int32_t bsdf;
     uint32_t seed;
     int32_t do_jittering;
+    int32_t ggx_height_correlated;
     float inverse_view[16];
     float inverse_projection[16];
 };

@@ -20,6 +20,7 @@ from ._lib import c_vp, i32, i64
 LIGHT_UNIFORM = 0
 LIGHT_POWER = 1
 BSDF_LAMBERTIAN = 1
+BSDF_PRINCIPLED = 3
 GBPT_ALIAS_NOALLOC_MAX_EMITTERS = 131072  # include/gbpt_render.h
 
 
@@ -29,14 +30,15 @@ class Material(ctypes.Structure):
 
 class SceneDesc(ctypes.Structure):
     _fields_ = [("positions", c_vp), ("n_vertices", i64), ("indices", c_vp), ("n_triangles", i64),
-                ("material_indices", c_vp), ("materials", c_vp), ("n_materials", i32)]
+                ("material_indices", c_vp), ("materials", c_vp), ("n_materials", i32),
+                ("principled_materials", c_vp)]
 
 
 class RenderSettingsC(ctypes.Structure):
     _fields_ = [("width", i32), ("height", i32), ("samples_per_launch", i32), ("nb_bounces", i32),
                 ("do_russian_roulette", i32), ("russian_roulette_min_depth", i32),
                 ("russian_roulette_throughput_clamp", ctypes.c_float), ("light_sampling", i32), ("bsdf", i32),
-                ("seed", ctypes.c_uint32), ("do_jittering", i32), ("reserved", i32),
+                ("seed", ctypes.c_uint32), ("do_jittering", i32), ("ggx_height_correlated", i32),
                 ("inverse_view", ctypes.c_float * 16), ("inverse_projection", ctypes.c_float * 16)]
 
 
@@ -104,6 +106,7 @@ class RenderSettings:
     bsdf: int = BSDF_LAMBERTIAN
     seed: int = 1
     do_jittering: bool = True
+    ggx_height_correlated: bool = False
     inverse_view: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
     inverse_projection: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
 
@@ -114,6 +117,7 @@ class RenderSettings:
             setattr(c, k, int(getattr(self, k)))
         c.do_russian_roulette = 1 if self.do_russian_roulette else 0
         c.do_jittering = 1 if self.do_jittering else 0
+        c.ggx_height_correlated = 1 if self.ggx_height_correlated else 0
         c.russian_roulette_throughput_clamp = float(self.russian_roulette_throughput_clamp)
         c.inverse_view[:] = [float(v) for v in np.asarray(self.inverse_view, np.float32).reshape(16)]
         c.inverse_projection[:] = [float(v) for v in np.asarray(self.inverse_projection, np.float32).reshape(16)]
@@ -132,9 +136,18 @@ def _load():
 
 
 class Scene:
-    def __init__(self, positions, indices, material_of_triangle, albedo, emission, stream=None, sah_bins=32,
-                 max_leaf_size=3):
+    def __init__(self, positions, indices, material_of_triangle, albedo=None, emission=None, stream=None, sah_bins=32,
+                 max_leaf_size=3, principled=None):
+        """albedo/emission: (M, 3) plain materials; principled: (M, 64) gbpt.materials records (the
+        reference's CPUMaterial parameters; base colour and emission come from them when albedo is
+        None)."""
         lib = _load()
+        self._pm = None
+        if principled is not None:
+            self._pm = np.ascontiguousarray(principled, np.float32).reshape(-1, 64)
+            if albedo is None:
+                albedo = self._pm[:, 0:3]
+                emission = self._pm[:, 4:7]
         self._pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
         self._idx = np.ascontiguousarray(indices, np.int32).reshape(-1, 3)
         self._mat_of = np.ascontiguousarray(material_of_triangle, np.int32).reshape(-1)
@@ -145,7 +158,8 @@ class Scene:
             self._mats[k].base_color[:] = [float(v) for v in alb[k]]
             self._mats[k].emission[:] = [float(v) for v in emi[k]]
         desc = SceneDesc(self._pos.ctypes.data, self._pos.shape[0], self._idx.ctypes.data, self._idx.shape[0],
-                         self._mat_of.ctypes.data, ctypes.addressof(self._mats), len(alb))
+                         self._mat_of.ctypes.data, ctypes.addressof(self._mats), len(alb),
+                         self._pm.ctypes.data if self._pm is not None else None)
         params = _lib.BvhParams(sah_bins, max_leaf_size, 0)
         h = c_vp()
         _lib.check(lib.gbpt_scene_create(ctypes.byref(desc), ctypes.byref(params), ctypes.byref(h), _stream(stream)))

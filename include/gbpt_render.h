@@ -11,6 +11,7 @@
 #define GBPT_RENDER_H
 
 #include "gbpt.h"
+#include "gbpt_bsdf.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -27,7 +28,12 @@ typedef struct gbpt_material {
 } gbpt_material;
 
 /* Mirrors the reference's Scene (src/Scene/SceneParser.h:109-170): flat triangle soup with a
- * material index per triangle. Host pointers. */
+ * material index per triangle. Host pointers.
+ * principled_materials (optional, n_materials entries) are the reference's CPUMaterial parameters
+ * (src/HostDeviceCommon/Material/MaterialCPU.h) in the gbpt_principled_material record; the
+ * library applies the reference's coat roughening (src/Device/includes/Material.h:122-146) once
+ * at upload, and takes base colour and emission from them when 'materials' is NULL. Materials
+ * with sheen > 0 are rejected (GBPT_ERROR_UNSUPPORTED). */
 typedef struct gbpt_scene_desc {
     const float* positions;          /* 3 per vertex */
     int64_t n_vertices;
@@ -36,6 +42,7 @@ typedef struct gbpt_scene_desc {
     const int32_t* material_indices; /* 1 per triangle */
     const gbpt_material* materials;
     int32_t n_materials;
+    const gbpt_principled_material* principled_materials;
 } gbpt_scene_desc;
 
 /* Uploads the scene, builds its BVH (gbpt_bvh_build), the emissive-triangle list (triangles
@@ -81,7 +88,8 @@ enum {
     GBPT_LIGHT_POWER = 1    /* LSS_BASE_POWER */
 };
 enum {
-    GBPT_BSDF_LAMBERTIAN = 1 /* BSDFOverride = BSDF_LAMBERTIAN (src/Device/includes/Dispatcher.h:21-82) */
+    GBPT_BSDF_LAMBERTIAN = 1, /* BSDFOverride = BSDF_LAMBERTIAN (src/Device/includes/Dispatcher.h:21-82) */
+    GBPT_BSDF_PRINCIPLED = 3  /* BSDF_PRINCIPLED: the layered BSDF of gbpt_bsdf.h (needs principled materials) */
 };
 
 /* Subset of HIPRTRenderSettings + HIPRTCamera used by the render path. */
@@ -96,7 +104,7 @@ typedef struct gbpt_render_settings {
     int32_t bsdf;                    /* GBPT_BSDF_* */
     uint32_t seed;
     int32_t do_jittering;            /* HIPRTCamera::do_jittering */
-    int32_t reserved;
+    int32_t ggx_height_correlated;   /* BRDFsData::GGX_masking_shadowing: 0 = height-uncorrelated (default) */
     float inverse_view[16];          /* row-major, points multiplied on the right */
     float inverse_projection[16];
 } gbpt_render_settings;

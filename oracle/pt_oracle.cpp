@@ -21,6 +21,13 @@
  * continuation 2, Russian roulette 1), so GPU and oracle images agree sample by sample up to
  * floating-point contraction.
  *
+ * orc_pt_render_principled runs the same estimator on principled materials with the BSDF
+ * evaluated and sampled by callbacks — the reference's own principled BSDF
+ * (src/Device/includes/BSDFs/Principled.h, compiled by oracle/Makefile 'ref') — with the light
+ * sample skipped for all-delta materials (MaterialUtils::can_do_light_sampling,
+ * src/HostDeviceCommon/Material/MaterialUtils.h:71-93) and one PCG draw seeding the Xorshift32
+ * generator of each BSDF sample, as the GPU kernels draw them.
+ *
  * orc_vose_alias restates Utils::compute_alias_table (src/Utils/Utils.cpp:63-131).
  */
 #include <algorithm>
@@ -333,6 +340,197 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
     return L;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Principled scenes: the same estimator with the BSDF evaluated and sampled through callbacks
+// (the reference's own principled BSDF, oracle/ref_bsdf.cpp) on 64-word material records and
+// 16-float queries (view, shading normal, geometric normal, light, eta in, eta out, inside, lobe).
+// Each BSDF sample is seeded with one 32-bit PCG draw (Xorshift32 seed, 0 -> 0x9E3779B9), as the
+// GPU kernels do. Volume tracking: a path is inside a non-thin transmissive object after a glass
+// refraction or diffuse transmission into it; its back face is then hit from inside.
+// ---------------------------------------------------------------------------------------------
+typedef void (*bsdf_eval_fn)(const float* mat, const float* q, float* out4);
+typedef void (*bsdf_sample_fn)(const float* mat, const float* q, uint32_t seed, float* out8, int32_t* lobe);
+
+struct PScene
+{
+    const float* pmats;  // effective materials, 64 words each
+    bsdf_eval_fn eval;
+    bsdf_sample_fn sample;
+    const float* mat(int m) const { return pmats + 64 * (size_t)m; }
+};
+
+bool smooth(float r) { return r <= 1.0e-2f; }
+
+bool can_light_sample(const float* m)
+{
+    const float rough = m[3], metallic = m[7], transmission = m[38], coat = m[25], coat_rough = m[26];
+    const float second_w = m[17], second_r = m[18];
+    bool smooth_base = smooth(rough) && (metallic == 1.0f || transmission == 1.0f);
+    bool smooth_coat = coat == 0.0f || smooth(coat_rough);
+    bool smooth_second = smooth(second_r) || second_w == 0.0f;
+    return !(smooth_base && smooth_coat && smooth_second);
+}
+
+void make_query(float* q, V view, V ns, V ng, V l, float eta_i, float eta_o, bool inside, int lobe)
+{
+    q[0] = view.x; q[1] = view.y; q[2] = view.z;
+    q[3] = ns.x; q[4] = ns.y; q[5] = ns.z;
+    q[6] = ng.x; q[7] = ng.y; q[8] = ng.z;
+    q[9] = l.x; q[10] = l.y; q[11] = l.z;
+    q[12] = eta_i; q[13] = eta_o; q[14] = inside ? 1.0f : 0.0f; q[15] = (float)lobe;
+}
+
+uint32_t bsdf_seed(Pcg& rng)
+{
+    uint32_t s = rng.u32();
+    return s != 0u ? s : 0x9E3779B9u;
+}
+
+V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, int pixel, int iteration)
+{
+    const int x = pixel % st.width, y = pixel / st.width;
+    Pcg rng = pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
+    float px = x + 0.5f, py = y + 0.5f;
+    if (st.jitter)
+    {
+        px += rng.next() - 0.5f;
+        py += rng.next() - 0.5f;
+    }
+    float xn = px / st.width * 2.0f - 1.0f, yn = py / st.height * 2.0f - 1.0f;
+    V o = mat_point(st.iv, mk(0, 0, 0));
+    V pv = mat_point(st.ip, mk(xn, yn, -1.0f));
+    V pw = mat_point(st.iv, pv);
+    V d = nrm(pw - o);
+    int skip = -1;
+    int medium = -1;
+    V tp = mk(1, 1, 1), L = mk(0, 0, 0);
+    for (int bounce = 0; bounce <= st.nb_bounces; bounce++)
+    {
+        float t;
+        int prim = closest(s, o, d, skip, t);
+        if (prim < 0) break;
+        V P = o + d * t;
+        V ng_raw = nrm(cross(s.b(prim) - s.a(prim), s.c(prim) - s.a(prim)));
+        V ng = ng_raw, ns = ng_raw;
+        V view = neg(d);
+        if (dot(view, ng) < 0.0f) { ng = neg(ng); ns = neg(ns); }
+        if (dot(view, ns) < 0.0f) ns = neg(ns);
+        V refl = ns * (2.0f * dot(view, ns)) - view;
+        if (dot(refl, ng) <= 0.0f)
+        {
+            refl = refl - nrm(ng * (dot(refl, ng) - 0.01f));
+            ns = nrm(view + refl);
+        }
+        const int mi = s.mat_of[prim];
+        const float* m = ps.mat(mi);
+        if (bounce == 0) L = L + s.emi(prim);
+        int32_t thin;
+        std::memcpy(&thin, m + 44, 4);
+        const bool transmissive = (m[38] > 0.0f || m[39] > 0.0f) && thin == 0;
+        const bool inside = transmissive && dot(view, ng_raw) < 0.0f;
+        const float eta_i = inside ? m[37] : (medium >= 0 ? ps.mat(medium)[37] : 1.0f);
+        const float eta_o = inside ? 1.0f : m[37];
+        float q[16], out[8];
+        if (s.ne > 0 && can_light_sample(m))
+        {
+            int e;
+            if (st.light == 1)
+            {
+                e = rng.index(s.ne);
+                if (rng.next() > s.alias_prob[e]) e = s.alias_idx[e];
+            }
+            else
+                e = rng.index(s.ne);
+            int lt = s.emissive[e];
+            float r1 = rng.next(), r2 = rng.next();
+            if (r2 > r1) { r1 *= 0.5f; r2 -= r1; }
+            else { r2 *= 0.5f; r1 -= r2; }
+            V la = s.a(lt), ab = s.b(lt) - la, ac = s.c(lt) - la;
+            V n = cross(ab, ac);
+            float ln = len(n);
+            V lp = la + ab * r1 + ac * r2;
+            V lnrm = n / ln;
+            float area = 0.5f * ln;
+            V Le = s.emi(lt);
+            float pa = light_pdf_area(s, lt, area, Le, st.light);
+            if (pa > 0.0f)
+            {
+                V tl = lp - P;
+                float dist = len(tl);
+                V wi = tl / dist;
+                make_query(q, view, ns, ng, wi, eta_i, eta_o, inside, 0);
+                ps.eval(m, q, out);
+                const float bp = out[3];
+                if (bp > 0.0f)
+                {
+                    float cl = std::max(0.0f, dot(lnrm, neg(wi)));
+                    if (cl > 1.0e-5f)
+                    {
+                        float lpdf = a2s(pa, dist, cl);
+                        float mis = balance(lpdf, bp);
+                        V f = mk(out[0], out[1], out[2]);
+                        V c = tp * (f * std::fabs(dot(ns, wi)) * Le * mis / lpdf);
+                        if (!black(c) && !occluded(s, P, wi, prim, dist - 1.0e-4f)) L = L + c;
+                    }
+                }
+            }
+        }
+        {
+            make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
+            int32_t lobe;
+            ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+            const float pdf = out[6];
+            V wi = mk(out[0], out[1], out[2]);
+            if (pdf > 0.0f && s.ne > 0)
+            {
+                V f = mk(out[3], out[4], out[5]);
+                V w = tp * (f * std::fabs(dot(ns, wi)) / pdf);
+                float th;
+                int lp = closest(s, P, wi, prim, th);
+                if (lp >= 0 && th < 1.0e35f - 1.0e-4f)
+                {
+                    V Le = s.emi(lp);
+                    if (!black(Le))
+                    {
+                        V n = cross(s.b(lp) - s.a(lp), s.c(lp) - s.a(lp));
+                        float ln = len(n);
+                        float cl = std::max(0.0f, dot(n / ln, neg(wi)));
+                        if (cl > 0.0f)
+                        {
+                            float lpdf = a2s(light_pdf_area(s, lp, 0.5f * ln, Le, st.light), th, cl);
+                            L = L + w * Le * balance(pdf, lpdf);
+                        }
+                    }
+                }
+            }
+        }
+        if (bounce == st.nb_bounces) break;
+        make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
+        int32_t lobe;
+        ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+        const float pdf = out[6];
+        if (pdf <= 0.0f) break;
+        V wi = mk(out[0], out[1], out[2]);
+        V f = mk(out[3], out[4], out[5]);
+        V att = f * std::fabs(dot(wi, ns)) / pdf;
+        if (st.do_rr && bounce >= st.rr_min)
+        {
+            float p = std::min(std::max(tp.x, std::max(tp.y, tp.z)), 1.0f);
+            if (rng.next() > p) break;
+            float sc = 1.0f / p;
+            if (st.rr_clamp > 0.0f) sc = std::min(sc, st.rr_clamp);
+            tp = tp * sc;
+        }
+        tp = tp * att;
+        tp = mk(std::max(tp.x, 1.0e-5f), std::max(tp.y, 1.0e-5f), std::max(tp.z, 1.0e-5f));
+        if (transmissive && (lobe == 64 || lobe == 256)) medium = inside ? -1 : mi;
+        o = P;
+        d = wi;
+        skip = prim;
+    }
+    return L;
+}
+
 }  // namespace
 
 extern "C" {
@@ -390,6 +588,44 @@ void orc_emissive_power(const float* tri_verts, const int* mat_of, const float* 
         const float* e = emission + 3 * mat_of[emissive[i]];
         out_power[i] = lum(mk(e[0], e[1], e[2])) * area;
     }
+}
+
+/* Principled scenes: as orc_pt_render, with 'pmats' (64-word effective materials) shaded through
+ * the given BSDF callbacks (the reference's own BSDF from oracle/_ref/libref.so). */
+void orc_pt_render_principled(const float* tri_verts, int n_tris, const int* mat_of, const float* albedo,
+                              const float* emission, const float* pmats, void* eval_fn, void* sample_fn,
+                              const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx,
+                              float power_sum, const int* settings_i, float rr_clamp, const float* inv_view,
+                              const float* inv_proj, double* out_rgb, int nthreads)
+{
+    Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
+    PScene ps{pmats, (bsdf_eval_fn)eval_fn, (bsdf_sample_fn)sample_fn};
+    Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
+                settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj};
+    const int npix = st.width * st.height;
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int w = 0; w < nthreads; w++)
+        pool.emplace_back([&]() {
+            for (;;)
+            {
+                int p = next.fetch_add(1);
+                if (p >= npix) break;
+                double r = 0, g = 0, b = 0;
+                for (int k = 0; k < st.spp; k++)
+                {
+                    V c = trace_path_principled(s, ps, st, p, st.iteration_base + k);
+                    r += c.x;
+                    g += c.y;
+                    b += c.z;
+                }
+                out_rgb[3 * p] += r;
+                out_rgb[3 * p + 1] += g;
+                out_rgb[3 * p + 2] += b;
+            }
+        });
+    for (auto& t : pool) t.join();
 }
 
 /* Vose alias table exactly as src/Utils/Utils.cpp:63-131: elements normalised in double by

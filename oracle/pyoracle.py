@@ -201,6 +201,44 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
     return out
 
 
+def pt_render_principled(soup, material_of, pmats_effective, emission, emissive, alias_prob, alias_idx, power_sum,
+                         settings, spp, iteration_base=0, nthreads=0):
+    """Path-tracing oracle for principled scenes: the estimator of pt_render with the BSDF
+    evaluated and sampled by the REFERENCE's own principled BSDF (oracle/_ref/libref.so, built
+    only where the reference tree exists). pmats_effective: (M, 64) records after coat
+    roughening. Returns FP64 per-pixel sums (H, W, 3)."""
+    lib = _pt_lib()
+    if not getattr(lib, "_ptp_sig", False):
+        lib.orc_pt_render_principled.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, _c_f, _c_f, ctypes.c_void_p,
+                                                 ctypes.c_void_p, _c_i, ctypes.c_int, _c_f, _c_i, ctypes.c_float, _c_i,
+                                                 ctypes.c_float, _c_f, _c_f, ctypes.POINTER(ctypes.c_double),
+                                                 ctypes.c_int]
+        lib._ptp_sig = True
+    ref = ctypes.CDLL(REF_SO)
+    eval_fn = ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value
+    sample_fn = ctypes.cast(ref.ref_principled_sample_one, ctypes.c_void_p).value
+    soup = np.ascontiguousarray(soup, np.float32)
+    mo = np.ascontiguousarray(material_of, np.int32)
+    pm = np.ascontiguousarray(pmats_effective, np.float32)
+    al = np.ascontiguousarray(pm[:, 0:3], np.float32)
+    em = np.ascontiguousarray(emission, np.float32)
+    ei = np.ascontiguousarray(emissive, np.int32)
+    ap = np.ascontiguousarray(alias_prob if alias_prob is not None else np.ones(len(ei)), np.float32)
+    ai = np.ascontiguousarray(alias_idx if alias_idx is not None else np.arange(len(ei)), np.int32)
+    s = settings
+    si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0, s.russian_roulette_min_depth,
+                   s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base], np.int32)
+    iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
+    ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
+    out = np.zeros((s.height, s.width, 3), np.float64)
+    lib.orc_pt_render_principled(_ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(al, _c_f), _ptr(em, _c_f),
+                                 _ptr(pm, _c_f), eval_fn, sample_fn, _ptr(ei, _c_i), len(ei), _ptr(ap, _c_f),
+                                 _ptr(ai, _c_i), float(power_sum), _ptr(si, _c_i),
+                                 float(s.russian_roulette_throughput_clamp), _ptr(iv, _c_f), _ptr(ip, _c_f),
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads)
+    return out
+
+
 def emissive_power(soup, material_of, emission, emissive) -> np.ndarray:
     """Float power list of the emissive triangles, as the reference computes it
     (src/Renderer/GPURenderer.cpp:256-275)."""

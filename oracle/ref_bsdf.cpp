@@ -103,6 +103,42 @@ struct Ctx
 
 float3 f3(const float* p) { return make_float3(p[0], p[1], p[2]); }
 
+void eval_query(const float* mat, const float* q, float* out)
+{
+    DeviceUnpackedEffectiveMaterial m = unpack(mat);
+    Ctx c(q, m);
+    BSDFIncidentLightInfo info = (BSDFIncidentLightInfo)(int)q[15];
+    BSDFContext ctx(f3(q), f3(q + 3), f3(q + 6), f3(q + 9), info, c.vs, false, m, 0, 0.0f);
+    float pdf = 0.0f;
+    ColorRGB32F col = principled_bsdf_eval(c.rd, ctx, pdf);
+    out[0] = col.r;
+    out[1] = col.g;
+    out[2] = col.b;
+    out[3] = pdf;
+}
+
+void sample_query(const float* mat, const float* q, uint32_t seed, float* o, int32_t* lobe, uint32_t* rng_after)
+{
+    DeviceUnpackedEffectiveMaterial m = unpack(mat);
+    Ctx c(q, m);
+    BSDFIncidentLightInfo info = BSDFIncidentLightInfo::NO_INFO;
+    BSDFContext ctx(f3(q), f3(q + 3), f3(q + 6), make_float3(0.0f, 0.0f, 0.0f), info, c.vs, false, m, 0, 0.0f);
+    Xorshift32Generator rng(seed);
+    float3 dir = make_float3(0.0f, 0.0f, 0.0f);
+    float pdf = 0.0f;
+    ColorRGB32F col = principled_bsdf_sample(c.rd, ctx, dir, pdf, rng);
+    o[0] = dir.x;
+    o[1] = dir.y;
+    o[2] = dir.z;
+    o[3] = col.r;
+    o[4] = col.g;
+    o[5] = col.b;
+    o[6] = pdf;
+    o[7] = 0.0f;
+    *lobe = (int32_t)info;
+    *rng_after = rng.m_state.seed;
+}
+
 }  // namespace
 
 extern "C" {
@@ -111,20 +147,7 @@ extern "C" {
 void ref_principled_eval(const float* mats, const int32_t* mat_index, const float* queries, int64_t n, float* out)
 {
 #pragma omp parallel for schedule(dynamic, 256)
-    for (int64_t i = 0; i < n; i++)
-    {
-        const float* q = queries + 16 * i;
-        DeviceUnpackedEffectiveMaterial m = unpack(mats + 64 * (int64_t)mat_index[i]);
-        Ctx c(q, m);
-        BSDFIncidentLightInfo info = (BSDFIncidentLightInfo)(int)q[15];
-        BSDFContext ctx(f3(q), f3(q + 3), f3(q + 6), f3(q + 9), info, c.vs, false, m, 0, 0.0f);
-        float pdf = 0.0f;
-        ColorRGB32F col = principled_bsdf_eval(c.rd, ctx, pdf);
-        out[4 * i] = col.r;
-        out[4 * i + 1] = col.g;
-        out[4 * i + 2] = col.b;
-        out[4 * i + 3] = pdf;
-    }
+    for (int64_t i = 0; i < n; i++) eval_query(mats + 64 * (int64_t)mat_index[i], queries + 16 * i, out + 4 * i);
 }
 
 void ref_principled_pdf(const float* mats, const int32_t* mat_index, const float* queries, int64_t n, float* out)
@@ -149,28 +172,17 @@ void ref_principled_sample(const float* mats, const int32_t* mat_index, const fl
 {
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++)
-    {
-        const float* q = queries + 16 * i;
-        DeviceUnpackedEffectiveMaterial m = unpack(mats + 64 * (int64_t)mat_index[i]);
-        Ctx c(q, m);
-        BSDFIncidentLightInfo info = BSDFIncidentLightInfo::NO_INFO;
-        BSDFContext ctx(f3(q), f3(q + 3), f3(q + 6), make_float3(0.0f, 0.0f, 0.0f), info, c.vs, false, m, 0, 0.0f);
-        Xorshift32Generator rng(seeds[i]);
-        float3 dir = make_float3(0.0f, 0.0f, 0.0f);
-        float pdf = 0.0f;
-        ColorRGB32F col = principled_bsdf_sample(c.rd, ctx, dir, pdf, rng);
-        float* o = out + 8 * i;
-        o[0] = dir.x;
-        o[1] = dir.y;
-        o[2] = dir.z;
-        o[3] = col.r;
-        o[4] = col.g;
-        o[5] = col.b;
-        o[6] = pdf;
-        o[7] = 0.0f;
-        info_out[i] = (int32_t)info;
-        rng_out[i] = rng.m_state.seed;
-    }
+        sample_query(mats + 64 * (int64_t)mat_index[i], queries + 16 * i, seeds[i], out + 8 * i, info_out + i, rng_out + i);
+}
+
+/* Single-query forms with the same layouts, handed to the path-tracing oracle (pt_oracle.cpp) as
+ * function pointers so that it shades with the reference's own BSDF. */
+void ref_principled_eval_one(const float* mat, const float* q, float* out) { eval_query(mat, q, out); }
+
+void ref_principled_sample_one(const float* mat, const float* q, uint32_t seed, float* out, int32_t* lobe)
+{
+    uint32_t rng_after;
+    sample_query(mat, q, seed, out, lobe, &rng_after);
 }
 
 }  // extern "C"

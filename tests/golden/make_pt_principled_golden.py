@@ -1,0 +1,72 @@
+"""Generates tests/golden/pt_principled_cornell.npz: a Cornell box with principled materials
+rendered by the path-tracing oracle (oracle/pt_oracle.cpp) shading with the REFERENCE's own
+principled BSDF (oracle/_ref/libref.so; energy compensation and regularization compiled out).
+
+The GPU path tracer draws the same random numbers (PCG per path, one PCG draw seeding the
+Xorshift32 generator of each BSDF sample), so its image agrees with this one sample by sample up
+to floating-point contraction. Materials: coated diffuse walls, a rough dielectric red wall, an
+anisotropic metal green wall, a rough glass short box (closed: paths enter and leave it), a mirror
+tall box (a delta BSDF: no light sampling), the area light. The scene and settings are stored with
+the image so the GPU test needs nothing else.
+Usage (where the reference tree is present):  python tests/golden/make_pt_principled_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "hiprt-path-tracer_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+from gbpt import materials as M, scenes  # noqa: E402
+from gbpt.render import LIGHT_UNIFORM, BSDF_PRINCIPLED, RenderSettings, look_at_camera  # noqa: E402
+import pyoracle  # noqa: E402
+
+OUT = os.path.join(HERE, "pt_principled_cornell.npz")
+
+MATERIALS = [
+    dict(base_color=(0.73, 0.73, 0.73), roughness=0.5, coat=0.5, coat_roughness=0.1),          # 0 white walls
+    dict(base_color=(0.63, 0.065, 0.05), roughness=0.4),                                        # 1 red wall
+    dict(base_color=(0.14, 0.45, 0.09), roughness=0.35, metallic=1.0, anisotropy=0.6),           # 2 green wall
+    dict(base_color=(0.0, 0.0, 0.0), emission=(17.0, 12.0, 4.0)),                               # 3 light
+    dict(base_color=(0.95, 0.95, 0.95), roughness=0.15, specular_transmission=1.0, ior=1.5),    # 4 short box
+    dict(base_color=(0.9, 0.9, 0.9), roughness=0.0, metallic=1.0),                              # 5 tall box
+]
+
+
+def scene():
+    cb = scenes.cornell_box()
+    mat_of = cb.material_of_triangle.copy()
+    mat_of[10:22] = 4
+    mat_of[22:34] = 5
+    raw = M.pack_many(MATERIALS)
+    eff = M.pack_many([M.coat_roughened(m) for m in MATERIALS])
+    return cb.mesh, mat_of, raw, eff
+
+
+def settings(width=32, height=32, spp=8):
+    iv, ip = look_at_camera((2.75, 2.75, -8.0), (2.75, 2.75, 0.0), vfov_deg=40.0, aspect=width / height)
+    return RenderSettings(width=width, height=height, samples_per_launch=spp, nb_bounces=4,
+                          russian_roulette_min_depth=3, light_sampling=LIGHT_UNIFORM, bsdf=BSDF_PRINCIPLED, seed=3,
+                          inverse_view=iv, inverse_projection=ip)
+
+
+def main():
+    pyoracle.build(ref=True)
+    mesh, mat_of, raw, eff = scene()
+    st = settings()
+    emission = raw[:, 4:7]
+    emissive = np.nonzero(np.any(emission[mat_of] != 0, axis=1))[0].astype(np.int32)
+    img = pyoracle.pt_render_principled(mesh.triangle_soup(), mat_of, eff, emission, emissive, None, None, 0.0, st,
+                                        st.samples_per_launch)
+    np.savez_compressed(OUT, positions=mesh.positions, indices=mesh.indices, material_of=mat_of, materials=raw,
+                        effective_materials=eff, inverse_view=st.inverse_view, inverse_projection=st.inverse_projection,
+                        settings=np.array([st.width, st.height, st.samples_per_launch, st.nb_bounces,
+                                           st.russian_roulette_min_depth, st.seed], np.int32), image=img)
+    print(f"wrote {OUT}: mean {img.mean() / st.samples_per_launch:.4f}, nonzero {np.mean(img.sum(-1) > 0):.3f}")
+
+
+if __name__ == "__main__":
+    main()

@@ -23,11 +23,11 @@ def test_eval_and_pdf_match_reference_golden(cuda):
     q = _dev(G.queries(g["eval_q"]))
     mi = _dev(g["eval_mat"].astype(np.int32))
     out = bsdf.eval(mats, mi, q).cpu().numpy()
-    flips = G.check_eval(out, g, max_flips=8)
+    frac, flips = G.check_eval(out, g, max_flips=8)
     pdf = bsdf.pdf(mats, mi, q).cpu().numpy()
     assert np.array_equal(pdf, out[:, 3])
     assert G.close(pdf[:, None], g["pdf_out"][:, None], rtol=1e-4).mean() > 0.998
-    print(f"eval: {flips} threshold flips of {len(out)}")
+    print(f"eval: {frac:.4%} within 1e-5, {flips} beyond 2e-4 of {len(out)}")
 
 
 def test_sampling_matches_reference_golden(cuda):
@@ -37,12 +37,17 @@ def test_sampling_matches_reference_golden(cuda):
     mi = _dev(g["sample_mat"].astype(np.int32))
     seeds = _dev(g["seeds"].view(np.int32))
     out, lobe, rng = bsdf.sample(mats, mi, q, seeds)
-    flips = G.check_sample(out.cpu().numpy(), lobe.cpu().numpy(), bsdf.as_uint32(rng), g, max_flips=16)
-    print(f"sample: {flips} threshold flips of {len(out)}")
+    frac, flips = G.check_sample(out.cpu().numpy(), lobe.cpu().numpy(), bsdf.as_uint32(rng), g, max_flips=16)
+    print(f"sample: {frac:.4%} within 1e-5, {flips} beyond 2e-4 of {len(out)}")
 
 
 def _albedo_by_quadrature(mats, m_idx, view, normal, eta_out, n_theta=512, n_phi=1024):
-    """Integral of f |cos| over the sphere, midpoint rule in (cos theta, phi) around the normal."""
+    """Integral of f |cos| over the sphere, midpoint rule in (cos theta, phi) around the normal.
+
+    Directions below the surface are evaluated as coming from the diffuse-transmission lobe (the
+    only transmission lobe sampled there for the rough materials below): the reference applies the
+    specular layer's fresnel attenuation to a refracted direction only when it was sampled from
+    that lobe (Principled.h:1305-1318), so a transmitted direction's value depends on that tag."""
     ct = (np.arange(n_theta) + 0.5) / n_theta * 2.0 - 1.0
     ph = (np.arange(n_phi) + 0.5) / n_phi * 2.0 * np.pi
     c, p = np.meshgrid(ct, ph, indexing="ij")
@@ -63,6 +68,8 @@ def _albedo_by_quadrature(mats, m_idx, view, normal, eta_out, n_theta=512, n_phi
     q[:, 9:12] = dirs
     q[:, 12] = 1.0
     q[:, 13] = eta_out
+    below = c.reshape(-1) < 0
+    q[below, 15] = bsdf.LOBES["diffuse_transmission"]
     rows = G.queries(q)
     f = bsdf.eval(mats, _dev(np.full(k, m_idx, np.int32)), _dev(rows)).cpu().numpy().astype(np.float64)
     cosv = np.abs(c.reshape(-1))
