@@ -11,35 +11,13 @@
 
 #include "render_common.h"
 #include "principled.h"
+#include "render_device.h"
 #include "render_kernels.h"
+#include "restir.h"
 #include "trace_core.h"
 
 namespace gbpt {
 namespace {
-
-// Appends one entry per calling thread with 'want' set; returns the slot index (or -1).
-// Warp-aggregated: one atomicAdd per warp (ballot + popc prefix).
-__device__ __forceinline__ int warp_append(int32_t* counter, bool want)
-{
-    const unsigned active = __activemask();
-    const unsigned mask = __ballot_sync(active, want);
-    if (!want) return -1;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(mask) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(counter, __popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
-}
-
-__device__ __forceinline__ void warp_count(unsigned long long* counter, bool c)
-{
-    const unsigned active = __activemask();
-    const unsigned mask = __ballot_sync(active, c);
-    if ((threadIdx.x & 31) == __ffs(active) - 1 && mask) atomicAdd(counter, (unsigned long long)__popc(mask));
-}
-
-__device__ __forceinline__ void store_rng(uint64_t* p, const Pcg32& r) { *p = r.state; }
 
 // ---------------------------------------------------------------------------------------------
 // camera rays (CameraRays, src/Device/kernels/CameraRays.h:155-176; HIPRTCamera::get_camera_ray,
@@ -104,101 +82,14 @@ __global__ void __launch_bounds__(128) trace_queue_kernel(const uint4* __restric
 }
 
 // ---------------------------------------------------------------------------------------------
-// Lambertian BSDF (src/Device/includes/BSDFs/Lambertian.h:14-58)
-// ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ V3 lambert_eval(V3 albedo, float NoL, float& pdf)
-{
-    pdf = 0.0f;
-    if (NoL <= 0.0f) return v3(0.0f, 0.0f, 0.0f);
-    pdf = NoL * kInvPi;
-    return albedo * kInvPi;
-}
-
-// fix_backfacing_normals (src/Device/includes/Intersect.h:142-176)
-__device__ __forceinline__ void fix_backfacing(V3 view, V3& ng, V3& ns)
-{
-    if (dot(view, ng) < 0.0f)
-    {
-        ng = -ng;
-        ns = -ns;
-    }
-    if (dot(view, ns) < 0.0f) ns = -ns;
-    V3 refl = 2.0f * dot(view, ns) * ns - view;
-    if (dot(refl, ng) <= 0.0f)
-    {
-        refl = refl - normalize((dot(refl, ng) - 0.01f) * ng);
-        ns = normalize(view + refl);
-    }
-}
-
-// ---------------------------------------------------------------------------------------------
-// light sample on an emissive triangle (sample_one_emissive_triangle_uniform / _power,
-// src/Device/includes/LightSampling/LightUtils.h:248-309; Heitz 2019 point, :150-199)
-// ---------------------------------------------------------------------------------------------
-struct LightSample
-{
-    V3 point, normal, emission;
-    float pdf_area;
-};
-
-__device__ __forceinline__ LightSample sample_light(const SceneView& s, const RenderConst& rc, Pcg32& rng)
-{
-    int e;
-    if (rc.light_sampling == GBPT_LIGHT_POWER)
-    {
-        e = rng.index(s.n_emissive);
-        if (rng.next() > __ldg(s.alias_prob + e)) e = __ldg(s.alias_index + e);
-    }
-    else
-        e = rng.index(s.n_emissive);
-    const int lt = __ldg(s.emissive + e);
-    float r1 = rng.next(), r2 = rng.next();
-    square_to_triangle(r1, r2);
-    V3 la, lb, lc;
-    load_triangle(s, lt, la, lb, lc);
-    const V3 ab = lb - la, ac = lc - la;
-    const V3 nrm = cross(ab, ac);
-    const float len = length(nrm);
-    LightSample ls;
-    ls.point = la + ab * r1 + ac * r2;
-    ls.normal = nrm / len;
-    const float area = 0.5f * len;
-    ls.emission = xyz(s.materials[__ldg(s.material_of + lt)].emission);
-    ls.pdf_area = 1.0f / area;
-    if (rc.light_sampling == GBPT_LIGHT_POWER)
-        ls.pdf_area *= (luminance(ls.emission) * area) / s.power_sum;
-    else
-        ls.pdf_area /= (float)s.n_emissive;
-    return ls;
-}
-
-// A BSDF sample draws its random numbers from a Xorshift32 generator (the reference's generator,
-// src/HostDeviceCommon/Xorshift.h) seeded by the path's PCG stream, so the same numbers can be
-// replayed through the reference's own BSDF.
-__device__ __forceinline__ bsdf::Xorshift32 bsdf_rng(Pcg32& rng)
-{
-    uint32_t seed = rng.next_u32();
-    return bsdf::Xorshift32{seed != 0u ? seed : 0x9E3779B9u};
-}
-
-// MaterialUtils::can_do_light_sampling (MaterialUtils.h:71-93): a material whose every lobe is a
-// delta distribution skips light sampling (and its random numbers).
-__device__ __forceinline__ bool can_light_sample(const bsdf::Material& m)
-{
-    const bool smooth_base = bsdf::is_smooth(m.roughness) && (m.metallic == 1.0f || m.transmission == 1.0f);
-    const bool smooth_coat = m.coat == 0.0f || bsdf::is_smooth(m.coat_roughness);
-    const bool smooth_second = bsdf::is_smooth(m.second_roughness) || m.second_weight == 0.0f;
-    return !(smooth_base && smooth_coat && smooth_second);
-}
-
-// ---------------------------------------------------------------------------------------------
 // shade: one path vertex per active path. PRINCIPLED selects the layered principled BSDF with
 // volume tracking (a path refracting into a non-thin transmissive material is inside it until it
 // refracts out), else the Lambertian BSDF override.
 // ---------------------------------------------------------------------------------------------
 template <bool PRINCIPLED>
 __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue next,
-                                                    Queue shadow, Queue bsdfq, int bounce, unsigned long long* stats)
+                                                    Queue shadow, Queue bsdfq, int bounce, unsigned long long* stats,
+                                                    ReservoirBuf restir)
 {
     const int n = *in.count;
     // iterate in whole warps so that the warp-aggregated appends see converged lanes
@@ -345,55 +236,97 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 md.eta_outgoing = md.inside ? 1.0f : m.ior;
                 next_medium = cur_medium;
 
-                // ---- next-event estimation: light sample ----
-                if (s.n_emissive > 0 && can_light_sample(m))
+                if (bounce == 0 && restir.s)
                 {
-                    const LightSample ls = sample_light(s, rc, rng);
-                    if (ls.pdf_area > 0.0f)
+                    // ---- direct lighting from the ReSTIR DI reservoir of the pixel
+                    // (evaluate_ReSTIR_DI_reservoir, src/Device/includes/ReSTIR/DI/FinalShading.h:13-85) ----
+                    const Reservoir R = load_reservoir(restir, slot);
+                    if (R.ucw > 0.0f)
                     {
-                        const V3 to_l = ls.point - P;
-                        const float dist = length(to_l);
-                        const V3 wi = to_l / dist;
+                        V3 wi = R.point - P;
+                        const float dist = length(wi);
+                        wi = wi / dist;
                         bsdf::Query q;
                         q.view = view;
                         q.ns = ns;
                         q.ng = ng;
                         q.light = wi;
                         float bsdf_pdf;
-                        const V3 f = bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
-                        if (bsdf_pdf > 0.0f)
+                        const V3 f = bsdf::eval(m, md, hc, q, R.flags & kRestirLobeMask, bsdf_pdf);
+                        float cosine = dot(ns, wi);
+                        if (R.flags & GBPT_LOBE_GLASS_REFRACT) cosine = fabsf(cosine);
+                        if (cosine > 0.0f)
                         {
-                            const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
-                            if (cos_l > 1.0e-5f)
+                            V3 la, lb, lc;
+                            load_triangle(s, R.tri, la, lb, lc);
+                            const V3 nl = normalize(cross(lb - la, lc - la));
+                            const float conv = fmaxf(0.0f, dot(nl, -wi)) / (dist * dist);
+                            const V3 Le = xyz(s.materials[__ldg(s.material_of + R.tri)].emission);
+                            const V3 c = tp * (f * R.ucw * Le * cosine * conv);
+                            if ((R.flags & kRestirFlagUnoccluded) || !rc.restir_final_visibility)
+                                L = L + c;
+                            else if (!is_black(c))
                             {
-                                const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
-                                const float mis = balance_heuristic(light_pdf, bsdf_pdf);
-                                const float cosine = fabsf(dot(ns, wi));
-                                light_contrib = tp * (f * cosine * ls.emission * mis / light_pdf);
-                                if (!is_black(light_contrib))
-                                {
-                                    want_shadow = true;
-                                    sh_o = f4(P, 0.0f);
-                                    sh_d = f4(wi, dist - 1.0e-4f);
-                                }
+                                light_contrib = c;
+                                want_shadow = true;
+                                sh_o = f4(P, 0.0f);
+                                sh_d = f4(wi, dist - 1.0e-4f);
                             }
                         }
                     }
                 }
-
-                // ---- next-event estimation: BSDF sample ----
+                else
                 {
-                    bsdf::Xorshift32 xr = bsdf_rng(rng);
-                    V3 wi;
-                    int lobe;
-                    float pdf;
-                    const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
-                    if (pdf > 0.0f && s.n_emissive > 0)
+                    // ---- next-event estimation: light sample ----
+                    if (s.n_emissive > 0 && can_light_sample(m))
                     {
-                        const V3 w = tp * (f * fabsf(dot(ns, wi)) / pdf);
-                        want_bsdf = true;
-                        bs_d = f4(wi, 1.0e35f - 1.0e-4f);
-                        bsdf_pending = f4(w, pdf);
+                        const LightSample ls = sample_light(s, rc, rng);
+                        if (ls.pdf_area > 0.0f)
+                        {
+                            const V3 to_l = ls.point - P;
+                            const float dist = length(to_l);
+                            const V3 wi = to_l / dist;
+                            bsdf::Query q;
+                            q.view = view;
+                            q.ns = ns;
+                            q.ng = ng;
+                            q.light = wi;
+                            float bsdf_pdf;
+                            const V3 f = bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
+                            if (bsdf_pdf > 0.0f)
+                            {
+                                const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
+                                if (cos_l > 1.0e-5f)
+                                {
+                                    const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
+                                    const float mis = balance_heuristic(light_pdf, bsdf_pdf);
+                                    const float cosine = fabsf(dot(ns, wi));
+                                    light_contrib = tp * (f * cosine * ls.emission * mis / light_pdf);
+                                    if (!is_black(light_contrib))
+                                    {
+                                        want_shadow = true;
+                                        sh_o = f4(P, 0.0f);
+                                        sh_d = f4(wi, dist - 1.0e-4f);
+                                    }
+                                }
+                            }
+                        }
+                    }
+
+                    // ---- next-event estimation: BSDF sample ----
+                    {
+                        bsdf::Xorshift32 xr = bsdf_rng(rng);
+                        V3 wi;
+                        int lobe;
+                        float pdf;
+                        const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                        if (pdf > 0.0f && s.n_emissive > 0)
+                        {
+                            const V3 w = tp * (f * fabsf(dot(ns, wi)) / pdf);
+                            want_bsdf = true;
+                            bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                            bsdf_pending = f4(w, pdf);
+                        }
                     }
                 }
 
@@ -714,17 +647,24 @@ cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Qu
     return cudaGetLastError();
 }
 
-cudaError_t launch_bounce(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
-                          const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
-                          unsigned long long* stats, int n_sm, cudaStream_t st)
+cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next, const Queue& shadow,
+                          const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st)
 {
     const int tgrid = grid_for(capacity, 128, n_sm * 16);
     reset_counts_kernel<<<1, 1, 0, st>>>(next.count, shadow.count, bsdfq.count);
     trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, in);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
+                         const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
+                         unsigned long long* stats, const ReservoirBuf& restir, int n_sm, cudaStream_t st)
+{
+    const int tgrid = grid_for(capacity, 128, n_sm * 16);
     if (rc.bsdf == GBPT_BSDF_PRINCIPLED)
-        shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats);
+        shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir);
     else
-        shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats);
+        shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir);
     trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, shadow);
     trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, bsdfq);
     resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq);

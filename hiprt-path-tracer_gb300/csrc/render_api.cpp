@@ -82,6 +82,16 @@ struct gbpt_renderer
     int64_t iteration = 0;
     int64_t samples = 0;
     int n_sm = 1;
+    // ReSTIR DI
+    bool restir = false;
+    gbpt_restir_di_settings restir_settings;
+    DevMem restir_mem;
+    gbpt::GBuffer gb[2];
+    int gb_cur = 0;
+    gbpt::ReservoirBuf res[5];  // initial, temporal, spatial ping, spatial pong, previous
+    int res_final = 0;
+    bool has_prev = false;
+    float prev_inverse_view[16];
 };
 
 namespace {
@@ -103,6 +113,59 @@ gbpt::Queue make_queue(DevMem& m, int64_t cap, bool closest_out, bool any_out)
 bool is_emissive(const gbpt_material& m) { return m.emission[0] > 0.0f || m.emission[1] > 0.0f || m.emission[2] > 0.0f; }
 
 float lerpf(float a, float b, float t) { return (1.0f - t) * a + t * b; }
+
+// inverse of a row-major 4x4 (Gauss-Jordan with partial pivoting, in double); false if singular
+bool invert4(const double* m, double* out)
+{
+    double a[4][8];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 8; j++) a[i][j] = j < 4 ? m[4 * i + j] : (j - 4 == i ? 1.0 : 0.0);
+    for (int c = 0; c < 4; c++)
+    {
+        int piv = c;
+        for (int r = c + 1; r < 4; r++)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (std::fabs(a[piv][c]) < 1e-300) return false;
+        if (piv != c)
+            for (int j = 0; j < 8; j++) std::swap(a[c][j], a[piv][j]);
+        const double d = a[c][c];
+        for (int j = 0; j < 8; j++) a[c][j] /= d;
+        for (int r = 0; r < 4; r++)
+            if (r != c)
+            {
+                const double f = a[r][c];
+                for (int j = 0; j < 8; j++) a[r][j] -= f * a[c][j];
+            }
+    }
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) out[4 * i + j] = a[i][j + 4];
+    return true;
+}
+
+// view-projection (world -> NDC, points on the right) of a camera given by its inverse view and
+// inverse projection: the inverse of inverse_view * inverse_projection
+bool view_projection(const float* iv, const float* ip, float* vp)
+{
+    double prod[16], inv[16];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+        {
+            double acc = 0.0;
+            for (int k = 0; k < 4; k++) acc += (double)iv[4 * i + k] * (double)ip[4 * k + j];
+            prod[4 * i + j] = acc;
+        }
+    if (!invert4(prod, inv)) return false;
+    for (int i = 0; i < 16; i++) vp[i] = (float)inv[i];
+    return true;
+}
+
+void camera_position(const float* iv, float* pos)
+{
+    const float w = iv[15] != 0.0f ? iv[15] : 1.0f;
+    pos[0] = iv[3] / w;
+    pos[1] = iv[7] / w;
+    pos[2] = iv[11] / w;
+}
 float pow4f(float x)
 {
     const float x2 = x * x;
@@ -373,6 +436,7 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
 gbpt_status gbpt_renderer_destroy(gbpt_renderer* r)
 {
     if (!r) return GBPT_OK;
+    r->restir_mem.release();
     r->mem.release();
     delete r;
     return GBPT_OK;
@@ -400,22 +464,232 @@ gbpt_status gbpt_pass_camera_rays(gbpt_renderer* r, void* stream)
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "camera rays");
 }
 
-gbpt_status gbpt_pass_bounce(gbpt_renderer* r, int32_t bounce, void* stream)
+gbpt_status gbpt_pass_extend(gbpt_renderer* r, int32_t bounce, void* stream)
 {
     if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
     if (bounce < 0 || bounce > r->rc.nb_bounces) return set_error(GBPT_ERROR_INVALID_ARG, "bounce out of range");
-    const gbpt::Queue& in = r->q[r->cur];
-    const gbpt::Queue& next = r->q[r->cur ^ 1];
-    cudaError_t e = gbpt::launch_bounce(r->scene->view, r->rc, r->pb, in, next, r->shadow, r->bsdfq, bounce, r->capacity,
-                                        r->stats, r->n_sm, (cudaStream_t)stream);
-    r->cur ^= 1;
-    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "bounce");
+    cudaError_t e = gbpt::launch_extend(r->scene->view, r->q[r->cur], r->q[r->cur ^ 1], r->shadow, r->bsdfq, r->capacity,
+                                        r->n_sm, (cudaStream_t)stream);
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "extend");
 }
+
+gbpt_status gbpt_pass_shade(gbpt_renderer* r, int32_t bounce, void* stream)
+{
+    if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
+    if (bounce < 0 || bounce > r->rc.nb_bounces) return set_error(GBPT_ERROR_INVALID_ARG, "bounce out of range");
+    gbpt::ReservoirBuf none = {nullptr, nullptr};
+    const gbpt::ReservoirBuf& restir = (r->restir && bounce == 0) ? r->res[r->res_final] : none;
+    cudaError_t e = gbpt::launch_shade(r->scene->view, r->rc, r->pb, r->q[r->cur], r->q[r->cur ^ 1], r->shadow, r->bsdfq,
+                                       bounce, r->capacity, r->stats, restir, r->n_sm, (cudaStream_t)stream);
+    r->cur ^= 1;
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "shade");
+}
+
+gbpt_status gbpt_pass_bounce(gbpt_renderer* r, int32_t bounce, void* stream)
+{
+    gbpt_status st = gbpt_pass_extend(r, bounce, stream);
+    return st == GBPT_OK ? gbpt_pass_shade(r, bounce, stream) : st;
+}
+
+namespace {
+
+gbpt::RestirConst restir_const(const gbpt_renderer* r)
+{
+    const gbpt_restir_di_settings& k = r->restir_settings;
+    gbpt::RestirConst c;
+    std::memset(&c, 0, sizeof(c));
+    c.light_candidates = k.light_candidates;
+    c.bsdf_candidates = k.bsdf_candidates;
+    c.visibility_reuse = k.do_visibility_reuse;
+    c.do_temporal = k.do_temporal;
+    c.temporal_search_count = k.temporal_search_count;
+    c.temporal_search_radius = k.temporal_search_radius;
+    c.do_spatial = k.do_spatial;
+    c.spatial_passes = k.spatial_passes;
+    c.spatial_neighbors = k.spatial_neighbors;
+    c.spatial_radius = k.spatial_radius;
+    c.m_cap = k.m_cap;
+    c.confidence_weights = k.use_confidence_weights;
+    c.bias_correction_visibility = k.bias_correction_visibility;
+    c.final_visibility = k.do_final_shading_visibility;
+    c.normal_similarity_cos = k.normal_similarity_cos;
+    c.plane_distance = k.plane_distance_threshold;
+    c.frame = (uint32_t)r->iteration;
+    c.seed = r->rc.seed;
+    c.has_prev = r->has_prev ? 1 : 0;
+    camera_position(r->rc.inverse_view, c.camera_pos);
+    camera_position(r->prev_inverse_view, c.prev_camera_pos);
+    return c;
+}
+
+// Spatial-neighbour seed of a frame and pass, shared by every pixel (coalesced spatial reuse)
+uint32_t spatial_seed(uint32_t frame, int pass, uint32_t seed)
+{
+    uint64_t z = ((uint64_t)frame << 32) ^ ((uint64_t)(uint32_t)pass << 16) ^ (uint64_t)seed ^ 0x5851F42D4C957F2DULL;
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    const uint32_t s = (uint32_t)((z ^ (z >> 31)) >> 16);
+    return s != 0u ? s : 0x9E3779B9u;
+}
+
+gbpt_status restir_ready(gbpt_renderer* r)
+{
+    if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
+    if (!r->restir) return set_error(GBPT_ERROR_INVALID_ARG, "ReSTIR DI is not enabled on this renderer");
+    return GBPT_OK;
+}
+
+}  // namespace
+
+gbpt_status gbpt_restir_di_default_settings(gbpt_restir_di_settings* s)
+{
+    if (!s) return set_error(GBPT_ERROR_INVALID_ARG, "settings is NULL");
+    std::memset(s, 0, sizeof(*s));
+    s->enabled = 1;
+    s->light_candidates = 4;
+    s->bsdf_candidates = 1;
+    s->do_visibility_reuse = 1;
+    s->do_temporal = 1;
+    s->temporal_search_count = 8;
+    s->temporal_search_radius = 4.0f;
+    s->do_spatial = 1;
+    s->spatial_passes = 1;
+    s->spatial_neighbors = 5;
+    s->spatial_radius = 16.0f;
+    s->m_cap = 3;
+    s->use_confidence_weights = 1;
+    s->bias_correction_visibility = 1;
+    s->do_final_shading_visibility = 1;
+    s->normal_similarity_cos = 0.906307787f;
+    s->plane_distance_threshold = 0.1f;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_settings* k)
+{
+    if (!r || !k) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    r->restir_mem.release();
+    r->restir = false;
+    r->has_prev = false;
+    r->rc.restir_final_visibility = 0;
+    if (!k->enabled) return GBPT_OK;
+    if (r->rc.bsdf != GBPT_BSDF_PRINCIPLED) return set_error(GBPT_ERROR_INVALID_ARG, "ReSTIR DI needs GBPT_BSDF_PRINCIPLED");
+    if (r->rc.spp != 1) return set_error(GBPT_ERROR_INVALID_ARG, "ReSTIR DI needs samples_per_launch = 1");
+    if (k->light_candidates < 0 || k->bsdf_candidates < 0 || k->light_candidates + k->bsdf_candidates == 0 ||
+        k->light_candidates > 4096 || k->bsdf_candidates > 64)
+        return set_error(GBPT_ERROR_INVALID_ARG, "candidate counts out of range");
+    if (k->do_spatial && (k->spatial_neighbors < 1 || k->spatial_neighbors > 32 || k->spatial_passes < 1 ||
+                          k->spatial_passes > 16 || !(k->spatial_radius > 0.0f)))
+        return set_error(GBPT_ERROR_INVALID_ARG, "spatial settings out of range (1..32 neighbours, 1..16 passes)");
+    if (k->do_temporal && (k->temporal_search_count < 0 || k->temporal_search_count > 64))
+        return set_error(GBPT_ERROR_INVALID_ARG, "temporal_search_count out of range");
+    const int64_t npix = (int64_t)r->rc.width * r->rc.height;
+    DevMem& M = r->restir_mem;
+    for (int g = 0; g < 2; g++)
+    {
+        r->gb[g].pos = M.alloc<float4>(npix);
+        r->gb[g].ns = M.alloc<float4>(npix);
+        r->gb[g].ng = M.alloc<float4>(npix);
+    }
+    for (int b = 0; b < 5; b++)
+    {
+        r->res[b].s = M.alloc<float4>(npix);
+        r->res[b].w = M.alloc<int4>(npix);
+    }
+    cudaError_t e = M.err;
+    for (int b = 0; b < 5 && e == cudaSuccess; b++)
+    {
+        e = cudaMemset(r->res[b].s, 0, npix * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMemset(r->res[b].w, 0, npix * sizeof(int4));
+    }
+    if (e != cudaSuccess)
+    {
+        M.release();
+        return cuda_error(e, "ReSTIR DI buffers");
+    }
+    r->restir_settings = *k;
+    r->restir = true;
+    r->gb_cur = 0;
+    r->res_final = 0;
+    r->rc.restir_final_visibility = k->do_final_shading_visibility;
+    std::memcpy(r->prev_inverse_view, r->rc.inverse_view, sizeof(r->prev_inverse_view));
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_set_camera(gbpt_renderer* r, const float* inverse_view, const float* inverse_projection)
+{
+    if (!r || !inverse_view || !inverse_projection) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    std::memcpy(r->rc.inverse_view, inverse_view, sizeof(r->rc.inverse_view));
+    std::memcpy(r->rc.inverse_projection, inverse_projection, sizeof(r->rc.inverse_projection));
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_pass_restir_di_initial(gbpt_renderer* r, void* stream)
+{
+    gbpt_status st = restir_ready(r);
+    if (st != GBPT_OK) return st;
+    cudaStream_t cs = (cudaStream_t)stream;
+    const int64_t npix = (int64_t)r->rc.width * r->rc.height;
+    const gbpt::GBuffer& gb = r->gb[r->gb_cur];
+    cudaError_t e = gbpt::launch_restir_gbuffer(r->scene->view, r->q[r->cur], gb, npix, r->n_sm, cs);
+    if (e == cudaSuccess)
+        e = gbpt::launch_restir_initial(r->scene->view, r->rc, restir_const(r), gb, r->res[0], r->n_sm, cs);
+    r->res_final = 0;
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI initial candidates");
+}
+
+gbpt_status gbpt_pass_restir_di_temporal(gbpt_renderer* r, void* stream)
+{
+    gbpt_status st = restir_ready(r);
+    if (st != GBPT_OK) return st;
+    gbpt::RestirConst k = restir_const(r);
+    if (!view_projection(r->prev_inverse_view, r->rc.inverse_projection, k.prev_view_projection))
+        return set_error(GBPT_ERROR_INVALID_ARG, "the previous camera matrices are singular");
+    cudaError_t e = gbpt::launch_restir_temporal(r->scene->view, r->rc, k, r->gb[r->gb_cur], r->gb[r->gb_cur ^ 1],
+                                                 r->res[0], r->res[4], r->res[1], r->n_sm, (cudaStream_t)stream);
+    r->res_final = 1;
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI temporal reuse");
+}
+
+gbpt_status gbpt_pass_restir_di_spatial(gbpt_renderer* r, int32_t pass_index, void* stream)
+{
+    gbpt_status st = restir_ready(r);
+    if (st != GBPT_OK) return st;
+    if (pass_index < 0 || pass_index >= r->restir_settings.spatial_passes)
+        return set_error(GBPT_ERROR_INVALID_ARG, "pass_index out of range");
+    const int in = r->res_final;
+    const int out = in == 2 ? 3 : 2;
+    cudaError_t e = gbpt::launch_restir_spatial(r->scene->view, r->rc, restir_const(r), r->gb[r->gb_cur], r->res[in],
+                                                r->res[out], pass_index,
+                                                spatial_seed((uint32_t)r->iteration, pass_index, r->rc.seed), r->n_sm,
+                                                (cudaStream_t)stream);
+    r->res_final = out;
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI spatial reuse");
+}
+
+namespace {
+
+// end of a ReSTIR frame: the final reservoirs become the previous frame's, the G-buffers swap
+cudaError_t restir_end_frame(gbpt_renderer* r, cudaStream_t cs)
+{
+    const int64_t npix = (int64_t)r->rc.width * r->rc.height;
+    const gbpt::ReservoirBuf& f = r->res[r->res_final];
+    cudaError_t e = cudaMemcpyAsync(r->res[4].s, f.s, npix * sizeof(float4), cudaMemcpyDeviceToDevice, cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r->res[4].w, f.w, npix * sizeof(int4), cudaMemcpyDeviceToDevice, cs);
+    r->gb_cur ^= 1;
+    r->has_prev = true;
+    std::memcpy(r->prev_inverse_view, r->rc.inverse_view, sizeof(r->prev_inverse_view));
+    return e;
+}
+
+}  // namespace
 
 gbpt_status gbpt_pass_accumulate(gbpt_renderer* r, void* stream)
 {
     if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
     cudaError_t e = gbpt::launch_accumulate(r->rc, r->pb, r->acc32, r->acc64, r->n_sm, (cudaStream_t)stream);
+    if (e == cudaSuccess && r->restir) e = restir_end_frame(r, (cudaStream_t)stream);
     r->iteration += r->rc.spp;
     r->samples += r->rc.spp;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "accumulate");
@@ -428,7 +702,16 @@ gbpt_status gbpt_render(gbpt_renderer* r, int32_t n_launches, void* stream)
     for (int32_t k = 0; k < n_launches; k++)
     {
         gbpt_status st = gbpt_pass_camera_rays(r, stream);
-        for (int b = 0; st == GBPT_OK && b <= r->rc.nb_bounces; b++) st = gbpt_pass_bounce(r, b, stream);
+        if (st == GBPT_OK && r->restir)
+        {
+            st = gbpt_pass_extend(r, 0, stream);
+            if (st == GBPT_OK) st = gbpt_pass_restir_di_initial(r, stream);
+            if (st == GBPT_OK && r->restir_settings.do_temporal) st = gbpt_pass_restir_di_temporal(r, stream);
+            for (int p = 0; st == GBPT_OK && r->restir_settings.do_spatial && p < r->restir_settings.spatial_passes; p++)
+                st = gbpt_pass_restir_di_spatial(r, p, stream);
+            if (st == GBPT_OK) st = gbpt_pass_shade(r, 0, stream);
+        }
+        for (int b = r->restir ? 1 : 0; st == GBPT_OK && b <= r->rc.nb_bounces; b++) st = gbpt_pass_bounce(r, b, stream);
         if (st == GBPT_OK) st = gbpt_pass_accumulate(r, stream);
         if (st != GBPT_OK) return st;
     }
@@ -445,6 +728,68 @@ gbpt_status gbpt_renderer_get_image(gbpt_renderer* r, float* rgb32, double* rgb6
     if (e == cudaSuccess && rgb64) e = cudaMemcpyAsync(rgb64, r->acc64, 3 * npix * sizeof(double), cudaMemcpyDeviceToHost, cs);
     if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "image read-back");
+}
+
+namespace {
+
+gbpt_status reservoir_buffer(gbpt_renderer* r, int32_t which, gbpt::ReservoirBuf& out)
+{
+    gbpt_status st = restir_ready(r);
+    if (st != GBPT_OK) return st;
+    switch (which)
+    {
+    case GBPT_RESERVOIRS_INITIAL: out = r->res[0]; break;
+    case GBPT_RESERVOIRS_TEMPORAL: out = r->res[1]; break;
+    case GBPT_RESERVOIRS_FINAL: out = r->res[r->res_final]; break;
+    case GBPT_RESERVOIRS_PREVIOUS: out = r->res[4]; break;
+    default: return set_error(GBPT_ERROR_INVALID_ARG, "unknown reservoir buffer");
+    }
+    return GBPT_OK;
+}
+
+}  // namespace
+
+gbpt_status gbpt_restir_di_get_reservoirs(gbpt_renderer* r, int32_t which, float* host_out, void* stream)
+{
+    gbpt::ReservoirBuf b;
+    gbpt_status st = reservoir_buffer(r, which, b);
+    if (st != GBPT_OK) return st;
+    if (!host_out) return set_error(GBPT_ERROR_INVALID_ARG, "host_out is NULL");
+    const int64_t npix = (int64_t)r->rc.width * r->rc.height;
+    std::vector<float4> s(npix);
+    std::vector<int4> w(npix);
+    cudaStream_t cs = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(s.data(), b.s, npix * sizeof(float4), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w.data(), b.w, npix * sizeof(int4), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) return cuda_error(e, "reservoir read-back");
+    for (int64_t i = 0; i < npix; i++)
+    {
+        std::memcpy(host_out + 8 * i, &s[i], 16);
+        std::memcpy(host_out + 8 * i + 4, &w[i], 16);
+    }
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_restir_di_set_reservoirs(gbpt_renderer* r, int32_t which, const float* host_in, void* stream)
+{
+    gbpt::ReservoirBuf b;
+    gbpt_status st = reservoir_buffer(r, which, b);
+    if (st != GBPT_OK) return st;
+    if (!host_in) return set_error(GBPT_ERROR_INVALID_ARG, "host_in is NULL");
+    const int64_t npix = (int64_t)r->rc.width * r->rc.height;
+    std::vector<float4> s(npix);
+    std::vector<int4> w(npix);
+    for (int64_t i = 0; i < npix; i++)
+    {
+        std::memcpy(&s[i], host_in + 8 * i, 16);
+        std::memcpy(&w[i], host_in + 8 * i + 4, 16);
+    }
+    cudaStream_t cs = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(b.s, s.data(), npix * sizeof(float4), cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.w, w.data(), npix * sizeof(int4), cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "reservoir upload");
 }
 
 gbpt_status gbpt_renderer_get_stats(gbpt_renderer* r, gbpt_render_stats* out, void* stream)

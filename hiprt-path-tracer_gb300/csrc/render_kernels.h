@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "restir.h"
+
 namespace gbpt {
 
 struct SceneView;
@@ -22,6 +24,7 @@ struct RenderConst
     uint32_t seed;
     int32_t do_jittering;
     int32_t ggx_height_correlated;
+    int32_t restir_final_visibility;  // ReSTIR DI final shading traces a shadow ray unless known unoccluded
     float inverse_view[16];
     float inverse_projection[16];
 };
@@ -35,9 +38,24 @@ cudaError_t launch_alias_table(const float* power, int n, double* partial, int n
                                float* prob, int32_t* alias, int32_t* smalls, int32_t* larges, cudaStream_t st);
 cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Queue& q, int32_t iteration_base,
                           unsigned long long* stats, int n_sm, cudaStream_t st);
-cudaError_t launch_bounce(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
-                          const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
-                          unsigned long long* stats, int n_sm, cudaStream_t st);
+// One bounce = extend (closest hit of the active queue) then shade (shade + shadow and BSDF-light
+// traversal + resolve). 'restir' (null buffers when ReSTIR DI is off) holds the final reservoirs
+// that replace next-event estimation at bounce 0.
+cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next, const Queue& shadow,
+                          const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st);
+cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
+                         const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
+                         unsigned long long* stats, const ReservoirBuf& restir, int n_sm, cudaStream_t st);
+cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int n_sm,
+                                  cudaStream_t st);
+cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
+                                  const ReservoirBuf& out, int n_sm, cudaStream_t st);
+cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
+                                   const GBuffer& gb_prev, const ReservoirBuf& initial, const ReservoirBuf& prev,
+                                   const ReservoirBuf& out, int n_sm, cudaStream_t st);
+cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
+                                  const ReservoirBuf& in, const ReservoirBuf& out, int pass, uint32_t neighbor_seed,
+                                  int n_sm, cudaStream_t st);
 cudaError_t launch_accumulate(const RenderConst& rc, const PathBuffers& pb, float* acc32, double* acc64, int n_sm,
                               cudaStream_t st);
 

@@ -1,0 +1,556 @@
+// ReSTIR DI at the camera hit (sm_103a): G-buffer fill, initial candidates with visibility reuse,
+// temporal reuse and spatial reuse with pairwise MIS and confidence weights.
+//
+// Follows the reference's passes (src/Device/kernels/ReSTIR/DI/InitialCandidates.h:180-538,
+// TemporalReuse.h:50-298, SpatialReuse.h:43-322; reservoir src/Device/includes/ReSTIR/DI/
+// Reservoir.h:22-187; target function TargetFunction.h:49-96; pairwise MIS weights
+// src/Device/includes/ReSTIR/TemporalMISWeight.h:164-250 and SpatialMISWeight.h:100-160;
+// neighbour selection UtilsSpatial.h, UtilsTemporal.h:27-98, NeighborSimilarity.h) with their
+// default options: light candidates from the emissive triangles only (no envmap, no light
+// presampling), visibility reuse on, bias correction with visibility, no visibility in the
+// spatial target function, geometric-normal and plane-distance neighbour heuristics.
+// One thread per pixel; the few rays a pixel needs (BSDF candidate, visibility, bias correction)
+// are traced inline with the shared traversal core. Each pass draws from its own PCG stream per
+// pixel; spatial neighbour offsets come from one per-frame Xorshift32 stream shared by all pixels
+// (the reference's coalesced spatial reuse), regenerated for the counting and the reuse loops.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "render_device.h"
+#include "restir.h"
+#include "trace_core.h"
+
+namespace gbpt {
+namespace {
+
+// ReSTIRDIReservoir::add_one_candidate (Reservoir.h:54-61)
+__device__ __forceinline__ void add_candidate(Reservoir& r, V3 point, int tri, int flags, float p_hat, float weight, float u)
+{
+    r.M++;
+    r.w_sum += weight;
+    if (u < weight / r.w_sum)
+    {
+        r.point = point;
+        r.tri = tri;
+        r.flags = flags;
+        r.p_hat = p_hat;
+    }
+}
+
+// ReSTIRDIReservoir::combine_with (Reservoir.h:77-101): draws a number only when the other
+// reservoir has a positive UCW
+template <typename Rng>
+__device__ __forceinline__ bool combine_with(Reservoir& r, const Reservoir& o, float mis, float p_hat, float jacobian,
+                                             Rng& rng)
+{
+    if (o.ucw <= 0.0f)
+    {
+        r.M += o.M;
+        return false;
+    }
+    const float w = mis * p_hat * o.ucw * jacobian;
+    r.M += o.M;
+    r.w_sum += w;
+    if (rng() < w / r.w_sum)
+    {
+        r.point = o.point;
+        r.tri = o.tri;
+        r.flags = o.flags;
+        r.p_hat = p_hat;
+        return true;
+    }
+    return false;
+}
+
+// end() / end_with_normalization() (Reservoir.h:103-121)
+__device__ __forceinline__ void end_reservoir(Reservoir& r)
+{
+    r.ucw = r.w_sum == 0.0f ? 0.0f : 1.0f / r.p_hat * r.w_sum;
+}
+
+__device__ __forceinline__ void end_with_normalization(Reservoir& r, float num, float den)
+{
+    if (r.w_sum == 0.0f || r.w_sum < 1.0e-10f || r.w_sum > 1.0e10f || den == 0.0f || num == 0.0f)
+        r.ucw = 0.0f;
+    else
+        r.ucw = 1.0f / r.p_hat * r.w_sum * num / den;
+    r.M = min(r.M, 1000000);
+}
+
+struct Surface
+{
+    V3 P, ns, ng, view;
+    int prim;
+    int mat;
+    bool inside;
+};
+
+__device__ __forceinline__ Surface load_surface(const GBuffer& gb, int pixel, const float* cam_pos)
+{
+    const float4 p = gb.pos[pixel], n = gb.ns[pixel], g = gb.ng[pixel];
+    Surface su;
+    su.P = xyz(p);
+    su.prim = __float_as_int(p.w);
+    su.ns = xyz(n);
+    su.mat = __float_as_int(n.w);
+    su.ng = xyz(g);
+    su.inside = __float_as_int(g.w) != 0;
+    su.view = normalize(v3(cam_pos[0], cam_pos[1], cam_pos[2]) - su.P);
+    return su;
+}
+
+__device__ __forceinline__ bsdf::Medium medium_of(const Surface& su, const bsdf::Material& m)
+{
+    bsdf::Medium md;
+    md.inside = su.inside;
+    md.eta_incident = su.inside ? m.ior : 1.0f;
+    md.eta_outgoing = su.inside ? 1.0f : m.ior;
+    return md;
+}
+
+__device__ __forceinline__ bool occluded(const SceneView& s, V3 P, V3 dir, float dist, int skip)
+{
+    uint32_t cn = 0, ct = 0;
+    const float4 h = core::trace_ray<true, false>(s.bvh_nodes, s.bvh_tris, f4(P, 0.0f), f4(dir, dist - 1.0e-4f), skip, cn, ct);
+    return __float_as_int(h.w) >= 0;
+}
+
+__device__ __forceinline__ V3 triangle_unit_normal(const SceneView& s, int tri)
+{
+    V3 a, b, c;
+    load_triangle(s, tri, a, b, c);
+    return normalize(cross(b - a, c - a));
+}
+
+__device__ __forceinline__ V3 emission_of(const SceneView& s, int tri)
+{
+    return xyz(s.materials[__ldg(s.material_of + tri)].emission);
+}
+
+// ReSTIR_DI_evaluate_target_function (TargetFunction.h:49-96)
+__device__ float target_function(const SceneView& s, bool hc, const Surface& su, const bsdf::Material& m, V3 point,
+                                 int tri, int flags, bool visibility)
+{
+    if (tri < 0) return 0.0f;
+    V3 dir = point - su.P;
+    const float dist = length(dir);
+    dir = dir / dist;
+    const float cosine = dot(su.ns, dir);
+    if (cosine <= 0.0f) return 0.0f;
+    bsdf::Query q;
+    q.view = su.view;
+    q.ns = su.ns;
+    q.ng = su.ng;
+    q.light = dir;
+    float pdf;
+    const V3 f = bsdf::eval(m, medium_of(su, m), hc, q, flags & kRestirLobeMask, pdf);
+    const float G = fmaxf(0.0f, dot(triangle_unit_normal(s, tri), -dir)) / (dist * dist);
+    const float p = luminance(f * emission_of(s, tri) * cosine * G);
+    if (p == 0.0f) return 0.0f;
+    if (visibility && occluded(s, su.P, dir, dist, su.prim)) return 0.0f;
+    return p;
+}
+
+// ReSTIR_DI_visibility_test_kill_reservoir (src/Device/includes/ReSTIR/Utils.h:25-64)
+__device__ void visibility_kill(const SceneView& s, Reservoir& r, const Surface& su)
+{
+    if (r.ucw <= 0.0f && r.w_sum <= 0.0f) return;
+    if (r.flags & kRestirFlagUnoccluded) return;
+    V3 dir = r.point - su.P;
+    const float dist = length(dir);
+    dir = dir / dist;
+    if (occluded(s, su.P, dir, dist, su.prim))
+        r.ucw = -1.0f;
+    else
+        r.flags |= kRestirFlagUnoccluded;
+}
+
+__device__ __forceinline__ Pcg32 pass_stream(const RestirConst& k, int pixel, int pass)
+{
+    return pcg_seed((uint32_t)pixel, k.frame * 16u + (uint32_t)pass, k.seed);
+}
+
+// neighbour heuristics (NeighborSimilarity.h:34-84): plane distance and geometric-normal angle;
+// positions/primitives from 'gb_pos' (the previous frame's G-buffer for the temporal pass), the
+// neighbour's normal from the current G-buffer as the reference reads it
+__device__ __forceinline__ bool similar(const GBuffer& gb_pos, const GBuffer& gb_cur, int n_idx, int c_idx, V3 P, V3 n_center,
+                                        const RestirConst& k)
+{
+    if (n_idx == c_idx) return true;
+    const float4 np = gb_pos.pos[n_idx];
+    if (__float_as_int(np.w) < 0) return false;
+    if (!(fabsf(dot(xyz(np) - P, n_center)) < k.plane_distance)) return false;
+    return dot(n_center, xyz(gb_cur.ng[n_idx])) > k.normal_similarity_cos;
+}
+
+// get_spatial_neighbor_pixel_index (UtilsSpatial.h:77-143): uniform disk of the reuse radius,
+// offsets rounded to whole pixels; the centre itself for index == count
+__device__ __forceinline__ int spatial_neighbor(int idx, int count, int cx, int cy, int W, int H, float radius,
+                                                bsdf::Xorshift32& nrng)
+{
+    if (idx == count) return cx + cy * W;
+    const float u = nrng();
+    const float v = nrng();
+    const float r = radius * sqrtf(v);
+    float sn, cs;
+    sincosf(kTwoPi * u, &sn, &cs);
+    const int nx = cx + (int)roundf(r * cs), ny = cy + (int)roundf(r * sn);
+    if (nx < 0 || nx >= W || ny < 0 || ny >= H) return -1;
+    return nx + ny * W;
+}
+
+// ---------------------------------------------------------------------------------------------
+// G-buffer from the camera hits (CameraRays, src/Device/kernels/CameraRays.h:178-201)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuffer gb)
+{
+    const int n = *q.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const int pixel = q.slot[i];
+        const float4 hit = q.hits[i];
+        const int prim = __float_as_int(hit.w);
+        if (prim < 0)
+        {
+            gb.pos[pixel] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+            continue;
+        }
+        const V3 o = xyz(q.origin_tmin[i]), d = xyz(q.dir_tmax[i]);
+        const V3 P = o + hit.x * d;
+        V3 a, b, c;
+        load_triangle(s, prim, a, b, c);
+        const V3 ng_raw = normalize(cross(b - a, c - a));
+        V3 ng = ng_raw, ns = ng_raw;
+        const V3 view = -d;
+        fix_backfacing(view, ng, ns);
+        const int mat = __ldg(s.material_of + prim);
+        const gbpt_principled_material& pm = s.pmats[mat];
+        const bool transmissive =
+            (pm.specular_transmission > 0.0f || pm.diffuse_transmission > 0.0f) && pm.thin_walled == 0;
+        const bool inside = transmissive && dot(view, ng_raw) < 0.0f;
+        gb.pos[pixel] = f4(P, __int_as_float(prim));
+        gb.ns[pixel] = f4(ns, __int_as_float(mat));
+        gb.ng[pixel] = f4(ng, __int_as_float(inside ? 1 : 0));
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// initial candidates (InitialCandidates.h:180-538)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) initial_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                      ReservoirBuf out)
+{
+    const int n_pix = rc.width * rc.height;
+    const bool hc = rc.ggx_height_correlated != 0;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        Reservoir r = empty_reservoir();
+        const Surface su = load_surface(gb, pixel, k.camera_pos);
+        if (su.prim < 0 || s.n_emissive == 0)
+        {
+            store_reservoir(out, pixel, r);
+            continue;
+        }
+        Pcg32 rng = pass_stream(k, pixel, 1);
+        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bsdf::Medium md = medium_of(su, m);
+        const float nl = (float)k.light_candidates, nb = (float)k.bsdf_candidates;
+
+        for (int c = 0; c < k.light_candidates; c++)
+        {
+            const LightSample ls = sample_light(s, rc, rng);
+            V3 wi = ls.point - su.P;
+            const float dist = length(wi);
+            wi = wi / dist;
+            const float cosine = fmaxf(0.0f, dot(su.ns, wi));
+            float weight = 0.0f, p_hat = 0.0f;
+            if (cosine > 0.0f && ls.pdf_area > 0.0f)
+            {
+                bsdf::Query q;
+                q.view = su.view;
+                q.ns = su.ns;
+                q.ng = su.ng;
+                q.light = wi;
+                float bsdf_pdf;
+                const V3 f = bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
+                if (bsdf_pdf > 0.0f)
+                {
+                    const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
+                    p_hat = luminance(f * ls.emission * dot(su.ns, wi) * (cos_l / (dist * dist)));
+                    const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
+                    const float mis = light_pdf == 0.0f ? 0.0f : light_pdf / (nl * light_pdf + nb * bsdf_pdf);
+                    weight = mis * p_hat / ls.pdf_area;
+                }
+            }
+            add_candidate(r, ls.point, ls.triangle, 0, p_hat, weight, rng.next());
+        }
+
+        for (int c = 0; c < k.bsdf_candidates; c++)
+        {
+            bsdf::Xorshift32 xr = bsdf_rng(rng);
+            V3 dir;
+            int lobe;
+            float pdf;
+            bsdf::sample(m, md, hc, su.view, su.ns, su.ng, xr, dir, lobe, pdf);
+            if (!(pdf > 0.0f)) continue;
+            uint32_t cn = 0, ct = 0;
+            const float4 h = core::trace_ray<false, false>(s.bvh_nodes, s.bvh_tris, f4(su.P, 0.0f),
+                                                           f4(dir, 1.0e35f - 1.0e-4f), su.prim, cn, ct);
+            const int lt = __float_as_int(h.w);
+            if (lt < 0) continue;
+            const V3 Le = emission_of(s, lt);
+            if (is_black(Le)) continue;
+            const V3 point = su.P + dir * h.x;
+            const int flags = kRestirFlagUnoccluded | (lobe & kRestirLobeMask);
+            const float p_hat = target_function(s, hc, su, m, point, lt, flags, false);
+            const V3 nlt = triangle_unit_normal(s, lt);
+            const float cos_l = fmaxf(0.0f, dot(nlt, -dir));
+            float light_pdf = 0.0f;
+            if (!(dot(dir, su.ns) < 0.0f))
+            {
+                V3 a, b, cc;
+                load_triangle(s, lt, a, b, cc);
+                const float area = 0.5f * length(cross(b - a, cc - a));
+                float pa = 1.0f / area;
+                if (rc.light_sampling == GBPT_LIGHT_POWER)
+                    pa *= (luminance(Le) * area) / s.power_sum;
+                else
+                    pa /= (float)s.n_emissive;
+                light_pdf = area_to_solid_angle_pdf(pa, h.x, cos_l);
+            }
+            const float mis = pdf / (nb * pdf + nl * light_pdf);
+            const float pdf_area = pdf / (h.x * h.x) * cos_l;
+            // the back of a one-sided emitter: zero area pdf (the reference's weight would be 0/0)
+            if (!(pdf_area > 0.0f)) continue;
+            add_candidate(r, point, lt, flags, p_hat, mis * p_hat / pdf_area, rng.next());
+        }
+        end_reservoir(r);
+        r.M = 1;
+        if (k.visibility_reuse) visibility_kill(s, r, su);
+        store_reservoir(out, pixel, r);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// temporal reuse (TemporalReuse.h:50-298, pairwise MIS TemporalMISWeight.h:164-250)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) temporal_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                       GBuffer gb_prev, ReservoirBuf initial, ReservoirBuf prev,
+                                                       ReservoirBuf out)
+{
+    const int W = rc.width, H = rc.height, n_pix = W * H;
+    const bool hc = rc.ggx_height_correlated != 0;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        const Reservoir init = load_reservoir(initial, pixel);
+        const Surface su = load_surface(gb, pixel, k.camera_pos);
+        if (su.prim < 0 || !k.has_prev)
+        {
+            store_reservoir(out, pixel, init);
+            continue;
+        }
+        Pcg32 rng = pass_stream(k, pixel, 2);
+        // backprojection into the previous frame, then up to 'temporal_search_count' jittered tries
+        const V3 ndc = mat_x_point(k.prev_view_projection, su.P);
+        const float px = (ndc.x + 1.0f) * 0.5f * (float)W - 0.5f;
+        const float py = (ndc.y + 1.0f) * 0.5f * (float)H - 0.5f;
+        int t_idx = -1;
+        for (int i = 0; i < k.temporal_search_count + 1; i++)
+        {
+            float ox = 0.0f, oy = 0.0f;
+            if (i > 0)
+            {
+                ox = (rng.next() - 0.5f) * k.temporal_search_radius;
+                oy = (rng.next() - 0.5f) * k.temporal_search_radius;
+            }
+            const int tx = (int)roundf(px + ox), ty = (int)roundf(py + oy);
+            if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
+            t_idx = tx + ty * W;
+            if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, k)) break;
+            t_idx = -1;
+        }
+        if (t_idx < 0)
+        {
+            store_reservoir(out, pixel, init);
+            continue;
+        }
+        const Reservoir tn = load_reservoir(prev, t_idx);
+        const Surface ts = load_surface(gb_prev, t_idx, k.prev_camera_pos);
+        if (tn.M == 0 || ts.prim < 0 || !is_black(xyz(s.materials[ts.mat].emission)))
+        {
+            store_reservoir(out, pixel, init);
+            continue;
+        }
+        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bsdf::Material tm = bsdf::load_material(s.pmats[ts.mat]);
+        const bool vis = k.bias_correction_visibility != 0;
+        Reservoir o = empty_reservoir();
+
+        // temporal neighbour, pairwise MIS weight against the canonical (initial) reservoir
+        const float t_at_center = tn.ucw > 0.0f ? target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, vis) : 0.0f;
+        const float tM = k.confidence_weights ? (float)tn.M : 1.0f;
+        const float cM = k.confidence_weights ? (float)init.M : 1.0f;
+        const float nsum = k.confidence_weights ? (float)tn.M : 1.0f;
+        const float denom = tn.p_hat * nsum + t_at_center * cM;
+        const float mi = denom == 0.0f ? 0.0f : tn.p_hat * tM / denom;
+        const float c_at_neighbor = target_function(s, hc, ts, tm, init.point, init.tri, init.flags, vis);
+        const float denom_mc = c_at_neighbor * nsum + init.p_hat * cM;
+        float mc = 0.0f;
+        if (denom_mc != 0.0f) mc += init.p_hat * cM / denom_mc * (k.confidence_weights ? tM / nsum : 1.0f);
+        if (combine_with(o, tn, mi, t_at_center, 1.0f, rng))
+        {
+            if (vis)
+                o.flags |= kRestirFlagUnoccluded;
+            else
+                o.flags &= ~kRestirFlagUnoccluded;
+        }
+        // canonical sample
+        if (combine_with(o, init, mc == 0.0f ? 1.0f : mc, init.p_hat, 1.0f, rng))
+        {
+            if (vis)
+                o.flags |= kRestirFlagUnoccluded;
+            else
+                o.flags |= init.flags & kRestirFlagUnoccluded;
+        }
+        end_with_normalization(o, 1.0f, 1.0f);
+        if (k.m_cap > 0) o.M = min(o.M, k.m_cap);
+        store_reservoir(out, pixel, o);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// spatial reuse (SpatialReuse.h:43-322, pairwise MIS SpatialMISWeight.h:100-160)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                      ReservoirBuf in, ReservoirBuf out, int pass, int last_pass,
+                                                      uint32_t neighbor_seed)
+{
+    const int W = rc.width, H = rc.height, n_pix = W * H;
+    const bool hc = rc.ggx_height_correlated != 0;
+    const int K = k.spatial_neighbors;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        const Surface su = load_surface(gb, pixel, k.camera_pos);
+        const Reservoir center = load_reservoir(in, pixel);
+        if (su.prim < 0)
+        {
+            store_reservoir(out, pixel, center);
+            continue;
+        }
+        Pcg32 rng = pass_stream(k, pixel, 3 + pass);
+        const int cx = pixel % W, cy = pixel / W;
+        // count the valid neighbours and their confidence (count_valid_spatial_neighbors)
+        bsdf::Xorshift32 nrng{neighbor_seed};
+        int valid = 0, m_sum = 0;
+        uint32_t cache = 0;
+        for (int j = 0; j < K; j++)
+        {
+            const int idx = spatial_neighbor(j, K, cx, cy, W, H, k.spatial_radius, nrng);
+            if (idx < 0) continue;
+            if (!similar(gb, gb, idx, pixel, su.P, su.ng, k)) continue;
+            m_sum += load_reservoir(in, idx).M;
+            valid++;
+            cache |= 1u << j;
+        }
+        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bool vis = k.bias_correction_visibility != 0;
+        const bool update_mc = center.M > 0 && center.ucw > 0.0f;
+        const float cM = k.confidence_weights ? (float)center.M : 1.0f;
+        const float nsum = k.confidence_weights ? (float)m_sum : 1.0f;
+        const float div = k.confidence_weights ? 1.0f : (float)valid;
+        float mc = 0.0f;
+        Reservoir o = empty_reservoir();
+        nrng = bsdf::Xorshift32{neighbor_seed};
+        for (int j = m_sum == 0 ? K : 0; j < K + 1; j++)
+        {
+            if (j < K && !(cache & (1u << j)))
+            {
+                nrng();
+                nrng();
+                continue;
+            }
+            const int idx = spatial_neighbor(j, K, cx, cy, W, H, k.spatial_radius, nrng);
+            if (idx < 0) continue;
+            const Reservoir nbr = load_reservoir(in, idx);
+            float t_at_center = 0.0f;
+            if (nbr.ucw > 0.0f)
+                t_at_center = j == K ? nbr.p_hat : target_function(s, hc, su, m, nbr.point, nbr.tri, nbr.flags, false);
+            float mis;
+            if (j < K)
+            {
+                const float rM = k.confidence_weights ? (float)nbr.M : 1.0f;
+                const float denom = nbr.p_hat * nsum + t_at_center / div * cM;
+                const float mi = denom == 0.0f ? 0.0f : nbr.p_hat * rM / denom;
+                if (update_mc)
+                {
+                    const Surface ns_ = load_surface(gb, idx, k.camera_pos);
+                    const bsdf::Material nm = bsdf::load_material(s.pmats[ns_.mat]);
+                    const float c_at_n = target_function(s, hc, ns_, nm, center.point, center.tri, center.flags, vis);
+                    const float nume_mc = center.p_hat / div * cM;
+                    const float denom_mc = c_at_n * nsum + center.p_hat / div * cM;
+                    const float conf = k.confidence_weights ? (nsum == 0.0f ? 0.0f : rM / nsum) : 1.0f;
+                    if (denom_mc != 0.0f) mc += nume_mc / denom_mc / div * conf;
+                }
+                mis = mi / div;
+            }
+            else
+                mis = mc == 0.0f ? 1.0f : mc;
+            if (combine_with(o, nbr, mis, t_at_center, 1.0f, rng))
+            {
+                if (j == K)
+                    o.flags |= nbr.flags & kRestirFlagUnoccluded;
+                else
+                    o.flags &= ~kRestirFlagUnoccluded;
+            }
+        }
+        end_with_normalization(o, 1.0f, 1.0f);
+        if (k.visibility_reuse && vis && (k.do_temporal || pass != last_pass)) visibility_kill(s, o, su);
+        store_reservoir(out, pixel, o);
+    }
+}
+
+inline int grid_for(int64_t n, int threads, int max_blocks)
+{
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > max_blocks) b = max_blocks;
+    return (int)b;
+}
+
+}  // namespace
+
+cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int n_sm,
+                                  cudaStream_t st)
+{
+    gbuffer_kernel<<<grid_for(n_pix, 256, n_sm * 8), 256, 0, st>>>(s, q, gb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
+                                  const ReservoirBuf& out, int n_sm, cudaStream_t st)
+{
+    const int64_t n = (int64_t)rc.width * rc.height;
+    initial_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
+                                   const GBuffer& gb_prev, const ReservoirBuf& initial, const ReservoirBuf& prev,
+                                   const ReservoirBuf& out, int n_sm, cudaStream_t st)
+{
+    const int64_t n = (int64_t)rc.width * rc.height;
+    temporal_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, gb_prev, initial, prev, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
+                                  const ReservoirBuf& in, const ReservoirBuf& out, int pass, uint32_t neighbor_seed,
+                                  int n_sm, cudaStream_t st)
+{
+    const int64_t n = (int64_t)rc.width * rc.height;
+    spatial_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, in, out, pass, k.spatial_passes - 1,
+                                                                 neighbor_seed);
+    return cudaGetLastError();
+}
+
+}  // namespace gbpt

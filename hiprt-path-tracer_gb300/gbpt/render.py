@@ -46,6 +46,18 @@ class RenderStatsC(ctypes.Structure):
     _fields_ = [("samples", i64), ("extension_rays", i64), ("shadow_rays", i64), ("bsdf_light_rays", i64)]
 
 
+class RestirDISettingsC(ctypes.Structure):
+    _fields_ = [("enabled", i32), ("light_candidates", i32), ("bsdf_candidates", i32), ("do_visibility_reuse", i32),
+                ("do_temporal", i32), ("temporal_search_count", i32), ("temporal_search_radius", ctypes.c_float),
+                ("do_spatial", i32), ("spatial_passes", i32), ("spatial_neighbors", i32),
+                ("spatial_radius", ctypes.c_float), ("m_cap", i32), ("use_confidence_weights", i32),
+                ("bias_correction_visibility", i32), ("do_final_shading_visibility", i32),
+                ("normal_similarity_cos", ctypes.c_float), ("plane_distance_threshold", ctypes.c_float),
+                ("reserved", i32 * 15)]
+
+
+RESERVOIRS_INITIAL, RESERVOIRS_TEMPORAL, RESERVOIRS_FINAL, RESERVOIRS_PREVIOUS = 0, 1, 2, 3
+
 RENDER_SIGNATURES = [
     ("gbpt_scene_create", ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(_lib.BvhParams),
                                          ctypes.POINTER(c_vp), c_vp]),
@@ -62,7 +74,29 @@ RENDER_SIGNATURES = [
     ("gbpt_renderer_get_image", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp]),
     ("gbpt_renderer_get_stats", ctypes.c_int, [c_vp, ctypes.POINTER(RenderStatsC), c_vp]),
     ("gbpt_alias_table_build_noalloc", ctypes.c_int, [c_vp, i32, c_vp, c_vp, c_vp, c_vp]),
+    ("gbpt_restir_di_default_settings", ctypes.c_int, [ctypes.POINTER(RestirDISettingsC)]),
+    ("gbpt_renderer_set_restir_di", ctypes.c_int, [c_vp, ctypes.POINTER(RestirDISettingsC)]),
+    ("gbpt_renderer_set_camera", ctypes.c_int, [c_vp, c_vp, c_vp]),
+    ("gbpt_pass_extend", ctypes.c_int, [c_vp, i32, c_vp]),
+    ("gbpt_pass_shade", ctypes.c_int, [c_vp, i32, c_vp]),
+    ("gbpt_pass_restir_di_initial", ctypes.c_int, [c_vp, c_vp]),
+    ("gbpt_pass_restir_di_temporal", ctypes.c_int, [c_vp, c_vp]),
+    ("gbpt_pass_restir_di_spatial", ctypes.c_int, [c_vp, i32, c_vp]),
+    ("gbpt_restir_di_get_reservoirs", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
+    ("gbpt_restir_di_set_reservoirs", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
 ]
+
+
+def restir_di_settings(**kw) -> RestirDISettingsC:
+    """The reference's ReSTIR DI defaults with the given fields overridden."""
+    lib = _load()
+    c = RestirDISettingsC()
+    _lib.check(lib.gbpt_restir_di_default_settings(ctypes.byref(c)))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
 
 
 def _stream(stream) -> int:
@@ -220,6 +254,40 @@ class Renderer:
 
     def pass_bounce(self, bounce: int, stream=None):
         _lib.check(self._lib.gbpt_pass_bounce(self._h, bounce, _stream(stream)))
+
+    def pass_extend(self, bounce: int, stream=None):
+        _lib.check(self._lib.gbpt_pass_extend(self._h, bounce, _stream(stream)))
+
+    def pass_shade(self, bounce: int, stream=None):
+        _lib.check(self._lib.gbpt_pass_shade(self._h, bounce, _stream(stream)))
+
+    def set_restir_di(self, settings: "RestirDISettingsC"):
+        _lib.check(self._lib.gbpt_renderer_set_restir_di(self._h, ctypes.byref(settings)))
+
+    def set_camera(self, inverse_view, inverse_projection):
+        iv = np.ascontiguousarray(inverse_view, np.float32).reshape(16)
+        ip = np.ascontiguousarray(inverse_projection, np.float32).reshape(16)
+        _lib.check(self._lib.gbpt_renderer_set_camera(self._h, iv.ctypes.data, ip.ctypes.data))
+
+    def pass_restir_initial(self, stream=None):
+        _lib.check(self._lib.gbpt_pass_restir_di_initial(self._h, _stream(stream)))
+
+    def pass_restir_temporal(self, stream=None):
+        _lib.check(self._lib.gbpt_pass_restir_di_temporal(self._h, _stream(stream)))
+
+    def pass_restir_spatial(self, pass_index: int = 0, stream=None):
+        _lib.check(self._lib.gbpt_pass_restir_di_spatial(self._h, pass_index, _stream(stream)))
+
+    def reservoirs(self, which: int, stream=None) -> np.ndarray:
+        """(H*W, 8) float32 reservoir records (words 4-5 are int32 bit patterns)."""
+        n = self.settings.width * self.settings.height
+        out = np.zeros((n, 8), np.float32)
+        _lib.check(self._lib.gbpt_restir_di_get_reservoirs(self._h, which, out.ctypes.data, _stream(stream)))
+        return out
+
+    def set_reservoirs(self, which: int, data: np.ndarray, stream=None):
+        d = np.ascontiguousarray(data, np.float32).reshape(-1, 8)
+        _lib.check(self._lib.gbpt_restir_di_set_reservoirs(self._h, which, d.ctypes.data, _stream(stream)))
 
     def pass_accumulate(self, stream=None):
         _lib.check(self._lib.gbpt_pass_accumulate(self._h, _stream(stream)))

@@ -141,6 +141,70 @@ GBPT_API gbpt_status gbpt_pass_accumulate(gbpt_renderer* r, void* stream);
 GBPT_API gbpt_status gbpt_renderer_get_image(gbpt_renderer* r, float* rgb32, double* rgb64, void* stream);
 GBPT_API gbpt_status gbpt_renderer_get_stats(gbpt_renderer* r, gbpt_render_stats* out, void* stream);
 
+/* ReSTIR DI at the camera hit (the reference's LSS_RESTIR_DI direct lighting,
+ * src/HostDeviceCommon/ReSTIR/ReSTIRDISettings.h:11-161 and KernelOptions/ReSTIRDIOptions.h;
+ * defaults in brackets). Requires GBPT_BSDF_PRINCIPLED and samples_per_launch = 1: one launch is
+ * one frame, whose final reservoirs feed the next frame's temporal pass. Always on: visibility
+ * reuse in the final reservoirs' shadow test, pairwise MIS bias correction, geometric-normal and
+ * plane-distance neighbour heuristics, no envmap or light presampling. */
+typedef struct gbpt_restir_di_settings {
+    int32_t enabled;
+    int32_t light_candidates;           /* number_of_initial_light_candidates [4] */
+    int32_t bsdf_candidates;            /* number_of_initial_bsdf_candidates [1] */
+    int32_t do_visibility_reuse;        /* ReSTIR_DI_DoVisibilityReuse [1] */
+    int32_t do_temporal;                /* common_temporal_pass.do_temporal_reuse_pass [1] */
+    int32_t temporal_search_count;      /* max_neighbor_search_count [8] */
+    float temporal_search_radius;       /* neighbor_search_radius, pixels [4] */
+    int32_t do_spatial;                 /* do_spatial_reuse_pass [1] */
+    int32_t spatial_passes;             /* number_of_passes [1] */
+    int32_t spatial_neighbors;          /* reuse_neighbor_count, 1..32 [5] */
+    float spatial_radius;               /* reuse_radius, pixels [16] */
+    int32_t m_cap;                      /* temporal M cap, 0 = none [3] */
+    int32_t use_confidence_weights;     /* [1] */
+    int32_t bias_correction_visibility; /* ReSTIR_DI_BiasCorrectionUseVisibility [1] */
+    int32_t do_final_shading_visibility;/* [1] */
+    float normal_similarity_cos;        /* normal_similarity_angle_precomp [0.906307787] */
+    float plane_distance_threshold;     /* [0.1] */
+    int32_t reserved[15];
+} gbpt_restir_di_settings;
+
+/* Fills 's' with the reference's defaults (enabled = 1). */
+GBPT_API gbpt_status gbpt_restir_di_default_settings(gbpt_restir_di_settings* s);
+/* Allocates the G-buffers and reservoir buffers and turns ReSTIR DI on (or off with enabled = 0). */
+GBPT_API gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_settings* s);
+/* Moves the camera for the next launch (row-major inverse view / projection as in
+ * gbpt_render_settings); the previous frame's camera is kept for temporal backprojection
+ * (HIPRTRenderData::prev_camera, src/HostDeviceCommon/RenderData.h:93-129). */
+GBPT_API gbpt_status gbpt_renderer_set_camera(gbpt_renderer* r, const float* inverse_view, const float* inverse_projection);
+
+/* Pass-level scheduling with ReSTIR DI (what gbpt_render does per launch):
+ *   gbpt_pass_camera_rays, gbpt_pass_extend(0), gbpt_pass_restir_di_initial,
+ *   gbpt_pass_restir_di_temporal, gbpt_pass_restir_di_spatial(0..passes-1), gbpt_pass_shade(0),
+ *   gbpt_pass_bounce(1..nb_bounces), gbpt_pass_accumulate (which also ends the frame).
+ * extend = closest hit of the bounce's queue; shade = shading, shadow and BSDF-light rays and
+ * their resolve (gbpt_pass_bounce = extend + shade). */
+GBPT_API gbpt_status gbpt_pass_extend(gbpt_renderer* r, int32_t bounce, void* stream);
+GBPT_API gbpt_status gbpt_pass_shade(gbpt_renderer* r, int32_t bounce, void* stream);
+/* Fills the G-buffer from the camera hits and runs ReSTIR_DI_InitialCandidates
+ * (src/Device/kernels/ReSTIR/DI/InitialCandidates.h:478). */
+GBPT_API gbpt_status gbpt_pass_restir_di_initial(gbpt_renderer* r, void* stream);
+/* ReSTIR_DI_TemporalReuse (src/Device/kernels/ReSTIR/DI/TemporalReuse.h:50). */
+GBPT_API gbpt_status gbpt_pass_restir_di_temporal(gbpt_renderer* r, void* stream);
+/* ReSTIR_DI_SpatialReuse (src/Device/kernels/ReSTIR/DI/SpatialReuse.h:43), pass 'pass_index'. */
+GBPT_API gbpt_status gbpt_pass_restir_di_spatial(gbpt_renderer* r, int32_t pass_index, void* stream);
+
+enum {
+    GBPT_RESERVOIRS_INITIAL = 0,
+    GBPT_RESERVOIRS_TEMPORAL = 1,
+    GBPT_RESERVOIRS_FINAL = 2,    /* what the shading of the current frame reads */
+    GBPT_RESERVOIRS_PREVIOUS = 3  /* the previous frame's final reservoirs (temporal input) */
+};
+/* Reservoir buffers as 8 words per pixel: light point xyz, target function, emissive triangle
+ * (int32), (M << 9) | flags (int32), weight sum, UCW (ReSTIRDIReservoir, Reservoir.h:22-187).
+ * Synchronous. 'set' lets a caller inject reservoirs, e.g. to test one pass on given candidates. */
+GBPT_API gbpt_status gbpt_restir_di_get_reservoirs(gbpt_renderer* r, int32_t which, float* host_out, void* stream);
+GBPT_API gbpt_status gbpt_restir_di_set_reservoirs(gbpt_renderer* r, int32_t which, const float* host_in, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,234 @@
+/*
+ * TEST INFRASTRUCTURE ONLY — helpers shared by the CPU oracles (pt_oracle.cpp, restir_oracle.cpp):
+ * float3 math, the PCG32 streams the GPU kernels use, the pinhole camera, brute-force
+ * Moller-Trumbore intersection with the self-hit filter (src/Renderer/Triangle.h:20-63), light
+ * pdfs, and the callback interface to the reference's principled BSDF. Compiled with
+ * -ffp-contract=off.
+ */
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+namespace {
+
+
+struct V { float x, y, z; };
+inline V mk(float x, float y, float z) { return V{x, y, z}; }
+inline V operator+(V a, V b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V operator-(V a, V b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V operator*(V a, V b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline V operator*(V a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+inline V operator/(V a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+inline V neg(V a) { return mk(-a.x, -a.y, -a.z); }
+inline float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V cross(V a, V b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline float len(V a) { return std::sqrt(dot(a, a)); }
+inline V nrm(V a) { return a / std::sqrt(dot(a, a)); }
+inline bool black(V a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+inline float lum(V c) { return 0.3086f * c.x + 0.6094f * c.y + 0.0820f * c.z; }
+
+struct Pcg
+{
+    uint64_t state, inc;
+    uint32_t u32()
+    {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    }
+    float next() { return (float)(u32() >> 8) * (1.0f / 16777216.0f); }
+    int index(int n)
+    {
+        int i = (int)(next() * (float)n);
+        return i < n - 1 ? i : n - 1;
+    }
+};
+
+uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+Pcg pcg_seed(uint32_t pixel, uint32_t iteration, uint32_t seed)
+{
+    Pcg r;
+    r.state = 0;
+    r.inc = ((uint64_t)seed << 1u) | 1u;
+    r.u32();
+    r.state += mix64(((uint64_t)iteration << 32) | pixel);
+    r.u32();
+    return r;
+}
+
+V mat_point(const float* m, V p)
+{
+    float x = m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3];
+    float y = m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7];
+    float z = m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11];
+    float w = m[12] * p.x + m[13] * p.y + m[14] * p.z + m[15];
+    float iw = 1.0f;
+    if (!(w < 1.0e-10f && w > -1.0e-10f)) iw = 1.0f / w;
+    return mk(x * iw, y * iw, z * iw);
+}
+
+struct Scene
+{
+    const float* tv;
+    int nt;
+    const int* mat_of;
+    const float* albedo;
+    const float* emission;
+    const int* emissive;
+    int ne;
+    const float* alias_prob;
+    const int* alias_idx;
+    float power_sum;
+    V a(int t) const { return mk(tv[9 * t], tv[9 * t + 1], tv[9 * t + 2]); }
+    V b(int t) const { return mk(tv[9 * t + 3], tv[9 * t + 4], tv[9 * t + 5]); }
+    V c(int t) const { return mk(tv[9 * t + 6], tv[9 * t + 7], tv[9 * t + 8]); }
+    V alb(int t) const { int m = mat_of[t]; return mk(albedo[3 * m], albedo[3 * m + 1], albedo[3 * m + 2]); }
+    V emi(int t) const { int m = mat_of[t]; return mk(emission[3 * m], emission[3 * m + 1], emission[3 * m + 2]); }
+};
+
+bool mt(V A, V B, V C, V o, V d, float& t)
+{
+    const float EPS = 0.0000001f;
+    V e1 = B - A, e2 = C - A;
+    V h = cross(d, e2);
+    float a = dot(e1, h);
+    if (a > -EPS && a < EPS) return false;
+    float f = 1.0f / a;
+    V s = o - A;
+    float u = f * dot(s, h);
+    if (u < 0.0f || u > 1.0f) return false;
+    V q = cross(s, e1);
+    float v = f * dot(d, q);
+    if (v < 0.0f || u + v > 1.0f) return false;
+    t = f * dot(e2, q);
+    return t > EPS;
+}
+
+// closest hit with the self-hit filter; returns prim or -1 (lowest index on exact ties)
+int closest(const Scene& s, V o, V d, int skip, float& t_out)
+{
+    int best = -1;
+    float bt = 0.0f;
+    for (int k = 0; k < s.nt; k++)
+    {
+        float t;
+        if (k == skip || !mt(s.a(k), s.b(k), s.c(k), o, d, t)) continue;
+        if (best < 0 || t < bt)
+        {
+            best = k;
+            bt = t;
+        }
+    }
+    t_out = bt;
+    return best;
+}
+
+bool occluded(const Scene& s, V o, V d, int skip, float tmax)
+{
+    float t;
+    int p = closest(s, o, d, skip, t);
+    return p >= 0 && t < tmax;
+}
+
+V cosine_sample(V n, float r1, float r2u)
+{
+    float r2 = 2.0f * r2u - 1.0f;
+    if (r1 < 1.0e-8f && r2 < -0.999999f && n.z > 0.999999f)
+    {
+        r1 += 1.0e-7f;
+        r2 += 1.0e-7f;
+    }
+    float theta = 6.28318530717958647693f * r1;
+    float sn = std::sqrt(std::max(0.0f, 1.0f - r2 * r2));
+    return nrm(n + mk(sn * std::cos(theta), sn * std::sin(theta), r2));
+}
+
+V lambert(V albedo, float NoL, float& pdf)
+{
+    pdf = 0.0f;
+    if (NoL <= 0.0f) return mk(0, 0, 0);
+    pdf = NoL * 0.31830988618379067154f;
+    return albedo * 0.31830988618379067154f;
+}
+
+float light_pdf_area(const Scene& s, int lt, float area, V Le, int strategy)
+{
+    float p = 1.0f / area;
+    if (strategy == 1)
+        p *= (lum(Le) * area) / s.power_sum;
+    else
+        p /= (float)s.ne;
+    return p;
+}
+
+float balance(float a, float b) { return a == 0.0f ? 0.0f : a / (a + b); }
+
+float a2s(float area_pdf, float dist, float cosl) { return cosl < 1.0e-8f ? 0.0f : area_pdf * dist * dist / cosl; }
+
+struct Settings
+{
+    int width, height, nb_bounces, do_rr, rr_min, light, seed, jitter, spp, iteration_base;
+    float rr_clamp;
+    const float* iv;
+    const float* ip;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Principled scenes: the same estimator with the BSDF evaluated and sampled through callbacks
+// (the reference's own principled BSDF, oracle/ref_bsdf.cpp) on 64-word material records and
+// 16-float queries (view, shading normal, geometric normal, light, eta in, eta out, inside, lobe).
+// Each BSDF sample is seeded with one 32-bit PCG draw (Xorshift32 seed, 0 -> 0x9E3779B9), as the
+// GPU kernels do. Volume tracking: a path is inside a non-thin transmissive object after a glass
+// refraction or diffuse transmission into it; its back face is then hit from inside.
+// ---------------------------------------------------------------------------------------------
+typedef void (*bsdf_eval_fn)(const float* mat, const float* q, float* out4);
+typedef void (*bsdf_sample_fn)(const float* mat, const float* q, uint32_t seed, float* out8, int32_t* lobe);
+
+struct PScene
+{
+    const float* pmats;  // effective materials, 64 words each
+    bsdf_eval_fn eval;
+    bsdf_sample_fn sample;
+    const float* mat(int m) const { return pmats + 64 * (size_t)m; }
+};
+
+bool smooth(float r) { return r <= 1.0e-2f; }
+
+bool can_light_sample(const float* m)
+{
+    const float rough = m[3], metallic = m[7], transmission = m[38], coat = m[25], coat_rough = m[26];
+    const float second_w = m[17], second_r = m[18];
+    bool smooth_base = smooth(rough) && (metallic == 1.0f || transmission == 1.0f);
+    bool smooth_coat = coat == 0.0f || smooth(coat_rough);
+    bool smooth_second = smooth(second_r) || second_w == 0.0f;
+    return !(smooth_base && smooth_coat && smooth_second);
+}
+
+void make_query(float* q, V view, V ns, V ng, V l, float eta_i, float eta_o, bool inside, int lobe)
+{
+    q[0] = view.x; q[1] = view.y; q[2] = view.z;
+    q[3] = ns.x; q[4] = ns.y; q[5] = ns.z;
+    q[6] = ng.x; q[7] = ng.y; q[8] = ng.z;
+    q[9] = l.x; q[10] = l.y; q[11] = l.z;
+    q[12] = eta_i; q[13] = eta_o; q[14] = inside ? 1.0f : 0.0f; q[15] = (float)lobe;
+}
+
+uint32_t bsdf_seed(Pcg& rng)
+{
+    uint32_t s = rng.u32();
+    return s != 0u ? s : 0x9E3779B9u;
+}
+
+}  // namespace

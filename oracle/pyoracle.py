@@ -239,6 +239,78 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
     return out
 
 
+def restir_spatial_seed(frame: int, pass_index: int, seed: int) -> int:
+    """Per-frame spatial-neighbour seed shared by all pixels (the library's spatial_seed,
+    csrc/render_api.cpp): splitmix64 finaliser of (frame, pass, seed)."""
+    m = (1 << 64) - 1
+    z = ((frame << 32) ^ (pass_index << 16) ^ seed ^ 0x5851F42D4C957F2D) & m
+    z = (z + 0x9E3779B97F4A7C15) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    s = ((z ^ (z >> 31)) >> 16) & 0xFFFFFFFF
+    return s if s != 0 else 0x9E3779B9
+
+
+def _restir_lib():
+    lib = _pt_lib()
+    if not getattr(lib, "_restir_sigs", False):
+        lib.orc_restir_gbuffer.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, _c_f, _c_f, _c_f, ctypes.c_int]
+        lib.orc_restir_pass.argtypes = [ctypes.c_int, _c_f, ctypes.c_int, _c_i, _c_f, _c_i, ctypes.c_int, _c_f, _c_i,
+                                        ctypes.c_float, _c_f, ctypes.c_void_p, ctypes.c_void_p, _c_i, _c_f, _c_f,
+                                        _c_f, _c_f, _c_f, _c_f, _c_f, ctypes.c_int, ctypes.c_uint32, ctypes.c_int]
+        lib._restir_sigs = True
+    return lib
+
+
+def restir_gbuffer(soup, material_of, pmats, width, height, seed, frame, jitter, inverse_view, inverse_projection,
+                   nthreads=0) -> np.ndarray:
+    """G-buffer of the camera hits, (W*H, 12) float32 (int fields as bit patterns)."""
+    lib = _restir_lib()
+    soup = np.ascontiguousarray(soup, np.float32)
+    mo = np.ascontiguousarray(material_of, np.int32)
+    pm = np.ascontiguousarray(pmats, np.float32)
+    iv = np.ascontiguousarray(inverse_view, np.float32).reshape(16)
+    ip = np.ascontiguousarray(inverse_projection, np.float32).reshape(16)
+    gb = np.zeros((width * height, 12), np.float32)
+    lib.orc_restir_gbuffer(_ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(pm, _c_f), width, height, seed, frame,
+                           1 if jitter else 0, _ptr(iv, _c_f), _ptr(ip, _c_f), _ptr(gb, _c_f), nthreads)
+    return gb
+
+
+def restir_pass(pass_kind, scene, pmats, settings_i, settings_f, prev_vp, gb, gb_prev=None, inp=None, prev=None,
+                spatial_index=0, spatial_seed=0, nthreads=0) -> np.ndarray:
+    """One ReSTIR DI pass of the oracle (0 initial, 1 temporal, 2 spatial) shading with the
+    reference's own BSDF; scene = dict(soup, material_of, emission, emissive, alias_prob, alias_idx,
+    power_sum). Returns (W*H, 8) reservoir records."""
+    lib = _restir_lib()
+    ref = ctypes.CDLL(REF_SO)
+    eval_fn = ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value
+    sample_fn = ctypes.cast(ref.ref_principled_sample_one, ctypes.c_void_p).value
+    soup = np.ascontiguousarray(scene["soup"], np.float32)
+    mo = np.ascontiguousarray(scene["material_of"], np.int32)
+    em = np.ascontiguousarray(scene["emission"], np.float32)
+    ei = np.ascontiguousarray(scene["emissive"], np.int32)
+    ap = np.ascontiguousarray(scene["alias_prob"], np.float32)
+    ai = np.ascontiguousarray(scene["alias_idx"], np.int32)
+    pm = np.ascontiguousarray(pmats, np.float32)
+    si = np.ascontiguousarray(settings_i, np.int32)
+    sf = np.ascontiguousarray(settings_f, np.float32)
+    vp = np.ascontiguousarray(prev_vp if prev_vp is not None else np.eye(4), np.float32).reshape(16)
+    n = int(si[0]) * int(si[1])
+    z = np.zeros((n, 8), np.float32)
+    gbp = np.ascontiguousarray(gb_prev if gb_prev is not None else gb, np.float32)
+    inp_ = np.ascontiguousarray(inp if inp is not None else z, np.float32)
+    prev_ = np.ascontiguousarray(prev if prev is not None else z, np.float32)
+    out = np.zeros((n, 8), np.float32)
+    gb = np.ascontiguousarray(gb, np.float32)
+    lib.orc_restir_pass(pass_kind, _ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(em, _c_f), _ptr(ei, _c_i),
+                        len(ei), _ptr(ap, _c_f), _ptr(ai, _c_i), float(scene["power_sum"]), _ptr(pm, _c_f), eval_fn,
+                        sample_fn, _ptr(si, _c_i), _ptr(sf, _c_f), _ptr(vp, _c_f), _ptr(gb, _c_f), _ptr(gbp, _c_f),
+                        _ptr(inp_, _c_f), _ptr(prev_, _c_f), _ptr(out, _c_f), spatial_index, spatial_seed, nthreads)
+    return out
+
+
 def emissive_power(soup, material_of, emission, emissive) -> np.ndarray:
     """Float power list of the emissive triangles, as the reference computes it
     (src/Renderer/GPURenderer.cpp:256-275)."""
