@@ -27,9 +27,9 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 10
     for n in names:
         assert hasattr(lib, n), n
-    from gbpt import bsdf, render
+    from gbpt import bsdf, guide, render
     bound = ({n for n, _, _ in _lib.SIGNATURES} | {n for n, _, _ in render.RENDER_SIGNATURES}
-             | {n for n, _, _ in bsdf.BSDF_SIGNATURES})
+             | {n for n, _, _ in bsdf.BSDF_SIGNATURES} | {n for n, _, _ in guide.GUIDE_SIGNATURES})
     assert bound == set(names)
 
 
@@ -75,3 +75,25 @@ def test_bsdf_entry_points_reject_bad_arguments():
     assert lib.gbpt_bsdf_eval(None, 0, None, None, 0, None, None, None) == 0
     assert lib.gbpt_bsdf_sample(None, 0, None, None, None, 5, None, None, None, None, None) == 1
     assert b"device pointers" in lib.gbpt_last_error()
+
+
+def test_guide_parameters_and_argument_checks():
+    """gbpt_guide_params matches its C layout; bad parameters are rejected before any device work."""
+    from gbpt import guide
+    assert ctypes.sizeof(guide.GuideParams) == 72
+    text = open(os.path.join(INCLUDE, "gbpt_guide.h")).read()
+    for name in ("LEVELS", "TABLE", "FEATURES", "IN", "HIDDEN", "OUT", "LOBES"):
+        m = re.search(rf"#define GBPT_GUIDE_{name} (\d+)", text)
+        assert m and int(m.group(1)) == getattr(guide, name), name
+    p = guide.default_params()
+    assert abs(p.learning_rate - 5e-3) < 1e-9 and p.max_batch == 1 << 18 and list(p.scene_max) == [1, 1, 1]
+    lib = guide._load()
+    h = ctypes.c_void_p()
+    bad = guide.default_params(max_batch=0)
+    assert lib.gbpt_guide_create(ctypes.byref(bad), ctypes.byref(h)) == 1 and not h.value
+    bad = guide.default_params(scene_min=(0, 2, 0))
+    assert lib.gbpt_guide_create(ctypes.byref(bad), ctypes.byref(h)) == 1
+    assert b"empty scene box" in lib.gbpt_last_error()
+    assert lib.gbpt_guide_train(None, None, None, None, None, 4, None, None) == 1
+    assert lib.gbpt_guide_infer(None, None, None, 4, None, None) == 1
+    assert lib.gbpt_guide_destroy(None) == 0
