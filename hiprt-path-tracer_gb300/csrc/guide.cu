@@ -47,6 +47,19 @@ constexpr size_t kSmemInfer = offsetof(Smem, dy);
 
 __device__ __forceinline__ int kmo(int r, int k, int K) { return umma::kmajor_offset(r, k, K); }
 
+__device__ __forceinline__ V3 load3(const float* __restrict__ a, int64_t row)
+{
+    return v3(a[3 * row], a[3 * row + 1], a[3 * row + 2]);
+}
+
+// rows in the batch: the device count when there is one (capped by n_max), else n_max
+__device__ __forceinline__ int64_t batch_size(const Batch& b)
+{
+    if (!b.count) return b.n_max;
+    const int64_t c = *b.count;
+    return c < 0 ? 0 : (c < b.n_max ? c : b.n_max);
+}
+
 __device__ __forceinline__ void copy_weights(Smem& sm, const uint16_t* packed)
 {
     const uint4* src = reinterpret_cast<const uint4*>(packed);
@@ -95,8 +108,8 @@ __device__ __forceinline__ void teardown(Smem& sm)
 
 // Forward of one tile up to the 48 raw outputs of this thread's row; h1/h2 keep the ReLU'd
 // activations in shared memory and m1/m2 their positivity bits. False if a wait gave up.
-__device__ bool forward_tile(Smem& sm, const Net& net, bool valid, V3 p, V3 n, float* raw, uint32_t* m1, uint32_t* m2,
-                             uint32_t& phase)
+__device__ bool forward_tile(Smem& sm, const Net& net, bool valid, V3 p, V3 n, V3 view, float* raw, uint32_t* m1,
+                             uint32_t* m2, uint32_t& phase)
 {
     const int t = threadIdx.x;
     {
@@ -106,7 +119,7 @@ __device__ bool forward_tile(Smem& sm, const Net& net, bool valid, V3 p, V3 n, f
             encode(d, net.params + kNumWeights, p, feat);
         else
             for (int i = 0; i < 16; i++) feat[i] = 0.0f;
-        input_row(feat, valid ? n : v3(0.0f), x);
+        input_row(feat, valid ? n : v3(0.0f), valid ? view : v3(0.0f), x);
         if (!valid) x[19] = 0.0f;
         for (int k = 0; k < kIn; k++) sm.x[kmo(t, k, kIn)] = __float2bfloat16(x[k]);
     }
@@ -154,11 +167,10 @@ __device__ __forceinline__ void accumulate_outer(float* out, const __nv_bfloat16
 // ---------------------------------------------------------------------------------------------
 // training: forward + loss + backward, persistent over tiles
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTile) train_kernel(Net net, const float* __restrict__ pos, const float* __restrict__ nrm,
-                                                      const float* __restrict__ dir, const float* __restrict__ weight,
-                                                      int64_t n, const float* __restrict__ weight_sum,
+__global__ void __launch_bounds__(kTile) train_kernel(Net net, Batch b, const float* __restrict__ weight_sum,
                                                       float* __restrict__ grads, float* __restrict__ loss, int* err)
 {
+    const int64_t n = batch_size(b);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
     const int t = threadIdx.x;
@@ -176,18 +188,19 @@ __global__ void __launch_bounds__(kTile) train_kernel(Net net, const float* __re
     {
         const int64_t row = tile * kTile + t;
         const bool valid = row < n;
-        V3 p = v3(0.0f), nn = v3(0.0f), w = v3(0.0f, 0.0f, 1.0f);
+        V3 p = v3(0.0f), nn = v3(0.0f), vw = v3(0.0f), w = v3(0.0f, 0.0f, 1.0f);
         float ws = 0.0f;
         if (valid)
         {
-            p = v3(pos[3 * row], pos[3 * row + 1], pos[3 * row + 2]);
-            nn = v3(nrm[3 * row], nrm[3 * row + 1], nrm[3 * row + 2]);
-            w = v3(dir[3 * row], dir[3 * row + 1], dir[3 * row + 2]);
-            ws = fmaxf(weight[row], 0.0f);
+            p = load3(b.pos, row);
+            nn = load3(b.nrm, row);
+            vw = load3(b.view, row);
+            w = load3(b.dir, row);
+            ws = fmaxf(b.weight[row], 0.0f);
         }
         float raw[kOut];
         uint32_t m1[2], m2[2];
-        ok = forward_tile(sm, net, valid, p, nn, raw, m1, m2, phase);
+        ok = forward_tile(sm, net, valid, p, nn, vw, raw, m1, m2, phase);
         if (!ok) break;
         // head, loss and its gradient for this row
         float draw[kOut];
@@ -236,9 +249,9 @@ __global__ void __launch_bounds__(kTile) train_kernel(Net net, const float* __re
 // ---------------------------------------------------------------------------------------------
 // inference: mixture per query (8 x (mu xyz, kappa, weight))
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTile) infer_kernel(Net net, const float* __restrict__ pos, const float* __restrict__ nrm,
-                                                      int64_t n, float* __restrict__ lobes_out, int* err)
+__global__ void __launch_bounds__(kTile) infer_kernel(Net net, Batch b, float* __restrict__ lobes_out, int* err)
 {
+    const int64_t n = batch_size(b);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
     const int t = threadIdx.x;
@@ -252,15 +265,16 @@ __global__ void __launch_bounds__(kTile) infer_kernel(Net net, const float* __re
     {
         const int64_t row = tile * kTile + t;
         const bool valid = row < n;
-        V3 p = v3(0.0f), nn = v3(0.0f);
+        V3 p = v3(0.0f), nn = v3(0.0f), vw = v3(0.0f);
         if (valid)
         {
-            p = v3(pos[3 * row], pos[3 * row + 1], pos[3 * row + 2]);
-            nn = v3(nrm[3 * row], nrm[3 * row + 1], nrm[3 * row + 2]);
+            p = load3(b.pos, row);
+            nn = load3(b.nrm, row);
+            vw = load3(b.view, row);
         }
         float raw[kOut];
         uint32_t m1[2], m2[2];
-        ok = forward_tile(sm, net, valid, p, nn, raw, m1, m2, phase);
+        ok = forward_tile(sm, net, valid, p, nn, vw, raw, m1, m2, phase);
         if (!ok) break;
         if (valid)
         {
@@ -356,8 +370,10 @@ __global__ void adam_kernel(float* __restrict__ params, const float* __restrict_
     }
 }
 
-__global__ void weight_sum_kernel(const float* __restrict__ w, int64_t n, float* __restrict__ out)
+__global__ void weight_sum_kernel(Batch b, float* __restrict__ out)
 {
+    const float* __restrict__ w = b.weight;
+    const int64_t n = batch_size(b);
     float acc = 0.0f;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         acc += fmaxf(w[i], 0.0f);
@@ -379,20 +395,19 @@ cudaError_t launch_guide_pack(const float* params, uint16_t* packed, cudaStream_
     return cudaGetLastError();
 }
 
-cudaError_t launch_guide_weight_sum(const float* weight, int64_t n, float* out_sum, cudaStream_t st)
+cudaError_t launch_guide_weight_sum(const Batch& b, float* out_sum, cudaStream_t st)
 {
     cudaError_t e = cudaMemsetAsync(out_sum, 0, sizeof(float), st);
     if (e != cudaSuccess) return e;
-    int64_t blocks = (n + 255) / 256;
+    int64_t blocks = (b.n_max + 255) / 256;
     if (blocks < 1) blocks = 1;
     if (blocks > 1024) blocks = 1024;
-    weight_sum_kernel<<<(int)blocks, 256, 0, st>>>(weight, n, out_sum);
+    weight_sum_kernel<<<(int)blocks, 256, 0, st>>>(b, out_sum);
     return cudaGetLastError();
 }
 
-cudaError_t launch_guide_train(const Net& net, const float* pos, const float* nrm, const float* dir, const float* weight,
-                               int64_t n, const float* weight_sum, float* grads, float* loss, int* err, int n_sm,
-                               cudaStream_t st)
+cudaError_t launch_guide_train(const Net& net, const Batch& b, const float* weight_sum, float* grads, float* loss, int* err,
+                               int n_sm, cudaStream_t st)
 {
     static bool attr_set = false;
     if (!attr_set)
@@ -401,14 +416,13 @@ cudaError_t launch_guide_train(const Net& net, const float* pos, const float* nr
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    const int64_t tiles = (n + kTile - 1) / kTile;
+    const int64_t tiles = (b.n_max + kTile - 1) / kTile;
     const int grid = (int)(tiles < n_sm ? (tiles < 1 ? 1 : tiles) : n_sm);
-    train_kernel<<<grid, kTile, kSmemTrain, st>>>(net, pos, nrm, dir, weight, n, weight_sum, grads, loss, err);
+    train_kernel<<<grid, kTile, kSmemTrain, st>>>(net, b, weight_sum, grads, loss, err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_guide_infer(const Net& net, const float* pos, const float* nrm, int64_t n, float* lobes, int* err,
-                               int n_sm, cudaStream_t st)
+cudaError_t launch_guide_infer(const Net& net, const Batch& b, float* lobes, int* err, int n_sm, cudaStream_t st)
 {
     static bool attr_set = false;
     if (!attr_set)
@@ -417,10 +431,10 @@ cudaError_t launch_guide_infer(const Net& net, const float* pos, const float* nr
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    const int64_t tiles = (n + kTile - 1) / kTile;
+    const int64_t tiles = (b.n_max + kTile - 1) / kTile;
     const int64_t cap = (int64_t)n_sm * 2;
     const int grid = (int)(tiles < cap ? (tiles < 1 ? 1 : tiles) : cap);
-    infer_kernel<<<grid, kTile, kSmemInfer, st>>>(net, pos, nrm, n, lobes, err);
+    infer_kernel<<<grid, kTile, kSmemInfer, st>>>(net, b, lobes, err);
     return cudaGetLastError();
 }
 

@@ -66,19 +66,40 @@ gbpt_status check_err(gbpt_guide* g, cudaStream_t cs)
     return GBPT_OK;
 }
 
-// forward + backward into g->grads (zeroed here); loss into g->scratch[1]
-gbpt_status compute_gradients(gbpt_guide* g, const float* pos, const float* nrm, const float* dir, const float* w,
-                              int64_t n, cudaStream_t cs)
+G::Batch host_batch(const float* pos, const float* nrm, const float* view, const float* dir, const float* w, int64_t n)
 {
-    if (n < 0 || n > g->p.max_batch) return set_error(GBPT_ERROR_INVALID_ARG, "n must be in 0..max_batch");
-    if (n > 0 && (!pos || !nrm || !dir || !w))
+    G::Batch b;
+    b.pos = pos;
+    b.nrm = nrm;
+    b.view = view;
+    b.dir = dir;
+    b.weight = w;
+    b.count = nullptr;
+    b.n_max = n;
+    return b;
+}
+
+// forward + backward into g->grads (zeroed here); loss into g->scratch[1]
+gbpt_status compute_gradients(gbpt_guide* g, const G::Batch& b, cudaStream_t cs)
+{
+    if (b.n_max < 0 || b.n_max > g->p.max_batch) return set_error(GBPT_ERROR_INVALID_ARG, "n must be in 0..max_batch");
+    if (b.n_max > 0 && (!b.pos || !b.nrm || !b.view || !b.dir || !b.weight))
         return set_error(GBPT_ERROR_INVALID_ARG, "training arrays must be device pointers");
     cudaError_t e = cudaMemsetAsync(g->grads, 0, sizeof(float) * G::kNumParams, cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(g->scratch + 1, 0, sizeof(float), cs);
-    if (e == cudaSuccess) e = G::launch_guide_weight_sum(w, n, g->scratch, cs);
-    if (e == cudaSuccess && n > 0)
-        e = G::launch_guide_train(net_of(g), pos, nrm, dir, w, n, g->scratch, g->grads, g->scratch + 1, g->err, g->n_sm, cs);
+    if (e == cudaSuccess) e = G::launch_guide_weight_sum(b, g->scratch, cs);
+    if (e == cudaSuccess && b.n_max > 0)
+        e = G::launch_guide_train(net_of(g), b, g->scratch, g->grads, g->scratch + 1, g->err, g->n_sm, cs);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide training launch");
+}
+
+gbpt_status adam_step(gbpt_guide* g, cudaStream_t cs)
+{
+    g->step++;
+    cudaError_t e = G::launch_guide_adam(g->params, g->grads, g->m, g->v, g->p.learning_rate, g->p.beta1, g->p.beta2,
+                                         g->p.epsilon, g->step, cs);
+    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, cs);
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide update");
 }
 
 }  // namespace
@@ -148,34 +169,31 @@ gbpt_status gbpt_guide_destroy(gbpt_guide* g)
     return GBPT_OK;
 }
 
-gbpt_status gbpt_guide_train(gbpt_guide* g, const float* position, const float* normal, const float* direction,
-                             const float* weight, int64_t n, float* loss, void* stream)
+gbpt_status gbpt_guide_train(gbpt_guide* g, const float* position, const float* normal, const float* view,
+                             const float* direction, const float* weight, int64_t n, float* loss, void* stream)
 {
     if (!g) return set_error(GBPT_ERROR_INVALID_ARG, "guide is NULL");
     cudaStream_t cs = (cudaStream_t)stream;
-    gbpt_status st = compute_gradients(g, position, normal, direction, weight, n, cs);
+    gbpt_status st = compute_gradients(g, host_batch(position, normal, view, direction, weight, n), cs);
     if (st != GBPT_OK) return st;
     if (loss)
     {
         cudaError_t e = cudaMemcpyAsync(loss, g->scratch + 1, sizeof(float), cudaMemcpyDeviceToHost, cs);
         if (e != cudaSuccess) return cuda_error(e, "loss read-back");
     }
-    g->step++;
-    cudaError_t e = G::launch_guide_adam(g->params, g->grads, g->m, g->v, g->p.learning_rate, g->p.beta1, g->p.beta2,
-                                         g->p.epsilon, g->step, cs);
-    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, cs);
-    if (e != cudaSuccess) return cuda_error(e, "guide update");
+    st = adam_step(g, cs);
+    if (st != GBPT_OK) return st;
     if (loss) return check_err(g, cs);
     return GBPT_OK;
 }
 
-gbpt_status gbpt_guide_gradients(gbpt_guide* g, const float* position, const float* normal, const float* direction,
-                                 const float* weight, int64_t n, float* grad_weights, float* grad_grid, float* loss,
-                                 void* stream)
+gbpt_status gbpt_guide_gradients(gbpt_guide* g, const float* position, const float* normal, const float* view,
+                                 const float* direction, const float* weight, int64_t n, float* grad_weights,
+                                 float* grad_grid, float* loss, void* stream)
 {
     if (!g) return set_error(GBPT_ERROR_INVALID_ARG, "guide is NULL");
     cudaStream_t cs = (cudaStream_t)stream;
-    gbpt_status st = compute_gradients(g, position, normal, direction, weight, n, cs);
+    gbpt_status st = compute_gradients(g, host_batch(position, normal, view, direction, weight, n), cs);
     if (st != GBPT_OK) return st;
     cudaError_t e = cudaSuccess;
     if (grad_weights)
@@ -188,15 +206,23 @@ gbpt_status gbpt_guide_gradients(gbpt_guide* g, const float* position, const flo
     return check_err(g, cs);
 }
 
-gbpt_status gbpt_guide_infer(gbpt_guide* g, const float* position, const float* normal, int64_t n, float* lobes,
-                             void* stream)
+gbpt_status gbpt_guide_infer(gbpt_guide* g, const float* position, const float* normal, const float* view, int64_t n,
+                             float* lobes, void* stream)
 {
     if (!g) return set_error(GBPT_ERROR_INVALID_ARG, "guide is NULL");
     if (n < 0) return set_error(GBPT_ERROR_INVALID_ARG, "n is negative");
     if (n == 0) return GBPT_OK;
-    if (!position || !normal || !lobes) return set_error(GBPT_ERROR_INVALID_ARG, "arrays must be device pointers");
-    cudaError_t e = G::launch_guide_infer(net_of(g), position, normal, n, lobes, g->err, g->n_sm, (cudaStream_t)stream);
+    if (!position || !normal || !view || !lobes) return set_error(GBPT_ERROR_INVALID_ARG, "arrays must be device pointers");
+    cudaError_t e = G::launch_guide_infer(net_of(g), host_batch(position, normal, view, nullptr, nullptr, n), lobes, g->err,
+                                          g->n_sm, (cudaStream_t)stream);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide inference launch");
+}
+
+gbpt_status gbpt_guide_error_flag(gbpt_guide* g, int32_t* flag)
+{
+    if (!g || !flag) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    cudaError_t e = cudaMemcpy(flag, g->err, sizeof(int), cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide status read-back");
 }
 
 gbpt_status gbpt_guide_get_params(gbpt_guide* g, float* weights, float* grid)
@@ -222,3 +248,25 @@ gbpt_status gbpt_guide_set_params(gbpt_guide* g, const float* weights, const flo
 }
 
 }  // extern "C"
+
+namespace gbpt {
+namespace guide {
+
+gbpt_status render_infer(gbpt_guide* g, const Batch& b, float* lobes, cudaStream_t cs)
+{
+    cudaError_t e = launch_guide_infer(net_of(g), b, lobes, g->err, g->n_sm, cs);
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide inference launch");
+}
+
+gbpt_status render_train(gbpt_guide* g, const Batch& b, cudaStream_t cs)
+{
+    Batch c = b;
+    if (c.n_max > g->p.max_batch) c.n_max = g->p.max_batch;
+    gbpt_status st = compute_gradients(g, c, cs);
+    return st == GBPT_OK ? adam_step(g, cs) : st;
+}
+
+int64_t max_batch(const gbpt_guide* g) { return g->p.max_batch; }
+
+}  // namespace guide
+}  // namespace gbpt

@@ -109,8 +109,9 @@ __device__ __forceinline__ void encode_backward(const Domain& d, float* __restri
     }
 }
 
-// Network input row: 16 grid features, the normal, a constant 1 (the bias input), zeros
-__device__ __forceinline__ void input_row(const float* feat, V3 n, float* x)
+// Network input row: 16 grid features, the normal, a constant 1 (the bias input), the direction
+// towards the viewer (outgoing direction of the shading point), zeros
+__device__ __forceinline__ void input_row(const float* feat, V3 n, V3 view, float* x)
 {
 #pragma unroll
     for (int i = 0; i < 16; i++) x[i] = feat[i];
@@ -118,8 +119,11 @@ __device__ __forceinline__ void input_row(const float* feat, V3 n, float* x)
     x[17] = n.y;
     x[18] = n.z;
     x[19] = 1.0f;
+    x[20] = view.x;
+    x[21] = view.y;
+    x[22] = view.z;
 #pragma unroll
-    for (int i = 20; i < kIn; i++) x[i] = 0.0f;
+    for (int i = 23; i < kIn; i++) x[i] = 0.0f;
 }
 
 __device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
@@ -203,29 +207,16 @@ __device__ __forceinline__ float head_backward(const float* raw, const Lobe* lob
     return logq;
 }
 
-// Samples a direction from the mixture with three uniforms (lobe choice, then Jakob's stable
-// vMF inversion around mu)
-__device__ __forceinline__ V3 sample_mixture(const Lobe* lobes, float u0, float u1, float u2)
+// Samples a vMF lobe with two uniforms (Jakob's numerically stable inversion of the cosine to
+// the mean, "Numerically stable sampling of the von Mises Fisher distribution on S2", 2012)
+__device__ __forceinline__ V3 sample_vmf(V3 mu, float k, float u1, float u2)
 {
-    int pick = kLobes - 1;
-    float acc = 0.0f;
-    for (int i = 0; i < kLobes; i++)
-    {
-        acc += lobes[i].weight;
-        if (u0 < acc)
-        {
-            pick = i;
-            break;
-        }
-    }
-    const Lobe& L = lobes[pick];
-    const float k = L.kappa;
     const float wz = fminf(1.0f, fmaxf(-1.0f, 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * k)) / k));
     const float r = sqrtf(fmaxf(0.0f, 1.0f - wz * wz));
     float sn, cs;
     sincosf(kTwoPi * u2, &sn, &cs);
     // frame around mu (Frisvad / Max)
-    const V3 n = L.mu;
+    const V3 n = mu;
     V3 t, b;
     if (n.z < -0.99998796f)
     {
@@ -239,6 +230,55 @@ __device__ __forceinline__ V3 sample_mixture(const Lobe* lobes, float u0, float 
         b = v3(t.y, 1.0f - n.y * n.y / (1.0f + n.z), -n.y);
     }
     return normalize(t * (r * cs) + b * (r * sn) + n * wz);
+}
+
+// Samples a direction from the mixture with three uniforms: the lobe by u0, then the lobe's vMF
+__device__ __forceinline__ V3 sample_mixture(const Lobe* lobes, float u0, float u1, float u2)
+{
+    int pick = kLobes - 1;
+    float acc = 0.0f;
+    for (int i = 0; i < kLobes; i++)
+    {
+        acc += lobes[i].weight;
+        if (u0 < acc)
+        {
+            pick = i;
+            break;
+        }
+    }
+    return sample_vmf(lobes[pick].mu, lobes[pick].kappa, u1, u2);
+}
+
+// Mixture read from global memory one lobe at a time (the path tracer's per-entry lobes,
+// 8 x (mu xyz, kappa, weight)); keeps the 40 values out of registers.
+__device__ __forceinline__ float mixture_pdf_at(const float* __restrict__ L, V3 w)
+{
+    float q = 0.0f;
+#pragma unroll 2
+    for (int i = 0; i < kLobes; i++)
+    {
+        const float* l = L + 5 * i;
+        const float wt = __ldg(l + 4);
+        if (wt > 0.0f) q += wt * expf(log_vmf(__ldg(l + 3), dot(v3(__ldg(l), __ldg(l + 1), __ldg(l + 2)), w)));
+    }
+    return q;
+}
+
+__device__ __forceinline__ V3 sample_mixture_at(const float* __restrict__ L, float u0, float u1, float u2)
+{
+    int pick = kLobes - 1;
+    float acc = 0.0f;
+    for (int i = 0; i < kLobes; i++)
+    {
+        acc += __ldg(L + 5 * i + 4);
+        if (u0 < acc)
+        {
+            pick = i;
+            break;
+        }
+    }
+    const float* l = L + 5 * pick;
+    return sample_vmf(v3(__ldg(l), __ldg(l + 1), __ldg(l + 2)), __ldg(l + 3), u1, u2);
 }
 
 }  // namespace guide

@@ -27,18 +27,37 @@ struct Net
     float lo[3], inv_ext[3];        // hash-grid domain
 };
 
+// A batch of rows: SoA position / normal / view / direction (3 floats per row) and weight;
+// the kernels process min(*count, n_max) rows when count is given (a device-side queue
+// counter), else n_max rows. view points from the shading point towards the viewer.
+struct Batch
+{
+    const float* pos;
+    const float* nrm;
+    const float* view;
+    const float* dir;     // training only
+    const float* weight;  // training only
+    const int32_t* count;
+    int64_t n_max;
+};
+
 cudaError_t launch_guide_init(float* params, uint32_t seed, cudaStream_t st);
 cudaError_t launch_guide_pack(const float* params, uint16_t* packed, cudaStream_t st);
-cudaError_t launch_guide_weight_sum(const float* weight, int64_t n, float* out_sum, cudaStream_t st);
-// Forward + loss + backward over n samples; accumulates into grads (FP32, zeroed by the caller)
+cudaError_t launch_guide_weight_sum(const Batch& b, float* out_sum, cudaStream_t st);
+// Forward + loss + backward over the batch; accumulates into grads (FP32, zeroed by the caller)
 // and *loss; *err set to 1 if a tensor-core wait gave up.
-cudaError_t launch_guide_train(const Net& net, const float* pos, const float* nrm, const float* dir, const float* weight,
-                               int64_t n, const float* weight_sum, float* grads, float* loss, int* err, int n_sm,
-                               cudaStream_t st);
-cudaError_t launch_guide_infer(const Net& net, const float* pos, const float* nrm, int64_t n, float* lobes, int* err,
+cudaError_t launch_guide_train(const Net& net, const Batch& b, const float* weight_sum, float* grads, float* loss, int* err,
                                int n_sm, cudaStream_t st);
+// Mixture per row: lobes[40 row + 5 i ..] = lobe i (mu xyz, kappa, weight)
+cudaError_t launch_guide_infer(const Net& net, const Batch& b, float* lobes, int* err, int n_sm, cudaStream_t st);
 cudaError_t launch_guide_adam(float* params, const float* grads, float* m, float* v, float lr, float beta1, float beta2,
                               float eps, int step, cudaStream_t st);
+
+// Entry points for the path tracer (guide_api.cpp): inference over a wavefront queue and one
+// training step (gradients + Adam) on the frame's records, both reading device-side counts.
+gbpt_status render_infer(gbpt_guide* g, const Batch& b, float* lobes, cudaStream_t cs);
+gbpt_status render_train(gbpt_guide* g, const Batch& b, cudaStream_t cs);
+int64_t max_batch(const gbpt_guide* g);
 
 }  // namespace guide
 }  // namespace gbpt

@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "render_common.h"
+#include "guide_device.h"
 #include "principled.h"
 #include "render_device.h"
 #include "render_kernels.h"
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(128) trace_queue_kernel(const uint4* __restric
 template <bool PRINCIPLED>
 __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue next,
                                                     Queue shadow, Queue bsdfq, int bounce, unsigned long long* stats,
-                                                    ReservoirBuf restir)
+                                                    ReservoirBuf restir, GuideView gv)
 {
     const int n = *in.count;
     // iterate in whole warps so that the warp-aggregated appends see converged lanes
@@ -107,10 +108,12 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
             prim = __float_as_int(hit.w);
             pb.shadow_entry[slot] = -1;
             pb.bsdf_entry[slot] = -1;
+            if (gv.train_entry) gv.train_entry[slot] = -1;
         }
         const bool alive = valid && prim >= 0;
 
-        bool want_shadow = false, want_bsdf = false, want_next = false;
+        bool want_shadow = false, want_bsdf = false, want_next = false, want_record = false;
+        V3 rec_tp = v3(0.0f), rec_dir = v3(0.0f);
         float4 sh_o, sh_d, bs_d, nx_d;
         V3 P = v3(0, 0, 0), tp = v3(0, 0, 0);
         V3 light_contrib = v3(0, 0, 0);
@@ -187,13 +190,35 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                     }
                 }
 
-                // ---- continuation (PathTracing.h:81-101, RussianRoulette.h:20-55) ----
+                // ---- continuation (PathTracing.h:81-101, RussianRoulette.h:20-55); with guiding,
+                // one-sample MIS of the learned mixture and cosine sampling ----
                 if (bounce < rc.nb_bounces)
                 {
-                    const float r1 = rng.next(), r2 = rng.next();
-                    const V3 wi = cosine_sample(ns, r1, r2);
+                    const float* GL = gv.lobes ? gv.lobes + 40 * (int64_t)i : nullptr;
+                    V3 wi, f;
                     float pdf;
-                    const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
+                    if (GL)
+                    {
+                        if (rng.next() < gv.prob)
+                        {
+                            const float u0 = rng.next(), u1 = rng.next(), u2 = rng.next();
+                            wi = guide::sample_mixture_at(GL, u0, u1, u2);
+                        }
+                        else
+                        {
+                            const float r1 = rng.next(), r2 = rng.next();
+                            wi = cosine_sample(ns, r1, r2);
+                        }
+                        float p_bsdf;
+                        f = lambert_eval(albedo, dot(ns, wi), p_bsdf);
+                        pdf = is_black(f) ? 0.0f : gv.prob * guide::mixture_pdf_at(GL, wi) + (1.0f - gv.prob) * p_bsdf;
+                    }
+                    else
+                    {
+                        const float r1 = rng.next(), r2 = rng.next();
+                        wi = cosine_sample(ns, r1, r2);
+                        f = lambert_eval(albedo, dot(ns, wi), pdf);
+                    }
                     if (pdf > 0.0f)
                     {
                         const V3 atten = f * fabsf(dot(wi, ns)) / pdf;
@@ -213,6 +238,10 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                         }
                         if (survive)
                         {
+                            want_record = GL && gv.train_entry &&
+                                          record_hash((uint32_t)slot, (uint32_t)bounce, gv.frame) < gv.rec_threshold;
+                            rec_tp = tp;
+                            rec_dir = wi;
                             t2 = t2 * atten;
                             t2 = v3(fmaxf(t2.x, 1.0e-5f), fmaxf(t2.y, 1.0e-5f), fmaxf(t2.z, 1.0e-5f));
                             tp = t2;
@@ -330,14 +359,42 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                     }
                 }
 
-                // ---- continuation ----
+                // ---- continuation; with guiding (materials without delta lobes or transmission),
+                // one-sample MIS of the learned mixture and BSDF sampling ----
                 if (bounce < rc.nb_bounces)
                 {
-                    bsdf::Xorshift32 xr = bsdf_rng(rng);
-                    V3 wi;
-                    int lobe;
+                    const float* GL = (gv.lobes && guidable(m)) ? gv.lobes + 40 * (int64_t)i : nullptr;
+                    V3 wi, f;
+                    int lobe = GBPT_LOBE_NONE;
                     float pdf;
-                    const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                    if (GL)
+                    {
+                        float p_bsdf;
+                        if (rng.next() < gv.prob)
+                        {
+                            const float u0 = rng.next(), u1 = rng.next(), u2 = rng.next();
+                            wi = guide::sample_mixture_at(GL, u0, u1, u2);
+                            bsdf::Query q;
+                            q.view = view;
+                            q.ns = ns;
+                            q.ng = ng;
+                            q.light = wi;
+                            // directions below the geometric surface carry no BSDF value, as in BSDF sampling
+                            f = dot(wi, ng) < 0.0f ? v3(0.0f) : bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, p_bsdf);
+                            if (dot(wi, ng) < 0.0f) p_bsdf = 0.0f;
+                        }
+                        else
+                        {
+                            bsdf::Xorshift32 xr = bsdf_rng(rng);
+                            f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, p_bsdf);
+                        }
+                        pdf = is_black(f) ? 0.0f : gv.prob * guide::mixture_pdf_at(GL, wi) + (1.0f - gv.prob) * p_bsdf;
+                    }
+                    else
+                    {
+                        bsdf::Xorshift32 xr = bsdf_rng(rng);
+                        f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                    }
                     if (pdf > 0.0f)
                     {
                         const V3 atten = f * fabsf(dot(wi, ns)) / pdf;
@@ -357,6 +414,10 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                         }
                         if (survive)
                         {
+                            want_record = GL && gv.train_entry &&
+                                          record_hash((uint32_t)slot, (uint32_t)bounce, gv.frame) < gv.rec_threshold;
+                            rec_tp = tp;
+                            rec_dir = wi;
                             t2 = t2 * atten;
                             t2 = v3(fmaxf(t2.x, 1.0e-5f), fmaxf(t2.y, 1.0e-5f), fmaxf(t2.z, 1.0e-5f));
                             tp = t2;
@@ -406,6 +467,25 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
             pb.throughput[slot] = f4(tp, 0.0f);
             if (PRINCIPLED) pb.medium[slot] = next_medium;
         }
+        if (gv.train_entry)  // uniform: every lane of the warp takes the branch
+        {
+            const int ri = warp_append(gv.rec_count, want_record);
+            if (want_record && ri < gv.rec_cap)
+            {
+                for (int a = 0; a < 3; a++)
+                {
+                    gv.rec_pos[3 * ri + a] = gv.in_pos[3 * (int64_t)i + a];
+                    gv.rec_nrm[3 * ri + a] = gv.in_nrm[3 * (int64_t)i + a];
+                    gv.rec_view[3 * ri + a] = gv.in_view[3 * (int64_t)i + a];
+                }
+                gv.rec_dir[3 * ri] = rec_dir.x;
+                gv.rec_dir[3 * ri + 1] = rec_dir.y;
+                gv.rec_dir[3 * ri + 2] = rec_dir.z;
+                gv.rec_tp[ri] = f4(rec_tp, 0.0f);
+                gv.rec_slot[ri] = slot;
+                gv.train_entry[slot] = ri;
+            }
+        }
         warp_count(stats + 1, want_shadow);
         warp_count(stats + 2, want_bsdf);
         warp_count(stats + 0, want_next);
@@ -416,7 +496,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
 // resolve: add the light-sample and BSDF-sample contributions of this bounce, in a fixed order
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue shadow,
-                                                      Queue bsdfq)
+                                                      Queue bsdfq, GuideView gv)
 {
     const int n = *in.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -424,7 +504,13 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst r
         const int slot = in.slot[i];
         const int se = pb.shadow_entry[slot];
         const int be = pb.bsdf_entry[slot];
-        if (se < 0 && be < 0) continue;
+        // a guiding record of this vertex snapshots the radiance after its direct lighting
+        const int te = gv.train_entry ? gv.train_entry[slot] : -1;
+        if (se < 0 && be < 0)
+        {
+            if (te >= 0) gv.rec_snap[te] = pb.radiance[slot];
+            continue;
+        }
         V3 add = v3(0, 0, 0);
         if (se >= 0 && !shadow.occluded[se]) add = add + xyz(pb.pending_light[slot]);
         if (be >= 0)
@@ -460,7 +546,61 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst r
             }
         }
         const float4 r = pb.radiance[slot];
-        pb.radiance[slot] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
+        const float4 nr = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
+        pb.radiance[slot] = nr;
+        if (te >= 0) gv.rec_snap[te] = nr;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// guiding: network inputs per queue entry (shading position, normal facing the viewer, view
+// direction) and, after the launch, the weights of the training records
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) guide_inputs_kernel(SceneView s, Queue in, GuideView gv)
+{
+    const int n = *in.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const float4 hit = in.hits[i];
+        const int prim = __float_as_int(hit.w);
+        V3 P = v3(0.0f), ng = v3(0.0f), view = v3(0.0f);
+        if (prim >= 0)
+        {
+            const V3 d = xyz(in.dir_tmax[i]);
+            P = xyz(in.origin_tmin[i]) + hit.x * d;
+            V3 a, b, c;
+            load_triangle(s, prim, a, b, c);
+            ng = normalize(cross(b - a, c - a));
+            view = -d;
+            if (dot(view, ng) < 0.0f) ng = -ng;
+        }
+        const int64_t o = 3 * (int64_t)i;
+        gv.in_pos[o] = P.x;
+        gv.in_pos[o + 1] = P.y;
+        gv.in_pos[o + 2] = P.z;
+        gv.in_nrm[o] = ng.x;
+        gv.in_nrm[o + 1] = ng.y;
+        gv.in_nrm[o + 2] = ng.z;
+        gv.in_view[o] = view.x;
+        gv.in_view[o + 1] = view.y;
+        gv.in_view[o + 2] = view.z;
+    }
+}
+
+__global__ void guide_weights_kernel(PathBuffers pb, GuideView gv)
+{
+    const int n = min(*gv.rec_count, gv.rec_cap);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    {
+        const V3 R = xyz(pb.radiance[gv.rec_slot[r]]);
+        const V3 S = xyz(gv.rec_snap[r]);
+        const V3 T = xyz(gv.rec_tp[r]);
+        const V3 ratio = v3(T.x > 0.0f ? fmaxf(R.x - S.x, 0.0f) / T.x : 0.0f, T.y > 0.0f ? fmaxf(R.y - S.y, 0.0f) / T.y : 0.0f,
+                            T.z > 0.0f ? fmaxf(R.z - S.z, 0.0f) / T.z : 0.0f);
+        float w = luminance(ratio);
+        if (!(w >= 0.0f)) w = 0.0f;  // NaN
+        if (gv.weight_clamp > 0.0f) w = fminf(w, gv.weight_clamp);
+        gv.rec_weight[r] = w;
     }
 }
 
@@ -658,16 +798,30 @@ cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next
 
 cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
                          const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
-                         unsigned long long* stats, const ReservoirBuf& restir, int n_sm, cudaStream_t st)
+                         unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv, int n_sm,
+                         cudaStream_t st)
 {
     const int tgrid = grid_for(capacity, 128, n_sm * 16);
     if (rc.bsdf == GBPT_BSDF_PRINCIPLED)
-        shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir);
+        shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv);
     else
-        shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir);
+        shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv);
     trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, shadow);
     trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, bsdfq);
-    resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq);
+    resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq, gv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_guide_inputs(const SceneView& s, const Queue& in, const GuideView& gv, int64_t capacity, int n_sm,
+                                cudaStream_t st)
+{
+    guide_inputs_kernel<<<grid_for(capacity, 128, n_sm * 16), 128, 0, st>>>(s, in, gv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_guide_weights(const PathBuffers& pb, const GuideView& gv, int n_sm, cudaStream_t st)
+{
+    guide_weights_kernel<<<grid_for(gv.rec_cap, 256, n_sm * 8), 256, 0, st>>>(pb, gv);
     return cudaGetLastError();
 }
 

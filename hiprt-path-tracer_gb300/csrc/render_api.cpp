@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/gbpt_render.h"
+#include "guide_kernels.h"
 #include "handles.h"
 #include "render_common.h"
 #include "render_kernels.h"
@@ -44,6 +45,7 @@ struct DevMem
     {
         for (void* p : ptrs) cudaFree(p);
         ptrs.clear();
+        err = cudaSuccess;
     }
 };
 
@@ -92,6 +94,12 @@ struct gbpt_renderer
     int res_final = 0;
     bool has_prev = false;
     float prev_inverse_view[16];
+    // learned path guiding
+    gbpt_guide* guide = nullptr;
+    gbpt_guide_render_settings guide_settings;
+    DevMem guide_mem;
+    gbpt::GuideView gv;  // gv.lobes == nullptr: off
+    float* guide_lobes = nullptr;
 };
 
 namespace {
@@ -437,6 +445,7 @@ gbpt_status gbpt_renderer_destroy(gbpt_renderer* r)
 {
     if (!r) return GBPT_OK;
     r->restir_mem.release();
+    r->guide_mem.release();
     r->mem.release();
     delete r;
     return GBPT_OK;
@@ -461,6 +470,8 @@ gbpt_status gbpt_pass_camera_rays(gbpt_renderer* r, void* stream)
     r->cur = 0;
     cudaError_t e = gbpt::launch_camera(r->rc, r->pb, r->q[0], (int32_t)r->iteration, r->stats, r->n_sm,
                                         (cudaStream_t)stream);
+    if (e == cudaSuccess && r->gv.rec_count) e = cudaMemsetAsync(r->gv.rec_count, 0, sizeof(int32_t), (cudaStream_t)stream);
+    r->gv.frame = (uint32_t)r->iteration;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "camera rays");
 }
 
@@ -479,8 +490,27 @@ gbpt_status gbpt_pass_shade(gbpt_renderer* r, int32_t bounce, void* stream)
     if (bounce < 0 || bounce > r->rc.nb_bounces) return set_error(GBPT_ERROR_INVALID_ARG, "bounce out of range");
     gbpt::ReservoirBuf none = {nullptr, nullptr};
     const gbpt::ReservoirBuf& restir = (r->restir && bounce == 0) ? r->res[r->res_final] : none;
-    cudaError_t e = gbpt::launch_shade(r->scene->view, r->rc, r->pb, r->q[r->cur], r->q[r->cur ^ 1], r->shadow, r->bsdfq,
-                                       bounce, r->capacity, r->stats, restir, r->n_sm, (cudaStream_t)stream);
+    cudaStream_t cs = (cudaStream_t)stream;
+    const gbpt::Queue& in = r->q[r->cur];
+    gbpt::GuideView gv = r->gv;
+    if (bounce >= r->rc.nb_bounces) gv.lobes = nullptr;  // no continuation at the last bounce
+    if (gv.lobes)
+    {
+        // network inputs and mixture for every entry of the shaded queue (count read on the device)
+        cudaError_t e = gbpt::launch_guide_inputs(r->scene->view, in, gv, r->capacity, r->n_sm, cs);
+        if (e != cudaSuccess) return cuda_error(e, "guide inputs");
+        gbpt::guide::Batch b;
+        std::memset(&b, 0, sizeof(b));
+        b.pos = gv.in_pos;
+        b.nrm = gv.in_nrm;
+        b.view = gv.in_view;
+        b.count = in.count;
+        b.n_max = r->capacity;
+        gbpt_status st = gbpt::guide::render_infer(r->guide, b, r->guide_lobes, cs);
+        if (st != GBPT_OK) return st;
+    }
+    cudaError_t e = gbpt::launch_shade(r->scene->view, r->rc, r->pb, in, r->q[r->cur ^ 1], r->shadow, r->bsdfq, bounce,
+                                       r->capacity, r->stats, restir, gv, r->n_sm, cs);
     r->cur ^= 1;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "shade");
 }
@@ -690,6 +720,24 @@ gbpt_status gbpt_pass_accumulate(gbpt_renderer* r, void* stream)
     if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
     cudaError_t e = gbpt::launch_accumulate(r->rc, r->pb, r->acc32, r->acc64, r->n_sm, (cudaStream_t)stream);
     if (e == cudaSuccess && r->restir) e = restir_end_frame(r, (cudaStream_t)stream);
+    if (e == cudaSuccess && r->gv.train_entry)
+    {
+        // one training step on this launch's guiding records
+        e = gbpt::launch_guide_weights(r->pb, r->gv, r->n_sm, (cudaStream_t)stream);
+        if (e == cudaSuccess)
+        {
+            gbpt::guide::Batch b;
+            b.pos = r->gv.rec_pos;
+            b.nrm = r->gv.rec_nrm;
+            b.view = r->gv.rec_view;
+            b.dir = r->gv.rec_dir;
+            b.weight = r->gv.rec_weight;
+            b.count = r->gv.rec_count;
+            b.n_max = r->gv.rec_cap;
+            gbpt_status st = gbpt::guide::render_train(r->guide, b, (cudaStream_t)stream);
+            if (st != GBPT_OK) return st;
+        }
+    }
     r->iteration += r->rc.spp;
     r->samples += r->rc.spp;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "accumulate");
@@ -804,6 +852,112 @@ gbpt_status gbpt_renderer_get_stats(gbpt_renderer* r, gbpt_render_stats* out, vo
     out->extension_rays = (int64_t)h[0];
     out->shadow_rays = (int64_t)h[1];
     out->bsdf_light_rays = (int64_t)h[2];
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_guide_render_default_settings(gbpt_guide_render_settings* s)
+{
+    if (!s) return set_error(GBPT_ERROR_INVALID_ARG, "settings is NULL");
+    std::memset(s, 0, sizeof(*s));
+    s->enabled = 1;
+    s->train = 1;
+    s->guide_probability = 0.5f;
+    s->max_records = 65536;
+    s->weight_clamp = 50.0f;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_guide_render_settings* s)
+{
+    if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
+    r->guide_mem.release();
+    std::memset(&r->gv, 0, sizeof(r->gv));
+    r->guide = nullptr;
+    r->guide_lobes = nullptr;
+    if (!g || !s || !s->enabled) return GBPT_OK;
+    if (!(s->guide_probability > 0.0f && s->guide_probability < 1.0f))
+        return set_error(GBPT_ERROR_INVALID_ARG, "guide_probability must be in (0, 1)");
+    if (s->train && (s->max_records < 1 || s->max_records > gbpt::guide::max_batch(g)))
+        return set_error(GBPT_ERROR_INVALID_ARG, "max_records must be in 1..the guide's max_batch");
+    if (s->weight_clamp < 0.0f) return set_error(GBPT_ERROR_INVALID_ARG, "weight_clamp is negative");
+    const int64_t cap = r->capacity;
+    DevMem& M = r->guide_mem;
+    gbpt::GuideView& gv = r->gv;
+    gv.in_pos = M.alloc<float>(3 * cap);
+    gv.in_nrm = M.alloc<float>(3 * cap);
+    gv.in_view = M.alloc<float>(3 * cap);
+    r->guide_lobes = M.alloc<float>(40 * cap);
+    gv.prob = s->guide_probability;
+    if (s->train)
+    {
+        const int64_t nr = s->max_records;
+        gv.train_entry = M.alloc<int32_t>(cap);
+        gv.rec_pos = M.alloc<float>(3 * nr);
+        gv.rec_nrm = M.alloc<float>(3 * nr);
+        gv.rec_view = M.alloc<float>(3 * nr);
+        gv.rec_dir = M.alloc<float>(3 * nr);
+        gv.rec_tp = M.alloc<float4>(nr);
+        gv.rec_snap = M.alloc<float4>(nr);
+        gv.rec_weight = M.alloc<float>(nr);
+        gv.rec_slot = M.alloc<int32_t>(nr);
+        gv.rec_count = M.alloc<int32_t>(1);
+        gv.rec_cap = s->max_records;
+        // expected vertices with a continuation per launch: paths x bounces (an upper estimate)
+        const double expected = (double)cap * (r->rc.nb_bounces > 0 ? r->rc.nb_bounces : 1);
+        const double frac = std::min(1.0, (double)s->max_records / expected);
+        gv.rec_threshold = frac >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(frac * 4294967296.0);
+        gv.weight_clamp = s->weight_clamp;
+    }
+    cudaError_t e = M.err;
+    if (e == cudaSuccess && gv.rec_count) e = cudaMemset(gv.rec_count, 0, sizeof(int32_t));
+    if (e != cudaSuccess)
+    {
+        M.release();
+        std::memset(&r->gv, 0, sizeof(r->gv));
+        r->guide_lobes = nullptr;
+        return e == cudaErrorMemoryAllocation ? set_error(GBPT_ERROR_OOM, "guiding buffers") : cuda_error(e, "guiding buffers");
+    }
+    gv.lobes = r->guide_lobes;
+    r->guide = g;
+    r->guide_settings = *s;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_renderer_get_guide_records(gbpt_renderer* r, float* host_out, int32_t capacity, int32_t* count,
+                                            void* stream)
+{
+    if (!r || !count) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    if (!r->gv.rec_count) return set_error(GBPT_ERROR_INVALID_ARG, "no guide with training attached");
+    cudaStream_t cs = (cudaStream_t)stream;
+    int32_t n = 0;
+    cudaError_t e = cudaMemcpyAsync(&n, r->gv.rec_count, sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) return cuda_error(e, "record count read-back");
+    *count = n;
+    const int64_t k = std::min<int64_t>(std::min<int64_t>(n, r->gv.rec_cap), capacity > 0 ? capacity : 0);
+    if (!host_out || k == 0) return GBPT_OK;
+    std::vector<float> p(3 * k), nr(3 * k), v(3 * k), d(3 * k), w(k);
+    std::vector<int32_t> sl(k);
+    e = cudaMemcpy(p.data(), r->gv.rec_pos, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(nr.data(), r->gv.rec_nrm, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(v.data(), r->gv.rec_view, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(d.data(), r->gv.rec_dir, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(w.data(), r->gv.rec_weight, k * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(sl.data(), r->gv.rec_slot, k * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "record read-back");
+    for (int64_t i = 0; i < k; i++)
+    {
+        float* o = host_out + 14 * i;
+        for (int a = 0; a < 3; a++)
+        {
+            o[a] = p[3 * i + a];
+            o[3 + a] = nr[3 * i + a];
+            o[6 + a] = v[3 * i + a];
+            o[9 + a] = d[3 * i + a];
+        }
+        o[12] = w[i];
+        std::memcpy(o + 13, &sl[i], sizeof(int32_t));
+    }
     return GBPT_OK;
 }
 

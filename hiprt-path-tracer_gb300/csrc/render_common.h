@@ -68,6 +68,36 @@ struct PathBuffers
     int32_t* medium;        // material index of the volume the path travels in, -1 = air
 };
 
+// Learned path guiding in the wavefront (all device pointers; lobes == nullptr: guiding off).
+// The continuation of a guidable vertex is drawn from the network's vMF mixture with probability
+// 'prob', else from the BSDF, and weighted by the one-sample MIS pdf prob q + (1 - prob) p_bsdf.
+// Training records hold (position, normal, view, sampled direction), the throughput before the
+// continuation and the path radiance after this vertex's direct lighting; after the launch the
+// record's weight is luminance((final radiance - snapshot) / throughput), the estimate of
+// f cos L_i / pdf of the sampled direction.
+struct GuideView
+{
+    const float* lobes;  // per entry of the shaded queue: 8 x (mu xyz, kappa, weight)
+    float* in_pos;       // per queue entry: network inputs (3 floats each)
+    float* in_nrm;
+    float* in_view;
+    float prob;
+    int32_t* train_entry;  // per path slot: record made at this bounce, -1 (null: no training)
+    float* rec_pos;        // per record: 3 floats each
+    float* rec_nrm;
+    float* rec_view;
+    float* rec_dir;
+    float4* rec_tp;
+    float4* rec_snap;
+    float* rec_weight;
+    int32_t* rec_slot;
+    int32_t* rec_count;
+    int32_t rec_cap;
+    uint32_t rec_threshold;  // a vertex is recorded when its hash is below this
+    uint32_t frame;
+    float weight_clamp;      // 0: none
+};
+
 #ifdef __CUDACC__
 // ---------------------------------------------------------------------------------------------
 // small vector helpers (the float3 type and operators shared with the BSDF live in hd_math.h)

@@ -126,4 +126,28 @@ __device__ __forceinline__ bool can_light_sample(const bsdf::Material& m)
     return !(smooth_base && smooth_coat && smooth_second);
 }
 
+// Guided sampling applies to materials whose BSDF has no delta lobe and no transmission: every
+// lobe then has a density that the one-sample MIS with the learned mixture can use.
+__device__ __forceinline__ bool guidable(const bsdf::Material& m)
+{
+    if (m.transmission > 0.0f || m.diffuse_transmission > 0.0f) return false;
+    if (bsdf::is_smooth(m.roughness) && (m.metallic > 0.0f || m.specular > 0.0f)) return false;
+    if (m.coat > 0.0f && bsdf::is_smooth(m.coat_roughness)) return false;
+    if (m.metallic > 0.0f && m.second_weight > 0.0f && bsdf::is_smooth(m.second_roughness)) return false;
+    return true;
+}
+
+// Hash deciding which path vertices become guiding training records (independent of the path's
+// random numbers, so recording never changes the rendered image)
+__device__ __forceinline__ uint32_t record_hash(uint32_t slot, uint32_t bounce, uint32_t frame)
+{
+    uint32_t h = slot * 0x9E3779B1u ^ (bounce * 0x85EBCA77u + frame * 0xC2B2AE3Du + 0x27D4EB2Fu);
+    h ^= h >> 16;
+    h *= 0x7FEB352Du;
+    h ^= h >> 15;
+    h *= 0x846CA68Bu;
+    h ^= h >> 16;
+    return h;
+}
+
 }  // namespace gbpt

@@ -11,6 +11,7 @@ namespace gbpt {
 struct SceneView;
 struct Queue;
 struct PathBuffers;
+struct GuideView;
 
 // Per-render constants, passed by value to every kernel.
 struct RenderConst
@@ -43,9 +44,17 @@ cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Qu
 // that replace next-event estimation at bounce 0.
 cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next, const Queue& shadow,
                           const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st);
+// 'gv' (null lobes when guiding is off) holds the learned mixture per entry of 'in' and the
+// training-record buffers.
 cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
                          const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
-                         unsigned long long* stats, const ReservoirBuf& restir, int n_sm, cudaStream_t st);
+                         unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv, int n_sm,
+                         cudaStream_t st);
+// Guiding network inputs for each entry of 'in' (after its closest hits are known)
+cudaError_t launch_guide_inputs(const SceneView& s, const Queue& in, const GuideView& gv, int64_t capacity, int n_sm,
+                                cudaStream_t st);
+// Training-record weights from the final path radiance (after the launch's last bounce)
+cudaError_t launch_guide_weights(const PathBuffers& pb, const GuideView& gv, int n_sm, cudaStream_t st);
 cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int n_sm,
                                   cudaStream_t st);
 cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,

@@ -34,9 +34,10 @@ GUIDE_SIGNATURES = [
     ("gbpt_guide_default_params", ctypes.c_int, [ctypes.POINTER(GuideParams)]),
     ("gbpt_guide_create", ctypes.c_int, [ctypes.POINTER(GuideParams), ctypes.POINTER(c_vp)]),
     ("gbpt_guide_destroy", ctypes.c_int, [c_vp]),
-    ("gbpt_guide_train", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_vp]),
-    ("gbpt_guide_gradients", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_f, c_f, c_vp]),
-    ("gbpt_guide_infer", ctypes.c_int, [c_vp, c_vp, c_vp, i64, c_vp, c_vp]),
+    ("gbpt_guide_train", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_vp]),
+    ("gbpt_guide_gradients", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_f, c_f, c_vp]),
+    ("gbpt_guide_infer", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, c_vp, c_vp]),
+    ("gbpt_guide_error_flag", ctypes.c_int, [c_vp, ctypes.POINTER(i32)]),
     ("gbpt_guide_get_params", ctypes.c_int, [c_vp, c_f, c_f]),
     ("gbpt_guide_set_params", ctypes.c_int, [c_vp, c_f, c_f]),
 ]
@@ -107,34 +108,43 @@ class Guide:
     def handle(self):
         return self._h
 
-    def train(self, position, normal, direction, weight, want_loss=True, stream=None):
+    def train(self, position, normal, view, direction, weight, want_loss=True, stream=None):
         n = weight.numel()
-        pos, nrm, d, w = (_dev(position, 3 * n), _dev(normal, 3 * n), _dev(direction, 3 * n), _dev(weight, n))
+        pos, nrm, v, d, w = (_dev(position, 3 * n), _dev(normal, 3 * n), _dev(view, 3 * n), _dev(direction, 3 * n),
+                             _dev(weight, n))
         loss = ctypes.c_float(0.0)
-        _lib.check(self._lib.gbpt_guide_train(self._h, pos.data_ptr(), nrm.data_ptr(), d.data_ptr(), w.data_ptr(), n,
-                                              ctypes.byref(loss) if want_loss else None, _stream(stream)))
+        _lib.check(self._lib.gbpt_guide_train(self._h, pos.data_ptr(), nrm.data_ptr(), v.data_ptr(), d.data_ptr(),
+                                              w.data_ptr(), n, ctypes.byref(loss) if want_loss else None,
+                                              _stream(stream)))
         return loss.value if want_loss else None
 
-    def gradients(self, position, normal, direction, weight, stream=None):
+    def gradients(self, position, normal, view, direction, weight, stream=None):
         """-> (grad_weights (WEIGHTS,), grad_grid (GRID_PARAMS,), loss) as numpy float32."""
         n = weight.numel()
-        pos, nrm, d, w = (_dev(position, 3 * n), _dev(normal, 3 * n), _dev(direction, 3 * n), _dev(weight, n))
+        pos, nrm, v, d, w = (_dev(position, 3 * n), _dev(normal, 3 * n), _dev(view, 3 * n), _dev(direction, 3 * n),
+                             _dev(weight, n))
         gw = np.zeros(WEIGHTS, np.float32)
         gg = np.zeros(GRID_PARAMS, np.float32)
         loss = ctypes.c_float(0.0)
-        _lib.check(self._lib.gbpt_guide_gradients(self._h, pos.data_ptr(), nrm.data_ptr(), d.data_ptr(), w.data_ptr(),
-                                                  n, _fptr(gw), _fptr(gg), ctypes.byref(loss), _stream(stream)))
+        _lib.check(self._lib.gbpt_guide_gradients(self._h, pos.data_ptr(), nrm.data_ptr(), v.data_ptr(), d.data_ptr(),
+                                                  w.data_ptr(), n, _fptr(gw), _fptr(gg), ctypes.byref(loss),
+                                                  _stream(stream)))
         return gw, gg, loss.value
 
-    def infer(self, position, normal, stream=None):
+    def infer(self, position, normal, view, stream=None):
         """-> (n, 8, 5) float32 CUDA tensor: per lobe (mu xyz, kappa, weight)."""
         import torch
         n = position.numel() // 3
-        pos, nrm = _dev(position, 3 * n), _dev(normal, 3 * n)
+        pos, nrm, v = _dev(position, 3 * n), _dev(normal, 3 * n), _dev(view, 3 * n)
         out = torch.empty((n, LOBES, 5), dtype=torch.float32, device="cuda")
-        _lib.check(self._lib.gbpt_guide_infer(self._h, pos.data_ptr(), nrm.data_ptr(), n, out.data_ptr(),
+        _lib.check(self._lib.gbpt_guide_infer(self._h, pos.data_ptr(), nrm.data_ptr(), v.data_ptr(), n, out.data_ptr(),
                                               _stream(stream)))
         return out
+
+    def error_flag(self) -> int:
+        f = i32(0)
+        _lib.check(self._lib.gbpt_guide_error_flag(self._h, ctypes.byref(f)))
+        return f.value
 
     def get_params(self):
         w = np.zeros(WEIGHTS, np.float32)

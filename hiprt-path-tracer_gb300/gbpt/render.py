@@ -84,7 +84,27 @@ RENDER_SIGNATURES = [
     ("gbpt_pass_restir_di_spatial", ctypes.c_int, [c_vp, i32, c_vp]),
     ("gbpt_restir_di_get_reservoirs", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
     ("gbpt_restir_di_set_reservoirs", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
+    ("gbpt_guide_render_default_settings", ctypes.c_int, [c_vp]),
+    ("gbpt_renderer_set_guide", ctypes.c_int, [c_vp, c_vp, c_vp]),
+    ("gbpt_renderer_get_guide_records", ctypes.c_int, [c_vp, c_vp, i32, c_vp, c_vp]),
 ]
+
+
+class GuideRenderSettingsC(ctypes.Structure):
+    _fields_ = [("enabled", i32), ("train", i32), ("guide_probability", ctypes.c_float), ("max_records", i32),
+                ("weight_clamp", ctypes.c_float), ("reserved", i32 * 11)]
+
+
+def guide_render_settings(**kw) -> GuideRenderSettingsC:
+    """Defaults of gbpt_guide_render_default_settings with the given fields overridden."""
+    lib = _load()
+    c = GuideRenderSettingsC()
+    _lib.check(lib.gbpt_guide_render_default_settings(ctypes.byref(c)))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
 
 
 def restir_di_settings(**kw) -> RestirDISettingsC:
@@ -288,6 +308,21 @@ class Renderer:
     def set_reservoirs(self, which: int, data: np.ndarray, stream=None):
         d = np.ascontiguousarray(data, np.float32).reshape(-1, 8)
         _lib.check(self._lib.gbpt_restir_di_set_reservoirs(self._h, which, d.ctypes.data, _stream(stream)))
+
+    def set_guide(self, guide, settings: "GuideRenderSettingsC | None" = None):
+        """Attaches a gbpt.guide.Guide (kept alive by the renderer) or detaches with None."""
+        self._guide = guide
+        s = settings if settings is not None else guide_render_settings()
+        _lib.check(self._lib.gbpt_renderer_set_guide(self._h, guide.handle if guide is not None else None,
+                                                     ctypes.byref(s)))
+
+    def guide_records(self, capacity: int = 1 << 16, stream=None):
+        """-> (count made by the last launch, (k, 14) float32 records; column 13 holds int32 slots)."""
+        out = np.zeros((capacity, 14), np.float32)
+        n = i32(0)
+        _lib.check(self._lib.gbpt_renderer_get_guide_records(self._h, out.ctypes.data, capacity, ctypes.byref(n),
+                                                             _stream(stream)))
+        return n.value, out[:min(n.value, capacity)]
 
     def pass_accumulate(self, stream=None):
         _lib.check(self._lib.gbpt_pass_accumulate(self._h, _stream(stream)))

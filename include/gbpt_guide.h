@@ -3,7 +3,8 @@
  * no path guiding; closest relatives are its NEE++ and ReGIR caches).
  *
  * A multiresolution hash-grid encoding of the shading position (8 levels x 2 features, 2^15
- * entries per level, resolutions 4..68 over the scene box) plus the shading normal feeds a
+ * entries per level, resolutions 4..68 over the scene box) plus the shading normal and the
+ * direction towards the viewer feeds a
  * 32 -> 64 -> 64 -> 48 ReLU MLP without biases (a constant input of 1 plays that role). Its
  * output is a mixture of 8 von Mises-Fisher lobes (direction, concentration kappa = softplus + 0.1,
  * clamped to 500, softmax weights). The MLP runs in BF16 on the tcgen05 tensor cores with FP32
@@ -50,19 +51,23 @@ GBPT_API gbpt_status gbpt_guide_default_params(gbpt_guide_params* p);
 GBPT_API gbpt_status gbpt_guide_create(const gbpt_guide_params* p, gbpt_guide** out);
 GBPT_API gbpt_status gbpt_guide_destroy(gbpt_guide* g);
 
-/* One Adam step on n training samples: position[3n], normal[3n], direction[3n] (unit vectors),
- * weight[n] (>= 0). *loss (host, may be NULL; synchronous when given) receives the normalised
- * batch loss before the step. */
-GBPT_API gbpt_status gbpt_guide_train(gbpt_guide* g, const float* position, const float* normal, const float* direction,
-                                      const float* weight, int64_t n, float* loss, void* stream);
+/* One Adam step on n training samples: position[3n], normal[3n], view[3n] (towards the viewer),
+ * direction[3n] (the sampled incident direction; unit vectors), weight[n] (negative counts as 0).
+ * *loss (host, may be NULL; synchronous when given) receives the normalised batch loss before the
+ * step. */
+GBPT_API gbpt_status gbpt_guide_train(gbpt_guide* g, const float* position, const float* normal, const float* view,
+                                      const float* direction, const float* weight, int64_t n, float* loss, void* stream);
 /* The gradients of the batch loss without an Adam step, copied to host arrays (either may be
  * NULL): grad_weights[GBPT_GUIDE_WEIGHTS], grad_grid[GBPT_GUIDE_GRID_PARAMS]. Synchronous. */
 GBPT_API gbpt_status gbpt_guide_gradients(gbpt_guide* g, const float* position, const float* normal,
-                                          const float* direction, const float* weight, int64_t n, float* grad_weights,
-                                          float* grad_grid, float* loss, void* stream);
+                                          const float* view, const float* direction, const float* weight, int64_t n,
+                                          float* grad_weights, float* grad_grid, float* loss, void* stream);
 /* Mixture per query: lobes[40 n] = 8 x (mu xyz, kappa, weight). */
-GBPT_API gbpt_status gbpt_guide_infer(gbpt_guide* g, const float* position, const float* normal, int64_t n, float* lobes,
-                                      void* stream);
+GBPT_API gbpt_status gbpt_guide_infer(gbpt_guide* g, const float* position, const float* normal, const float* view,
+                                      int64_t n, float* lobes, void* stream);
+/* 1 if a bounded tensor-core wait of a guide kernel gave up since creation (the kernel then
+ * stopped early and its outputs are incomplete), else 0. Synchronous. */
+GBPT_API gbpt_status gbpt_guide_error_flag(gbpt_guide* g, int32_t* flag);
 /* Parameters to / from host arrays (either may be NULL). Synchronous. */
 GBPT_API gbpt_status gbpt_guide_get_params(gbpt_guide* g, float* weights, float* grid);
 GBPT_API gbpt_status gbpt_guide_set_params(gbpt_guide* g, const float* weights, const float* grid);

@@ -11,7 +11,7 @@ hand BF16 operands to the tensor cores (the MLP input X, the weights, the hidden
 H2, the output gradient dY and the hidden gradients dH2 and dH1), so the remaining GPU/oracle
 difference is FP32 accumulation order and transcendental rounding.
 
-Network: hash-grid features (8 levels x 2, trilinear) ++ normal ++ [1] ++ zeros (32 inputs) ->
+Network: hash-grid features (8 levels x 2, trilinear) ++ normal ++ [1] ++ view ++ zeros (32 inputs) ->
 ReLU(X W1) (64) -> ReLU(H1 W2) (64) -> H2 W3 (48 raw outputs) -> 8 vMF lobes (raw[5i:5i+3]
 direction, softplus(raw[5i+3]) + 0.1 clamped to 500 concentration, softmax(raw[5i+4]) weights).
 Outputs 40..47 are unused. Loss: sum_i w_i / sum(w) * -log q(d_i).
@@ -95,12 +95,13 @@ def encode(grid, cor):
     return np.concatenate(feats, 1)
 
 
-def input_rows(feat, N):
+def input_rows(feat, N, V):
     n = feat.shape[0]
     x = np.zeros((n, IN))
     x[:, :16] = feat
     x[:, 16:19] = N
     x[:, 19] = 1.0
+    x[:, 20:23] = V
     return x
 
 
@@ -133,12 +134,12 @@ def mixture_pdf(mu, kappa, weight, d):
     return (weight * np.exp(log_vmf(kappa, c))).sum(1)
 
 
-def forward(weights, grid, lo, inv_ext, P, N, bf16_ops=True):
+def forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops=True):
     """-> dict with the input X, pre-activations D1, D2, activations H1, H2, raw outputs."""
     rnd = bf16 if bf16_ops else (lambda a: np.asarray(a, np.float64))
     W1, W2, W3 = (rnd(w) for w in split_weights(weights))
     cor = corners(lo, inv_ext, P)
-    X = rnd(input_rows(encode(grid, cor), np.asarray(N, np.float64)))
+    X = rnd(input_rows(encode(grid, cor), np.asarray(N, np.float64), np.asarray(V, np.float64)))
     D1 = X @ W1
     H1 = rnd(np.maximum(D1, 0.0))
     D2 = H1 @ W2
@@ -172,10 +173,10 @@ def loss_and_draw(raw, d, w):
     return float((scale * -logq).sum()), draw, logq
 
 
-def gradients(weights, grid, lo, inv_ext, P, N, D, w, bf16_ops=True):
+def gradients(weights, grid, lo, inv_ext, P, N, V, D, w, bf16_ops=True):
     """-> (loss, grad_weights (WEIGHTS,), grad_grid (GRID_PARAMS,)) of the batch loss."""
     rnd = bf16 if bf16_ops else (lambda a: np.asarray(a, np.float64))
-    f = forward(weights, grid, lo, inv_ext, P, N, bf16_ops)
+    f = forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops)
     W1, W2, W3 = f["W"]
     loss, draw, _ = loss_and_draw(f["raw"], np.asarray(D, np.float64), w)
     dY = rnd(draw)
@@ -193,14 +194,14 @@ def gradients(weights, grid, lo, inv_ext, P, N, D, w, bf16_ops=True):
     return loss, gw, gg.reshape(-1)
 
 
-def batch_loss(weights, grid, lo, inv_ext, P, N, D, w, bf16_ops=False):
-    f = forward(weights, grid, lo, inv_ext, P, N, bf16_ops)
+def batch_loss(weights, grid, lo, inv_ext, P, N, V, D, w, bf16_ops=False):
+    f = forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops)
     return loss_and_draw(f["raw"], np.asarray(D, np.float64), w)[0]
 
 
-def infer(weights, grid, lo, inv_ext, P, N, bf16_ops=True):
+def infer(weights, grid, lo, inv_ext, P, N, V, bf16_ops=True):
     """-> (n, 8, 5): per lobe (mu xyz, kappa, weight), the layout of gbpt_guide_infer."""
-    f = forward(weights, grid, lo, inv_ext, P, N, bf16_ops)
+    f = forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops)
     mu, kappa, pi, _ = head(f["raw"])
     return np.concatenate([mu, kappa[..., None], pi[..., None]], -1)
 
@@ -229,12 +230,13 @@ def random_params(seed=0, grid_scale=1e-2):
 
 
 def random_batch(n, seed=0, lo=(0, 0, 0), hi=(1, 1, 1)):
-    """Seeded training samples: positions in the box, unit normals and directions, weights >= 0."""
+    """Seeded training samples: positions in the box, unit normals, view and incident directions,
+    weights >= 0 (a fifth of them zero)."""
     rng = np.random.default_rng(seed)
     P = rng.uniform(lo, hi, (n, 3))
-    N = rng.normal(size=(n, 3))
-    N /= np.linalg.norm(N, axis=1, keepdims=True)
-    D = rng.normal(size=(n, 3))
-    D /= np.linalg.norm(D, axis=1, keepdims=True)
+    N, V, D = (rng.normal(size=(n, 3)) for _ in range(3))
+    for a in (N, V, D):
+        a /= np.linalg.norm(a, axis=1, keepdims=True)
     w = rng.exponential(1.0, n) * (rng.random(n) < 0.8)
-    return P.astype(np.float32), N.astype(np.float32), D.astype(np.float32), w.astype(np.float32)
+    f = np.float32
+    return P.astype(f), N.astype(f), V.astype(f), D.astype(f), w.astype(f)

@@ -94,6 +94,6 @@ def test_guide_parameters_and_argument_checks():
     bad = guide.default_params(scene_min=(0, 2, 0))
     assert lib.gbpt_guide_create(ctypes.byref(bad), ctypes.byref(h)) == 1
     assert b"empty scene box" in lib.gbpt_last_error()
-    assert lib.gbpt_guide_train(None, None, None, None, None, 4, None, None) == 1
-    assert lib.gbpt_guide_infer(None, None, None, 4, None, None) == 1
+    assert lib.gbpt_guide_train(None, None, None, None, None, None, 4, None, None) == 1
+    assert lib.gbpt_guide_infer(None, None, None, None, 4, None, None) == 1
     assert lib.gbpt_guide_destroy(None) == 0

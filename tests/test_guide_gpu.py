@@ -43,10 +43,10 @@ def _blocks(gw, gg):
 def test_inference_matches_oracle(cuda):
     g = _guide()
     w, grid = _with_grid(g)
-    P, N, _, _ = G.random_batch(1000, 21)  # not a multiple of the 128-row tile
-    got = g.infer(_t(P), _t(N)).cpu().numpy()
+    P, N, V, _, _ = G.random_batch(1000, 21)  # not a multiple of the 128-row tile
+    got = g.infer(_t(P), _t(N), _t(V)).cpu().numpy()
     lo, inv = G.domain(g.params.scene_min, g.params.scene_max)
-    want = G.infer(w, grid, lo, inv, P, N)
+    want = G.infer(w, grid, lo, inv, P, N, V)
     close = np.abs(got - want) <= LOBE_ATOL + LOBE_RTOL * np.abs(want)
     assert close.mean() >= LOBE_FRACTION, close.mean()
     assert np.abs(got - want).max() < 5e-2
@@ -59,10 +59,10 @@ def test_inference_matches_oracle(cuda):
 def test_gradients_match_oracle(cuda, n):
     g = _guide()
     w, grid = _with_grid(g)
-    P, N, D, wt = G.random_batch(n, 100 + n)
-    gw, gg, loss = g.gradients(_t(P), _t(N), _t(D), _t(wt))
+    P, N, V, D, wt = G.random_batch(n, 100 + n)
+    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
     lo, inv = G.domain(g.params.scene_min, g.params.scene_max)
-    l0, ow, og = G.gradients(w, grid, lo, inv, P, N, D, wt)
+    l0, ow, og = G.gradients(w, grid, lo, inv, P, N, V, D, wt)
     assert abs(loss - l0) <= 1e-4 * max(1.0, abs(l0)), (loss, l0)
     for name, (a, b) in {k: (v, _blocks(ow, og)[k]) for k, v in _blocks(gw, gg).items()}.items():
         nb = np.linalg.norm(b)
@@ -76,25 +76,25 @@ def test_gradients_match_oracle(cuda, n):
 
 def test_zero_and_negative_weights(cuda):
     g = _guide()
-    P, N, D, wt = G.random_batch(300, 5)
+    P, N, V, D, wt = G.random_batch(300, 5)
     wt[:] = 0.0
-    gw, gg, loss = g.gradients(_t(P), _t(N), _t(D), _t(wt))
+    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
     assert loss == 0.0 and not gw.any() and not gg.any()
     wt = np.random.default_rng(1).normal(size=300).astype(np.float32)  # negatives count as zero
-    gw, gg, loss = g.gradients(_t(P), _t(N), _t(D), _t(wt))
+    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
     w, grid = g.get_params()
     lo, inv = G.domain(g.params.scene_min, g.params.scene_max)
-    l0, ow, _ = G.gradients(w, grid, lo, inv, P, N, D, wt)
+    l0, ow, _ = G.gradients(w, grid, lo, inv, P, N, V, D, wt)
     assert abs(loss - l0) <= 1e-4 * abs(l0)
     assert np.linalg.norm(gw - ow) <= GRAD_RTOL * np.linalg.norm(ow)
 
 
 def test_adam_step_matches_oracle(cuda):
     g = _guide()
-    P, N, D, wt = G.random_batch(2048, 9)
-    gw, gg, _ = g.gradients(_t(P), _t(N), _t(D), _t(wt))
+    P, N, V, D, wt = G.random_batch(2048, 9)
+    gw, gg, _ = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
     w0, grid0 = g.get_params()
-    g.train(_t(P), _t(N), _t(D), _t(wt))
+    g.train(_t(P), _t(N), _t(V), _t(D), _t(wt))
     w1, grid1 = g.get_params()
     p = g.params
     zeros = np.zeros(G.WEIGHTS + G.GRID_PARAMS, np.float32)
@@ -131,13 +131,15 @@ def test_online_training_learns_position_dependent_lobes(cuda):
         mu = P - 0.5
         mu /= np.linalg.norm(mu, axis=1, keepdims=True)
         D = _vmf_sample(mu, 20.0, rng)
-        losses.append(g.train(_t(P), _t(np.tile([0.0, 0, 1], (4096, 1))), _t(D), _t(np.ones(4096))))
+        up = _t(np.tile([0.0, 0, 1], (4096, 1)))
+        losses.append(g.train(_t(P), up, up, _t(D), _t(np.ones(4096))))
     assert losses[0] > 2.0
     assert np.mean(losses[-20:]) < 0.3, losses[-20:]
     P = rng.random((512, 3))
     mu = P - 0.5
     mu /= np.linalg.norm(mu, axis=1, keepdims=True)
-    lobes = g.infer(_t(P), _t(np.tile([0.0, 0, 1], (512, 1)))).cpu().numpy()
+    up = _t(np.tile([0.0, 0, 1], (512, 1)))
+    lobes = g.infer(_t(P), up, up).cpu().numpy()
     q = G.mixture_pdf(lobes[:, :, :3], lobes[:, :, 3], lobes[:, :, 4], mu)
     # the target density at its mode is 20 / (2 pi) = 3.2; the uniform density is 0.08
     assert np.median(q) > 1.0, np.median(q)
@@ -147,8 +149,9 @@ def test_empty_batch_and_bad_arguments(cuda):
     from gbpt import GbptError
     g = _guide(max_batch=256)
     e = _t(np.zeros((0, 3)))
-    assert g.train(e, e, e, _t(np.zeros(0))) == 0.0
-    assert g.infer(e, e).shape == (0, 8, 5)
-    P, N, D, wt = G.random_batch(300, 1)
+    assert g.train(e, e, e, e, _t(np.zeros(0))) == 0.0
+    assert g.infer(e, e, e).shape == (0, 8, 5)
+    P, N, V, D, wt = G.random_batch(300, 1)
     with pytest.raises(GbptError):
-        g.train(_t(P), _t(N), _t(D), _t(wt))  # above max_batch
+        g.train(_t(P), _t(N), _t(V), _t(D), _t(wt))  # above max_batch
+    assert g.error_flag() == 0

@@ -7,14 +7,14 @@ import guide_oracle as G
 
 def _setup(n=96, seed=3):
     weights, grid = G.random_params(seed, grid_scale=0.2)
-    P, N, D, w = G.random_batch(n, seed + 1)
+    P, N, V, D, w = G.random_batch(n, seed + 1)
     lo, inv = G.domain((0, 0, 0), (1, 1, 1))
-    return weights, grid, lo, inv, P, N, D, w
+    return weights, grid, lo, inv, P, N, V, D, w
 
 
 def test_weight_gradients_match_central_differences():
-    weights, grid, lo, inv, P, N, D, w = _setup()
-    _, gw, _ = G.gradients(weights, grid, lo, inv, P, N, D, w, bf16_ops=False)
+    weights, grid, lo, inv, P, N, V, D, w = _setup()
+    _, gw, _ = G.gradients(weights, grid, lo, inv, P, N, V, D, w, bf16_ops=False)
     rng = np.random.default_rng(0)
     idx = np.concatenate([rng.choice(np.arange(G.OFF_W1, G.OFF_W2), 12, replace=False),
                           rng.choice(np.arange(G.OFF_W2, G.OFF_W3), 12, replace=False),
@@ -24,13 +24,13 @@ def test_weight_gradients_match_central_differences():
         wp, wm = weights.copy(), weights.copy()
         wp[i] += h
         wm[i] -= h
-        fd = (G.batch_loss(wp, grid, lo, inv, P, N, D, w) - G.batch_loss(wm, grid, lo, inv, P, N, D, w)) / (2 * h)
+        fd = (G.batch_loss(wp, grid, lo, inv, P, N, V, D, w) - G.batch_loss(wm, grid, lo, inv, P, N, V, D, w)) / (2 * h)
         assert abs(fd - gw[i]) <= 1e-6 + 1e-4 * abs(fd), (i, fd, gw[i])
 
 
 def test_grid_gradients_match_central_differences():
-    weights, grid, lo, inv, P, N, D, w = _setup()
-    _, _, gg = G.gradients(weights, grid, lo, inv, P, N, D, w, bf16_ops=False)
+    weights, grid, lo, inv, P, N, V, D, w = _setup()
+    _, _, gg = G.gradients(weights, grid, lo, inv, P, N, V, D, w, bf16_ops=False)
     touched = np.nonzero(gg)[0]
     assert touched.size > 100
     rng = np.random.default_rng(1)
@@ -39,7 +39,7 @@ def test_grid_gradients_match_central_differences():
         gp, gm = grid.copy(), grid.copy()
         gp[i] += h
         gm[i] -= h
-        fd = (G.batch_loss(weights, gp, lo, inv, P, N, D, w) - G.batch_loss(weights, gm, lo, inv, P, N, D, w)) / (2 * h)
+        fd = (G.batch_loss(weights, gp, lo, inv, P, N, V, D, w) - G.batch_loss(weights, gm, lo, inv, P, N, V, D, w)) / (2 * h)
         assert abs(fd - gg[i]) <= 1e-7 + 1e-4 * abs(fd), (i, fd, gg[i])
 
 
@@ -88,7 +88,7 @@ def test_bf16_rounding_is_round_to_nearest_even():
 
 
 def test_bf16_loss_is_close_to_fp64_loss():
-    weights, grid, lo, inv, P, N, D, w = _setup(256)
-    l64 = G.batch_loss(weights, grid, lo, inv, P, N, D, w, bf16_ops=False)
-    l16 = G.batch_loss(weights, grid, lo, inv, P, N, D, w, bf16_ops=True)
+    weights, grid, lo, inv, P, N, V, D, w = _setup(256)
+    l64 = G.batch_loss(weights, grid, lo, inv, P, N, V, D, w, bf16_ops=False)
+    l16 = G.batch_loss(weights, grid, lo, inv, P, N, V, D, w, bf16_ops=True)
     assert abs(l64 - l16) < 2e-2 * abs(l64)
