@@ -1,14 +1,16 @@
-// Guiding network kernels (sm_103a): hash-grid encoding, the 32-64-64-48 MLP on tcgen05 tensor
-// cores (BF16 operands in shared memory, FP32 accumulators in TMEM), the vMF-mixture head and its
-// loss, the backward pass, Adam and the BF16 weight packing.
+// Guiding network kernels (sm_103a): hash-grid + spherical-harmonic encoding, the 64-64-64-64-48
+// MLP on the tcgen05 tensor cores (BF16 operands in shared memory, FP32 accumulators in TMEM), the
+// vMF-mixture head and its loss, the backward pass, Adam and the BF16 packing of weights and grid.
 //
 // One CTA of 128 threads processes tiles of 128 samples (M = 128, one sample per thread and per
-// TMEM lane). Per tile: encode -> X; D1 = X W1 -> ReLU -> H1; D2 = H1 W2 -> ReLU -> H2;
-// D3 = H2 W3 -> head. Training continues with dY (loss gradient of the 48 raw outputs) ->
-// dH2 = dY W3^T (masked by ReLU') -> dH1 = dH2 W2^T (masked) -> dX = dH1 W1^T -> hash-grid scatter;
-// the weight gradients dW3 = H2^T dY, dW2 = H1^T dH2, dW1 = X^T dH1 are reduced over the tile in
-// shared memory by the CUDA cores and flushed once per CTA. The MMAs are issued by thread 0 and
-// completed through an mbarrier; every wait is bounded and reports through an error flag.
+// TMEM lane). Forward: X -> H1 = ReLU(X W1) -> H2 -> H3 -> raw = H3 W4 -> head. Training continues
+// with the loss gradient dY of the raw outputs and, per layer l = 4..1,
+//   dH_{l-1} = (dH_l W_l^T) masked by ReLU'    (M = 128 samples, tensor core)
+//   dW_l    += H_{l-1}^T dH_l                   (M = the layer's 64 inputs, K = the tile's samples)
+// The weight gradients accumulate in TMEM across all tiles of the CTA and are flushed once. Their
+// A operand H^T is 64 rows: the MMA runs with M = 128 and the upper 64 rows of D (read from the
+// next 16 KB of shared memory) are ignored. MMAs are issued by thread 0 and completed through an
+// mbarrier; every wait is bounded and reports through an error flag.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -23,27 +25,38 @@ namespace {
 
 constexpr int kTile = 128;
 constexpr int kWaitLimit = 1 << 24;
-constexpr uint32_t kTmemCols = 256;
-// TMEM columns (accumulators start on multiples of 64): forward D1 @0, D2 @64, D3 @128 (48 wide);
-// backward dH2 @192, dH1 @0, dX @64 (32 wide)
+// TMEM columns. Training (512 allocated): F @0 (forward D / backward dH, up to 64 wide), the
+// weight-gradient accumulators dW1 @128, dW2 @192, dW3 @256 (64 wide), dW4 @320 (48 wide).
+// Inference: F only (64 allocated).
+constexpr uint32_t kTmemTrain = 512;
+constexpr uint32_t kTmemInfer = 64;
+constexpr uint32_t kColF = 0;
+__device__ __forceinline__ uint32_t col_dw(int l) { return 128u + 64u * (uint32_t)l; }
 
-struct Smem
+using bf16 = __nv_bfloat16;
+
+struct SmemTrain
 {
     uint64_t mbar;
     uint32_t tmem;
     uint32_t pad;
-    __nv_bfloat16 w[kPackedWeights];
-    __nv_bfloat16 x[kTile * kIn];
-    __nv_bfloat16 h1[kTile * kHid];
-    __nv_bfloat16 h2[kTile * kHid];
-    __nv_bfloat16 dy[kTile * kOut];
-    __nv_bfloat16 dh2[kTile * kHid];
-    __nv_bfloat16 dh1[kTile * kHid];
-    float dw[kNumWeights];
+    bf16 w[kPackedWeights];
+    // transposed layer inputs X^T, H1^T, H2^T, H3^T (64 rows x K = 128 samples): the A operands
+    // of dW1..dW4; each is followed by 16 KB of shared memory that the M = 128 MMA reads as rows
+    // 64..127 (results ignored)
+    bf16 tr[4][kHid * kTile];
+    bf16 act[2][kTile * kHid];  // K-major activations / output gradients (A operands), ping-pong
+    bf16 gt[2][kHid * kTile];   // transposed output gradients (B operands of dW), ping-pong
 };
-constexpr size_t kSmemTrain = sizeof(Smem);
-// inference needs the weights and the forward activations only
-constexpr size_t kSmemInfer = offsetof(Smem, dy);
+
+struct SmemInfer
+{
+    uint64_t mbar;
+    uint32_t tmem;
+    uint32_t pad;
+    bf16 w[kFwdWeights];
+    bf16 act[2][kTile * kHid];
+};
 
 __device__ __forceinline__ int kmo(int r, int k, int K) { return umma::kmajor_offset(r, k, K); }
 
@@ -60,11 +73,11 @@ __device__ __forceinline__ int64_t batch_size(const Batch& b)
     return c < 0 ? 0 : (c < b.n_max ? c : b.n_max);
 }
 
-__device__ __forceinline__ void copy_weights(Smem& sm, const uint16_t* packed)
+__device__ __forceinline__ void copy_weights(bf16* dst, const uint16_t* packed, int count)
 {
     const uint4* src = reinterpret_cast<const uint4*>(packed);
-    uint4* dst = reinterpret_cast<uint4*>(sm.w);
-    for (int i = threadIdx.x; i < kPackedWeights / 8; i += blockDim.x) dst[i] = src[i];
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int i = threadIdx.x; i < count / 8; i += blockDim.x) d[i] = src[i];
 }
 
 // makes this thread's shared-memory writes visible to the tensor core, then syncs the CTA
@@ -76,92 +89,96 @@ __device__ __forceinline__ void publish_smem()
     umma::fence_after();
 }
 
-// issue (thread 0) + wait (all) one GEMM; false if the wait gave up
-__device__ __forceinline__ bool run_gemm(Smem& sm, uint32_t col, const __nv_bfloat16* A, const __nv_bfloat16* B, int N,
-                                         int K, uint32_t& phase)
+// all threads: wait for the MMAs committed to the mbarrier; false (on every thread) if it gave up
+__device__ __forceinline__ bool wait_mma(uint64_t* mbar, uint32_t& phase)
 {
-    if (threadIdx.x == 0) umma::gemm_commit(sm.tmem + col, A, B, N, K, &sm.mbar);
-    const bool ok = umma::mbar_wait(&sm.mbar, phase, kWaitLimit);
+    const bool ok = umma::mbar_wait(mbar, phase, kWaitLimit);
     phase ^= 1u;
     umma::fence_after();
-    return __syncthreads_and(ok ? 1 : 0) != 0;  // every thread takes the same branch
+    return __syncthreads_and(ok ? 1 : 0) != 0;
 }
 
-__device__ __forceinline__ void load_cols(const Smem& sm, int col, int count, float* out)
+// issue (thread 0) + wait (all) one forward GEMM into F
+__device__ __forceinline__ bool run_gemm(uint64_t* mbar, uint32_t tmem, const bf16* A, const bf16* B, int N, int K,
+                                         uint32_t& phase)
+{
+    if (threadIdx.x == 0) umma::gemm_commit(tmem + kColF, A, B, N, K, mbar);
+    return wait_mma(mbar, phase);
+}
+
+__device__ __forceinline__ void load_cols(uint32_t tmem, uint32_t col, int count, float* out)
 {
     const int warp = threadIdx.x >> 5;
-    for (int c = 0; c < count; c += 16) umma::tmem_ld16(umma::lane_addr(sm.tmem, warp, col + c), out + c);
+    for (int c = 0; c < count; c += 16) umma::tmem_ld16(umma::lane_addr(tmem, warp, (int)col + c), out + c);
 }
 
-__device__ __forceinline__ void setup(Smem& sm)
-{
-    if (threadIdx.x < 32) umma::tmem_alloc(&sm.tmem, kTmemCols);
-    if (threadIdx.x == 0) umma::mbar_init(&sm.mbar);
-}
-
-__device__ __forceinline__ void teardown(Smem& sm)
-{
-    umma::fence_before();
-    __syncthreads();
-    if (threadIdx.x < 32) umma::tmem_dealloc(sm.tmem, kTmemCols);
-}
-
-// Forward of one tile up to the 48 raw outputs of this thread's row; h1/h2 keep the ReLU'd
-// activations in shared memory and m1/m2 their positivity bits. False if a wait gave up.
-__device__ bool forward_tile(Smem& sm, const Net& net, bool valid, V3 p, V3 n, V3 view, float* raw, uint32_t* m1,
-                             uint32_t* m2, uint32_t& phase)
+// stores this thread's row of n values as BF16: K-major into 'a' (row t, K = n) and, when 't_out'
+// is given, transposed into it (row k, K = 128 samples)
+__device__ __forceinline__ void store_row(bf16* a, bf16* t_out, const float* v, int n)
 {
     const int t = threadIdx.x;
+    for (int k = 0; k < n; k++)
     {
-        float feat[16], x[kIn];
-        const Domain d = {{net.lo[0], net.lo[1], net.lo[2]}, {net.inv_ext[0], net.inv_ext[1], net.inv_ext[2]}};
-        if (valid)
-            encode(d, net.params + kNumWeights, p, feat);
-        else
-            for (int i = 0; i < 16; i++) feat[i] = 0.0f;
-        input_row(feat, valid ? n : v3(0.0f), valid ? view : v3(0.0f), x);
-        if (!valid) x[19] = 0.0f;
-        for (int k = 0; k < kIn; k++) sm.x[kmo(t, k, kIn)] = __float2bfloat16(x[k]);
+        const bf16 b = __float2bfloat16(v[k]);
+        a[kmo(t, k, n)] = b;
+        if (t_out) t_out[kmo(k, t, kTile)] = b;
     }
-    publish_smem();
-    if (!run_gemm(sm, 0, sm.x, sm.w + kW1f, kHid, kIn, phase)) return false;
-    float h[kHid];
-    load_cols(sm, 0, kHid, h);
-    m1[0] = m1[1] = 0u;
-    for (int k = 0; k < kHid; k++)
-    {
-        const float v = fmaxf(h[k], 0.0f);
-        if (h[k] > 0.0f) m1[k >> 5] |= 1u << (k & 31);
-        sm.h1[kmo(t, k, kHid)] = __float2bfloat16(v);
-    }
-    publish_smem();
-    if (!run_gemm(sm, 64, sm.h1, sm.w + kW2f, kHid, kHid, phase)) return false;
-    load_cols(sm, 64, kHid, h);
-    m2[0] = m2[1] = 0u;
-    for (int k = 0; k < kHid; k++)
-    {
-        const float v = fmaxf(h[k], 0.0f);
-        if (h[k] > 0.0f) m2[k >> 5] |= 1u << (k & 31);
-        sm.h2[kmo(t, k, kHid)] = __float2bfloat16(v);
-    }
-    publish_smem();
-    if (!run_gemm(sm, 128, sm.h2, sm.w + kW3f, kOut, kHid, phase)) return false;
-    load_cols(sm, 128, kOut, raw);
-    return true;
 }
 
-// out[o] += sum over the tile's rows of A[r][i] * B[r][j], o = i * NB + j (A: K-major with KA
-// columns, B: K-major with NB columns); the tile's 128 threads split the outputs
-__device__ __forceinline__ void accumulate_outer(float* out, const __nv_bfloat16* A, int KA, const __nv_bfloat16* B, int NB)
+// ReLU of the 64 accumulator columns with their positivity mask bits
+__device__ __forceinline__ void relu(float* h, uint32_t* mask)
 {
-    for (int o = threadIdx.x; o < KA * NB; o += blockDim.x)
+    mask[0] = mask[1] = 0u;
+    for (int k = 0; k < kHid; k++)
     {
-        const int i = o / NB, j = o - i * NB;
-        float acc = 0.0f;
-        for (int r = 0; r < kTile; r++)
-            acc += __bfloat162float(A[kmo(r, i, KA)]) * __bfloat162float(B[kmo(r, j, NB)]);
-        out[o] += acc;
+        if (h[k] > 0.0f)
+            mask[k >> 5] |= 1u << (k & 31);
+        else
+            h[k] = 0.0f;
     }
+}
+
+// gradient of a hidden layer's output masked by ReLU'
+__device__ __forceinline__ void mask_grad(float* g, const uint32_t* mask)
+{
+    for (int k = 0; k < kHid; k++)
+        if (!((mask[k >> 5] >> (k & 31)) & 1u)) g[k] = 0.0f;
+}
+
+// Forward of one tile up to the 48 raw outputs of this thread's row. 'act' holds two ping-pong
+// K-major buffers; 'tr' (training only, else null) receives the transposed inputs of every layer
+// and 'masks' the three ReLU masks. False if a wait gave up.
+__device__ bool forward_tile(uint64_t* mbar, uint32_t tmem, const bf16* w, bf16 (*act)[kTile * kHid],
+                             bf16 (*tr)[kHid * kTile], const Net& net, bool valid, V3 p, V3 n, V3 view, float* raw,
+                             uint32_t (*masks)[2], uint32_t& phase)
+{
+    {
+        float feat[kGridFeatures], x[kIn];
+        const Domain d = {{net.lo[0], net.lo[1], net.lo[2]}, {net.inv_ext[0], net.inv_ext[1], net.inv_ext[2]}};
+        if (valid)
+        {
+            encode(d, net.grid_bf16, p, feat);
+            input_row(feat, n, view, x);
+        }
+        else
+            for (int k = 0; k < kIn; k++) x[k] = 0.0f;
+        store_row(act[0], tr ? tr[0] : nullptr, x, kIn);
+    }
+    publish_smem();
+    const int wf[3] = {kW1f, kW2f, kW3f};
+    float h[kHid];
+    for (int l = 0; l < 3; l++)
+    {
+        if (!run_gemm(mbar, tmem, act[l & 1], w + wf[l], kHid, kHid, phase)) return false;
+        load_cols(tmem, kColF, kHid, h);
+        uint32_t scratch[2];
+        relu(h, masks ? masks[l] : scratch);
+        store_row(act[(l + 1) & 1], tr ? tr[l + 1] : nullptr, h, kHid);
+        publish_smem();
+    }
+    if (!run_gemm(mbar, tmem, act[1], w + kW4f, kOut, kHid, phase)) return false;
+    load_cols(tmem, kColF, kOut, raw);
+    return true;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -170,26 +187,27 @@ __device__ __forceinline__ void accumulate_outer(float* out, const __nv_bfloat16
 __global__ void __launch_bounds__(kTile) train_kernel(Net net, Batch b, const float* __restrict__ weight_sum,
                                                       float* __restrict__ grads, float* __restrict__ loss, int* err)
 {
-    const int64_t n = batch_size(b);
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+    SmemTrain& sm = *reinterpret_cast<SmemTrain*>(smem_raw);
     const int t = threadIdx.x;
-    copy_weights(sm, net.packed);
-    for (int i = t; i < kNumWeights; i += blockDim.x) sm.dw[i] = 0.0f;
-    setup(sm);
+    const int64_t n = batch_size(b);
+    copy_weights(sm.w, net.packed, kPackedWeights);
+    if (t < 32) umma::tmem_alloc(&sm.tmem, kTmemTrain);
+    if (t == 0) umma::mbar_init(&sm.mbar);
     publish_smem();
+    const uint32_t tmem = sm.tmem;
     const float inv_wsum = *weight_sum > 0.0f ? 1.0f / *weight_sum : 0.0f;
     const Domain d = {{net.lo[0], net.lo[1], net.lo[2]}, {net.inv_ext[0], net.inv_ext[1], net.inv_ext[2]}};
     uint32_t phase = 0;
     float loss_acc = 0.0f;
-    bool ok = true;
+    bool ok = true, first = true;
     const int64_t n_tiles = (n + kTile - 1) / kTile;
     for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x)
     {
         const int64_t row = tile * kTile + t;
         const bool valid = row < n;
         V3 p = v3(0.0f), nn = v3(0.0f), vw = v3(0.0f), w = v3(0.0f, 0.0f, 1.0f);
-        float ws = 0.0f;
+        float ws = 0.0f, pb = -1.0f;
         if (valid)
         {
             p = load3(b.pos, row);
@@ -197,67 +215,93 @@ __global__ void __launch_bounds__(kTile) train_kernel(Net net, Batch b, const fl
             vw = load3(b.view, row);
             w = load3(b.dir, row);
             ws = fmaxf(b.weight[row], 0.0f);
+            if (b.bsdf_pdf) pb = fmaxf(b.bsdf_pdf[row], 0.0f);
         }
         float raw[kOut];
-        uint32_t m1[2], m2[2];
-        ok = forward_tile(sm, net, valid, p, nn, vw, raw, m1, m2, phase);
+        uint32_t masks[3][2];
+        ok = forward_tile(&sm.mbar, tmem, sm.w, sm.act, sm.tr, net, valid, p, nn, vw, raw, masks, phase);
         if (!ok) break;
-        // head, loss and its gradient for this row
-        float draw[kOut];
+        // head, loss and its gradient for this row -> dY (K-major, K = 48) and dY^T
         {
+            float draw[kOut];
             Lobe lobes[kLobes];
-            float len[kLobes];
-            head(raw, lobes, len);
+            float len[kLobes], alpha;
+            head(raw, lobes, len, alpha);
             const float scale = valid ? ws * inv_wsum : 0.0f;
-            const float logq = head_backward(raw, lobes, len, w, scale, draw);
-            if (scale > 0.0f) loss_acc += -scale * logq;
+            const float l = head_backward(raw, lobes, len, alpha, w, scale, pb, draw);
+            if (scale > 0.0f) loss_acc += l;
+            store_row(sm.act[0], sm.gt[0], draw, kOut);
         }
-        for (int k = 0; k < kOut; k++) sm.dy[kmo(t, k, kOut)] = __float2bfloat16(draw[k]);
         publish_smem();
-        accumulate_outer(sm.dw + kOffW3, sm.h2, kHid, sm.dy, kOut);  // dW3 = H2^T dY
-        ok = run_gemm(sm, 192, sm.dy, sm.w + kW3b, kHid, kOut, phase);  // dH2 = dY W3^T
-        if (!ok) break;
+        // layers 4..1: dH_{l-1} = dH_l W_l^T into F and dW_l += H_{l-1}^T dH_l, one commit
+        const int wb[4] = {kW1b, kW2b, kW3b, kW4b};
         float g[kHid];
-        load_cols(sm, 192, kHid, g);
-        for (int k = 0; k < kHid; k++)
-            sm.dh2[kmo(t, k, kHid)] = __float2bfloat16((m2[k >> 5] >> (k & 31)) & 1u ? g[k] : 0.0f);
-        publish_smem();
-        accumulate_outer(sm.dw + kOffW2, sm.h1, kHid, sm.dh2, kHid);  // dW2 = H1^T dH2
-        ok = run_gemm(sm, 0, sm.dh2, sm.w + kW2b, kHid, kHid, phase);  // dH1 = dH2 W2^T
-        if (!ok) break;
-        load_cols(sm, 0, kHid, g);
-        for (int k = 0; k < kHid; k++)
-            sm.dh1[kmo(t, k, kHid)] = __float2bfloat16((m1[k >> 5] >> (k & 31)) & 1u ? g[k] : 0.0f);
-        publish_smem();
-        accumulate_outer(sm.dw + kOffW1, sm.x, kIn, sm.dh1, kHid);  // dW1 = X^T dH1
-        ok = run_gemm(sm, 64, sm.dh1, sm.w + kW1b, kIn, kHid, phase);  // dX = dH1 W1^T
-        if (!ok) break;
-        float dx[kIn];
-        load_cols(sm, 64, kIn, dx);
-        if (valid) encode_backward(d, grads + kNumWeights, p, dx);
+        for (int l = 3; l >= 0 && ok; l--)
+        {
+            const int n_out = l == 3 ? kOut : kHid;  // width of dH_l
+            const int cur = (3 - l) & 1;             // buffers holding dH_l
+            if (t == 0)
+            {
+                umma::gemm_issue(tmem + kColF, sm.act[cur], sm.w + wb[l], l == 0 ? kGridFeatures : kHid, n_out, false);
+                umma::gemm_issue(tmem + col_dw(l), sm.tr[l], sm.gt[cur], n_out, kTile, !first);
+                umma::commit(&sm.mbar);
+            }
+            ok = wait_mma(&sm.mbar, phase);
+            if (!ok) break;
+            if (l > 0)
+            {
+                load_cols(tmem, kColF, kHid, g);
+                mask_grad(g, masks[l - 1]);
+                store_row(sm.act[cur ^ 1], sm.gt[cur ^ 1], g, kHid);
+                publish_smem();
+            }
+            else
+            {
+                load_cols(tmem, kColF, kGridFeatures, g);
+                if (valid) encode_backward(d, grads + kNumWeights, p, g);
+            }
+        }
+        first = false;
         __syncthreads();  // the next tile overwrites the shared tiles
     }
     if (!ok && t == 0) atomicExch(err, 1);
-    __syncthreads();
-    for (int i = t; i < kNumWeights; i += blockDim.x)
-        if (sm.dw[i] != 0.0f) atomicAdd(grads + i, sm.dw[i]);
+    // flush the weight-gradient accumulators: rows 0..63 (lanes of warps 0 and 1) = input units
+    if (ok && !first && t < 64)
+    {
+        const int offs[4] = {kOffW1, kOffW2, kOffW3, kOffW4};
+        for (int l = 0; l < 4; l++)
+        {
+            const int n_out = l == 3 ? kOut : kHid;
+            float v[16];
+            for (int c = 0; c < n_out; c += 16)
+            {
+                umma::tmem_ld16(umma::lane_addr(tmem, t >> 5, (int)col_dw(l) + c), v);
+                for (int j = 0; j < 16; j++)
+                    if (v[j] != 0.0f) atomicAdd(grads + offs[l] + t * n_out + c + j, v[j]);
+            }
+        }
+    }
     for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
     if ((t & 31) == 0 && loss_acc != 0.0f) atomicAdd(loss, loss_acc);
-    teardown(sm);
+    umma::fence_before();
+    __syncthreads();
+    if (t < 32) umma::tmem_dealloc(tmem, kTmemTrain);
 }
 
 // ---------------------------------------------------------------------------------------------
-// inference: mixture per query (8 x (mu xyz, kappa, weight))
+// inference: mixture per query (8 x (mu xyz, kappa, weight), alpha, 3 zeros)
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTile) infer_kernel(Net net, Batch b, float* __restrict__ lobes_out, int* err)
+__global__ void __launch_bounds__(kTile) infer_kernel(Net net, Batch b, float* __restrict__ out, int* err)
 {
-    const int64_t n = batch_size(b);
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+    SmemInfer& sm = *reinterpret_cast<SmemInfer*>(smem_raw);
     const int t = threadIdx.x;
-    copy_weights(sm, net.packed);
-    setup(sm);
+    const int64_t n = batch_size(b);
+    copy_weights(sm.w, net.packed, kFwdWeights);
+    if (t < 32) umma::tmem_alloc(&sm.tmem, kTmemInfer);
+    if (t == 0) umma::mbar_init(&sm.mbar);
     publish_smem();
+    const uint32_t tmem = sm.tmem;
     uint32_t phase = 0;
     bool ok = true;
     const int64_t n_tiles = (n + kTile - 1) / kTile;
@@ -273,28 +317,36 @@ __global__ void __launch_bounds__(kTile) infer_kernel(Net net, Batch b, float* _
             vw = load3(b.view, row);
         }
         float raw[kOut];
-        uint32_t m1[2], m2[2];
-        ok = forward_tile(sm, net, valid, p, nn, vw, raw, m1, m2, phase);
+        ok = forward_tile(&sm.mbar, tmem, sm.w, sm.act, nullptr, net, valid, p, nn, vw, raw, nullptr, phase);
         if (!ok) break;
         if (valid)
         {
             Lobe L[kLobes];
-            float len[kLobes];
-            head(raw, L, len);
-            float* o = lobes_out + 40 * row;
-            for (int i = 0; i < kLobes; i++)
+            float len[kLobes], alpha;
+            head(raw, L, len, alpha);
+            float4* o = reinterpret_cast<float4*>(out + (int64_t)kRow * row);
+            for (int i = 0; i < kLobes; i += 4)
             {
-                o[5 * i] = L[i].mu.x;
-                o[5 * i + 1] = L[i].mu.y;
-                o[5 * i + 2] = L[i].mu.z;
-                o[5 * i + 3] = L[i].kappa;
-                o[5 * i + 4] = L[i].weight;
+                // lobes i..i+3 = 20 floats = 5 float4
+                float v[20];
+                for (int j = 0; j < 4; j++)
+                {
+                    v[5 * j] = L[i + j].mu.x;
+                    v[5 * j + 1] = L[i + j].mu.y;
+                    v[5 * j + 2] = L[i + j].mu.z;
+                    v[5 * j + 3] = L[i + j].kappa;
+                    v[5 * j + 4] = L[i + j].weight;
+                }
+                for (int q = 0; q < 5; q++) o[(5 * i) / 4 + q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
             }
+            o[10] = make_float4(alpha, 0.0f, 0.0f, 0.0f);
         }
         __syncthreads();
     }
     if (!ok && t == 0) atomicExch(err, 1);
-    teardown(sm);
+    umma::fence_before();
+    __syncthreads();
+    if (t < 32) umma::tmem_dealloc(tmem, kTmemInfer);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -314,13 +366,11 @@ __device__ __forceinline__ float hash_uniform(uint32_t i, uint32_t seed)
 // Glorot-uniform weights, grid features uniform in [-1e-4, 1e-4]
 __global__ void init_kernel(float* params, uint32_t seed)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += gridDim.x * blockDim.x)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += (int64_t)gridDim.x * blockDim.x)
     {
         const float u = 2.0f * hash_uniform((uint32_t)i, seed) - 1.0f;
         float s;
-        if (i < kOffW2)
-            s = sqrtf(6.0f / (kIn + kHid));
-        else if (i < kOffW3)
+        if (i < kOffW4)
             s = sqrtf(6.0f / (kHid + kHid));
         else if (i < kNumWeights)
             s = sqrtf(6.0f / (kHid + kOut));
@@ -330,36 +380,34 @@ __global__ void init_kernel(float* params, uint32_t seed)
     }
 }
 
-__global__ void pack_kernel(const float* __restrict__ params, __nv_bfloat16* __restrict__ packed)
+__global__ void pack_kernel(const float* __restrict__ params, bf16* __restrict__ packed, uint32_t* __restrict__ grid_bf16)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNumWeights; i += gridDim.x * blockDim.x)
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kNumWeights; i += stride)
     {
-        const __nv_bfloat16 v = __float2bfloat16(params[i]);
-        if (i < kOffW2)
-        {
-            const int a = i / kHid, b = i % kHid;  // W1[a in 32][b out 64]
-            packed[kW1f + kmo(b, a, kIn)] = v;
-            packed[kW1b + kmo(a, b, kHid)] = v;
-        }
-        else if (i < kOffW3)
-        {
-            const int j = i - kOffW2, a = j / kHid, b = j % kHid;  // W2[a][b]
-            packed[kW2f + kmo(b, a, kHid)] = v;
-            packed[kW2b + kmo(a, b, kHid)] = v;
-        }
-        else
-        {
-            const int j = i - kOffW3, a = j / kOut, b = j % kOut;  // W3[a in 64][b out 48]
-            packed[kW3f + kmo(b, a, kHid)] = v;
-            packed[kW3b + kmo(a, b, kOut)] = v;
-        }
+        const bf16 v = __float2bfloat16(params[i]);
+        const int l = i < kOffW4 ? (int)(i / (kHid * kHid)) : 3;
+        const int base = l == 3 ? kOffW4 : l * kHid * kHid;
+        const int n_out = l == 3 ? kOut : kHid;
+        const int j = (int)i - base, a = j / n_out, o = j % n_out;  // W_l[a = input][o = output]
+        const int fwd[4] = {kW1f, kW2f, kW3f, kW4f}, bwd[4] = {kW1b, kW2b, kW3b, kW4b};
+        packed[fwd[l] + kmo(o, a, kHid)] = v;   // W^T: row = output, K = input (64)
+        packed[bwd[l] + kmo(a, o, n_out)] = v;  // W: row = input, K = output
+    }
+    const float2* g = reinterpret_cast<const float2*>(params + kNumWeights);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)kLevels * kTable; i += stride)
+    {
+        const float2 v = g[i];
+        const uint32_t lo = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v.x));
+        const uint32_t hi = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v.y));
+        grid_bf16[i] = lo | (hi << 16);
     }
 }
 
 __global__ void adam_kernel(float* __restrict__ params, const float* __restrict__ grads, float* __restrict__ m,
                             float* __restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += gridDim.x * blockDim.x)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += (int64_t)gridDim.x * blockDim.x)
     {
         const float g = grads[i];
         const float mi = b1 * m[i] + (1.0f - b1) * g;
@@ -385,13 +433,13 @@ __global__ void weight_sum_kernel(Batch b, float* __restrict__ out)
 
 cudaError_t launch_guide_init(float* params, uint32_t seed, cudaStream_t st)
 {
-    init_kernel<<<512, 256, 0, st>>>(params, seed);
+    init_kernel<<<2048, 256, 0, st>>>(params, seed);
     return cudaGetLastError();
 }
 
-cudaError_t launch_guide_pack(const float* params, uint16_t* packed, cudaStream_t st)
+cudaError_t launch_guide_pack(const float* params, uint16_t* packed, uint32_t* grid_bf16, cudaStream_t st)
 {
-    pack_kernel<<<(kNumWeights + 255) / 256, 256, 0, st>>>(params, reinterpret_cast<__nv_bfloat16*>(packed));
+    pack_kernel<<<2048, 256, 0, st>>>(params, reinterpret_cast<bf16*>(packed), grid_bf16);
     return cudaGetLastError();
 }
 
@@ -412,13 +460,13 @@ cudaError_t launch_guide_train(const Net& net, const Batch& b, const float* weig
     static bool attr_set = false;
     if (!attr_set)
     {
-        cudaError_t e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTrain);
+        cudaError_t e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemTrain));
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     const int64_t tiles = (b.n_max + kTile - 1) / kTile;
     const int grid = (int)(tiles < n_sm ? (tiles < 1 ? 1 : tiles) : n_sm);
-    train_kernel<<<grid, kTile, kSmemTrain, st>>>(net, b, weight_sum, grads, loss, err);
+    train_kernel<<<grid, kTile, sizeof(SmemTrain), st>>>(net, b, weight_sum, grads, loss, err);
     return cudaGetLastError();
 }
 
@@ -427,14 +475,14 @@ cudaError_t launch_guide_infer(const Net& net, const Batch& b, float* lobes, int
     static bool attr_set = false;
     if (!attr_set)
     {
-        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemInfer);
+        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemInfer));
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     const int64_t tiles = (b.n_max + kTile - 1) / kTile;
-    const int64_t cap = (int64_t)n_sm * 2;
+    const int64_t cap = (int64_t)n_sm * 3;  // three 62 KB CTAs fit one SM
     const int grid = (int)(tiles < cap ? (tiles < 1 ? 1 : tiles) : cap);
-    infer_kernel<<<grid, kTile, kSmemInfer, st>>>(net, b, lobes, err);
+    infer_kernel<<<grid, kTile, sizeof(SmemInfer), st>>>(net, b, lobes, err);
     return cudaGetLastError();
 }
 
@@ -442,7 +490,7 @@ cudaError_t launch_guide_adam(float* params, const float* grads, float* m, float
                               float eps, int step, cudaStream_t st)
 {
     const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
-    adam_kernel<<<1024, 256, 0, st>>>(params, grads, m, v, lr, beta1, beta2, eps, c1, c2);
+    adam_kernel<<<2048, 256, 0, st>>>(params, grads, m, v, lr, beta1, beta2, eps, c1, c2);
     return cudaGetLastError();
 }
 

@@ -23,6 +23,7 @@ struct gbpt_guide
     float* m = nullptr;
     float* v = nullptr;
     uint16_t* packed = nullptr;
+    uint32_t* grid_bf16 = nullptr;
     float* scratch = nullptr;  // [weight sum, loss]
     int* err = nullptr;
     int step = 0;
@@ -36,6 +37,7 @@ G::Net net_of(const gbpt_guide* g)
     G::Net n;
     n.params = g->params;
     n.packed = g->packed;
+    n.grid_bf16 = g->grid_bf16;
     for (int a = 0; a < 3; a++)
     {
         n.lo[a] = g->p.scene_min[a];
@@ -52,6 +54,7 @@ void release(gbpt_guide* g)
     cudaFree(g->m);
     cudaFree(g->v);
     cudaFree(g->packed);
+    cudaFree(g->grid_bf16);
     cudaFree(g->scratch);
     cudaFree(g->err);
 }
@@ -66,7 +69,8 @@ gbpt_status check_err(gbpt_guide* g, cudaStream_t cs)
     return GBPT_OK;
 }
 
-G::Batch host_batch(const float* pos, const float* nrm, const float* view, const float* dir, const float* w, int64_t n)
+G::Batch host_batch(const float* pos, const float* nrm, const float* view, const float* dir, const float* w,
+                    const float* bsdf_pdf, int64_t n)
 {
     G::Batch b;
     b.pos = pos;
@@ -74,6 +78,7 @@ G::Batch host_batch(const float* pos, const float* nrm, const float* view, const
     b.view = view;
     b.dir = dir;
     b.weight = w;
+    b.bsdf_pdf = bsdf_pdf;
     b.count = nullptr;
     b.n_max = n;
     return b;
@@ -98,7 +103,7 @@ gbpt_status adam_step(gbpt_guide* g, cudaStream_t cs)
     g->step++;
     cudaError_t e = G::launch_guide_adam(g->params, g->grads, g->m, g->v, g->p.learning_rate, g->p.beta1, g->p.beta2,
                                          g->p.epsilon, g->step, cs);
-    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, cs);
+    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, g->grid_bf16, cs);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide update");
 }
 
@@ -115,7 +120,7 @@ gbpt_status gbpt_guide_default_params(gbpt_guide_params* p)
         p->scene_min[a] = 0.0f;
         p->scene_max[a] = 1.0f;
     }
-    p->learning_rate = 5.0e-3f;
+    p->learning_rate = 1.0e-2f;
     p->beta1 = 0.9f;
     p->beta2 = 0.99f;
     p->epsilon = 1.0e-8f;
@@ -143,13 +148,14 @@ gbpt_status gbpt_guide_create(const gbpt_guide_params* p, gbpt_guide** out)
     if (e == cudaSuccess) e = cudaMalloc(&g->m, np);
     if (e == cudaSuccess) e = cudaMalloc(&g->v, np);
     if (e == cudaSuccess) e = cudaMalloc(&g->packed, sizeof(uint16_t) * G::kPackedWeights);
+    if (e == cudaSuccess) e = cudaMalloc(&g->grid_bf16, sizeof(uint32_t) * GBPT_GUIDE_LEVELS * GBPT_GUIDE_TABLE);
     if (e == cudaSuccess) e = cudaMalloc(&g->scratch, 2 * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&g->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(g->m, 0, np);
     if (e == cudaSuccess) e = cudaMemset(g->v, 0, np);
     if (e == cudaSuccess) e = cudaMemset(g->err, 0, sizeof(int));
     if (e == cudaSuccess) e = G::launch_guide_init(g->params, p->seed, nullptr);
-    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, nullptr);
+    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, g->grid_bf16, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess)
     {
@@ -170,11 +176,12 @@ gbpt_status gbpt_guide_destroy(gbpt_guide* g)
 }
 
 gbpt_status gbpt_guide_train(gbpt_guide* g, const float* position, const float* normal, const float* view,
-                             const float* direction, const float* weight, int64_t n, float* loss, void* stream)
+                             const float* direction, const float* weight, const float* bsdf_pdf, int64_t n, float* loss,
+                             void* stream)
 {
     if (!g) return set_error(GBPT_ERROR_INVALID_ARG, "guide is NULL");
     cudaStream_t cs = (cudaStream_t)stream;
-    gbpt_status st = compute_gradients(g, host_batch(position, normal, view, direction, weight, n), cs);
+    gbpt_status st = compute_gradients(g, host_batch(position, normal, view, direction, weight, bsdf_pdf, n), cs);
     if (st != GBPT_OK) return st;
     if (loss)
     {
@@ -188,12 +195,12 @@ gbpt_status gbpt_guide_train(gbpt_guide* g, const float* position, const float* 
 }
 
 gbpt_status gbpt_guide_gradients(gbpt_guide* g, const float* position, const float* normal, const float* view,
-                                 const float* direction, const float* weight, int64_t n, float* grad_weights,
-                                 float* grad_grid, float* loss, void* stream)
+                                 const float* direction, const float* weight, const float* bsdf_pdf, int64_t n,
+                                 float* grad_weights, float* grad_grid, float* loss, void* stream)
 {
     if (!g) return set_error(GBPT_ERROR_INVALID_ARG, "guide is NULL");
     cudaStream_t cs = (cudaStream_t)stream;
-    gbpt_status st = compute_gradients(g, host_batch(position, normal, view, direction, weight, n), cs);
+    gbpt_status st = compute_gradients(g, host_batch(position, normal, view, direction, weight, bsdf_pdf, n), cs);
     if (st != GBPT_OK) return st;
     cudaError_t e = cudaSuccess;
     if (grad_weights)
@@ -213,7 +220,7 @@ gbpt_status gbpt_guide_infer(gbpt_guide* g, const float* position, const float* 
     if (n < 0) return set_error(GBPT_ERROR_INVALID_ARG, "n is negative");
     if (n == 0) return GBPT_OK;
     if (!position || !normal || !view || !lobes) return set_error(GBPT_ERROR_INVALID_ARG, "arrays must be device pointers");
-    cudaError_t e = G::launch_guide_infer(net_of(g), host_batch(position, normal, view, nullptr, nullptr, n), lobes, g->err,
+    cudaError_t e = G::launch_guide_infer(net_of(g), host_batch(position, normal, view, nullptr, nullptr, nullptr, n), lobes, g->err,
                                           g->n_sm, (cudaStream_t)stream);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide inference launch");
 }
@@ -242,7 +249,7 @@ gbpt_status gbpt_guide_set_params(gbpt_guide* g, const float* weights, const flo
     if (weights) e = cudaMemcpy(g->params, weights, sizeof(float) * G::kNumWeights, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && grid)
         e = cudaMemcpy(g->params + G::kNumWeights, grid, sizeof(float) * GBPT_GUIDE_GRID_PARAMS, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, nullptr);
+    if (e == cudaSuccess) e = G::launch_guide_pack(g->params, g->packed, g->grid_bf16, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "guide parameter upload");
 }

@@ -1,8 +1,9 @@
-// Device math of the guiding network: hash-grid encoding, the vMF-mixture head (pdf, log-pdf
-// gradient, sampling), shared by the training / inference kernels (guide.cu) and the path
-// tracer's guided sampling (render.cu).
+// Device math of the guiding network: hash-grid encoding, spherical-harmonic encoding, the
+// vMF-mixture head (pdf, loss gradient, sampling), shared by the training / inference kernels
+// (guide.cu) and the path tracer's guided sampling (render.cu).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -21,13 +22,19 @@ constexpr int kIn = GBPT_GUIDE_IN;
 constexpr int kHid = GBPT_GUIDE_HIDDEN;
 constexpr int kOut = GBPT_GUIDE_OUT;
 constexpr int kLobes = GBPT_GUIDE_LOBES;
+constexpr int kRow = GBPT_GUIDE_ROW;
+constexpr int kGridFeatures = kLevels * kFeat;  // inputs 0..31
+constexpr int kNormalIn = kGridFeatures;        // inputs 32..34
+constexpr int kShIn = kNormalIn + 3;            // inputs 35..50
+constexpr int kAlphaOut = kLobes * 5;           // raw output 40
 constexpr float kKappaMin = 0.1f;
 constexpr float kKappaMax = 500.0f;
+constexpr float kAlphaMin = 0.05f;
 
-// resolutions floor(4 * 1.5^l)
+// resolutions floor(16 * 256^(l / 15)): 16 .. 4096, geometric
 __host__ __device__ __forceinline__ int level_res(int l)
 {
-    const int r[8] = {4, 6, 9, 13, 20, 30, 45, 68};
+    const int r[16] = {16, 23, 33, 48, 70, 101, 147, 212, 307, 445, 645, 933, 1351, 1955, 2830, 4096};
     return r[l];
 }
 
@@ -44,90 +51,124 @@ struct Domain
     float lo[3], inv_ext[3];
 };
 
-// Trilinear hash-grid lookup: 16 features of point p (in scene coordinates)
-__device__ __forceinline__ void encode(const Domain& d, const float* __restrict__ grid, V3 p, float* feat)
+// Cell of point u (unit-box coordinates) at a level: lower corner and fractional position
+__device__ __forceinline__ void level_cell(const float* u, int res, uint32_t* i0, float* f)
 {
-    const float u[3] = {clampf(0.0f, 1.0f, (p.x - d.lo[0]) * d.inv_ext[0]), clampf(0.0f, 1.0f, (p.y - d.lo[1]) * d.inv_ext[1]),
-                        clampf(0.0f, 1.0f, (p.z - d.lo[2]) * d.inv_ext[2])};
 #pragma unroll
+    for (int a = 0; a < 3; a++)
+    {
+        const float x = u[a] * (float)res;
+        int xi = (int)floorf(x);
+        xi = xi < 0 ? 0 : (xi > res - 1 ? res - 1 : xi);
+        i0[a] = (uint32_t)xi;
+        f[a] = x - (float)xi;
+    }
+}
+
+__device__ __forceinline__ void unit_coords(const Domain& d, V3 p, float* u)
+{
+    u[0] = clampf(0.0f, 1.0f, (p.x - d.lo[0]) * d.inv_ext[0]);
+    u[1] = clampf(0.0f, 1.0f, (p.y - d.lo[1]) * d.inv_ext[1]);
+    u[2] = clampf(0.0f, 1.0f, (p.z - d.lo[2]) * d.inv_ext[2]);
+}
+
+__device__ __forceinline__ float corner_weight(int c, const float* f)
+{
+    return ((c & 1) ? f[0] : 1.0f - f[0]) * ((c & 2) ? f[1] : 1.0f - f[1]) * ((c & 4) ? f[2] : 1.0f - f[2]);
+}
+
+// Trilinear hash-grid lookup through the BF16 copy of the features (2 per entry in one 32-bit
+// word, feature 0 in the low half): 32 features of point p (scene coordinates)
+__device__ __forceinline__ void encode(const Domain& d, const uint32_t* __restrict__ grid_bf16, V3 p, float* feat)
+{
+    float u[3];
+    unit_coords(d, p, u);
+#pragma unroll 4
     for (int l = 0; l < kLevels; l++)
     {
         const int res = level_res(l);
         uint32_t i0[3];
         float f[3];
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-        {
-            const float x = u[a] * (float)res;
-            int xi = (int)floorf(x);
-            xi = xi < 0 ? 0 : (xi > res - 1 ? res - 1 : xi);
-            i0[a] = (uint32_t)xi;
-            f[a] = x - (float)xi;
-        }
+        level_cell(u, res, i0, f);
         float f0 = 0.0f, f1 = 0.0f;
+        const uint32_t* g = grid_bf16 + (size_t)l * kTable;
 #pragma unroll
         for (int c = 0; c < 8; c++)
         {
-            const float w = ((c & 1) ? f[0] : 1.0f - f[0]) * ((c & 2) ? f[1] : 1.0f - f[1]) * ((c & 4) ? f[2] : 1.0f - f[2]);
+            const float w = corner_weight(c, f);
             const uint32_t s = grid_slot(res, i0[0] + (c & 1), i0[1] + ((c >> 1) & 1), i0[2] + ((c >> 2) & 1));
-            const float2 g = *reinterpret_cast<const float2*>(grid + ((size_t)l * kTable + s) * kFeat);
-            f0 += w * g.x;
-            f1 += w * g.y;
+            const uint32_t v = __ldg(g + s);
+            f0 += w * __uint_as_float(v << 16);
+            f1 += w * __uint_as_float(v & 0xFFFF0000u);
         }
         feat[2 * l] = f0;
         feat[2 * l + 1] = f1;
     }
 }
 
-// Scatters d(loss)/d(features) back to the grid with the same trilinear weights
+// Scatters d(loss)/d(features) to the FP32 grid gradient with the same trilinear weights
 __device__ __forceinline__ void encode_backward(const Domain& d, float* __restrict__ grad_grid, V3 p, const float* dfeat)
 {
-    const float u[3] = {clampf(0.0f, 1.0f, (p.x - d.lo[0]) * d.inv_ext[0]), clampf(0.0f, 1.0f, (p.y - d.lo[1]) * d.inv_ext[1]),
-                        clampf(0.0f, 1.0f, (p.z - d.lo[2]) * d.inv_ext[2])};
+    float u[3];
+    unit_coords(d, p, u);
     for (int l = 0; l < kLevels; l++)
     {
         if (dfeat[2 * l] == 0.0f && dfeat[2 * l + 1] == 0.0f) continue;
         const int res = level_res(l);
         uint32_t i0[3];
         float f[3];
-        for (int a = 0; a < 3; a++)
-        {
-            const float x = u[a] * (float)res;
-            int xi = (int)floorf(x);
-            xi = xi < 0 ? 0 : (xi > res - 1 ? res - 1 : xi);
-            i0[a] = (uint32_t)xi;
-            f[a] = x - (float)xi;
-        }
+        level_cell(u, res, i0, f);
+        float* gl = grad_grid + (size_t)l * kTable * kFeat;
         for (int c = 0; c < 8; c++)
         {
-            const float w = ((c & 1) ? f[0] : 1.0f - f[0]) * ((c & 2) ? f[1] : 1.0f - f[1]) * ((c & 4) ? f[2] : 1.0f - f[2]);
+            const float w = corner_weight(c, f);
             const uint32_t s = grid_slot(res, i0[0] + (c & 1), i0[1] + ((c >> 1) & 1), i0[2] + ((c >> 2) & 1));
-            float* g = grad_grid + ((size_t)l * kTable + s) * kFeat;
-            atomicAdd(g, w * dfeat[2 * l]);
-            atomicAdd(g + 1, w * dfeat[2 * l + 1]);
+            atomicAdd(gl + 2 * s, w * dfeat[2 * l]);
+            atomicAdd(gl + 2 * s + 1, w * dfeat[2 * l + 1]);
         }
     }
 }
 
-// Network input row: 16 grid features, the normal, a constant 1 (the bias input), the direction
-// towards the viewer (outgoing direction of the shading point), zeros
+// Real spherical harmonics of bands 0..3 (16 values) of a unit vector, orthonormal on the sphere:
+// normalisation sqrt((2l+1)/(4 pi) (l-|m|)!/(l+|m|)!), times sqrt(2) for m != 0, no
+// Condon-Shortley phase; the polynomials are the Cartesian forms of the associated Legendre
+// functions of z times cos / sin of m phi.
+__host__ __device__ __forceinline__ void sh16(float x, float y, float z, float* o)
+{
+    const float xx = x * x, yy = y * y, zz = z * z;
+    o[0] = 0.28209479177387814f;
+    o[1] = 0.48860251190291992f * y;
+    o[2] = 0.48860251190291992f * z;
+    o[3] = 0.48860251190291992f * x;
+    o[4] = 1.0925484305920792f * x * y;
+    o[5] = 1.0925484305920792f * y * z;
+    o[6] = 0.31539156525252005f * (3.0f * zz - 1.0f);
+    o[7] = 1.0925484305920792f * x * z;
+    o[8] = 0.54627421529603959f * (xx - yy);
+    o[9] = 0.59004358992664352f * y * (3.0f * xx - yy);
+    o[10] = 2.8906114426405538f * x * y * z;
+    o[11] = 0.45704579946446572f * y * (5.0f * zz - 1.0f);
+    o[12] = 0.37317633259011546f * z * (5.0f * zz - 3.0f);
+    o[13] = 0.45704579946446572f * x * (5.0f * zz - 1.0f);
+    o[14] = 1.4453057213202769f * z * (xx - yy);
+    o[15] = 0.59004358992664352f * x * (xx - 3.0f * yy);
+}
+
+// Network input row: 32 grid features, the normal, SH16 of the view direction, zeros
 __device__ __forceinline__ void input_row(const float* feat, V3 n, V3 view, float* x)
 {
 #pragma unroll
-    for (int i = 0; i < 16; i++) x[i] = feat[i];
-    x[16] = n.x;
-    x[17] = n.y;
-    x[18] = n.z;
-    x[19] = 1.0f;
-    x[20] = view.x;
-    x[21] = view.y;
-    x[22] = view.z;
+    for (int i = 0; i < kGridFeatures; i++) x[i] = feat[i];
+    x[kNormalIn] = n.x;
+    x[kNormalIn + 1] = n.y;
+    x[kNormalIn + 2] = n.z;
+    sh16(view.x, view.y, view.z, x + kShIn);
 #pragma unroll
-    for (int i = 23; i < kIn; i++) x[i] = 0.0f;
+    for (int i = kShIn + 16; i < kIn; i++) x[i] = 0.0f;
 }
 
-__device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
-__device__ __forceinline__ float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }
+__host__ __device__ __forceinline__ float softplus(float x) { return x > 20.0f ? x : log1pf(expf(x)); }
+__host__ __device__ __forceinline__ float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }
 
 struct Lobe
 {
@@ -135,9 +176,10 @@ struct Lobe
     float kappa, weight;
 };
 
-// Mixture from the 48 raw outputs: lobe i from raw[5i..5i+4] (direction xyz, concentration,
-// weight logit). Also returns the norms of the raw directions (for the backward pass).
-__device__ __forceinline__ void head(const float* raw, Lobe* lobes, float* dir_len)
+// Mixture from the raw outputs: lobe i from raw[5i..5i+4] (direction xyz, concentration, weight
+// logit); also the norms of the raw directions (for the backward pass) and the probability of
+// sampling the mixture.
+__device__ __forceinline__ void head(const float* raw, Lobe* lobes, float* dir_len, float& alpha)
 {
     float mx = -1e30f;
 #pragma unroll
@@ -156,10 +198,11 @@ __device__ __forceinline__ void head(const float* raw, Lobe* lobes, float* dir_l
     }
 #pragma unroll
     for (int i = 0; i < kLobes; i++) lobes[i].weight /= sum;
+    alpha = kAlphaMin + (1.0f - 2.0f * kAlphaMin) * sigmoid(raw[kAlphaOut]);
 }
 
 // log of the vMF density kappa / (2 pi (1 - e^{-2 kappa})) exp(kappa (mu.w - 1))
-__device__ __forceinline__ float log_vmf(float kappa, float c)
+__host__ __device__ __forceinline__ float log_vmf(float kappa, float c)
 {
     return logf(kappa) - 1.8378770664093453f - log1pf(-expf(-2.0f * kappa)) + kappa * (c - 1.0f);
 }
@@ -171,9 +214,12 @@ __device__ __forceinline__ float mixture_pdf(const Lobe* lobes, V3 w)
     return q;
 }
 
-// d(-scale * log q(w))/d(raw) for the 48 raw outputs; returns log q.
-__device__ __forceinline__ float head_backward(const float* raw, const Lobe* lobes, const float* dir_len, V3 w, float scale,
-                                               float* draw)
+// Gradient of the sample's loss with respect to the 48 raw outputs, scale = w / sum(w):
+//   -scale log q(w)                                    -> lobe outputs 0..39
+//   -scale log(alpha q + (1 - alpha) p_bsdf), q fixed  -> output 40 (only when p_bsdf >= 0)
+// Returns the sample's loss.
+__device__ __forceinline__ float head_backward(const float* raw, const Lobe* lobes, const float* dir_len, float alpha, V3 w,
+                                               float scale, float p_bsdf, float* draw)
 {
     float lv[kLobes];
     float mx = -1e30f;
@@ -204,7 +250,19 @@ __device__ __forceinline__ float head_backward(const float* raw, const Lobe* lob
         draw[5 * i + 1] = -scale * gm.y;
         draw[5 * i + 2] = -scale * gm.z;
     }
-    return logq;
+    float loss = -scale * logq;
+    if (p_bsdf >= 0.0f && scale > 0.0f)
+    {
+        const float q = expf(logq);
+        const float c = alpha * q + (1.0f - alpha) * p_bsdf;
+        if (c > 0.0f)
+        {
+            const float sg = sigmoid(raw[kAlphaOut]);
+            draw[kAlphaOut] = -scale * (q - p_bsdf) / c * (1.0f - 2.0f * kAlphaMin) * sg * (1.0f - sg);
+            loss += -scale * logf(c);
+        }
+    }
+    return loss;
 }
 
 // Samples a vMF lobe with two uniforms (Jakob's numerically stable inversion of the cosine to
@@ -215,7 +273,8 @@ __device__ __forceinline__ V3 sample_vmf(V3 mu, float k, float u1, float u2)
     const float r = sqrtf(fmaxf(0.0f, 1.0f - wz * wz));
     float sn, cs;
     sincosf(kTwoPi * u2, &sn, &cs);
-    // frame around mu (Frisvad / Max)
+    // frame around mu (Frisvad, "Building an orthonormal basis from a 3D unit vector without
+    // normalization", 2012)
     const V3 n = mu;
     V3 t, b;
     if (n.z < -0.99998796f)
@@ -232,25 +291,8 @@ __device__ __forceinline__ V3 sample_vmf(V3 mu, float k, float u1, float u2)
     return normalize(t * (r * cs) + b * (r * sn) + n * wz);
 }
 
-// Samples a direction from the mixture with three uniforms: the lobe by u0, then the lobe's vMF
-__device__ __forceinline__ V3 sample_mixture(const Lobe* lobes, float u0, float u1, float u2)
-{
-    int pick = kLobes - 1;
-    float acc = 0.0f;
-    for (int i = 0; i < kLobes; i++)
-    {
-        acc += lobes[i].weight;
-        if (u0 < acc)
-        {
-            pick = i;
-            break;
-        }
-    }
-    return sample_vmf(lobes[pick].mu, lobes[pick].kappa, u1, u2);
-}
-
-// Mixture read from global memory one lobe at a time (the path tracer's per-entry lobes,
-// 8 x (mu xyz, kappa, weight)); keeps the 40 values out of registers.
+// Mixture of one inferred row read from global memory one lobe at a time (the path tracer's
+// per-entry rows: 8 x (mu xyz, kappa, weight), alpha); keeps the values out of registers.
 __device__ __forceinline__ float mixture_pdf_at(const float* __restrict__ L, V3 w)
 {
     float q = 0.0f;
@@ -264,6 +306,7 @@ __device__ __forceinline__ float mixture_pdf_at(const float* __restrict__ L, V3 
     return q;
 }
 
+// Samples the row's mixture with three uniforms: the lobe by u0, then the lobe's vMF
 __device__ __forceinline__ V3 sample_mixture_at(const float* __restrict__ L, float u0, float u1, float u2)
 {
     int pick = kLobes - 1;
@@ -280,6 +323,8 @@ __device__ __forceinline__ V3 sample_mixture_at(const float* __restrict__ L, flo
     const float* l = L + 5 * pick;
     return sample_vmf(v3(__ldg(l), __ldg(l + 1), __ldg(l + 2)), __ldg(l + 3), u1, u2);
 }
+
+__device__ __forceinline__ float alpha_at(const float* __restrict__ L) { return __ldg(L + kAlphaOut); }
 
 }  // namespace guide
 }  // namespace gbpt

@@ -114,6 +114,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
 
         bool want_shadow = false, want_bsdf = false, want_next = false, want_record = false;
         V3 rec_tp = v3(0.0f), rec_dir = v3(0.0f);
+        float rec_pb = 0.0f;
         float4 sh_o, sh_d, bs_d, nx_d;
         V3 P = v3(0, 0, 0), tp = v3(0, 0, 0);
         V3 light_contrib = v3(0, 0, 0);
@@ -194,12 +195,13 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 // one-sample MIS of the learned mixture and cosine sampling ----
                 if (bounce < rc.nb_bounces)
                 {
-                    const float* GL = gv.lobes ? gv.lobes + 40 * (int64_t)i : nullptr;
+                    const float* GL = gv.lobes ? gv.lobes + guide::kRow * (int64_t)i : nullptr;
                     V3 wi, f;
                     float pdf;
                     if (GL)
                     {
-                        if (rng.next() < gv.prob)
+                        const float alpha = gv.prob > 0.0f ? gv.prob : guide::alpha_at(GL);
+                        if (rng.next() < alpha)
                         {
                             const float u0 = rng.next(), u1 = rng.next(), u2 = rng.next();
                             wi = guide::sample_mixture_at(GL, u0, u1, u2);
@@ -211,7 +213,8 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                         }
                         float p_bsdf;
                         f = lambert_eval(albedo, dot(ns, wi), p_bsdf);
-                        pdf = is_black(f) ? 0.0f : gv.prob * guide::mixture_pdf_at(GL, wi) + (1.0f - gv.prob) * p_bsdf;
+                        pdf = is_black(f) ? 0.0f : alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * p_bsdf;
+                        rec_pb = p_bsdf;
                     }
                     else
                     {
@@ -363,14 +366,15 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 // one-sample MIS of the learned mixture and BSDF sampling ----
                 if (bounce < rc.nb_bounces)
                 {
-                    const float* GL = (gv.lobes && guidable(m)) ? gv.lobes + 40 * (int64_t)i : nullptr;
+                    const float* GL = (gv.lobes && guidable(m)) ? gv.lobes + guide::kRow * (int64_t)i : nullptr;
                     V3 wi, f;
                     int lobe = GBPT_LOBE_NONE;
                     float pdf;
                     if (GL)
                     {
+                        const float alpha = gv.prob > 0.0f ? gv.prob : guide::alpha_at(GL);
                         float p_bsdf;
-                        if (rng.next() < gv.prob)
+                        if (rng.next() < alpha)
                         {
                             const float u0 = rng.next(), u1 = rng.next(), u2 = rng.next();
                             wi = guide::sample_mixture_at(GL, u0, u1, u2);
@@ -388,7 +392,8 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                             bsdf::Xorshift32 xr = bsdf_rng(rng);
                             f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, p_bsdf);
                         }
-                        pdf = is_black(f) ? 0.0f : gv.prob * guide::mixture_pdf_at(GL, wi) + (1.0f - gv.prob) * p_bsdf;
+                        pdf = is_black(f) ? 0.0f : alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * p_bsdf;
+                        rec_pb = p_bsdf;
                     }
                     else
                     {
@@ -482,6 +487,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 gv.rec_dir[3 * ri + 1] = rec_dir.y;
                 gv.rec_dir[3 * ri + 2] = rec_dir.z;
                 gv.rec_tp[ri] = f4(rec_tp, 0.0f);
+                gv.rec_pbsdf[ri] = rec_pb;
                 gv.rec_slot[ri] = slot;
                 gv.train_entry[slot] = ri;
             }

@@ -732,6 +732,7 @@ gbpt_status gbpt_pass_accumulate(gbpt_renderer* r, void* stream)
             b.view = r->gv.rec_view;
             b.dir = r->gv.rec_dir;
             b.weight = r->gv.rec_weight;
+            b.bsdf_pdf = r->gv.rec_pbsdf;
             b.count = r->gv.rec_count;
             b.n_max = r->gv.rec_cap;
             gbpt_status st = gbpt::guide::render_train(r->guide, b, (cudaStream_t)stream);
@@ -861,8 +862,8 @@ gbpt_status gbpt_guide_render_default_settings(gbpt_guide_render_settings* s)
     std::memset(s, 0, sizeof(*s));
     s->enabled = 1;
     s->train = 1;
-    s->guide_probability = 0.5f;
-    s->max_records = 65536;
+    s->guide_probability = 0.0f;
+    s->max_records = 1 << 18;
     s->weight_clamp = 50.0f;
     return GBPT_OK;
 }
@@ -875,8 +876,8 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
     r->guide = nullptr;
     r->guide_lobes = nullptr;
     if (!g || !s || !s->enabled) return GBPT_OK;
-    if (!(s->guide_probability > 0.0f && s->guide_probability < 1.0f))
-        return set_error(GBPT_ERROR_INVALID_ARG, "guide_probability must be in (0, 1)");
+    if (!(s->guide_probability >= 0.0f && s->guide_probability < 1.0f))
+        return set_error(GBPT_ERROR_INVALID_ARG, "guide_probability must be in [0, 1)");
     if (s->train && (s->max_records < 1 || s->max_records > gbpt::guide::max_batch(g)))
         return set_error(GBPT_ERROR_INVALID_ARG, "max_records must be in 1..the guide's max_batch");
     if (s->weight_clamp < 0.0f) return set_error(GBPT_ERROR_INVALID_ARG, "weight_clamp is negative");
@@ -886,7 +887,7 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
     gv.in_pos = M.alloc<float>(3 * cap);
     gv.in_nrm = M.alloc<float>(3 * cap);
     gv.in_view = M.alloc<float>(3 * cap);
-    r->guide_lobes = M.alloc<float>(40 * cap);
+    r->guide_lobes = M.alloc<float>((int64_t)GBPT_GUIDE_ROW * cap);
     gv.prob = s->guide_probability;
     if (s->train)
     {
@@ -899,6 +900,7 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
         gv.rec_tp = M.alloc<float4>(nr);
         gv.rec_snap = M.alloc<float4>(nr);
         gv.rec_weight = M.alloc<float>(nr);
+        gv.rec_pbsdf = M.alloc<float>(nr);
         gv.rec_slot = M.alloc<int32_t>(nr);
         gv.rec_count = M.alloc<int32_t>(1);
         gv.rec_cap = s->max_records;
@@ -936,18 +938,19 @@ gbpt_status gbpt_renderer_get_guide_records(gbpt_renderer* r, float* host_out, i
     *count = n;
     const int64_t k = std::min<int64_t>(std::min<int64_t>(n, r->gv.rec_cap), capacity > 0 ? capacity : 0);
     if (!host_out || k == 0) return GBPT_OK;
-    std::vector<float> p(3 * k), nr(3 * k), v(3 * k), d(3 * k), w(k);
+    std::vector<float> p(3 * k), nr(3 * k), v(3 * k), d(3 * k), w(k), pb(k);
     std::vector<int32_t> sl(k);
     e = cudaMemcpy(p.data(), r->gv.rec_pos, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(nr.data(), r->gv.rec_nrm, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(v.data(), r->gv.rec_view, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(d.data(), r->gv.rec_dir, 3 * k * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(w.data(), r->gv.rec_weight, k * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(pb.data(), r->gv.rec_pbsdf, k * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(sl.data(), r->gv.rec_slot, k * sizeof(int32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_error(e, "record read-back");
     for (int64_t i = 0; i < k; i++)
     {
-        float* o = host_out + 14 * i;
+        float* o = host_out + 15 * i;
         for (int a = 0; a < 3; a++)
         {
             o[a] = p[3 * i + a];
@@ -956,7 +959,8 @@ gbpt_status gbpt_renderer_get_guide_records(gbpt_renderer* r, float* host_out, i
             o[9 + a] = d[3 * i + a];
         }
         o[12] = w[i];
-        std::memcpy(o + 13, &sl[i], sizeof(int32_t));
+        o[13] = pb[i];
+        std::memcpy(o + 14, &sl[i], sizeof(int32_t));
     }
     return GBPT_OK;
 }

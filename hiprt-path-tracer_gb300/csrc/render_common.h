@@ -70,14 +70,15 @@ struct PathBuffers
 
 // Learned path guiding in the wavefront (all device pointers; lobes == nullptr: guiding off).
 // The continuation of a guidable vertex is drawn from the network's vMF mixture with probability
-// 'prob', else from the BSDF, and weighted by the one-sample MIS pdf prob q + (1 - prob) p_bsdf.
+// alpha (the network's selection output, or 'prob' when that is > 0), else from the BSDF, and
+// weighted by the one-sample MIS pdf alpha q + (1 - alpha) p_bsdf.
 // Training records hold (position, normal, view, sampled direction), the throughput before the
 // continuation and the path radiance after this vertex's direct lighting; after the launch the
 // record's weight is luminance((final radiance - snapshot) / throughput), the estimate of
 // f cos L_i / pdf of the sampled direction.
 struct GuideView
 {
-    const float* lobes;  // per entry of the shaded queue: 8 x (mu xyz, kappa, weight)
+    const float* lobes;  // per entry of the shaded queue: 8 x (mu xyz, kappa, weight), alpha
     float* in_pos;       // per queue entry: network inputs (3 floats each)
     float* in_nrm;
     float* in_view;
@@ -90,6 +91,7 @@ struct GuideView
     float4* rec_tp;
     float4* rec_snap;
     float* rec_weight;
+    float* rec_pbsdf;  // BSDF pdf of the recorded direction (trains the selection probability)
     int32_t* rec_slot;
     int32_t* rec_count;
     int32_t rec_cap;

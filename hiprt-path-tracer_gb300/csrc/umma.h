@@ -78,13 +78,27 @@ __device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t adesc, uint64_t bd
                  "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate ? 1 : 0));
 }
 
-// D(128 x N) = A(128 x K) * B(N x K)^T over all K / 16 steps, then commit to 'mbar'. One thread.
+// D(128 x N) (+)= A(128 x K) * B(N x K)^T over all K / 16 steps; accumulate = false overwrites D.
+// One thread.
+__device__ __forceinline__ void gemm_issue(uint32_t tmem_d, const __nv_bfloat16* A, const __nv_bfloat16* B, int N, int K,
+                                           bool accumulate)
+{
+    const uint32_t id = idesc_bf16(128, N);
+    for (int ks = 0; ks < K / 16; ks++) mma(tmem_d, tile_desc(A, K, ks), tile_desc(B, K, ks), id, accumulate || ks > 0);
+}
+
+// Arrives on 'mbar' once every MMA issued so far by this thread has completed
+__device__ __forceinline__ void commit(uint64_t* mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar)));
+}
+
+// D(128 x N) = A(128 x K) * B(N x K)^T, then commit to 'mbar'. One thread.
 __device__ __forceinline__ void gemm_commit(uint32_t tmem_d, const __nv_bfloat16* A, const __nv_bfloat16* B, int N, int K,
                                             uint64_t* mbar)
 {
-    const uint32_t id = idesc_bf16(128, N);
-    for (int ks = 0; ks < K / 16; ks++) mma(tmem_d, tile_desc(A, K, ks), tile_desc(B, K, ks), id, ks > 0);
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar)));
+    gemm_issue(tmem_d, A, B, N, K, false);
+    commit(mbar);
 }
 
 // Waits for the mbarrier phase 'parity' with at most 'limit' polls; false if it gave up.

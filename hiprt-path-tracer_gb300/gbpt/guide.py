@@ -18,10 +18,10 @@ i32 = ctypes.c_int32
 u32 = ctypes.c_uint32
 i64 = ctypes.c_int64
 
-LEVELS, TABLE, FEATURES = 8, 32768, 2
+LEVELS, TABLE, FEATURES = 16, 524288, 2
 GRID_PARAMS = LEVELS * TABLE * FEATURES
-IN, HIDDEN, OUT, LOBES = 32, 64, 48, 8
-WEIGHTS = IN * HIDDEN + HIDDEN * HIDDEN + HIDDEN * OUT
+IN, HIDDEN, OUT, LOBES, ROW = 64, 64, 48, 8, 44
+WEIGHTS = 3 * HIDDEN * HIDDEN + HIDDEN * OUT
 
 
 class GuideParams(ctypes.Structure):
@@ -34,8 +34,8 @@ GUIDE_SIGNATURES = [
     ("gbpt_guide_default_params", ctypes.c_int, [ctypes.POINTER(GuideParams)]),
     ("gbpt_guide_create", ctypes.c_int, [ctypes.POINTER(GuideParams), ctypes.POINTER(c_vp)]),
     ("gbpt_guide_destroy", ctypes.c_int, [c_vp]),
-    ("gbpt_guide_train", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_vp]),
-    ("gbpt_guide_gradients", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_f, c_f, c_vp]),
+    ("gbpt_guide_train", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_vp]),
+    ("gbpt_guide_gradients", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, i64, c_f, c_f, c_f, c_vp]),
     ("gbpt_guide_infer", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, c_vp, c_vp]),
     ("gbpt_guide_error_flag", ctypes.c_int, [c_vp, ctypes.POINTER(i32)]),
     ("gbpt_guide_get_params", ctypes.c_int, [c_vp, c_f, c_f]),
@@ -63,6 +63,11 @@ def default_params(**kw) -> GuideParams:
         else:
             setattr(p, k, v)
     return p
+
+
+def split_rows(rows):
+    """(n, ROW) inferred rows -> lobes (n, 8, 5) and alpha (n,) views."""
+    return rows[:, :LOBES * 5].reshape(-1, LOBES, 5), rows[:, LOBES * 5]
 
 
 def _fptr(a: np.ndarray):
@@ -108,35 +113,37 @@ class Guide:
     def handle(self):
         return self._h
 
-    def train(self, position, normal, view, direction, weight, want_loss=True, stream=None):
+    def train(self, position, normal, view, direction, weight, bsdf_pdf=None, want_loss=True, stream=None):
         n = weight.numel()
         pos, nrm, v, d, w = (_dev(position, 3 * n), _dev(normal, 3 * n), _dev(view, 3 * n), _dev(direction, 3 * n),
                              _dev(weight, n))
+        pb = None if bsdf_pdf is None else _dev(bsdf_pdf, n)
         loss = ctypes.c_float(0.0)
         _lib.check(self._lib.gbpt_guide_train(self._h, pos.data_ptr(), nrm.data_ptr(), v.data_ptr(), d.data_ptr(),
-                                              w.data_ptr(), n, ctypes.byref(loss) if want_loss else None,
-                                              _stream(stream)))
+                                              w.data_ptr(), None if pb is None else pb.data_ptr(), n,
+                                              ctypes.byref(loss) if want_loss else None, _stream(stream)))
         return loss.value if want_loss else None
 
-    def gradients(self, position, normal, view, direction, weight, stream=None):
+    def gradients(self, position, normal, view, direction, weight, bsdf_pdf=None, stream=None):
         """-> (grad_weights (WEIGHTS,), grad_grid (GRID_PARAMS,), loss) as numpy float32."""
         n = weight.numel()
         pos, nrm, v, d, w = (_dev(position, 3 * n), _dev(normal, 3 * n), _dev(view, 3 * n), _dev(direction, 3 * n),
                              _dev(weight, n))
+        pb = None if bsdf_pdf is None else _dev(bsdf_pdf, n)
         gw = np.zeros(WEIGHTS, np.float32)
         gg = np.zeros(GRID_PARAMS, np.float32)
         loss = ctypes.c_float(0.0)
         _lib.check(self._lib.gbpt_guide_gradients(self._h, pos.data_ptr(), nrm.data_ptr(), v.data_ptr(), d.data_ptr(),
-                                                  w.data_ptr(), n, _fptr(gw), _fptr(gg), ctypes.byref(loss),
-                                                  _stream(stream)))
+                                                  w.data_ptr(), None if pb is None else pb.data_ptr(), n, _fptr(gw),
+                                                  _fptr(gg), ctypes.byref(loss), _stream(stream)))
         return gw, gg, loss.value
 
     def infer(self, position, normal, view, stream=None):
-        """-> (n, 8, 5) float32 CUDA tensor: per lobe (mu xyz, kappa, weight)."""
+        """-> (n, ROW) float32 CUDA tensor: 8 x (mu xyz, kappa, weight), alpha, 3 unused."""
         import torch
         n = position.numel() // 3
         pos, nrm, v = _dev(position, 3 * n), _dev(normal, 3 * n), _dev(view, 3 * n)
-        out = torch.empty((n, LOBES, 5), dtype=torch.float32, device="cuda")
+        out = torch.empty((n, ROW), dtype=torch.float32, device="cuda")
         _lib.check(self._lib.gbpt_guide_infer(self._h, pos.data_ptr(), nrm.data_ptr(), v.data_ptr(), n, out.data_ptr(),
                                               _stream(stream)))
         return out

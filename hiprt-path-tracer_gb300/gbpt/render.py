@@ -317,8 +317,9 @@ class Renderer:
                                                      ctypes.byref(s)))
 
     def guide_records(self, capacity: int = 1 << 16, stream=None):
-        """-> (count made by the last launch, (k, 14) float32 records; column 13 holds int32 slots)."""
-        out = np.zeros((capacity, 14), np.float32)
+        """-> (count made by the last launch, (k, 15) float32 records: position, normal, view, direction,
+        weight, BSDF pdf, slot (int32 bits))."""
+        out = np.zeros((capacity, 15), np.float32)
         n = i32(0)
         _lib.check(self._lib.gbpt_renderer_get_guide_records(self._h, out.ctypes.data, capacity, ctypes.byref(n),
                                                              _stream(stream)))

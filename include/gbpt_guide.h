@@ -2,18 +2,22 @@
  * gbpt — learned direction proposal for path guiding (no counterpart in the reference, which has
  * no path guiding; closest relatives are its NEE++ and ReGIR caches).
  *
- * A multiresolution hash-grid encoding of the shading position (8 levels x 2 features, 2^15
- * entries per level, resolutions 4..68 over the scene box) plus the shading normal and the
- * direction towards the viewer feeds a
- * 32 -> 64 -> 64 -> 48 ReLU MLP without biases (a constant input of 1 plays that role). Its
- * output is a mixture of 8 von Mises-Fisher lobes (direction, concentration kappa = softplus + 0.1,
- * clamped to 500, softmax weights). The MLP runs in BF16 on the tcgen05 tensor cores with FP32
- * accumulation; the hash grid, the head, the loss and Adam run in FP32.
- * Training minimises the KL divergence from the radiance-weighted target to the mixture: per
- * sample the loss is -w * log q(direction) with w = luminance(incident radiance * f * cos) / pdf,
- * normalised by the batch's sum of w. Forward, backward and Adam are hand-written kernels.
- * Sampling combines the mixture with BSDF sampling by one-sample MIS (gbpt_renderer_set_guide), so
- * the estimator stays unbiased. All pointers are device pointers unless stated.
+ * Encoding: a multiresolution hash grid of the shading position, 16 levels x 2 features, 2^19
+ * entries per level, resolutions floor(16 * 256^(l/15)) = 16 .. 4096 over the scene box (dense
+ * indexing where (res+1)^3 fits, else the XOR-of-primes hash), features kept as FP32 master values
+ * and read through a BF16 copy; plus the shading normal and the degree-4 real spherical-harmonic
+ * encoding (16 coefficients) of the direction towards the viewer. 64 inputs (13 zero).
+ * Network: 64 -> 64 -> 64 -> 64 -> 48, ReLU, no biases (the constant SH band plays that role),
+ * BF16 weights and activations on the tcgen05 tensor cores with FP32 accumulation (forward,
+ * backward and the weight gradients, accumulated in tensor memory).
+ * Head: 8 von Mises-Fisher lobes (direction = normalised raw[5i..5i+2], concentration
+ * kappa = softplus(raw[5i+3]) + 0.1 clamped to 500, weight = softmax(raw[5i+4])) and the
+ * probability of sampling the mixture instead of the BSDF, alpha = 0.05 + 0.9 sigmoid(raw[40]).
+ * Loss per sample, with w = weight / sum of the batch's weights:
+ *   -w log q(direction)  (the KL divergence from the radiance-weighted target to the mixture),
+ *   -w log(alpha q + (1 - alpha) p_bsdf)  with q held fixed (trains alpha; needs p_bsdf).
+ * Adam with FP32 master weights, moments and gradients. All pointers are device pointers unless
+ * stated.
  */
 #ifndef GBPT_GUIDE_H
 #define GBPT_GUIDE_H
@@ -24,23 +28,24 @@
 extern "C" {
 #endif
 
-#define GBPT_GUIDE_LEVELS 8
-#define GBPT_GUIDE_TABLE 32768
+#define GBPT_GUIDE_LEVELS 16
+#define GBPT_GUIDE_TABLE 524288
 #define GBPT_GUIDE_FEATURES 2
 #define GBPT_GUIDE_GRID_PARAMS (GBPT_GUIDE_LEVELS * GBPT_GUIDE_TABLE * GBPT_GUIDE_FEATURES)
-#define GBPT_GUIDE_IN 32
+#define GBPT_GUIDE_IN 64
 #define GBPT_GUIDE_HIDDEN 64
 #define GBPT_GUIDE_OUT 48
 #define GBPT_GUIDE_LOBES 8
-/* W1 [32][64], W2 [64][64], W3 [64][48], row = input unit, column = output unit, concatenated */
-#define GBPT_GUIDE_WEIGHTS (GBPT_GUIDE_IN * GBPT_GUIDE_HIDDEN + GBPT_GUIDE_HIDDEN * GBPT_GUIDE_HIDDEN + \
-                            GBPT_GUIDE_HIDDEN * GBPT_GUIDE_OUT)
+/* floats per inferred row: 8 x (mu xyz, kappa, weight), alpha, 3 unused */
+#define GBPT_GUIDE_ROW 44
+/* W1 [64][64], W2 [64][64], W3 [64][64], W4 [64][48], row = input unit, column = output unit */
+#define GBPT_GUIDE_WEIGHTS (3 * GBPT_GUIDE_HIDDEN * GBPT_GUIDE_HIDDEN + GBPT_GUIDE_HIDDEN * GBPT_GUIDE_OUT)
 
 typedef struct gbpt_guide gbpt_guide;
 
 typedef struct gbpt_guide_params {
     float scene_min[3], scene_max[3]; /* hash-grid domain (positions are clamped into it) */
-    float learning_rate;              /* Adam, default 5e-3 */
+    float learning_rate;              /* Adam, default 1e-2 */
     float beta1, beta2, epsilon;      /* default 0.9, 0.99, 1e-8 */
     uint32_t seed;                    /* initialisation */
     int32_t max_batch;                /* largest training batch, default 1 << 18 */
@@ -52,17 +57,19 @@ GBPT_API gbpt_status gbpt_guide_create(const gbpt_guide_params* p, gbpt_guide** 
 GBPT_API gbpt_status gbpt_guide_destroy(gbpt_guide* g);
 
 /* One Adam step on n training samples: position[3n], normal[3n], view[3n] (towards the viewer),
- * direction[3n] (the sampled incident direction; unit vectors), weight[n] (negative counts as 0).
- * *loss (host, may be NULL; synchronous when given) receives the normalised batch loss before the
- * step. */
+ * direction[3n] (the sampled incident direction; unit vectors), weight[n] (negative counts as 0),
+ * bsdf_pdf[n] (the BSDF's solid-angle pdf of direction; NULL: alpha is not trained).
+ * *loss (host, may be NULL; synchronous when given) receives the batch loss before the step. */
 GBPT_API gbpt_status gbpt_guide_train(gbpt_guide* g, const float* position, const float* normal, const float* view,
-                                      const float* direction, const float* weight, int64_t n, float* loss, void* stream);
+                                      const float* direction, const float* weight, const float* bsdf_pdf, int64_t n,
+                                      float* loss, void* stream);
 /* The gradients of the batch loss without an Adam step, copied to host arrays (either may be
  * NULL): grad_weights[GBPT_GUIDE_WEIGHTS], grad_grid[GBPT_GUIDE_GRID_PARAMS]. Synchronous. */
 GBPT_API gbpt_status gbpt_guide_gradients(gbpt_guide* g, const float* position, const float* normal,
-                                          const float* view, const float* direction, const float* weight, int64_t n,
-                                          float* grad_weights, float* grad_grid, float* loss, void* stream);
-/* Mixture per query: lobes[40 n] = 8 x (mu xyz, kappa, weight). */
+                                          const float* view, const float* direction, const float* weight,
+                                          const float* bsdf_pdf, int64_t n, float* grad_weights, float* grad_grid,
+                                          float* loss, void* stream);
+/* Mixture per query: lobes[GBPT_GUIDE_ROW n] = 8 x (mu xyz, kappa, weight), alpha, 3 unused. */
 GBPT_API gbpt_status gbpt_guide_infer(gbpt_guide* g, const float* position, const float* normal, const float* view,
                                       int64_t n, float* lobes, void* stream);
 /* 1 if a bounded tensor-core wait of a guide kernel gave up since creation (the kernel then

@@ -208,9 +208,10 @@ GBPT_API gbpt_status gbpt_restir_di_set_reservoirs(gbpt_renderer* r, int32_t whi
 /* ---- learned path guiding (the network: include/gbpt_guide.h) ----
  * With a guide attached, each bounce runs the network on the shaded queue (after extend, inside
  * gbpt_pass_shade) and draws the continuation of every vertex whose material has neither delta
- * lobes nor transmission from the vMF mixture with probability guide_probability, else from the
- * BSDF; the path weight uses the one-sample MIS pdf p q + (1 - p) p_bsdf, so the image stays
- * unbiased whatever the network has learned. Direct lighting (NEE, ReSTIR DI) is unchanged.
+ * lobes nor transmission from the vMF mixture with probability alpha (the network's learned
+ * selection probability, or guide_probability when that is > 0), else from the BSDF; the path
+ * weight uses the one-sample MIS pdf alpha q + (1 - alpha) p_bsdf, so the image stays unbiased
+ * whatever the network has learned. Direct lighting (NEE, ReSTIR DI) is unchanged.
  * With train = 1, vertices are recorded (a hash of pixel sample, bounce and frame picks about
  * max_records per launch) and gbpt_pass_accumulate ends the launch with one Adam step on them.
  * gbpt_renderer_reset restarts the sample index, so the launches after it draw the random numbers
@@ -220,8 +221,8 @@ typedef struct gbpt_guide gbpt_guide;
 typedef struct gbpt_guide_render_settings {
     int32_t enabled;          /* [1] */
     int32_t train;            /* [1] */
-    float guide_probability;  /* [0.5], in (0, 1) */
-    int32_t max_records;      /* per launch, <= the guide's max_batch [65536] */
+    float guide_probability;  /* fixed alpha in (0, 1), or 0 = the network's [0] */
+    int32_t max_records;      /* per launch, <= the guide's max_batch [2^18] */
     float weight_clamp;       /* upper bound of a record's weight, 0 = none [50] */
     int32_t reserved[11];
 } gbpt_guide_render_settings;
@@ -229,8 +230,8 @@ typedef struct gbpt_guide_render_settings {
 GBPT_API gbpt_status gbpt_guide_render_default_settings(gbpt_guide_render_settings* s);
 /* Attaches 'g' (not owned; it must outlive its use) or detaches it (g NULL or enabled = 0). */
 GBPT_API gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_guide_render_settings* s);
-/* The last launch's training records, 14 floats each: position xyz, normal xyz, view xyz,
- * direction xyz, weight, pixel-sample slot (int32 bits). Copies min(count, capacity) records to
+/* The last launch's training records, 15 floats each: position xyz, normal xyz, view xyz,
+ * direction xyz, weight, BSDF pdf of the direction, pixel-sample slot (int32 bits). Copies min(count, capacity) records to
  * host_out (may be NULL) and the number made (before the max_records cap) to *count. Synchronous. */
 GBPT_API gbpt_status gbpt_renderer_get_guide_records(gbpt_renderer* r, float* host_out, int32_t capacity, int32_t* count,
                                                      void* stream);

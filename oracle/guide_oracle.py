@@ -4,31 +4,35 @@ product path).
 The reference renderer has no learned path guiding (its closest relatives are the NEE++ visibility
 cache and ReGIR light grids), so there is no reference output to pin this oracle to. It is pinned
 instead by mathematics: its analytic gradients are checked against FP64 central differences of its
-own loss, its vMF lobes integrate to one, and the CUDA kernels are checked against it.
+own loss, its vMF lobes integrate to one, its spherical harmonics are orthonormal, and the CUDA
+kernels are checked against it.
 
-Everything runs in float64 numpy. With bf16=True the oracle rounds exactly where the CUDA kernels
-hand BF16 operands to the tensor cores (the MLP input X, the weights, the hidden activations H1 and
-H2, the output gradient dY and the hidden gradients dH2 and dH1), so the remaining GPU/oracle
-difference is FP32 accumulation order and transcendental rounding.
+Everything runs in float64 numpy. With bf16_ops=True the oracle rounds exactly where the CUDA
+kernels hand BF16 values on: the grid features (read through a BF16 copy), the MLP input X, the
+weights, the hidden activations, the output gradient dY and the hidden gradients, so the remaining
+GPU/oracle difference is FP32 accumulation order and transcendental rounding.
 
-Network: hash-grid features (8 levels x 2, trilinear) ++ normal ++ [1] ++ view ++ zeros (32 inputs) ->
-ReLU(X W1) (64) -> ReLU(H1 W2) (64) -> H2 W3 (48 raw outputs) -> 8 vMF lobes (raw[5i:5i+3]
-direction, softplus(raw[5i+3]) + 0.1 clamped to 500 concentration, softmax(raw[5i+4]) weights).
-Outputs 40..47 are unused. Loss: sum_i w_i / sum(w) * -log q(d_i).
+Network: hash-grid features (16 levels x 2, trilinear, 2^19 entries per level) ++ normal ++
+SH16(view) ++ zeros (64 inputs) -> ReLU(X W1) -> ReLU(H1 W2) -> ReLU(H2 W3) (64 each) -> H3 W4
+(48 raw outputs) -> 8 vMF lobes (raw[5i:5i+3] direction, softplus(raw[5i+3]) + 0.1 clamped to 500
+concentration, softmax(raw[5i+4]) weights) and alpha = 0.05 + 0.9 sigmoid(raw[40]).
+Loss per sample with s = w / sum(w): -s log q(d) and, when the BSDF pdf p_b is given,
+-s log(alpha q(d) + (1 - alpha) p_b) with q held fixed (its gradient reaches raw[40] only).
 """
 from __future__ import annotations
 
 import numpy as np
 
-LEVELS, TABLE, FEATURES = 8, 32768, 2
+LEVELS, TABLE, FEATURES = 16, 1 << 19, 2
 GRID_PARAMS = LEVELS * TABLE * FEATURES
-IN, HIDDEN, OUT, LOBES = 32, 64, 48, 8
-OFF_W1, OFF_W2 = 0, IN * HIDDEN
-OFF_W3 = OFF_W2 + HIDDEN * HIDDEN
-WEIGHTS = OFF_W3 + HIDDEN * OUT
-RES = (4, 6, 9, 13, 20, 30, 45, 68)
-KAPPA_MIN, KAPPA_MAX = 0.1, 500.0
+IN, HIDDEN, OUT, LOBES, ROW = 64, 64, 48, 8, 44
+OFF_W = (0, 4096, 8192, 12288)
+WEIGHTS = 12288 + 64 * 48
+SHAPES = ((IN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, OUT))
+RES = tuple(int(np.floor(16 * 256 ** (l / 15))) for l in range(LEVELS))
+KAPPA_MIN, KAPPA_MAX, ALPHA_MIN = 0.1, 500.0, 0.05
 LOG_2PI = np.log(2.0 * np.pi)
+N_GRID_FEATURES, NORMAL_IN, SH_IN, ALPHA_OUT = 32, 32, 35, 40
 
 
 def bf16(a) -> np.ndarray:
@@ -44,8 +48,7 @@ def bf16(a) -> np.ndarray:
 
 def split_weights(weights):
     w = np.asarray(weights, np.float64)
-    return (w[OFF_W1:OFF_W2].reshape(IN, HIDDEN), w[OFF_W2:OFF_W3].reshape(HIDDEN, HIDDEN),
-            w[OFF_W3:WEIGHTS].reshape(HIDDEN, OUT))
+    return tuple(w[o:o + a * b].reshape(a, b) for o, (a, b) in zip(OFF_W, SHAPES))
 
 
 def grid_slot(res: int, x, y, z):
@@ -95,13 +98,28 @@ def encode(grid, cor):
     return np.concatenate(feats, 1)
 
 
+def sh16(d):
+    """Real spherical harmonics of bands 0..3 of unit vectors (n, 3) -> (n, 16), orthonormal."""
+    x, y, z = d[:, 0], d[:, 1], d[:, 2]
+    pi = np.pi
+    c1 = np.sqrt(3 / (4 * pi))
+    c2a, c2b, c2c = np.sqrt(15 / (4 * pi)), np.sqrt(5 / (16 * pi)), np.sqrt(15 / (16 * pi))
+    c3a, c3b, c3c = np.sqrt(35 / (32 * pi)), np.sqrt(105 / (4 * pi)), np.sqrt(21 / (32 * pi))
+    c3d, c3e = np.sqrt(7 / (16 * pi)), np.sqrt(105 / (16 * pi))
+    return np.stack([
+        np.full_like(x, np.sqrt(1 / (4 * pi))),
+        c1 * y, c1 * z, c1 * x,
+        c2a * x * y, c2a * y * z, c2b * (3 * z * z - 1), c2a * x * z, c2c * (x * x - y * y),
+        c3a * y * (3 * x * x - y * y), c3b * x * y * z, c3c * y * (5 * z * z - 1), c3d * z * (5 * z * z - 3),
+        c3c * x * (5 * z * z - 1), c3e * z * (x * x - y * y), c3a * x * (x * x - 3 * y * y)], 1)
+
+
 def input_rows(feat, N, V):
     n = feat.shape[0]
     x = np.zeros((n, IN))
-    x[:, :16] = feat
-    x[:, 16:19] = N
-    x[:, 19] = 1.0
-    x[:, 20:23] = V
+    x[:, :N_GRID_FEATURES] = feat
+    x[:, NORMAL_IN:NORMAL_IN + 3] = N
+    x[:, SH_IN:SH_IN + 16] = sh16(np.asarray(V, np.float64))
     return x
 
 
@@ -114,7 +132,7 @@ def sigmoid(x):
 
 
 def head(raw):
-    """-> mu (n, 8, 3), kappa (n, 8), weight (n, 8), raw direction norms (n, 8)."""
+    """-> mu (n, 8, 3), kappa (n, 8), weight (n, 8), raw direction norms (n, 8), alpha (n,)."""
     r = raw[:, :LOBES * 5].reshape(-1, LOBES, 5)
     a = r[:, :, :3]
     ln = np.sqrt((a * a).sum(-1) + 1e-12)
@@ -122,7 +140,8 @@ def head(raw):
     kappa = np.minimum(softplus(r[:, :, 3]) + KAPPA_MIN, KAPPA_MAX)
     lg = r[:, :, 4]
     e = np.exp(lg - lg.max(1, keepdims=True))
-    return mu, kappa, e / e.sum(1, keepdims=True), ln
+    alpha = ALPHA_MIN + (1 - 2 * ALPHA_MIN) * sigmoid(raw[:, ALPHA_OUT])
+    return mu, kappa, e / e.sum(1, keepdims=True), ln, alpha
 
 
 def log_vmf(kappa, c):
@@ -135,25 +154,28 @@ def mixture_pdf(mu, kappa, weight, d):
 
 
 def forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops=True):
-    """-> dict with the input X, pre-activations D1, D2, activations H1, H2, raw outputs."""
+    """-> dict with the input X, pre-activations D1..D3, activations H1..H3, raw outputs."""
     rnd = bf16 if bf16_ops else (lambda a: np.asarray(a, np.float64))
-    W1, W2, W3 = (rnd(w) for w in split_weights(weights))
+    W = tuple(rnd(w) for w in split_weights(weights))
     cor = corners(lo, inv_ext, P)
-    X = rnd(input_rows(encode(grid, cor), np.asarray(N, np.float64), np.asarray(V, np.float64)))
-    D1 = X @ W1
-    H1 = rnd(np.maximum(D1, 0.0))
-    D2 = H1 @ W2
-    H2 = rnd(np.maximum(D2, 0.0))
-    raw = H2 @ W3
-    return dict(cor=cor, X=X, D1=D1, H1=H1, D2=D2, H2=H2, raw=raw, W=(W1, W2, W3))
+    g = rnd(grid)
+    X = rnd(input_rows(encode(g, cor), np.asarray(N, np.float64), np.asarray(V, np.float64)))
+    acts, pre = [X], []
+    for l in range(3):
+        D = acts[-1] @ W[l]
+        pre.append(D)
+        acts.append(rnd(np.maximum(D, 0.0)))
+    raw = acts[-1] @ W[3]
+    return dict(cor=cor, acts=acts, pre=pre, raw=raw, W=W)
 
 
-def loss_and_draw(raw, d, w):
-    """Batch loss and its gradient with respect to the raw outputs (n, 48)."""
+def loss_and_draw(raw, d, w, p_bsdf=None, q_fixed=None):
+    """Batch loss and its gradient with respect to the raw outputs (n, 48). q_fixed (n,) replaces q
+    in the alpha term (the value that term holds fixed), for finite-difference checks."""
     w = np.maximum(np.asarray(w, np.float64), 0.0)
     total = w.sum()
     scale = w / total if total > 0 else np.zeros_like(w)
-    mu, kappa, pi, ln = head(raw)
+    mu, kappa, pi, ln, alpha = head(raw)
     c = np.einsum("nlk,nk->nl", mu, d)
     lv = np.log(np.maximum(pi, 1e-30)) + log_vmf(kappa, c)
     m = lv.max(1, keepdims=True)
@@ -170,40 +192,62 @@ def loss_and_draw(raw, d, w):
     dl[:, :, 3] = np.where(clamped, 0.0, -s * resp * dlogv * sigmoid(r[:, :, 3]))
     gm = (d[:, None, :] - c[..., None] * mu) * (resp * kappa / ln)[..., None]
     dl[:, :, :3] = -s[..., None] * gm
-    return float((scale * -logq).sum()), draw, logq
+    loss = float((scale * -logq).sum())
+    if p_bsdf is not None:
+        pb = np.maximum(np.asarray(p_bsdf, np.float64), 0.0)
+        q = np.exp(logq) if q_fixed is None else np.asarray(q_fixed, np.float64)
+        mix = alpha * q + (1 - alpha) * pb
+        ok = (mix > 0) & (scale > 0)
+        sg = sigmoid(raw[:, ALPHA_OUT])
+        safe = np.where(ok, mix, 1.0)
+        draw[:, ALPHA_OUT] = np.where(ok, -scale * (q - pb) / safe * (1 - 2 * ALPHA_MIN) * sg * (1 - sg), 0.0)
+        loss += float(np.where(ok, -scale * np.log(safe), 0.0).sum())
+    return loss, draw, logq
 
 
-def gradients(weights, grid, lo, inv_ext, P, N, V, D, w, bf16_ops=True):
+def gradients(weights, grid, lo, inv_ext, P, N, V, D, w, p_bsdf=None, bf16_ops=True):
     """-> (loss, grad_weights (WEIGHTS,), grad_grid (GRID_PARAMS,)) of the batch loss."""
     rnd = bf16 if bf16_ops else (lambda a: np.asarray(a, np.float64))
     f = forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops)
-    W1, W2, W3 = f["W"]
-    loss, draw, _ = loss_and_draw(f["raw"], np.asarray(D, np.float64), w)
-    dY = rnd(draw)
-    gW3 = f["H2"].T @ dY
-    dH2 = rnd((dY @ W3.T) * (f["D2"] > 0))
-    gW2 = f["H1"].T @ dH2
-    dH1 = rnd((dH2 @ W2.T) * (f["D1"] > 0))
-    gW1 = f["X"].T @ dH1
-    dX = dH1 @ W1.T
+    W = f["W"]
+    loss, draw, _ = loss_and_draw(f["raw"], np.asarray(D, np.float64), w, p_bsdf)
+    dH = rnd(draw)
+    gW = [None] * 4
+    for l in range(3, -1, -1):
+        gW[l] = f["acts"][l].T @ dH
+        g = dH @ W[l].T
+        if l > 0:
+            dH = rnd(g * (f["pre"][l - 1] > 0))
+        else:
+            dX = g
     gg = np.zeros((LEVELS, TABLE, FEATURES))
     for l, (slots, ws) in enumerate(f["cor"]):
         contrib = ws[:, :, None] * dX[:, None, 2 * l:2 * l + 2]
         np.add.at(gg[l], slots.reshape(-1), contrib.reshape(-1, 2))
-    gw = np.concatenate([gW1.reshape(-1), gW2.reshape(-1), gW3.reshape(-1)])
-    return loss, gw, gg.reshape(-1)
+    return loss, np.concatenate([g.reshape(-1) for g in gW]), gg.reshape(-1)
 
 
-def batch_loss(weights, grid, lo, inv_ext, P, N, V, D, w, bf16_ops=False):
+def batch_loss(weights, grid, lo, inv_ext, P, N, V, D, w, p_bsdf=None, bf16_ops=False, q_fixed=None):
     f = forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops)
-    return loss_and_draw(f["raw"], np.asarray(D, np.float64), w)[0]
+    return loss_and_draw(f["raw"], np.asarray(D, np.float64), w, p_bsdf, q_fixed)[0]
+
+
+def mixture_pdf_of(weights, grid, lo, inv_ext, P, N, V, D, bf16_ops=False):
+    """q(D) per sample under the given parameters (what the alpha term holds fixed)."""
+    f = forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops)
+    mu, kappa, pi, _, _ = head(f["raw"])
+    return mixture_pdf(mu, kappa, pi, np.asarray(D, np.float64))
 
 
 def infer(weights, grid, lo, inv_ext, P, N, V, bf16_ops=True):
-    """-> (n, 8, 5): per lobe (mu xyz, kappa, weight), the layout of gbpt_guide_infer."""
+    """-> (n, 44) rows in the layout of gbpt_guide_infer: 8 x (mu xyz, kappa, weight), alpha, 0, 0, 0."""
     f = forward(weights, grid, lo, inv_ext, P, N, V, bf16_ops)
-    mu, kappa, pi, _ = head(f["raw"])
-    return np.concatenate([mu, kappa[..., None], pi[..., None]], -1)
+    mu, kappa, pi, _, alpha = head(f["raw"])
+    lobes = np.concatenate([mu, kappa[..., None], pi[..., None]], -1).reshape(-1, LOBES * 5)
+    out = np.zeros((lobes.shape[0], ROW))
+    out[:, :LOBES * 5] = lobes
+    out[:, ALPHA_OUT] = alpha
+    return out
 
 
 def adam(params, grads, m, v, step, lr, b1, b2, eps):
@@ -222,7 +266,7 @@ def random_params(seed=0, grid_scale=1e-2):
     """Glorot-uniform weights and uniform grid features (for CPU-only checks)."""
     rng = np.random.default_rng(seed)
     parts = []
-    for fan_in, fan_out in ((IN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, OUT)):
+    for fan_in, fan_out in SHAPES:
         s = np.sqrt(6.0 / (fan_in + fan_out))
         parts.append(rng.uniform(-s, s, fan_in * fan_out))
     grid = rng.uniform(-grid_scale, grid_scale, GRID_PARAMS)
@@ -231,12 +275,13 @@ def random_params(seed=0, grid_scale=1e-2):
 
 def random_batch(n, seed=0, lo=(0, 0, 0), hi=(1, 1, 1)):
     """Seeded training samples: positions in the box, unit normals, view and incident directions,
-    weights >= 0 (a fifth of them zero)."""
+    weights >= 0 (a fifth of them zero) and BSDF pdfs (cosine lobes around the normal)."""
     rng = np.random.default_rng(seed)
     P = rng.uniform(lo, hi, (n, 3))
     N, V, D = (rng.normal(size=(n, 3)) for _ in range(3))
     for a in (N, V, D):
         a /= np.linalg.norm(a, axis=1, keepdims=True)
     w = rng.exponential(1.0, n) * (rng.random(n) < 0.8)
+    pb = np.maximum((N * D).sum(1), 0.0) / np.pi
     f = np.float32
-    return P.astype(f), N.astype(f), V.astype(f), D.astype(f), w.astype(f)
+    return P.astype(f), N.astype(f), V.astype(f), D.astype(f), w.astype(f), pb.astype(f)

@@ -82,11 +82,11 @@ def test_guide_parameters_and_argument_checks():
     from gbpt import guide
     assert ctypes.sizeof(guide.GuideParams) == 72
     text = open(os.path.join(INCLUDE, "gbpt_guide.h")).read()
-    for name in ("LEVELS", "TABLE", "FEATURES", "IN", "HIDDEN", "OUT", "LOBES"):
+    for name in ("LEVELS", "TABLE", "FEATURES", "IN", "HIDDEN", "OUT", "LOBES", "ROW"):
         m = re.search(rf"#define GBPT_GUIDE_{name} (\d+)", text)
         assert m and int(m.group(1)) == getattr(guide, name), name
     p = guide.default_params()
-    assert abs(p.learning_rate - 5e-3) < 1e-9 and p.max_batch == 1 << 18 and list(p.scene_max) == [1, 1, 1]
+    assert abs(p.learning_rate - 1e-2) < 1e-9 and p.max_batch == 1 << 18 and list(p.scene_max) == [1, 1, 1]
     lib = guide._load()
     h = ctypes.c_void_p()
     bad = guide.default_params(max_batch=0)
@@ -94,6 +94,6 @@ def test_guide_parameters_and_argument_checks():
     bad = guide.default_params(scene_min=(0, 2, 0))
     assert lib.gbpt_guide_create(ctypes.byref(bad), ctypes.byref(h)) == 1
     assert b"empty scene box" in lib.gbpt_last_error()
-    assert lib.gbpt_guide_train(None, None, None, None, None, None, 4, None, None) == 1
+    assert lib.gbpt_guide_train(None, None, None, None, None, None, None, 4, None, None) == 1
     assert lib.gbpt_guide_infer(None, None, None, None, 4, None, None) == 1
     assert lib.gbpt_guide_destroy(None) == 0

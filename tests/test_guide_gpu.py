@@ -1,6 +1,6 @@
-"""GPU: the guiding network's tcgen05 kernels against the FP64 oracle (which rounds GEMM operands to
-BF16 where the kernels do): inference, loss, weight and hash-grid gradients, the Adam step, and
-online training on a synthetic position-dependent vMF target."""
+"""GPU: the guiding network's tcgen05 kernels against the FP64 oracle (which rounds to BF16 where the
+kernels do): inference, loss, weight and hash-grid gradients, the Adam step, and online training on
+a synthetic position-dependent vMF target."""
 import numpy as np
 import pytest
 
@@ -8,14 +8,15 @@ import guide_oracle as G
 
 pytestmark = pytest.mark.gpu
 
-# GPU/oracle differences: FP32 accumulation order and transcendental rounding, amplified where a
-# value sits on a BF16 rounding boundary (one BF16 step is 2^-8 relative). Measured on the oracle by
-# perturbing its inputs at FP32 precision: block-relative L2 error of the gradients <= 3e-3,
-# output lobes identical except for a few rows at 5e-3.
-GRAD_RTOL = 1e-2
-LOBE_ATOL = 1e-4
-LOBE_RTOL = 1e-3
-LOBE_FRACTION = 0.995
+# GPU/oracle differences come from FP32 accumulation order and transcendental rounding, amplified
+# where a value sits on a BF16 rounding boundary (one BF16 step is 2^-8 relative) and, through the
+# normalisation of the lobe directions, by 1 / |raw direction| for the few samples whose raw
+# direction is short. Measured on the oracle by perturbing its inputs at FP32 precision with the
+# conditioned test network below: block-relative L2 error of the gradients up to 1.6e-2, the
+# output rows identical except for a few at 5e-3.
+GRAD_RTOL = 5e-2
+GRAD_COS = 0.999
+ROW_ATOL, ROW_RTOL, ROW_FRACTION = 1e-3, 1e-2, 0.99
 
 
 def _t(a):
@@ -28,73 +29,91 @@ def _guide(seed=7, **kw):
     return guide.Guide(seed=seed, **kw)
 
 
-def _with_grid(g, scale=0.1, seed=11):
-    """Replaces the tiny initial grid features by larger ones so the encoding matters."""
+def _conditioned(g, scale=0.1, seed=11):
+    """Larger grid features (so the encoding matters) and lobe-direction columns of W4 scaled by 10
+    (so raw directions are rarely short and the comparison is well conditioned)."""
     w, _ = g.get_params()
+    W4 = w[G.OFF_W[3]:].reshape(64, 48)
+    for i in range(8):
+        W4[:, 5 * i:5 * i + 3] *= 10.0
     grid = np.random.default_rng(seed).uniform(-scale, scale, G.GRID_PARAMS).astype(np.float32)
     g.set_params(w, grid)
     return w, grid
 
 
 def _blocks(gw, gg):
-    return dict(W1=gw[G.OFF_W1:G.OFF_W2], W2=gw[G.OFF_W2:G.OFF_W3], W3=gw[G.OFF_W3:G.WEIGHTS], grid=gg)
+    out = {f"W{l + 1}": gw[o:o + a * b] for l, (o, (a, b)) in enumerate(zip(G.OFF_W, G.SHAPES))}
+    out["grid"] = gg
+    return out
+
+
+def _close(a, b):
+    nb = np.linalg.norm(b)
+    if nb == 0:
+        return np.linalg.norm(a) == 0, 0.0, 1.0
+    rel = np.linalg.norm(a - b) / nb
+    cos = float(a @ b / (np.linalg.norm(a) * nb + 1e-30))
+    return rel <= GRAD_RTOL and cos >= GRAD_COS, rel, cos
 
 
 def test_inference_matches_oracle(cuda):
     g = _guide()
-    w, grid = _with_grid(g)
-    P, N, V, _, _ = G.random_batch(1000, 21)  # not a multiple of the 128-row tile
+    w, grid = _conditioned(g)
+    P, N, V, _, _, _ = G.random_batch(1000, 21)  # not a multiple of the 128-row tile
     got = g.infer(_t(P), _t(N), _t(V)).cpu().numpy()
     lo, inv = G.domain(g.params.scene_min, g.params.scene_max)
     want = G.infer(w, grid, lo, inv, P, N, V)
-    close = np.abs(got - want) <= LOBE_ATOL + LOBE_RTOL * np.abs(want)
-    assert close.mean() >= LOBE_FRACTION, close.mean()
-    assert np.abs(got - want).max() < 5e-2
-    np.testing.assert_allclose(got[:, :, 4].sum(1), 1.0, atol=1e-5)
-    np.testing.assert_allclose(np.linalg.norm(got[:, :, :3], axis=2), 1.0, atol=1e-5)
-    assert (got[:, :, 3] >= 0.1).all() and (got[:, :, 3] <= 500).all()
+    close = np.abs(got - want) <= ROW_ATOL + ROW_RTOL * np.abs(want)
+    assert close.mean() >= ROW_FRACTION, close.mean()
+    lobes = got[:, :40].reshape(-1, 8, 5)
+    np.testing.assert_allclose(lobes[:, :, 4].sum(1), 1.0, atol=1e-5)
+    np.testing.assert_allclose(np.linalg.norm(lobes[:, :, :3], axis=2), 1.0, atol=1e-5)
+    assert (lobes[:, :, 3] >= 0.1).all() and (lobes[:, :, 3] <= 500).all()
+    assert (got[:, 40] >= 0.05).all() and (got[:, 40] <= 0.95).all() and (got[:, 41:] == 0).all()
 
 
 @pytest.mark.parametrize("n", [1, 127, 1000, 5000])
 def test_gradients_match_oracle(cuda, n):
     g = _guide()
-    w, grid = _with_grid(g)
-    P, N, V, D, wt = G.random_batch(n, 100 + n)
-    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
+    w, grid = _conditioned(g)
+    P, N, V, D, wt, pb = G.random_batch(n, 100 + n)
+    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt), _t(pb))
     lo, inv = G.domain(g.params.scene_min, g.params.scene_max)
-    l0, ow, og = G.gradients(w, grid, lo, inv, P, N, V, D, wt)
+    l0, ow, og = G.gradients(w, grid, lo, inv, P, N, V, D, wt, pb)
     assert abs(loss - l0) <= 1e-4 * max(1.0, abs(l0)), (loss, l0)
-    for name, (a, b) in {k: (v, _blocks(ow, og)[k]) for k, v in _blocks(gw, gg).items()}.items():
-        nb = np.linalg.norm(b)
-        if nb == 0:
-            assert np.linalg.norm(a) == 0, name
-            continue
-        assert np.linalg.norm(a - b) <= GRAD_RTOL * nb, (name, np.linalg.norm(a - b) / nb)
-    # untouched grid entries get exactly zero gradient
-    assert np.array_equal(gg == 0, og == 0) or ((gg == 0) != (og == 0)).mean() < 1e-4
+    want = _blocks(ow, og)
+    for name, a in _blocks(gw, gg).items():
+        ok, rel, cos = _close(a, want[name])
+        assert ok, (name, rel, cos)
+    # the BF16 emulation matters: the kernels are closer to it than to the exact FP64 gradients
+    if n >= 1000:
+        _, fw, fg = G.gradients(w, grid, lo, inv, P, N, V, D, wt, pb, bf16_ops=False)
+        assert np.linalg.norm(gw - ow) < np.linalg.norm(gw - fw)
 
 
 def test_zero_and_negative_weights(cuda):
     g = _guide()
-    P, N, V, D, wt = G.random_batch(300, 5)
+    P, N, V, D, wt, pb = G.random_batch(300, 5)
     wt[:] = 0.0
-    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
+    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt), _t(pb))
     assert loss == 0.0 and not gw.any() and not gg.any()
+    w, grid = _conditioned(g)
     wt = np.random.default_rng(1).normal(size=300).astype(np.float32)  # negatives count as zero
-    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
-    w, grid = g.get_params()
+    gw, gg, loss = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))  # no BSDF pdf: alpha untrained
     lo, inv = G.domain(g.params.scene_min, g.params.scene_max)
     l0, ow, _ = G.gradients(w, grid, lo, inv, P, N, V, D, wt)
     assert abs(loss - l0) <= 1e-4 * abs(l0)
-    assert np.linalg.norm(gw - ow) <= GRAD_RTOL * np.linalg.norm(ow)
+    ok, rel, cos = _close(gw, ow)
+    assert ok, (rel, cos)
+    assert not gw[G.OFF_W[3] + G.ALPHA_OUT::48].any()  # the alpha column of W4
 
 
 def test_adam_step_matches_oracle(cuda):
     g = _guide()
-    P, N, V, D, wt = G.random_batch(2048, 9)
-    gw, gg, _ = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt))
+    P, N, V, D, wt, pb = G.random_batch(2048, 9)
+    gw, gg, _ = g.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt), _t(pb))
     w0, grid0 = g.get_params()
-    g.train(_t(P), _t(N), _t(V), _t(D), _t(wt))
+    g.train(_t(P), _t(N), _t(V), _t(D), _t(wt), _t(pb))
     w1, grid1 = g.get_params()
     p = g.params
     zeros = np.zeros(G.WEIGHTS + G.GRID_PARAMS, np.float32)
@@ -126,23 +145,44 @@ def test_online_training_learns_position_dependent_lobes(cuda):
     g = _guide(seed=3)
     rng = np.random.default_rng(0)
     losses = []
+    up = _t(np.tile([0.0, 0, 1], (4096, 1)))
     for _ in range(250):
         P = rng.random((4096, 3))
         mu = P - 0.5
         mu /= np.linalg.norm(mu, axis=1, keepdims=True)
         D = _vmf_sample(mu, 20.0, rng)
-        up = _t(np.tile([0.0, 0, 1], (4096, 1)))
         losses.append(g.train(_t(P), up, up, _t(D), _t(np.ones(4096))))
     assert losses[0] > 2.0
     assert np.mean(losses[-20:]) < 0.3, losses[-20:]
     P = rng.random((512, 3))
     mu = P - 0.5
     mu /= np.linalg.norm(mu, axis=1, keepdims=True)
-    up = _t(np.tile([0.0, 0, 1], (512, 1)))
-    lobes = g.infer(_t(P), up, up).cpu().numpy()
+    rows = g.infer(_t(P), up[:512], up[:512]).cpu().numpy()
+    lobes = rows[:, :40].reshape(-1, 8, 5)
     q = G.mixture_pdf(lobes[:, :, :3], lobes[:, :, 3], lobes[:, :, 4], mu)
     # the target density at its mode is 20 / (2 pi) = 3.2; the uniform density is 0.08
     assert np.median(q) > 1.0, np.median(q)
+    assert g.error_flag() == 0
+
+
+def test_selection_probability_learns_where_the_bsdf_is_good(cuda):
+    """Training alpha with the mixture term: where the BSDF pdf equals the target (the samples are
+    drawn from it) alpha falls; where the BSDF pdf is far below the target it rises. The two groups
+    differ by their normal, an input the network sees directly."""
+    g = _guide(seed=4)
+    rng = np.random.default_rng(1)
+    n = 4096
+    good = np.arange(n) < n // 2
+    nrm = np.where(good[:, None], [[1.0, 0, 0]], [[-1.0, 0, 0]])
+    up = _t(np.tile([0.0, 0, 1], (n, 1)))
+    for _ in range(150):
+        P = rng.random((n, 3))
+        D = _vmf_sample(np.tile([0.0, 0, 1], (n, 1)), 20.0, rng)
+        pdf = 20.0 / (2 * np.pi) * np.exp(20.0 * (D[:, 2] - 1.0))
+        pb = np.where(good, pdf, pdf / 100.0)  # the target itself / a BSDF 100x below the target
+        g.train(_t(P), _t(nrm), up, _t(D), _t(np.ones(n)), _t(pb))
+    alpha = g.infer(_t(rng.random((n, 3))), _t(nrm), up).cpu().numpy()[:, 40]
+    assert alpha[good].mean() < 0.4 and alpha[~good].mean() > 0.6, (alpha[good].mean(), alpha[~good].mean())
 
 
 def test_empty_batch_and_bad_arguments(cuda):
@@ -150,8 +190,8 @@ def test_empty_batch_and_bad_arguments(cuda):
     g = _guide(max_batch=256)
     e = _t(np.zeros((0, 3)))
     assert g.train(e, e, e, e, _t(np.zeros(0))) == 0.0
-    assert g.infer(e, e, e).shape == (0, 8, 5)
-    P, N, V, D, wt = G.random_batch(300, 1)
+    assert g.infer(e, e, e).shape == (0, 44)
+    P, N, V, D, wt, _ = G.random_batch(300, 1)
     with pytest.raises(GbptError):
         g.train(_t(P), _t(N), _t(V), _t(D), _t(wt))  # above max_batch
     assert g.error_flag() == 0

@@ -77,8 +77,8 @@ def test_training_records_are_well_formed(cuda, indirect_reference):
     r.render(1)
     n, rec = r.guide_records()
     assert n > 1000 and rec.shape[0] == min(n, 1 << 16)
-    pos, nrm, view, d, w = rec[:, 0:3], rec[:, 3:6], rec[:, 6:9], rec[:, 9:12], rec[:, 12]
-    slot = rec[:, 13].view(np.int32)
+    pos, nrm, view, d, w, pb = rec[:, 0:3], rec[:, 3:6], rec[:, 6:9], rec[:, 9:12], rec[:, 12], rec[:, 13]
+    slot = rec[:, 14].view(np.int32)
     assert (pos >= -1e-3).all() and (pos <= 5.5 + 1e-3).all()
     for v in (nrm, view, d):
         np.testing.assert_allclose(np.linalg.norm(v, axis=1), 1.0, atol=1e-4)
@@ -87,6 +87,10 @@ def test_training_records_are_well_formed(cuda, indirect_reference):
     assert ((nrm * d).sum(1) > -0.1).all() and ((nrm * d).sum(1) > 0).mean() > 0.99
     assert np.isfinite(w).all() and (w >= 0).all() and (w <= 50.0).all() and (w > 0).mean() > 0.05
     assert (slot >= 0).all() and (slot < 32 * 32 * 4).all()
+    # the recorded BSDF pdf is the Lambertian cos / pi of the recorded direction (about the shading
+    # normal, which equals the recorded geometric normal unless it was bent)
+    close = np.abs(pb - np.maximum((nrm * d).sum(1), 0) / np.pi) < 2e-3
+    assert close.mean() > 0.99, close.mean()
     assert g.error_flag() == 0
 
 
