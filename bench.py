@@ -182,6 +182,148 @@ def cpu_baseline_sample(impl, primary, bounce, shadow, frac):
                       f"{len(samples[2])} shadow), {dt:.2f}s"}, dt
 
 
+def _orbit(eye, target, deg):
+    a = np.radians(deg)
+    c, s = np.cos(a), np.sin(a)
+    ex, ez = eye[0] - target[0], eye[2] - target[2]
+    return (target[0] + c * ex + s * ez, eye[1], target[2] - s * ex + c * ez)
+
+
+def _relmse(img, ref):
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
+    """Path-tracing workloads (one GPU, inputs resident; timed with CUDA events on the current stream):
+
+    cornell     the Cornell box, 256 x 256, 64 launches x 1 spp, 4 bounces, RR from bounce 3, uniform
+                light sampling NEE + BSDF MIS, Lambertian; relMSE against a 16384-spp FP64 image;
+                cpu_baseline = the oracle's restatement of the reference's CPU estimator on all host
+                cores over a bounded sample.
+    restir      the many-light principled scene (16,777,216 + 10,000 emissive triangles), 1920 x 1080,
+                8 frames with the camera orbiting 0.5 degrees per frame, 3 indirect bounces, power
+                light sampling, ReSTIR DI (32 light + 1 BSDF candidates, visibility reuse, M-cap 20,
+                1 spatial pass of 5 neighbours in 30 px).
+    guided      the same scene at guided_res, 8 bounces, 64 spp per image: plain BSDF sampling against
+                learned guiding (training online every launch, its time included), both over 4
+                independent 64-spp images after a 64-spp warm-up; relMSE against a 2048-spp plain FP64
+                image. time_to_equal_relmse_speedup = (relMSE x time) plain / (relMSE x time) guided.
+    """
+    import torch
+    import gbpt
+    from gbpt import guide, scenes
+    from gbpt.render import (BSDF_PRINCIPLED, LIGHT_POWER, RenderSettings, guide_render_settings, look_at_camera,
+                             restir_di_settings)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    out = {}
+    # ---- Cornell box ----
+    cb = scenes.cornell_box()
+    cscene = gbpt.Scene.from_cornell(cb)
+    ref = gbpt.Renderer(cscene, gbpt.cornell_settings(256, 256, samples_per_launch=256, seed=1000))
+    ref.render(64)
+    torch.cuda.synchronize()
+    cref = ref.image_sums()[1] / (256 * 64)
+    del ref
+    r = gbpt.Renderer(cscene, gbpt.cornell_settings(256, 256, samples_per_launch=1, seed=1))
+    r.render(3)
+    r.reset()
+    ms = timed(lambda: r.render(64))
+    st = r.stats()
+    rays = st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
+    out["cornell"] = {"config": "256x256, 64 launches x 1 spp, 4 bounces, RR from 3, uniform NEE + BSDF MIS, Lambert",
+                      "ms": ms, "samples_per_s": 256 * 256 * 64 / (ms * 1e-3), "mrays_per_s": rays / (ms * 1e-3) / 1e6,
+                      "relmse_vs_16384spp_fp64": _relmse(r.image_sums()[1] / 64, cref)}
+    del r
+    if cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import pyoracle
+        pyoracle.build(ref=False)
+        lt = cscene.light_table()
+        cores = os.cpu_count() or 1
+        cst = gbpt.cornell_settings(256, 256, samples_per_launch=1, seed=1)
+        t0 = time.perf_counter()
+        spp = 4
+        pyoracle.pt_render(cb.mesh.triangle_soup(), cb.material_of_triangle, cb.albedo, cb.emission, lt["emissive"],
+                           lt["probas"], lt["alias"], lt["power_sum"], cst, spp, nthreads=cores)
+        dt = time.perf_counter() - t0
+        out["cornell"]["cpu_baseline"] = {"value": 256 * 256 * spp / dt, "unit": "samples/s", "cores": cores,
+                                          "kind": "port", "sample": f"256x256 x {spp} spp, {dt:.2f}s"}
+    del cscene
+
+    # ---- many-light principled scene ----
+    t0 = time.time()
+    S = scenes.many_light_scene()
+    scene = gbpt.Scene(S.mesh.positions, S.mesh.indices, S.material_of_triangle, principled=S.materials)
+    torch.cuda.synchronize()
+    log(f"many-light scene: {S.mesh.n_triangles} triangles, scene + BVH {time.time() - t0:.1f}s")
+
+    def settings(w, h, spp, nb, seed, eye=None):
+        iv, ip = look_at_camera(eye or S.eye, S.target, vfov_deg=S.vfov_deg, aspect=w / h)
+        return RenderSettings(width=w, height=h, samples_per_launch=spp, nb_bounces=nb, light_sampling=LIGHT_POWER,
+                              bsdf=BSDF_PRINCIPLED, seed=seed, inverse_view=iv, inverse_projection=ip)
+
+    r = gbpt.Renderer(scene, settings(1920, 1080, 1, 3, 1))
+    r.set_restir_di(restir_di_settings(light_candidates=32, bsdf_candidates=1, m_cap=20, spatial_passes=1,
+                                       spatial_neighbors=5, spatial_radius=30))
+    r.render(3)
+    r.reset()
+    frame_ms = []
+    for f in range(8):
+        iv, ip = look_at_camera(_orbit(S.eye, S.target, 0.5 * f), S.target, vfov_deg=S.vfov_deg, aspect=1920 / 1080)
+        r.set_camera(iv, ip)
+        frame_ms.append(timed(lambda: r.render(1)))
+    st = r.stats()
+    rays = st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
+    tot = sum(frame_ms)
+    out["restir"] = {"config": "many-light scene 16.8M + 10k emissive tris, 1920x1080, 8 frames orbiting 0.5 deg, 3 bounces, "
+                               "ReSTIR DI 32+1 candidates, visibility reuse, M-cap 20, 1 spatial pass 5 neighbours 30 px",
+                     "ms_per_frame": tot / 8, "frame_ms": frame_ms, "samples_per_s": 1920 * 1080 * 8 / (tot * 1e-3),
+                     "mrays_per_s_traced": rays / (tot * 1e-3) / 1e6}
+    del r
+
+    # ---- guided against plain ----
+    W, H = guided_res
+    ref = gbpt.Renderer(scene, settings(W, H, 64, 8, 1000))
+    ref.render(32)
+    torch.cuda.synchronize()
+    gref = ref.image_sums()[1] / 2048
+    del ref
+    plain = []
+    for k in range(4):
+        p = gbpt.Renderer(scene, settings(W, H, 4, 8, 100 + k))
+        t = timed(lambda: p.render(16))
+        plain.append((t, _relmse(p.image_sums()[1] / 64, gref)))
+        del p
+    g = gbpt.Renderer(scene, settings(W, H, 4, 8, 200))
+    gd = guide.Guide(scene_min=S.box[0], scene_max=S.box[1])
+    g.set_guide(gd, guide_render_settings())
+    g.render(16)
+    guided = []
+    for k in range(4):
+        torch.cuda.synchronize()
+        prev = g.image_sums()[1]
+        t = timed(lambda: g.render(16))
+        guided.append((t, _relmse((g.image_sums()[1] - prev) / 64, gref)))
+    tp, ep = np.mean([a for a, _ in plain]), np.mean([b for _, b in plain])
+    tg, eg = np.mean([a for a, _ in guided]), np.mean([b for _, b in guided])
+    out["guided"] = {"config": f"many-light scene, {W}x{H}, 8 bounces, 64 spp per image, power NEE + MIS; guide: 16-level "
+                               "hash grid + 3x64 MLP, 8 vMF lobes + learned selection, 2^18 records/launch, Adam 1e-2",
+                     "plain_ms": tp, "plain_relmse": ep, "guided_ms": tg, "guided_relmse": eg,
+                     "plain_relmse_each": [b for _, b in plain], "guided_relmse_each": [b for _, b in guided],
+                     "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg), "guide_error_flag": gd.error_flag()}
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -220,6 +362,7 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=0.5)
     ap.add_argument("--ref-fraction", type=float, default=1.0 / 256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-render", action="store_true", help="skip the path-tracing workloads")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 2048x1024 primary + 1M bounce + 1M shadow rays, no e2e/CPU legs")
     args = ap.parse_args()
@@ -229,6 +372,7 @@ def main():
     if args.small:
         WIDTH, HEIGHT, N_BOUNCE, N_SHADOW = 2048, 1024, 1024 * 1024, 1024 * 1024
         args.no_cpu_baseline = True
+        args.no_render = True
         args.e2e_steps = 0
 
     rank = int(os.environ.get("RANK", "0"))
@@ -393,6 +537,10 @@ def main():
         del P, B, S
         base, _ = cpu_baseline_sample(make_cpu_impl(mesh, log=log), primary, bounce, shadow, args.cpu_fraction)
         line["cpu_baseline"] = base
+    if rank == 0 and not args.no_render:
+        del bvh
+        torch.cuda.empty_cache()
+        line["render"] = render_workloads(log, cpu_baseline=not args.no_cpu_baseline)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

@@ -108,13 +108,19 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
             prim = __float_as_int(hit.w);
             pb.shadow_entry[slot] = -1;
             pb.bsdf_entry[slot] = -1;
-            if (gv.train_entry) gv.train_entry[slot] = -1;
+            if (gv.train_entry)
+            {
+                gv.train_entry[slot] = -1;
+                gv.train_light_entry[slot] = -1;
+            }
         }
         const bool alive = valid && prim >= 0;
 
         bool want_shadow = false, want_bsdf = false, want_next = false, want_record = false;
-        V3 rec_tp = v3(0.0f), rec_dir = v3(0.0f);
-        float rec_pb = 0.0f;
+        bool guided_vertex = false, rec_vertex = false;
+        V3 rec_tp = v3(0.0f), rec_dir = v3(0.0f), lrec_dir = v3(0.0f);
+        float rec_pb = 0.0f, lrec_w = 0.0f, lrec_pb = 0.0f;
+        const uint32_t rec_thr = gv.train_entry ? *gv.rec_threshold : 0u;
         float4 sh_o, sh_d, bs_d, nx_d;
         V3 P = v3(0, 0, 0), tp = v3(0, 0, 0);
         V3 light_contrib = v3(0, 0, 0);
@@ -144,6 +150,12 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
             if constexpr (!PRINCIPLED)
             {
                 const V3 albedo = xyz(s.materials[mat].base_color);
+                // guided vertex: the continuation is drawn from the learned mixture / the BSDF and
+                // doubles as the BSDF technique of next-event estimation (MIS pdf alpha q + (1-alpha) p)
+                const float* GL = (gv.lobes && bounce < rc.nb_bounces) ? gv.lobes + guide::kRow * (int64_t)i : nullptr;
+                const float alpha = GL ? (gv.prob > 0.0f ? gv.prob : guide::alpha_at(GL)) : 0.0f;
+                guided_vertex = GL != nullptr;
+                rec_vertex = GL && gv.train_entry && record_hash((uint32_t)slot, (uint32_t)bounce, gv.frame) < rec_thr;
                 // ---- next-event estimation: light sample (sample_one_light_MIS, Lights.h:123-185) ----
                 if (s.n_emissive > 0)
                 {
@@ -161,9 +173,15 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                             if (cos_l > 1.0e-5f)
                             {
                                 const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
-                                const float mis = balance_heuristic(light_pdf, bsdf_pdf);
+                                const float other =
+                                    GL ? alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * bsdf_pdf : bsdf_pdf;
+                                const float mis = balance_heuristic(light_pdf, other);
                                 const float cosine = fabsf(dot(ns, wi));
-                                light_contrib = tp * (f * cosine * ls.emission * mis / light_pdf);
+                                const V3 est = f * cosine * ls.emission * mis / light_pdf;
+                                light_contrib = tp * est;
+                                lrec_dir = wi;
+                                lrec_w = luminance(est);
+                                lrec_pb = bsdf_pdf;
                                 if (!is_black(light_contrib))
                                 {
                                     want_shadow = true;
@@ -176,6 +194,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 }
 
                 // ---- next-event estimation: BSDF sample (Lights.h:187-226) ----
+                if (!GL)
                 {
                     const float r1 = rng.next(), r2 = rng.next();
                     const V3 wi = cosine_sample(ns, r1, r2);
@@ -195,12 +214,10 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 // one-sample MIS of the learned mixture and cosine sampling ----
                 if (bounce < rc.nb_bounces)
                 {
-                    const float* GL = gv.lobes ? gv.lobes + guide::kRow * (int64_t)i : nullptr;
                     V3 wi, f;
                     float pdf;
                     if (GL)
                     {
-                        const float alpha = gv.prob > 0.0f ? gv.prob : guide::alpha_at(GL);
                         if (rng.next() < alpha)
                         {
                             const float u0 = rng.next(), u1 = rng.next(), u2 = rng.next();
@@ -215,6 +232,13 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                         f = lambert_eval(albedo, dot(ns, wi), p_bsdf);
                         pdf = is_black(f) ? 0.0f : alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * p_bsdf;
                         rec_pb = p_bsdf;
+                        if (pdf > 0.0f && s.n_emissive > 0)
+                        {
+                            // the BSDF-technique ray of next-event estimation, along the continuation
+                            want_bsdf = true;
+                            bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                            bsdf_pending = f4(tp * (f * fabsf(dot(ns, wi)) / pdf), pdf);
+                        }
                     }
                     else
                     {
@@ -241,8 +265,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                         }
                         if (survive)
                         {
-                            want_record = GL && gv.train_entry &&
-                                          record_hash((uint32_t)slot, (uint32_t)bounce, gv.frame) < gv.rec_threshold;
+                            want_record = rec_vertex;
                             rec_tp = tp;
                             rec_dir = wi;
                             t2 = t2 * atten;
@@ -267,8 +290,17 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 md.eta_incident = md.inside ? m.ior : (cur_medium >= 0 ? s.pmats[cur_medium].ior : 1.0f);
                 md.eta_outgoing = md.inside ? 1.0f : m.ior;
                 next_medium = cur_medium;
+                // guided vertex (materials without delta lobes or transmission): the continuation is
+                // drawn from the learned mixture / the BSDF and, outside ReSTIR's bounce 0, doubles as
+                // the BSDF technique of next-event estimation (MIS pdf alpha q + (1 - alpha) p)
+                const float* GL = (gv.lobes && bounce < rc.nb_bounces && guidable(m))
+                                      ? gv.lobes + guide::kRow * (int64_t)i : nullptr;
+                const float alpha = GL ? (gv.prob > 0.0f ? gv.prob : guide::alpha_at(GL)) : 0.0f;
+                const bool restir_vertex = bounce == 0 && restir.s;
+                guided_vertex = GL != nullptr;
+                rec_vertex = GL && gv.train_entry && record_hash((uint32_t)slot, (uint32_t)bounce, gv.frame) < rec_thr;
 
-                if (bounce == 0 && restir.s)
+                if (restir_vertex)
                 {
                     // ---- direct lighting from the ReSTIR DI reservoir of the pixel
                     // (evaluate_ReSTIR_DI_reservoir, src/Device/includes/ReSTIR/DI/FinalShading.h:13-85) ----
@@ -331,9 +363,15 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                                 if (cos_l > 1.0e-5f)
                                 {
                                     const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
-                                    const float mis = balance_heuristic(light_pdf, bsdf_pdf);
+                                    const float other =
+                                        GL ? alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * bsdf_pdf : bsdf_pdf;
+                                    const float mis = balance_heuristic(light_pdf, other);
                                     const float cosine = fabsf(dot(ns, wi));
-                                    light_contrib = tp * (f * cosine * ls.emission * mis / light_pdf);
+                                    const V3 est = f * cosine * ls.emission * mis / light_pdf;
+                                    light_contrib = tp * est;
+                                    lrec_dir = wi;
+                                    lrec_w = luminance(est);
+                                    lrec_pb = bsdf_pdf;
                                     if (!is_black(light_contrib))
                                     {
                                         want_shadow = true;
@@ -346,6 +384,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                     }
 
                     // ---- next-event estimation: BSDF sample ----
+                    if (!GL)
                     {
                         bsdf::Xorshift32 xr = bsdf_rng(rng);
                         V3 wi;
@@ -366,13 +405,11 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 // one-sample MIS of the learned mixture and BSDF sampling ----
                 if (bounce < rc.nb_bounces)
                 {
-                    const float* GL = (gv.lobes && guidable(m)) ? gv.lobes + guide::kRow * (int64_t)i : nullptr;
                     V3 wi, f;
                     int lobe = GBPT_LOBE_NONE;
                     float pdf;
                     if (GL)
                     {
-                        const float alpha = gv.prob > 0.0f ? gv.prob : guide::alpha_at(GL);
                         float p_bsdf;
                         if (rng.next() < alpha)
                         {
@@ -394,6 +431,13 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                         }
                         pdf = is_black(f) ? 0.0f : alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * p_bsdf;
                         rec_pb = p_bsdf;
+                        if (pdf > 0.0f && s.n_emissive > 0 && !restir_vertex)
+                        {
+                            // the BSDF-technique ray of next-event estimation, along the continuation
+                            want_bsdf = true;
+                            bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                            bsdf_pending = f4(tp * (f * fabsf(dot(ns, wi)) / pdf), pdf);
+                        }
                     }
                     else
                     {
@@ -419,8 +463,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                         }
                         if (survive)
                         {
-                            want_record = GL && gv.train_entry &&
-                                          record_hash((uint32_t)slot, (uint32_t)bounce, gv.frame) < gv.rec_threshold;
+                            want_record = rec_vertex;
                             rec_tp = tp;
                             rec_dir = wi;
                             t2 = t2 * atten;
@@ -491,6 +534,26 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 gv.rec_slot[ri] = slot;
                 gv.train_entry[slot] = ri;
             }
+            const bool want_lrec = rec_vertex && want_shadow && lrec_w > 0.0f;
+            const int li = warp_append(gv.rec_count, want_lrec);
+            if (want_lrec && li < gv.rec_cap)
+            {
+                for (int a = 0; a < 3; a++)
+                {
+                    gv.rec_pos[3 * li + a] = gv.in_pos[3 * (int64_t)i + a];
+                    gv.rec_nrm[3 * li + a] = gv.in_nrm[3 * (int64_t)i + a];
+                    gv.rec_view[3 * li + a] = gv.in_view[3 * (int64_t)i + a];
+                }
+                gv.rec_dir[3 * li] = lrec_dir.x;
+                gv.rec_dir[3 * li + 1] = lrec_dir.y;
+                gv.rec_dir[3 * li + 2] = lrec_dir.z;
+                gv.rec_weight[li] = gv.weight_clamp > 0.0f ? fminf(lrec_w, gv.weight_clamp) : lrec_w;
+                gv.rec_pbsdf[li] = lrec_pb;
+                gv.rec_slot[li] = -1;
+                gv.train_light_entry[slot] = li;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, guided_vertex);
+            if ((threadIdx.x & 31) == 0 && m) atomicAdd(gv.rec_candidates, __popc(m));
         }
         warp_count(stats + 1, want_shadow);
         warp_count(stats + 2, want_bsdf);
@@ -510,8 +573,11 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst r
         const int slot = in.slot[i];
         const int se = pb.shadow_entry[slot];
         const int be = pb.bsdf_entry[slot];
-        // a guiding record of this vertex snapshots the radiance after its direct lighting
+        // a guiding record of this vertex snapshots the radiance after its direct lighting; its
+        // light-sample record loses its weight when the shadow ray is occluded
         const int te = gv.train_entry ? gv.train_entry[slot] : -1;
+        const int tle = gv.train_entry ? gv.train_light_entry[slot] : -1;
+        if (tle >= 0 && (se < 0 || shadow.occluded[se])) gv.rec_weight[tle] = 0.0f;
         if (se < 0 && be < 0)
         {
             if (te >= 0) gv.rec_snap[te] = pb.radiance[slot];
@@ -519,6 +585,10 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst r
         }
         V3 add = v3(0, 0, 0);
         if (se >= 0 && !shadow.occluded[se]) add = add + xyz(pb.pending_light[slot]);
+        const float4 r = pb.radiance[slot];
+        // a guiding record's snapshot: after the light sample, before the BSDF-technique emission
+        // (which arrives along the recorded direction and belongs to its training target)
+        if (te >= 0) gv.rec_snap[te] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
         if (be >= 0)
         {
             const float4 h = bsdfq.hits[be];
@@ -551,10 +621,7 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst r
                 }
             }
         }
-        const float4 r = pb.radiance[slot];
-        const float4 nr = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
-        pb.radiance[slot] = nr;
-        if (te >= 0) gv.rec_snap[te] = nr;
+        pb.radiance[slot] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
     }
 }
 
@@ -593,12 +660,24 @@ __global__ void __launch_bounds__(128) guide_inputs_kernel(SceneView s, Queue in
     }
 }
 
+// Recording fraction for the next launch: up to two records per candidate vertex, so that about
+// rec_cap records are made; the candidate counter restarts
+__global__ void guide_threshold_kernel(GuideView gv)
+{
+    const double cand = (double)max(*gv.rec_candidates, 1);
+    const double frac = (double)gv.rec_cap / (2.0 * cand);
+    *gv.rec_threshold = frac >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(frac * 4294967296.0);
+    *gv.rec_candidates = 0;
+}
+
 __global__ void guide_weights_kernel(PathBuffers pb, GuideView gv)
 {
     const int n = min(*gv.rec_count, gv.rec_cap);
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
     {
-        const V3 R = xyz(pb.radiance[gv.rec_slot[r]]);
+        const int sl = gv.rec_slot[r];
+        if (sl < 0) continue;  // light-sample record: weight already final
+        const V3 R = xyz(pb.radiance[sl]);
         const V3 S = xyz(gv.rec_snap[r]);
         const V3 T = xyz(gv.rec_tp[r]);
         const V3 ratio = v3(T.x > 0.0f ? fmaxf(R.x - S.x, 0.0f) / T.x : 0.0f, T.y > 0.0f ? fmaxf(R.y - S.y, 0.0f) / T.y : 0.0f,
@@ -828,6 +907,7 @@ cudaError_t launch_guide_inputs(const SceneView& s, const Queue& in, const Guide
 cudaError_t launch_guide_weights(const PathBuffers& pb, const GuideView& gv, int n_sm, cudaStream_t st)
 {
     guide_weights_kernel<<<grid_for(gv.rec_cap, 256, n_sm * 8), 256, 0, st>>>(pb, gv);
+    guide_threshold_kernel<<<1, 1, 0, st>>>(gv);
     return cudaGetLastError();
 }
 

@@ -893,6 +893,9 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
     {
         const int64_t nr = s->max_records;
         gv.train_entry = M.alloc<int32_t>(cap);
+        gv.train_light_entry = M.alloc<int32_t>(cap);
+        gv.rec_candidates = M.alloc<int32_t>(1);
+        gv.rec_threshold = M.alloc<uint32_t>(1);
         gv.rec_pos = M.alloc<float>(3 * nr);
         gv.rec_nrm = M.alloc<float>(3 * nr);
         gv.rec_view = M.alloc<float>(3 * nr);
@@ -904,14 +907,20 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
         gv.rec_slot = M.alloc<int32_t>(nr);
         gv.rec_count = M.alloc<int32_t>(1);
         gv.rec_cap = s->max_records;
-        // expected vertices with a continuation per launch: paths x bounces (an upper estimate)
-        const double expected = (double)cap * (r->rc.nb_bounces > 0 ? r->rc.nb_bounces : 1);
-        const double frac = std::min(1.0, (double)s->max_records / expected);
-        gv.rec_threshold = frac >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(frac * 4294967296.0);
         gv.weight_clamp = s->weight_clamp;
     }
     cudaError_t e = M.err;
-    if (e == cudaSuccess && gv.rec_count) e = cudaMemset(gv.rec_count, 0, sizeof(int32_t));
+    if (e == cudaSuccess && gv.rec_count)
+    {
+        // first launch: assume every path sample reaches every bounce (two records per vertex);
+        // later launches adapt to the counted candidates
+        const double expected = 2.0 * (double)cap * (r->rc.nb_bounces > 0 ? r->rc.nb_bounces : 1);
+        const double frac = std::min(1.0, (double)s->max_records / expected);
+        const uint32_t thr = frac >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(frac * 4294967296.0);
+        e = cudaMemset(gv.rec_count, 0, sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMemset(gv.rec_candidates, 0, sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMemcpy(gv.rec_threshold, &thr, sizeof(uint32_t), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess)
     {
         M.release();

@@ -72,10 +72,14 @@ struct PathBuffers
 // The continuation of a guidable vertex is drawn from the network's vMF mixture with probability
 // alpha (the network's selection output, or 'prob' when that is > 0), else from the BSDF, and
 // weighted by the one-sample MIS pdf alpha q + (1 - alpha) p_bsdf.
-// Training records hold (position, normal, view, sampled direction), the throughput before the
-// continuation and the path radiance after this vertex's direct lighting; after the launch the
-// record's weight is luminance((final radiance - snapshot) / throughput), the estimate of
-// f cos L_i / pdf of the sampled direction.
+// Training records hold (position, normal, view, direction) and a weight, the MIS-weighted estimate
+// of f cos L_i / pdf of that direction, for the two techniques of a recorded vertex:
+//   continuation: throughput before the continuation and the path radiance after the light sample;
+//                 after the launch the weight is luminance((final radiance - snapshot) / throughput)
+//   light sample: weight = luminance(f cos Le w_light / p_light), zeroed if the shadow ray is
+//                 occluded (slot -1: no snapshot)
+// Vertices are recorded when a hash of (slot, bounce, frame) is below a device-side threshold that
+// the end of each launch adapts to the launch's number of candidate vertices.
 struct GuideView
 {
     const float* lobes;  // per entry of the shaded queue: 8 x (mu xyz, kappa, weight), alpha
@@ -83,7 +87,8 @@ struct GuideView
     float* in_nrm;
     float* in_view;
     float prob;
-    int32_t* train_entry;  // per path slot: record made at this bounce, -1 (null: no training)
+    int32_t* train_entry;        // per path slot: continuation record made at this bounce, -1 (null: no training)
+    int32_t* train_light_entry;  // per path slot: light-sample record made at this bounce, -1
     float* rec_pos;        // per record: 3 floats each
     float* rec_nrm;
     float* rec_view;
@@ -94,8 +99,9 @@ struct GuideView
     float* rec_pbsdf;  // BSDF pdf of the recorded direction (trains the selection probability)
     int32_t* rec_slot;
     int32_t* rec_count;
+    int32_t* rec_candidates;         // guided vertices seen this launch
+    uint32_t* rec_threshold;         // a vertex is recorded when its hash is below this (device)
     int32_t rec_cap;
-    uint32_t rec_threshold;  // a vertex is recorded when its hash is below this
     uint32_t frame;
     float weight_clamp;      // 0: none
 };

@@ -302,3 +302,87 @@ def cornell_box() -> CornellBox:
     emission = np.asarray([(0, 0, 0), (0, 0, 0), (0, 0, 0), CORNELL_LIGHT_EMISSION], F32)
     mat = np.asarray(mats, np.int32)
     return CornellBox(Mesh(pos, idx), mat, albedo, emission, np.nonzero(mat == 3)[0].astype(np.int32))
+
+
+@dataclass
+class ManyLightScene:
+    mesh: Mesh
+    material_of_triangle: np.ndarray  # (T,) int32
+    materials: np.ndarray             # (M, 64) principled records (gbpt.materials layout)
+    n_emitters: int
+    box: tuple                        # scene bounds (lo xyz, hi xyz)
+    eye: tuple                        # camera at frame 0 (orbits about the y axis through target)
+    target: tuple
+    vfov_deg: float
+
+
+def many_light_scene(tile_cells: int = 128, grid=(32, 16), n_emitters: int = 10_000, seed: int = 1,
+                     spacing: float = 2.0) -> ManyLightScene:
+    """The many-light principled scene: grid[0] x grid[1] instances of a tile_cells^2-cell fBm
+    heightfield tile (amplitude 0.2, 6 octaves, over [-1, 1]^2: the traversal scene's heightfield at
+    a lower resolution), each rotated about y by U[0, 2 pi) and centred on a spacing-wide grid cell,
+    flattened; one random principled material per instance (gbpt.materials.random_principled);
+    n_emitters emissive triangles of side 0.05 (equilateral, facing down within 60 degrees of -y),
+    centres uniform over the grid in x/z at U[0.1, 1.0] above the surface, radiance log-uniform in
+    [1, 1000] times a colour U[0.2, 1]^3, one material each. Defaults: 512 x 32,768 = 16,777,216
+    triangles + 10,000 emitters."""
+    from . import materials as M
+    rng = np.random.Generator(np.random.PCG64(seed + 7))
+    tile = heightfield(tile_cells, 0.2, seed, 6)
+    nx, nz = grid
+    n_inst = nx * nz
+    ang = rng.uniform(0.0, 2.0 * np.pi, n_inst)
+    cx = (np.arange(nx) - (nx - 1) / 2.0) * spacing
+    cz = (np.arange(nz) - (nz - 1) / 2.0) * spacing
+    centres = np.stack(np.meshgrid(cx, cz, indexing="xy"), -1).reshape(-1, 2)  # instance k = j * nx + i
+    tp = tile.positions.astype(np.float64)
+    c, s = np.cos(ang)[:, None], np.sin(ang)[:, None]
+    X = c * tp[None, :, 0] + s * tp[None, :, 2] + centres[:, :1]
+    Z = -s * tp[None, :, 0] + c * tp[None, :, 2] + centres[:, 1:]
+    Y = np.broadcast_to(tp[None, :, 1], X.shape)
+    pos = np.stack([X, Y, Z], -1).reshape(-1, 3)
+    nv = tp.shape[0]
+    idx = (tile.indices[None, :, :] + (np.arange(n_inst) * nv)[:, None, None]).reshape(-1, 3)
+    mat_of = np.repeat(np.arange(n_inst, dtype=np.int32), tile.indices.shape[0])
+
+    # emitters: surface height from the owning instance's fBm (local coordinates clamped to the tile)
+    ex = rng.uniform(cx[0] - spacing / 2, cx[-1] + spacing / 2, n_emitters)
+    ez = rng.uniform(cz[0] - spacing / 2, cz[-1] + spacing / 2, n_emitters)
+    ii = np.clip(np.round((ex - cx[0]) / spacing).astype(int), 0, nx - 1)
+    jj = np.clip(np.round((ez - cz[0]) / spacing).astype(int), 0, nz - 1)
+    k = jj * nx + ii
+    dx, dz = ex - centres[k, 0], ez - centres[k, 1]
+    lx = np.clip(np.cos(ang[k]) * dx - np.sin(ang[k]) * dz, -1, 1)
+    lz = np.clip(np.sin(ang[k]) * dx + np.cos(ang[k]) * dz, -1, 1)
+    ground = 0.2 * value_noise_fbm(lx, lz, seed=seed, octaves=6)
+    ey = ground + rng.uniform(0.1, 1.0, n_emitters)
+    # equilateral triangle of side 0.05 in a plane whose normal is within 60 degrees of -y
+    theta = np.arccos(rng.uniform(np.cos(np.radians(60.0)), 1.0, n_emitters))
+    phi = rng.uniform(0, 2 * np.pi, n_emitters)
+    nrm = np.stack([np.sin(theta) * np.cos(phi), -np.cos(theta), np.sin(theta) * np.sin(phi)], -1)
+    a = np.where(np.abs(nrm[:, :1]) < 0.9, np.array([[1.0, 0, 0]]), np.array([[0.0, 0, 1]]))
+    u = _normalize(np.cross(nrm, a))
+    v = np.cross(nrm, u)
+    r = 0.05 / np.sqrt(3.0)  # circumradius
+    beta = rng.uniform(0, 2 * np.pi, n_emitters)[:, None]
+    corners = []
+    for q in range(3):
+        t = beta + q * 2.0 * np.pi / 3.0
+        corners.append(np.stack([ex, ey, ez], -1) + r * (np.cos(t) * u + np.sin(t) * v))
+    # winding so that the geometric normal (b - a) x (c - a) is nrm
+    tri = np.stack([corners[0], corners[2], corners[1]], 1)
+    g = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    flip = (g * nrm).sum(-1) < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    e_pos = tri.reshape(-1, 3)
+    e_idx = np.arange(3 * n_emitters).reshape(-1, 3) + pos.shape[0]
+    rad = np.exp(rng.uniform(0.0, np.log(1000.0), n_emitters))[:, None] * rng.uniform(0.2, 1.0, (n_emitters, 3))
+
+    mats = M.pack_many(M.random_principled(rng, n_inst))
+    emat = np.stack([M.pack(base_color=(0.0, 0.0, 0.0), emission=tuple(float(x) for x in e)) for e in rad])
+    mesh = Mesh(np.concatenate([pos, e_pos]).astype(F32), np.concatenate([idx, e_idx]).astype(np.int32))
+    mat_of = np.concatenate([mat_of, n_inst + np.arange(n_emitters, dtype=np.int32)])
+    lo = tuple(float(x) for x in mesh.positions.min(0))
+    hi = tuple(float(x) for x in mesh.positions.max(0))
+    return ManyLightScene(mesh, mat_of, np.concatenate([mats, emat]).astype(F32), n_emitters, (lo, hi),
+                          eye=(0.0, 7.0, -26.0), target=(0.0, 0.0, 0.0), vfov_deg=45.0)

@@ -212,8 +212,11 @@ GBPT_API gbpt_status gbpt_restir_di_set_reservoirs(gbpt_renderer* r, int32_t whi
  * selection probability, or guide_probability when that is > 0), else from the BSDF; the path
  * weight uses the one-sample MIS pdf alpha q + (1 - alpha) p_bsdf, so the image stays unbiased
  * whatever the network has learned. Direct lighting (NEE, ReSTIR DI) is unchanged.
- * With train = 1, vertices are recorded (a hash of pixel sample, bounce and frame picks about
- * max_records per launch) and gbpt_pass_accumulate ends the launch with one Adam step on them.
+ * With train = 1, guided vertices are recorded (a hash of pixel sample, bounce and frame picks
+ * about max_records records per launch, the fraction adapting to the previous launch's vertex
+ * count): one record for the continuation and one for the light sample, each weighted by its
+ * MIS-weighted estimate of f cos L_i / pdf; gbpt_pass_accumulate ends the launch with one Adam
+ * step on them.
  * gbpt_renderer_reset restarts the sample index, so the launches after it draw the random numbers
  * of the launches the network was trained on: for an estimate independent of the training
  * samples, keep rendering (differences of accumulated images) or change the seed. */
@@ -231,7 +234,8 @@ GBPT_API gbpt_status gbpt_guide_render_default_settings(gbpt_guide_render_settin
 /* Attaches 'g' (not owned; it must outlive its use) or detaches it (g NULL or enabled = 0). */
 GBPT_API gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_guide_render_settings* s);
 /* The last launch's training records, 15 floats each: position xyz, normal xyz, view xyz,
- * direction xyz, weight, BSDF pdf of the direction, pixel-sample slot (int32 bits). Copies min(count, capacity) records to
+ * direction xyz, weight, BSDF pdf of the direction, pixel-sample slot (int32 bits; -1 for a
+ * light-sample record). Copies min(count, capacity) records to
  * host_out (may be NULL) and the number made (before the max_records cap) to *count. Synchronous. */
 GBPT_API gbpt_status gbpt_renderer_get_guide_records(gbpt_renderer* r, float* host_out, int32_t capacity, int32_t* count,
                                                      void* stream);

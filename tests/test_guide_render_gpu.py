@@ -86,7 +86,9 @@ def test_training_records_are_well_formed(cuda, indirect_reference):
     # Lambertian continuations leave above the surface (the shading normal may be bent slightly)
     assert ((nrm * d).sum(1) > -0.1).all() and ((nrm * d).sum(1) > 0).mean() > 0.99
     assert np.isfinite(w).all() and (w >= 0).all() and (w <= 50.0).all() and (w > 0).mean() > 0.05
-    assert (slot >= 0).all() and (slot < 32 * 32 * 4).all()
+    # continuation records carry their path slot, light-sample records -1
+    assert ((slot >= 0) | (slot == -1)).all() and (slot < 32 * 32 * 4).all()
+    assert (slot == -1).any() and (slot >= 0).any()
     # the recorded BSDF pdf is the Lambertian cos / pi of the recorded direction (about the shading
     # normal, which equals the recorded geometric normal unless it was bent)
     close = np.abs(pb - np.maximum((nrm * d).sum(1), 0) / np.pi) < 2e-3
