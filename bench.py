@@ -40,6 +40,7 @@ RAY_IN_BYTES = 36  # origin+tmin, direction+tmax, last_prim
 CLOSEST_OUT_BYTES = 16
 ANY_OUT_BYTES = 1
 NODE_BYTES = 80
+KERNEL_NAMES = {1: "trace_ray_kernel", 2: "trace_persistent"}
 TRI_BYTES = 36  # algorithmic: three float3 vertex records
 
 
@@ -321,7 +322,61 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
                      "plain_ms": tp, "plain_relmse": ep, "guided_ms": tg, "guided_relmse": eg,
                      "plain_relmse_each": [b for _, b in plain], "guided_relmse_each": [b for _, b in guided],
                      "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg), "guide_error_flag": gd.error_flag()}
+    # ---- guided against plain on the indirectly lit Cornell box ----
+    out["guided_indirect_cornell"] = guided_indirect_cornell(timed)
     return out
+
+
+def indirect_cornell_scene():
+    """The Cornell box with its light lowered to y = 4.5 and turned to face the ceiling: the room is
+    lit almost only by the bright patch the light makes on the ceiling."""
+    import gbpt
+    from gbpt import scenes
+    cb = scenes.cornell_box()
+    pos = cb.mesh.positions.copy()
+    for t in cb.emissive_triangles:
+        i = cb.mesh.indices[t]
+        pos[i, 1] = 4.5
+        pos[[i[1], i[2]]] = pos[[i[2], i[1]]]
+    return gbpt.Scene(pos, cb.mesh.indices, cb.material_of_triangle, cb.albedo, cb.emission)
+
+
+def guided_indirect_cornell(timed, res=128, warm_launches=100):
+    """Plain against guided path tracing on the indirectly lit Cornell box, res x res, 4 bounces,
+    Lambertian: 4 independent 64-spp images each after the guide's warm-up of warm_launches x 4 spp
+    (not timed); relMSE against a 16384-spp plain FP64 image."""
+    import torch
+    import gbpt
+    from gbpt import guide
+    from gbpt.render import guide_render_settings
+    scene = indirect_cornell_scene()
+    ref = gbpt.Renderer(scene, gbpt.cornell_settings(res, res, samples_per_launch=256, seed=1000))
+    ref.render(64)
+    torch.cuda.synchronize()
+    cref = ref.image_sums()[1] / 16384
+    del ref
+    plain = []
+    for k in range(4):
+        p = gbpt.Renderer(scene, gbpt.cornell_settings(res, res, samples_per_launch=4, seed=100 + k))
+        t = timed(lambda: p.render(16))
+        plain.append((t, _relmse(p.image_sums()[1] / 64, cref)))
+    g = gbpt.Renderer(scene, gbpt.cornell_settings(res, res, samples_per_launch=4, seed=200))
+    gd = guide.Guide(scene_min=(0, 0, 0), scene_max=(5.5, 5.5, 5.5))
+    g.set_guide(gd, guide_render_settings())
+    g.render(warm_launches)
+    guided = []
+    for k in range(4):
+        torch.cuda.synchronize()
+        prev = g.image_sums()[1]
+        t = timed(lambda: g.render(16))
+        guided.append((t, _relmse((g.image_sums()[1] - prev) / 64, cref)))
+    tp, ep = np.mean([a for a, _ in plain]), np.mean([b for _, b in plain])
+    tg, eg = np.mean([a for a, _ in guided]), np.mean([b for _, b in guided])
+    return {"config": f"Cornell box lit through the ceiling, {res}x{res}, 4 bounces, Lambert, 64 spp per image, guide warm-up "
+                      f"{warm_launches} x 4 spp (untimed); training continues during the timed images",
+            "plain_ms": tp, "plain_relmse": ep, "guided_ms": tg, "guided_relmse": eg,
+            "equal_spp_relmse_ratio": eg / ep, "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg),
+            "guide_error_flag": gd.error_flag()}
 
 
 def run_reference(args, rank, world):
@@ -429,16 +484,25 @@ def main():
     stream = torch.cuda.current_stream()
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
 
+    # launch configurations picked by the autotuner per ray class (outside the timed region)
+    t0 = time.time()
+    cfg_p, _ = bvh.autotune(*P, store=False)
+    cfg_b, _ = bvh.autotune(*B, store=False)
+    cfg_s, _ = bvh.autotune(*S, any_hit=True, store=False)
+    log(f"autotune {time.time() - t0:.1f}s: primary {cfg_p}, bounce {cfg_b}, shadow {cfg_s}")
+    bvh.set_trace_config(False, **cfg_b)
+    bvh.set_trace_config(True, **cfg_s)
+
     def step(e=None):
         if e is not None:
             e[0].record(stream)
-        bvh.closest(*P, out=hits_p)
+        bvh.closest_cfg(*P, out=hits_p, **cfg_p)
         if e is not None:
             e[1].record(stream)
-        bvh.closest(*B, out=hits_b)
+        bvh.closest_cfg(*B, out=hits_b, **cfg_b)
         if e is not None:
             e[2].record(stream)
-        bvh.occluded(*S, out=occ_s)
+        bvh.occluded_cfg(*S, out=occ_s, **cfg_s)
         if e is not None:
             e[3].record(stream)
 
@@ -487,7 +551,9 @@ def main():
     out_s = torch.empty((len(shadow),), dtype=torch.uint8).pin_memory()
 
     def e2e_step():
+        bvh.set_trace_config(False, **cfg_p)
         bvh.closest_host(*hp, out=out_p.numpy())
+        bvh.set_trace_config(False, **cfg_b)
         bvh.closest_host(*hb, out=out_b.numpy())
         bvh.occluded_host(*hs, out=out_s.numpy())
 
@@ -522,7 +588,8 @@ def main():
                       "tris_per_ray": {"primary": cp[1] / len(primary), "bounce": cb[1] / len(bounce),
                                        "shadow": cs[1] / len(shadow)},
                       "bvh_build_s": st["build_seconds"], "bvh_nodes": st["n_nodes"], "bvh_depth": st["wide_depth"]},
-        "roofline": {"bound": "hbm", "kernel": "trace_kernel<closest> (primary + bounce launches)",
+        "roofline": {"bound": "hbm", "kernel": "closest-hit traversal (primary + bounce launches: "
+                     f"{KERNEL_NAMES[cfg_p['kernel']]} + {KERNEL_NAMES[cfg_b['kernel']]})",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "algorithmic_bytes_per_launch": alg_closest / 2,
@@ -531,6 +598,7 @@ def main():
                 "h2d_bytes_per_step": n_rays * RAY_IN_BYTES,
                 "d2h_bytes_per_step": (len(primary) + len(bounce)) * CLOSEST_OUT_BYTES + len(shadow) * ANY_OUT_BYTES},
         "gpu_launches": 3 * args.steps,
+        "trace_configs": {"primary": cfg_p, "bounce": cfg_b, "shadow": cfg_s},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -6,6 +6,7 @@
 // thread-local message; nothing exits, aborts or traps.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -128,6 +129,7 @@ gbpt_status gbpt_bvh_build(const int32_t* indices, const float* positions, int64
     b->dev.tris = dt;
     b->dev.n_nodes = (int64_t)host.nodes.size();
     b->dev.n_tris = (int64_t)(host.tris.size() / 12);
+    b->dev.depth = host.wide_depth;
     std::memset(&b->stats, 0, sizeof(b->stats));
     b->stats.n_triangles = n_triangles;
     b->stats.n_bvh_triangles = b->dev.n_tris;
@@ -169,7 +171,7 @@ gbpt_status gbpt_trace_closest(const gbpt_bvh* bvh, const float* origin_tmin, co
     if (n_rays > 0 && !hits) return fail(GBPT_ERROR_INVALID_ARG, "hits is NULL");
     if (!aligned16(hits)) return fail(GBPT_ERROR_INVALID_ARG, "hits must be 16-byte aligned");
     cudaError_t e = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, hits, nullptr, false, nullptr,
-                                       (cudaStream_t)stream);
+                                       (cudaStream_t)stream, &bvh->cfg[0]);
     return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "closest-hit launch");
 }
 
@@ -180,7 +182,7 @@ gbpt_status gbpt_trace_any(const gbpt_bvh* bvh, const float* origin_tmin, const 
     if (s != GBPT_OK) return s;
     if (n_rays > 0 && !occluded) return fail(GBPT_ERROR_INVALID_ARG, "occluded is NULL");
     cudaError_t e = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, nullptr, occluded, true,
-                                       nullptr, (cudaStream_t)stream);
+                                       nullptr, (cudaStream_t)stream, &bvh->cfg[1]);
     return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "any-hit launch");
 }
 
@@ -219,7 +221,7 @@ static gbpt_status trace_host(const gbpt_bvh* bvh, const float* origin_tmin, con
     if (e == cudaSuccess && d_lp) e = cudaMemcpyAsync(d_lp, last_prim, (size_t)n * 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
         e = gbpt::launch_trace(bvh->dev, d_o, d_d, d_lp, n, any_hit ? nullptr : (float*)d_out,
-                               any_hit ? (uint8_t*)d_out : nullptr, any_hit, nullptr, st);
+                               any_hit ? (uint8_t*)d_out : nullptr, any_hit, nullptr, st, &bvh->cfg[any_hit ? 1 : 0]);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, st);
     cudaError_t ef = cudaFreeAsync(buf, st);
     if (e == cudaSuccess) e = ef;
@@ -238,6 +240,155 @@ gbpt_status gbpt_trace_any_host(const gbpt_bvh* bvh, const float* origin_tmin, c
                                 const int32_t* last_prim, int64_t n_rays, uint8_t* occluded, void* stream)
 {
     return trace_host(bvh, origin_tmin, dir_tmax, last_prim, n_rays, occluded, true, (cudaStream_t)stream);
+}
+
+namespace {
+
+gbpt::TraceConfig from_c(const gbpt_trace_config& c)
+{
+    gbpt::TraceConfig t;
+    t.kernel = c.kernel;
+    t.block = c.block;
+    t.refill_below = c.refill_below;
+    t.postpone_below = c.postpone_below;
+    t.blocks_per_sm = c.blocks_per_sm;
+    return t;
+}
+
+gbpt_trace_config to_c(const gbpt::TraceConfig& t)
+{
+    gbpt_trace_config c;
+    std::memset(&c, 0, sizeof(c));
+    c.kernel = t.kernel;
+    c.block = t.block;
+    c.refill_below = t.refill_below;
+    c.postpone_below = t.postpone_below;
+    c.blocks_per_sm = t.blocks_per_sm;
+    return c;
+}
+
+}  // namespace
+
+gbpt_status gbpt_bvh_set_trace_config(gbpt_bvh* bvh, int32_t any_hit, const gbpt_trace_config* cfg)
+{
+    if (!bvh || !cfg) return fail(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    const gbpt::TraceConfig t = from_c(*cfg);
+    if (!gbpt::valid_trace_config(t)) return fail(GBPT_ERROR_INVALID_ARG, "invalid trace configuration");
+    bvh->cfg[any_hit ? 1 : 0] = t;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_bvh_get_trace_config(const gbpt_bvh* bvh, int32_t any_hit, gbpt_trace_config* cfg)
+{
+    if (!bvh || !cfg) return fail(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    *cfg = to_c(bvh->cfg[any_hit ? 1 : 0]);
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_trace_closest_cfg(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                   const int32_t* last_prim, int64_t n_rays, float* hits, const gbpt_trace_config* cfg,
+                                   void* stream)
+{
+    gbpt_status s = check_rays(bvh, origin_tmin, dir_tmax, n_rays);
+    if (s != GBPT_OK) return s;
+    if (n_rays > 0 && !hits) return fail(GBPT_ERROR_INVALID_ARG, "hits is NULL");
+    if (!aligned16(hits)) return fail(GBPT_ERROR_INVALID_ARG, "hits must be 16-byte aligned");
+    const gbpt::TraceConfig t = cfg ? from_c(*cfg) : bvh->cfg[0];
+    if (!gbpt::valid_trace_config(t)) return fail(GBPT_ERROR_INVALID_ARG, "invalid trace configuration");
+    cudaError_t e = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, hits, nullptr, false, nullptr,
+                                       (cudaStream_t)stream, &t);
+    return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "closest-hit launch");
+}
+
+gbpt_status gbpt_trace_any_cfg(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                               const int32_t* last_prim, int64_t n_rays, uint8_t* occluded, const gbpt_trace_config* cfg,
+                               void* stream)
+{
+    gbpt_status s = check_rays(bvh, origin_tmin, dir_tmax, n_rays);
+    if (s != GBPT_OK) return s;
+    if (n_rays > 0 && !occluded) return fail(GBPT_ERROR_INVALID_ARG, "occluded is NULL");
+    const gbpt::TraceConfig t = cfg ? from_c(*cfg) : bvh->cfg[1];
+    if (!gbpt::valid_trace_config(t)) return fail(GBPT_ERROR_INVALID_ARG, "invalid trace configuration");
+    cudaError_t e = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, nullptr, occluded, true,
+                                       nullptr, (cudaStream_t)stream, &t);
+    return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "any-hit launch");
+}
+
+gbpt_status gbpt_trace_autotune(gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax, const int32_t* last_prim,
+                                int64_t n_rays, int32_t any_hit, int32_t store, gbpt_trace_config* best_out,
+                                float* best_ms_out, void* stream)
+{
+    gbpt_status s = check_rays(bvh, origin_tmin, dir_tmax, n_rays);
+    if (s != GBPT_OK) return s;
+    if (n_rays <= 0) return fail(GBPT_ERROR_INVALID_ARG, "autotuning needs rays");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool ah = any_hit != 0;
+    void* out = nullptr;
+    cudaError_t e = cudaMallocAsync(&out, (size_t)n_rays * (ah ? 1 : 16), st);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune scratch");
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    // time per launch: the faster of two runs (the first also warms the caches)
+    auto timed = [&](const gbpt::TraceConfig& c, float& ms) -> cudaError_t {
+        ms = 1e30f;
+        for (int rep = 0; rep < 2; rep++)
+        {
+            cudaError_t err = cudaEventRecord(ev0, st);
+            if (err == cudaSuccess)
+                err = gbpt::launch_trace(bvh->dev, origin_tmin, dir_tmax, last_prim, n_rays, ah ? nullptr : (float*)out,
+                                         ah ? (uint8_t*)out : nullptr, ah, nullptr, st, &c);
+            if (err == cudaSuccess) err = cudaEventRecord(ev1, st);
+            if (err == cudaSuccess) err = cudaEventSynchronize(ev1);
+            float t = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&t, ev0, ev1);
+            if (err != cudaSuccess) return err;
+            ms = std::min(ms, t);
+        }
+        return cudaSuccess;
+    };
+    gbpt::TraceConfig best = bvh->cfg[ah ? 1 : 0];
+    float best_ms = 0.0f;
+    e = timed(best, best_ms);
+    const int kernels[] = {gbpt::kTraceKernelPerRay, gbpt::kTraceKernelPersistent};
+    const int blocks[] = {64, 128, 256};
+    const int refills[] = {4, 8, 12, 16, 20, 24};
+    const int postpones[] = {0, 4, 8, 12, 16, 24};
+    const int per_sm[] = {2, 4, 8, 12, 16};
+    for (int pass = 0; pass < 2 && e == cudaSuccess; pass++)
+    {
+        for (int coord = 0; coord < 5 && e == cudaSuccess; coord++)
+        {
+            if (coord >= 2 && best.kernel != gbpt::kTraceKernelPersistent) break;
+            const int* vals = coord == 0 ? kernels : coord == 1 ? blocks : coord == 2 ? refills : coord == 3 ? postpones : per_sm;
+            const int nv = coord == 0 ? 2 : coord == 1 ? 3 : coord == 4 ? 5 : 6;
+            for (int k = 0; k < nv && e == cudaSuccess; k++)
+            {
+                gbpt::TraceConfig c = best;
+                int* field = coord == 0 ? &c.kernel : coord == 1 ? &c.block : coord == 2 ? &c.refill_below
+                                                                  : coord == 3 ? &c.postpone_below : &c.blocks_per_sm;
+                if (*field == vals[k]) continue;
+                *field = vals[k];
+                float ms = 0.0f;
+                e = timed(c, ms);
+                if (e == cudaSuccess && ms < best_ms)
+                {
+                    best = c;
+                    best_ms = ms;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    cudaError_t ef = cudaFreeAsync(out, st);
+    if (e == cudaSuccess) e = ef;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune");
+    if (store) bvh->cfg[ah ? 1 : 0] = best;
+    if (best_out) *best_out = to_c(best);
+    if (best_ms_out) *best_ms_out = best_ms;
+    return GBPT_OK;
 }
 
 }  // extern "C"

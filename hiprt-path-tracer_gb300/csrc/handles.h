@@ -11,6 +11,7 @@ struct gbpt_bvh
     gbpt::DeviceBVH dev;
     gbpt_bvh_stats stats;
     int device = 0;
+    gbpt::TraceConfig cfg[2] = {gbpt::default_trace_config(false), gbpt::default_trace_config(true)};
 };
 
 namespace gbpt {

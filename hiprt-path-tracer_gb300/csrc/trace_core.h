@@ -11,9 +11,10 @@
 //
 // The triangle test is the reference's Moller-Trumbore (src/Renderer/Triangle.h:20-63) written
 // with explicitly rounded operations (__fmul_rn/__fadd_rn/__fsub_rn/__fdiv_rn), which the compiler
-// never contracts into FMAs, so t/u/v match the reference's CPU results bit for bit. Box tests use
-// FMAs and a small relative slack: they only prune, so their rounding cannot change a result as
-// long as they stay conservative.
+// never contracts into FMAs, so t/u/v match the reference's CPU results bit for bit. Box tests only
+// prune, so their rounding cannot change a result as long as they stay conservative: each node
+// widens its children's slab intervals by an absolute slack that bounds every rounding of the test
+// (derivation at intersect_children).
 #pragma once
 
 #include <stddef.h>
@@ -45,6 +46,13 @@ inline float __int_as_float(int32_t u) { float f; std::memcpy(&f, &u, 4); return
 inline int32_t __float_as_int(float f) { int32_t u; std::memcpy(&u, &f, 4); return u; }
 inline uint32_t __clz(uint32_t x) { return x ? (uint32_t)__builtin_clz(x) : 32u; }
 inline uint32_t __popc(uint32_t x) { return (uint32_t)__builtin_popcount(x); }
+inline uint32_t __byte_perm(uint32_t x, uint32_t y, uint32_t s)
+{
+    const uint64_t v = ((uint64_t)y << 32) | x;
+    uint32_t r = 0;
+    for (int i = 0; i < 4; i++) r |= (uint32_t)((v >> (8 * ((s >> (4 * i)) & 7u))) & 0xFFu) << (8 * i);
+    return r;
+}
 inline int __ffs(uint32_t x) { return __builtin_ffs((int)x); }
 using ::copysignf;
 using ::fabsf;
@@ -57,7 +65,6 @@ namespace gbpt {
 namespace core {
 
 constexpr float kMtEps = 0.0000001f;     // EPSILON of src/Renderer/Triangle.h:24
-constexpr float kBoxSlack = 1.0f / 131072.0f;  // relative widening of box slab intervals (2^-17)
 
 GBPT_HD float dot_rn(float ax, float ay, float az, float bx, float by, float bz)
 {
@@ -98,7 +105,40 @@ GBPT_HD float safe_rcp(float d)
     return __frcp_rn(fabsf(d) < tiny ? copysignf(tiny, d) : d);
 }
 
+// Quantised plane q (byte k of word w) as the float 2^23 + 256 q, built by one byte permute
+GBPT_HD float plane_magic(uint32_t w, int k)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7404u | ((uint32_t)k << 4)));
+}
+
 GBPT_HD uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
+
+// Per-axis slab constants of a node: a child plane q on this axis is entered at
+// t = fma(2^23 + 256 q, s8, base), with s8 = 2^(e-127) id / 256 (exact: power-of-two scalings)
+// and base = (p - o) id - 2^15 * 2^(e-127) id, so that t = q 2^(e-127) id + (p - o) id.
+// Rounding: (p - o), the product with id (itself a rounded reciprocal), base and the final FMA
+// each err by at most one half ulp of a value bounded by |a| + 2^15 |s| + 255 |s| (a = (p - o) id,
+// s = 2^(e-127) id), i.e. in total below 8 (|a| + 2^16 |s|) 2^-24. The slack
+// eps = (|a| + 2^16 |s|) 2^-20 is twice that: subtracted from the near planes' base and added to
+// the far planes' (those two roundings are covered by the same margin), it keeps the test
+// conservative for every child.
+struct AxisSlab
+{
+    float s8, near_base, far_base;
+};
+
+GBPT_HD AxisSlab axis_slab(float p, float o, uint32_t e, float id)
+{
+    const float s = __uint_as_float(e << 23) * id;
+    const float a = (p - o) * id;
+    const float base = fmaf(-32768.0f, s, a);
+    const float eps = (fabsf(a) + 65536.0f * fabsf(s)) * (1.0f / 1048576.0f);
+    AxisSlab r;
+    r.s8 = s * (1.0f / 256.0f);
+    r.near_base = base - eps;
+    r.far_base = base + eps;
+    return r;
+}
 
 // Intersects the 8 children of one node; returns the hit mask (bits 24-31: internal children by
 // octant-ordered slot, bits 0-23: triangles relative to the node's triangle base).
@@ -106,11 +146,9 @@ GBPT_HD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 
                                                        const uint4 w4, float ox, float oy, float oz, float idx,
                                                        float idy, float idz, float tmin, float tmax, uint32_t oct_inv)
 {
-    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-    const float sx = __uint_as_float((w0.w & 0xFFu) << 23) * idx;
-    const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23) * idy;
-    const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23) * idz;
-    const float ax = (px - ox) * idx, ay = (py - oy) * idy, az = (pz - oz) * idz;
+    const AxisSlab X = axis_slab(__uint_as_float(w0.x), ox, w0.w & 0xFFu, idx);
+    const AxisSlab Y = axis_slab(__uint_as_float(w0.y), oy, (w0.w >> 8) & 0xFFu, idy);
+    const AxisSlab Z = axis_slab(__uint_as_float(w0.z), oz, (w0.w >> 16) & 0xFFu, idz);
 
     // near/far planes per axis by ray sign: words hold 4 children's bytes each
     uint32_t nx0 = w2.x, nx1 = w2.y, fx0 = w3.z, fx1 = w3.w;
@@ -124,17 +162,16 @@ GBPT_HD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 
 #pragma unroll
     for (int i = 0; i < 8; i++)
     {
-        const uint32_t meta = byte_of(i < 4 ? w1.z : w1.w, i & 3);
-        const uint32_t qnx = byte_of(i < 4 ? nx0 : nx1, i & 3), qfx = byte_of(i < 4 ? fx0 : fx1, i & 3);
-        const uint32_t qny = byte_of(i < 4 ? ny0 : ny1, i & 3), qfy = byte_of(i < 4 ? fy0 : fy1, i & 3);
-        const uint32_t qnz = byte_of(i < 4 ? nz0 : nz1, i & 3), qfz = byte_of(i < 4 ? fz0 : fz1, i & 3);
-        const float tx0 = fmaf((float)qnx, sx, ax), tx1 = fmaf((float)qfx, sx, ax);
-        const float ty0 = fmaf((float)qny, sy, ay), ty1 = fmaf((float)qfy, sy, ay);
-        const float tz0 = fmaf((float)qnz, sz, az), tz1 = fmaf((float)qfz, sz, az);
-        float t_enter = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, tmin));
-        float t_exit = fminf(fminf(tx1, ty1), fminf(tz1, tmax));
-        t_enter -= fabsf(t_enter) * kBoxSlack;
-        t_exit += fabsf(t_exit) * kBoxSlack;
+        const int k = i & 3;
+        const float tx0 = fmaf(plane_magic(i < 4 ? nx0 : nx1, k), X.s8, X.near_base);
+        const float tx1 = fmaf(plane_magic(i < 4 ? fx0 : fx1, k), X.s8, X.far_base);
+        const float ty0 = fmaf(plane_magic(i < 4 ? ny0 : ny1, k), Y.s8, Y.near_base);
+        const float ty1 = fmaf(plane_magic(i < 4 ? fy0 : fy1, k), Y.s8, Y.far_base);
+        const float tz0 = fmaf(plane_magic(i < 4 ? nz0 : nz1, k), Z.s8, Z.near_base);
+        const float tz1 = fmaf(plane_magic(i < 4 ? fz0 : fz1, k), Z.s8, Z.far_base);
+        const float t_enter = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, tmin));
+        const float t_exit = fminf(fminf(tx1, ty1), fminf(tz1, tmax));
+        const uint32_t meta = byte_of(i < 4 ? w1.z : w1.w, k);
         const bool inner = (meta & 0x18u) == 0x18u;
         const uint32_t bit_index = inner ? ((meta & 0x1Fu) ^ oct_inv) : (meta & 0x1Fu);
         const uint32_t child_bits = meta >> 5;

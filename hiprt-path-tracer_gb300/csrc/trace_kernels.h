@@ -12,10 +12,27 @@ struct DeviceBVH
     const void* tris = nullptr;   // float4[3 * n_tris]
     int64_t n_nodes = 0;
     int64_t n_tris = 0;
+    int32_t depth = 0;  // wide depth (bounds the traversal stack's node groups)
 };
 
+// Launch configuration of a traversal (the fields of gbpt_trace_config)
+constexpr int kTraceKernelPerRay = 1;      // one thread per ray
+constexpr int kTraceKernelPersistent = 2;  // persistent warps with lane refill and triangle postponing
+struct TraceConfig
+{
+    int32_t kernel;
+    int32_t block;           // threads per block
+    int32_t refill_below;    // persistent: refill when fewer lanes than this trace
+    int32_t postpone_below;  // persistent: triangle steps need at least this many lanes
+    int32_t blocks_per_sm;   // persistent grid
+};
+
+TraceConfig default_trace_config(bool any_hit);
+bool valid_trace_config(const TraceConfig& c);
+
+// cfg == nullptr: default_trace_config(any_hit). counters != nullptr: the counting per-ray kernel.
 cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const float* dir_tmax,
                          const int32_t* last_prim, int64_t n_rays, float* hits, uint8_t* occluded, bool any_hit,
-                         unsigned long long* counters, cudaStream_t stream);
+                         unsigned long long* counters, cudaStream_t stream, const TraceConfig* cfg = nullptr);
 
 }  // namespace gbpt

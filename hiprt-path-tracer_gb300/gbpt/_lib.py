@@ -30,6 +30,11 @@ class BvhStats(ctypes.Structure):
                 ("device_bytes", i64), ("build_seconds", ctypes.c_double), ("upload_seconds", ctypes.c_double)]
 
 
+class TraceConfig(ctypes.Structure):
+    _fields_ = [("kernel", i32), ("block", i32), ("refill_below", i32), ("postpone_below", i32),
+                ("blocks_per_sm", i32), ("reserved", i32 * 3)]
+
+
 class GbptError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"gbpt status {status}: {message}")
@@ -49,6 +54,12 @@ SIGNATURES = [
     ("gbpt_trace_closest_host", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, c_vp, c_vp]),
     ("gbpt_trace_any_host", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, c_vp, c_vp]),
     ("gbpt_trace_count", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, i32, c_vp, c_vp]),
+    ("gbpt_bvh_set_trace_config", ctypes.c_int, [c_vp, i32, ctypes.POINTER(TraceConfig)]),
+    ("gbpt_bvh_get_trace_config", ctypes.c_int, [c_vp, i32, ctypes.POINTER(TraceConfig)]),
+    ("gbpt_trace_closest_cfg", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, c_vp, ctypes.POINTER(TraceConfig), c_vp]),
+    ("gbpt_trace_any_cfg", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, c_vp, ctypes.POINTER(TraceConfig), c_vp]),
+    ("gbpt_trace_autotune", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, i64, i32, i32, ctypes.POINTER(TraceConfig),
+                                           c_f, c_vp]),
 ]
 
 

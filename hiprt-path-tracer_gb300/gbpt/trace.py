@@ -94,6 +94,47 @@ class BVH:
                                             _ptr(out), _stream_handle(stream)))
         return out
 
+    # ---- launch configuration and autotuning -------------------------------------------------
+    def trace_config(self, any_hit: bool = False) -> dict:
+        c = _lib.TraceConfig()
+        _lib.check(self._lib.gbpt_bvh_get_trace_config(self.handle, 1 if any_hit else 0, ctypes.byref(c)))
+        return {f: getattr(c, f) for f, _ in c._fields_ if f != "reserved"}
+
+    def set_trace_config(self, any_hit: bool = False, **cfg) -> None:
+        c = _lib.TraceConfig(**{**self.trace_config(any_hit), **cfg})
+        _lib.check(self._lib.gbpt_bvh_set_trace_config(self.handle, 1 if any_hit else 0, ctypes.byref(c)))
+
+    def autotune(self, origin_tmin, dir_tmax, last_prim=None, any_hit: bool = False, store: bool = True, stream=None):
+        """Times candidate launch configurations on this device batch; returns (config, ms per launch)."""
+        c = _lib.TraceConfig()
+        ms = ctypes.c_float(0.0)
+        n = origin_tmin.shape[0]
+        _lib.check(self._lib.gbpt_trace_autotune(self.handle, _ptr(origin_tmin), _ptr(dir_tmax), _ptr(last_prim), n,
+                                                 1 if any_hit else 0, 1 if store else 0, ctypes.byref(c),
+                                                 ctypes.byref(ms), _stream_handle(stream)))
+        return {f: getattr(c, f) for f, _ in c._fields_ if f != "reserved"}, ms.value
+
+    def closest_cfg(self, origin_tmin, dir_tmax, last_prim=None, out=None, stream=None, **cfg):
+        """Closest hits with an explicit launch configuration (fields of gbpt_trace_config)."""
+        import torch
+        n = origin_tmin.shape[0]
+        if out is None:
+            out = torch.empty((n, 4), dtype=torch.float32, device=origin_tmin.device)
+        c = _lib.TraceConfig(**{**self.trace_config(False), **cfg})
+        _lib.check(self._lib.gbpt_trace_closest_cfg(self.handle, _ptr(origin_tmin), _ptr(dir_tmax), _ptr(last_prim), n,
+                                                    _ptr(out), ctypes.byref(c), _stream_handle(stream)))
+        return out
+
+    def occluded_cfg(self, origin_tmin, dir_tmax, last_prim=None, out=None, stream=None, **cfg):
+        import torch
+        n = origin_tmin.shape[0]
+        if out is None:
+            out = torch.empty((n,), dtype=torch.uint8, device=origin_tmin.device)
+        c = _lib.TraceConfig(**{**self.trace_config(True), **cfg})
+        _lib.check(self._lib.gbpt_trace_any_cfg(self.handle, _ptr(origin_tmin), _ptr(dir_tmax), _ptr(last_prim), n,
+                                                _ptr(out), ctypes.byref(c), _stream_handle(stream)))
+        return out
+
     def count(self, origin_tmin, dir_tmax, last_prim=None, any_hit: bool = False, stream=None):
         """(nodes visited, triangles tested) summed over the batch, from the counting kernels."""
         import torch

@@ -114,6 +114,44 @@ GBPT_API gbpt_status gbpt_trace_count(const gbpt_bvh* bvh, const float* origin_t
                                       const int32_t* last_prim, int64_t n_rays, int32_t any_hit,
                                       unsigned long long* counters, void* stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Launch configuration and autotuning of the traversal kernels. Every configuration returns the
+ * same results (the closest hit does not depend on the visiting order; any-hit returns the
+ * occlusion bit); only the speed differs, and it depends on the ray batch's coherence.
+ * ---------------------------------------------------------------------------------------- */
+enum {
+    GBPT_TRACE_KERNEL_PER_RAY = 1,    /* one thread per ray */
+    GBPT_TRACE_KERNEL_PERSISTENT = 2  /* persistent warps: lane refill + triangle postponing */
+};
+typedef struct gbpt_trace_config {
+    int32_t kernel;          /* GBPT_TRACE_KERNEL_* */
+    int32_t block;           /* threads per block: 32, 64, 128 or 256 */
+    int32_t refill_below;    /* persistent: refill a warp when fewer lanes than this trace (1..32) */
+    int32_t postpone_below;  /* persistent: triangle steps need this many lanes, else postponed (0..32) */
+    int32_t blocks_per_sm;   /* persistent: resident blocks per SM (1..64) */
+    int32_t reserved[3];
+} gbpt_trace_config;
+
+/* The configuration gbpt_trace_closest (any_hit = 0) / gbpt_trace_any (any_hit = 1) and their
+ * host variants use for this BVH (defaults: persistent closest-hit, per-ray any-hit). */
+GBPT_API gbpt_status gbpt_bvh_set_trace_config(gbpt_bvh* bvh, int32_t any_hit, const gbpt_trace_config* cfg);
+GBPT_API gbpt_status gbpt_bvh_get_trace_config(const gbpt_bvh* bvh, int32_t any_hit, gbpt_trace_config* cfg);
+/* Traversal with an explicit configuration (NULL: the BVH's). */
+GBPT_API gbpt_status gbpt_trace_closest_cfg(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                            const int32_t* last_prim, int64_t n_rays, float* hits,
+                                            const gbpt_trace_config* cfg, void* stream);
+GBPT_API gbpt_status gbpt_trace_any_cfg(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                        const int32_t* last_prim, int64_t n_rays, uint8_t* occluded,
+                                        const gbpt_trace_config* cfg, void* stream);
+/* Autotuner: times candidate configurations (kernel, block size, refill and postpone thresholds,
+ * resident blocks) on the given device ray batch with CUDA events, coordinate by coordinate from
+ * the current best, each candidate run twice and its faster run kept; writes the fastest to *best
+ * and its time per launch to *best_ms (either may be NULL). Results go to scratch memory. Stores
+ * the result as the BVH's configuration for the class when store != 0. Synchronous. */
+GBPT_API gbpt_status gbpt_trace_autotune(gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
+                                         const int32_t* last_prim, int64_t n_rays, int32_t any_hit, int32_t store,
+                                         gbpt_trace_config* best, float* best_ms, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -121,3 +121,35 @@ def test_full_size_scene_sampled(cuda, oracle):
     assert (got[hit, 0] > 0).all() and (prim < mesh.n_triangles).all()
     # determinism: a second launch returns identical bits
     assert np.array_equal(got.view(np.uint32), _closest(bvh, rays, cuda).view(np.uint32))
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_every_launch_configuration_gives_identical_results(cuda, any_hit):
+    """Per-ray and persistent kernels over block sizes and refill / postpone thresholds return the
+    same hits bit for bit (the closest hit does not depend on the visiting order), and the
+    autotuner returns a valid configuration whose results are again identical."""
+    mesh, closest, _, shadow, _, _ = load_golden("terrain")
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    rays = shadow if any_hit else closest
+    o, d, lp = _dev(rays, cuda)
+    run = bvh.occluded_cfg if any_hit else bvh.closest_cfg
+    base = run(o, d, lp, kernel=1, block=128).cpu().numpy()
+    configs = [dict(kernel=1, block=b) for b in (32, 64, 256)]
+    configs += [dict(kernel=2, block=b, refill_below=r, postpone_below=p, blocks_per_sm=s)
+                for b, r, p, s in [(128, 12, 8, 8), (64, 1, 0, 2), (256, 32, 32, 16), (128, 4, 24, 1), (32, 20, 4, 64)]]
+    for cfg in configs:
+        got = run(o, d, lp, **cfg).cpu().numpy()
+        assert np.array_equal(got.view(np.uint8), base.view(np.uint8)), cfg
+    best, ms = bvh.autotune(o, d, lp, any_hit=any_hit)
+    assert ms > 0 and best["kernel"] in (1, 2) and bvh.trace_config(any_hit) == best
+    got = (bvh.occluded if any_hit else bvh.closest)(o, d, lp).cpu().numpy()
+    assert np.array_equal(got.view(np.uint8), base.view(np.uint8))
+
+
+def test_trace_config_validation(cuda):
+    from gbpt import GbptError
+    mesh, *_ = load_golden("cornell")
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    for bad in (dict(kernel=3), dict(block=96), dict(refill_below=0), dict(postpone_below=33), dict(blocks_per_sm=0)):
+        with pytest.raises(GbptError):
+            bvh.set_trace_config(False, **bad)
