@@ -40,7 +40,7 @@ RAY_IN_BYTES = 36  # origin+tmin, direction+tmax, last_prim
 CLOSEST_OUT_BYTES = 16
 ANY_OUT_BYTES = 1
 NODE_BYTES = 80
-KERNEL_NAMES = {1: "trace_ray_kernel", 2: "trace_persistent"}
+KERNEL_NAMES = {1: "trace_ray_kernel", 2: "trace_persistent", 3: "trace_fetch"}
 TRI_BYTES = 36  # algorithmic: three float3 vertex records
 
 
@@ -418,6 +418,8 @@ def main():
     ap.add_argument("--ref-fraction", type=float, default=1.0 / 256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the path-tracing workloads")
+    ap.add_argument("--configs", default=None,
+                    help="JSON {primary, bounce, shadow} launch configurations to use instead of autotuning")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 2048x1024 primary + 1M bounce + 1M shadow rays, no e2e/CPU legs")
     args = ap.parse_args()
@@ -486,10 +488,15 @@ def main():
 
     # launch configurations picked by the autotuner per ray class (outside the timed region)
     t0 = time.time()
-    cfg_p, _ = bvh.autotune(*P, store=False)
-    cfg_b, _ = bvh.autotune(*B, store=False)
-    cfg_s, _ = bvh.autotune(*S, any_hit=True, store=False)
-    log(f"autotune {time.time() - t0:.1f}s: primary {cfg_p}, bounce {cfg_b}, shadow {cfg_s}")
+    if args.configs:
+        given = json.loads(args.configs)
+        cfg_p, cfg_b, cfg_s = given["primary"], given["bounce"], given["shadow"]
+    else:
+        cfg_p, _ = bvh.autotune(*P, store=False)
+        cfg_b, _ = bvh.autotune(*B, store=False)
+        cfg_s, _ = bvh.autotune(*S, any_hit=True, store=False)
+    log(f"launch configurations ({'given' if args.configs else f'autotuned in {time.time() - t0:.1f}s'}): "
+        f"primary {cfg_p}, bounce {cfg_b}, shadow {cfg_s}")
     bvh.set_trace_config(False, **cfg_b)
     bvh.set_trace_config(True, **cfg_s)
 

@@ -350,7 +350,7 @@ gbpt_status gbpt_trace_autotune(gbpt_bvh* bvh, const float* origin_tmin, const f
     gbpt::TraceConfig best = bvh->cfg[ah ? 1 : 0];
     float best_ms = 0.0f;
     e = timed(best, best_ms);
-    const int kernels[] = {gbpt::kTraceKernelPerRay, gbpt::kTraceKernelPersistent};
+    const int kernels[] = {gbpt::kTraceKernelPerRay, gbpt::kTraceKernelPersistent, gbpt::kTraceKernelFetch};
     const int blocks[] = {64, 128, 256};
     const int refills[] = {4, 8, 12, 16, 20, 24};
     const int postpones[] = {0, 4, 8, 12, 16, 24};
@@ -359,9 +359,10 @@ gbpt_status gbpt_trace_autotune(gbpt_bvh* bvh, const float* origin_tmin, const f
     {
         for (int coord = 0; coord < 5 && e == cudaSuccess; coord++)
         {
-            if (coord >= 2 && best.kernel != gbpt::kTraceKernelPersistent) break;
+            if (best.kernel == gbpt::kTraceKernelPerRay && coord >= 2) break;
+            if (best.kernel == gbpt::kTraceKernelFetch && (coord == 2 || coord == 3)) continue;
             const int* vals = coord == 0 ? kernels : coord == 1 ? blocks : coord == 2 ? refills : coord == 3 ? postpones : per_sm;
-            const int nv = coord == 0 ? 2 : coord == 1 ? 3 : coord == 4 ? 5 : 6;
+            const int nv = coord == 0 ? 3 : coord == 1 ? 3 : coord == 4 ? 5 : 6;
             for (int k = 0; k < nv && e == cudaSuccess; k++)
             {
                 gbpt::TraceConfig c = best;

@@ -187,6 +187,41 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
     }
 }
 
+// Per-lane fetch: the per-ray loop (a node, then all triangles of its hit leaves, then a pop), and
+// a lane whose ray finished takes the next ray of its warp's chunk at once (a shared-memory
+// counter per warp), so lanes do not wait for the warp's longest ray.
+template <bool ANY_HIT>
+__global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                   const float4* __restrict__ origin_tmin,
+                                                   const float4* __restrict__ dir_tmax,
+                                                   const int32_t* __restrict__ last_prim, int64_t n_rays,
+                                                   int64_t rays_per_warp, float4* __restrict__ hits,
+                                                   uint8_t* __restrict__ occluded)
+{
+    __shared__ unsigned int next_ray[8];  // per warp of the block (<= 256 threads)
+    const int wib = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) next_ray[wib] = 0u;
+    __syncwarp();
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t base = warp * rays_per_warp;
+    const int64_t end = base + rays_per_warp < n_rays ? base + rays_per_warp : n_rays;
+    if (base >= end) return;
+    for (;;)
+    {
+        const int64_t ray = base + (int64_t)atomicAdd(&next_ray[wib], 1u);
+        if (ray >= end) break;
+        uint32_t cn = 0, ct = 0;
+        const float4 h = core::trace_ray<ANY_HIT, false>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
+                                                         last_prim ? last_prim[ray] : -1, cn, ct);
+        if (ANY_HIT)
+        {
+            if (occluded) occluded[ray] = __float_as_int(h.w) >= 0 ? 1 : 0;
+        }
+        else if (hits)
+            hits[ray] = h;
+    }
+}
+
 // per-ray traversal, one thread per ray; COUNT adds node / triangle counters (statistics)
 template <bool ANY_HIT, bool COUNT>
 __global__ void __launch_bounds__(256) trace_ray_kernel(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
@@ -247,7 +282,8 @@ TraceConfig default_trace_config(bool any_hit)
 bool valid_trace_config(const TraceConfig& c)
 {
     const bool block_ok = c.block == 32 || c.block == 64 || c.block == 128 || c.block == 256;
-    return (c.kernel == kTraceKernelPerRay || c.kernel == kTraceKernelPersistent) && block_ok && c.refill_below >= 1 &&
+    return (c.kernel == kTraceKernelPerRay || c.kernel == kTraceKernelPersistent || c.kernel == kTraceKernelFetch) &&
+           block_ok && c.refill_below >= 1 &&
            c.refill_below <= 32 && c.postpone_below >= 0 && c.postpone_below <= 32 && c.blocks_per_sm >= 1 &&
            c.blocks_per_sm <= 64;
 }
@@ -284,8 +320,23 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
                                                                                    h, occluded, nullptr);
         return cudaGetLastError();
     }
-    // persistent grid: blocks_per_sm blocks per SM, each warp owning a contiguous chunk of rays
+    // persistent grids: blocks_per_sm blocks per SM, each warp owning a contiguous chunk of rays
     const int threads = cfg.block;
+    if (cfg.kernel == kTraceKernelFetch)
+    {
+        const int64_t max_blocks = (int64_t)sm_count() * cfg.blocks_per_sm;
+        const int64_t needed = (n_rays + threads - 1) / threads;
+        const int64_t blocks = needed < max_blocks ? needed : max_blocks;
+        const int64_t warps = blocks * (threads / 32);
+        const int64_t per_warp = (n_rays + warps - 1) / warps;
+        if (any_hit)
+            trace_fetch<true><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+                                                                        occluded);
+        else
+            trace_fetch<false><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+                                                                         occluded);
+        return cudaGetLastError();
+    }
     const int64_t max_blocks = (int64_t)sm_count() * cfg.blocks_per_sm;
     const int64_t needed = (n_rays + threads - 1) / threads;
     const int64_t blocks = needed < max_blocks ? needed : max_blocks;

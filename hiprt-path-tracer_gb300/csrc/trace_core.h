@@ -158,6 +158,19 @@ GBPT_HD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 
     if (idy < 0.0f) { uint32_t t0 = ny0, t1 = ny1; ny0 = fy0; ny1 = fy1; fy0 = t0; fy1 = t1; }
     if (idz < 0.0f) { uint32_t t0 = nz0, t1 = nz1; nz0 = fz0; nz1 = fz1; fz0 = t0; fz1 = t1; }
 
+    // child meta bytes decoded four at a time: a child is internal when bits 3 and 4 are both set;
+    // its hit-mask bit index is meta & 31, xor-ed with the ray octant for internal children; its
+    // bits are meta >> 5 (the internal flag, or the unary triangle count)
+    uint32_t bidx[2], cbits[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+    {
+        const uint32_t m = h == 0 ? w1.z : w1.w;
+        const uint32_t inner = (m & (m << 1) & 0x10101010u) >> 4;  // 1 per internal child's byte
+        bidx[h] = (m & 0x1F1F1F1Fu) ^ (inner * oct_inv);         // oct_inv <= 7: no carries
+        cbits[h] = (m >> 5) & 0x07070707u;
+    }
+
     uint32_t hitmask = 0;
 #pragma unroll
     for (int i = 0; i < 8; i++)
@@ -171,10 +184,8 @@ GBPT_HD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 
         const float tz1 = fmaf(plane_magic(i < 4 ? fz0 : fz1, k), Z.s8, Z.far_base);
         const float t_enter = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, tmin));
         const float t_exit = fminf(fminf(tx1, ty1), fminf(tz1, tmax));
-        const uint32_t meta = byte_of(i < 4 ? w1.z : w1.w, k);
-        const bool inner = (meta & 0x18u) == 0x18u;
-        const uint32_t bit_index = inner ? ((meta & 0x1Fu) ^ oct_inv) : (meta & 0x1Fu);
-        const uint32_t child_bits = meta >> 5;
+        const uint32_t bit_index = byte_of(bidx[i >> 2], k);
+        const uint32_t child_bits = byte_of(cbits[i >> 2], k);
         if (t_enter <= t_exit) hitmask |= child_bits << bit_index;
     }
     return hitmask;

@@ -18,6 +18,7 @@ struct DeviceBVH
 // Launch configuration of a traversal (the fields of gbpt_trace_config)
 constexpr int kTraceKernelPerRay = 1;      // one thread per ray
 constexpr int kTraceKernelPersistent = 2;  // persistent warps with lane refill and triangle postponing
+constexpr int kTraceKernelFetch = 3;       // persistent warps, each lane fetching its next ray when done
 struct TraceConfig
 {
     int32_t kernel;

@@ -121,14 +121,15 @@ GBPT_API gbpt_status gbpt_trace_count(const gbpt_bvh* bvh, const float* origin_t
  * ---------------------------------------------------------------------------------------- */
 enum {
     GBPT_TRACE_KERNEL_PER_RAY = 1,    /* one thread per ray */
-    GBPT_TRACE_KERNEL_PERSISTENT = 2  /* persistent warps: lane refill + triangle postponing */
+    GBPT_TRACE_KERNEL_PERSISTENT = 2, /* persistent warps: lane refill + triangle postponing */
+    GBPT_TRACE_KERNEL_FETCH = 3       /* persistent warps: each lane fetches its next ray when done */
 };
 typedef struct gbpt_trace_config {
     int32_t kernel;          /* GBPT_TRACE_KERNEL_* */
     int32_t block;           /* threads per block: 32, 64, 128 or 256 */
-    int32_t refill_below;    /* persistent: refill a warp when fewer lanes than this trace (1..32) */
-    int32_t postpone_below;  /* persistent: triangle steps need this many lanes, else postponed (0..32) */
-    int32_t blocks_per_sm;   /* persistent: resident blocks per SM (1..64) */
+    int32_t refill_below;    /* PERSISTENT: refill a warp when fewer lanes than this trace (1..32) */
+    int32_t postpone_below;  /* PERSISTENT: triangle steps need this many lanes, else postponed (0..32) */
+    int32_t blocks_per_sm;   /* PERSISTENT and FETCH: blocks per SM of the grid (1..64) */
     int32_t reserved[3];
 } gbpt_trace_config;
 

@@ -137,11 +137,12 @@ def test_every_launch_configuration_gives_identical_results(cuda, any_hit):
     configs = [dict(kernel=1, block=b) for b in (32, 64, 256)]
     configs += [dict(kernel=2, block=b, refill_below=r, postpone_below=p, blocks_per_sm=s)
                 for b, r, p, s in [(128, 12, 8, 8), (64, 1, 0, 2), (256, 32, 32, 16), (128, 4, 24, 1), (32, 20, 4, 64)]]
+    configs += [dict(kernel=3, block=b, blocks_per_sm=s) for b, s in [(128, 8), (256, 4), (32, 64), (64, 1)]]
     for cfg in configs:
         got = run(o, d, lp, **cfg).cpu().numpy()
         assert np.array_equal(got.view(np.uint8), base.view(np.uint8)), cfg
     best, ms = bvh.autotune(o, d, lp, any_hit=any_hit)
-    assert ms > 0 and best["kernel"] in (1, 2) and bvh.trace_config(any_hit) == best
+    assert ms > 0 and best["kernel"] in (1, 2, 3) and bvh.trace_config(any_hit) == best
     got = (bvh.occluded if any_hit else bvh.closest)(o, d, lp).cpu().numpy()
     assert np.array_equal(got.view(np.uint8), base.view(np.uint8))
 
@@ -150,6 +151,6 @@ def test_trace_config_validation(cuda):
     from gbpt import GbptError
     mesh, *_ = load_golden("cornell")
     bvh = gbpt.BVH(mesh.indices, mesh.positions)
-    for bad in (dict(kernel=3), dict(block=96), dict(refill_below=0), dict(postpone_below=33), dict(blocks_per_sm=0)):
+    for bad in (dict(kernel=4), dict(block=96), dict(refill_below=0), dict(postpone_below=33), dict(blocks_per_sm=0)):
         with pytest.raises(GbptError):
             bvh.set_trace_config(False, **bad)
