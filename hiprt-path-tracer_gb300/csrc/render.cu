@@ -24,6 +24,25 @@ namespace {
 // camera rays (CameraRays, src/Device/kernels/CameraRays.h:155-176; HIPRTCamera::get_camera_ray,
 // src/HostDeviceCommon/HIPRTCamera.h:31-52)
 // ---------------------------------------------------------------------------------------------
+// Camera ray of a pixel sample and its path's PCG stream (seeded by pixel and sample index)
+__device__ __forceinline__ void camera_ray(const RenderConst& rc, int pixel, int sample, V3& origin, V3& dir, Pcg32& rng)
+{
+    const int x = pixel % rc.width, y = pixel / rc.width;
+    rng = pcg_seed((uint32_t)pixel, (uint32_t)sample, rc.seed);
+    float px = x + 0.5f, py = y + 0.5f;
+    if (rc.do_jittering)
+    {
+        px += rng.next() - 0.5f;
+        py += rng.next() - 0.5f;
+    }
+    const float xn = px / rc.width * 2.0f - 1.0f;
+    const float yn = py / rc.height * 2.0f - 1.0f;
+    origin = mat_x_point(rc.inverse_view, v3(0.0f, 0.0f, 0.0f));
+    const V3 p_vs = mat_x_point(rc.inverse_projection, v3(xn, yn, -1.0f));
+    const V3 p_ws = mat_x_point(rc.inverse_view, p_vs);
+    dir = normalize(p_ws - origin);
+}
+
 __global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers pb, Queue q, int32_t iteration_base,
                                                      unsigned long long* stats)
 {
@@ -33,20 +52,9 @@ __global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers
     {
         const int pixel = (int)(slot % n_pix);
         const int s = (int)(slot / n_pix);
-        const int x = pixel % rc.width, y = pixel / rc.width;
-        Pcg32 rng = pcg_seed((uint32_t)pixel, (uint32_t)(iteration_base + s), rc.seed);
-        float px = x + 0.5f, py = y + 0.5f;
-        if (rc.do_jittering)
-        {
-            px += rng.next() - 0.5f;
-            py += rng.next() - 0.5f;
-        }
-        const float xn = px / rc.width * 2.0f - 1.0f;
-        const float yn = py / rc.height * 2.0f - 1.0f;
-        const V3 origin = mat_x_point(rc.inverse_view, v3(0.0f, 0.0f, 0.0f));
-        const V3 p_vs = mat_x_point(rc.inverse_projection, v3(xn, yn, -1.0f));
-        const V3 p_ws = mat_x_point(rc.inverse_view, p_vs);
-        const V3 dir = normalize(p_ws - origin);
+        V3 origin, dir;
+        Pcg32 rng;
+        camera_ray(rc, pixel, iteration_base + s, origin, dir, rng);
         q.origin_tmin[slot] = f4(origin, 0.0f);
         q.dir_tmax[slot] = f4(dir, INFINITY);
         q.last_prim[slot] = -1;
@@ -68,13 +76,23 @@ __global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers
 // ---------------------------------------------------------------------------------------------
 template <bool ANY_HIT>
 __global__ void __launch_bounds__(128) trace_queue_kernel(const uint4* __restrict__ nodes,
-                                                          const float4* __restrict__ tris, Queue q)
+                                                          const float4* __restrict__ tris, Queue q,
+                                                          const BatchJob* __restrict__ jobs,
+                                                          const int32_t* __restrict__ job_of_slot)
 {
     const int n = *q.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
+        const uint4* nd = nodes;
+        const float4* tr = tris;
+        if (jobs)
+        {
+            const BatchJob* J = jobs + job_of_slot[q.slot[i]];
+            nd = J->s.bvh_nodes;
+            tr = J->s.bvh_tris;
+        }
         uint32_t cn = 0, ct = 0;
-        const float4 h = core::trace_ray<ANY_HIT, false>(nodes, tris, q.origin_tmin[i], q.dir_tmax[i], q.last_prim[i], cn, ct);
+        const float4 h = core::trace_ray<ANY_HIT, false>(nd, tr, q.origin_tmin[i], q.dir_tmax[i], q.last_prim[i], cn, ct);
         if (ANY_HIT)
             q.occluded[i] = __float_as_int(h.w) >= 0 ? 1 : 0;
         else
@@ -88,9 +106,9 @@ __global__ void __launch_bounds__(128) trace_queue_kernel(const uint4* __restric
 // refracts out), else the Lambertian BSDF override.
 // ---------------------------------------------------------------------------------------------
 template <bool PRINCIPLED>
-__global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue next,
+__global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc0, PathBuffers pb, Queue in, Queue next,
                                                     Queue shadow, Queue bsdfq, int bounce, unsigned long long* stats,
-                                                    ReservoirBuf restir, GuideView gv)
+                                                    ReservoirBuf restir, GuideView gv, const BatchJob* __restrict__ jobs)
 {
     const int n = *in.count;
     // iterate in whole warps so that the warp-aggregated appends see converged lanes
@@ -114,6 +132,10 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
                 gv.train_light_entry[slot] = -1;
             }
         }
+        // batched rendering: the scene and settings of the slot's job
+        const BatchJob* J = (jobs && valid) ? jobs + pb.job[slot] : nullptr;
+        const SceneView s = J ? J->s : s0;
+        const RenderConst rc = J ? J->rc : rc0;
         const bool alive = valid && prim >= 0;
 
         bool want_shadow = false, want_bsdf = false, want_next = false, want_record = false;
@@ -564,13 +586,16 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, RenderConst rc,
 // ---------------------------------------------------------------------------------------------
 // resolve: add the light-sample and BSDF-sample contributions of this bounce, in a fixed order
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) resolve_kernel(SceneView s, RenderConst rc, PathBuffers pb, Queue in, Queue shadow,
-                                                      Queue bsdfq, GuideView gv)
+__global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst rc0, PathBuffers pb, Queue in, Queue shadow,
+                                                      Queue bsdfq, GuideView gv, const BatchJob* __restrict__ jobs)
 {
     const int n = *in.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const int slot = in.slot[i];
+        const BatchJob* J = jobs ? jobs + pb.job[slot] : nullptr;
+        const SceneView s = J ? J->s : s0;
+        const RenderConst rc = J ? J->rc : rc0;
         const int se = pb.shadow_entry[slot];
         const int be = pb.bsdf_entry[slot];
         // a guiding record of this vertex snapshots the radiance after its direct lighting; its
@@ -717,6 +742,114 @@ __global__ void __launch_bounds__(256) accumulate_kernel(RenderConst rc, PathBuf
         acc64[3 * p + 1] = G;
         acc64[3 * p + 2] = B;
     }
+}
+
+// ---------------------------------------------------------------------------------------------
+// batched rendering: all jobs' paths share every wavefront launch; blockIdx.y selects the job in
+// the per-job kernels. The iteration index lives in device memory so that a captured CUDA graph
+// of one iteration replays unchanged.
+// ---------------------------------------------------------------------------------------------
+// samples per pixel job J renders in iteration it (0 once the job is done)
+__device__ __forceinline__ int batch_samples(const BatchJob& J, int it)
+{
+    if (it >= J.iterations) return 0;
+    const int left = J.spp_total - it * J.rc.spp;
+    return left < J.rc.spp ? left : J.rc.spp;
+}
+
+__global__ void __launch_bounds__(256) camera_batch_kernel(const BatchJob* __restrict__ jobs, PathBuffers pb, Queue q,
+                                                           const int32_t* __restrict__ iteration,
+                                                           unsigned long long* stats)
+{
+    const int job = blockIdx.y;
+    const BatchJob& J = jobs[job];
+    const RenderConst rc = J.rc;
+    const int it = *iteration;
+    const int64_t n_pix = (int64_t)rc.width * rc.height;
+    const int64_t n = n_pix * batch_samples(J, it);
+    const int64_t n_round = (n + 31) & ~(int64_t)31;  // whole warps for the aggregated appends
+    for (int64_t local = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; local < n_round;
+         local += (int64_t)gridDim.x * blockDim.x)
+    {
+        const bool valid = local < n;
+        V3 origin = v3(0.0f), dir = v3(0.0f);
+        Pcg32 rng;
+        rng.state = 0;
+        rng.inc = 0;
+        if (valid) camera_ray(rc, (int)(local % n_pix), it * rc.spp + (int)(local / n_pix), origin, dir, rng);
+        const int qi = warp_append(q.count, valid);
+        if (valid)
+        {
+            const int64_t slot = J.slot_base + local;
+            q.origin_tmin[qi] = f4(origin, 0.0f);
+            q.dir_tmax[qi] = f4(dir, INFINITY);
+            q.last_prim[qi] = -1;
+            q.slot[qi] = (int32_t)slot;
+            pb.throughput[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            pb.radiance[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (pb.medium) pb.medium[slot] = -1;
+            pb.job[slot] = job;
+            store_rng(pb.rng + slot, rng);
+        }
+        warp_count(stats + 0, valid);
+    }
+}
+
+// per job: its pixels' samples of this iteration, in sample order, into its accumulators
+__global__ void __launch_bounds__(256) accumulate_batch_kernel(const BatchJob* __restrict__ jobs, PathBuffers pb,
+                                                               const int32_t* __restrict__ iteration,
+                                                               float* __restrict__ acc32, double* __restrict__ acc64)
+{
+    const BatchJob& J = jobs[blockIdx.y];
+    const int samples = batch_samples(J, *iteration);
+    const int64_t n_pix = (int64_t)J.rc.width * J.rc.height;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_pix && samples > 0;
+         p += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t a = 3 * (J.pixel_base + p);
+        float r = acc32[a], g = acc32[a + 1], b = acc32[a + 2];
+        double R = acc64[a], G = acc64[a + 1], B = acc64[a + 2];
+        for (int k = 0; k < samples; k++)
+        {
+            const float4 v = pb.radiance[J.slot_base + (int64_t)k * n_pix + p];
+            r += v.x;
+            g += v.y;
+            b += v.z;
+            R += v.x;
+            G += v.y;
+            B += v.z;
+        }
+        acc32[a] = r;
+        acc32[a + 1] = g;
+        acc32[a + 2] = b;
+        acc64[a] = R;
+        acc64[a + 1] = G;
+        acc64[a + 2] = B;
+    }
+}
+
+// end of an iteration: stamps the global timer for the jobs that just finished, then advances
+// the iteration index (one block)
+__global__ void batch_step_kernel(const BatchJob* __restrict__ jobs, int n_jobs, int32_t* iteration,
+                                  unsigned long long* done_ns)
+{
+    const int it = *iteration;
+    for (int j = threadIdx.x; j < n_jobs; j += blockDim.x)
+        if (it + 1 == jobs[j].iterations)
+        {
+            unsigned long long t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            done_ns[j] = t;
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) *iteration = it + 1;
+}
+
+__global__ void stamp_kernel(unsigned long long* out)
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *out = t;
 }
 
 __global__ void reset_counts_kernel(int32_t* a, int32_t* b, int32_t* c)
@@ -873,27 +1006,28 @@ cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Qu
 }
 
 cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next, const Queue& shadow,
-                          const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st)
+                          const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st, const BatchJob* jobs,
+                          const int32_t* job_of_slot)
 {
     const int tgrid = grid_for(capacity, 128, n_sm * 16);
     reset_counts_kernel<<<1, 1, 0, st>>>(next.count, shadow.count, bsdfq.count);
-    trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, in);
+    trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, in, jobs, job_of_slot);
     return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
                          const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
                          unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv, int n_sm,
-                         cudaStream_t st)
+                         cudaStream_t st, const BatchJob* jobs)
 {
     const int tgrid = grid_for(capacity, 128, n_sm * 16);
     if (rc.bsdf == GBPT_BSDF_PRINCIPLED)
-        shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv);
+        shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv, jobs);
     else
-        shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv);
-    trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, shadow);
-    trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, bsdfq);
-    resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq, gv);
+        shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv, jobs);
+    trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, shadow, jobs, pb.job);
+    trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, bsdfq, jobs, pb.job);
+    resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq, gv, jobs);
     return cudaGetLastError();
 }
 
@@ -915,6 +1049,32 @@ cudaError_t launch_accumulate(const RenderConst& rc, const PathBuffers& pb, floa
                               cudaStream_t st)
 {
     accumulate_kernel<<<grid_for((int64_t)rc.width * rc.height, 256, n_sm * 8), 256, 0, st>>>(rc, pb, acc32, acc64);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_camera(const BatchJob* jobs, int n_jobs, int64_t max_job_paths, const PathBuffers& pb,
+                                const Queue& q, const int32_t* iteration, unsigned long long* stats, int n_sm,
+                                cudaStream_t st)
+{
+    reset_counts_kernel<<<1, 1, 0, st>>>(q.count, nullptr, nullptr);
+    const int gx = grid_for(max_job_paths, 256, (n_sm * 8 + n_jobs - 1) / n_jobs + 1);
+    camera_batch_kernel<<<dim3(gx, n_jobs), 256, 0, st>>>(jobs, pb, q, iteration, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_accumulate(const BatchJob* jobs, int n_jobs, int64_t max_job_pixels, const PathBuffers& pb,
+                                    const int32_t* iteration, float* acc32, double* acc64, int32_t* iteration_rw,
+                                    unsigned long long* done_ns, int n_sm, cudaStream_t st)
+{
+    const int gx = grid_for(max_job_pixels, 256, (n_sm * 8 + n_jobs - 1) / n_jobs + 1);
+    accumulate_batch_kernel<<<dim3(gx, n_jobs), 256, 0, st>>>(jobs, pb, iteration, acc32, acc64);
+    batch_step_kernel<<<1, 256, 0, st>>>(jobs, n_jobs, iteration_rw, done_ns);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stamp(unsigned long long* out, cudaStream_t st)
+{
+    stamp_kernel<<<1, 1, 0, st>>>(out);
     return cudaGetLastError();
 }
 

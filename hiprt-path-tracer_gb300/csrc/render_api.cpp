@@ -371,10 +371,10 @@ gbpt_status gbpt_scene_get_light_table(const gbpt_scene* s, int32_t* n_emissive,
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "light table read-back");
 }
 
-gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_settings* st, gbpt_renderer** out)
+namespace {
+
+gbpt_status check_settings(const gbpt_scene* scene, const gbpt_render_settings* st)
 {
-    if (!out) return set_error(GBPT_ERROR_INVALID_ARG, "out is NULL");
-    *out = nullptr;
     if (!scene || !st) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
     if (st->width <= 0 || st->height <= 0 || st->samples_per_launch <= 0)
         return set_error(GBPT_ERROR_INVALID_ARG, "width, height and samples_per_launch must be positive");
@@ -385,19 +385,16 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
         return set_error(GBPT_ERROR_UNSUPPORTED, "bsdf must be GBPT_BSDF_LAMBERTIAN or GBPT_BSDF_PRINCIPLED");
     if (st->bsdf == GBPT_BSDF_PRINCIPLED && !scene->principled)
         return set_error(GBPT_ERROR_INVALID_ARG, "GBPT_BSDF_PRINCIPLED needs a scene created with principled_materials");
-    const int64_t cap = (int64_t)st->width * st->height * st->samples_per_launch;
-    if (cap > (int64_t)1 << 30) return set_error(GBPT_ERROR_INVALID_ARG, "width*height*samples_per_launch exceeds 2^30 paths");
+    return GBPT_OK;
+}
 
-    gbpt_renderer* r = new (std::nothrow) gbpt_renderer();
-    if (!r) return set_error(GBPT_ERROR_OOM, "host allocation failed");
-    r->scene = scene;
-    r->capacity = cap;
-    r->n_sm = sm_count();
-    gbpt::RenderConst& rc = r->rc;
+gbpt::RenderConst render_const(const gbpt_render_settings* st, int32_t spp)
+{
+    gbpt::RenderConst rc;
     std::memset(&rc, 0, sizeof(rc));
     rc.width = st->width;
     rc.height = st->height;
-    rc.spp = st->samples_per_launch;
+    rc.spp = spp;
     rc.nb_bounces = st->nb_bounces;
     rc.do_rr = st->do_russian_roulette;
     rc.rr_min_depth = st->russian_roulette_min_depth;
@@ -409,20 +406,49 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
     rc.ggx_height_correlated = st->ggx_height_correlated;
     std::memcpy(rc.inverse_view, st->inverse_view, sizeof(rc.inverse_view));
     std::memcpy(rc.inverse_projection, st->inverse_projection, sizeof(rc.inverse_projection));
+    return rc;
+}
+
+// Path state and the four queues of a wavefront of 'cap' paths
+void alloc_paths(DevMem& M, int64_t cap, bool principled, bool batched, gbpt::PathBuffers& pb, gbpt::Queue* q,
+                 gbpt::Queue& shadow, gbpt::Queue& bsdfq)
+{
+    std::memset(&pb, 0, sizeof(pb));
+    pb.throughput = M.alloc<float4>(cap);
+    pb.radiance = M.alloc<float4>(cap);
+    pb.rng = M.alloc<uint64_t>(cap);
+    pb.pending_light = M.alloc<float4>(cap);
+    pb.pending_bsdf = M.alloc<float4>(cap);
+    pb.shadow_entry = M.alloc<int32_t>(cap);
+    pb.bsdf_entry = M.alloc<int32_t>(cap);
+    pb.medium = principled ? M.alloc<int32_t>(cap) : nullptr;
+    pb.job = batched ? M.alloc<int32_t>(cap) : nullptr;
+    q[0] = make_queue(M, cap, true, false);
+    q[1] = make_queue(M, cap, true, false);
+    shadow = make_queue(M, cap, false, true);
+    bsdfq = make_queue(M, cap, true, false);
+}
+
+}  // namespace
+
+gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_settings* st, gbpt_renderer** out)
+{
+    if (!out) return set_error(GBPT_ERROR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    gbpt_status chk = check_settings(scene, st);
+    if (chk != GBPT_OK) return chk;
+    const int64_t cap = (int64_t)st->width * st->height * st->samples_per_launch;
+    if (cap > (int64_t)1 << 30) return set_error(GBPT_ERROR_INVALID_ARG, "width*height*samples_per_launch exceeds 2^30 paths");
+
+    gbpt_renderer* r = new (std::nothrow) gbpt_renderer();
+    if (!r) return set_error(GBPT_ERROR_OOM, "host allocation failed");
+    r->scene = scene;
+    r->capacity = cap;
+    r->n_sm = sm_count();
+    r->rc = render_const(st, st->samples_per_launch);
 
     DevMem& M = r->mem;
-    r->pb.throughput = M.alloc<float4>(cap);
-    r->pb.radiance = M.alloc<float4>(cap);
-    r->pb.rng = M.alloc<uint64_t>(cap);
-    r->pb.pending_light = M.alloc<float4>(cap);
-    r->pb.pending_bsdf = M.alloc<float4>(cap);
-    r->pb.shadow_entry = M.alloc<int32_t>(cap);
-    r->pb.bsdf_entry = M.alloc<int32_t>(cap);
-    r->pb.medium = st->bsdf == GBPT_BSDF_PRINCIPLED ? M.alloc<int32_t>(cap) : nullptr;
-    r->q[0] = make_queue(M, cap, true, false);
-    r->q[1] = make_queue(M, cap, true, false);
-    r->shadow = make_queue(M, cap, false, true);
-    r->bsdfq = make_queue(M, cap, true, false);
+    alloc_paths(M, cap, st->bsdf == GBPT_BSDF_PRINCIPLED, false, r->pb, r->q, r->shadow, r->bsdfq);
     const int64_t npix = (int64_t)st->width * st->height;
     r->acc32 = M.alloc<float>(3 * npix);
     r->acc64 = M.alloc<double>(3 * npix);
@@ -971,6 +997,216 @@ gbpt_status gbpt_renderer_get_guide_records(gbpt_renderer* r, float* host_out, i
         o[13] = pb[i];
         std::memcpy(o + 14, &sl[i], sizeof(int32_t));
     }
+    return GBPT_OK;
+}
+
+struct gbpt_batch
+{
+    std::vector<gbpt::BatchJob> host_jobs;
+    std::vector<const gbpt_scene*> scenes;
+    gbpt_batch_params params;
+    DevMem mem;
+    gbpt::BatchJob* jobs = nullptr;
+    gbpt::PathBuffers pb;
+    gbpt::Queue q[2], shadow, bsdfq;
+    int64_t capacity = 0, max_job_paths = 0, max_job_pixels = 0, total_pixels = 0;
+    int max_bounces = 0, max_iterations = 0, n_sm = 1;
+    float* acc32 = nullptr;
+    double* acc64 = nullptr;
+    int32_t* iteration = nullptr;
+    unsigned long long* stamps = nullptr;  // [0] render start, [1 + j] job j done (global timer, ns)
+    unsigned long long* stats = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// One iteration of the batch: camera rays, the bounce loop over all jobs, accumulation + step
+cudaError_t batch_iteration(gbpt_batch* b, cudaStream_t st)
+{
+    const gbpt::BatchJob& j0 = b->host_jobs[0];
+    cudaError_t e = gbpt::launch_batch_camera(b->jobs, (int)b->host_jobs.size(), b->max_job_paths, b->pb, b->q[0],
+                                              b->iteration, b->stats, b->n_sm, st);
+    gbpt::ReservoirBuf none = {nullptr, nullptr};
+    gbpt::GuideView no_guide;
+    std::memset(&no_guide, 0, sizeof(no_guide));
+    for (int bounce = 0; e == cudaSuccess && bounce <= b->max_bounces; bounce++)
+    {
+        const gbpt::Queue& in = b->q[bounce & 1];
+        const gbpt::Queue& next = b->q[(bounce & 1) ^ 1];
+        e = gbpt::launch_extend(j0.s, in, next, b->shadow, b->bsdfq, b->capacity, b->n_sm, st, b->jobs, b->pb.job);
+        if (e == cudaSuccess)
+            e = gbpt::launch_shade(j0.s, j0.rc, b->pb, in, next, b->shadow, b->bsdfq, bounce, b->capacity, b->stats + 1,
+                                   none, no_guide, b->n_sm, st, b->jobs);
+    }
+    if (e == cudaSuccess)
+        e = gbpt::launch_batch_accumulate(b->jobs, (int)b->host_jobs.size(), b->max_job_pixels, b->pb, b->iteration,
+                                          b->acc32, b->acc64, b->iteration, b->stamps + 1, b->n_sm, st);
+    return e;
+}
+
+void batch_release(gbpt_batch* b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    b->mem.release();
+}
+
+}  // namespace
+
+gbpt_status gbpt_batch_default_params(gbpt_batch_params* p)
+{
+    if (!p) return set_error(GBPT_ERROR_INVALID_ARG, "params is NULL");
+    std::memset(p, 0, sizeof(*p));
+    p->samples_per_iteration = 4;
+    p->use_graph = 1;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_batch_create(const gbpt_batch_job* jobs, int32_t n_jobs, const gbpt_batch_params* p, gbpt_batch** out)
+{
+    if (!out) return set_error(GBPT_ERROR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (!jobs || !p || n_jobs < 1) return set_error(GBPT_ERROR_INVALID_ARG, "need at least one job and params");
+    if (p->samples_per_iteration < 1 || p->samples_per_iteration > 1024)
+        return set_error(GBPT_ERROR_INVALID_ARG, "samples_per_iteration must be in 1..1024");
+    gbpt_batch* b = new (std::nothrow) gbpt_batch();
+    if (!b) return set_error(GBPT_ERROR_OOM, "host allocation failed");
+    b->params = *p;
+    b->n_sm = sm_count();
+    const int k = p->samples_per_iteration;
+    for (int j = 0; j < n_jobs; j++)
+    {
+        const gbpt_render_settings* st = &jobs[j].settings;
+        gbpt_status chk = check_settings(jobs[j].scene, st);
+        if (chk == GBPT_OK && st->bsdf != jobs[0].settings.bsdf)
+            chk = set_error(GBPT_ERROR_INVALID_ARG, "all jobs of a batch must use the same bsdf mode");
+        if (chk != GBPT_OK)
+        {
+            delete b;
+            return chk;
+        }
+        gbpt::BatchJob J;
+        std::memset(&J, 0, sizeof(J));
+        J.s = jobs[j].scene->view;
+        J.rc = render_const(st, k);
+        J.slot_base = b->capacity;
+        J.pixel_base = b->total_pixels;
+        J.spp_total = st->samples_per_launch;
+        J.iterations = (st->samples_per_launch + k - 1) / k;
+        const int64_t npix = (int64_t)st->width * st->height;
+        b->capacity += npix * k;
+        b->total_pixels += npix;
+        b->max_job_paths = std::max(b->max_job_paths, npix * k);
+        b->max_job_pixels = std::max(b->max_job_pixels, npix);
+        b->max_bounces = std::max(b->max_bounces, st->nb_bounces);
+        b->max_iterations = std::max(b->max_iterations, J.iterations);
+        b->host_jobs.push_back(J);
+        b->scenes.push_back(jobs[j].scene);
+    }
+    if (b->capacity > (int64_t)1 << 30)
+    {
+        delete b;
+        return set_error(GBPT_ERROR_INVALID_ARG, "the jobs' paths per iteration exceed 2^30");
+    }
+    DevMem& M = b->mem;
+    alloc_paths(M, b->capacity, jobs[0].settings.bsdf == GBPT_BSDF_PRINCIPLED, true, b->pb, b->q, b->shadow, b->bsdfq);
+    b->jobs = M.alloc<gbpt::BatchJob>(n_jobs);
+    b->acc32 = M.alloc<float>(3 * b->total_pixels);
+    b->acc64 = M.alloc<double>(3 * b->total_pixels);
+    b->iteration = M.alloc<int32_t>(1);
+    b->stamps = M.alloc<unsigned long long>(1 + n_jobs);
+    b->stats = M.alloc<unsigned long long>(4);
+    cudaError_t e = M.err;
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->jobs, b->host_jobs.data(), sizeof(gbpt::BatchJob) * n_jobs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && p->use_graph)
+    {
+        // capture one iteration; the graph reads the iteration index from device memory
+        e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess)
+        {
+            cudaError_t ei = batch_iteration(b, b->capture_stream);
+            e = cudaStreamEndCapture(b->capture_stream, &b->graph);
+            if (e == cudaSuccess) e = ei;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    }
+    if (e != cudaSuccess)
+    {
+        batch_release(b);
+        delete b;
+        return e == cudaErrorMemoryAllocation ? set_error(GBPT_ERROR_OOM, "batch buffers") : cuda_error(e, "batch create");
+    }
+    *out = b;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_batch_destroy(gbpt_batch* b)
+{
+    if (!b) return GBPT_OK;
+    batch_release(b);
+    delete b;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_batch_render(gbpt_batch* b, void* stream)
+{
+    if (!b) return set_error(GBPT_ERROR_INVALID_ARG, "batch is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(b->acc32, 0, 3 * b->total_pixels * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->acc64, 0, 3 * b->total_pixels * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->iteration, 0, sizeof(int32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->stats, 0, 4 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = gbpt::launch_stamp(b->stamps, st);
+    for (int it = 0; e == cudaSuccess && it < b->max_iterations; it++)
+        e = b->exec ? cudaGraphLaunch(b->exec, st) : batch_iteration(b, st);
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "batch render");
+}
+
+gbpt_status gbpt_batch_job_seconds(gbpt_batch* b, double* seconds)
+{
+    if (!b || !seconds) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    std::vector<unsigned long long> t(1 + b->host_jobs.size());
+    cudaError_t e = cudaMemcpy(t.data(), b->stamps, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "stamp read-back");
+    for (size_t j = 0; j < b->host_jobs.size(); j++) seconds[j] = (double)(t[1 + j] - t[0]) * 1e-9;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_batch_get_image(gbpt_batch* b, int32_t job, float* rgb32, double* rgb64, void* stream)
+{
+    if (!b) return set_error(GBPT_ERROR_INVALID_ARG, "batch is NULL");
+    if (job < 0 || job >= (int32_t)b->host_jobs.size()) return set_error(GBPT_ERROR_INVALID_ARG, "job out of range");
+    const gbpt::BatchJob& J = b->host_jobs[job];
+    const int64_t npix = (int64_t)J.rc.width * J.rc.height;
+    cudaStream_t cs = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (rgb32) e = cudaMemcpyAsync(rgb32, b->acc32 + 3 * J.pixel_base, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess && rgb64)
+        e = cudaMemcpyAsync(rgb64, b->acc64 + 3 * J.pixel_base, 3 * npix * sizeof(double), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "batch image read-back");
+}
+
+gbpt_status gbpt_batch_get_stats(gbpt_batch* b, gbpt_render_stats* out, void* stream)
+{
+    if (!b || !out) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    unsigned long long h[4];
+    cudaStream_t cs = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(h, b->stats, sizeof(h), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) return cuda_error(e, "stats read-back");
+    int64_t samples = 0;
+    for (const gbpt::BatchJob& J : b->host_jobs) samples += (int64_t)J.rc.width * J.rc.height * J.spp_total;
+    out->samples = samples;
+    out->extension_rays = (int64_t)(h[0] + h[1]);
+    out->shadow_rays = (int64_t)h[2];
+    out->bsdf_light_rays = (int64_t)h[3];
     return GBPT_OK;
 }
 

@@ -66,6 +66,7 @@ struct PathBuffers
     int32_t* shadow_entry;  // queue index of the slot's shadow ray this bounce, -1 if none
     int32_t* bsdf_entry;    // queue index of the slot's BSDF-light ray this bounce, -1 if none
     int32_t* medium;        // material index of the volume the path travels in, -1 = air
+    int32_t* job;           // batched rendering: the job of each slot (null for a single renderer)
 };
 
 // Learned path guiding in the wavefront (all device pointers; lobes == nullptr: guiding off).

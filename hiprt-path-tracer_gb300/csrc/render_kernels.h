@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "render_common.h"
 #include "restir.h"
 
 namespace gbpt {
@@ -30,6 +31,18 @@ struct RenderConst
     float inverse_projection[16];
 };
 
+// One job of a batched render (device table): its scene and settings (rc.spp = samples per
+// iteration), its first path slot and first accumulator pixel, and its total samples per pixel.
+struct BatchJob
+{
+    SceneView s;
+    RenderConst rc;
+    int64_t slot_base;
+    int64_t pixel_base;
+    int32_t spp_total;
+    int32_t iterations;  // ceil(spp_total / rc.spp)
+};
+
 cudaError_t launch_light_table(const SceneView& s, float* power, double* partial, int n_partial, double* sum64,
                                double* q, float* prob, int32_t* alias, int32_t* smalls, int32_t* larges,
                                cudaStream_t st);
@@ -42,14 +55,16 @@ cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Qu
 // One bounce = extend (closest hit of the active queue) then shade (shade + shadow and BSDF-light
 // traversal + resolve). 'restir' (null buffers when ReSTIR DI is off) holds the final reservoirs
 // that replace next-event estimation at bounce 0.
+// jobs / job_of_slot (batched rendering, else null): each ray traverses its slot's job's BVH.
 cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next, const Queue& shadow,
-                          const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st);
+                          const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st,
+                          const BatchJob* jobs = nullptr, const int32_t* job_of_slot = nullptr);
 // 'gv' (null lobes when guiding is off) holds the learned mixture per entry of 'in' and the
 // training-record buffers.
 cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
                          const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
                          unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv, int n_sm,
-                         cudaStream_t st);
+                         cudaStream_t st, const BatchJob* jobs = nullptr);
 // Guiding network inputs for each entry of 'in' (after its closest hits are known)
 cudaError_t launch_guide_inputs(const SceneView& s, const Queue& in, const GuideView& gv, int64_t capacity, int n_sm,
                                 cudaStream_t st);
@@ -67,5 +82,16 @@ cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, con
                                   int n_sm, cudaStream_t st);
 cudaError_t launch_accumulate(const RenderConst& rc, const PathBuffers& pb, float* acc32, double* acc64, int n_sm,
                               cudaStream_t st);
+// Batched rendering (jobs: device table of n_jobs; iteration: device index of the iteration):
+// camera rays of every job's samples of this iteration appended to q; per-job accumulation, then
+// the completion stamps (global timer, ns) of the jobs that finish and the iteration advance.
+cudaError_t launch_batch_camera(const BatchJob* jobs, int n_jobs, int64_t max_job_paths, const PathBuffers& pb,
+                                const Queue& q, const int32_t* iteration, unsigned long long* stats, int n_sm,
+                                cudaStream_t st);
+cudaError_t launch_batch_accumulate(const BatchJob* jobs, int n_jobs, int64_t max_job_pixels, const PathBuffers& pb,
+                                    const int32_t* iteration, float* acc32, double* acc64, int32_t* iteration_rw,
+                                    unsigned long long* done_ns, int n_sm, cudaStream_t st);
+// Writes the global timer (ns) to *out
+cudaError_t launch_stamp(unsigned long long* out, cudaStream_t st);
 
 }  // namespace gbpt

@@ -87,7 +87,22 @@ RENDER_SIGNATURES = [
     ("gbpt_guide_render_default_settings", ctypes.c_int, [c_vp]),
     ("gbpt_renderer_set_guide", ctypes.c_int, [c_vp, c_vp, c_vp]),
     ("gbpt_renderer_get_guide_records", ctypes.c_int, [c_vp, c_vp, i32, c_vp, c_vp]),
+    ("gbpt_batch_default_params", ctypes.c_int, [c_vp]),
+    ("gbpt_batch_create", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
+    ("gbpt_batch_destroy", ctypes.c_int, [c_vp]),
+    ("gbpt_batch_render", ctypes.c_int, [c_vp, c_vp]),
+    ("gbpt_batch_job_seconds", ctypes.c_int, [c_vp, c_vp]),
+    ("gbpt_batch_get_image", ctypes.c_int, [c_vp, i32, c_vp, c_vp, c_vp]),
+    ("gbpt_batch_get_stats", ctypes.c_int, [c_vp, c_vp, c_vp]),
 ]
+
+
+class BatchJobC(ctypes.Structure):
+    _fields_ = [("scene", c_vp), ("settings", RenderSettingsC)]
+
+
+class BatchParamsC(ctypes.Structure):
+    _fields_ = [("samples_per_iteration", i32), ("use_graph", i32), ("reserved", i32 * 6)]
 
 
 class GuideRenderSettingsC(ctypes.Structure):
@@ -361,3 +376,57 @@ def cornell_settings(width=256, height=256, **kw) -> RenderSettings:
     for k, v in kw.items():
         setattr(s, k, v)
     return s
+
+
+class Batch:
+    """Many independent render jobs in one wavefront (gbpt_batch_*): jobs is a list of
+    (Scene, RenderSettings) whose samples_per_launch is each job's total samples per pixel."""
+
+    def __init__(self, jobs, samples_per_iteration: int = 4, use_graph: bool = True):
+        lib = _load()
+        self._lib = lib
+        self._scenes = [sc for sc, _ in jobs]  # keep the scenes alive
+        self.settings = [st for _, st in jobs]
+        arr = (BatchJobC * len(jobs))()
+        for k, (sc, st) in enumerate(jobs):
+            arr[k].scene = sc.handle
+            arr[k].settings = st.to_c()
+        p = BatchParamsC()
+        _lib.check(lib.gbpt_batch_default_params(ctypes.byref(p)))
+        p.samples_per_iteration = samples_per_iteration
+        p.use_graph = 1 if use_graph else 0
+        h = c_vp()
+        _lib.check(lib.gbpt_batch_create(arr, len(jobs), ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+
+    def render(self, stream=None):
+        _lib.check(self._lib.gbpt_batch_render(self._h, _stream(stream)))
+
+    def job_seconds(self) -> np.ndarray:
+        out = np.zeros(len(self.settings), np.float64)
+        _lib.check(self._lib.gbpt_batch_job_seconds(self._h, out.ctypes.data))
+        return out
+
+    def image_sums(self, job: int, stream=None):
+        st = self.settings[job]
+        a32 = np.zeros((st.height, st.width, 3), np.float32)
+        a64 = np.zeros((st.height, st.width, 3), np.float64)
+        _lib.check(self._lib.gbpt_batch_get_image(self._h, job, a32.ctypes.data, a64.ctypes.data, _stream(stream)))
+        return a32, a64
+
+    def stats(self, stream=None) -> dict:
+        s = RenderStatsC()
+        _lib.check(self._lib.gbpt_batch_get_stats(self._h, ctypes.byref(s), _stream(stream)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def destroy(self):
+        if getattr(self, "_h", None):
+            _lib.check(self._lib.gbpt_batch_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+

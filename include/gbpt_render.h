@@ -240,6 +240,44 @@ GBPT_API gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, co
 GBPT_API gbpt_status gbpt_renderer_get_guide_records(gbpt_renderer* r, float* host_out, int32_t capacity, int32_t* count,
                                                      void* stream);
 
+/* ---- batched rendering: many independent jobs in one wavefront ----
+ * Every job has its own scene (BVH, materials, lights) and settings (resolution, camera, bounces,
+ * seed, ...; settings.samples_per_launch is the job's TOTAL samples per pixel). All jobs' paths
+ * share every wavefront launch: one camera launch, then per bounce one extension, shading,
+ * shadow, BSDF-light and resolve launch over the union of the jobs' queues, one accumulation
+ * launch; a ray traverses its own job's BVH. An iteration renders samples_per_iteration samples
+ * of every pixel of every unfinished job; jobs finish after ceil(spp / samples_per_iteration)
+ * iterations. With use_graph one iteration is captured as a CUDA graph and replayed (the
+ * iteration index lives in device memory). A job's image equals, bit for bit, the image of a
+ * gbpt_renderer with samples_per_launch = samples_per_iteration run for the same samples (the
+ * last launch truncated to the job's spp), because each path keeps its pixel and sample index
+ * and its PCG stream. All jobs must use the same bsdf mode; ReSTIR DI and guiding are per
+ * renderer and not available in a batch. */
+typedef struct gbpt_batch gbpt_batch;
+typedef struct gbpt_batch_job {
+    const gbpt_scene* scene;
+    gbpt_render_settings settings;
+} gbpt_batch_job;
+typedef struct gbpt_batch_params {
+    int32_t samples_per_iteration; /* [4] */
+    int32_t use_graph;             /* [1] */
+    int32_t reserved[6];
+} gbpt_batch_params;
+
+GBPT_API gbpt_status gbpt_batch_default_params(gbpt_batch_params* p);
+GBPT_API gbpt_status gbpt_batch_create(const gbpt_batch_job* jobs, int32_t n_jobs, const gbpt_batch_params* p,
+                                       gbpt_batch** out);
+GBPT_API gbpt_status gbpt_batch_destroy(gbpt_batch* b);
+/* Renders every job from zero to completion; asynchronous on 'stream'. */
+GBPT_API gbpt_status gbpt_batch_render(gbpt_batch* b, void* stream);
+/* Per job: seconds from the start of the last gbpt_batch_render to the end of the job's last
+ * iteration (device global timer). Synchronous. */
+GBPT_API gbpt_status gbpt_batch_job_seconds(gbpt_batch* b, double* seconds);
+/* A job's FP32 / FP64 radiance sums (width*height*3 each; either may be NULL). Synchronous. */
+GBPT_API gbpt_status gbpt_batch_get_image(gbpt_batch* b, int32_t job, float* rgb32, double* rgb64, void* stream);
+/* Rays traced by the last render, summed over the jobs (samples = sum of width*height*spp). */
+GBPT_API gbpt_status gbpt_batch_get_stats(gbpt_batch* b, gbpt_render_stats* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
