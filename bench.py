@@ -10,6 +10,11 @@ Workload (the traversal microbenchmark scene, FP32):
           (tmax = distance - 1e-4).
 A step = the three launches over the resident batch (closest primary, closest bounce, any shadow).
 The ray batch (604 MB in, 196 MB out per step) is larger than L2, so no extra flush is done.
+Launch configurations are picked per ray class by the autotuner before the timed region.
+
+The same JSON line carries "render": path-tracing workloads on the same GPU (Cornell box samples/s,
+many-light ReSTIR DI frames at 1080p, guided against plain path tracing, and 48 batched jobs in one
+wavefront with a CUDA graph per iteration); see render_workloads and batch_workload.
 
 --impl reference times the reference's CPU traversal instead (the reference's own code from
 oracle/_ref where it was compiled for this machine, else the oracle's restatement of it) on all
@@ -324,7 +329,106 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
                      "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg), "guide_error_flag": gd.error_flag()}
     # ---- guided against plain on the indirectly lit Cornell box ----
     out["guided_indirect_cornell"] = guided_indirect_cornell(timed)
+    del scene
+    torch.cuda.empty_cache()
+    # ---- batched jobs ----
+    out["batch"] = batch_workload(timed, log)
     return out
+
+
+def batch_jobs(n_jobs=48, seed=1):
+    """The batched workload's jobs, drawn from seed: resolution uniform over {128, 256, 512, 1024}^2,
+    a heightfield of 64^2..512^2 cells (fBm amplitude 0.2, 8k-524k triangles) plus 0..2000 emissive
+    triangles above it, random principled materials (the many-light distribution), bounces
+    U[2, 16], spp U[4, 64], camera above the tile looking at its centre, power light sampling."""
+    import gbpt
+    from gbpt import materials as M, scenes
+    from gbpt.render import BSDF_PRINCIPLED, LIGHT_POWER, RenderSettings, look_at_camera
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(n_jobs):
+        res = int(rng.choice([128, 256, 512, 1024]))
+        cells = int(rng.integers(64, 513))
+        n_emit = int(rng.integers(0, 2001))
+        hf = scenes.heightfield(cells=cells, amplitude=0.2, seed=int(rng.integers(1, 1 << 30)))
+        parts, mat_of = [hf], [rng.integers(0, 4, hf.n_triangles)]
+        mats = M.random_principled(rng, 4)
+        if n_emit:
+            em = scenes.random_triangles(n_emit, seed=int(rng.integers(1, 1 << 30)), lo=(-1.0, 0.35, -1.0),
+                                         hi=(1.0, 1.2, 1.0), sigma=0.02)
+            parts.append(em)
+            rad = np.exp(rng.uniform(0.0, np.log(1000.0), n_emit))
+            mats += [dict(base_color=(0.0, 0.0, 0.0), emission=(float(r), float(r) * 0.8, float(r) * 0.6)) for r in rad]
+            mat_of.append(4 + np.arange(n_emit))
+        else:  # no emitters: a single bright emissive quad-like triangle pair keeps the job lit
+            em = scenes.Mesh(np.array([[-0.3, 1.5, -0.3], [0.3, 1.5, -0.3], [0.3, 1.5, 0.3], [-0.3, 1.5, 0.3]], np.float32),
+                             np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+            parts.append(em)
+            mats.append(dict(base_color=(0.0, 0.0, 0.0), emission=(20.0, 18.0, 15.0)))
+            mat_of.append(np.array([4, 4]))
+        mesh = scenes.merge(*parts)
+        scene = gbpt.Scene(mesh.positions, mesh.indices, np.concatenate(mat_of).astype(np.int32),
+                           principled=M.pack_many(mats))
+        ang = rng.uniform(0, 2 * np.pi)
+        eye = (2.2 * np.cos(ang), 1.6, 2.2 * np.sin(ang))
+        iv, ip = look_at_camera(eye, (0.0, 0.0, 0.0), vfov_deg=50.0, aspect=1.0)
+        st = RenderSettings(width=res, height=res, samples_per_launch=int(rng.integers(4, 65)),
+                            nb_bounces=int(rng.integers(2, 17)), light_sampling=LIGHT_POWER, bsdf=BSDF_PRINCIPLED,
+                            seed=int(rng.integers(1, 1 << 30)), inverse_view=iv, inverse_projection=ip)
+        jobs.append((scene, st, {"res": res, "triangles": int(mesh.n_triangles), "emitters": n_emit,
+                                 "bounces": st.nb_bounces, "spp": st.samples_per_launch}))
+    return jobs
+
+
+def batch_workload(timed, log, ref_factor=4):
+    """48 jobs in one batched wavefront (one launch per stage for all jobs, one iteration captured
+    as a CUDA graph and replayed). samples_per_iteration is picked by timing candidates on the jobs
+    clipped to 8 spp; per-job relMSE against an FP64 image of ref_factor x the job's spp (the same
+    batch machinery, other seeds); job-completion latency from device timer stamps."""
+    import torch
+    import gbpt
+    from gbpt.render import RenderSettings
+    t0 = time.time()
+    jobs = batch_jobs()
+    log(f"batch: {len(jobs)} jobs built in {time.time() - t0:.1f}s")
+    pairs = [(sc, st) for sc, st, _ in jobs]
+    # autotune samples_per_iteration on the jobs clipped to 8 spp
+    clip = [(sc, RenderSettings(**{**st.__dict__, "samples_per_launch": min(8, st.samples_per_launch)})) for sc, st in pairs]
+    tune = {}
+    for k in (1, 2, 4, 8):
+        b = gbpt.Batch(clip, samples_per_iteration=k)
+        b.render()
+        tune[k] = timed(lambda: b.render())
+        del b
+    k_best = min(tune, key=tune.get)
+    b = gbpt.Batch(pairs, samples_per_iteration=k_best)
+    b.render()
+    ms = timed(lambda: b.render())
+    secs = b.job_seconds()
+    st = b.stats()
+    imgs = [b.image_sums(j)[1] / pairs[j][1].samples_per_launch for j in range(len(pairs))]
+    del b
+    ref_pairs = [(sc, RenderSettings(**{**s.__dict__, "samples_per_launch": ref_factor * s.samples_per_launch,
+                                       "seed": s.seed + 7919})) for sc, s in pairs]
+    rb = gbpt.Batch(ref_pairs, samples_per_iteration=k_best)
+    t_ref = timed(lambda: rb.render())
+    rel = []
+    for j in range(len(pairs)):
+        ref = rb.image_sums(j)[1] / ref_pairs[j][1].samples_per_launch
+        rel.append(_relmse(imgs[j], ref))
+    del rb
+    samples = st["samples"]
+    rays = st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
+    return {"config": "48 jobs from seed 1: res {128,256,512,1024}^2, heightfield 64^2..512^2 cells + 0..2000 emitters, "
+                      "principled, bounces U[2,16], spp U[4,64]; one wavefront, one graph per iteration",
+            "samples_per_iteration": k_best, "autotune_ms_8spp": tune, "ms": ms, "samples": samples,
+            "samples_per_s": samples / (ms * 1e-3), "mrays_per_s": rays / (ms * 1e-3) / 1e6,
+            "job_latency_s": {"p50": float(np.percentile(secs, 50)), "p99": float(np.percentile(secs, 99)),
+                              "max": float(secs.max())},
+            "relmse_vs_fp64": {"reference_spp_factor": ref_factor, "reference_ms": t_ref,
+                               "median": float(np.median(rel)), "max": float(np.max(rel)),
+                               "each": [round(x, 5) for x in rel]},
+            "jobs": [j for _, _, j in jobs]}
 
 
 def indirect_cornell_scene():
