@@ -490,6 +490,14 @@ gbpt_status gbpt_renderer_reset(gbpt_renderer* r, void* stream)
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "reset");
 }
 
+gbpt_status gbpt_renderer_set_sample_index(gbpt_renderer* r, int64_t first_sample)
+{
+    if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
+    if (first_sample < 0 || first_sample > INT32_MAX) return set_error(GBPT_ERROR_INVALID_ARG, "sample index out of range");
+    r->iteration = first_sample;
+    return GBPT_OK;
+}
+
 gbpt_status gbpt_pass_camera_rays(gbpt_renderer* r, void* stream)
 {
     if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");

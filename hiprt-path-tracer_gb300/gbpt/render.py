@@ -87,6 +87,7 @@ RENDER_SIGNATURES = [
     ("gbpt_guide_render_default_settings", ctypes.c_int, [c_vp]),
     ("gbpt_renderer_set_guide", ctypes.c_int, [c_vp, c_vp, c_vp]),
     ("gbpt_renderer_get_guide_records", ctypes.c_int, [c_vp, c_vp, i32, c_vp, c_vp]),
+    ("gbpt_renderer_set_sample_index", ctypes.c_int, [c_vp, i64]),
     ("gbpt_batch_default_params", ctypes.c_int, [c_vp]),
     ("gbpt_batch_create", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
     ("gbpt_batch_destroy", ctypes.c_int, [c_vp]),
@@ -283,6 +284,10 @@ class Renderer:
 
     def reset(self, stream=None):
         _lib.check(self._lib.gbpt_renderer_reset(self._h, _stream(stream)))
+
+    def set_sample_index(self, first_sample: int):
+        """Sample index of the next launch (sample-range sharding across ranks)."""
+        _lib.check(self._lib.gbpt_renderer_set_sample_index(self._h, int(first_sample)))
 
     def pass_camera_rays(self, stream=None):
         _lib.check(self._lib.gbpt_pass_camera_rays(self._h, _stream(stream)))

@@ -120,6 +120,10 @@ GBPT_API gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_re
                                           gbpt_renderer** out);
 GBPT_API gbpt_status gbpt_renderer_destroy(gbpt_renderer* r);
 GBPT_API gbpt_status gbpt_renderer_reset(gbpt_renderer* r, void* stream);
+/* Sample index of the next launch's first sample (the PCG streams are seeded by pixel and sample
+ * index): a rank rendering launches [a, a + n) of a sample-range-sharded image sets a * spp here
+ * after gbpt_renderer_reset, and the ranks' FP64 sums add up to the single-GPU image. */
+GBPT_API gbpt_status gbpt_renderer_set_sample_index(gbpt_renderer* r, int64_t first_sample);
 
 /* Full frame: n_launches x (camera rays + nb_bounces+1 wavefront bounces + accumulate), each
  * launch adding samples_per_launch samples per pixel. Replaces the render loop of

@@ -147,3 +147,22 @@ def test_pass_entry_points_equal_render(cuda):
     assert np.array_equal(full, parts)
     s = r.stats()
     assert s["samples"] == 24 * 24 * 2 and s["extension_rays"] >= 24 * 24 * 2
+
+
+def test_sample_range_shards_add_up_to_the_full_image(cuda):
+    """Two renderers covering launches [0, 3) and [3, 5) (set_sample_index) sum to the 5-launch
+    image: the sharding the multi-GPU path uses, one renderer per rank."""
+    from gbpt import sharding
+    cb = scenes.cornell_box()
+    scene = gbpt.Scene.from_cornell(cb)
+    st = gbpt.cornell_settings(32, 32, samples_per_launch=2, seed=4)
+    _, _, full = _render(scene, st, launches=5)
+    total = np.zeros_like(full)
+    for rank in range(2):
+        first, count = sharding.sample_range(rank, 2, 5)
+        r = gbpt.Renderer(scene, st)
+        r.set_sample_index(first * st.samples_per_launch)
+        r.render(count)
+        torch.cuda.synchronize()
+        total += r.image_sums()[1]
+    np.testing.assert_allclose(total, full, rtol=1e-12, atol=1e-12)
