@@ -7,7 +7,8 @@ Workload (the traversal microbenchmark scene, FP32):
   rays    16,777,216 per step: 8,388,608 primary (4096 x 2048 pinhole at (0,1.5,-2.5) aimed at the
           origin, 30 degree vertical FOV), 4,194,304 cosine-hemisphere bounce rays from primary hits,
           4,194,304 any-hit shadow rays to uniform points on a 0.5 x 0.5 quad at y = 2
-          (tmax = distance - 1e-4).
+          (tmax = distance - 1e-4). Primary rays are emitted in 4x8-pixel tiles (8-row bands); bounce
+          and shadow rays follow the order of the primary rays they continue.
 A step = the three launches over the resident batch (closest primary, closest bounce, any shadow).
 The ray batch (604 MB in, 196 MB out per step) is larger than L2, so no extra flush is done.
 Launch configurations are picked per ray class by the autotuner before the timed region.
@@ -51,7 +52,7 @@ TRI_BYTES = 36  # algorithmic: three float3 vertex records
 
 def workload_config(n_tris):
     return {"workload": "bvh-traversal-microbench", "triangles": n_tris, "rays_per_step": WIDTH * HEIGHT + N_BOUNCE + N_SHADOW,
-            "primary": f"{WIDTH}x{HEIGHT} pinhole, vfov {VFOV} deg", "bounce": N_BOUNCE, "shadow_any_hit": N_SHADOW,
+            "primary": f"{WIDTH}x{HEIGHT} pinhole, vfov {VFOV} deg, emitted in 4x8-pixel tiles (8-row bands)", "bounce": N_BOUNCE, "shadow_any_hit": N_SHADOW,
             "bvh": "binned SAH 32 bins, leaf<=3, 8-wide quantised (80 B nodes)",
             "l2": f"inputs larger than L2 ({(WIDTH * HEIGHT + N_BOUNCE + N_SHADOW) * RAY_IN_BYTES / 1e6:.0f} MB of rays per step); no flush"}
 
@@ -63,7 +64,7 @@ def build_workload(seed=1, log=print):
     t0 = time.time()
     mesh = scenes.traversal_scene(cells=1024, n_random=200_000, seed=seed)
     log(f"scene: {mesh.n_triangles} triangles in {time.time() - t0:.1f}s")
-    primary = scenes.pinhole_rays(WIDTH, HEIGHT, vfov_deg=VFOV)
+    primary = scenes.pinhole_rays(WIDTH, HEIGHT, vfov_deg=VFOV, order="bands")
     return mesh, primary
 
 
@@ -72,8 +73,10 @@ def secondary_rays(mesh, primary, primary_hits, seed=1):
     pts, nrm, prim = scenes.hit_points_normals(mesh, primary, primary_hits)
     hit_idx = np.nonzero(prim >= 0)[0]
     rng = np.random.Generator(np.random.PCG64(seed + 100))
-    pick_b = rng.choice(hit_idx, N_BOUNCE, replace=len(hit_idx) < N_BOUNCE)
-    pick_s = rng.choice(hit_idx, N_SHADOW, replace=len(hit_idx) < N_SHADOW)
+    # rays are emitted in the order of the primary rays they continue (as a wavefront's queues
+    # keep path order); their directions stay incoherent
+    pick_b = np.sort(rng.choice(hit_idx, N_BOUNCE, replace=len(hit_idx) < N_BOUNCE))
+    pick_s = np.sort(rng.choice(hit_idx, N_SHADOW, replace=len(hit_idx) < N_SHADOW))
     bounce = scenes.bounce_rays(pts[pick_b], nrm[pick_b], prim[pick_b], seed=seed + 2)
     shadow, _ = scenes.shadow_rays(pts[pick_s], prim[pick_s], seed=seed + 3)
     return bounce, shadow

@@ -43,22 +43,46 @@ __device__ __forceinline__ void camera_ray(const RenderConst& rc, int pixel, int
     dir = normalize(p_ws - origin);
 }
 
+// Pixel of the l-th camera ray of a sample plane: the image is walked in bands of 8 rows and,
+// inside a band, column by column (8 pixels of one column, then the next column), so that a warp
+// of 32 consecutive rays covers a 4 x 8 pixel tile (coherent traversal). A bijection for any W, H.
+__device__ __forceinline__ int64_t band_pixel(int64_t l, int W, int H)
+{
+    const int64_t band = 8LL * W;
+    const int64_t full = H / 8;
+    int64_t x, y;
+    if (l < full * band)
+    {
+        const int64_t b = l / band, r = l - b * band;
+        x = r >> 3;
+        y = b * 8 + (r & 7);
+    }
+    else
+    {
+        const int64_t bh = H - full * 8, r = l - full * band;
+        x = r / bh;
+        y = full * 8 + r % bh;
+    }
+    return y * W + x;
+}
+
 __global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers pb, Queue q, int32_t iteration_base,
                                                      unsigned long long* stats)
 {
     const int64_t n_pix = (int64_t)rc.width * rc.height;
     const int64_t n = n_pix * rc.spp;
-    for (int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; slot < n; slot += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     {
-        const int pixel = (int)(slot % n_pix);
-        const int s = (int)(slot / n_pix);
+        const int s = (int)(i / n_pix);
+        const int pixel = (int)band_pixel(i - (int64_t)s * n_pix, rc.width, rc.height);
+        const int64_t slot = pixel + (int64_t)s * n_pix;  // path slot: accumulation order is by slot
         V3 origin, dir;
         Pcg32 rng;
         camera_ray(rc, pixel, iteration_base + s, origin, dir, rng);
-        q.origin_tmin[slot] = f4(origin, 0.0f);
-        q.dir_tmax[slot] = f4(dir, INFINITY);
-        q.last_prim[slot] = -1;
-        q.slot[slot] = (int32_t)slot;
+        q.origin_tmin[i] = f4(origin, 0.0f);
+        q.dir_tmax[i] = f4(dir, INFINITY);
+        q.last_prim[i] = -1;
+        q.slot[i] = (int32_t)slot;
         pb.throughput[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         pb.radiance[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (pb.medium) pb.medium[slot] = -1;
@@ -776,11 +800,18 @@ __global__ void __launch_bounds__(256) camera_batch_kernel(const BatchJob* __res
         Pcg32 rng;
         rng.state = 0;
         rng.inc = 0;
-        if (valid) camera_ray(rc, (int)(local % n_pix), it * rc.spp + (int)(local / n_pix), origin, dir, rng);
+        int64_t pslot = 0;
+        if (valid)
+        {
+            const int s = (int)(local / n_pix);
+            const int pixel = (int)band_pixel(local - (int64_t)s * n_pix, rc.width, rc.height);
+            pslot = pixel + (int64_t)s * n_pix;
+            camera_ray(rc, pixel, it * rc.spp + s, origin, dir, rng);
+        }
         const int qi = warp_append(q.count, valid);
         if (valid)
         {
-            const int64_t slot = J.slot_base + local;
+            const int64_t slot = J.slot_base + pslot;
             q.origin_tmin[qi] = f4(origin, 0.0f);
             q.dir_tmax[qi] = f4(dir, INFINITY);
             q.last_prim[qi] = -1;

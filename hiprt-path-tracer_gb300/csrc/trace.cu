@@ -1,7 +1,8 @@
 // Closest-hit and any-hit traversal kernels of the 8-wide compressed BVH (sm_103a).
 //
-// The production kernels are persistent warps: each warp owns a contiguous chunk of the ray batch
-// and refills the lanes whose ray has finished (ballot + prefix) whenever fewer than kRefillBelow
+// The production kernels are persistent warps: each warp owns the groups of 32 consecutive rays
+// g = warp, warp + n_warps, ... (coherent within a group, balanced across warps when the batch's
+// cost varies along it) and refills the lanes whose ray has finished (ballot + prefix) whenever fewer than kRefillBelow
 // lanes are still tracing, so lanes do not idle while the warp's slowest ray finishes. One loop
 // iteration advances every active lane by one step: one node (8 child boxes), one triangle, or one
 // stack pop. Triangle work is postponed (its group pushed on the stack) while fewer than
@@ -23,6 +24,13 @@ namespace {
 constexpr int kThreads = 128;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
+// v-th ray of a warp: its (v / 32)-th group of 32 consecutive rays, the groups being dealt
+// round-robin over the warps of the grid
+__device__ __forceinline__ int64_t warp_ray(int64_t v, int64_t warp, int64_t n_warps)
+{
+    return ((v >> 5) * n_warps + warp) * 32 + (v & 31);
+}
+
 // refill_below: refill the warp when fewer lanes than this are tracing; postpone_below: run
 // triangle steps only when at least this many lanes have them (else postpone)
 template <bool ANY_HIT>
@@ -37,8 +45,9 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int64_t next = warp * rays_per_warp;  // warp-uniform cursor into the warp's chunk
-    const int64_t end = next + rays_per_warp < n_rays ? next + rays_per_warp : n_rays;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int64_t next = 0;  // warp-uniform cursor over the warp's own rays
+    const int64_t end = rays_per_warp;
 
     int64_t ray = -1;
     float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, idx = 0, idy = 0, idz = 0, tmin = 0, tmax = 0;
@@ -58,8 +67,9 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
         {
             if (ray < 0)
             {
-                const int64_t r = next + __popc(idle & ((1u << lane) - 1u));
-                if (r < end)
+                const int64_t v = next + __popc(idle & ((1u << lane) - 1u));
+                const int64_t r = warp_ray(v, warp, n_warps);
+                if (v < end && r < n_rays)
                 {
                     ray = r;
                     const float4 ot = origin_tmin[r], dt = dir_tmax[r];
@@ -203,13 +213,12 @@ __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nod
     if ((threadIdx.x & 31) == 0) next_ray[wib] = 0u;
     __syncwarp();
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t base = warp * rays_per_warp;
-    const int64_t end = base + rays_per_warp < n_rays ? base + rays_per_warp : n_rays;
-    if (base >= end) return;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (;;)
     {
-        const int64_t ray = base + (int64_t)atomicAdd(&next_ray[wib], 1u);
-        if (ray >= end) break;
+        const int64_t v = (int64_t)atomicAdd(&next_ray[wib], 1u);
+        const int64_t ray = warp_ray(v, warp, n_warps);
+        if (v >= rays_per_warp || ray >= n_rays) break;
         uint32_t cn = 0, ct = 0;
         const float4 h = core::trace_ray<ANY_HIT, false>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
                                                          last_prim ? last_prim[ray] : -1, cn, ct);
@@ -328,7 +337,7 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
         const int64_t needed = (n_rays + threads - 1) / threads;
         const int64_t blocks = needed < max_blocks ? needed : max_blocks;
         const int64_t warps = blocks * (threads / 32);
-        const int64_t per_warp = (n_rays + warps - 1) / warps;
+        const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
         if (any_hit)
             trace_fetch<true><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
                                                                         occluded);
@@ -341,7 +350,7 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
     const int64_t needed = (n_rays + threads - 1) / threads;
     const int64_t blocks = needed < max_blocks ? needed : max_blocks;
     const int64_t warps = blocks * (threads / 32);
-    const int64_t per_warp = (n_rays + warps - 1) / warps;
+    const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
     const int post_cap = kTraversalStack - bvh.depth - 1 > 0 ? kTraversalStack - bvh.depth - 1 : 0;
     if (any_hit)
         trace_persistent<true><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,

@@ -148,9 +148,29 @@ def _normalize(v: np.ndarray) -> np.ndarray:
     return v / np.linalg.norm(v, axis=-1, keepdims=True)
 
 
+def band_order(width: int, height: int) -> np.ndarray:
+    """Pixel index (row-major) of each position in band order: bands of 8 rows, each walked column by
+    column (8 pixels of a column, then the next), so 32 consecutive rays cover a 4 x 8 tile; the
+    last band has height % 8 rows. The order of the renderer's camera kernel (band_pixel)."""
+    l = np.arange(width * height, dtype=np.int64)
+    band = 8 * width
+    full = height // 8
+    x = np.empty_like(l)
+    y = np.empty_like(l)
+    m = l < full * band
+    b, r = l[m] // band, l[m] % band
+    x[m], y[m] = r >> 3, b * 8 + (r & 7)
+    if (~m).any():
+        bh = height - full * 8
+        r = l[~m] - full * band
+        x[~m], y[~m] = r // bh, full * 8 + r % bh
+    return y * width + x
+
+
 def pinhole_rays(width: int, height: int, eye=(0.0, 1.5, -2.5), target=(0.0, 0.0, 0.0),
-                 vfov_deg: float = 60.0, up=(0.0, 1.0, 0.0)) -> RayBatch:
-    """One ray through each pixel centre, row-major from the top-left pixel."""
+                 vfov_deg: float = 60.0, up=(0.0, 1.0, 0.0), order: str = "rows") -> RayBatch:
+    """One ray through each pixel centre: order "rows" is row-major from the top-left pixel,
+    "bands" is band_order (4 x 8 pixel tiles per 32 rays, the coherent order a renderer emits)."""
     eye = np.asarray(eye, np.float64)
     fwd = _normalize(np.asarray(target, np.float64) - eye)
     right = _normalize(np.cross(np.asarray(up, np.float64), fwd))
@@ -169,6 +189,11 @@ def pinhole_rays(width: int, height: int, eye=(0.0, 1.5, -2.5), target=(0.0, 0.0
     dt = np.empty((n, 4), F32)
     dt[:, :3] = d.astype(F32)
     dt[:, 3] = np.inf
+    if order == "bands":
+        perm = band_order(width, height)
+        o, dt = o[perm], dt[perm]
+    elif order != "rows":
+        raise ValueError(order)
     return RayBatch(o, dt, np.full(n, -1, np.int32))
 
 

@@ -85,3 +85,14 @@ def test_two_rank_sample_sharding_reproduces_the_single_render(tmp_path, oracle)
         got = np.load(tmp_path / f"rank{r}.npy")
         np.testing.assert_allclose(got, full, rtol=1e-12, atol=1e-12)
     assert full.sum() > 0
+
+
+def test_band_order_is_a_bijection_of_4x8_tiles():
+    from gbpt import scenes
+    for w, h in ((4096, 2048), (13, 11), (17, 23), (3, 5), (8, 8), (1, 1)):
+        p = scenes.band_order(w, h)
+        assert np.array_equal(np.sort(p), np.arange(w * h))
+    p = scenes.band_order(64, 16)
+    x, y = p % 64, p // 64
+    for k in range(0, 64 * 16, 32):  # every 32 consecutive rays form a 4 x 8 tile
+        assert x[k:k + 32].max() - x[k:k + 32].min() == 3 and y[k:k + 32].max() - y[k:k + 32].min() == 7
