@@ -155,6 +155,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                 gv.train_entry[slot] = -1;
                 gv.train_light_entry[slot] = -1;
             }
+            if (rc0.direct_ris) pb.ris[slot] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
         }
         // batched rendering: the scene and settings of the slot's job
         const BatchJob* J = (jobs && valid) ? jobs + pb.job[slot] : nullptr;
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
         float4 sh_o, sh_d, bs_d, nx_d;
         V3 P = v3(0, 0, 0), tp = v3(0, 0, 0);
         V3 light_contrib = v3(0, 0, 0);
+        float light_target = 0.0f;  // RIS: target function of the kept light candidate
         float4 bsdf_pending = make_float4(0, 0, 0, 0);
         int next_medium = -1;
         Pcg32 rng;
@@ -202,8 +204,38 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                 const float alpha = GL ? (gv.prob > 0.0f ? gv.prob : guide::alpha_at(GL)) : 0.0f;
                 guided_vertex = GL != nullptr;
                 rec_vertex = GL && gv.train_entry && record_hash((uint32_t)slot, (uint32_t)bounce, gv.frame) < rec_thr;
+                const bool ris = rc.direct_ris && !GL && s.n_emissive > 0;
+                if (ris)
+                {
+                    // ---- RIS direct lighting (sample_lights_RIS, RIS.h:83-255): light candidates
+                    // now; the BSDF candidate's ray is traced and the reservoir finished in resolve ----
+                    const RisPick pk = ris_light_candidates(s, rc, rng, P, ns, rc.ris_light, rc.ris_bsdf,
+                                                            [&](V3 wi, float& pdf) { return lambert_eval(albedo, dot(ns, wi), pdf); });
+                    if (pk.kept)
+                    {
+                        light_contrib = tp * pk.contrib;
+                        light_target = pk.target;
+                        want_shadow = true;
+                        sh_o = f4(P, 0.0f);
+                        sh_d = f4(pk.dir, pk.dist - 1.0e-4f);
+                    }
+                    pb.ris[slot] = f4(tp, pk.wsum);
+                    if (rc.ris_bsdf > 0)
+                    {
+                        const float r1 = rng.next(), r2 = rng.next();
+                        const V3 wi = cosine_sample(ns, r1, r2);
+                        float pdf;
+                        const V3 f = lambert_eval(albedo, dot(ns, wi), pdf);
+                        if (pdf > 0.0f)
+                        {
+                            want_bsdf = true;
+                            bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                            bsdf_pending = f4(f * fabsf(dot(ns, wi)), pdf);
+                        }
+                    }
+                }
                 // ---- next-event estimation: light sample (sample_one_light_MIS, Lights.h:123-185) ----
-                if (s.n_emissive > 0)
+                else if (s.n_emissive > 0)
                 {
                     const LightSample ls = sample_light(s, rc, rng);
                     if (ls.pdf_area > 0.0f)
@@ -240,7 +272,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                 }
 
                 // ---- next-event estimation: BSDF sample (Lights.h:187-226) ----
-                if (!GL)
+                if (!GL && !ris)
                 {
                     const float r1 = rng.next(), r2 = rng.next();
                     const V3 wi = cosine_sample(ns, r1, r2);
@@ -387,8 +419,46 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                 }
                 else
                 {
+                    const bool ris = rc.direct_ris && !GL && s.n_emissive > 0;
+                    if (ris)
+                    {
+                        // ---- RIS direct lighting (sample_lights_RIS, RIS.h:83-255; no light
+                        // candidates when the material cannot be light-sampled, RIS.h:91-92) ----
+                        const int M = can_light_sample(m) ? rc.ris_light : 0;
+                        const RisPick pk = ris_light_candidates(s, rc, rng, P, ns, M, rc.ris_bsdf, [&](V3 wi, float& pdf) {
+                            bsdf::Query q;
+                            q.view = view;
+                            q.ns = ns;
+                            q.ng = ng;
+                            q.light = wi;
+                            return bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, pdf);
+                        });
+                        if (pk.kept)
+                        {
+                            light_contrib = tp * pk.contrib;
+                            light_target = pk.target;
+                            want_shadow = true;
+                            sh_o = f4(P, 0.0f);
+                            sh_d = f4(pk.dir, pk.dist - 1.0e-4f);
+                        }
+                        pb.ris[slot] = f4(tp, M > 0 ? pk.wsum : -0.5f);
+                        if (rc.ris_bsdf > 0)
+                        {
+                            bsdf::Xorshift32 xr = bsdf_rng(rng);
+                            V3 wi;
+                            int lobe;
+                            float pdf;
+                            const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                            if (pdf > 0.0f)
+                            {
+                                want_bsdf = true;
+                                bs_d = f4(wi, 1.0e35f - 1.0e-4f);
+                                bsdf_pending = f4(f * fabsf(dot(ns, wi)), pdf);
+                            }
+                        }
+                    }
                     // ---- next-event estimation: light sample ----
-                    if (s.n_emissive > 0 && can_light_sample(m))
+                    if (!ris && s.n_emissive > 0 && can_light_sample(m))
                     {
                         const LightSample ls = sample_light(s, rc, rng);
                         if (ls.pdf_area > 0.0f)
@@ -430,7 +500,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                     }
 
                     // ---- next-event estimation: BSDF sample ----
-                    if (!GL)
+                    if (!GL && !ris)
                     {
                         bsdf::Xorshift32 xr = bsdf_rng(rng);
                         V3 wi;
@@ -539,7 +609,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             shadow.last_prim[si] = prim;
             shadow.slot[si] = slot;
             pb.shadow_entry[slot] = si;
-            pb.pending_light[slot] = f4(light_contrib, 0.0f);
+            pb.pending_light[slot] = f4(light_contrib, light_target);
         }
         const int bi = warp_append(bsdfq.count, want_bsdf);
         if (want_bsdf)
@@ -627,6 +697,69 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst 
         const int te = gv.train_entry ? gv.train_entry[slot] : -1;
         const int tle = gv.train_entry ? gv.train_light_entry[slot] : -1;
         if (tle >= 0 && (se < 0 || shadow.occluded[se])) gv.rec_weight[tle] = 0.0f;
+        if (rc.direct_ris)
+        {
+            const float4 ra = pb.ris[slot];
+            if (ra.w > -0.75f)
+            {
+                // ---- RIS direct lighting, continued: the BSDF candidate (RIS.h:200-249) is added
+                // to the light candidates' reservoir, then the kept sample is shaded
+                // (evaluate_reservoir_sample, RIS.h:19-80; UCW = w_sum / p^) ----
+                const int M = ra.w >= 0.0f ? rc.ris_light : 0, N = rc.ris_bsdf;
+                float w_b = 0.0f, t_b = 0.0f;
+                V3 c_b = v3(0.0f);
+                if (be >= 0)
+                {
+                    const float4 h = bsdfq.hits[be];
+                    const int lprim = __float_as_int(h.w);
+                    if (lprim >= 0)
+                    {
+                        const V3 Le = xyz(s.materials[__ldg(s.material_of + lprim)].emission);
+                        V3 a, b, c;
+                        load_triangle(s, lprim, a, b, c);
+                        const V3 nrm = cross(b - a, c - a);
+                        const float len = length(nrm);
+                        const V3 wi = xyz(bsdfq.dir_tmax[be]);
+                        const float cos_l = fmaxf(0.0f, dot(nrm / len, -wi));
+                        if (!is_black(Le) && cos_l > 0.0f)
+                        {
+                            const float area = 0.5f * len;
+                            float pdf_area = 1.0f / area;
+                            if (rc.light_sampling == GBPT_LIGHT_POWER)
+                                pdf_area *= (luminance(Le) * area) / s.power_sum;
+                            else
+                                pdf_area /= (float)s.n_emissive;
+                            const float light_pdf = area_to_solid_angle_pdf(pdf_area, h.x, cos_l);
+                            const float4 pend = pb.pending_bsdf[slot];  // f |cos|, BSDF pdf
+                            c_b = xyz(pend) * Le;
+                            t_b = luminance(c_b);
+                            w_b = balance_counts(pend.w, (float)N, light_pdf, (float)M) * t_b / pend.w;
+                        }
+                    }
+                }
+                const float4 pl = pb.pending_light[slot];  // T f Le cos of the kept light, its p^
+                const bool light_ok = se >= 0 && !shadow.occluded[se];
+                float wsum = fmaxf(ra.w, 0.0f);
+                bool take_bsdf = false;
+                if (N > 0)
+                {
+                    wsum += w_b;
+                    Pcg32 prng;
+                    prng.inc = pcg_inc(rc.seed);
+                    prng.state = pb.rng[slot];
+                    take_bsdf = prng.next() < w_b / wsum;
+                    store_rng(pb.rng + slot, prng);
+                }
+                V3 add = v3(0.0f);
+                if (take_bsdf)
+                    add = xyz(ra) * c_b * (wsum / t_b);
+                else if (light_ok && pl.w > 0.0f)
+                    add = xyz(pl) * (wsum / pl.w);
+                const float4 r = pb.radiance[slot];
+                pb.radiance[slot] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
+                continue;
+            }
+        }
         if (se < 0 && be < 0)
         {
             if (te >= 0) gv.rec_snap[te] = pb.radiance[slot];

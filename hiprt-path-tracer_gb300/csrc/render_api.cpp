@@ -385,6 +385,12 @@ gbpt_status check_settings(const gbpt_scene* scene, const gbpt_render_settings* 
         return set_error(GBPT_ERROR_UNSUPPORTED, "bsdf must be GBPT_BSDF_LAMBERTIAN or GBPT_BSDF_PRINCIPLED");
     if (st->bsdf == GBPT_BSDF_PRINCIPLED && !scene->principled)
         return set_error(GBPT_ERROR_INVALID_ARG, "GBPT_BSDF_PRINCIPLED needs a scene created with principled_materials");
+    if (st->direct_lighting != GBPT_DIRECT_MIS && st->direct_lighting != GBPT_DIRECT_RIS)
+        return set_error(GBPT_ERROR_INVALID_ARG, "unknown direct_lighting");
+    if (st->direct_lighting == GBPT_DIRECT_RIS &&
+        (st->ris_light_candidates < 0 || st->ris_light_candidates > 64 || st->ris_bsdf_candidates < 0 ||
+         st->ris_bsdf_candidates > 1 || st->ris_light_candidates + st->ris_bsdf_candidates == 0))
+        return set_error(GBPT_ERROR_INVALID_ARG, "RIS needs 0..64 light and 0..1 BSDF candidates, at least one");
     return GBPT_OK;
 }
 
@@ -404,6 +410,9 @@ gbpt::RenderConst render_const(const gbpt_render_settings* st, int32_t spp)
     rc.seed = st->seed;
     rc.do_jittering = st->do_jittering;
     rc.ggx_height_correlated = st->ggx_height_correlated;
+    rc.direct_ris = st->direct_lighting == GBPT_DIRECT_RIS ? 1 : 0;
+    rc.ris_light = st->ris_light_candidates;
+    rc.ris_bsdf = st->ris_bsdf_candidates;
     std::memcpy(rc.inverse_view, st->inverse_view, sizeof(rc.inverse_view));
     std::memcpy(rc.inverse_projection, st->inverse_projection, sizeof(rc.inverse_projection));
     return rc;
@@ -423,6 +432,7 @@ void alloc_paths(DevMem& M, int64_t cap, bool principled, bool batched, gbpt::Pa
     pb.bsdf_entry = M.alloc<int32_t>(cap);
     pb.medium = principled ? M.alloc<int32_t>(cap) : nullptr;
     pb.job = batched ? M.alloc<int32_t>(cap) : nullptr;
+    pb.ris = M.alloc<float4>(cap);
     q[0] = make_queue(M, cap, true, false);
     q[1] = make_queue(M, cap, true, false);
     shadow = make_queue(M, cap, false, true);

@@ -67,6 +67,9 @@ struct PathBuffers
     int32_t* bsdf_entry;    // queue index of the slot's BSDF-light ray this bounce, -1 if none
     int32_t* medium;        // material index of the volume the path travels in, -1 = air
     int32_t* job;           // batched rendering: the job of each slot (null for a single renderer)
+    float4* ris;            // RIS vertex: throughput before the continuation (rgb) and the light
+                            // candidates' weight sum (w); w = -0.5: RIS without light candidates,
+                            // w = -1: not a RIS vertex
 };
 
 // Learned path guiding in the wavefront (all device pointers; lobes == nullptr: guiding off).

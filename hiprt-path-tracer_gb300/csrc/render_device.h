@@ -107,6 +107,71 @@ __device__ __forceinline__ LightSample sample_light(const SceneView& s, const Re
     return ls;
 }
 
+// Balance heuristic with sample counts as the reference writes it (Sampling.h:103-116): the count
+// of technique a is left out of the numerator because RIS divides it out again.
+__device__ __forceinline__ float balance_counts(float pdf_a, float n_a, float pdf_b, float n_b)
+{
+    return pdf_a == 0.0f ? 0.0f : pdf_a / (n_a * pdf_a + n_b * pdf_b);
+}
+
+// The light candidates of RIS direct lighting (sample_bsdf_and_lights_RIS_reservoir,
+// src/Device/includes/RIS/RIS.h:96-198): M light samples, target p^ = luminance(f Le cos), weight
+// balance(p_light, M, p_bsdf, N) p^ / p_light, one weighted-reservoir draw per candidate
+// (RIS_Reservoir.h add_one_candidate: M++, w_sum += w, keep if u < w / w_sum). 'eval(wi, pdf)'
+// evaluates the BSDF (f without the cosine) and its pdf.
+struct RisPick
+{
+    V3 point, contrib, dir;  // contrib = f Le cos of the kept candidate
+    float target, dist, wsum;
+    bool kept;
+};
+
+template <class Eval>
+__device__ __forceinline__ RisPick ris_light_candidates(const SceneView& s, const RenderConst& rc, Pcg32& rng, V3 P, V3 ns,
+                                                        int M, int N, Eval eval)
+{
+    RisPick r;
+    r.kept = false;
+    r.wsum = 0.0f;
+    r.target = 0.0f;
+    r.dist = 0.0f;
+    r.point = r.contrib = r.dir = v3(0.0f);
+    for (int i = 0; i < M; i++)
+    {
+        const LightSample ls = sample_light(s, rc, rng);
+        float w = 0.0f, target = 0.0f, dist = 0.0f;
+        V3 c = v3(0.0f), wi = v3(0.0f);
+        if (ls.pdf_area > 0.0f)
+        {
+            const V3 tl = ls.point - P;
+            dist = length(tl);
+            wi = tl / dist;
+            const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
+            const float cos_p = fabsf(dot(ns, wi));
+            if (cos_p > 0.0f && cos_l > 1.0e-6f)
+            {
+                float p_bsdf;
+                const V3 f = eval(wi, p_bsdf);
+                c = f * ls.emission * cos_p;
+                target = luminance(c);
+                const float p_light = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
+                w = balance_counts(p_light, (float)M, p_bsdf, (float)N) * target / p_light;
+            }
+        }
+        r.wsum += w;
+        if (rng.next() < w / r.wsum)
+        {
+            r.kept = true;
+            r.point = ls.point;
+            r.contrib = c;
+            r.dir = wi;
+            r.dist = dist;
+            r.target = target;
+        }
+    }
+    return r;
+}
+
 // A BSDF sample draws its random numbers from a Xorshift32 generator (the reference's generator,
 // src/HostDeviceCommon/Xorshift.h) seeded by the path's PCG stream, so the same numbers can be
 // replayed through the reference's own BSDF.

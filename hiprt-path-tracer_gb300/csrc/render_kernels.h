@@ -27,6 +27,8 @@ struct RenderConst
     int32_t do_jittering;
     int32_t ggx_height_correlated;
     int32_t restir_final_visibility;  // ReSTIR DI final shading traces a shadow ray unless known unoccluded
+    int32_t direct_ris;               // GBPT_DIRECT_RIS
+    int32_t ris_light, ris_bsdf;      // RIS candidates
     float inverse_view[16];
     float inverse_projection[16];
 };

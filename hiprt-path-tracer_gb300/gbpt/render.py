@@ -21,6 +21,7 @@ LIGHT_UNIFORM = 0
 LIGHT_POWER = 1
 BSDF_LAMBERTIAN = 1
 BSDF_PRINCIPLED = 3
+DIRECT_MIS, DIRECT_RIS = 0, 1
 GBPT_ALIAS_NOALLOC_MAX_EMITTERS = 131072  # include/gbpt_render.h
 
 
@@ -39,6 +40,8 @@ class RenderSettingsC(ctypes.Structure):
                 ("do_russian_roulette", i32), ("russian_roulette_min_depth", i32),
                 ("russian_roulette_throughput_clamp", ctypes.c_float), ("light_sampling", i32), ("bsdf", i32),
                 ("seed", ctypes.c_uint32), ("do_jittering", i32), ("ggx_height_correlated", i32),
+                ("direct_lighting", i32), ("ris_light_candidates", i32), ("ris_bsdf_candidates", i32),
+                ("reserved_settings", i32),
                 ("inverse_view", ctypes.c_float * 16), ("inverse_projection", ctypes.c_float * 16)]
 
 
@@ -177,13 +180,16 @@ class RenderSettings:
     seed: int = 1
     do_jittering: bool = True
     ggx_height_correlated: bool = False
+    direct_lighting: int = 0  # DIRECT_MIS
+    ris_light_candidates: int = 4
+    ris_bsdf_candidates: int = 1
     inverse_view: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
     inverse_projection: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
 
     def to_c(self) -> RenderSettingsC:
         c = RenderSettingsC()
         for k in ("width", "height", "samples_per_launch", "nb_bounces", "russian_roulette_min_depth",
-                  "light_sampling", "bsdf", "seed"):
+                  "light_sampling", "bsdf", "seed", "direct_lighting", "ris_light_candidates", "ris_bsdf_candidates"):
             setattr(c, k, int(getattr(self, k)))
         c.do_russian_roulette = 1 if self.do_russian_roulette else 0
         c.do_jittering = 1 if self.do_jittering else 0

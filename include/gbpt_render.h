@@ -93,6 +93,16 @@ enum {
 };
 
 /* Subset of HIPRTRenderSettings + HIPRTCamera used by the render path. */
+/* Direct lighting at a path vertex (DirectLightSamplingBaseStrategy,
+ * src/HostDeviceCommon/KernelOptions/DirectLightSamplingOptions.h):
+ *   GBPT_DIRECT_MIS: one light sample and one BSDF sample combined by the balance heuristic
+ *     (LSS_ONE_LIGHT_MIS, sample_one_light_MIS, src/Device/includes/LightSampling/Lights.h:123-226);
+ *   GBPT_DIRECT_RIS: resampled importance sampling over ris_light_candidates light samples and
+ *     ris_bsdf_candidates BSDF samples (LSS_RIS_BSDF_AND_LIGHT, the reference's default,
+ *     src/Device/includes/RIS/RIS.h:83-255), one shadow ray for the selected light sample.
+ * Vertices guided by the learned proposal and the ReSTIR DI bounce keep their own estimators. */
+enum { GBPT_DIRECT_MIS = 0, GBPT_DIRECT_RIS = 1 };
+
 typedef struct gbpt_render_settings {
     int32_t width, height;
     int32_t samples_per_launch;      /* spp traced together in one wavefront (>= 1) */
@@ -105,6 +115,10 @@ typedef struct gbpt_render_settings {
     uint32_t seed;
     int32_t do_jittering;            /* HIPRTCamera::do_jittering */
     int32_t ggx_height_correlated;   /* BRDFsData::GGX_masking_shadowing: 0 = height-uncorrelated (default) */
+    int32_t direct_lighting;         /* GBPT_DIRECT_* (DirectLightSamplingBaseStrategy) */
+    int32_t ris_light_candidates;    /* RISSettings::number_of_light_candidates [4] */
+    int32_t ris_bsdf_candidates;     /* RISSettings::number_of_bsdf_candidates, 0 or 1 [1] */
+    int32_t reserved_settings;
     float inverse_view[16];          /* row-major, points multiplied on the right */
     float inverse_projection[16];
 } gbpt_render_settings;

@@ -183,6 +183,8 @@ struct Settings
     float rr_clamp;
     const float* iv;
     const float* ip;
+    int direct = 0;             // 0: one light + one BSDF sample with MIS, 1: RIS
+    int ris_m = 4, ris_n = 1;   // RIS light / BSDF candidates
 };
 
 // ---------------------------------------------------------------------------------------------

@@ -43,6 +43,134 @@
 
 namespace {
 
+// ---------------------------------------------------------------------------------------------
+// RIS direct lighting (sample_bsdf_and_lights_RIS_reservoir + evaluate_reservoir_sample,
+// src/Device/includes/RIS/RIS.h:19-255; RISReservoir, src/Device/includes/RIS/RIS_Reservoir.h):
+// M light candidates with target p^ = luminance(f Le |cos|) and weight balance(p_l, M, p_b, N)
+// p^ / p_l, then N (0 or 1) BSDF candidates whose ray is traced to find an emitter, weight
+// balance(p_b, N, p_l, M) p^ / p_b; one reservoir draw per candidate (u < w / w_sum keeps it);
+// UCW = w_sum / p^ of the kept sample; a kept light sample is shaded through a shadow ray, a
+// kept BSDF sample without one. The balance heuristic leaves the count out of the numerator as
+// the reference's does (src/Device/includes/Sampling.h:103-116).
+// Random numbers (the GPU kernels' order): per light candidate the light sample's draws then the
+// reservoir draw; the BSDF candidate's sample draws; then the vertex's continuation draws; then
+// (in the GPU's resolve pass) the BSDF candidate's reservoir draw.
+// ---------------------------------------------------------------------------------------------
+float bal(float a, float na, float b, float nb) { return a == 0.0f ? 0.0f : a / (na * a + nb * b); }
+
+struct LightDraw
+{
+    V lp, lnrm, Le;
+    float pa;
+};
+
+LightDraw draw_light(const Scene& s, const Settings& st, Pcg& rng)
+{
+    int e;
+    if (st.light == 1)
+    {
+        e = rng.index(s.ne);
+        if (rng.next() > s.alias_prob[e]) e = s.alias_idx[e];
+    }
+    else
+        e = rng.index(s.ne);
+    int lt = s.emissive[e];
+    float r1 = rng.next(), r2 = rng.next();
+    if (r2 > r1) { r1 *= 0.5f; r2 -= r1; }
+    else { r2 *= 0.5f; r1 -= r2; }
+    V la = s.a(lt), ab = s.b(lt) - la, ac = s.c(lt) - la;
+    V n = cross(ab, ac);
+    float ln = len(n);
+    LightDraw d;
+    d.lp = la + ab * r1 + ac * r2;
+    d.lnrm = n / ln;
+    d.Le = s.emi(lt);
+    d.pa = light_pdf_area(s, lt, 0.5f * ln, d.Le, st.light);
+    return d;
+}
+
+struct Ris
+{
+    bool active = false, kept = false;
+    V lp = mk(0, 0, 0), dir = mk(0, 0, 0), c_l = mk(0, 0, 0), c_b = mk(0, 0, 0);
+    float dist = 0, t_l = 0, t_b = 0, w_l = 0, w_b = 0;
+    int M = 0;
+};
+
+// light candidates; eval(wi, pdf) -> f
+template <class Eval>
+void ris_lights(const Scene& s, const Settings& st, Pcg& rng, V P, V ns, int M, int N, Eval eval, Ris& r)
+{
+    r.active = true;
+    r.M = M;
+    for (int i = 0; i < M; i++)
+    {
+        LightDraw ld = draw_light(s, st, rng);
+        float w = 0.0f, target = 0.0f, dist = 0.0f;
+        V c = mk(0, 0, 0), wi = mk(0, 0, 0);
+        if (ld.pa > 0.0f)
+        {
+            V tl = ld.lp - P;
+            dist = len(tl);
+            wi = tl / dist;
+            float cl = std::max(0.0f, dot(ld.lnrm, neg(wi)));
+            float cp = std::fabs(dot(ns, wi));
+            if (cp > 0.0f && cl > 1.0e-6f)
+            {
+                float pb;
+                V f = eval(wi, pb);
+                c = f * ld.Le * cp;
+                target = lum(c);
+                float pl = a2s(ld.pa, dist, cl);
+                w = bal(pl, (float)M, pb, (float)N) * target / pl;
+            }
+        }
+        r.w_l += w;
+        if (rng.next() < w / r.w_l)
+        {
+            r.kept = true;
+            r.lp = ld.lp;
+            r.dir = wi;
+            r.dist = dist;
+            r.c_l = c;
+            r.t_l = target;
+        }
+    }
+}
+
+// BSDF candidate given its sampled direction, BSDF value and pdf: traces the ray to an emitter
+void ris_bsdf(const Scene& s, const Settings& st, V P, V ns, int prim, V wi, V f, float pdf, int N, Ris& r)
+{
+    if (pdf <= 0.0f) return;
+    float th;
+    int lp = closest(s, P, wi, prim, th);
+    if (lp < 0 || !(th < 1.0e35f - 1.0e-4f)) return;
+    V Le = s.emi(lp);
+    V n = cross(s.b(lp) - s.a(lp), s.c(lp) - s.a(lp));
+    float ln = len(n);
+    float cl = std::max(0.0f, dot(n / ln, neg(wi)));
+    if (black(Le) || !(cl > 0.0f)) return;
+    float lpdf = a2s(light_pdf_area(s, lp, 0.5f * ln, Le, st.light), th, cl);
+    r.c_b = f * std::fabs(dot(ns, wi)) * Le;
+    r.t_b = lum(r.c_b);
+    r.w_b = bal(pdf, (float)N, lpdf, (float)r.M) * r.t_b / pdf;
+}
+
+// the reservoir's last draw (BSDF candidate) and the shading of the kept sample
+V ris_finish(const Scene& s, const Settings& st, Pcg& rng, V P, int prim, V tp, const Ris& r)
+{
+    float wsum = r.w_l;
+    bool take_bsdf = false;
+    if (st.ris_n > 0)
+    {
+        wsum += r.w_b;
+        take_bsdf = rng.next() < r.w_b / wsum;
+    }
+    if (take_bsdf) return tp * r.c_b * (wsum / r.t_b);
+    if (r.kept && r.t_l > 0.0f && !occluded(s, P, r.dir, prim, r.dist - 1.0e-4f)) return tp * r.c_l * (wsum / r.t_l);
+    return mk(0, 0, 0);
+}
+
 V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
 {
     const int x = pixel % st.width, y = pixel / st.width;
@@ -79,7 +207,22 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
         }
         V albedo = s.alb(prim);
         if (bounce == 0) L = L + s.emi(prim);
-        if (s.ne > 0)
+        Ris ris;
+        const V tp0 = tp;
+        if (st.direct == 1 && s.ne > 0)
+        {
+            ris_lights(s, st, rng, P, ns, st.ris_m, st.ris_n,
+                       [&](V wi, float& pb) { return lambert(albedo, dot(ns, wi), pb); }, ris);
+            if (st.ris_n > 0)
+            {
+                float r1 = rng.next(), r2 = rng.next();
+                V wi = cosine_sample(ns, r1, r2);
+                float pdf;
+                V f = lambert(albedo, dot(ns, wi), pdf);
+                ris_bsdf(s, st, P, ns, prim, wi, f, pdf, st.ris_n, ris);
+            }
+        }
+        else if (s.ne > 0)
         {
             int e;
             if (st.light == 1)
@@ -121,6 +264,7 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
                 }
             }
         }
+        if (!ris.active)
         {
             float r1 = rng.next(), r2 = rng.next();
             V wi = cosine_sample(ns, r1, r2);
@@ -148,26 +292,32 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
                 }
             }
         }
-        if (bounce == st.nb_bounces) break;
-        float r1 = rng.next(), r2 = rng.next();
-        V wi = cosine_sample(ns, r1, r2);
-        float pdf;
-        V f = lambert(albedo, dot(ns, wi), pdf);
-        if (pdf <= 0.0f) break;
-        V att = f * std::fabs(dot(wi, ns)) / pdf;
-        if (st.do_rr && bounce >= st.rr_min)
-        {
-            float p = std::min(std::max(tp.x, std::max(tp.y, tp.z)), 1.0f);
-            if (rng.next() > p) break;
-            float sc = 1.0f / p;
-            if (st.rr_clamp > 0.0f) sc = std::min(sc, st.rr_clamp);
-            tp = tp * sc;
-        }
-        tp = tp * att;
-        tp = mk(std::max(tp.x, 1.0e-5f), std::max(tp.y, 1.0e-5f), std::max(tp.z, 1.0e-5f));
-        o = P;
-        d = wi;
-        skip = prim;
+        // continuation (its draws precede the RIS reservoir's last draw, as on the GPU)
+        auto cont = [&]() {
+            float r1 = rng.next(), r2 = rng.next();
+            V wi = cosine_sample(ns, r1, r2);
+            float pdf;
+            V f = lambert(albedo, dot(ns, wi), pdf);
+            if (pdf <= 0.0f) return false;
+            V att = f * std::fabs(dot(wi, ns)) / pdf;
+            if (st.do_rr && bounce >= st.rr_min)
+            {
+                float p = std::min(std::max(tp.x, std::max(tp.y, tp.z)), 1.0f);
+                if (rng.next() > p) return false;
+                float sc = 1.0f / p;
+                if (st.rr_clamp > 0.0f) sc = std::min(sc, st.rr_clamp);
+                tp = tp * sc;
+            }
+            tp = tp * att;
+            tp = mk(std::max(tp.x, 1.0e-5f), std::max(tp.y, 1.0e-5f), std::max(tp.z, 1.0e-5f));
+            o = P;
+            d = wi;
+            skip = prim;
+            return true;
+        };
+        const bool go = bounce < st.nb_bounces && cont();
+        if (ris.active) L = L + ris_finish(s, st, rng, P, prim, tp0, ris);
+        if (!go) break;
     }
     return L;
 }
@@ -217,7 +367,29 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
         const float eta_i = inside ? m[37] : (medium >= 0 ? ps.mat(medium)[37] : 1.0f);
         const float eta_o = inside ? 1.0f : m[37];
         float q[16], out[8];
-        if (s.ne > 0 && can_light_sample(m))
+        Ris ris;
+        const V tp0 = tp;
+        if (st.direct == 1 && s.ne > 0)
+        {
+            const int M = can_light_sample(m) ? st.ris_m : 0;
+            ris_lights(s, st, rng, P, ns, M, st.ris_n,
+                       [&](V wi, float& pb) {
+                           float qq[16], oo[8];
+                           make_query(qq, view, ns, ng, wi, eta_i, eta_o, inside, 0);
+                           ps.eval(m, qq, oo);
+                           pb = oo[3];
+                           return mk(oo[0], oo[1], oo[2]);
+                       },
+                       ris);
+            if (st.ris_n > 0)
+            {
+                make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
+                int32_t lobe;
+                ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+                ris_bsdf(s, st, P, ns, prim, mk(out[0], out[1], out[2]), mk(out[3], out[4], out[5]), out[6], st.ris_n, ris);
+            }
+        }
+        else if (s.ne > 0 && can_light_sample(m))
         {
             int e;
             if (st.light == 1)
@@ -261,6 +433,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                 }
             }
         }
+        if (!ris.active)
         {
             make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
             int32_t lobe;
@@ -290,29 +463,34 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                 }
             }
         }
-        if (bounce == st.nb_bounces) break;
-        make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
-        int32_t lobe;
-        ps.sample(m, q, bsdf_seed(rng), out, &lobe);
-        const float pdf = out[6];
-        if (pdf <= 0.0f) break;
-        V wi = mk(out[0], out[1], out[2]);
-        V f = mk(out[3], out[4], out[5]);
-        V att = f * std::fabs(dot(wi, ns)) / pdf;
-        if (st.do_rr && bounce >= st.rr_min)
-        {
-            float p = std::min(std::max(tp.x, std::max(tp.y, tp.z)), 1.0f);
-            if (rng.next() > p) break;
-            float sc = 1.0f / p;
-            if (st.rr_clamp > 0.0f) sc = std::min(sc, st.rr_clamp);
-            tp = tp * sc;
-        }
-        tp = tp * att;
-        tp = mk(std::max(tp.x, 1.0e-5f), std::max(tp.y, 1.0e-5f), std::max(tp.z, 1.0e-5f));
-        if (transmissive && (lobe == 64 || lobe == 256)) medium = inside ? -1 : mi;
-        o = P;
-        d = wi;
-        skip = prim;
+        auto cont = [&]() {
+            make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
+            int32_t lobe;
+            ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+            const float pdf = out[6];
+            if (pdf <= 0.0f) return false;
+            V wi = mk(out[0], out[1], out[2]);
+            V f = mk(out[3], out[4], out[5]);
+            V att = f * std::fabs(dot(wi, ns)) / pdf;
+            if (st.do_rr && bounce >= st.rr_min)
+            {
+                float p = std::min(std::max(tp.x, std::max(tp.y, tp.z)), 1.0f);
+                if (rng.next() > p) return false;
+                float sc = 1.0f / p;
+                if (st.rr_clamp > 0.0f) sc = std::min(sc, st.rr_clamp);
+                tp = tp * sc;
+            }
+            tp = tp * att;
+            tp = mk(std::max(tp.x, 1.0e-5f), std::max(tp.y, 1.0e-5f), std::max(tp.z, 1.0e-5f));
+            if (transmissive && (lobe == 64 || lobe == 256)) medium = inside ? -1 : mi;
+            o = P;
+            d = wi;
+            skip = prim;
+            return true;
+        };
+        const bool go = bounce < st.nb_bounces && cont();
+        if (ris.active) L = L + ris_finish(s, st, rng, P, prim, tp0, ris);
+        if (!go) break;
     }
     return L;
 }
@@ -322,7 +500,8 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
 extern "C" {
 
 /* settings_i: width, height, nb_bounces, do_rr, rr_min_depth, light_sampling (0 uniform, 1 power),
- * seed, do_jittering, spp, iteration_base. Adds the samples of iterations
+ * seed, do_jittering, spp, iteration_base, direct lighting (0 MIS, 1 RIS), RIS light candidates,
+ * RIS BSDF candidates. Adds the samples of iterations
  * [iteration_base, iteration_base + spp) to out_rgb (W*H*3 doubles). */
 void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const float* albedo, const float* emission,
                    const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx, float power_sum,
@@ -331,7 +510,8 @@ void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const 
 {
     Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
-                settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj};
+                settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
+                settings_i[10], settings_i[11], settings_i[12]};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};
@@ -387,7 +567,8 @@ void orc_pt_render_principled(const float* tri_verts, int n_tris, const int* mat
     Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
     PScene ps{pmats, (bsdf_eval_fn)eval_fn, (bsdf_sample_fn)sample_fn};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
-                settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj};
+                settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
+                settings_i[10], settings_i[11], settings_i[12]};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};

@@ -190,7 +190,9 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
     ai = np.ascontiguousarray(alias_idx if alias_idx is not None else np.arange(len(ei)), np.int32)
     s = settings
     si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0, s.russian_roulette_min_depth,
-                   s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base], np.int32)
+                   s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base,
+                   getattr(s, "direct_lighting", 0), getattr(s, "ris_light_candidates", 4),
+                   getattr(s, "ris_bsdf_candidates", 1)], np.int32)
     iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
     ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
     out = np.zeros((s.height, s.width, 3), np.float64)
@@ -227,7 +229,9 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
     ai = np.ascontiguousarray(alias_idx if alias_idx is not None else np.arange(len(ei)), np.int32)
     s = settings
     si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0, s.russian_roulette_min_depth,
-                   s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base], np.int32)
+                   s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base,
+                   getattr(s, "direct_lighting", 0), getattr(s, "ris_light_candidates", 4),
+                   getattr(s, "ris_bsdf_candidates", 1)], np.int32)
     iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
     ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
     out = np.zeros((s.height, s.width, 3), np.float64)

@@ -25,6 +25,7 @@ from gbpt.render import LIGHT_UNIFORM, BSDF_PRINCIPLED, RenderSettings, look_at_
 import pyoracle  # noqa: E402
 
 OUT = os.path.join(HERE, "pt_principled_cornell.npz")
+OUT_RIS = os.path.join(HERE, "pt_principled_ris_cornell.npz")
 
 MATERIALS = [
     dict(base_color=(0.73, 0.73, 0.73), roughness=0.5, coat=0.5, coat_roughness=0.1),          # 0 white walls
@@ -66,6 +67,13 @@ def main():
                         settings=np.array([st.width, st.height, st.samples_per_launch, st.nb_bounces,
                                            st.russian_roulette_min_depth, st.seed], np.int32), image=img)
     print(f"wrote {OUT}: mean {img.mean() / st.samples_per_launch:.4f}, nonzero {np.mean(img.sum(-1) > 0):.3f}")
+    # the same scene with RIS direct lighting (4 light + 1 BSDF candidates), the reference's
+    # default strategy
+    st.direct_lighting, st.ris_light_candidates, st.ris_bsdf_candidates = 1, 4, 1
+    ris = pyoracle.pt_render_principled(mesh.triangle_soup(), mat_of, eff, emission, emissive, None, None, 0.0, st,
+                                        st.samples_per_launch)
+    np.savez_compressed(OUT_RIS, image=ris, ris=np.array([4, 1], np.int32))
+    print(f"wrote {OUT_RIS}: mean {ris.mean() / st.samples_per_launch:.4f}")
 
 
 if __name__ == "__main__":
