@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "render_common.h"
+#include "envmap.h"
 #include "guide_device.h"
 #include "principled.h"
 #include "render_device.h"
@@ -125,6 +126,119 @@ __global__ void __launch_bounds__(128) trace_queue_kernel(const uint4* __restric
 }
 
 // ---------------------------------------------------------------------------------------------
+// envmap direct lighting (sample_environment_map, src/Device/includes/LightSampling/Envmap.h:251-285)
+// of every vertex of the shaded queue, run before shade so that its random numbers come first at a
+// vertex: an envmap sample and a separate BSDF sample, each with an any-hit ray to 1e35 in envq,
+// resolved with the vertex's other samples. Its own kernel keeps the shade kernels' registers as
+// they are when no envmap is sampled. The ReSTIR DI bounce keeps it too: its reservoirs hold
+// emissive triangles only.
+// ---------------------------------------------------------------------------------------------
+template <bool PRINCIPLED>
+__global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0, PathBuffers pb, Queue in, Queue envq,
+                                                  unsigned long long* stats, const BatchJob* __restrict__ jobs)
+{
+    const int n = *in.count;
+    const int n_round = (n + 31) & ~31;  // whole warps for the warp-aggregated appends
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += gridDim.x * blockDim.x)
+    {
+        const bool valid = i < n;
+        int slot = 0, prim = -1;
+        float4 hit = make_float4(0, 0, 0, 0);
+        if (valid)
+        {
+            slot = in.slot[i];
+            hit = in.hits[i];
+            prim = __float_as_int(hit.w);
+            pb.env_entry[slot] = -1;
+            pb.envb_entry[slot] = -1;
+        }
+        const BatchJob* J = (jobs && valid) ? jobs + pb.job[slot] : nullptr;
+        const SceneView s = J ? J->s : s0;
+        const RenderConst rc = J ? J->rc : rc0;
+        EnvDirect ed;
+        V3 P = v3(0.0f);
+        if (valid && prim >= 0 && env_sampled(s.env))
+        {
+            Pcg32 rng;
+            rng.inc = pcg_inc(rc.seed);
+            rng.state = pb.rng[slot];
+            const V3 d = xyz(in.dir_tmax[i]);
+            P = xyz(in.origin_tmin[i]) + hit.x * d;
+            V3 a, b, c;
+            load_triangle(s, prim, a, b, c);
+            const V3 ng_raw = normalize(cross(b - a, c - a));
+            V3 ng = ng_raw;
+            V3 ns = ng;
+            const V3 view = -d;
+            fix_backfacing(view, ng, ns);
+            const int mat = __ldg(s.material_of + prim);
+            const V3 tp = xyz(pb.throughput[slot]);
+            if constexpr (!PRINCIPLED)
+            {
+                const V3 albedo = xyz(s.materials[mat].base_color);
+                ed = env_direct(
+                    s.env, rng, ns, tp, true, [&](V3 wi, float& pdf) { return lambert_eval(albedo, dot(ns, wi), pdf); },
+                    [&](V3& wi, float& pdf) {
+                        const float r1 = rng.next(), r2 = rng.next();
+                        wi = cosine_sample(ns, r1, r2);
+                        return lambert_eval(albedo, dot(ns, wi), pdf);
+                    });
+            }
+            else
+            {
+                const bsdf::Material m = bsdf::load_material(s.pmats[mat]);
+                const bool hc = rc.ggx_height_correlated != 0;
+                // the vertex's volume state, as shade derives it
+                const int cur_medium = pb.medium[slot];
+                const bool transmissive = (m.transmission > 0.0f || m.diffuse_transmission > 0.0f) && !m.thin_walled;
+                bsdf::Medium md;
+                md.inside = transmissive && dot(view, ng_raw) < 0.0f;
+                md.eta_incident = md.inside ? m.ior : (cur_medium >= 0 ? s.pmats[cur_medium].ior : 1.0f);
+                md.eta_outgoing = md.inside ? 1.0f : m.ior;
+                ed = env_direct(
+                    s.env, rng, ns, tp, can_light_sample(m),
+                    [&](V3 wi, float& pdf) {
+                        bsdf::Query q;
+                        q.view = view;
+                        q.ns = ns;
+                        q.ng = ng;
+                        q.light = wi;
+                        return bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, pdf);
+                    },
+                    [&](V3& wi, float& pdf) {
+                        bsdf::Xorshift32 xr = bsdf_rng(rng);
+                        int lobe;
+                        return bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                    });
+            }
+            store_rng(pb.rng + slot, rng);
+        }
+        const int ei = warp_append(envq.count, ed.want_l);
+        if (ed.want_l)
+        {
+            envq.origin_tmin[ei] = f4(P, 0.0f);
+            envq.dir_tmax[ei] = f4(ed.dir_l, 1.0e35f);
+            envq.last_prim[ei] = prim;
+            envq.slot[ei] = slot;
+            pb.env_entry[slot] = ei;
+            pb.pending_env[slot] = f4(ed.c_l, 0.0f);
+        }
+        const int bi = warp_append(envq.count, ed.want_b);
+        if (ed.want_b)
+        {
+            envq.origin_tmin[bi] = f4(P, 0.0f);
+            envq.dir_tmax[bi] = f4(ed.dir_b, 1.0e35f);
+            envq.last_prim[bi] = prim;
+            envq.slot[bi] = slot;
+            pb.envb_entry[slot] = bi;
+            pb.pending_envb[slot] = f4(ed.c_b, 0.0f);
+        }
+        warp_count(stats + 1, ed.want_l);
+        warp_count(stats + 1, ed.want_b);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
 // shade: one path vertex per active path. PRINCIPLED selects the layered principled BSDF with
 // volume tracking (a path refracting into a non-thin transmissive material is inside it until it
 // refracts out), else the Lambertian BSDF override.
@@ -162,6 +276,16 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
         const SceneView s = J ? J->s : s0;
         const RenderConst rc = J ? J->rc : rc0;
         const bool alive = valid && prim >= 0;
+        // a ray that left the scene: the world's radiance (path_tracing_miss_gather_envmap)
+        if (valid && prim < 0 && s.env.ambient != GBPT_AMBIENT_NONE)
+        {
+            const V3 c = env_miss(s.env, xyz(in.dir_tmax[i]), bounce, xyz(pb.throughput[slot]));
+            if (!is_black(c))
+            {
+                const float4 r = pb.radiance[slot];
+                pb.radiance[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
+            }
+        }
 
         bool want_shadow = false, want_bsdf = false, want_next = false, want_record = false;
         bool guided_vertex = false, rec_vertex = false;
@@ -681,7 +805,8 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
 // resolve: add the light-sample and BSDF-sample contributions of this bounce, in a fixed order
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst rc0, PathBuffers pb, Queue in, Queue shadow,
-                                                      Queue bsdfq, GuideView gv, const BatchJob* __restrict__ jobs)
+                                                      Queue bsdfq, Queue envq, GuideView gv,
+                                                      const BatchJob* __restrict__ jobs)
 {
     const int n = *in.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -692,6 +817,11 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst 
         const RenderConst rc = J ? J->rc : rc0;
         const int se = pb.shadow_entry[slot];
         const int be = pb.bsdf_entry[slot];
+        // envmap direct lighting of this vertex: the envmap sample, then the BSDF sample
+        const int ee = pb.env_entry ? pb.env_entry[slot] : -1;
+        const int eb = pb.env_entry ? pb.envb_entry[slot] : -1;
+        const bool env_l = ee >= 0 && !envq.occluded[ee];
+        const bool env_b = eb >= 0 && !envq.occluded[eb];
         // a guiding record of this vertex snapshots the radiance after its direct lighting; its
         // light-sample record loses its weight when the shadow ray is occluded
         const int te = gv.train_entry ? gv.train_entry[slot] : -1;
@@ -755,22 +885,28 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst 
                     add = xyz(ra) * c_b * (wsum / t_b);
                 else if (light_ok && pl.w > 0.0f)
                     add = xyz(pl) * (wsum / pl.w);
-                const float4 r = pb.radiance[slot];
-                pb.radiance[slot] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
+                V3 rad = xyz(pb.radiance[slot]);
+                if (env_l) rad = rad + xyz(pb.pending_env[slot]);
+                if (env_b) rad = rad + xyz(pb.pending_envb[slot]);
+                rad = rad + add;
+                pb.radiance[slot] = f4(rad, 0.0f);
                 continue;
             }
         }
-        if (se < 0 && be < 0)
+        if (se < 0 && be < 0 && !env_l && !env_b)
         {
             if (te >= 0) gv.rec_snap[te] = pb.radiance[slot];
             continue;
         }
-        V3 add = v3(0, 0, 0);
-        if (se >= 0 && !shadow.occluded[se]) add = add + xyz(pb.pending_light[slot]);
-        const float4 r = pb.radiance[slot];
-        // a guiding record's snapshot: after the light sample, before the BSDF-technique emission
-        // (which arrives along the recorded direction and belongs to its training target)
-        if (te >= 0) gv.rec_snap[te] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
+        // added one by one: the light sample, the envmap's two samples, the BSDF sample
+        V3 rad = xyz(pb.radiance[slot]);
+        if (se >= 0 && !shadow.occluded[se]) rad = rad + xyz(pb.pending_light[slot]);
+        if (env_l) rad = rad + xyz(pb.pending_env[slot]);
+        if (env_b) rad = rad + xyz(pb.pending_envb[slot]);
+        // a guiding record's snapshot: after the vertex's light and envmap samples, before the
+        // BSDF-technique emission (which arrives along the recorded direction and belongs to its
+        // training target)
+        if (te >= 0) gv.rec_snap[te] = f4(rad, 0.0f);
         if (be >= 0)
         {
             const float4 h = bsdfq.hits[be];
@@ -798,12 +934,12 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst 
                         const float light_pdf = area_to_solid_angle_pdf(pdf_area, h.x, cos_l);
                         const float4 pend = pb.pending_bsdf[slot];
                         const float mis = balance_heuristic(pend.w, light_pdf);
-                        add = add + xyz(pend) * Le * mis;
+                        rad = rad + xyz(pend) * Le * mis;
                     }
                 }
             }
         }
-        pb.radiance[slot] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, 0.0f);
+        pb.radiance[slot] = f4(rad, 0.0f);
     }
 }
 
@@ -1180,18 +1316,30 @@ cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next
 }
 
 cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
-                         const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
-                         unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv, int n_sm,
-                         cudaStream_t st, const BatchJob* jobs)
+                         const Queue& next, const Queue& shadow, const Queue& bsdfq, const Queue& envq, int bounce,
+                         int64_t capacity, unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv,
+                         int n_sm, cudaStream_t st, const BatchJob* jobs)
 {
     const int tgrid = grid_for(capacity, 128, n_sm * 16);
-    if (rc.bsdf == GBPT_BSDF_PRINCIPLED)
+    const bool principled = rc.bsdf == GBPT_BSDF_PRINCIPLED;
+    if (pb.env_entry)
+    {
+        reset_counts_kernel<<<1, 1, 0, st>>>(envq.count, nullptr, nullptr);
+        if (principled)
+            env_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, envq, stats, jobs);
+        else
+            env_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, envq, stats, jobs);
+    }
+    if (principled)
         shade_kernel<true><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv, jobs);
     else
         shade_kernel<false><<<tgrid, 128, 0, st>>>(s, rc, pb, in, next, shadow, bsdfq, bounce, stats, restir, gv, jobs);
     trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, shadow, jobs, pb.job);
     trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, bsdfq, jobs, pb.job);
-    resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq, gv, jobs);
+    if (pb.env_entry)
+        trace_queue_kernel<true><<<grid_for(2 * capacity, 128, n_sm * 16), 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, envq,
+                                                                                         jobs, pb.job);
+    resolve_kernel<<<tgrid, 128, 0, st>>>(s, rc, pb, in, shadow, bsdfq, envq, gv, jobs);
     return cudaGetLastError();
 }
 

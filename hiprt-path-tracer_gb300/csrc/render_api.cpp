@@ -67,6 +67,12 @@ struct gbpt_scene
     gbpt::SceneView view;
     int32_t n_emissive = 0;
     double power_sum64 = 0.0;
+    // the world: ambient light and envmap tables (view.env points into env_mem)
+    DevMem env_mem;
+    float* env_cdf = nullptr;
+    uint2* env_alias = nullptr;
+    double env_sum64 = 0.0;
+    mutable int batch_refs = 0;  // batches holding a copy of 'view' (the world cannot change under them)
 };
 
 struct gbpt_renderer
@@ -100,6 +106,11 @@ struct gbpt_renderer
     DevMem guide_mem;
     gbpt::GuideView gv;  // gv.lobes == nullptr: off
     float* guide_lobes = nullptr;
+    // envmap direct lighting: per-path entries and the any-hit queue (allocated once the scene's
+    // envmap is importance sampled)
+    DevMem env_mem;
+    gbpt::Queue envq;
+    bool env_ready = false;
 };
 
 namespace {
@@ -343,6 +354,7 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
 gbpt_status gbpt_scene_destroy(gbpt_scene* s)
 {
     if (!s) return GBPT_OK;
+    s->env_mem.release();
     s->mem.release();
     gbpt_status st = gbpt_bvh_destroy(s->bvh);
     delete s;
@@ -369,6 +381,201 @@ gbpt_status gbpt_scene_get_light_table(const gbpt_scene* s, int32_t* n_emissive,
     if (e == cudaSuccess && n > 0 && probas) e = cudaMemcpy(probas, s->view.alias_prob, n * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && n > 0 && alias) e = cudaMemcpy(alias, s->view.alias_index, n * sizeof(int32_t), cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "light table read-back");
+}
+
+namespace {
+
+bool scene_env_sampled(const gbpt_scene* s)
+{
+    const gbpt::EnvView& e = s->view.env;
+    return e.ambient == GBPT_AMBIENT_ENVMAP && e.sampling != GBPT_ENVMAP_NO_SAMPLING && e.intensity > 0.0f;
+}
+
+bool finite_nonneg(float x) { return std::isfinite(x) && x >= 0.0f; }
+
+// Vose's alias method over q (texel luminances scaled to mean 1) with FIFO small/large queues
+// filled in index order: the partition of Utils::compute_alias_table (src/Utils/Utils.cpp:63-131).
+// Runs on the host: it is one sequential O(n) pass, and on one GPU thread each of its steps would
+// wait on a dependent memory access. Output: (probability as float bits, alias index) per texel.
+void vose_host(std::vector<double>& q, std::vector<uint2>& out)
+{
+    const size_t n = q.size();
+    std::vector<float> prob(n, 0.0f);
+    std::vector<int32_t> alias(n), smalls, larges;
+    smalls.reserve(n);
+    larges.reserve(n);
+    for (size_t i = 0; i < n; i++)
+    {
+        alias[i] = (int32_t)i;
+        (q[i] < 1.0 ? smalls : larges).push_back((int32_t)i);
+    }
+    size_t sh = 0, lh = 0;
+    while (sh < smalls.size() && lh < larges.size())
+    {
+        const int32_t si = smalls[sh++], li = larges[lh++];
+        prob[si] = (float)q[si];
+        alias[si] = li;
+        q[li] = (q[li] + q[si]) - 1.0;
+        if (q[li] > 1.0)
+            larges.push_back(li);
+        else
+            smalls.push_back(li);
+    }
+    while (lh < larges.size()) prob[larges[lh++]] = 1.0f;
+    while (sh < smalls.size()) prob[smalls[sh++]] = 1.0f;
+    out.resize(n);
+    for (size_t i = 0; i < n; i++)
+    {
+        uint32_t bits;
+        std::memcpy(&bits, &prob[i], sizeof(bits));
+        out[i] = make_uint2(bits, (uint32_t)alias[i]);
+    }
+}
+
+}  // namespace
+
+gbpt_status gbpt_world_default(gbpt_world_desc* w)
+{
+    if (!w) return set_error(GBPT_ERROR_INVALID_ARG, "world is NULL");
+    std::memset(w, 0, sizeof(*w));
+    w->ambient = GBPT_AMBIENT_NONE;
+    w->envmap_intensity = 1.0f;
+    for (int k = 0; k < 3; k++) w->envmap_to_world[4 * k] = w->world_to_envmap[4 * k] = 1.0f;
+    w->envmap_sampling = GBPT_ENVMAP_ALIAS_TABLE;
+    w->envmap_bsdf_mis = 1;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_set_world(gbpt_scene* s, const gbpt_world_desc* w, void* stream)
+{
+    if (!s || !w) return set_error(GBPT_ERROR_INVALID_ARG, "NULL argument");
+    if (s->batch_refs > 0) return set_error(GBPT_ERROR_INVALID_ARG, "a batch renders this scene: destroy it before changing the world");
+    if (w->ambient < GBPT_AMBIENT_NONE || w->ambient > GBPT_AMBIENT_ENVMAP)
+        return set_error(GBPT_ERROR_INVALID_ARG, "unknown ambient light type");
+    for (int k = 0; k < 3; k++)
+        if (!finite_nonneg(w->uniform_color[k])) return set_error(GBPT_ERROR_INVALID_ARG, "uniform_color must be finite and >= 0");
+    gbpt::EnvView v;
+    std::memset(&v, 0, sizeof(v));
+    v.ambient = w->ambient;
+    for (int k = 0; k < 3; k++) v.uniform[k] = w->uniform_color[k];
+    DevMem fresh;
+    double sum64 = 0.0;
+    float* cdf = nullptr;
+    uint2* alias = nullptr;
+    if (w->ambient == GBPT_AMBIENT_ENVMAP)
+    {
+        const int64_t W = w->envmap_width, H = w->envmap_height, n = W * H;
+        if (!w->envmap_rgb || W < 1 || H < 1 || W > 65536 || H > 65536 || n > ((int64_t)1 << 28))
+            return set_error(GBPT_ERROR_INVALID_ARG, "envmap needs texels and 1 <= width, height <= 65536 with at most 2^28 texels");
+        if (!finite_nonneg(w->envmap_intensity)) return set_error(GBPT_ERROR_INVALID_ARG, "envmap_intensity must be finite and >= 0");
+        if (w->envmap_sampling < GBPT_ENVMAP_NO_SAMPLING || w->envmap_sampling > GBPT_ENVMAP_ALIAS_TABLE)
+            return set_error(GBPT_ERROR_INVALID_ARG, "unknown envmap_sampling");
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+            {
+                double acc = 0.0;
+                for (int k = 0; k < 3; k++) acc += (double)w->envmap_to_world[3 * i + k] * w->world_to_envmap[3 * k + j];
+                if (!std::isfinite(acc) || std::fabs(acc - (i == j ? 1.0 : 0.0)) > 1.0e-3)
+                    return set_error(GBPT_ERROR_INVALID_ARG, "world_to_envmap is not the inverse of envmap_to_world");
+            }
+        for (int64_t i = 0; i < 3 * n; i++)
+            if (!finite_nonneg(w->envmap_rgb[i]))
+                return set_error(GBPT_ERROR_INVALID_ARG, "envmap texel " + std::to_string(i / 3) + " is not finite and >= 0");
+        cudaStream_t cs = (cudaStream_t)stream;
+        const int n_tiles = gbpt::envmap_scan_tiles(n);
+        DevMem tmp;
+        float* drgb = tmp.alloc<float>(3 * n);
+        float* dlum = tmp.alloc<float>(n);
+        double* dtile = tmp.alloc<double>(2 * (size_t)n_tiles + 1);
+        uint32_t* texels = fresh.alloc<uint32_t>(n);
+        cdf = fresh.alloc<float>(n);
+        alias = fresh.alloc<uint2>(n);
+        cudaError_t e = tmp.err != cudaSuccess ? tmp.err : fresh.err;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(drgb, w->envmap_rgb, 3 * n * sizeof(float), cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess)
+            e = gbpt::launch_envmap_tables(drgb, n, texels, dlum, cdf, dtile, dtile + n_tiles, dtile + 2 * n_tiles, cs);
+        std::vector<float> lum(n);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(lum.data(), dlum, n * sizeof(float), cudaMemcpyDeviceToHost, cs);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&sum64, dtile + 2 * n_tiles, sizeof(double), cudaMemcpyDeviceToHost, cs);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+        std::vector<uint2> table;
+        if (e == cudaSuccess)
+        {
+            if (sum64 > 0.0)
+            {
+                // alias table of the luminances normalised by the FP64 sum
+                std::vector<double> q(n);
+                for (int64_t i = 0; i < n; i++) q[i] = (double)lum[i] / sum64 * (double)n;
+                vose_host(q, table);
+            }
+            else
+                table.assign(n, make_uint2(0x3F800000u, 0u));  // black envmap: nothing to sample
+            e = cudaMemcpyAsync(alias, table.data(), n * sizeof(uint2), cudaMemcpyHostToDevice, cs);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+        tmp.release();
+        if (e != cudaSuccess)
+        {
+            fresh.release();
+            return cuda_error(e, "envmap tables");
+        }
+        v.texels = texels;
+        v.cdf = cdf;
+        v.alias = alias;
+        v.width = (int32_t)W;
+        v.height = (int32_t)H;
+        v.intensity = w->envmap_intensity;
+        v.total_sum = (float)sum64;
+        std::memcpy(v.to_world, w->envmap_to_world, sizeof(v.to_world));
+        std::memcpy(v.to_env, w->world_to_envmap, sizeof(v.to_env));
+        // a black envmap is never sampled (its pdfs would divide by a zero sum)
+        v.sampling = sum64 > 0.0 ? w->envmap_sampling : GBPT_ENVMAP_NO_SAMPLING;
+        v.bsdf_mis = w->envmap_bsdf_mis ? 1 : 0;
+        v.bilinear = w->envmap_bilinear ? 1 : 0;
+        v.scale_background = w->envmap_scale_background ? 1 : 0;
+    }
+    if (!s->env_mem.ptrs.empty())
+    {
+        // renderers on other streams may still read the old tables
+        const cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess)
+        {
+            fresh.release();
+            return cuda_error(e, "world change");
+        }
+    }
+    s->env_mem.release();
+    s->env_mem = fresh;
+    s->env_cdf = cdf;
+    s->env_alias = alias;
+    s->env_sum64 = sum64;
+    s->view.env = v;
+    return GBPT_OK;
+}
+
+gbpt_status gbpt_scene_get_envmap_tables(const gbpt_scene* s, uint32_t* texels, float* cdf, float* probas,
+                                         int32_t* alias, float* total_sum, double* total_sum64)
+{
+    if (!s) return set_error(GBPT_ERROR_INVALID_ARG, "scene is NULL");
+    const gbpt::EnvView& v = s->view.env;
+    if (v.ambient != GBPT_AMBIENT_ENVMAP) return set_error(GBPT_ERROR_INVALID_ARG, "the scene's world has no envmap");
+    const int64_t n = (int64_t)v.width * v.height;
+    if (total_sum) *total_sum = v.total_sum;
+    if (total_sum64) *total_sum64 = s->env_sum64;
+    cudaError_t e = cudaSuccess;
+    if (texels) e = cudaMemcpy(texels, v.texels, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && cdf) e = cudaMemcpy(cdf, v.cdf, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && (probas || alias))
+    {
+        std::vector<uint2> t(n);
+        e = cudaMemcpy(t.data(), v.alias, n * sizeof(uint2), cudaMemcpyDeviceToHost);
+        for (int64_t i = 0; e == cudaSuccess && i < n; i++)
+        {
+            if (probas) std::memcpy(probas + i, &t[i].x, sizeof(float));
+            if (alias) alias[i] = (int32_t)t[i].y;
+        }
+    }
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "envmap table read-back");
 }
 
 namespace {
@@ -439,6 +646,38 @@ void alloc_paths(DevMem& M, int64_t cap, bool principled, bool batched, gbpt::Pa
     bsdfq = make_queue(M, cap, true, false);
 }
 
+// Envmap direct lighting of a wavefront of 'cap' paths: per-path entries and contributions, and
+// the any-hit queue of the envmap-sample and BSDF-sample rays (two per path)
+void alloc_env(DevMem& M, int64_t cap, gbpt::PathBuffers& pb, gbpt::Queue& envq)
+{
+    pb.env_entry = M.alloc<int32_t>(cap);
+    pb.envb_entry = M.alloc<int32_t>(cap);
+    pb.pending_env = M.alloc<float4>(cap);
+    pb.pending_envb = M.alloc<float4>(cap);
+    envq = make_queue(M, 2 * cap, false, true);
+}
+
+// Allocates a renderer's envmap buffers the first time its scene's envmap is importance sampled
+gbpt_status ensure_env(gbpt_renderer* r, cudaStream_t cs)
+{
+    if (r->env_ready || !scene_env_sampled(r->scene)) return GBPT_OK;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(cs, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone)
+        return set_error(GBPT_ERROR_INVALID_ARG,
+                         "the scene's envmap is sampled but this renderer has not shaded since: run one launch outside the stream capture first");
+    alloc_env(r->env_mem, r->capacity, r->pb, r->envq);
+    if (r->env_mem.err != cudaSuccess)
+    {
+        const cudaError_t e = r->env_mem.err;
+        r->env_mem.release();
+        r->pb.env_entry = r->pb.envb_entry = nullptr;
+        r->pb.pending_env = r->pb.pending_envb = nullptr;
+        return cuda_error(e, "envmap buffers");
+    }
+    r->env_ready = true;
+    return GBPT_OK;
+}
+
 }  // namespace
 
 gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_settings* st, gbpt_renderer** out)
@@ -482,6 +721,7 @@ gbpt_status gbpt_renderer_destroy(gbpt_renderer* r)
     if (!r) return GBPT_OK;
     r->restir_mem.release();
     r->guide_mem.release();
+    r->env_mem.release();
     r->mem.release();
     delete r;
     return GBPT_OK;
@@ -553,8 +793,12 @@ gbpt_status gbpt_pass_shade(gbpt_renderer* r, int32_t bounce, void* stream)
         gbpt_status st = gbpt::guide::render_infer(r->guide, b, r->guide_lobes, cs);
         if (st != GBPT_OK) return st;
     }
-    cudaError_t e = gbpt::launch_shade(r->scene->view, r->rc, r->pb, in, r->q[r->cur ^ 1], r->shadow, r->bsdfq, bounce,
-                                       r->capacity, r->stats, restir, gv, r->n_sm, cs);
+    gbpt_status env_st = ensure_env(r, cs);
+    if (env_st != GBPT_OK) return env_st;
+    gbpt::PathBuffers pb = r->pb;
+    if (!scene_env_sampled(r->scene)) pb.env_entry = nullptr;  // envmap direct lighting off
+    cudaError_t e = gbpt::launch_shade(r->scene->view, r->rc, pb, in, r->q[r->cur ^ 1], r->shadow, r->bsdfq, r->envq,
+                                       bounce, r->capacity, r->stats, restir, gv, r->n_sm, cs);
     r->cur ^= 1;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "shade");
 }
@@ -1026,7 +1270,7 @@ struct gbpt_batch
     DevMem mem;
     gbpt::BatchJob* jobs = nullptr;
     gbpt::PathBuffers pb;
-    gbpt::Queue q[2], shadow, bsdfq;
+    gbpt::Queue q[2], shadow, bsdfq, envq;
     int64_t capacity = 0, max_job_paths = 0, max_job_pixels = 0, total_pixels = 0;
     int max_bounces = 0, max_iterations = 0, n_sm = 1;
     float* acc32 = nullptr;
@@ -1056,8 +1300,8 @@ cudaError_t batch_iteration(gbpt_batch* b, cudaStream_t st)
         const gbpt::Queue& next = b->q[(bounce & 1) ^ 1];
         e = gbpt::launch_extend(j0.s, in, next, b->shadow, b->bsdfq, b->capacity, b->n_sm, st, b->jobs, b->pb.job);
         if (e == cudaSuccess)
-            e = gbpt::launch_shade(j0.s, j0.rc, b->pb, in, next, b->shadow, b->bsdfq, bounce, b->capacity, b->stats + 1,
-                                   none, no_guide, b->n_sm, st, b->jobs);
+            e = gbpt::launch_shade(j0.s, j0.rc, b->pb, in, next, b->shadow, b->bsdfq, b->envq, bounce, b->capacity,
+                                   b->stats + 1, none, no_guide, b->n_sm, st, b->jobs);
     }
     if (e == cudaSuccess)
         e = gbpt::launch_batch_accumulate(b->jobs, (int)b->host_jobs.size(), b->max_job_pixels, b->pb, b->iteration,
@@ -1132,6 +1376,9 @@ gbpt_status gbpt_batch_create(const gbpt_batch_job* jobs, int32_t n_jobs, const 
     }
     DevMem& M = b->mem;
     alloc_paths(M, b->capacity, jobs[0].settings.bsdf == GBPT_BSDF_PRINCIPLED, true, b->pb, b->q, b->shadow, b->bsdfq);
+    bool any_env = false;
+    for (const gbpt_scene* sc : b->scenes) any_env = any_env || scene_env_sampled(sc);
+    if (any_env) alloc_env(M, b->capacity, b->pb, b->envq);
     b->jobs = M.alloc<gbpt::BatchJob>(n_jobs);
     b->acc32 = M.alloc<float>(3 * b->total_pixels);
     b->acc64 = M.alloc<double>(3 * b->total_pixels);
@@ -1160,6 +1407,7 @@ gbpt_status gbpt_batch_create(const gbpt_batch_job* jobs, int32_t n_jobs, const 
         delete b;
         return e == cudaErrorMemoryAllocation ? set_error(GBPT_ERROR_OOM, "batch buffers") : cuda_error(e, "batch create");
     }
+    for (const gbpt_scene* sc : b->scenes) sc->batch_refs++;
     *out = b;
     return GBPT_OK;
 }
@@ -1168,6 +1416,7 @@ gbpt_status gbpt_batch_destroy(gbpt_batch* b)
 {
     if (!b) return GBPT_OK;
     batch_release(b);
+    for (const gbpt_scene* sc : b->scenes) sc->batch_refs--;
     delete b;
     return GBPT_OK;
 }

@@ -29,6 +29,27 @@ struct DeviceMaterial
     float4 emission;    // rgb = emission colour * strength, w unused
 };
 
+// The world around the scene (WorldSettings, src/HostDeviceCommon/WorldSettings.h:14-53): nothing,
+// a uniform colour, or an equirectangular Y-up environment map. Texel (x, y) covers u in
+// [x/W, (x+1)/W), v in [y/H, (y+1)/H); v = 0 is the -y pole. Device pointers.
+struct EnvView
+{
+    const uint32_t* texels;  // RGB9E5 shared-exponent texels (RGBE9995Packed), W*H
+    const float* cdf;        // running luminance sum over texels in row-major order (binary search)
+    const uint2* alias;      // per texel: (probability as float bits, alias index) (alias table)
+    int32_t width, height;
+    float intensity;         // envmap_intensity
+    float total_sum;         // luminance sum of the unscaled texels (envmap_total_sum)
+    float to_world[9];       // row-major rotation, world direction = to_world * envmap direction
+    float to_env[9];         // its inverse
+    float uniform[3];        // uniform_light_color
+    int32_t ambient;         // GBPT_AMBIENT_*
+    int32_t sampling;        // GBPT_ENVMAP_* (EnvmapSamplingStrategy)
+    int32_t bsdf_mis;        // EnvmapSamplingDoBSDFMIS
+    int32_t bilinear;        // EnvmapSamplingDoBilinearFiltering
+    int32_t scale_background;  // envmap_scale_background_intensity
+};
+
 struct SceneView
 {
     const float4* vertices;       // xyz per vertex
@@ -43,6 +64,7 @@ struct SceneView
     const uint4* bvh_nodes;
     const float4* bvh_tris;
     const gbpt_principled_material* pmats;  // effective principled materials (NULL: Lambertian scene)
+    EnvView env;
 };
 
 struct Queue
@@ -70,6 +92,13 @@ struct PathBuffers
     float4* ris;            // RIS vertex: throughput before the continuation (rgb) and the light
                             // candidates' weight sum (w); w = -0.5: RIS without light candidates,
                             // w = -1: not a RIS vertex
+    // environment-map direct lighting (null when the scene's envmap is not importance sampled):
+    // the envmap sample's and the separate BSDF sample's contributions, each waiting on its
+    // any-hit ray in the envmap queue
+    int32_t* env_entry;     // queue index of the envmap-sample ray this bounce, -1 if none
+    int32_t* envb_entry;    // queue index of the BSDF-sample ray this bounce, -1 if none
+    float4* pending_env;
+    float4* pending_envb;
 };
 
 // Learned path guiding in the wavefront (all device pointers; lobes == nullptr: guiding off).

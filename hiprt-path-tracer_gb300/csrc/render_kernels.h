@@ -62,11 +62,18 @@ cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next
                           const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st,
                           const BatchJob* jobs = nullptr, const int32_t* job_of_slot = nullptr);
 // 'gv' (null lobes when guiding is off) holds the learned mixture per entry of 'in' and the
-// training-record buffers.
+// training-record buffers. 'envq' (any-hit, 2 entries per path) takes the envmap direct-lighting
+// rays when pb.env_entry is set (the scene's envmap is importance sampled).
 cudaError_t launch_shade(const SceneView& s, const RenderConst& rc, const PathBuffers& pb, const Queue& in,
-                         const Queue& next, const Queue& shadow, const Queue& bsdfq, int bounce, int64_t capacity,
-                         unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv, int n_sm,
-                         cudaStream_t st, const BatchJob* jobs = nullptr);
+                         const Queue& next, const Queue& shadow, const Queue& bsdfq, const Queue& envq, int bounce,
+                         int64_t capacity, unsigned long long* stats, const ReservoirBuf& restir, const GuideView& gv,
+                         int n_sm, cudaStream_t st, const BatchJob* jobs = nullptr);
+// Envmap tables: RGB9E5 texels and float luminance of n RGB float texels, the FP64 running sum
+// over texels rounded to float (cdf) and the FP64 total (*sum64). tile_total / tile_offset hold
+// envmap_scan_tiles(n) doubles each.
+int envmap_scan_tiles(int64_t n);
+cudaError_t launch_envmap_tables(const float* rgb, int64_t n, uint32_t* texels, float* lum, float* cdf,
+                                 double* tile_total, double* tile_offset, double* sum64, cudaStream_t st);
 // Guiding network inputs for each entry of 'in' (after its closest hits are known)
 cudaError_t launch_guide_inputs(const SceneView& s, const Queue& in, const GuideView& gv, int64_t capacity, int n_sm,
                                 cudaStream_t st);

@@ -61,12 +61,27 @@ class RestirDISettingsC(ctypes.Structure):
 
 RESERVOIRS_INITIAL, RESERVOIRS_TEMPORAL, RESERVOIRS_FINAL, RESERVOIRS_PREVIOUS = 0, 1, 2, 3
 
+AMBIENT_NONE, AMBIENT_UNIFORM, AMBIENT_ENVMAP = 0, 1, 2
+ENVMAP_NO_SAMPLING, ENVMAP_BINARY_SEARCH, ENVMAP_ALIAS_TABLE = 0, 1, 2
+
+
+class WorldDescC(ctypes.Structure):
+    _fields_ = [("ambient", i32), ("uniform_color", ctypes.c_float * 3), ("envmap_rgb", c_vp),
+                ("envmap_width", i32), ("envmap_height", i32), ("envmap_intensity", ctypes.c_float),
+                ("envmap_scale_background", i32), ("envmap_to_world", ctypes.c_float * 9),
+                ("world_to_envmap", ctypes.c_float * 9), ("envmap_sampling", i32), ("envmap_bsdf_mis", i32),
+                ("envmap_bilinear", i32)]
+
+
 RENDER_SIGNATURES = [
     ("gbpt_scene_create", ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(_lib.BvhParams),
                                          ctypes.POINTER(c_vp), c_vp]),
     ("gbpt_scene_destroy", ctypes.c_int, [c_vp]),
     ("gbpt_scene_get_bvh", ctypes.c_int, [c_vp, ctypes.POINTER(c_vp)]),
     ("gbpt_scene_get_light_table", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    ("gbpt_world_default", ctypes.c_int, [ctypes.POINTER(WorldDescC)]),
+    ("gbpt_scene_set_world", ctypes.c_int, [c_vp, ctypes.POINTER(WorldDescC), c_vp]),
+    ("gbpt_scene_get_envmap_tables", ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     ("gbpt_renderer_create", ctypes.c_int, [c_vp, ctypes.POINTER(RenderSettingsC), ctypes.POINTER(c_vp)]),
     ("gbpt_renderer_destroy", ctypes.c_int, [c_vp]),
     ("gbpt_renderer_reset", ctypes.c_int, [c_vp, c_vp]),
@@ -211,6 +226,44 @@ def _load():
     return lib
 
 
+class World:
+    """The world around a scene (the reference's WorldSettings): ambient AMBIENT_NONE, AMBIENT_UNIFORM
+    (uniform_color seen by every miss) or AMBIENT_ENVMAP (envmap: (H, W, 3) float texels, row 0 at
+    the -y pole; rotation: 3x3 envmap-to-world matrix)."""
+
+    def __init__(self, ambient=AMBIENT_NONE, uniform_color=(0.0, 0.0, 0.0), envmap=None, intensity=1.0,
+                 scale_background=False, rotation=None, sampling=ENVMAP_ALIAS_TABLE, bsdf_mis=True, bilinear=False):
+        self.ambient = int(ambient)
+        self.uniform_color = tuple(float(c) for c in uniform_color)
+        self.envmap = None if envmap is None else np.ascontiguousarray(envmap, np.float32)
+        if self.envmap is not None and (self.envmap.ndim != 3 or self.envmap.shape[2] != 3):
+            raise ValueError("envmap must be (H, W, 3)")
+        self.intensity = float(intensity)
+        self.scale_background = bool(scale_background)
+        self.rotation = np.eye(3, dtype=np.float32) if rotation is None else np.asarray(rotation, np.float32).reshape(3, 3)
+        self.inverse_rotation = np.linalg.inv(self.rotation.astype(np.float64)).astype(np.float32)
+        self.sampling = int(sampling)
+        self.bsdf_mis = bool(bsdf_mis)
+        self.bilinear = bool(bilinear)
+
+    def to_c(self) -> WorldDescC:
+        w = WorldDescC()
+        _lib.check(_load().gbpt_world_default(ctypes.byref(w)))
+        w.ambient = self.ambient
+        w.uniform_color[:] = list(self.uniform_color)
+        if self.envmap is not None:
+            w.envmap_rgb = self.envmap.ctypes.data
+            w.envmap_height, w.envmap_width = self.envmap.shape[:2]
+        w.envmap_intensity = self.intensity
+        w.envmap_scale_background = int(self.scale_background)
+        w.envmap_to_world[:] = [float(v) for v in self.rotation.reshape(-1)]
+        w.world_to_envmap[:] = [float(v) for v in self.inverse_rotation.reshape(-1)]
+        w.envmap_sampling = self.sampling
+        w.envmap_bsdf_mis = int(self.bsdf_mis)
+        w.envmap_bilinear = int(self.bilinear)
+        return w
+
+
 class Scene:
     def __init__(self, positions, indices, material_of_triangle, albedo=None, emission=None, stream=None, sah_bins=32,
                  max_leaf_size=3, principled=None):
@@ -241,6 +294,7 @@ class Scene:
         _lib.check(lib.gbpt_scene_create(ctypes.byref(desc), ctypes.byref(params), ctypes.byref(h), _stream(stream)))
         self._h = h
         self._lib = lib
+        self.world = World()
 
     @classmethod
     def from_cornell(cls, cb, **kw):
@@ -261,6 +315,29 @@ class Scene:
         _lib.check(self._lib.gbpt_scene_get_light_table(self._h, None, e.ctypes.data, p.ctypes.data, a.ctypes.data,
                                                         ctypes.addressof(s32), ctypes.addressof(s64)))
         return {"emissive": e, "probas": p, "alias": a, "power_sum": s32.value, "power_sum64": s64.value}
+
+    def set_world(self, world: "World", stream=None):
+        """Sets the world (ambient light / envmap); builds the envmap tables on the device."""
+        w = world.to_c()
+        _lib.check(self._lib.gbpt_scene_set_world(self._h, ctypes.byref(w), _stream(stream)))
+        self.world = world
+
+    def envmap_tables(self):
+        """Device envmap tables: RGB9E5 texels, CDF, alias probabilities and indices (H, W each)."""
+        # the library answers first whether the scene's world has an envmap
+        _lib.check(self._lib.gbpt_scene_get_envmap_tables(self._h, None, None, None, None, None, None))
+        h, w = self.world.envmap.shape[:2]
+        tex = np.zeros((h, w), np.uint32)
+        cdf = np.zeros((h, w), np.float32)
+        prob = np.zeros((h, w), np.float32)
+        alias = np.zeros((h, w), np.int32)
+        s32 = ctypes.c_float()
+        s64 = ctypes.c_double()
+        _lib.check(self._lib.gbpt_scene_get_envmap_tables(self._h, tex.ctypes.data, cdf.ctypes.data, prob.ctypes.data,
+                                                          alias.ctypes.data, ctypes.addressof(s32),
+                                                          ctypes.addressof(s64)))
+        return {"texels": tex, "cdf": cdf, "probas": prob, "alias": alias, "total_sum": s32.value,
+                "total_sum64": s64.value}
 
     def destroy(self):
         if getattr(self, "_h", None):

@@ -329,6 +329,35 @@ def cornell_box() -> CornellBox:
     return CornellBox(Mesh(pos, idx), mat, albedo, emission, np.nonzero(mat == 3)[0].astype(np.int32))
 
 
+def envmap_directions(width: int, height: int) -> np.ndarray:
+    """World direction (identity rotation) of each texel centre of an equirectangular envmap, as the
+    reference maps (u, v): phi = 2 pi u, theta = pi v, d = (-sin theta cos phi, -cos theta,
+    -sin theta sin phi); row 0 is the -y pole. Returns (height, width, 3) float64."""
+    u = (np.arange(width) + 0.5) / width
+    v = (np.arange(height) + 0.5) / height
+    phi = 2.0 * np.pi * u[None, :]
+    theta = np.pi * v[:, None]
+    return np.stack([-np.sin(theta) * np.cos(phi), -np.cos(theta) * np.ones_like(phi), -np.sin(theta) * np.sin(phi)],
+                    axis=-1)
+
+
+def sky_envmap(width: int = 64, height: int = 32, sun_dir=(0.35, 0.6, -0.72), sun_radius_deg: float = 8.0,
+               sun_radiance=(30.0, 26.0, 20.0), seed: int = 1) -> np.ndarray:
+    """Seeded synthetic outdoor envmap (height, width, 3) float32: a blue sky brightening towards
+    the horizon, a dim brown ground below it, a warm sun disc of sun_radius_deg around sun_dir
+    covering a few texels, and +-10% seeded texel noise."""
+    d = envmap_directions(width, height)
+    y = d[..., 1]
+    sky = np.stack([0.25 + 0.35 * (1 - y), 0.45 + 0.3 * (1 - y), 0.9 + 0.1 * (1 - y)], -1) * (y >= 0)[..., None]
+    ground = np.array([0.12, 0.09, 0.06]) * (y < 0)[..., None]
+    sd = np.asarray(sun_dir, np.float64)
+    sd = sd / np.linalg.norm(sd)
+    sun = (d @ sd > np.cos(np.radians(sun_radius_deg)))[..., None] * np.asarray(sun_radiance)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    img = (sky + ground + sun) * rng.uniform(0.9, 1.1, (height, width, 1))
+    return img.astype(F32)
+
+
 @dataclass
 class ManyLightScene:
     mesh: Mesh

@@ -83,6 +83,57 @@ GBPT_API gbpt_status gbpt_scene_get_light_table(const gbpt_scene* scene, int32_t
 GBPT_API gbpt_status gbpt_alias_table_build_noalloc(const float* power, int32_t n, float* probas, int32_t* alias,
                                                     double* power_sum64, void* stream);
 
+/* ---- the world around the scene: ambient light and environment map ----
+ * Mirrors WorldSettings (src/HostDeviceCommon/WorldSettings.h:14-53), RendererEnvmap
+ * (src/Renderer/RendererEnvmap.cpp:40-209) and the envmap kernel options
+ * (src/HostDeviceCommon/KernelOptions/KernelOptions.h:53-55,155-170). */
+enum {
+    GBPT_AMBIENT_NONE = 0,    /* AmbientLightType::NONE: misses are black */
+    GBPT_AMBIENT_UNIFORM = 1, /* AmbientLightType::UNIFORM: misses see uniform_color at every bounce */
+    GBPT_AMBIENT_ENVMAP = 2   /* AmbientLightType::ENVMAP */
+};
+enum {
+    GBPT_ENVMAP_NO_SAMPLING = 0,   /* ESS_NO_SAMPLING: the envmap is only found by misses */
+    GBPT_ENVMAP_BINARY_SEARCH = 1, /* ESS_BINARY_SEARCH: texel drawn by a search of the luminance CDF */
+    GBPT_ENVMAP_ALIAS_TABLE = 2    /* ESS_ALIAS_TABLE (the reference's default) */
+};
+
+/* envmap_rgb: width*height RGB float texels (finite, >= 0), row-major, row 0 at v = 0 — the -y
+ * pole (the reference's envmap after its vertical flip at load). Direction of (u, v):
+ * phi = 2 pi u, theta = pi v, d = (-sin theta cos phi, -cos theta, -sin theta sin phi) in envmap
+ * space, rotated to the world by envmap_to_world (row-major, d_world = M d). world_to_envmap is its
+ * inverse (the reference keeps both matrices; the library checks that they are inverses). */
+typedef struct gbpt_world_desc {
+    int32_t ambient;                /* GBPT_AMBIENT_* */
+    float uniform_color[3];         /* uniform_light_color */
+    const float* envmap_rgb;        /* host pointer (GBPT_AMBIENT_ENVMAP) */
+    int32_t envmap_width, envmap_height;
+    float envmap_intensity;         /* scale on every texel (envmap_intensity) */
+    int32_t envmap_scale_background;/* 0: camera misses see the unscaled texel [0] */
+    float envmap_to_world[9];
+    float world_to_envmap[9];
+    int32_t envmap_sampling;        /* GBPT_ENVMAP_* [GBPT_ENVMAP_ALIAS_TABLE] */
+    int32_t envmap_bsdf_mis;        /* EnvmapSamplingDoBSDFMIS: a BSDF sample MIS-combined with the envmap sample [1] */
+    int32_t envmap_bilinear;        /* EnvmapSamplingDoBilinearFiltering [0] */
+} gbpt_world_desc;
+
+/* Fills *w with the reference's defaults: no ambient light, identity rotation, intensity 1, alias
+ * table sampling with BSDF MIS, nearest-texel lookups. */
+GBPT_API gbpt_status gbpt_world_default(gbpt_world_desc* w);
+/* Sets the scene's world; renderers of the scene see it from their next launch (a batch created
+ * before the call keeps the world it captured). For an envmap the library packs the texels to
+ * RGB9E5 and, on the device, takes each texel's luminance from the float input, their FP64 sum,
+ * the FP64 running sum over texels stored as float (the binary-search CDF) and the Vose alias
+ * table of the luminances normalised by the FP64 sum (Image32Bit::compute_cdf and
+ * compute_alias_table, src/Image/Image.cpp:625-672, which sum in float). Synchronous. */
+GBPT_API gbpt_status gbpt_scene_set_world(gbpt_scene* scene, const gbpt_world_desc* w, void* stream);
+/* Copies the envmap's device tables to host arrays of width*height entries (any may be NULL):
+ * packed texels, CDF, alias probabilities and indices; total_sum = the float sum the sampler
+ * uses, total_sum64 = the FP64 sum. GBPT_ERROR_INVALID_ARG when the world has no envmap. */
+GBPT_API gbpt_status gbpt_scene_get_envmap_tables(const gbpt_scene* scene, uint32_t* texels, float* cdf,
+                                                  float* probas, int32_t* alias, float* total_sum,
+                                                  double* total_sum64);
+
 enum {
     GBPT_LIGHT_UNIFORM = 0, /* LSS_BASE_UNIFORM */
     GBPT_LIGHT_POWER = 1    /* LSS_BASE_POWER */

@@ -177,6 +177,8 @@ float balance(float a, float b) { return a == 0.0f ? 0.0f : a / (a + b); }
 
 float a2s(float area_pdf, float dist, float cosl) { return cosl < 1.0e-8f ? 0.0f : area_pdf * dist * dist / cosl; }
 
+struct OrcEnv;  // the world around the scene (pt_oracle.cpp)
+
 struct Settings
 {
     int width, height, nb_bounces, do_rr, rr_min, light, seed, jitter, spp, iteration_base;
@@ -185,6 +187,7 @@ struct Settings
     const float* ip;
     int direct = 0;             // 0: one light + one BSDF sample with MIS, 1: RIS
     int ris_m = 4, ris_n = 1;   // RIS light / BSDF candidates
+    const OrcEnv* env = nullptr;  // ambient light / envmap (null: none)
 };
 
 // ---------------------------------------------------------------------------------------------

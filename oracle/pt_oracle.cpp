@@ -171,6 +171,244 @@ V ris_finish(const Scene& s, const Settings& st, Pcg& rng, V P, int prim, V tp, 
     return mk(0, 0, 0);
 }
 
+// ---------------------------------------------------------------------------------------------
+// The world and its environment map:
+//   - RGB9E5 texels: RGBE9995Packed::pack / unpack (src/HostDeviceCommon/Packing.h:441-485);
+//   - tables: luminance_of_pixel from the float texels (src/Image/Image.cpp:526-546), the running
+//     sum of compute_cdf (Image.cpp:625-645) accumulated in double and stored as float, the Vose
+//     table of compute_alias_table (Image.cpp:650-672) through orc_vose_alias below;
+//   - lookups: eval_envmap_no_pdf (src/Device/includes/LightSampling/Envmap.h:27-37) through
+//     sample_environment_map_texture (src/Device/includes/Texture.h:209-240), nearest or bilinear;
+//   - sampling: envmap_cdf_search / envmap_sample / envmap_eval (Envmap.h:39-170): a texel by alias
+//     table (index draw, alias-test draw) or CDF search (one draw), the direction of its (x/W, y/H)
+//     corner, radiance and pdf read through the texture lookup at that corner;
+//   - direct lighting: sample_environment_map_with_mis (Envmap.h:173-249), an envmap sample
+//     (skipped when the material cannot be light-sampled) and a separate BSDF sample, balance
+//     heuristic, any-hit visibility to 1e35; the ReSTIR DI bounce is not restated here;
+//   - misses: path_tracing_miss_gather_envmap (src/Device/includes/PathTracing.h:122-169).
+// Guards shared with the GPU kernels: asin's argument clamped to [-1, 1], texel indices clamped to
+// the image, alias index split by integer division.
+// Random numbers at a vertex: first the envmap texel draws (2 alias / 1 CDF) and the BSDF sample's
+// draws (2 Lambertian / 1 Xorshift32 seed), then the emissive direct lighting's, then the
+// continuation's (the GPU's envmap pass runs before its shade pass). Contributions are added in
+// the order light sample, envmap sample, envmap BSDF sample, MIS BSDF sample.
+// ---------------------------------------------------------------------------------------------
+struct OrcEnv
+{
+    int32_t ambient;  // 0 none, 1 uniform, 2 envmap
+    float uniform[3];
+    const uint32_t* texels;
+    const float* cdf;
+    const float* probas;
+    const int32_t* alias;
+    int32_t width, height;
+    float intensity, total_sum;
+    float to_world[9], to_env[9];  // row-major, d' = M d
+    int32_t sampling;              // 0 none, 1 binary search, 2 alias table
+    int32_t bsdf_mis, bilinear, scale_background;
+};
+
+const float kInv2Pi = 0.15915494309189533577f, kInvPiF = 0.31830988618379067154f;
+const float kTwoPiF = 6.28318530717958647693f, kPiF = 3.14159265358979323846f;
+const float kTwoPiSq = 19.73920880217871723767f;
+
+uint32_t fbits(float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+float bitsf(uint32_t u)
+{
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+uint32_t rgb9e5_pack(float r, float g, float b)
+{
+    const float hi = bitsf(0x477F8000u), lo = bitsf(0x37800000u);
+    r = std::min(std::max(r, 0.0f), hi);
+    g = std::min(std::max(g, 0.0f), hi);
+    b = std::min(std::max(b, 0.0f), hi);
+    const float m = std::max(std::max(lo, r), std::max(g, b));
+    const float bias = bitsf((fbits(m) + 0x07804000u) & 0x7F800000u);
+    const uint32_t R = fbits(r + bias), G = fbits(g + bias), B = fbits(b + bias);
+    const uint32_t E = (fbits(bias) << 4) + 0x10000000u;
+    return E | (B << 18) | (G << 9) | (R & 0x1FFu);
+}
+
+V rgb9e5_unpack(uint32_t t)
+{
+    const float sc = std::ldexp(1.0f, (int)(t >> 27) - 24);
+    return mk((float)(t & 0x1FFu) * sc, (float)((t >> 9) & 0x1FFu) * sc, (float)((t >> 18) & 0x1FFu) * sc);
+}
+
+V mat3(const float* m, V d)
+{
+    return mk(m[0] * d.x + m[1] * d.y + m[2] * d.z, m[3] * d.x + m[4] * d.y + m[5] * d.z,
+              m[6] * d.x + m[7] * d.y + m[8] * d.z);
+}
+
+V env_texel(const OrcEnv& e, int x, int y)
+{
+    x = std::min(std::max(x, 0), e.width - 1);
+    y = std::min(std::max(y, 0), e.height - 1);
+    return rgb9e5_unpack(e.texels[(size_t)y * e.width + x]) * e.intensity;
+}
+
+V env_texture(const OrcEnv& e, float u, float v)
+{
+    const float fx = u * (float)(e.width - 1), fy = v * (float)(e.height - 1);
+    if (!e.bilinear) return env_texel(e, (int)fx, (int)fy);
+    const int x0 = (int)fx, y0 = (int)fy;
+    const float tx = fx - std::floor(fx), ty = fy - std::floor(fy);
+    const int x1 = std::min(x0 + 1, e.width - 1), y1 = std::min(y0 + 1, e.height - 1);
+    const V a = env_texel(e, x0, y0) * (1.0f - tx) + env_texel(e, x1, y0) * tx;
+    const V b = env_texel(e, x0, y1) * (1.0f - tx) + env_texel(e, x1, y1) * tx;
+    return a * (1.0f - ty) + b * ty;
+}
+
+V env_lookup(const OrcEnv& e, V d)
+{
+    const V r = mat3(e.to_env, d);
+    const float u = 0.5f + std::atan2(r.z, r.x) * kInv2Pi;
+    const float v = 0.5f + std::asin(std::min(1.0f, std::max(-1.0f, r.y))) * kInvPiF;
+    return env_texture(e, u, v);
+}
+
+float env_pdf(const OrcEnv& e, V L, float sin_theta)
+{
+    float pdf = lum(L) / (e.total_sum * e.intensity);
+    pdf *= (float)(e.width * e.height);
+    return pdf / (kTwoPiSq * sin_theta);
+}
+
+void env_cdf_search(const OrcEnv& e, float value, int& x, int& y)
+{
+    int lo = 0, hi = e.height - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi) >> 1;
+        if (value < e.cdf[(size_t)mid * e.width + (e.width - 1)])
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    y = std::min(lo, e.height - 1);
+    lo = 0;
+    hi = e.width - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi) >> 1;
+        if (value < e.cdf[(size_t)y * e.width + mid])
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    x = std::min(lo, e.width - 1);
+}
+
+struct EnvSampleO
+{
+    V dir, L;
+    float pdf;
+};
+
+// direction, radiance and pdf of a sampled texel (envmap_sample after the texel choice)
+EnvSampleO env_sample_texel(const OrcEnv& e, int x, int y)
+{
+    const float u = (float)x / (float)e.width, v = (float)y / (float)e.height;
+    const float phi = u * kTwoPiF;
+    const float theta = std::max(1.0e-5f, v * kPiF);
+    const float ct = std::cos(theta), sn = std::sin(theta);
+    EnvSampleO s;
+    s.dir = mat3(e.to_world, mk(-sn * std::cos(phi), -ct, -sn * std::sin(phi)));
+    s.L = env_texture(e, u, v);
+    s.pdf = env_pdf(e, s.L, sn);
+    return s;
+}
+
+EnvSampleO env_sample(const OrcEnv& e, Pcg& rng)
+{
+    int x, y;
+    if (e.sampling == 1)
+        env_cdf_search(e, rng.next() * e.total_sum, x, y);
+    else
+    {
+        int i = rng.index(e.width * e.height);
+        if (rng.next() > e.probas[i]) i = e.alias[i];
+        y = i / e.width;
+        x = i - y * e.width;
+    }
+    return env_sample_texel(e, x, y);
+}
+
+V env_eval(const OrcEnv& e, V d, float& pdf)
+{
+    const V L = env_lookup(e, d);
+    pdf = env_pdf(e, L, std::sin(std::acos(-d.y)));
+    return L;
+}
+
+bool env_sampled(const OrcEnv* e) { return e && e->ambient == 2 && e->sampling != 0 && e->intensity > 0.0f; }
+
+V env_miss(const OrcEnv* e, V d, int bounce, V tp)
+{
+    if (!e) return mk(0, 0, 0);
+    if (e->ambient == 1) return mk(e->uniform[0], e->uniform[1], e->uniform[2]) * tp;
+    if (e->ambient != 2 || !(e->intensity > 0.0f)) return mk(0, 0, 0);
+    const bool sampled = e->sampling != 0;
+    if (sampled && bounce > 0) return mk(0, 0, 0);
+    V c = env_lookup(*e, d);
+    if (!e->scale_background && (sampled || bounce == 0)) c = c / e->intensity;
+    return c * tp;
+}
+
+struct EnvDirectO
+{
+    V c_l = mk(0, 0, 0), c_b = mk(0, 0, 0);
+};
+
+// envmap sample + separate BSDF sample; eval(wi, pdf) -> f, sample(wi, pdf) -> f
+template <class Eval, class Sample>
+EnvDirectO env_direct(const OrcEnv& e, const Scene& s, Pcg& rng, V P, int prim, V ns, V tp, bool light_ok, Eval eval,
+                      Sample sample)
+{
+    EnvDirectO r;
+    const EnvSampleO es = env_sample(e, rng);
+    if (light_ok)
+    {
+        const float cosine = dot(ns, es.dir);
+        if (es.pdf > 0.0f && cosine > 0.0f)
+        {
+            float bp;
+            const V f = eval(es.dir, bp);
+            const float mis = e.bsdf_mis ? balance(es.pdf, bp) : 1.0f;
+            const V c = tp * (f * cosine * mis * es.L / es.pdf);
+            if (!black(c) && !occluded(s, P, es.dir, prim, 1.0e35f)) r.c_l = c;
+        }
+    }
+    if (e.bsdf_mis)
+    {
+        V wi;
+        float pdf;
+        const V f = sample(wi, pdf);
+        if (pdf > 0.0f)
+        {
+            const float cosine = std::fabs(dot(ns, wi));
+            float pe;
+            const V L = env_eval(e, wi, pe);
+            if (pe > 0.0f)
+            {
+                const V c = tp * (L * balance(pdf, pe) * cosine * f / pdf);
+                if (!black(c) && !occluded(s, P, wi, prim, 1.0e35f)) r.c_b = c;
+            }
+        }
+    }
+    return r;
+}
+
 V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
 {
     const int x = pixel % st.width, y = pixel / st.width;
@@ -192,7 +430,11 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
     {
         float t;
         int prim = closest(s, o, d, skip, t);
-        if (prim < 0) break;
+        if (prim < 0)
+        {
+            L = L + env_miss(st.env, d, bounce, tp);
+            break;
+        }
         V P = o + d * t;
         V ng = nrm(cross(s.b(prim) - s.a(prim), s.c(prim) - s.a(prim)));
         V ns = ng;
@@ -207,6 +449,17 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
         }
         V albedo = s.alb(prim);
         if (bounce == 0) L = L + s.emi(prim);
+        // envmap direct lighting: its draws come first at a vertex (the GPU's envmap pass runs
+        // before shade); its contributions are added after the light sample's
+        EnvDirectO ed;
+        if (env_sampled(st.env))
+            ed = env_direct(
+                *st.env, s, rng, P, prim, ns, tp, true, [&](V wi, float& pb) { return lambert(albedo, dot(ns, wi), pb); },
+                [&](V& wi, float& pdf) {
+                    float r1 = rng.next(), r2 = rng.next();
+                    wi = cosine_sample(ns, r1, r2);
+                    return lambert(albedo, dot(ns, wi), pdf);
+                });
         Ris ris;
         const V tp0 = tp;
         if (st.direct == 1 && s.ne > 0)
@@ -264,6 +517,7 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
                 }
             }
         }
+        V bsdf_c = mk(0, 0, 0);  // MIS BSDF sample, added after the envmap's samples as on the GPU
         if (!ris.active)
         {
             float r1 = rng.next(), r2 = rng.next();
@@ -286,12 +540,15 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
                         if (cl > 0.0f)
                         {
                             float lpdf = a2s(light_pdf_area(s, lp, 0.5f * ln, Le, st.light), th, cl);
-                            L = L + w * Le * balance(pdf, lpdf);
+                            bsdf_c = w * Le * balance(pdf, lpdf);
                         }
                     }
                 }
             }
         }
+        L = L + ed.c_l;
+        L = L + ed.c_b;
+        L = L + bsdf_c;
         // continuation (its draws precede the RIS reservoir's last draw, as on the GPU)
         auto cont = [&]() {
             float r1 = rng.next(), r2 = rng.next();
@@ -344,7 +601,11 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
     {
         float t;
         int prim = closest(s, o, d, skip, t);
-        if (prim < 0) break;
+        if (prim < 0)
+        {
+            L = L + env_miss(st.env, d, bounce, tp);
+            break;
+        }
         V P = o + d * t;
         V ng_raw = nrm(cross(s.b(prim) - s.a(prim), s.c(prim) - s.a(prim)));
         V ng = ng_raw, ns = ng_raw;
@@ -367,6 +628,27 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
         const float eta_i = inside ? m[37] : (medium >= 0 ? ps.mat(medium)[37] : 1.0f);
         const float eta_o = inside ? 1.0f : m[37];
         float q[16], out[8];
+        // envmap direct lighting first, as on the GPU
+        EnvDirectO ed;
+        if (env_sampled(st.env))
+            ed = env_direct(
+                *st.env, s, rng, P, prim, ns, tp, can_light_sample(m),
+                [&](V wi, float& pb) {
+                    float qq[16], oo[8];
+                    make_query(qq, view, ns, ng, wi, eta_i, eta_o, inside, 0);
+                    ps.eval(m, qq, oo);
+                    pb = oo[3];
+                    return mk(oo[0], oo[1], oo[2]);
+                },
+                [&](V& wi, float& pdf) {
+                    float qq[16], oo[8];
+                    make_query(qq, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
+                    int32_t lobe;
+                    ps.sample(m, qq, bsdf_seed(rng), oo, &lobe);
+                    wi = mk(oo[0], oo[1], oo[2]);
+                    pdf = oo[6];
+                    return mk(oo[3], oo[4], oo[5]);
+                });
         Ris ris;
         const V tp0 = tp;
         if (st.direct == 1 && s.ne > 0)
@@ -433,6 +715,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                 }
             }
         }
+        V bsdf_c = mk(0, 0, 0);  // MIS BSDF sample, added after the envmap's samples as on the GPU
         if (!ris.active)
         {
             make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
@@ -457,12 +740,15 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                         if (cl > 0.0f)
                         {
                             float lpdf = a2s(light_pdf_area(s, lp, 0.5f * ln, Le, st.light), th, cl);
-                            L = L + w * Le * balance(pdf, lpdf);
+                            bsdf_c = w * Le * balance(pdf, lpdf);
                         }
                     }
                 }
             }
         }
+        L = L + ed.c_l;
+        L = L + ed.c_b;
+        L = L + bsdf_c;
         auto cont = [&]() {
             make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
             int32_t lobe;
@@ -501,17 +787,17 @@ extern "C" {
 
 /* settings_i: width, height, nb_bounces, do_rr, rr_min_depth, light_sampling (0 uniform, 1 power),
  * seed, do_jittering, spp, iteration_base, direct lighting (0 MIS, 1 RIS), RIS light candidates,
- * RIS BSDF candidates. Adds the samples of iterations
+ * RIS BSDF candidates. env: the world (NULL: none). Adds the samples of iterations
  * [iteration_base, iteration_base + spp) to out_rgb (W*H*3 doubles). */
 void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const float* albedo, const float* emission,
                    const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx, float power_sum,
                    const int* settings_i, float rr_clamp, const float* inv_view, const float* inv_proj, double* out_rgb,
-                   int nthreads)
+                   int nthreads, const OrcEnv* env)
 {
     Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
-                settings_i[10], settings_i[11], settings_i[12]};
+                settings_i[10], settings_i[11], settings_i[12], env};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};
@@ -562,13 +848,13 @@ void orc_pt_render_principled(const float* tri_verts, int n_tris, const int* mat
                               const float* emission, const float* pmats, void* eval_fn, void* sample_fn,
                               const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx,
                               float power_sum, const int* settings_i, float rr_clamp, const float* inv_view,
-                              const float* inv_proj, double* out_rgb, int nthreads)
+                              const float* inv_proj, double* out_rgb, int nthreads, const OrcEnv* env)
 {
     Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
     PScene ps{pmats, (bsdf_eval_fn)eval_fn, (bsdf_sample_fn)sample_fn};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
-                settings_i[10], settings_i[11], settings_i[12]};
+                settings_i[10], settings_i[11], settings_i[12], env};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};
@@ -632,6 +918,96 @@ void orc_vose_alias(const float* input, int n, double total_sum, float* out_prob
     {
         out_prob[smalls.front()] = 1.0f;
         smalls.pop_front();
+    }
+}
+
+/* ---- envmap tables and functions (pinned against the reference's own code in tests) ---- */
+
+/* RGB9E5 packing of n RGB float texels and the float luminance of each (luminance_of_pixel) */
+void orc_env_pack(const float* rgb, int64_t n, uint32_t* texels, float* luminance)
+{
+    for (int64_t i = 0; i < n; i++)
+    {
+        const float r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
+        if (texels) texels[i] = rgb9e5_pack(r, g, b);
+        if (luminance) luminance[i] = ((r * 0.3086f) + (g * 0.6094f)) + (b * 0.0820f);
+    }
+}
+
+void orc_env_unpack(const uint32_t* texels, int64_t n, float* rgb)
+{
+    for (int64_t i = 0; i < n; i++)
+    {
+        const V c = rgb9e5_unpack(texels[i]);
+        rgb[3 * i] = c.x;
+        rgb[3 * i + 1] = c.y;
+        rgb[3 * i + 2] = c.z;
+    }
+}
+
+/* running sum of the luminances in double, each stored as float; *total = the double sum */
+void orc_env_cdf(const float* luminance, int64_t n, float* cdf, double* total)
+{
+    double run = 0.0;
+    for (int64_t i = 0; i < n; i++)
+    {
+        run += (double)luminance[i];
+        cdf[i] = (float)run;
+    }
+    *total = run;
+}
+
+/* eval_envmap_no_pdf of n world directions */
+void orc_env_lookup(const OrcEnv* e, const float* dirs, int n, float* rgb)
+{
+    for (int i = 0; i < n; i++)
+    {
+        const V c = env_lookup(*e, mk(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+        rgb[3 * i] = c.x;
+        rgb[3 * i + 1] = c.y;
+        rgb[3 * i + 2] = c.z;
+    }
+}
+
+/* envmap_eval: radiance and pdf of n world directions */
+void orc_env_eval(const OrcEnv* e, const float* dirs, int n, float* rgb, float* pdf)
+{
+    for (int i = 0; i < n; i++)
+    {
+        const V c = env_eval(*e, mk(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]), pdf[i]);
+        rgb[3 * i] = c.x;
+        rgb[3 * i + 1] = c.y;
+        rgb[3 * i + 2] = c.z;
+    }
+}
+
+/* envmap_sample from given draws: alias table (index[i], u[i]) when values is NULL, else the CDF
+ * search of values[i]; out: direction, radiance, pdf and the texel (x, y) */
+void orc_env_sample(const OrcEnv* e, const int32_t* index, const float* u, const float* values, int n, float* dir,
+                    float* rgb, float* pdf, int32_t* xy)
+{
+    for (int i = 0; i < n; i++)
+    {
+        int x, y;
+        if (values)
+            env_cdf_search(*e, values[i], x, y);
+        else
+        {
+            int k = index[i];
+            if (u[i] > e->probas[k]) k = e->alias[k];
+            y = k / e->width;
+            x = k - y * e->width;
+        }
+        const EnvSampleO s = env_sample_texel(*e, x, y);
+        dir[3 * i] = s.dir.x;
+        dir[3 * i + 1] = s.dir.y;
+        dir[3 * i + 2] = s.dir.z;
+        rgb[3 * i] = s.L.x;
+        rgb[3 * i + 1] = s.L.y;
+        rgb[3 * i + 2] = s.L.z;
+        pdf[i] = s.pdf;
+        xy[2 * i] = x;
+        xy[2 * i + 1] = y;
     }
 }
 

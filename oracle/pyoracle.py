@@ -4,6 +4,8 @@
   (trace_oracle.cpp). Built anywhere by ``make -C oracle``.
 * ``_ref/libref.so``: the reference's own CPU code compiled behind clean-room shims
   (ref_trace.cpp). Built only where the reference tree is present (``make -C oracle ref``).
+* ``_ref/libref_env.so`` / ``libref_env_bilinear.so``: the reference's own envmap packing, lookups
+  and sampling (ref_envmap.cpp), nearest-texel and bilinear builds.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
 """
@@ -18,6 +20,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
+REF_ENV_SO = os.path.join(HERE, "_ref", "libref_env.so")
+REF_ENV_BILINEAR_SO = os.path.join(HERE, "_ref", "libref_env_bilinear.so")
 
 _c_f = ctypes.POINTER(ctypes.c_float)
 _c_i = ctypes.POINTER(ctypes.c_int32)
@@ -163,13 +167,93 @@ class RefBVH:
         return occ
 
 
+class OrcEnvC(ctypes.Structure):
+    """OrcEnv of pt_oracle.cpp: the world around the scene."""
+    _fields_ = [("ambient", ctypes.c_int32), ("uniform", ctypes.c_float * 3), ("texels", ctypes.c_void_p),
+                ("cdf", ctypes.c_void_p), ("probas", ctypes.c_void_p), ("alias", ctypes.c_void_p),
+                ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("intensity", ctypes.c_float),
+                ("total_sum", ctypes.c_float), ("to_world", ctypes.c_float * 9), ("to_env", ctypes.c_float * 9),
+                ("sampling", ctypes.c_int32), ("bsdf_mis", ctypes.c_int32), ("bilinear", ctypes.c_int32),
+                ("scale_background", ctypes.c_int32)]
+
+
+class OracleEnv:
+    """The world for the oracle. Envmap tables (texels, cdf, probas, alias: H x W) come from the
+    library under test or from env_tables() below; rotation is the envmap-to-world matrix."""
+
+    def __init__(self, ambient=2, uniform=(0.0, 0.0, 0.0), texels=None, cdf=None, probas=None, alias=None,
+                 intensity=1.0, total_sum=0.0, rotation=None, inverse_rotation=None, sampling=2, bsdf_mis=True,
+                 bilinear=False, scale_background=False):
+        c = OrcEnvC()
+        c.ambient = int(ambient)
+        c.uniform[:] = [float(v) for v in uniform]
+        self._keep = []
+        if texels is not None:
+            arrs = [np.ascontiguousarray(texels, np.uint32), np.ascontiguousarray(cdf, np.float32),
+                    np.ascontiguousarray(probas, np.float32), np.ascontiguousarray(alias, np.int32)]
+            self._keep = arrs
+            c.texels, c.cdf, c.probas, c.alias = (a.ctypes.data for a in arrs)
+            c.height, c.width = arrs[0].shape[:2]
+        rot = np.eye(3, dtype=np.float32) if rotation is None else np.asarray(rotation, np.float32).reshape(3, 3)
+        inv = (np.linalg.inv(rot.astype(np.float64)).astype(np.float32) if inverse_rotation is None
+               else np.asarray(inverse_rotation, np.float32).reshape(3, 3))
+        c.to_world[:] = [float(v) for v in rot.reshape(-1)]
+        c.to_env[:] = [float(v) for v in inv.reshape(-1)]
+        c.intensity = float(intensity)
+        c.total_sum = float(total_sum)
+        c.sampling = int(sampling) if total_sum > 0 else 0
+        c.bsdf_mis = int(bool(bsdf_mis))
+        c.bilinear = int(bool(bilinear))
+        c.scale_background = int(bool(scale_background))
+        self.c = c
+
+    @classmethod
+    def from_world(cls, world, tables=None):
+        """From a gbpt World (duck-typed) and, for an envmap, the tables the library built."""
+        if tables is None:
+            return cls(ambient=world.ambient, uniform=world.uniform_color)
+        return cls(ambient=world.ambient, uniform=world.uniform_color, texels=tables["texels"], cdf=tables["cdf"],
+                   probas=tables["probas"], alias=tables["alias"], intensity=world.intensity,
+                   total_sum=tables["total_sum"], rotation=world.rotation, inverse_rotation=world.inverse_rotation,
+                   sampling=world.sampling, bsdf_mis=world.bsdf_mis, bilinear=world.bilinear,
+                   scale_background=world.scale_background)
+
+    def ref(self) -> "RefEnvC":
+        r = RefEnvC()
+        c = self.c
+        r.texels, r.cdf, r.probas, r.alias = c.texels, c.cdf, c.probas, c.alias
+        r.width, r.height, r.intensity, r.total_sum = c.width, c.height, c.intensity, c.total_sum
+        r.to_world[:] = list(c.to_world)
+        r.to_env[:] = list(c.to_env)
+        return r
+
+
+class RefEnvC(ctypes.Structure):
+    """RefEnv of ref_envmap.cpp."""
+    _fields_ = [("texels", ctypes.c_void_p), ("cdf", ctypes.c_void_p), ("probas", ctypes.c_void_p),
+                ("alias", ctypes.c_void_p), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("intensity", ctypes.c_float), ("total_sum", ctypes.c_float), ("to_world", ctypes.c_float * 9),
+                ("to_env", ctypes.c_float * 9)]
+
+
+def _env_ptr(env):
+    return ctypes.byref(env.c) if env is not None else None
+
+
 def _pt_lib():
     orc = Oracle()
     lib = orc.lib
     if not getattr(lib, "_pt_sigs", False):
         lib.orc_pt_render.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, _c_f, _c_i, ctypes.c_int, _c_f, _c_i,
                                       ctypes.c_float, _c_i, ctypes.c_float, _c_f, _c_f,
-                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p]
+        _u32 = ctypes.POINTER(ctypes.c_uint32)
+        lib.orc_env_pack.argtypes = [_c_f, _i64, _u32, _c_f]
+        lib.orc_env_unpack.argtypes = [_u32, _i64, _c_f]
+        lib.orc_env_cdf.argtypes = [_c_f, _i64, _c_f, ctypes.POINTER(ctypes.c_double)]
+        lib.orc_env_lookup.argtypes = [ctypes.c_void_p, _c_f, ctypes.c_int, _c_f]
+        lib.orc_env_eval.argtypes = [ctypes.c_void_p, _c_f, ctypes.c_int, _c_f, _c_f]
+        lib.orc_env_sample.argtypes = [ctypes.c_void_p, _c_i, _c_f, _c_f, ctypes.c_int, _c_f, _c_f, _c_f, _c_i]
         lib.orc_vose_alias.argtypes = [_c_f, ctypes.c_int, ctypes.c_double, _c_f, _c_i]
         lib.orc_emissive_power.argtypes = [_c_f, _c_i, _c_f, _c_i, ctypes.c_int, _c_f]
         lib._pt_sigs = True
@@ -177,9 +261,9 @@ def _pt_lib():
 
 
 def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_idx, power_sum, settings, spp,
-              iteration_base=0, nthreads=0):
+              iteration_base=0, nthreads=0, env: OracleEnv | None = None):
     """Path-tracing oracle (Lambertian scenes). Returns the FP64 per-pixel sums (H, W, 3) of
-    'spp' samples per pixel, drawn with the same PCG sequence as the GPU kernels."""
+    'spp' samples per pixel, drawn with the same PCG sequence as the GPU kernels. env: the world."""
     lib = _pt_lib()
     soup = np.ascontiguousarray(soup, np.float32)
     mo = np.ascontiguousarray(material_of, np.int32)
@@ -199,12 +283,12 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
     lib.orc_pt_render(_ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(al, _c_f), _ptr(em, _c_f), _ptr(ei, _c_i),
                       len(ei), _ptr(ap, _c_f), _ptr(ai, _c_i), float(power_sum), _ptr(si, _c_i),
                       float(s.russian_roulette_throughput_clamp), _ptr(iv, _c_f), _ptr(ip, _c_f),
-                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads)
+                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads, _env_ptr(env))
     return out
 
 
 def pt_render_principled(soup, material_of, pmats_effective, emission, emissive, alias_prob, alias_idx, power_sum,
-                         settings, spp, iteration_base=0, nthreads=0):
+                         settings, spp, iteration_base=0, nthreads=0, env: OracleEnv | None = None):
     """Path-tracing oracle for principled scenes: the estimator of pt_render with the BSDF
     evaluated and sampled by the REFERENCE's own principled BSDF (oracle/_ref/libref.so, built
     only where the reference tree exists). pmats_effective: (M, 64) records after coat
@@ -214,7 +298,7 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
         lib.orc_pt_render_principled.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, _c_f, _c_f, ctypes.c_void_p,
                                                  ctypes.c_void_p, _c_i, ctypes.c_int, _c_f, _c_i, ctypes.c_float, _c_i,
                                                  ctypes.c_float, _c_f, _c_f, ctypes.POINTER(ctypes.c_double),
-                                                 ctypes.c_int]
+                                                 ctypes.c_int, ctypes.c_void_p]
         lib._ptp_sig = True
     ref = ctypes.CDLL(REF_SO)
     eval_fn = ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value
@@ -239,8 +323,144 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
                                  _ptr(pm, _c_f), eval_fn, sample_fn, _ptr(ei, _c_i), len(ei), _ptr(ap, _c_f),
                                  _ptr(ai, _c_i), float(power_sum), _ptr(si, _c_i),
                                  float(s.russian_roulette_throughput_clamp), _ptr(iv, _c_f), _ptr(ip, _c_f),
-                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads)
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads, _env_ptr(env))
     return out
+
+
+# ---- envmap: tables, lookups and sampling of the oracle, and the reference's own (pin) ----
+def env_pack(rgb):
+    """(H, W, 3) float texels -> RGB9E5 words (H, W) and float luminances (H, W)."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    h, w = rgb.shape[:2]
+    tex = np.zeros((h, w), np.uint32)
+    lum = np.zeros((h, w), np.float32)
+    _pt_lib().orc_env_pack(_ptr(rgb, _c_f), h * w, tex.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ptr(lum, _c_f))
+    return tex, lum
+
+
+def env_unpack(texels):
+    tex = np.ascontiguousarray(texels, np.uint32)
+    out = np.zeros(tex.shape + (3,), np.float32)
+    _pt_lib().orc_env_unpack(tex.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), tex.size, _ptr(out, _c_f))
+    return out
+
+
+def env_tables(rgb, total_sum64=None):
+    """The oracle's envmap tables: texels, CDF (double running sum stored as float), alias table of
+    the luminances normalised by total_sum64 (default: the oracle's own double sum)."""
+    tex, lum = env_pack(rgb)
+    cdf = np.zeros_like(lum)
+    tot = ctypes.c_double()
+    _pt_lib().orc_env_cdf(_ptr(lum, _c_f), lum.size, _ptr(cdf, _c_f), ctypes.byref(tot))
+    s64 = tot.value if total_sum64 is None else float(total_sum64)
+    prob, alias = vose_alias(lum.reshape(-1), s64)
+    return {"texels": tex, "luminance": lum, "cdf": cdf, "probas": prob.reshape(lum.shape),
+            "alias": alias.reshape(lum.shape), "total_sum": float(np.float32(s64)), "total_sum64": s64}
+
+
+def env_lookup(env: OracleEnv, dirs):
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros_like(d)
+    _pt_lib().orc_env_lookup(ctypes.byref(env.c), _ptr(d, _c_f), len(d), _ptr(out, _c_f))
+    return out
+
+
+def env_eval(env: OracleEnv, dirs):
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros_like(d)
+    pdf = np.zeros(len(d), np.float32)
+    _pt_lib().orc_env_eval(ctypes.byref(env.c), _ptr(d, _c_f), len(d), _ptr(out, _c_f), _ptr(pdf, _c_f))
+    return out, pdf
+
+
+def env_sample(env: OracleEnv, index=None, u=None, values=None):
+    """Texel by alias draws (index, u) or CDF values -> (direction, radiance, pdf, (x, y))."""
+    n = len(values) if values is not None else len(index)
+    ix = None if index is None else np.ascontiguousarray(index, np.int32)
+    uu = None if u is None else np.ascontiguousarray(u, np.float32)
+    vv = None if values is None else np.ascontiguousarray(values, np.float32)
+    d = np.zeros((n, 3), np.float32)
+    c = np.zeros((n, 3), np.float32)
+    p = np.zeros(n, np.float32)
+    xy = np.zeros((n, 2), np.int32)
+    _pt_lib().orc_env_sample(ctypes.byref(env.c), _ptr(ix, _c_i), _ptr(uu, _c_f), _ptr(vv, _c_f), n, _ptr(d, _c_f),
+                             _ptr(c, _c_f), _ptr(p, _c_f), _ptr(xy, _c_i))
+    return d, c, p, xy
+
+
+def ref_env_available() -> bool:
+    return os.path.exists(REF_ENV_SO) and os.path.exists(REF_ENV_BILINEAR_SO)
+
+
+def _ref_env_lib(bilinear: bool):
+    lib = ctypes.CDLL(REF_ENV_BILINEAR_SO if bilinear else REF_ENV_SO)
+    if not getattr(lib, "_sigs", False):
+        _u32 = ctypes.POINTER(ctypes.c_uint32)
+        lib.ref_env_rgbe_pack.argtypes = [_c_f, ctypes.c_int, _u32]
+        lib.ref_env_rgbe_unpack.argtypes = [_u32, ctypes.c_int, _c_f]
+        lib.ref_env_lookup.argtypes = [ctypes.c_void_p, _c_f, ctypes.c_int, _c_f]
+        lib.ref_env_eval.argtypes = [ctypes.c_void_p, _c_f, ctypes.c_int, _c_f, _c_f]
+        lib.ref_env_sample.argtypes = [ctypes.c_void_p, _u32, ctypes.c_int, _c_f, _c_f, _c_f, _c_i, _c_f]
+        lib.ref_env_cdf_search.argtypes = [ctypes.c_void_p, _c_f, ctypes.c_int, _c_i]
+        lib._sigs = True
+    return lib
+
+
+def ref_env_pack(rgb):
+    rgb = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+    out = np.zeros(len(rgb), np.uint32)
+    _ref_env_lib(False).ref_env_rgbe_pack(_ptr(rgb, _c_f), len(rgb), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    return out
+
+
+def ref_env_unpack(texels):
+    t = np.ascontiguousarray(texels, np.uint32).reshape(-1)
+    out = np.zeros((len(t), 3), np.float32)
+    _ref_env_lib(False).ref_env_rgbe_unpack(t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), len(t), _ptr(out, _c_f))
+    return out
+
+
+def ref_env_lookup(env: OracleEnv, dirs):
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros_like(d)
+    r = env.ref()
+    _ref_env_lib(bool(env.c.bilinear)).ref_env_lookup(ctypes.byref(r), _ptr(d, _c_f), len(d), _ptr(out, _c_f))
+    return out
+
+
+def ref_env_eval(env: OracleEnv, dirs):
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros_like(d)
+    pdf = np.zeros(len(d), np.float32)
+    r = env.ref()
+    _ref_env_lib(bool(env.c.bilinear)).ref_env_eval(ctypes.byref(r), _ptr(d, _c_f), len(d), _ptr(out, _c_f),
+                                                    _ptr(pdf, _c_f))
+    return out, pdf
+
+
+def ref_env_sample(env: OracleEnv, seeds):
+    """The reference's envmap_sample (alias table) from Xorshift32 seeds -> direction, radiance,
+    pdf, and the two draws it made (table index, alias-test number)."""
+    sd = np.ascontiguousarray(seeds, np.uint32)
+    n = len(sd)
+    d = np.zeros((n, 3), np.float32)
+    c = np.zeros((n, 3), np.float32)
+    p = np.zeros(n, np.float32)
+    idx = np.zeros(n, np.int32)
+    u = np.zeros(n, np.float32)
+    r = env.ref()
+    _ref_env_lib(bool(env.c.bilinear)).ref_env_sample(ctypes.byref(r), sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                                      n, _ptr(d, _c_f), _ptr(c, _c_f), _ptr(p, _c_f), _ptr(idx, _c_i),
+                                                      _ptr(u, _c_f))
+    return d, c, p, idx, u
+
+
+def ref_env_cdf_search(env: OracleEnv, values):
+    v = np.ascontiguousarray(values, np.float32)
+    xy = np.zeros((len(v), 2), np.int32)
+    r = env.ref()
+    _ref_env_lib(False).ref_env_cdf_search(ctypes.byref(r), _ptr(v, _c_f), len(v), _ptr(xy, _c_i))
+    return xy
 
 
 def restir_spatial_seed(frame: int, pass_index: int, seed: int) -> int:

@@ -97,3 +97,24 @@ def test_guide_parameters_and_argument_checks():
     assert lib.gbpt_guide_train(None, None, None, None, None, None, None, 4, None, None) == 1
     assert lib.gbpt_guide_infer(None, None, None, None, 4, None, None) == 1
     assert lib.gbpt_guide_destroy(None) == 0
+
+
+def test_world_descriptor_layout_defaults_and_checks():
+    """gbpt_world_desc matches its C layout; defaults are the reference's; bad worlds are rejected
+    before any device work."""
+    from gbpt import render
+    text = open(os.path.join(INCLUDE, "gbpt_render.h")).read()
+    body = text[text.index("typedef struct gbpt_world_desc {"):text.index("} gbpt_world_desc;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = [n.strip().split("[")[0] for decl in re.findall(r"(?:int32_t|float|const float\*)\s+([^;]+);", body)
+             for n in decl.split(",")]
+    assert names == [f for f, _ in render.WorldDescC._fields_]
+    assert ctypes.sizeof(render.WorldDescC) == 128
+    lib = render._load()
+    w = render.WorldDescC()
+    assert lib.gbpt_world_default(ctypes.byref(w)) == 0
+    assert w.ambient == render.AMBIENT_NONE and w.envmap_intensity == 1.0
+    assert w.envmap_sampling == render.ENVMAP_ALIAS_TABLE and w.envmap_bsdf_mis == 1 and w.envmap_bilinear == 0
+    assert list(w.envmap_to_world) == [1, 0, 0, 0, 1, 0, 0, 0, 1] == list(w.world_to_envmap)
+    assert lib.gbpt_scene_set_world(None, ctypes.byref(w), None) == 1
+    assert lib.gbpt_scene_get_envmap_tables(None, None, None, None, None, None, None) == 1
