@@ -209,6 +209,8 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
                 light sampling NEE + BSDF MIS, Lambertian; relMSE against a 16384-spp FP64 image;
                 cpu_baseline = the oracle's restatement of the reference's CPU estimator on all host
                 cores over a bounded sample.
+    envmap      the Cornell box under a 2048 x 1024 sky, 512 x 512: envmap table build time and samples/s
+                with alias-table envmap sampling, against the same scene without a world.
     restir      the many-light principled scene (16,777,216 + 10,000 emissive triangles), 1920 x 1080,
                 8 frames with the camera orbiting 0.5 degrees per frame, 3 indirect bounces, power
                 light sampling, ReSTIR DI (32 light + 1 BSDF candidates, visibility reuse, M-cap 20,
@@ -267,6 +269,8 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
         dt = time.perf_counter() - t0
         out["cornell"]["cpu_baseline"] = {"value": 256 * 256 * spp / dt, "unit": "samples/s", "cores": cores,
                                           "kind": "port", "sample": f"256x256 x {spp} spp, {dt:.2f}s"}
+    # ---- the Cornell box under an importance-sampled environment map ----
+    out["envmap"] = envmap_workload(timed, cscene)
     del cscene
 
     # ---- many-light principled scene ----
@@ -337,6 +341,44 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
     # ---- batched jobs ----
     out["batch"] = batch_workload(timed, log)
     return out
+
+
+def envmap_workload(timed, cscene, res=512, launches=32):
+    """The Cornell box (open side facing the camera, 60 degree FOV) under a seeded 2048 x 1024 sky
+    with a sun: table build time (RGB9E5 packing, FP64 CDF and sum on the device, Vose alias table
+    on the host; 2M and 8M texels), then res^2 x launches x 1 spp with the envmap sampled by alias
+    table (envmap pass + shade + shadow / BSDF-light / envmap any-hit rays), against the same scene
+    without a world."""
+    import torch
+    import gbpt
+    from gbpt import scenes
+    from gbpt.render import AMBIENT_ENVMAP, World
+    iv, ip = gbpt.look_at_camera((2.75, 2.75, -8.0), (2.75, 2.75, 0.0), vfov_deg=60.0)
+    st = gbpt.cornell_settings(res, res, samples_per_launch=1, seed=1, inverse_view=iv, inverse_projection=ip)
+    build_ms = {}
+    for w, h in ((2048, 1024), (4096, 2048)):
+        sky = scenes.sky_envmap(w, h, seed=3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cscene.set_world(World(ambient=AMBIENT_ENVMAP, envmap=sky))
+        build_ms[f"{w}x{h}"] = (time.perf_counter() - t0) * 1e3
+    cscene.set_world(World(ambient=AMBIENT_ENVMAP, envmap=scenes.sky_envmap(2048, 1024, seed=3)))
+    res_out = {}
+    for tag in ("envmap", "no_world"):
+        if tag == "no_world":
+            cscene.set_world(World())
+        r = gbpt.Renderer(cscene, st)
+        r.render(3)
+        r.reset()
+        ms = timed(lambda: r.render(launches))
+        s = r.stats()
+        rays = s["extension_rays"] + s["shadow_rays"] + s["bsdf_light_rays"]
+        res_out[tag] = {"ms": ms, "samples_per_s": res * res * launches / (ms * 1e-3),
+                        "mrays_per_s": rays / (ms * 1e-3) / 1e6}
+        del r
+    return {"config": f"Cornell box under a 2048x1024 sky (sun), {res}x{res}, {launches} x 1 spp, 4 bounces, "
+                      "alias-table envmap sampling + BSDF MIS, uniform NEE + BSDF MIS, Lambert",
+            "table_build_ms": build_ms, **res_out}
 
 
 def batch_jobs(n_jobs=48, seed=1):
