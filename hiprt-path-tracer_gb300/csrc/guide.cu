@@ -11,6 +11,8 @@
 // A operand H^T is 64 rows: the MMA runs with M = 128 and the upper 64 rows of D (read from the
 // next 16 KB of shared memory) are ignored. MMAs are issued by thread 0 and completed through an
 // mbarrier; every wait is bounded and reports through an error flag.
+#include <cstddef>
+
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -35,12 +37,14 @@ __device__ __forceinline__ uint32_t col_dw(int l) { return 128u + 64u * (uint32_
 
 using bf16 = __nv_bfloat16;
 
+// Operand arrays start on 16-byte boundaries: the weights are copied and the activations stored in
+// 16-byte words, and the shared-memory matrix descriptors address 16-byte units.
 struct SmemTrain
 {
     uint64_t mbar;
     uint32_t tmem;
     uint32_t pad;
-    bf16 w[kPackedWeights];
+    alignas(16) bf16 w[kPackedWeights];
     // transposed layer inputs X^T, H1^T, H2^T, H3^T (64 rows x K = 128 samples): the A operands
     // of dW1..dW4; each is followed by 16 KB of shared memory that the M = 128 MMA reads as rows
     // 64..127 (results ignored)
@@ -49,14 +53,25 @@ struct SmemTrain
     bf16 gt[2][kHid * kTile];   // transposed output gradients (B operands of dW), ping-pong
 };
 
+// Inference keeps one operand buffer: every MMA has completed (its mbarrier wait) before the
+// epilogue overwrites its input with the next layer's, so 47 KB per CTA and four CTAs per SM.
 struct SmemInfer
 {
     uint64_t mbar;
     uint32_t tmem;
     uint32_t pad;
-    bf16 w[kFwdWeights];
-    bf16 act[2][kTile * kHid];
+    alignas(16) bf16 w[kFwdWeights];
+    alignas(16) bf16 act[kTile * kHid];
 };
+constexpr int kInferCtasPerSm = 4;
+static_assert(offsetof(SmemInfer, w) % 16 == 0 && offsetof(SmemInfer, act) % 16 == 0,
+              "inference operands must start on 16-byte boundaries");
+static_assert(sizeof(SmemInfer) * kInferCtasPerSm <= 227 * 1024 && kTmemInfer * kInferCtasPerSm <= 512,
+              "four inference CTAs per SM");
+static_assert(offsetof(SmemTrain, w) % 16 == 0 && offsetof(SmemTrain, tr) % 16 == 0 &&
+                  offsetof(SmemTrain, act) % 16 == 0 && offsetof(SmemTrain, gt) % 16 == 0,
+              "training operands must start on 16-byte boundaries");
+
 
 __device__ __forceinline__ int kmo(int r, int k, int K) { return umma::kmajor_offset(r, k, K); }
 
@@ -112,16 +127,24 @@ __device__ __forceinline__ void load_cols(uint32_t tmem, uint32_t col, int count
     for (int c = 0; c < count; c += 16) umma::tmem_ld16(umma::lane_addr(tmem, warp, (int)col + c), out + c);
 }
 
-// stores this thread's row of n values as BF16: K-major into 'a' (row t, K = n) and, when 't_out'
-// is given, transposed into it (row k, K = 128 samples)
+// stores this thread's row of n values (n a multiple of 8) as BF16, rounded to nearest even:
+// K-major into 'a' (row t, K = n), eight values per 16-byte store (8 consecutive k of a row are 16
+// contiguous bytes of a core matrix), and, when 't_out' is given, transposed into it (row k,
+// K = 128 samples)
 __device__ __forceinline__ void store_row(bf16* a, bf16* t_out, const float* v, int n)
 {
     const int t = threadIdx.x;
-    for (int k = 0; k < n; k++)
+    for (int k0 = 0; k0 < n; k0 += 8)
     {
-        const bf16 b = __float2bfloat16(v[k]);
-        a[kmo(t, k, n)] = b;
-        if (t_out) t_out[kmo(k, t, kTile)] = b;
+        uint32_t w[4];
+        for (int j = 0; j < 4; j++)
+        {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v[k0 + 2 * j], v[k0 + 2 * j + 1]);
+            w[j] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        *reinterpret_cast<uint4*>(a + kmo(t, k0, n)) = make_uint4(w[0], w[1], w[2], w[3]);
+        if (t_out)
+            for (int j = 0; j < 8; j++) t_out[kmo(k0 + j, t, kTile)] = __float2bfloat16(v[k0 + j]);
     }
 }
 
@@ -145,13 +168,15 @@ __device__ __forceinline__ void mask_grad(float* g, const uint32_t* mask)
         if (!((mask[k >> 5] >> (k & 31)) & 1u)) g[k] = 0.0f;
 }
 
-// Forward of one tile up to the 48 raw outputs of this thread's row. 'act' holds two ping-pong
-// K-major buffers; 'tr' (training only, else null) receives the transposed inputs of every layer
-// and 'masks' the three ReLU masks. False if a wait gave up.
-__device__ bool forward_tile(uint64_t* mbar, uint32_t tmem, const bf16* w, bf16 (*act)[kTile * kHid],
+// Forward of one tile up to the 48 raw outputs of this thread's row. act0 / act1: the K-major
+// operand buffers of even / odd layers (one buffer may serve both); 'tr' (training only, else
+// null) receives the transposed inputs of every layer and 'masks' the three ReLU masks. False if
+// a wait gave up.
+__device__ bool forward_tile(uint64_t* mbar, uint32_t tmem, const bf16* w, bf16* act0, bf16* act1,
                              bf16 (*tr)[kHid * kTile], const Net& net, bool valid, V3 p, V3 n, V3 view, float* raw,
                              uint32_t (*masks)[2], uint32_t& phase)
 {
+    bf16* const act[2] = {act0, act1};
     {
         float feat[kGridFeatures], x[kIn];
         const Domain d = {{net.lo[0], net.lo[1], net.lo[2]}, {net.inv_ext[0], net.inv_ext[1], net.inv_ext[2]}};
@@ -219,7 +244,7 @@ __global__ void __launch_bounds__(kTile) train_kernel(Net net, Batch b, const fl
         }
         float raw[kOut];
         uint32_t masks[3][2];
-        ok = forward_tile(&sm.mbar, tmem, sm.w, sm.act, sm.tr, net, valid, p, nn, vw, raw, masks, phase);
+        ok = forward_tile(&sm.mbar, tmem, sm.w, sm.act[0], sm.act[1], sm.tr, net, valid, p, nn, vw, raw, masks, phase);
         if (!ok) break;
         // head, loss and its gradient for this row -> dY (K-major, K = 48) and dY^T
         {
@@ -317,7 +342,7 @@ __global__ void __launch_bounds__(kTile) infer_kernel(Net net, Batch b, float* _
             vw = load3(b.view, row);
         }
         float raw[kOut];
-        ok = forward_tile(&sm.mbar, tmem, sm.w, sm.act, nullptr, net, valid, p, nn, vw, raw, nullptr, phase);
+        ok = forward_tile(&sm.mbar, tmem, sm.w, sm.act, sm.act, nullptr, net, valid, p, nn, vw, raw, nullptr, phase);
         if (!ok) break;
         if (valid)
         {
@@ -480,7 +505,7 @@ cudaError_t launch_guide_infer(const Net& net, const Batch& b, float* lobes, int
         attr_set = true;
     }
     const int64_t tiles = (b.n_max + kTile - 1) / kTile;
-    const int64_t cap = (int64_t)n_sm * 3;  // three 62 KB CTAs fit one SM
+    const int64_t cap = (int64_t)n_sm * kInferCtasPerSm;
     const int grid = (int)(tiles < cap ? (tiles < 1 ? 1 : tiles) : cap);
     infer_kernel<<<grid, kTile, sizeof(SmemInfer), st>>>(net, b, lobes, err);
     return cudaGetLastError();

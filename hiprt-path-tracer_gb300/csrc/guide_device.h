@@ -83,7 +83,9 @@ __device__ __forceinline__ void encode(const Domain& d, const uint32_t* __restri
 {
     float u[3];
     unit_coords(d, p, u);
-#pragma unroll 4
+    // fully unrolled: the level resolutions and the dense / hashed choice become constants and
+    // the 128 gathers can be issued together
+#pragma unroll
     for (int l = 0; l < kLevels; l++)
     {
         const int res = level_res(l);

@@ -297,6 +297,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
         V3 light_contrib = v3(0, 0, 0);
         float light_target = 0.0f;  // RIS: target function of the kept light candidate
         float4 bsdf_pending = make_float4(0, 0, 0, 0);
+        float guide_pdf_out = 0.0f;  // MIS pdf of this vertex's continuation when it is guided
         int next_medium = -1;
         Pcg32 rng;
         rng.inc = pcg_inc(rc.seed);
@@ -317,7 +318,20 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             const int mat = __ldg(s.material_of + prim);
             tp = xyz(pb.throughput[slot]);
             V3 L = v3(0, 0, 0);
-            if (bounce == 0) L = xyz(s.materials[mat].emission);
+            if (bounce == 0)
+                L = xyz(s.materials[mat].emission);
+            else if (pb.guide_pdf)
+            {
+                // the previous vertex's guided continuation is next-event estimation's BSDF
+                // technique there: the emission it found here, weighted against light sampling
+                const float gprev = pb.guide_pdf[slot];
+                const V3 Le = xyz(s.materials[mat].emission);
+                if (gprev > 0.0f && !is_black(Le))
+                {
+                    const float lp = emitter_hit_pdf(s, rc, prim, Le, hit.x, d);
+                    if (lp > 0.0f) L = tp * Le * balance_heuristic(gprev, lp);
+                }
+            }
 
             if constexpr (!PRINCIPLED)
             {
@@ -434,13 +448,9 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                         f = lambert_eval(albedo, dot(ns, wi), p_bsdf);
                         pdf = is_black(f) ? 0.0f : alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * p_bsdf;
                         rec_pb = p_bsdf;
-                        if (pdf > 0.0f && s.n_emissive > 0)
-                        {
-                            // the BSDF-technique ray of next-event estimation, along the continuation
-                            want_bsdf = true;
-                            bs_d = f4(wi, 1.0e35f - 1.0e-4f);
-                            bsdf_pending = f4(tp * (f * fabsf(dot(ns, wi)) / pdf), pdf);
-                        }
+                        // next-event estimation's BSDF technique is the continuation itself: the
+                        // emission its extension ray finds is weighted at the next vertex
+                        if (pdf > 0.0f && s.n_emissive > 0) guide_pdf_out = pdf;
                     }
                     else
                     {
@@ -671,13 +681,9 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                         }
                         pdf = is_black(f) ? 0.0f : alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * p_bsdf;
                         rec_pb = p_bsdf;
-                        if (pdf > 0.0f && s.n_emissive > 0 && !restir_vertex)
-                        {
-                            // the BSDF-technique ray of next-event estimation, along the continuation
-                            want_bsdf = true;
-                            bs_d = f4(wi, 1.0e35f - 1.0e-4f);
-                            bsdf_pending = f4(tp * (f * fabsf(dot(ns, wi)) / pdf), pdf);
-                        }
+                        // next-event estimation's BSDF technique is the continuation itself (not on
+                        // the ReSTIR DI bounce, whose reservoirs replace it)
+                        if (pdf > 0.0f && s.n_emissive > 0 && !restir_vertex) guide_pdf_out = pdf;
                     }
                     else
                     {
@@ -754,6 +760,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             next.slot[ni] = slot;
             pb.throughput[slot] = f4(tp, 0.0f);
             if (PRINCIPLED) pb.medium[slot] = next_medium;
+            if (pb.guide_pdf) pb.guide_pdf[slot] = guide_pdf_out;
         }
         if (gv.train_entry)  // uniform: every lane of the warp takes the branch
         {

@@ -106,6 +106,7 @@ struct gbpt_renderer
     DevMem guide_mem;
     gbpt::GuideView gv;  // gv.lobes == nullptr: off
     float* guide_lobes = nullptr;
+    float* guide_pdf = nullptr;  // per path: MIS pdf of the last guided continuation
     // envmap direct lighting: per-path entries and the any-hit queue (allocated once the scene's
     // envmap is importance sampled)
     DevMem env_mem;
@@ -797,6 +798,7 @@ gbpt_status gbpt_pass_shade(gbpt_renderer* r, int32_t bounce, void* stream)
     if (env_st != GBPT_OK) return env_st;
     gbpt::PathBuffers pb = r->pb;
     if (!scene_env_sampled(r->scene)) pb.env_entry = nullptr;  // envmap direct lighting off
+    pb.guide_pdf = r->guide_pdf;  // null without a guide
     cudaError_t e = gbpt::launch_shade(r->scene->view, r->rc, pb, in, r->q[r->cur ^ 1], r->shadow, r->bsdfq, r->envq,
                                        bounce, r->capacity, r->stats, restir, gv, r->n_sm, cs);
     r->cur ^= 1;
@@ -1163,6 +1165,7 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
     std::memset(&r->gv, 0, sizeof(r->gv));
     r->guide = nullptr;
     r->guide_lobes = nullptr;
+    r->guide_pdf = nullptr;
     if (!g || !s || !s->enabled) return GBPT_OK;
     if (!(s->guide_probability >= 0.0f && s->guide_probability < 1.0f))
         return set_error(GBPT_ERROR_INVALID_ARG, "guide_probability must be in [0, 1)");
@@ -1176,6 +1179,7 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
     gv.in_nrm = M.alloc<float>(3 * cap);
     gv.in_view = M.alloc<float>(3 * cap);
     r->guide_lobes = M.alloc<float>((int64_t)GBPT_GUIDE_ROW * cap);
+    r->guide_pdf = M.alloc<float>(cap);
     gv.prob = s->guide_probability;
     if (s->train)
     {
@@ -1214,6 +1218,7 @@ gbpt_status gbpt_renderer_set_guide(gbpt_renderer* r, gbpt_guide* g, const gbpt_
         M.release();
         std::memset(&r->gv, 0, sizeof(r->gv));
         r->guide_lobes = nullptr;
+        r->guide_pdf = nullptr;
         return e == cudaErrorMemoryAllocation ? set_error(GBPT_ERROR_OOM, "guiding buffers") : cuda_error(e, "guiding buffers");
     }
     gv.lobes = r->guide_lobes;

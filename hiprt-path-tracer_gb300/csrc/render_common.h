@@ -92,6 +92,10 @@ struct PathBuffers
     float4* ris;            // RIS vertex: throughput before the continuation (rgb) and the light
                             // candidates' weight sum (w); w = -0.5: RIS without light candidates,
                             // w = -1: not a RIS vertex
+    // guided rendering (null otherwise): the one-sample MIS pdf of each path's last continuation
+    // when it was a guided continuation (which doubles as next-event estimation's BSDF technique),
+    // else 0; emission found by the next extension ray is weighted against light sampling with it
+    float* guide_pdf;
     // environment-map direct lighting (null when the scene's envmap is not importance sampled):
     // the envmap sample's and the separate BSDF sample's contributions, each waiting on its
     // any-hit ray in the envmap queue

@@ -107,6 +107,28 @@ __device__ __forceinline__ LightSample sample_light(const SceneView& s, const Re
     return ls;
 }
 
+// Solid-angle pdf with which light sampling would have chosen the point at distance 'dist' on
+// emissive triangle 'prim' (emission Le, one-sided: 0 seen from behind) along unit direction wi
+// (pdf_of_emissive_triangle_hit_area_measure, LightUtils.h:52-77, to solid angle,
+// PDFConversion.h:19-38); 0 when the triangle is not seen from its front
+__device__ __forceinline__ float emitter_hit_pdf(const SceneView& s, const RenderConst& rc, int prim, V3 Le, float dist,
+                                                 V3 wi)
+{
+    V3 a, b, c;
+    load_triangle(s, prim, a, b, c);
+    const V3 nrm = cross(b - a, c - a);
+    const float len = length(nrm);
+    const float cos_l = fmaxf(0.0f, dot(nrm / len, -wi));
+    if (!(cos_l > 0.0f)) return 0.0f;
+    const float area = 0.5f * len;
+    float pdf_area = 1.0f / area;
+    if (rc.light_sampling == GBPT_LIGHT_POWER)
+        pdf_area *= (luminance(Le) * area) / s.power_sum;
+    else
+        pdf_area /= (float)s.n_emissive;
+    return area_to_solid_angle_pdf(pdf_area, dist, cos_l);
+}
+
 // Balance heuristic with sample counts as the reference writes it (Sampling.h:103-116): the count
 // of technique a is left out of the numerator because RIS divides it out again.
 __device__ __forceinline__ float balance_counts(float pdf_a, float n_a, float pdf_b, float n_b)
