@@ -215,10 +215,13 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
                 8 frames with the camera orbiting 0.5 degrees per frame, 3 indirect bounces, power
                 light sampling, ReSTIR DI (32 light + 1 BSDF candidates, visibility reuse, M-cap 20,
                 1 spatial pass of 5 neighbours in 30 px).
-    guided      the same scene at guided_res, 8 bounces, 64 spp per image: plain BSDF sampling against
-                learned guiding (training online every launch, its time included), both over 4
-                independent 64-spp images after a 64-spp warm-up; relMSE against a 2048-spp plain FP64
-                image. time_to_equal_relmse_speedup = (relMSE x time) plain / (relMSE x time) guided.
+    guided      the same scene at guided_res, 8 bounces, 64 x 1 spp per image, ReSTIR DI at the primary
+                vertex in both arms (configs[2]'s plain method): plain continuations against learned
+                guiding (training online every launch, its time included), both over 4 consecutive
+                64-spp images after a 64-launch warm-up; relMSE against a 2048-spp plain FP64 image.
+                time_to_equal_relmse_speedup = (relMSE x time) plain / (relMSE x time) guided. Also the
+                relMSE of the primary vertex's direct light alone (0 bounces, against a direct-only
+                reference) and its share of the full image's relMSE.
     """
     import torch
     import gbpt
@@ -304,36 +307,54 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
                      "mrays_per_s_traced": rays / (tot * 1e-3) / 1e6}
     del r
 
-    # ---- guided against plain ----
+    # ---- guided against plain, both with ReSTIR DI at the primary vertex (configs[2]'s plain
+    # method; the guide acts on the continuations and on later bounces' BSDF technique) ----
     W, H = guided_res
     ref = gbpt.Renderer(scene, settings(W, H, 64, 8, 1000))
     ref.render(32)
     torch.cuda.synchronize()
     gref = ref.image_sums()[1] / 2048
     del ref
-    plain = []
-    for k in range(4):
-        p = gbpt.Renderer(scene, settings(W, H, 4, 8, 100 + k))
-        t = timed(lambda: p.render(16))
-        plain.append((t, _relmse(p.image_sums()[1] / 64, gref)))
-        del p
-    g = gbpt.Renderer(scene, settings(W, H, 4, 8, 200))
-    gd = guide.Guide(scene_min=S.box[0], scene_max=S.box[1])
-    g.set_guide(gd, guide_render_settings())
-    g.render(16)
-    guided = []
-    for k in range(4):
-        torch.cuda.synchronize()
-        prev = g.image_sums()[1]
-        t = timed(lambda: g.render(16))
-        guided.append((t, _relmse((g.image_sums()[1] - prev) / 64, gref)))
+    rs = restir_di_settings(light_candidates=32, bsdf_candidates=1, m_cap=20, spatial_passes=1, spatial_neighbors=5,
+                            spatial_radius=30)
+
+    def arm(guided, seed, nb=8, ref_img=None, images=4):
+        r = gbpt.Renderer(scene, settings(W, H, 1, nb, seed))
+        r.set_restir_di(rs)
+        gd = None
+        if guided:
+            gd = guide.Guide(scene_min=S.box[0], scene_max=S.box[1])
+            r.set_guide(gd, guide_render_settings())
+        r.render(64)  # warm-up: temporal reservoirs and, guided, 64 training steps
+        res = []
+        for _ in range(images):
+            torch.cuda.synchronize()
+            prev = r.image_sums()[1]
+            t = timed(lambda: r.render(64))
+            res.append((t, _relmse((r.image_sums()[1] - prev) / 64, gref if ref_img is None else ref_img)))
+        return res, gd
+
+    plain, _ = arm(False, 100)
+    guided, gd = arm(True, 200)
+    # how much of the error the primary vertex's direct light carries: the same estimator with no
+    # bounce, against a direct-only reference
+    dref = gbpt.Renderer(scene, settings(W, H, 64, 0, 1001))
+    dref.render(32)
+    torch.cuda.synchronize()
+    direct_ref = dref.image_sums()[1] / 2048
+    del dref
+    direct, _ = arm(False, 300, nb=0, ref_img=direct_ref, images=2)
     tp, ep = np.mean([a for a, _ in plain]), np.mean([b for _, b in plain])
     tg, eg = np.mean([a for a, _ in guided]), np.mean([b for _, b in guided])
-    out["guided"] = {"config": f"many-light scene, {W}x{H}, 8 bounces, 64 spp per image, power NEE + MIS; guide: 16-level "
-                               "hash grid + 3x64 MLP, 8 vMF lobes + learned selection, 2^18 records/launch, Adam 1e-2",
+    out["guided"] = {"config": f"many-light scene, {W}x{H}, 8 bounces, 64 x 1 spp per image, ReSTIR DI at the primary vertex "
+                               "(32+1 candidates, M-cap 20, 1 spatial pass x 5 in 30 px) and power NEE + MIS after it "
+                               "in both arms; guide: 16-level hash grid + 3x64 MLP, 8 vMF lobes + learned selection, "
+                               "2^18 records/launch, Adam 1e-2; relMSE vs a 2048-spp plain FP64 image",
                      "plain_ms": tp, "plain_relmse": ep, "guided_ms": tg, "guided_relmse": eg,
                      "plain_relmse_each": [b for _, b in plain], "guided_relmse_each": [b for _, b in guided],
-                     "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg), "guide_error_flag": gd.error_flag()}
+                     "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg), "guide_error_flag": gd.error_flag(),
+                     "primary_direct_only_relmse": float(np.mean([b for _, b in direct])),
+                     "primary_direct_share_of_relmse": float(np.mean([b for _, b in direct])) / ep}
     # ---- guided against plain on the indirectly lit Cornell box ----
     out["guided_indirect_cornell"] = guided_indirect_cornell(timed)
     del scene
