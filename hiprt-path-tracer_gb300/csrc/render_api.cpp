@@ -97,6 +97,7 @@ struct gbpt_renderer
     gbpt::GBuffer gb[2];
     int gb_cur = 0;
     gbpt::ReservoirBuf res[5];  // initial, temporal, spatial ping, spatial pong, previous
+    float4* presampled = nullptr;  // light presampling records (null: off)
     int res_final = 0;
     bool has_prev = false;
     float prev_inverse_view[16];
@@ -813,6 +814,8 @@ gbpt_status gbpt_pass_bounce(gbpt_renderer* r, int32_t bounce, void* stream)
 
 namespace {
 
+uint32_t spatial_seed(uint32_t frame, int pass, uint32_t seed);
+
 gbpt::RestirConst restir_const(const gbpt_renderer* r)
 {
     const gbpt_restir_di_settings& k = r->restir_settings;
@@ -839,6 +842,15 @@ gbpt::RestirConst restir_const(const gbpt_renderer* r)
     c.has_prev = r->has_prev ? 1 : 0;
     camera_position(r->rc.inverse_view, c.camera_pos);
     camera_position(r->prev_inverse_view, c.prev_camera_pos);
+    if (r->presampled)
+    {
+        c.presampled = r->presampled;
+        c.presample_subsets = k.presampling_subsets;
+        c.presample_size = k.presampling_subset_size;
+        c.presample_tile = k.presampling_tile_size;
+        // the frame's subset seed: the spatial-seed hash at a pass index no spatial pass uses
+        c.presample_seed = spatial_seed(c.frame, 31, c.seed);
+    }
     return c;
 }
 
@@ -883,6 +895,11 @@ gbpt_status gbpt_restir_di_default_settings(gbpt_restir_di_settings* s)
     s->do_final_shading_visibility = 1;
     s->normal_similarity_cos = 0.906307787f;
     s->plane_distance_threshold = 0.1f;
+    s->do_fused_spatiotemporal = 0;
+    s->do_light_presampling = 0;
+    s->presampling_subsets = 128;
+    s->presampling_subset_size = 1024;
+    s->presampling_tile_size = 8;
     return GBPT_OK;
 }
 
@@ -892,6 +909,7 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
     r->restir_mem.release();
     r->restir = false;
     r->has_prev = false;
+    r->presampled = nullptr;
     r->rc.restir_final_visibility = 0;
     if (!k->enabled) return GBPT_OK;
     if (r->rc.bsdf != GBPT_BSDF_PRINCIPLED) return set_error(GBPT_ERROR_INVALID_ARG, "ReSTIR DI needs GBPT_BSDF_PRINCIPLED");
@@ -902,8 +920,15 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
     if (k->do_spatial && (k->spatial_neighbors < 1 || k->spatial_neighbors > 32 || k->spatial_passes < 1 ||
                           k->spatial_passes > 16 || !(k->spatial_radius > 0.0f)))
         return set_error(GBPT_ERROR_INVALID_ARG, "spatial settings out of range (1..32 neighbours, 1..16 passes)");
-    if (k->do_temporal && (k->temporal_search_count < 0 || k->temporal_search_count > 64))
+    if ((k->do_temporal || k->do_fused_spatiotemporal) && (k->temporal_search_count < 0 || k->temporal_search_count > 64))
         return set_error(GBPT_ERROR_INVALID_ARG, "temporal_search_count out of range");
+    if (k->do_fused_spatiotemporal && (k->spatial_neighbors < 1 || k->spatial_neighbors > 32 || k->spatial_passes < 1 ||
+                                       k->spatial_passes > 16 || !(k->spatial_radius > 0.0f)))
+        return set_error(GBPT_ERROR_INVALID_ARG, "spatial settings out of range (1..32 neighbours, 1..16 passes)");
+    if (k->do_light_presampling &&
+        (k->presampling_subsets < 1 || k->presampling_subset_size < 1 || k->presampling_tile_size < 1 ||
+         (int64_t)k->presampling_subsets * k->presampling_subset_size > ((int64_t)1 << 24)))
+        return set_error(GBPT_ERROR_INVALID_ARG, "light presampling sizes out of range (at most 2^24 records)");
     const int64_t npix = (int64_t)r->rc.width * r->rc.height;
     DevMem& M = r->restir_mem;
     for (int g = 0; g < 2; g++)
@@ -917,6 +942,9 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
         r->res[b].s = M.alloc<float4>(npix);
         r->res[b].w = M.alloc<int4>(npix);
     }
+    r->presampled = k->do_light_presampling
+                        ? M.alloc<float4>(2 * (size_t)k->presampling_subsets * k->presampling_subset_size)
+                        : nullptr;
     cudaError_t e = M.err;
     for (int b = 0; b < 5 && e == cudaSuccess; b++)
     {
@@ -926,6 +954,7 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
     if (e != cudaSuccess)
     {
         M.release();
+        r->presampled = nullptr;
         return cuda_error(e, "ReSTIR DI buffers");
     }
     r->restir_settings = *k;
@@ -952,9 +981,11 @@ gbpt_status gbpt_pass_restir_di_initial(gbpt_renderer* r, void* stream)
     cudaStream_t cs = (cudaStream_t)stream;
     const int64_t npix = (int64_t)r->rc.width * r->rc.height;
     const gbpt::GBuffer& gb = r->gb[r->gb_cur];
+    const gbpt::RestirConst k = restir_const(r);
     cudaError_t e = gbpt::launch_restir_gbuffer(r->scene->view, r->q[r->cur], gb, npix, r->n_sm, cs);
-    if (e == cudaSuccess)
-        e = gbpt::launch_restir_initial(r->scene->view, r->rc, restir_const(r), gb, r->res[0], r->n_sm, cs);
+    if (e == cudaSuccess && r->presampled)
+        e = gbpt::launch_restir_presample(r->scene->view, r->rc, k, r->presampled, r->n_sm, cs);
+    if (e == cudaSuccess) e = gbpt::launch_restir_initial(r->scene->view, r->rc, k, gb, r->res[0], r->n_sm, cs);
     r->res_final = 0;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI initial candidates");
 }
@@ -970,6 +1001,19 @@ gbpt_status gbpt_pass_restir_di_temporal(gbpt_renderer* r, void* stream)
                                                  r->res[0], r->res[4], r->res[1], r->n_sm, (cudaStream_t)stream);
     r->res_final = 1;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI temporal reuse");
+}
+
+gbpt_status gbpt_pass_restir_di_spatiotemporal(gbpt_renderer* r, void* stream)
+{
+    gbpt_status st = restir_ready(r);
+    if (st != GBPT_OK) return st;
+    gbpt::RestirConst k = restir_const(r);
+    if (!view_projection(r->prev_inverse_view, r->rc.inverse_projection, k.prev_view_projection))
+        return set_error(GBPT_ERROR_INVALID_ARG, "the previous camera matrices are singular");
+    cudaError_t e = gbpt::launch_restir_spatiotemporal(r->scene->view, r->rc, k, r->gb[r->gb_cur], r->gb[r->gb_cur ^ 1],
+                                                       r->res[0], r->res[4], r->res[2], r->n_sm, (cudaStream_t)stream);
+    r->res_final = 2;
+    return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI spatiotemporal reuse");
 }
 
 gbpt_status gbpt_pass_restir_di_spatial(gbpt_renderer* r, int32_t pass_index, void* stream)
@@ -1045,9 +1089,18 @@ gbpt_status gbpt_render(gbpt_renderer* r, int32_t n_launches, void* stream)
         {
             st = gbpt_pass_extend(r, 0, stream);
             if (st == GBPT_OK) st = gbpt_pass_restir_di_initial(r, stream);
-            if (st == GBPT_OK && r->restir_settings.do_temporal) st = gbpt_pass_restir_di_temporal(r, stream);
-            for (int p = 0; st == GBPT_OK && r->restir_settings.do_spatial && p < r->restir_settings.spatial_passes; p++)
-                st = gbpt_pass_restir_di_spatial(r, p, stream);
+            if (r->restir_settings.do_fused_spatiotemporal)
+            {
+                if (st == GBPT_OK) st = gbpt_pass_restir_di_spatiotemporal(r, stream);
+                for (int p = 1; st == GBPT_OK && p < r->restir_settings.spatial_passes; p++)
+                    st = gbpt_pass_restir_di_spatial(r, p, stream);
+            }
+            else
+            {
+                if (st == GBPT_OK && r->restir_settings.do_temporal) st = gbpt_pass_restir_di_temporal(r, stream);
+                for (int p = 0; st == GBPT_OK && r->restir_settings.do_spatial && p < r->restir_settings.spatial_passes; p++)
+                    st = gbpt_pass_restir_di_spatial(r, p, stream);
+            }
             if (st == GBPT_OK) st = gbpt_pass_shade(r, 0, stream);
         }
         for (int b = r->restir ? 1 : 0; st == GBPT_OK && b <= r->rc.nb_bounces; b++) st = gbpt_pass_bounce(r, b, stream);

@@ -81,11 +81,18 @@ cudaError_t launch_guide_inputs(const SceneView& s, const Queue& in, const Guide
 cudaError_t launch_guide_weights(const PathBuffers& pb, const GuideView& gv, int n_sm, cudaStream_t st);
 cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int n_sm,
                                   cudaStream_t st);
+// Light presampling of the frame into out (2 float4 per record, k.presample_subsets * size records)
+cudaError_t launch_restir_presample(const SceneView& s, const RenderConst& rc, const RestirConst& k, float4* out,
+                                    int n_sm, cudaStream_t st);
 cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                   const ReservoirBuf& out, int n_sm, cudaStream_t st);
 cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                    const GBuffer& gb_prev, const ReservoirBuf& initial, const ReservoirBuf& prev,
                                    const ReservoirBuf& out, int n_sm, cudaStream_t st);
+// Fused spatiotemporal reuse: initial + previous final reservoirs (and G-buffers) -> out
+cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& rc, const RestirConst& k,
+                                         const GBuffer& gb, const GBuffer& gb_prev, const ReservoirBuf& initial,
+                                         const ReservoirBuf& prev, const ReservoirBuf& out, int n_sm, cudaStream_t st);
 cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                   const ReservoirBuf& in, const ReservoirBuf& out, int pass, uint32_t neighbor_seed,
                                   int n_sm, cudaStream_t st);

@@ -200,6 +200,37 @@ __device__ __forceinline__ int spatial_neighbor(int idx, int count, int cx, int 
 }
 
 // ---------------------------------------------------------------------------------------------
+// light presampling (ReSTIR_DI_LightsPresampling, src/Device/kernels/ReSTIR/DI/LightsPresampling.h:
+// 74-109; use_presampled_light_candidate, InitialCandidates.h:33-69): once per frame, subsets of
+// light samples drawn from the scene's light distribution; a pixel's light candidates come from
+// the subset its tile draws, so neighbouring pixels read the same few kilobytes of light data
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) presample_kernel(SceneView s, RenderConst rc, RestirConst k, float4* out)
+{
+    const int n = k.presample_subsets * k.presample_size;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        Pcg32 rng = pcg_seed((uint32_t)i, k.frame, k.seed ^ 0x5BD1E995u);
+        const LightSample ls = sample_light(s, rc, rng);
+        out[2 * i] = f4(ls.point, __int_as_float(ls.triangle));
+        out[2 * i + 1] = f4(ls.normal, ls.pdf_area);
+    }
+}
+
+// the frame's subset for the tile of pixel (x, y): Cantor pairing of the tile coordinates scales
+// the frame's seed of a Xorshift32 draw
+__device__ __forceinline__ int presampled_subset(const RestirConst& k, int x, int y)
+{
+    const uint32_t tx = (uint32_t)(x / k.presample_tile), ty = (uint32_t)(y / k.presample_tile);
+    const uint32_t cantor = (tx + ty + 1u) * (tx + ty) / 2u + ty;
+    uint32_t seed = k.presample_seed * (cantor + 1u);
+    if (seed == 0u) seed = 0x9E3779B9u;
+    bsdf::Xorshift32 xr{seed};
+    const int i = (int)(xr() * (float)k.presample_subsets);
+    return min(i, k.presample_subsets - 1);
+}
+
+// ---------------------------------------------------------------------------------------------
 // G-buffer from the camera hits (CameraRays, src/Device/kernels/CameraRays.h:178-201)
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuffer gb)
@@ -255,10 +286,24 @@ __global__ void __launch_bounds__(128) initial_kernel(SceneView s, RenderConst r
         const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
         const bsdf::Medium md = medium_of(su, m);
         const float nl = (float)k.light_candidates, nb = (float)k.bsdf_candidates;
+        const int subset = k.presampled ? presampled_subset(k, pixel % rc.width, pixel / rc.width) : 0;
 
         for (int c = 0; c < k.light_candidates; c++)
         {
-            const LightSample ls = sample_light(s, rc, rng);
+            LightSample ls;
+            if (k.presampled)
+            {
+                // a light of the tile's presampled subset, with the pdf it was drawn with
+                const int e = subset * k.presample_size + rng.index(k.presample_size);
+                const float4 a = __ldg(k.presampled + 2 * e), b = __ldg(k.presampled + 2 * e + 1);
+                ls.point = xyz(a);
+                ls.triangle = __float_as_int(a.w);
+                ls.normal = xyz(b);
+                ls.pdf_area = b.w;
+                ls.emission = emission_of(s, ls.triangle);
+            }
+            else
+                ls = sample_light(s, rc, rng);
             V3 wi = ls.point - su.P;
             const float dist = length(wi);
             wi = wi / dist;
@@ -509,6 +554,141 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// fused spatiotemporal reuse (FusedSpatiotemporalReuse.h:152-566, pairwise MIS
+// SpatiotemporalMISWeight.h:140-224): the temporal neighbour, then K spatial neighbours from the
+// previous frame's final reservoirs around the backprojected position (heuristics and MIS surfaces
+// from the previous G-buffer), then the canonical initial reservoir, in one pass. The temporal
+// neighbour is one more member of the pairwise MIS set. Neighbour offsets: a Xorshift32 stream
+// seeded per pixel by one draw of the pixel's stream. As in the reference's fused kernel, an
+// emissive temporal neighbour is resampled.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                             GBuffer gb_prev, ReservoirBuf initial, ReservoirBuf prev,
+                                                             ReservoirBuf out)
+{
+    const int W = rc.width, H = rc.height, n_pix = W * H;
+    const bool hc = rc.ggx_height_correlated != 0;
+    const int K = k.spatial_neighbors;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        const Reservoir init = load_reservoir(initial, pixel);
+        const Surface su = load_surface(gb, pixel, k.camera_pos);
+        if (su.prim < 0 || !k.has_prev)
+        {
+            store_reservoir(out, pixel, init);
+            continue;
+        }
+        Pcg32 rng = pass_stream(k, pixel, 2);
+        uint32_t nseed = rng.next_u32();
+        if (nseed == 0u) nseed = 0x9E3779B9u;
+        const V3 ndc = mat_x_point(k.prev_view_projection, su.P);
+        const float px = (ndc.x + 1.0f) * 0.5f * (float)W - 0.5f;
+        const float py = (ndc.y + 1.0f) * 0.5f * (float)H - 0.5f;
+        const int tx0 = (int)roundf(px), ty0 = (int)roundf(py);
+        int t_idx = -1;
+        for (int i = 0; i < k.temporal_search_count + 1; i++)
+        {
+            float ox = 0.0f, oy = 0.0f;
+            if (i > 0)
+            {
+                ox = (rng.next() - 0.5f) * k.temporal_search_radius;
+                oy = (rng.next() - 0.5f) * k.temporal_search_radius;
+            }
+            const int tx = (int)roundf(px + ox), ty = (int)roundf(py + oy);
+            if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
+            t_idx = tx + ty * W;
+            if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, k)) break;
+            t_idx = -1;
+        }
+        const Reservoir tn = t_idx >= 0 ? load_reservoir(prev, t_idx) : empty_reservoir();
+        const bool t_ok = t_idx >= 0 && tn.M > 0;
+        // valid spatial neighbours and their confidence (count_valid_spatiotemporal_neighbors)
+        bsdf::Xorshift32 nrng{nseed};
+        int valid = 0, m_sum = 0;
+        uint32_t cache = 0;
+        for (int j = 0; j < K; j++)
+        {
+            const int idx = spatial_neighbor(j, K, tx0, ty0, W, H, k.spatial_radius, nrng);
+            if (idx < 0) continue;
+            if (!similar(gb_prev, gb, idx, pixel, su.P, su.ng, k)) continue;
+            m_sum += load_reservoir(prev, idx).M;
+            valid++;
+            cache |= 1u << j;
+        }
+        if (t_ok)
+        {
+            valid++;
+            m_sum += tn.M;
+        }
+        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bool vis = k.bias_correction_visibility != 0;
+        const bool update_mc = init.M > 0 && init.ucw > 0.0f;
+        const float cM = k.confidence_weights ? (float)init.M : 1.0f;
+        const float nsum = k.confidence_weights ? (float)m_sum : 1.0f;
+        const float div = k.confidence_weights ? 1.0f : (float)valid;
+        float mc = 0.0f;
+        // pairwise MIS weight of a neighbour reservoir (surface nsu), accumulating the canonical one
+        auto pairwise = [&](const Reservoir& nb, float t_at_center, int n_idx) {
+            const float rM = k.confidence_weights ? (float)nb.M : 1.0f;
+            const float denom = nb.p_hat * nsum + t_at_center / div * cM;
+            const float mi = denom == 0.0f ? 0.0f : nb.p_hat * rM / denom;
+            if (update_mc)
+            {
+                const Surface nsu = load_surface(gb_prev, n_idx, k.prev_camera_pos);
+                const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
+                const float c_at_n = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, vis);
+                const float nume_mc = init.p_hat / div * cM;
+                const float denom_mc = c_at_n * nsum + init.p_hat / div * cM;
+                const float conf = k.confidence_weights ? (nsum == 0.0f ? 0.0f : rM / nsum) : 1.0f;
+                if (denom_mc != 0.0f) mc += nume_mc / denom_mc / div * conf;
+            }
+            return mi / div;
+        };
+        Reservoir o = empty_reservoir();
+        if (t_ok)
+        {
+            const float t_at_center = tn.ucw > 0.0f ? target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, vis) : 0.0f;
+            const float mis = pairwise(tn, t_at_center, t_idx);
+            if (combine_with(o, tn, mis, t_at_center, 1.0f, rng))
+            {
+                if (vis)
+                    o.flags |= kRestirFlagUnoccluded;
+                else
+                    o.flags &= ~kRestirFlagUnoccluded;
+            }
+        }
+        nrng = bsdf::Xorshift32{nseed};
+        for (int j = m_sum == 0 ? K : 0; j < K + 1; j++)
+        {
+            if (j < K && !(cache & (1u << j)))
+            {
+                nrng();
+                nrng();
+                continue;
+            }
+            const int idx = j == K ? pixel : spatial_neighbor(j, K, tx0, ty0, W, H, k.spatial_radius, nrng);
+            if (idx < 0) continue;
+            const Reservoir nb = j == K ? init : load_reservoir(prev, idx);
+            float t_at_center = 0.0f;
+            if (nb.ucw > 0.0f)
+                t_at_center = j == K ? nb.p_hat : target_function(s, hc, su, m, nb.point, nb.tri, nb.flags, false);
+            const float mis = j < K ? pairwise(nb, t_at_center, idx) : (mc == 0.0f ? 1.0f : mc);
+            if (combine_with(o, nb, mis, t_at_center, 1.0f, rng))
+            {
+                if (j == K)
+                    o.flags |= nb.flags & kRestirFlagUnoccluded;
+                else
+                    o.flags &= ~kRestirFlagUnoccluded;
+            }
+        }
+        end_with_normalization(o, 1.0f, 1.0f);
+        if (k.visibility_reuse && vis) visibility_kill(s, o, su);
+        if (k.m_cap > 0) o.M = min(o.M, k.m_cap);
+        store_reservoir(out, pixel, o);
+    }
+}
+
 inline int grid_for(int64_t n, int threads, int max_blocks)
 {
     int64_t b = (n + threads - 1) / threads;
@@ -526,6 +706,15 @@ cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuf
     return cudaGetLastError();
 }
 
+cudaError_t launch_restir_presample(const SceneView& s, const RenderConst& rc, const RestirConst& k, float4* out,
+                                    int n_sm, cudaStream_t st)
+{
+    const int64_t n = (int64_t)k.presample_subsets * k.presample_size;
+    if (n <= 0 || s.n_emissive <= 0) return cudaSuccess;
+    presample_kernel<<<grid_for(n, 256, n_sm * 8), 256, 0, st>>>(s, rc, k, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                   const ReservoirBuf& out, int n_sm, cudaStream_t st)
 {
@@ -540,6 +729,15 @@ cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, co
 {
     const int64_t n = (int64_t)rc.width * rc.height;
     temporal_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, gb_prev, initial, prev, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& rc, const RestirConst& k,
+                                         const GBuffer& gb, const GBuffer& gb_prev, const ReservoirBuf& initial,
+                                         const ReservoirBuf& prev, const ReservoirBuf& out, int n_sm, cudaStream_t st)
+{
+    const int64_t n = (int64_t)rc.width * rc.height;
+    spatiotemporal_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, gb_prev, initial, prev, out);
     return cudaGetLastError();
 }
 

@@ -46,6 +46,12 @@ struct RestirConst
     float camera_pos[3];
     float prev_camera_pos[3];
     float prev_view_projection[16];
+    // light presampling (null: off): presample_subsets x presample_size records of two float4,
+    // (point on the light, triangle bits) and (light normal, area pdf); the pixels of a
+    // presample_tile^2 block share the subset that presample_seed picks for the frame
+    const float4* presampled;
+    int32_t presample_subsets, presample_size, presample_tile;
+    uint32_t presample_seed;
 };
 
 #ifdef __CUDACC__

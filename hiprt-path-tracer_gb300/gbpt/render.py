@@ -56,7 +56,8 @@ class RestirDISettingsC(ctypes.Structure):
                 ("spatial_radius", ctypes.c_float), ("m_cap", i32), ("use_confidence_weights", i32),
                 ("bias_correction_visibility", i32), ("do_final_shading_visibility", i32),
                 ("normal_similarity_cos", ctypes.c_float), ("plane_distance_threshold", ctypes.c_float),
-                ("reserved", i32 * 15)]
+                ("do_fused_spatiotemporal", i32), ("do_light_presampling", i32), ("presampling_subsets", i32),
+                ("presampling_subset_size", i32), ("presampling_tile_size", i32), ("reserved", i32 * 10)]
 
 
 RESERVOIRS_INITIAL, RESERVOIRS_TEMPORAL, RESERVOIRS_FINAL, RESERVOIRS_PREVIOUS = 0, 1, 2, 3
@@ -100,6 +101,7 @@ RENDER_SIGNATURES = [
     ("gbpt_pass_restir_di_initial", ctypes.c_int, [c_vp, c_vp]),
     ("gbpt_pass_restir_di_temporal", ctypes.c_int, [c_vp, c_vp]),
     ("gbpt_pass_restir_di_spatial", ctypes.c_int, [c_vp, i32, c_vp]),
+    ("gbpt_pass_restir_di_spatiotemporal", ctypes.c_int, [c_vp, c_vp]),
     ("gbpt_restir_di_get_reservoirs", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
     ("gbpt_restir_di_set_reservoirs", ctypes.c_int, [c_vp, i32, c_vp, c_vp]),
     ("gbpt_guide_render_default_settings", ctypes.c_int, [c_vp]),
@@ -397,6 +399,9 @@ class Renderer:
 
     def pass_restir_temporal(self, stream=None):
         _lib.check(self._lib.gbpt_pass_restir_di_temporal(self._h, _stream(stream)))
+
+    def pass_restir_spatiotemporal(self, stream=None):
+        _lib.check(self._lib.gbpt_pass_restir_di_spatiotemporal(self._h, _stream(stream)))
 
     def pass_restir_spatial(self, pass_index: int = 0, stream=None):
         _lib.check(self._lib.gbpt_pass_restir_di_spatial(self._h, pass_index, _stream(stream)))

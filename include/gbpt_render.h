@@ -120,8 +120,8 @@ typedef struct gbpt_world_desc {
 /* Fills *w with the reference's defaults: no ambient light, identity rotation, intensity 1, alias
  * table sampling with BSDF MIS, nearest-texel lookups. */
 GBPT_API gbpt_status gbpt_world_default(gbpt_world_desc* w);
-/* Sets the scene's world; renderers of the scene see it from their next launch (a batch created
- * before the call keeps the world it captured). For an envmap the library packs the texels to
+/* Sets the scene's world; renderers of the scene see it from their next launch. Fails with
+ * GBPT_ERROR_INVALID_ARG while a batch renders the scene (destroy the batch first). For an envmap the library packs the texels to
  * RGB9E5 and, on the device, takes each texel's luminance from the float input, their FP64 sum,
  * the FP64 running sum over texels stored as float (the binary-search CDF) and the Vose alias
  * table of the luminances normalised by the FP64 sum (Image32Bit::compute_cdf and
@@ -215,7 +215,8 @@ GBPT_API gbpt_status gbpt_renderer_get_stats(gbpt_renderer* r, gbpt_render_stats
  * defaults in brackets). Requires GBPT_BSDF_PRINCIPLED and samples_per_launch = 1: one launch is
  * one frame, whose final reservoirs feed the next frame's temporal pass. Always on: visibility
  * reuse in the final reservoirs' shadow test, pairwise MIS bias correction, geometric-normal and
- * plane-distance neighbour heuristics, no envmap or light presampling. */
+ * plane-distance neighbour heuristics; the envmap is not a ReSTIR candidate (vertices sample it
+ * on their own). */
 typedef struct gbpt_restir_di_settings {
     int32_t enabled;
     int32_t light_candidates;           /* number_of_initial_light_candidates [4] */
@@ -234,7 +235,12 @@ typedef struct gbpt_restir_di_settings {
     int32_t do_final_shading_visibility;/* [1] */
     float normal_similarity_cos;        /* normal_similarity_angle_precomp [0.906307787] */
     float plane_distance_threshold;     /* [0.1] */
-    int32_t reserved[15];
+    int32_t do_fused_spatiotemporal;    /* do_fused_spatiotemporal: one pass of temporal + spatial reuse [0] */
+    int32_t do_light_presampling;       /* ReSTIR_DI_DoLightPresampling [0] */
+    int32_t presampling_subsets;        /* light_presampling.number_of_subsets [128] */
+    int32_t presampling_subset_size;    /* light_presampling.subset_size [1024] */
+    int32_t presampling_tile_size;      /* light_presampling.tile_size, pixels [8] */
+    int32_t reserved[10];
 } gbpt_restir_di_settings;
 
 /* Fills 's' with the reference's defaults (enabled = 1). */
@@ -249,7 +255,9 @@ GBPT_API gbpt_status gbpt_renderer_set_camera(gbpt_renderer* r, const float* inv
 /* Pass-level scheduling with ReSTIR DI (what gbpt_render does per launch):
  *   gbpt_pass_camera_rays, gbpt_pass_extend(0), gbpt_pass_restir_di_initial,
  *   gbpt_pass_restir_di_temporal, gbpt_pass_restir_di_spatial(0..passes-1), gbpt_pass_shade(0),
- *   gbpt_pass_bounce(1..nb_bounces), gbpt_pass_accumulate (which also ends the frame).
+ *   gbpt_pass_bounce(1..nb_bounces), gbpt_pass_accumulate (which also ends the frame);
+ *   with do_fused_spatiotemporal, gbpt_pass_restir_di_spatiotemporal then
+ *   gbpt_pass_restir_di_spatial(1..passes-1) replace the temporal and spatial passes.
  * extend = closest hit of the bounce's queue; shade = shading, shadow and BSDF-light rays and
  * their resolve (gbpt_pass_bounce = extend + shade). */
 GBPT_API gbpt_status gbpt_pass_extend(gbpt_renderer* r, int32_t bounce, void* stream);
@@ -261,6 +269,11 @@ GBPT_API gbpt_status gbpt_pass_restir_di_initial(gbpt_renderer* r, void* stream)
 GBPT_API gbpt_status gbpt_pass_restir_di_temporal(gbpt_renderer* r, void* stream);
 /* ReSTIR_DI_SpatialReuse (src/Device/kernels/ReSTIR/DI/SpatialReuse.h:43), pass 'pass_index'. */
 GBPT_API gbpt_status gbpt_pass_restir_di_spatial(gbpt_renderer* r, int32_t pass_index, void* stream);
+/* ReSTIR_DI_SpatiotemporalReuse (src/Device/kernels/ReSTIR/DI/FusedSpatiotemporalReuse.h:152): the
+ * temporal neighbour and the spatial neighbours (taken from the previous frame's final reservoirs
+ * around the backprojected position) and the initial candidates resampled in one pass; its output
+ * is the final reservoirs (spatial pass 0). */
+GBPT_API gbpt_status gbpt_pass_restir_di_spatiotemporal(gbpt_renderer* r, void* stream);
 
 enum {
     GBPT_RESERVOIRS_INITIAL = 0,

@@ -482,7 +482,11 @@ def _restir_lib():
                                            ctypes.c_int, ctypes.c_int, _c_f, _c_f, _c_f, ctypes.c_int]
         lib.orc_restir_pass.argtypes = [ctypes.c_int, _c_f, ctypes.c_int, _c_i, _c_f, _c_i, ctypes.c_int, _c_f, _c_i,
                                         ctypes.c_float, _c_f, ctypes.c_void_p, ctypes.c_void_p, _c_i, _c_f, _c_f,
-                                        _c_f, _c_f, _c_f, _c_f, _c_f, ctypes.c_int, ctypes.c_uint32, ctypes.c_int]
+                                        _c_f, _c_f, _c_f, _c_f, _c_f, ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
+                                        _c_f, _c_i]
+        lib.orc_restir_presample.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, _c_i, ctypes.c_int, _c_f, _c_i,
+                                             ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
+                                             ctypes.c_uint32, _c_f]
         lib._restir_sigs = True
     return lib
 
@@ -502,11 +506,33 @@ def restir_gbuffer(soup, material_of, pmats, width, height, seed, frame, jitter,
     return gb
 
 
+def restir_presample(scene, strategy, subsets, size, frame, seed) -> np.ndarray:
+    """The oracle's light presampling records of a frame, (subsets * size, 8) float32."""
+    lib = _restir_lib()
+    soup = np.ascontiguousarray(scene["soup"], np.float32)
+    mo = np.ascontiguousarray(scene["material_of"], np.int32)
+    em = np.ascontiguousarray(scene["emission"], np.float32)
+    ei = np.ascontiguousarray(scene["emissive"], np.int32)
+    ap = np.ascontiguousarray(scene["alias_prob"], np.float32)
+    ai = np.ascontiguousarray(scene["alias_idx"], np.int32)
+    out = np.zeros((subsets * size, 8), np.float32)
+    lib.orc_restir_presample(_ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(em, _c_f), _ptr(ei, _c_i), len(ei),
+                             _ptr(ap, _c_f), _ptr(ai, _c_i), float(scene["power_sum"]), int(strategy), subsets * size,
+                             frame, seed, _ptr(out, _c_f))
+    return out
+
+
+def restir_presample_seed(frame: int, seed: int) -> int:
+    """The frame's presampled-subset seed (the library's spatial seed hash at pass index 31)."""
+    return restir_spatial_seed(frame, 31, seed)
+
+
 def restir_pass(pass_kind, scene, pmats, settings_i, settings_f, prev_vp, gb, gb_prev=None, inp=None, prev=None,
-                spatial_index=0, spatial_seed=0, nthreads=0) -> np.ndarray:
-    """One ReSTIR DI pass of the oracle (0 initial, 1 temporal, 2 spatial) shading with the
-    reference's own BSDF; scene = dict(soup, material_of, emission, emissive, alias_prob, alias_idx,
-    power_sum). Returns (W*H, 8) reservoir records."""
+                spatial_index=0, spatial_seed=0, nthreads=0, presampled=None, presample_i=None) -> np.ndarray:
+    """One ReSTIR DI pass of the oracle (0 initial, 1 temporal, 2 spatial, 3 fused spatiotemporal)
+    shading with the reference's own BSDF; scene = dict(soup, material_of, emission, emissive,
+    alias_prob, alias_idx, power_sum). presampled / presample_i (subsets, size, tile, seed): light
+    presampling for the initial pass. Returns (W*H, 8) reservoir records."""
     lib = _restir_lib()
     ref = ctypes.CDLL(REF_SO)
     eval_fn = ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value
@@ -528,10 +554,13 @@ def restir_pass(pass_kind, scene, pmats, settings_i, settings_f, prev_vp, gb, gb
     prev_ = np.ascontiguousarray(prev if prev is not None else z, np.float32)
     out = np.zeros((n, 8), np.float32)
     gb = np.ascontiguousarray(gb, np.float32)
+    ps_ = None if presampled is None else np.ascontiguousarray(presampled, np.float32)
+    pi_ = None if presample_i is None else np.array([int(v) & 0xFFFFFFFF for v in presample_i], np.uint32).view(np.int32)
     lib.orc_restir_pass(pass_kind, _ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(em, _c_f), _ptr(ei, _c_i),
                         len(ei), _ptr(ap, _c_f), _ptr(ai, _c_i), float(scene["power_sum"]), _ptr(pm, _c_f), eval_fn,
                         sample_fn, _ptr(si, _c_i), _ptr(sf, _c_f), _ptr(vp, _c_f), _ptr(gb, _c_f), _ptr(gbp, _c_f),
-                        _ptr(inp_, _c_f), _ptr(prev_, _c_f), _ptr(out, _c_f), spatial_index, spatial_seed, nthreads)
+                        _ptr(inp_, _c_f), _ptr(prev_, _c_f), _ptr(out, _c_f), spatial_index, spatial_seed, nthreads,
+                        _ptr(ps_, _c_f), _ptr(pi_, _c_i))
     return out
 
 

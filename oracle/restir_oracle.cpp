@@ -98,6 +98,11 @@ struct RSettings
     float temporal_radius, spatial_radius, normal_cos, plane_dist;
     float cam[3], prev_cam[3];
     const float* prev_vp;
+    // light presampling (presampled null: off): records of 8 floats (point, triangle bits,
+    // normal, area pdf), 'subsets' x 'size' of them; tiles of 'tile' pixels share a subset
+    const float* presampled = nullptr;
+    int subsets = 0, size = 0, tile = 8;
+    uint32_t presample_seed = 0;
 };
 
 struct Surf
@@ -258,6 +263,36 @@ LS sample_light(const Scene& s, int strategy, Pcg& rng)
     return ls;
 }
 
+// Light presampling (ReSTIR_DI_LightsPresampling, src/Device/kernels/ReSTIR/DI/
+// LightsPresampling.h:74-109): record i is a light sample from its own PCG stream
+// pcg_seed(i, frame, seed ^ 0x5BD1E995), as the GPU kernel draws it.
+void presample(const Scene& s, int strategy, int n, uint32_t frame, uint32_t seed, float* out)
+{
+    for (int i = 0; i < n; i++)
+    {
+        Pcg rng = pcg_seed((uint32_t)i, frame, seed ^ 0x5BD1E995u);
+        LS ls = sample_light(s, strategy, rng);
+        float* o = out + 8 * (size_t)i;
+        o[0] = ls.point.x; o[1] = ls.point.y; o[2] = ls.point.z;
+        std::memcpy(o + 3, &ls.tri, 4);
+        o[4] = ls.normal.x; o[5] = ls.normal.y; o[6] = ls.normal.z;
+        o[7] = ls.pdf_area;
+    }
+}
+
+// the frame's subset for the tile of pixel (x, y) (use_presampled_light_candidate,
+// InitialCandidates.h:33-69): Cantor pairing of the tile coordinates scales the frame's seed
+int presampled_subset(const RSettings& st, int x, int y)
+{
+    const uint32_t tx = (uint32_t)(x / st.tile), ty = (uint32_t)(y / st.tile);
+    const uint32_t cantor = (tx + ty + 1u) * (tx + ty) / 2u + ty;
+    uint32_t seed = st.presample_seed * (cantor + 1u);
+    if (seed == 0u) seed = 0x9E3779B9u;
+    Xor32 xr{seed};
+    const int i = (int)(xr.next() * (float)st.subsets);
+    return std::min(i, st.subsets - 1);
+}
+
 Res initial_pixel(const Ctx& c, const float* gb, int pixel)
 {
     Res r;
@@ -266,9 +301,22 @@ Res initial_pixel(const Ctx& c, const float* gb, int pixel)
     Pcg rng = stream(c.st, pixel, 1);
     const float* m = c.ps.mat(su.mat);
     const float nl = (float)c.st.n_light, nb = (float)c.st.n_bsdf;
+    const int subset = c.st.presampled ? presampled_subset(c.st, pixel % c.st.width, pixel / c.st.width) : 0;
     for (int k = 0; k < c.st.n_light; k++)
     {
-        LS ls = sample_light(c.s, c.st.light_strategy, rng);
+        LS ls;
+        if (c.st.presampled)
+        {
+            const int e = subset * c.st.size + rng.index(c.st.size);
+            const float* p = c.st.presampled + 8 * (size_t)e;
+            ls.point = mk(p[0], p[1], p[2]);
+            std::memcpy(&ls.tri, p + 3, 4);
+            ls.normal = mk(p[4], p[5], p[6]);
+            ls.pdf_area = p[7];
+            ls.emission = c.s.emi(ls.tri);
+        }
+        else
+            ls = sample_light(c.s, c.st.light_strategy, rng);
         V wi = ls.point - su.P;
         float dist = len(wi);
         wi = wi / dist;
@@ -482,6 +530,128 @@ Res spatial_pixel(const Ctx& c, const float* gb, const float* in, int pixel, int
     return o;
 }
 
+// Fused spatiotemporal reuse (ReSTIR_DI_SpatiotemporalReuse, src/Device/kernels/ReSTIR/DI/
+// FusedSpatiotemporalReuse.h:152-566; pairwise MIS SpatiotemporalMISWeight.h:140-224): one pass
+// that resamples the temporal neighbour, then K spatial neighbours taken from the PREVIOUS frame's
+// final reservoirs around the backprojected position (positions for the heuristics and surfaces
+// for the MIS terms from the previous G-buffer), then the canonical initial reservoir. The
+// temporal neighbour counts as one more neighbour of the pairwise MIS set (its M joins the
+// confidence sum). Neighbour offsets come from a Xorshift32 stream seeded per pixel by one draw of
+// the pixel's stream (the reference seeds it per pixel in this pass); visibility reuse on the
+// output; M-cap. As in the reference's fused kernel, an emissive temporal neighbour is resampled.
+Res spatiotemporal_pixel(const Ctx& c, const float* gb, const float* gb_prev, const float* initial, const float* prev,
+                         int pixel)
+{
+    const Res init = load_res(initial, pixel);
+    const Surf su = load_surf(gb, pixel, c.st.cam);
+    if (su.prim < 0 || !c.st.has_prev) return init;
+    Pcg rng = stream(c.st, pixel, 2);
+    uint32_t nseed = rng.u32();
+    if (nseed == 0u) nseed = 0x9E3779B9u;
+    const int W = c.st.width, H = c.st.height, K = c.st.spatial_neighbors;
+    V ndc = mat_point(c.st.prev_vp, su.P);
+    float px = (ndc.x + 1.0f) * 0.5f * (float)W - 0.5f;
+    float py = (ndc.y + 1.0f) * 0.5f * (float)H - 0.5f;
+    const int tx0 = (int)std::round(px), ty0 = (int)std::round(py);
+    int t_idx = -1;
+    for (int i = 0; i < c.st.temporal_search + 1; i++)
+    {
+        float ox = 0.0f, oy = 0.0f;
+        if (i > 0)
+        {
+            ox = (rng.next() - 0.5f) * c.st.temporal_radius;
+            oy = (rng.next() - 0.5f) * c.st.temporal_radius;
+        }
+        int tx = (int)std::round(px + ox), ty = (int)std::round(py + oy);
+        if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
+        t_idx = tx + ty * W;
+        if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, c.st)) break;
+        t_idx = -1;
+    }
+    Res tn;
+    if (t_idx >= 0) tn = load_res(prev, t_idx);
+    const bool t_ok = t_idx >= 0 && tn.M > 0;
+    // valid spatial neighbours and their confidence
+    Xor32 nr{nseed};
+    int valid = 0, m_sum = 0;
+    uint32_t cache = 0;
+    for (int j = 0; j < K; j++)
+    {
+        int idx = spatial_neighbor(j, K, tx0, ty0, W, H, c.st.spatial_radius, nr);
+        if (idx < 0) continue;
+        if (!similar(gb_prev, gb, idx, pixel, su.P, su.ng, c.st)) continue;
+        m_sum += load_res(prev, idx).M;
+        valid++;
+        cache |= 1u << j;
+    }
+    if (t_ok)
+    {
+        valid++;
+        m_sum += tn.M;
+    }
+    const bool vis = c.st.bias_vis != 0;
+    const bool update_mc = init.M > 0 && init.ucw > 0.0f;
+    const float cM = c.st.confidence ? (float)init.M : 1.0f;
+    const float nsum = c.st.confidence ? (float)m_sum : 1.0f;
+    const float div = c.st.confidence ? 1.0f : (float)valid;
+    float mc = 0.0f;
+    // pairwise MIS weight of a neighbour reservoir, accumulating the canonical weight
+    auto pairwise = [&](const Res& nb, float t_at_center, const Surf& nsu) {
+        float rM = c.st.confidence ? (float)nb.M : 1.0f;
+        float denom = nb.p_hat * nsum + t_at_center / div * cM;
+        float mi = denom == 0.0f ? 0.0f : nb.p_hat * rM / denom;
+        if (update_mc)
+        {
+            float c_at_n = target(c, nsu, init.point, init.tri, init.flags, vis);
+            float nume_mc = init.p_hat / div * cM;
+            float denom_mc = c_at_n * nsum + init.p_hat / div * cM;
+            float conf = c.st.confidence ? (nsum == 0.0f ? 0.0f : rM / nsum) : 1.0f;
+            if (denom_mc != 0.0f) mc += nume_mc / denom_mc / div * conf;
+        }
+        return mi / div;
+    };
+    Res o;
+    if (t_ok)
+    {
+        const float t_at_center = tn.ucw > 0.0f ? target(c, su, tn.point, tn.tri, tn.flags, vis) : 0.0f;
+        const float mis = pairwise(tn, t_at_center, load_surf(gb_prev, t_idx, c.st.prev_cam));
+        if (combine(o, tn, mis, t_at_center, rng))
+        {
+            if (vis)
+                o.flags |= kUnoccluded;
+            else
+                o.flags &= ~kUnoccluded;
+        }
+    }
+    nr = Xor32{nseed};
+    for (int j = m_sum == 0 ? K : 0; j < K + 1; j++)
+    {
+        if (j < K && !(cache & (1u << j)))
+        {
+            nr.next();
+            nr.next();
+            continue;
+        }
+        const int idx = j == K ? pixel : spatial_neighbor(j, K, tx0, ty0, W, H, c.st.spatial_radius, nr);
+        if (idx < 0) continue;
+        const Res nb = j == K ? init : load_res(prev, idx);
+        float t_at_center = 0.0f;
+        if (nb.ucw > 0.0f) t_at_center = j == K ? nb.p_hat : target(c, su, nb.point, nb.tri, nb.flags, false);
+        const float mis = j < K ? pairwise(nb, t_at_center, load_surf(gb_prev, idx, c.st.prev_cam)) : (mc == 0.0f ? 1.0f : mc);
+        if (combine(o, nb, mis, t_at_center, rng))
+        {
+            if (j == K)
+                o.flags |= nb.flags & kUnoccluded;
+            else
+                o.flags &= ~kUnoccluded;
+        }
+    }
+    end_norm(o);
+    if (c.st.visibility_reuse && vis) visibility_kill(c, o, su);
+    if (c.st.m_cap > 0) o.M = std::min(o.M, c.st.m_cap);
+    return o;
+}
+
 template <typename F>
 void parallel_pixels(int n, int nthreads, F f)
 {
@@ -591,7 +761,10 @@ void orc_restir_gbuffer(const float* tri_verts, int n_tris, const int* mat_of, c
 
 /* One ReSTIR DI pass over all pixels. pass: 0 = initial (out <- candidates), 1 = temporal
  * (in = initial, prev = previous final reservoirs, gb_prev = previous G-buffer), 2 = spatial pass
- * 'spatial_index' (in -> out) with the given neighbour seed.
+ * 'spatial_index' (in -> out) with the given neighbour seed, 3 = fused spatiotemporal (in =
+ * initial, prev = previous final reservoirs, gb_prev = previous G-buffer).
+ * presampled (NULL: off): light presampling records (orc_restir_presample) with presample_i =
+ * subsets, subset size, tile size, the frame's subset seed (bits).
  * settings_i: width, height, seed, frame, has_prev, light strategy (0 uniform, 1 power), light
  *   candidates, bsdf candidates, visibility reuse, do temporal, temporal search count, spatial
  *   passes, spatial neighbours, m cap, confidence weights, bias-correction visibility.
@@ -601,11 +774,20 @@ void orc_restir_pass(int pass, const float* tri_verts, int n_tris, const int* ma
                      const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx, float power_sum,
                      const float* pmats, void* eval_fn, void* sample_fn, const int* settings_i, const float* settings_f,
                      const float* prev_vp, const float* gb, const float* gb_prev, const float* in, const float* prev,
-                     float* out, int spatial_index, uint32_t spatial_seed, int nthreads)
+                     float* out, int spatial_index, uint32_t spatial_seed, int nthreads, const float* presampled,
+                     const int* presample_i)
 {
     Scene s{tri_verts, n_tris, mat_of, nullptr, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
     PScene ps{pmats, (bsdf_eval_fn)eval_fn, (bsdf_sample_fn)sample_fn};
     RSettings st = settings_from(settings_i, settings_f, prev_vp);
+    if (presampled)
+    {
+        st.presampled = presampled;
+        st.subsets = presample_i[0];
+        st.size = presample_i[1];
+        st.tile = presample_i[2];
+        st.presample_seed = (uint32_t)presample_i[3];
+    }
     Ctx c{s, ps, st};
     const int n = st.width * st.height;
     parallel_pixels(n, nthreads, [&](int pixel) {
@@ -614,10 +796,21 @@ void orc_restir_pass(int pass, const float* tri_verts, int n_tris, const int* ma
             r = initial_pixel(c, gb, pixel);
         else if (pass == 1)
             r = temporal_pixel(c, gb, gb_prev, in, prev, pixel);
+        else if (pass == 3)
+            r = spatiotemporal_pixel(c, gb, gb_prev, in, prev, pixel);
         else
             r = spatial_pixel(c, gb, in, pixel, spatial_index, st.spatial_passes - 1, spatial_seed);
         store_res(out, pixel, r);
     });
+}
+
+/* Light presampling records of a frame: n = subsets * size records of 8 floats. */
+void orc_restir_presample(const float* tri_verts, int n_tris, const int* mat_of, const float* emission,
+                          const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx,
+                          float power_sum, int strategy, int n, uint32_t frame, uint32_t seed, float* out)
+{
+    Scene s{tri_verts, n_tris, mat_of, nullptr, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
+    presample(s, strategy, n, frame, seed, out);
 }
 
 }  // extern "C"

@@ -6,6 +6,9 @@ Per frame it stores the camera G-buffer and the reservoirs after the initial-can
 and spatial passes; frame 1 moves the camera by half a degree so that the temporal pass
 backprojects. The GPU test runs the same passes (same PCG streams and Xorshift32 BSDF seeds) and,
 separately, each reuse pass on these stored input reservoirs ("given identical candidates").
+Also: the fused spatiotemporal pass of frame 1 on frame 1's initial and frame 0's final
+reservoirs (fused_f1), and frame 0's initial candidates drawn from presampled lights
+(PRESAMPLE subsets x size, tiles of 8 pixels; ps_f0_initial).
 Usage (where the reference tree is present):  python tests/golden/make_restir_golden.py
 """
 import math
@@ -35,6 +38,7 @@ RESTIR_I = dict(light_candidates=8, bsdf_candidates=1, do_visibility_reuse=1, do
                 spatial_passes=1, spatial_neighbors=5, m_cap=20, use_confidence_weights=1, bias_correction_visibility=1)
 RESTIR_F = dict(temporal_search_radius=4.0, spatial_radius=8.0, normal_similarity_cos=0.906307787,
                 plane_distance_threshold=0.1)
+PRESAMPLE = dict(presampling_subsets=16, presampling_subset_size=64, presampling_tile_size=8)
 
 
 def scene():
@@ -146,6 +150,15 @@ def main():
         valid = final[:, 7] > 0
         print(f"frame {frame}: hit {np.mean(gb[:, 3].view(np.int32) >= 0):.2f}, valid reservoirs {valid.mean():.2f}, "
               f"mean M {final[:, 5].view(np.int32).__rshift__(9).mean():.2f}")
+        if frame == 0:
+            recs = pyoracle.restir_presample(sc, 1, PRESAMPLE["presampling_subsets"],
+                                             PRESAMPLE["presampling_subset_size"], frame, SEED)
+            pi = (PRESAMPLE["presampling_subsets"], PRESAMPLE["presampling_subset_size"],
+                  PRESAMPLE["presampling_tile_size"], pyoracle.restir_presample_seed(frame, SEED))
+            out["ps_f0_initial"] = pyoracle.restir_pass(0, sc, eff, si, sf, vp, gb, presampled=recs, presample_i=pi)
+        else:
+            out["fused_f1"] = pyoracle.restir_pass(3, sc, eff, si, sf, vp, gb, gb_prev=prev_gb, inp=init,
+                                                   prev=prev_final)
         prev_gb, prev_final, prev_iv = gb, final, iv
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT}")

@@ -135,3 +135,90 @@ def test_restir_direct_lighting_unbiased_against_nee(cuda):
     batches = frames.reshape(16, 16).mean(axis=1)
     sigma = batches.std(ddof=1) / np.sqrt(len(batches))
     assert abs(frames.mean() - want.mean()) < 4 * sigma + 2e-3 * want.mean(), (frames.mean(), want.mean(), sigma)
+
+
+def _frame_fused(r, g, frame, inject=None):
+    """One frame with the fused spatiotemporal pass; returns the initial and final reservoirs."""
+    r.set_camera(g[f"f{frame}_inverse_view"], g[f"f{frame}_inverse_projection"])
+    r.pass_camera_rays()
+    r.pass_extend(0)
+    r.pass_restir_initial()
+    out = {"initial": r.reservoirs(render.RESERVOIRS_INITIAL)}
+    if inject is not None:
+        r.set_reservoirs(render.RESERVOIRS_INITIAL, inject["initial"])
+        r.set_reservoirs(render.RESERVOIRS_PREVIOUS, inject["previous"])
+    r.pass_restir_spatiotemporal()
+    out["final"] = r.reservoirs(render.RESERVOIRS_FINAL)
+    r.pass_shade(0)
+    r.pass_accumulate()
+    torch.cuda.synchronize()
+    return out
+
+
+def test_fused_spatiotemporal_matches_oracle_on_given_candidates(cuda):
+    """ReSTIR_DI_SpatiotemporalReuse (FusedSpatiotemporalReuse.h): frame 1's fused pass on frame 1's
+    initial and frame 0's final reservoirs of the oracle, against the oracle's fused output."""
+    g = np.load(GOLDEN)
+    scene, _ = _renderer(g)
+    st = RenderSettings(width=W, height=H, samples_per_launch=1, nb_bounces=0, light_sampling=LIGHT_POWER,
+                        bsdf=BSDF_PRINCIPLED, seed=SEED, inverse_view=g["f0_inverse_view"],
+                        inverse_projection=g["f0_inverse_projection"])
+    r = gbpt.Renderer(scene, st)
+    r.set_restir_di(render.restir_di_settings(**RESTIR, do_fused_spatiotemporal=1))
+    _frame_fused(r, g, 0)
+    out = _frame_fused(r, g, 1, {"initial": g["f1_initial"], "previous": g["f0_final"]})
+    assert compare_reservoirs(out["final"], g["fused_f1"], 0.99) >= 0.99
+
+
+def test_presampled_initial_candidates_match_oracle(cuda):
+    """Light presampling (ReSTIR_DI_LightsPresampling + use_presampled_light_candidate): frame 0's
+    initial candidates drawn from 16 presampled subsets of 64 lights, tiles of 8 x 8 pixels."""
+    g = np.load(GOLDEN)
+    scene, _ = _renderer(g)
+    st = RenderSettings(width=W, height=H, samples_per_launch=1, nb_bounces=0, light_sampling=LIGHT_POWER,
+                        bsdf=BSDF_PRINCIPLED, seed=SEED, inverse_view=g["f0_inverse_view"],
+                        inverse_projection=g["f0_inverse_projection"])
+    r = gbpt.Renderer(scene, st)
+    r.set_restir_di(render.restir_di_settings(**RESTIR, do_light_presampling=1, presampling_subsets=16,
+                                              presampling_subset_size=64, presampling_tile_size=8))
+    out = _frame_to_reservoirs(r, g, 0)
+    compare_reservoirs(out["initial"], g["ps_f0_initial"], 0.98)
+
+
+@pytest.mark.parametrize("fused,presampled", [(1, 0), (1, 1), (0, 1)])
+def test_fused_and_presampled_restir_unbiased_against_nee(cuda, fused, presampled):
+    """As the separate-pass test: the mean over frames of ReSTIR DI direct lighting with the fused
+    spatiotemporal pass and / or light presampling equals plain NEE + MIS within a few standard
+    errors."""
+    g = np.load(GOLDEN)
+    scene = gbpt.Scene(g["positions"], g["indices"], g["material_of"], principled=g["materials"])
+    base = dict(width=W, height=H, nb_bounces=0, light_sampling=LIGHT_POWER, bsdf=BSDF_PRINCIPLED,
+                inverse_view=g["f0_inverse_view"], inverse_projection=g["f0_inverse_projection"])
+    ref = gbpt.Renderer(scene, RenderSettings(samples_per_launch=1024, seed=99, **base))
+    ref.render(16)
+    torch.cuda.synchronize()
+    want = ref.image_sums()[1] / (1024 * 16)
+    r = gbpt.Renderer(scene, RenderSettings(samples_per_launch=1, seed=7, **base))
+    r.set_restir_di(render.restir_di_settings(**RESTIR, do_fused_spatiotemporal=fused, do_light_presampling=presampled,
+                                              presampling_subsets=16, presampling_subset_size=64))
+    frames, prev = [], np.zeros_like(want)
+    for f in range(256):
+        r.render(1)
+        cur = r.image_sums()[1]
+        frames.append((cur - prev).mean())
+        prev = cur
+    frames = np.array(frames)
+    batches = frames.reshape(16, 16).mean(axis=1)
+    sigma = batches.std(ddof=1) / np.sqrt(len(batches))
+    assert abs(frames.mean() - want.mean()) < 4 * sigma + 2e-3 * want.mean(), (frames.mean(), want.mean(), sigma)
+
+
+def test_restir_settings_validation(cuda):
+    from gbpt import GbptError
+    g = np.load(GOLDEN)
+    _, r = _renderer(g)
+    for bad in (dict(do_light_presampling=1, presampling_subsets=0), dict(do_light_presampling=1, presampling_subset_size=-1),
+                dict(do_light_presampling=1, presampling_subsets=1 << 13, presampling_subset_size=1 << 12),
+                dict(do_fused_spatiotemporal=1, spatial_neighbors=40)):
+        with pytest.raises(GbptError):
+            r.set_restir_di(render.restir_di_settings(**{**RESTIR, **bad}))
