@@ -288,24 +288,32 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
         return RenderSettings(width=w, height=h, samples_per_launch=spp, nb_bounces=nb, light_sampling=LIGHT_POWER,
                               bsdf=BSDF_PRINCIPLED, seed=seed, inverse_view=iv, inverse_projection=ip)
 
-    r = gbpt.Renderer(scene, settings(1920, 1080, 1, 3, 1))
-    r.set_restir_di(restir_di_settings(light_candidates=32, bsdf_candidates=1, m_cap=20, spatial_passes=1,
-                                       spatial_neighbors=5, spatial_radius=30))
-    r.render(3)
-    r.reset()
-    frame_ms = []
-    for f in range(8):
-        iv, ip = look_at_camera(_orbit(S.eye, S.target, 0.5 * f), S.target, vfov_deg=S.vfov_deg, aspect=1920 / 1080)
-        r.set_camera(iv, ip)
-        frame_ms.append(timed(lambda: r.render(1)))
-    st = r.stats()
-    rays = st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
+    def restir_frames(**extra):
+        r = gbpt.Renderer(scene, settings(1920, 1080, 1, 3, 1))
+        r.set_restir_di(restir_di_settings(light_candidates=32, bsdf_candidates=1, m_cap=20, spatial_passes=1,
+                                           spatial_neighbors=5, spatial_radius=30, **extra))
+        r.render(3)
+        r.reset()
+        frame_ms = []
+        for f in range(8):
+            iv, ip = look_at_camera(_orbit(S.eye, S.target, 0.5 * f), S.target, vfov_deg=S.vfov_deg, aspect=1920 / 1080)
+            r.set_camera(iv, ip)
+            frame_ms.append(timed(lambda: r.render(1)))
+        st = r.stats()
+        del r
+        return frame_ms, st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
+
+    frame_ms, rays = restir_frames()
     tot = sum(frame_ms)
+    fused_ms, _ = restir_frames(do_fused_spatiotemporal=1)
+    fused_ps_ms, _ = restir_frames(do_fused_spatiotemporal=1, do_light_presampling=1)
     out["restir"] = {"config": "many-light scene 16.8M + 10k emissive tris, 1920x1080, 8 frames orbiting 0.5 deg, 3 bounces, "
                                "ReSTIR DI 32+1 candidates, visibility reuse, M-cap 20, 1 spatial pass 5 neighbours 30 px",
                      "ms_per_frame": tot / 8, "frame_ms": frame_ms, "samples_per_s": 1920 * 1080 * 8 / (tot * 1e-3),
-                     "mrays_per_s_traced": rays / (tot * 1e-3) / 1e6}
-    del r
+                     "mrays_per_s_traced": rays / (tot * 1e-3) / 1e6,
+                     "fused_spatiotemporal_ms_per_frame": sum(fused_ms) / 8,
+                     "fused_and_light_presampling_ms_per_frame": sum(fused_ps_ms) / 8,
+                     "light_presampling": "128 subsets x 1024 lights, 8x8-pixel tiles"}
 
     # ---- guided against plain, both with ReSTIR DI at the primary vertex (configs[2]'s plain
     # method; the guide acts on the continuations and on later bounces' BSDF technique) ----

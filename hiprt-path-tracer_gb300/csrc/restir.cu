@@ -628,55 +628,65 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
         const float nsum = k.confidence_weights ? (float)m_sum : 1.0f;
         const float div = k.confidence_weights ? 1.0f : (float)valid;
         float mc = 0.0f;
-        // pairwise MIS weight of a neighbour reservoir (surface nsu), accumulating the canonical one
-        auto pairwise = [&](const Reservoir& nb, float t_at_center, int n_idx) {
-            const float rM = k.confidence_weights ? (float)nb.M : 1.0f;
-            const float denom = nb.p_hat * nsum + t_at_center / div * cM;
-            const float mi = denom == 0.0f ? 0.0f : nb.p_hat * rM / denom;
-            if (update_mc)
-            {
-                const Surface nsu = load_surface(gb_prev, n_idx, k.prev_camera_pos);
-                const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
-                const float c_at_n = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, vis);
-                const float nume_mc = init.p_hat / div * cM;
-                const float denom_mc = c_at_n * nsum + init.p_hat / div * cM;
-                const float conf = k.confidence_weights ? (nsum == 0.0f ? 0.0f : rM / nsum) : 1.0f;
-                if (denom_mc != 0.0f) mc += nume_mc / denom_mc / div * conf;
-            }
-            return mi / div;
-        };
+        // One loop over the resampled reservoirs in the reference's order: the temporal neighbour
+        // (j = -1), the spatial neighbours (0..K-1), the canonical initial reservoir (K); each
+        // target-function evaluation has one call site, keeping the kernel's code small.
         Reservoir o = empty_reservoir();
-        if (t_ok)
-        {
-            const float t_at_center = tn.ucw > 0.0f ? target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, vis) : 0.0f;
-            const float mis = pairwise(tn, t_at_center, t_idx);
-            if (combine_with(o, tn, mis, t_at_center, 1.0f, rng))
-            {
-                if (vis)
-                    o.flags |= kRestirFlagUnoccluded;
-                else
-                    o.flags &= ~kRestirFlagUnoccluded;
-            }
-        }
         nrng = bsdf::Xorshift32{nseed};
-        for (int j = m_sum == 0 ? K : 0; j < K + 1; j++)
+        const int first = t_ok ? -1 : (m_sum == 0 ? K : 0);
+        for (int j = first; j < K + 1; j++)
         {
-            if (j < K && !(cache & (1u << j)))
+            if (j == 0 && m_sum == 0) j = K;  // no spatial neighbour to resample: the canonical one
+            if (j >= 0 && j < K && !(cache & (1u << j)))
             {
                 nrng();
                 nrng();
                 continue;
             }
-            const int idx = j == K ? pixel : spatial_neighbor(j, K, tx0, ty0, W, H, k.spatial_radius, nrng);
+            int idx;
+            if (j < 0)
+                idx = t_idx;
+            else if (j == K)
+                idx = pixel;
+            else
+                idx = spatial_neighbor(j, K, tx0, ty0, W, H, k.spatial_radius, nrng);
             if (idx < 0) continue;
-            const Reservoir nb = j == K ? init : load_reservoir(prev, idx);
+            const Reservoir nb = j < 0 ? tn : (j == K ? init : load_reservoir(prev, idx));
             float t_at_center = 0.0f;
             if (nb.ucw > 0.0f)
-                t_at_center = j == K ? nb.p_hat : target_function(s, hc, su, m, nb.point, nb.tri, nb.flags, false);
-            const float mis = j < K ? pairwise(nb, t_at_center, idx) : (mc == 0.0f ? 1.0f : mc);
+                t_at_center = j == K ? nb.p_hat
+                                     : target_function(s, hc, su, m, nb.point, nb.tri, nb.flags, j < 0 && vis);
+            float mis;
+            if (j < K)
+            {
+                // pairwise MIS weight of a neighbour, accumulating the canonical one (mc)
+                const float rM = k.confidence_weights ? (float)nb.M : 1.0f;
+                const float denom = nb.p_hat * nsum + t_at_center / div * cM;
+                const float mi = denom == 0.0f ? 0.0f : nb.p_hat * rM / denom;
+                if (update_mc)
+                {
+                    const Surface nsu = load_surface(gb_prev, idx, k.prev_camera_pos);
+                    const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
+                    const float c_at_n = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, vis);
+                    const float nume_mc = init.p_hat / div * cM;
+                    const float denom_mc = c_at_n * nsum + init.p_hat / div * cM;
+                    const float conf = k.confidence_weights ? (nsum == 0.0f ? 0.0f : rM / nsum) : 1.0f;
+                    if (denom_mc != 0.0f) mc += nume_mc / denom_mc / div * conf;
+                }
+                mis = mi / div;
+            }
+            else
+                mis = mc == 0.0f ? 1.0f : mc;
             if (combine_with(o, nb, mis, t_at_center, 1.0f, rng))
             {
-                if (j == K)
+                if (j < 0)
+                {
+                    if (vis)
+                        o.flags |= kRestirFlagUnoccluded;
+                    else
+                        o.flags &= ~kRestirFlagUnoccluded;
+                }
+                else if (j == K)
                     o.flags |= nb.flags & kRestirFlagUnoccluded;
                 else
                     o.flags &= ~kRestirFlagUnoccluded;
