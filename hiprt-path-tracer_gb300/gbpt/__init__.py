@@ -6,4 +6,5 @@ builds/loads the library, generates seeded synthetic scenes, and wraps the C ent
 from . import scenes  # noqa: F401
 from ._lib import GbptError, load, lib_path  # noqa: F401
 from .trace import BVH, hit_prim  # noqa: F401
-from .render import Batch, Renderer, RenderSettings, Scene, World, cornell_settings, look_at_camera  # noqa: F401
+from .render import (Batch, GltfScene, Renderer, RenderSettings, Scene, World, cornell_settings,  # noqa: F401
+                     load_gltf, look_at_camera)

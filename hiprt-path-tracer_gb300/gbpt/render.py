@@ -10,6 +10,7 @@
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -74,7 +75,17 @@ class WorldDescC(ctypes.Structure):
                 ("envmap_bilinear", i32)]
 
 
+class GltfCameraC(ctypes.Structure):
+    _fields_ = [("present", i32), ("position", ctypes.c_float * 3), ("forward", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3), ("yfov", ctypes.c_float), ("aspect_ratio", ctypes.c_float),
+                ("znear", ctypes.c_float), ("zfar", ctypes.c_float)]
+
+
 RENDER_SIGNATURES = [
+    ("gbpt_gltf_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_vp)]),
+    ("gbpt_gltf_scene_desc", ctypes.c_int, [c_vp, ctypes.POINTER(SceneDesc)]),
+    ("gbpt_gltf_get_camera", ctypes.c_int, [c_vp, ctypes.POINTER(GltfCameraC)]),
+    ("gbpt_gltf_destroy", ctypes.c_int, [c_vp]),
     ("gbpt_scene_create", ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(_lib.BvhParams),
                                          ctypes.POINTER(c_vp), c_vp]),
     ("gbpt_scene_destroy", ctypes.c_int, [c_vp]),
@@ -351,6 +362,64 @@ class Scene:
             self.destroy()
         except Exception:
             pass
+
+
+@dataclass
+class GltfScene:
+    """A glTF 2.0 file read by gbpt_gltf_load: world-space triangles, per-triangle material indices,
+    principled material records (M, 64) and the file's camera (None when it has none)."""
+    positions: np.ndarray
+    indices: np.ndarray
+    material_of_triangle: np.ndarray
+    principled: np.ndarray
+    camera: dict | None
+
+    def create_scene(self, **kw) -> "Scene":
+        return Scene(self.positions, self.indices, self.material_of_triangle, principled=self.principled, **kw)
+
+    def camera_matrices(self, aspect=None, near=0.1, far=100.0):
+        """(inverse_view, inverse_projection) of the file's camera with its vertical field of view
+        (the glTF yfov; the reference's ASSIMP route widens it by 0.425 rad). near/far default to
+        the reference's fixed clip planes (src/Scene/SceneParser.cpp:258-259)."""
+        c = self.camera
+        if c is None:
+            raise ValueError("the glTF scene has no perspective camera")
+        if aspect is None:
+            aspect = c["aspect_ratio"] or 1.0
+        eye = np.asarray(c["position"], np.float64)
+        return look_at_camera(eye, eye + np.asarray(c["forward"], np.float64), c["up"],
+                              vfov_deg=float(np.degrees(c["yfov"])), aspect=aspect, near=near, far=far)
+
+
+def load_gltf(path) -> GltfScene:
+    """Reads a .gltf/.glb file through gbpt_gltf_load (the library's own parser)."""
+    lib = _load()
+    h = c_vp()
+    _lib.check(lib.gbpt_gltf_load(os.fsencode(os.fspath(path)), ctypes.byref(h)))
+    try:
+        d = SceneDesc()
+        _lib.check(lib.gbpt_gltf_scene_desc(h, ctypes.byref(d)))
+        nv, nt, nm = int(d.n_vertices), int(d.n_triangles), int(d.n_materials)
+
+        def copy(ptr, n, dtype):
+            if n == 0:
+                return np.zeros(0, dtype)
+            buf = (ctypes.c_char * (n * np.dtype(dtype).itemsize)).from_address(ptr)
+            return np.frombuffer(buf, dtype).copy()
+
+        pos = copy(d.positions, nv * 3, np.float32).reshape(nv, 3)
+        idx = copy(d.indices, nt * 3, np.int32).reshape(nt, 3)
+        mat = copy(d.material_indices, nt, np.int32)
+        pm = copy(d.principled_materials, nm * 64, np.float32).reshape(nm, 64)
+        cam = GltfCameraC()
+        _lib.check(lib.gbpt_gltf_get_camera(h, ctypes.byref(cam)))
+        camera = None
+        if cam.present:
+            camera = {"position": tuple(cam.position), "forward": tuple(cam.forward), "up": tuple(cam.up),
+                      "yfov": cam.yfov, "aspect_ratio": cam.aspect_ratio, "znear": cam.znear, "zfar": cam.zfar}
+        return GltfScene(pos, idx, mat, pm, camera)
+    finally:
+        lib.gbpt_gltf_destroy(h)
 
 
 class Renderer:

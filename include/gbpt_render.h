@@ -63,6 +63,39 @@ GBPT_API gbpt_status gbpt_scene_get_bvh(const gbpt_scene* scene, const gbpt_bvh*
 GBPT_API gbpt_status gbpt_scene_get_light_table(const gbpt_scene* scene, int32_t* n_emissive, int32_t* emissive,
                                                 float* probas, int32_t* alias, float* power_sum, double* power_sum64);
 
+/* ---- scene ingestion from glTF 2.0 (the reference's sample scenes in data/GLTFs) ----
+ * Replaces SceneParser::parse_scene_file (src/Scene/SceneParser.cpp:19-226, ASSIMP with
+ * aiProcess_PreTransformVertices | aiProcess_Triangulate) and read_material_properties
+ * (SceneParser.cpp:391-438) for this path: a .gltf file with external or base64 buffers; the
+ * default scene's node tree flattened to world space (matrix or TRS); triangle primitives (mode 4),
+ * indexed (u8/u16/u32) or not, float VEC3 positions with any byte stride. Materials follow the
+ * reference's mapping: base colour, metallic and roughness factors (glTF defaults), emissive
+ * factor times KHR_materials_emissive_strength, and, when their extension is present,
+ * KHR_materials_ior, _transmission, _clearcoat (factor, roughness), _specular (factor; tint and
+ * colour to 1) and _volume (attenuation colour and distance); every other field keeps
+ * CPUMaterial's default; then CPUMaterial::make_safe's clamps. Primitives without a material get
+ * the glTF default material, appended after the file's materials. Also a .glb container. Not read:
+ * textures, vertex normals and texture coordinates (the renderer shades with geometric normals),
+ * skins and morph targets (the base mesh is loaded); sparse accessors, non-float positions and
+ * unknown required extensions are errors. Triangle order is node traversal order (ASSIMP's
+ * pre-transform step groups meshes by material instead). A KHR_materials_sheen material loads
+ * with sheen = 1, as the reference maps it, which gbpt_scene_create then rejects. */
+typedef struct gbpt_gltf gbpt_gltf;
+typedef struct gbpt_gltf_camera {
+    int32_t present;                 /* 1 when a node of the scene carries a perspective camera */
+    float position[3], forward[3], up[3]; /* world space, from the first camera node's transform */
+    float yfov;                      /* radians (the glTF value; the reference's ASSIMP route adds 0.425) */
+    float aspect_ratio;              /* 0 when the file gives none */
+    float znear, zfar;
+} gbpt_gltf_camera;
+
+GBPT_API gbpt_status gbpt_gltf_load(const char* path, gbpt_gltf** out);
+/* The loaded scene as a scene description (principled materials only; pointers owned by 'g',
+ * valid until gbpt_gltf_destroy) for gbpt_scene_create. */
+GBPT_API gbpt_status gbpt_gltf_scene_desc(const gbpt_gltf* g, gbpt_scene_desc* out);
+GBPT_API gbpt_status gbpt_gltf_get_camera(const gbpt_gltf* g, gbpt_gltf_camera* out);
+GBPT_API gbpt_status gbpt_gltf_destroy(gbpt_gltf* g);
+
 /* Largest emitter count gbpt_alias_table_build_noalloc accepts. */
 #define GBPT_ALIAS_NOALLOC_MAX_EMITTERS 131072
 
