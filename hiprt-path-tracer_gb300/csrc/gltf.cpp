@@ -482,6 +482,22 @@ struct Mat4
         for (int row = 0; row < 3; ++row)
             out[row] = m[row] * v[0] + m[4 + row] * v[1] + m[8 + row] * v[2];
     }
+    // The inverse transpose of the 3x3 part (cofactors over the determinant) in the 3x3 corner.
+    Mat4 inverse_transpose3() const
+    {
+        auto at = [&](int r, int c) { return m[c * 4 + r]; };
+        const double det = det3();
+        Mat4 out;
+        if (det == 0.0)
+            return out;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+                // cofactor C(r, c); (M^-1)^T = C / det
+                out.m[c * 4 + r] = (at(r1, c1) * at(r2, c2) - at(r1, c2) * at(r2, c1)) / det;
+            }
+        return out;
+    }
     double det3() const
     {
         return m[0] * (m[5] * m[10] - m[9] * m[6]) - m[4] * (m[1] * m[10] - m[9] * m[2])
@@ -682,11 +698,11 @@ public:
     }
 
     // Float VEC3 elements of an accessor (positions).
-    std::vector<float> vec3f(int64_t index) const
+    std::vector<float> vec3f(int64_t index, const char* what) const
     {
         const Accessor& a = accessors.at(size_t(index));
         if (a.component != 5126 || a.width != 3)
-            fail("glTF: POSITION must be a float VEC3 accessor", GBPT_ERROR_UNSUPPORTED);
+            fail(std::string("glTF: ") + what + " must be a float VEC3 accessor", GBPT_ERROR_UNSUPPORTED);
         std::vector<float> out(a.count * 3, 0.0f);
         if (a.view < 0)
             return out;
@@ -864,6 +880,7 @@ gbpt_principled_material material_from_gltf(const Json& mat)
 struct gbpt_gltf
 {
     std::vector<float> positions;          // world space, 3 per vertex
+    std::vector<float> normals;            // world space, 3 per vertex (zero: none); empty when no primitive has any
     std::vector<int32_t> indices;          // 3 per triangle
     std::vector<int32_t> material_indices; // 1 per triangle
     std::vector<gbpt_principled_material> materials;
@@ -937,6 +954,7 @@ private:
     gbpt_gltf& out_;
     int32_t default_material_ = -1;
     int64_t camera_index_ = -1;
+    bool any_normals_ = false;
 
     static size_t node_index(const Json& v, size_t n)
     {
@@ -968,8 +986,14 @@ private:
             const Json* attrs = prim.find("attributes");
             if (!attrs || !attrs->has("POSITION"))
                 fail("glTF: primitive without POSITION");
-            const std::vector<float> pos = doc_.vec3f(index_of(*attrs, "POSITION", 0, doc_.accessors.size(), "accessor"));
+            const std::vector<float> pos = doc_.vec3f(index_of(*attrs, "POSITION", 0, doc_.accessors.size(), "accessor"), "POSITION");
             const size_t nv = pos.size() / 3;
+            std::vector<float> nrm;
+            if (attrs->has("NORMAL")) {
+                nrm = doc_.vec3f(index_of(*attrs, "NORMAL", 0, doc_.accessors.size(), "accessor"), "NORMAL");
+                if (nrm.size() != pos.size())
+                    fail("glTF: NORMAL and POSITION counts differ");
+            }
             std::vector<uint32_t> idx;
             if (prim.has("indices")) {
                 idx = doc_.scalars_u32(index_of(prim, "indices", 0, doc_.accessors.size(), "accessor"));
@@ -991,6 +1015,26 @@ private:
             out_.positions.resize((base + nv) * 3);
             for (size_t v = 0; v < nv; ++v)
                 world.point(&pos[v * 3], &out_.positions[(base + v) * 3]);
+            // normals to world space by the inverse transpose of the node's 3x3 part, normalised
+            // (what ASSIMP's pre-transform step does to them); zero where the primitive has none
+            if (!nrm.empty() && !any_normals_) {
+                out_.normals.assign(base * 3, 0.0f);  // earlier primitives had none
+                any_normals_ = true;
+            }
+            if (any_normals_) {
+                out_.normals.resize((base + nv) * 3, 0.0f);
+                if (!nrm.empty()) {
+                    const Mat4 it = world.inverse_transpose3();
+                    for (size_t v = 0; v < nv; ++v) {
+                        const double n[3] = {nrm[v * 3], nrm[v * 3 + 1], nrm[v * 3 + 2]};
+                        double w[3];
+                        it.vector(n, w);
+                        normalise(w);
+                        for (int k = 0; k < 3; ++k)
+                            out_.normals[(base + v) * 3 + k] = float(w[k]);
+                    }
+                }
+            }
 
             // triangles of the primitive (glTF 2.0 section 3.7.2.1: lists, strips, fans)
             auto emit = [&](uint32_t a, uint32_t b, uint32_t c) {
@@ -1095,6 +1139,7 @@ gbpt_status gbpt_gltf_scene_desc(const gbpt_gltf* g, gbpt_scene_desc* out)
     out->materials = nullptr;
     out->n_materials = int32_t(g->materials.size());
     out->principled_materials = g->materials.data();
+    out->vertex_normals = g->normals.empty() ? nullptr : g->normals.data();
     return GBPT_OK;
 }
 

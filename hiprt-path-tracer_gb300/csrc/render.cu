@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0,
             load_triangle(s, prim, a, b, c);
             const V3 ng_raw = normalize(cross(b - a, c - a));
             V3 ng = ng_raw;
-            V3 ns = ng;
+            V3 ns = shading_normal(s, prim, hit.y, hit.z, ng_raw);
             const V3 view = -d;
             fix_backfacing(view, ng, ns);
             const int mat = __ldg(s.material_of + prim);
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             load_triangle(s, prim, a, b, c);
             const V3 ng_raw = normalize(cross(b - a, c - a));
             V3 ng = ng_raw;
-            V3 ns = ng;
+            V3 ns = shading_normal(s, prim, hit.y, hit.z, ng_raw);
             const V3 view = -d;
             fix_backfacing(view, ng, ns);
             const int mat = __ldg(s.material_of + prim);

@@ -262,6 +262,20 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
         for (int k = 0; k < 3; k++)
             if (!std::isfinite(materials[m].emission[k]) || materials[m].emission[k] < 0.0f)
                 return set_error(GBPT_ERROR_INVALID_ARG, "material " + std::to_string(m) + " has an invalid emission");
+    // smooth-shading normals: finite; a zero normal marks a vertex without one
+    std::vector<float4> normals;
+    if (d->vertex_normals)
+    {
+        normals.resize(d->n_vertices);
+        for (int64_t v = 0; v < d->n_vertices; v++)
+        {
+            const float* n = d->vertex_normals + 3 * v;
+            if (!std::isfinite(n[0]) || !std::isfinite(n[1]) || !std::isfinite(n[2]))
+                return set_error(GBPT_ERROR_INVALID_ARG, "vertex " + std::to_string(v) + " has a non-finite normal");
+            const bool has = n[0] != 0.0f || n[1] != 0.0f || n[2] != 0.0f;
+            normals[v] = make_float4(n[0], n[1], n[2], has ? 1.0f : 0.0f);
+        }
+    }
 
     gbpt_scene* s = new (std::nothrow) gbpt_scene();
     if (!s) return set_error(GBPT_ERROR_OOM, "host allocation failed");
@@ -303,6 +317,7 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     double* dq = M.alloc<double>(ne);
     int32_t* dsmall = M.alloc<int32_t>(ne);
     int32_t* dlarge = M.alloc<int32_t>(ne);
+    float4* dn = normals.empty() ? nullptr : M.alloc<float4>(normals.size());
     gbpt_principled_material* dpm = nullptr;
     std::vector<gbpt_principled_material> pmats;
     if (d->principled_materials)
@@ -314,6 +329,8 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     if (e == cudaSuccess && dpm)
         e = cudaMemcpyAsync(dpm, pmats.data(), pmats.size() * sizeof(gbpt_principled_material), cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dv, verts.data(), verts.size() * sizeof(float4), cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess && dn)
+        e = cudaMemcpyAsync(dn, normals.data(), normals.size() * sizeof(float4), cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(di, d->indices, 3 * d->n_triangles * sizeof(int32_t), cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess)
@@ -336,6 +353,7 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     v.bvh_nodes = static_cast<const uint4*>(s->bvh->dev.nodes);
     v.bvh_tris = static_cast<const float4*>(s->bvh->dev.tris);
     v.pmats = dpm;
+    v.normals = dn;
     s->principled = dpm != nullptr;
     s->n_emissive = ne;
     if (e == cudaSuccess) e = gbpt::launch_light_table(v, dpower, dpartial, n_partial, dsum, dq, dprob, dalias, dsmall, dlarge, cs);

@@ -65,6 +65,7 @@ struct SceneView
     const float4* bvh_tris;
     const gbpt_principled_material* pmats;  // effective principled materials (NULL: Lambertian scene)
     EnvView env;
+    const float4* normals;        // per vertex: smooth-shading normal, w = 1 when present (NULL: none)
 };
 
 struct Queue
@@ -265,6 +266,20 @@ __device__ __forceinline__ void load_triangle(const SceneView& s, int prim, V3& 
     a = xyz(__ldg(s.vertices + i0));
     b = xyz(__ldg(s.vertices + i1));
     c = xyz(__ldg(s.vertices + i2));
+}
+
+// get_shading_normal (src/Device/includes/Intersect.h:114-134) without normal maps: the vertex
+// normals interpolated at the hit's barycentrics (uv_interpolate, src/Device/includes/Texture.h:248-251)
+// when the triangle's first vertex has one, else the geometric normal. Called before the backface fix.
+__device__ __forceinline__ V3 shading_normal(const SceneView& s, int prim, float u, float v, V3 ng)
+{
+    if (!s.normals) return ng;
+    const int i0 = __ldg(s.indices + 3 * prim);
+    const float4 n0 = __ldg(s.normals + i0);
+    if (n0.w == 0.0f) return ng;
+    const float4 n1 = __ldg(s.normals + __ldg(s.indices + 3 * prim + 1));
+    const float4 n2 = __ldg(s.normals + __ldg(s.indices + 3 * prim + 2));
+    return normalize(xyz(n1) * u + xyz(n2) * v + xyz(n0) * (1.0f - u - v));
 }
 
 #endif  // __CUDACC__

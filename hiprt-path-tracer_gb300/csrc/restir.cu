@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuf
         V3 a, b, c;
         load_triangle(s, prim, a, b, c);
         const V3 ng_raw = normalize(cross(b - a, c - a));
-        V3 ng = ng_raw, ns = ng_raw;
+        V3 ng = ng_raw, ns = shading_normal(s, prim, hit.y, hit.z, ng_raw);
         const V3 view = -d;
         fix_backfacing(view, ng, ns);
         const int mat = __ldg(s.material_of + prim);

@@ -33,7 +33,7 @@ class Material(ctypes.Structure):
 class SceneDesc(ctypes.Structure):
     _fields_ = [("positions", c_vp), ("n_vertices", i64), ("indices", c_vp), ("n_triangles", i64),
                 ("material_indices", c_vp), ("materials", c_vp), ("n_materials", i32),
-                ("principled_materials", c_vp)]
+                ("principled_materials", c_vp), ("vertex_normals", c_vp)]
 
 
 class RenderSettingsC(ctypes.Structure):
@@ -279,10 +279,10 @@ class World:
 
 class Scene:
     def __init__(self, positions, indices, material_of_triangle, albedo=None, emission=None, stream=None, sah_bins=32,
-                 max_leaf_size=3, principled=None):
+                 max_leaf_size=3, principled=None, vertex_normals=None):
         """albedo/emission: (M, 3) plain materials; principled: (M, 64) gbpt.materials records (the
         reference's CPUMaterial parameters; base colour and emission come from them when albedo is
-        None)."""
+        None); vertex_normals: (V, 3) smooth-shading normals (a zero row: none at that vertex)."""
         lib = _load()
         self._pm = None
         if principled is not None:
@@ -299,9 +299,15 @@ class Scene:
         for k in range(len(alb)):
             self._mats[k].base_color[:] = [float(v) for v in alb[k]]
             self._mats[k].emission[:] = [float(v) for v in emi[k]]
+        self._nrm = None
+        if vertex_normals is not None:
+            self._nrm = np.ascontiguousarray(vertex_normals, np.float32).reshape(-1, 3)
+            if self._nrm.shape[0] != self._pos.shape[0]:
+                raise ValueError("vertex_normals needs one normal per vertex")
         desc = SceneDesc(self._pos.ctypes.data, self._pos.shape[0], self._idx.ctypes.data, self._idx.shape[0],
                          self._mat_of.ctypes.data, ctypes.addressof(self._mats), len(alb),
-                         self._pm.ctypes.data if self._pm is not None else None)
+                         self._pm.ctypes.data if self._pm is not None else None,
+                         self._nrm.ctypes.data if self._nrm is not None else None)
         params = _lib.BvhParams(sah_bins, max_leaf_size, 0)
         h = c_vp()
         _lib.check(lib.gbpt_scene_create(ctypes.byref(desc), ctypes.byref(params), ctypes.byref(h), _stream(stream)))
@@ -367,15 +373,18 @@ class Scene:
 @dataclass
 class GltfScene:
     """A glTF 2.0 file read by gbpt_gltf_load: world-space triangles, per-triangle material indices,
-    principled material records (M, 64) and the file's camera (None when it has none)."""
+    principled material records (M, 64), the file's camera (None when it has none) and world-space
+    vertex normals (None when no primitive has any)."""
     positions: np.ndarray
     indices: np.ndarray
     material_of_triangle: np.ndarray
     principled: np.ndarray
     camera: dict | None
+    vertex_normals: np.ndarray | None = None
 
     def create_scene(self, **kw) -> "Scene":
-        return Scene(self.positions, self.indices, self.material_of_triangle, principled=self.principled, **kw)
+        return Scene(self.positions, self.indices, self.material_of_triangle, principled=self.principled,
+                     vertex_normals=self.vertex_normals, **kw)
 
     def camera_matrices(self, aspect=None, near=0.1, far=100.0):
         """(inverse_view, inverse_projection) of the file's camera with its vertical field of view
@@ -411,13 +420,14 @@ def load_gltf(path) -> GltfScene:
         idx = copy(d.indices, nt * 3, np.int32).reshape(nt, 3)
         mat = copy(d.material_indices, nt, np.int32)
         pm = copy(d.principled_materials, nm * 64, np.float32).reshape(nm, 64)
+        nrm = copy(d.vertex_normals, nv * 3, np.float32).reshape(nv, 3) if d.vertex_normals else None
         cam = GltfCameraC()
         _lib.check(lib.gbpt_gltf_get_camera(h, ctypes.byref(cam)))
         camera = None
         if cam.present:
             camera = {"position": tuple(cam.position), "forward": tuple(cam.forward), "up": tuple(cam.up),
                       "yfov": cam.yfov, "aspect_ratio": cam.aspect_ratio, "znear": cam.znear, "zfar": cam.zfar}
-        return GltfScene(pos, idx, mat, pm, camera)
+        return GltfScene(pos, idx, mat, pm, camera, nrm)
     finally:
         lib.gbpt_gltf_destroy(h)
 

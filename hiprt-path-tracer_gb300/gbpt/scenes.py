@@ -329,6 +329,61 @@ def cornell_box() -> CornellBox:
     return CornellBox(Mesh(pos, idx), mat, albedo, emission, np.nonzero(mat == 3)[0].astype(np.int32))
 
 
+def uv_sphere(centre, radius: float, n_lat: int = 8, n_lon: int = 16):
+    """A latitude/longitude sphere: (Mesh, (V, 3) outward unit vertex normals). Coarse on purpose:
+    shaded with its vertex normals it looks round, with its geometric normals faceted."""
+    c = np.asarray(centre, np.float64)
+    th = np.linspace(0.0, np.pi, n_lat + 1)
+    ph = np.linspace(0.0, 2.0 * np.pi, n_lon + 1)
+    dirs = np.stack([np.sin(th)[:, None] * np.cos(ph)[None, :], np.repeat(np.cos(th)[:, None], n_lon + 1, 1),
+                     np.sin(th)[:, None] * np.sin(ph)[None, :]], -1).reshape(-1, 3)
+    pos = (c + radius * dirs).astype(F32)
+    tris = []
+    for i in range(n_lat):
+        for j in range(n_lon):
+            a, b = i * (n_lon + 1) + j, i * (n_lon + 1) + j + 1
+            cc, d = a + n_lon + 1, b + n_lon + 1
+            if i > 0:
+                tris.append((a, b, cc))  # outward winding
+            if i < n_lat - 1:
+                tris.append((b, d, cc))
+    idx = np.asarray(tris, np.int32)
+    return Mesh(pos, idx), (dirs / np.linalg.norm(dirs, axis=1, keepdims=True)).astype(F32)
+
+
+@dataclass
+class SmoothScene:
+    mesh: Mesh
+    material_of_triangle: np.ndarray  # (T,) int32
+    albedo: np.ndarray                # (M, 3)
+    emission: np.ndarray              # (M, 3)
+    vertex_normals: np.ndarray        # (V, 3): zero on the box, the sphere normals on the spheres
+
+    def corner_normals(self) -> np.ndarray:
+        """(T, 3, 3) normals at each triangle's corners (the oracle's layout)."""
+        return np.ascontiguousarray(self.vertex_normals[self.mesh.indices])
+
+
+def smooth_cornell() -> SmoothScene:
+    """The Cornell box's walls and light (flat shading: zero vertex normals) with two coarse
+    spheres shaded by their vertex normals in place of the boxes: a white one (material 0) of
+    radius 1.1 at (1.85, 1.1, 1.69) and one of material 4 (a fifth material, white) of radius 1.3
+    at (3.68, 1.3, 3.51)."""
+    cb = cornell_box()
+    keep = np.r_[0:10, 34:36]  # walls and light
+    walls = Mesh(cb.mesh.positions[cb.mesh.indices[keep]].reshape(-1, 3),
+                 np.arange(3 * len(keep), dtype=np.int32).reshape(-1, 3))
+    s1, n1 = uv_sphere((1.85, 1.1, 1.69), 1.1)
+    s2, n2 = uv_sphere((3.68, 1.3, 3.51), 1.3, n_lat=10, n_lon=20)
+    mesh = merge(walls, s1, s2)
+    mat = np.concatenate([cb.material_of_triangle[keep], np.zeros(s1.n_triangles, np.int32),
+                          np.full(s2.n_triangles, 4, np.int32)])
+    albedo = np.concatenate([cb.albedo, [[0.8, 0.8, 0.8]]]).astype(F32)
+    emission = np.concatenate([cb.emission, [[0.0, 0.0, 0.0]]]).astype(F32)
+    normals = np.concatenate([np.zeros((walls.positions.shape[0], 3), F32), n1, n2])
+    return SmoothScene(mesh, mat, albedo, emission, normals)
+
+
 def envmap_directions(width: int, height: int) -> np.ndarray:
     """World direction (identity rotation) of each texel centre of an equirectangular envmap, as the
     reference maps (u, v): phi = 2 pi u, theta = pi v, d = (-sin theta cos phi, -cos theta,

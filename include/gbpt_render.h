@@ -43,6 +43,13 @@ typedef struct gbpt_scene_desc {
     const gbpt_material* materials;
     int32_t n_materials;
     const gbpt_principled_material* principled_materials;
+    /* Optional smooth-shading normals, 3 per vertex (NULL: every triangle shades with its
+     * geometric normal). A triangle whose first vertex has a zero normal shades flat, as the
+     * reference's per-vertex has_vertex_normals flag (src/HostDeviceCommon/RenderBuffers.h:34-37)
+     * selects it in get_shading_normal (src/Device/includes/Intersect.h:114-134): the shading
+     * normal is normalize(n_b u + n_c v + n_a (1 - u - v)) at the hit's barycentrics, then the
+     * backface fix. Normal maps are not built. */
+    const float* vertex_normals;
 } gbpt_scene_desc;
 
 /* Uploads the scene, builds its BVH (gbpt_bvh_build), the emissive-triangle list (triangles
@@ -75,8 +82,7 @@ GBPT_API gbpt_status gbpt_scene_get_light_table(const gbpt_scene* scene, int32_t
  * colour to 1) and _volume (attenuation colour and distance); every other field keeps
  * CPUMaterial's default; then CPUMaterial::make_safe's clamps. Primitives without a material get
  * the glTF default material, appended after the file's materials. Also a .glb container. Not read:
- * textures, vertex normals and texture coordinates (the renderer shades with geometric normals),
- * skins and morph targets (the base mesh is loaded); sparse accessors, non-float positions and
+ * textures and texture coordinates, skins and morph targets (the base mesh is loaded); sparse accessors, non-float positions and
  * unknown required extensions are errors. Triangle order is node traversal order (ASSIMP's
  * pre-transform step groups meshes by material instead). A KHR_materials_sheen material loads
  * with sheen = 1, as the reference maps it, which gbpt_scene_create then rejects. */
@@ -90,8 +96,10 @@ typedef struct gbpt_gltf_camera {
 } gbpt_gltf_camera;
 
 GBPT_API gbpt_status gbpt_gltf_load(const char* path, gbpt_gltf** out);
-/* The loaded scene as a scene description (principled materials only; pointers owned by 'g',
- * valid until gbpt_gltf_destroy) for gbpt_scene_create. */
+/* The loaded scene as a scene description (principled materials only; vertex normals from the
+ * primitives' NORMAL attributes moved to world space by the inverse transpose of their node's
+ * transform and normalised, zero for primitives without one, NULL when no primitive has one;
+ * pointers owned by 'g', valid until gbpt_gltf_destroy) for gbpt_scene_create. */
 GBPT_API gbpt_status gbpt_gltf_scene_desc(const gbpt_gltf* g, gbpt_scene_desc* out);
 GBPT_API gbpt_status gbpt_gltf_get_camera(const gbpt_gltf* g, gbpt_gltf_camera* out);
 GBPT_API gbpt_status gbpt_gltf_destroy(gbpt_gltf* g);

@@ -162,7 +162,7 @@ class _Doc:
 
 def load(path: str) -> dict:
     """{'positions' (V,3) f32, 'indices' (T,3) i32, 'material_of' (T,) i32, 'materials' [dict],
-    'camera' dict | None} of a .gltf/.glb file."""
+    'camera' dict | None, 'normals' (V,3) f32 | None} of a .gltf/.glb file."""
     doc = _Doc(path)
     j = doc.j
     nodes = j.get("nodes", [])
@@ -173,12 +173,13 @@ def load(path: str) -> dict:
     else:
         children = {c for n in nodes for c in n.get("children", [])}
         roots = [i for i in range(len(nodes)) if i not in children]
-    pos_out, tri_out, mat_out = [], [], []
+    pos_out, tri_out, mat_out, nrm_out = [], [], [], []
+    any_normals = False
     n_vertices = 0
     camera, camera_index = None, None
 
     def visit(i, parent):
-        nonlocal n_vertices, camera, camera_index
+        nonlocal n_vertices, camera, camera_index, any_normals
         node = nodes[i]
         world = parent @ _node_matrix(node)
         if "mesh" in node:
@@ -199,6 +200,16 @@ def load(path: str) -> dict:
                         materials.append(map_material({}))
                     mi = default_material[0]
                 wp = (p @ world[:3, :3].T + world[:3, 3]).astype(np.float32)
+                if "NORMAL" in prim["attributes"]:
+                    # inverse transpose of the node's 3x3 part, then normalised (ASSIMP's
+                    # pre-transform step applies the same to normals)
+                    nn = doc.accessor(prim["attributes"]["NORMAL"]).astype(np.float64) @ np.linalg.inv(world[:3, :3])
+                    ln = np.linalg.norm(nn, axis=1, keepdims=True)
+                    nn = np.where(ln > 0, nn / np.where(ln > 0, ln, 1.0), nn)
+                    nrm_out.append(nn.astype(np.float32))
+                    any_normals = True
+                else:
+                    nrm_out.append(np.zeros((nv, 3), np.float32))
                 tris = []
                 n = len(idx)
                 if mode == 4:
@@ -237,4 +248,5 @@ def load(path: str) -> dict:
         "material_of": np.concatenate(mat_out) if mat_out else np.zeros(0, np.int32),
         "materials": materials,
         "camera": camera,
+        "normals": np.concatenate(nrm_out) if any_normals else None,
     }

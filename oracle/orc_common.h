@@ -91,6 +91,7 @@ struct Scene
     const float* alias_prob;
     const int* alias_idx;
     float power_sum;
+    const float* tn = nullptr;  // corner normals, 9 per triangle (NULL: flat shading everywhere)
     V a(int t) const { return mk(tv[9 * t], tv[9 * t + 1], tv[9 * t + 2]); }
     V b(int t) const { return mk(tv[9 * t + 3], tv[9 * t + 4], tv[9 * t + 5]); }
     V c(int t) const { return mk(tv[9 * t + 6], tv[9 * t + 7], tv[9 * t + 8]); }
@@ -114,6 +115,33 @@ bool mt(V A, V B, V C, V o, V d, float& t)
     if (v < 0.0f || u + v > 1.0f) return false;
     t = f * dot(e2, q);
     return t > EPS;
+}
+
+// Barycentrics (u, v) of the ray's hit on triangle t (the Moller-Trumbore values of mt()).
+void mt_uv(const Scene& s, int t, V o, V d, float& u, float& v)
+{
+    V A = s.a(t), B = s.b(t), C = s.c(t);
+    V e1 = B - A, e2 = C - A;
+    V h = cross(d, e2);
+    float f = 1.0f / dot(e1, h);
+    V sv = o - A;
+    u = f * dot(sv, h);
+    V q = cross(sv, e1);
+    v = f * dot(d, q);
+}
+
+// get_shading_normal (src/Device/includes/Intersect.h:114-134) without normal maps: corner normals
+// interpolated as uv_interpolate does (src/Device/includes/Texture.h:248-251) when the triangle's
+// first corner has one, else the geometric normal.
+V shading_normal(const Scene& s, int t, V o, V d, V ng)
+{
+    if (!s.tn) return ng;
+    const float* n = s.tn + 9 * (size_t)t;
+    if (n[0] == 0.0f && n[1] == 0.0f && n[2] == 0.0f) return ng;
+    float u, v;
+    mt_uv(s, t, o, d, u, v);
+    V na = mk(n[0], n[1], n[2]), nb = mk(n[3], n[4], n[5]), nc = mk(n[6], n[7], n[8]);
+    return nrm(nb * u + nc * v + na * (1.0f - u - v));
 }
 
 // closest hit with the self-hit filter; returns prim or -1 (lowest index on exact ties)

@@ -437,7 +437,7 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
         }
         V P = o + d * t;
         V ng = nrm(cross(s.b(prim) - s.a(prim), s.c(prim) - s.a(prim)));
-        V ns = ng;
+        V ns = shading_normal(s, prim, o, d, ng);
         V view = neg(d);
         if (dot(view, ng) < 0.0f) { ng = neg(ng); ns = neg(ns); }
         if (dot(view, ns) < 0.0f) ns = neg(ns);
@@ -608,7 +608,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
         }
         V P = o + d * t;
         V ng_raw = nrm(cross(s.b(prim) - s.a(prim), s.c(prim) - s.a(prim)));
-        V ng = ng_raw, ns = ng_raw;
+        V ng = ng_raw, ns = shading_normal(s, prim, o, d, ng_raw);
         V view = neg(d);
         if (dot(view, ng) < 0.0f) { ng = neg(ng); ns = neg(ns); }
         if (dot(view, ns) < 0.0f) ns = neg(ns);
@@ -787,14 +787,15 @@ extern "C" {
 
 /* settings_i: width, height, nb_bounces, do_rr, rr_min_depth, light_sampling (0 uniform, 1 power),
  * seed, do_jittering, spp, iteration_base, direct lighting (0 MIS, 1 RIS), RIS light candidates,
- * RIS BSDF candidates. env: the world (NULL: none). Adds the samples of iterations
+ * RIS BSDF candidates. env: the world (NULL: none). tri_normals: corner normals, 9 floats per
+ * triangle (NULL: flat shading). Adds the samples of iterations
  * [iteration_base, iteration_base + spp) to out_rgb (W*H*3 doubles). */
 void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const float* albedo, const float* emission,
                    const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx, float power_sum,
                    const int* settings_i, float rr_clamp, const float* inv_view, const float* inv_proj, double* out_rgb,
-                   int nthreads, const OrcEnv* env)
+                   int nthreads, const OrcEnv* env, const float* tri_normals)
 {
-    Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
+    Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum, tri_normals};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
                 settings_i[10], settings_i[11], settings_i[12], env};
@@ -848,9 +849,10 @@ void orc_pt_render_principled(const float* tri_verts, int n_tris, const int* mat
                               const float* emission, const float* pmats, void* eval_fn, void* sample_fn,
                               const int* emissive, int n_emissive, const float* alias_prob, const int* alias_idx,
                               float power_sum, const int* settings_i, float rr_clamp, const float* inv_view,
-                              const float* inv_proj, double* out_rgb, int nthreads, const OrcEnv* env)
+                              const float* inv_proj, double* out_rgb, int nthreads, const OrcEnv* env,
+                              const float* tri_normals)
 {
-    Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum};
+    Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum, tri_normals};
     PScene ps{pmats, (bsdf_eval_fn)eval_fn, (bsdf_sample_fn)sample_fn};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,

@@ -246,7 +246,7 @@ def _pt_lib():
     if not getattr(lib, "_pt_sigs", False):
         lib.orc_pt_render.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, _c_f, _c_i, ctypes.c_int, _c_f, _c_i,
                                       ctypes.c_float, _c_i, ctypes.c_float, _c_f, _c_f,
-                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p]
+                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p, _c_f]
         _u32 = ctypes.POINTER(ctypes.c_uint32)
         lib.orc_env_pack.argtypes = [_c_f, _i64, _u32, _c_f]
         lib.orc_env_unpack.argtypes = [_u32, _i64, _c_f]
@@ -260,11 +260,21 @@ def _pt_lib():
     return lib
 
 
+def _corner_normals(normals):
+    """(T, 3, 3) corner normals of the triangle soup as a float pointer, or NULL."""
+    if normals is None:
+        return None, None
+    n = np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+    return n, _ptr(n, _c_f)
+
+
 def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_idx, power_sum, settings, spp,
-              iteration_base=0, nthreads=0, env: OracleEnv | None = None):
+              iteration_base=0, nthreads=0, env: OracleEnv | None = None, normals=None):
     """Path-tracing oracle (Lambertian scenes). Returns the FP64 per-pixel sums (H, W, 3) of
-    'spp' samples per pixel, drawn with the same PCG sequence as the GPU kernels. env: the world."""
+    'spp' samples per pixel, drawn with the same PCG sequence as the GPU kernels. env: the world;
+    normals: (T, 3, 3) smooth-shading corner normals (None: flat)."""
     lib = _pt_lib()
+    keep, nptr = _corner_normals(normals)
     soup = np.ascontiguousarray(soup, np.float32)
     mo = np.ascontiguousarray(material_of, np.int32)
     al = np.ascontiguousarray(albedo, np.float32)
@@ -283,22 +293,25 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
     lib.orc_pt_render(_ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(al, _c_f), _ptr(em, _c_f), _ptr(ei, _c_i),
                       len(ei), _ptr(ap, _c_f), _ptr(ai, _c_i), float(power_sum), _ptr(si, _c_i),
                       float(s.russian_roulette_throughput_clamp), _ptr(iv, _c_f), _ptr(ip, _c_f),
-                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads, _env_ptr(env))
+                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads, _env_ptr(env), nptr)
+    del keep
     return out
 
 
 def pt_render_principled(soup, material_of, pmats_effective, emission, emissive, alias_prob, alias_idx, power_sum,
-                         settings, spp, iteration_base=0, nthreads=0, env: OracleEnv | None = None):
+                         settings, spp, iteration_base=0, nthreads=0, env: OracleEnv | None = None, normals=None):
     """Path-tracing oracle for principled scenes: the estimator of pt_render with the BSDF
     evaluated and sampled by the REFERENCE's own principled BSDF (oracle/_ref/libref.so, built
     only where the reference tree exists). pmats_effective: (M, 64) records after coat
-    roughening. Returns FP64 per-pixel sums (H, W, 3)."""
+    roughening; normals: (T, 3, 3) smooth-shading corner normals (None: flat). Returns FP64
+    per-pixel sums (H, W, 3)."""
     lib = _pt_lib()
+    keep, nptr = _corner_normals(normals)
     if not getattr(lib, "_ptp_sig", False):
         lib.orc_pt_render_principled.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, _c_f, _c_f, ctypes.c_void_p,
                                                  ctypes.c_void_p, _c_i, ctypes.c_int, _c_f, _c_i, ctypes.c_float, _c_i,
                                                  ctypes.c_float, _c_f, _c_f, ctypes.POINTER(ctypes.c_double),
-                                                 ctypes.c_int, ctypes.c_void_p]
+                                                 ctypes.c_int, ctypes.c_void_p, _c_f]
         lib._ptp_sig = True
     ref = ctypes.CDLL(REF_SO)
     eval_fn = ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value
@@ -323,7 +336,8 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
                                  _ptr(pm, _c_f), eval_fn, sample_fn, _ptr(ei, _c_i), len(ei), _ptr(ap, _c_f),
                                  _ptr(ai, _c_i), float(power_sum), _ptr(si, _c_i),
                                  float(s.russian_roulette_throughput_clamp), _ptr(iv, _c_f), _ptr(ip, _c_f),
-                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads, _env_ptr(env))
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nthreads, _env_ptr(env), nptr)
+    del keep
     return out
 
 

@@ -7,7 +7,8 @@ Xorshift32 generator of each BSDF sample), so its image agrees with this one sam
 to floating-point contraction. Materials: coated diffuse walls, a rough dielectric red wall, an
 anisotropic metal green wall, a rough glass short box (closed: paths enter and leave it), a mirror
 tall box (a delta BSDF: no light sampling), the area light. The scene and settings are stored with
-the image so the GPU test needs nothing else.
+the image so the GPU test needs nothing else. A third file renders the smooth-shading scene (two
+coarse spheres shaded with their vertex normals).
 Usage (where the reference tree is present):  python tests/golden/make_pt_principled_golden.py
 """
 import os
@@ -26,6 +27,8 @@ import pyoracle  # noqa: E402
 
 OUT = os.path.join(HERE, "pt_principled_cornell.npz")
 OUT_RIS = os.path.join(HERE, "pt_principled_ris_cornell.npz")
+OUT_SMOOTH = os.path.join(HERE, "pt_principled_smooth_cornell.npz")
+
 
 MATERIALS = [
     dict(base_color=(0.73, 0.73, 0.73), roughness=0.5, coat=0.5, coat_roughness=0.1),          # 0 white walls
@@ -34,6 +37,13 @@ MATERIALS = [
     dict(base_color=(0.0, 0.0, 0.0), emission=(17.0, 12.0, 4.0)),                               # 3 light
     dict(base_color=(0.95, 0.95, 0.95), roughness=0.15, specular_transmission=1.0, ior=1.5),    # 4 short box
     dict(base_color=(0.9, 0.9, 0.9), roughness=0.0, metallic=1.0),                              # 5 tall box
+]
+
+# the smooth-shading scene (gbpt.scenes.smooth_cornell): walls and light as above, a rough glass
+# sphere and a glossy metal sphere, both shaded with their vertex normals
+SMOOTH_MATERIALS = MATERIALS[:4] + [
+    dict(base_color=(0.9, 0.6, 0.3), roughness=0.25, metallic=1.0),                             # 4 metal sphere
+    dict(base_color=(0.95, 0.95, 0.95), roughness=0.1, specular_transmission=1.0, ior=1.5),     # 5 glass sphere
 ]
 
 
@@ -74,6 +84,25 @@ def main():
                                         st.samples_per_launch)
     np.savez_compressed(OUT_RIS, image=ris, ris=np.array([4, 1], np.int32))
     print(f"wrote {OUT_RIS}: mean {ris.mean() / st.samples_per_launch:.4f}")
+    # smooth shading: vertex normals on the spheres
+    sc = scenes.smooth_cornell()
+    mat_of = sc.material_of_triangle.copy()
+    n_walls = 12
+    n_s1 = int(np.sum(mat_of[n_walls:] == 0))
+    mat_of[n_walls:n_walls + n_s1] = 5
+    raw = M.pack_many(SMOOTH_MATERIALS)
+    eff = M.pack_many([M.coat_roughened(m) for m in SMOOTH_MATERIALS])
+    st = settings(spp=16)
+    emission = raw[:, 4:7]
+    emissive = np.nonzero(np.any(emission[mat_of] != 0, axis=1))[0].astype(np.int32)
+    img = pyoracle.pt_render_principled(sc.mesh.triangle_soup(), mat_of, eff, emission, emissive, None, None, 0.0, st,
+                                        st.samples_per_launch, normals=sc.corner_normals())
+    np.savez_compressed(OUT_SMOOTH, positions=sc.mesh.positions, indices=sc.mesh.indices, material_of=mat_of,
+                        materials=raw, vertex_normals=sc.vertex_normals, inverse_view=st.inverse_view,
+                        inverse_projection=st.inverse_projection,
+                        settings=np.array([st.width, st.height, st.samples_per_launch, st.nb_bounces,
+                                           st.russian_roulette_min_depth, st.seed], np.int32), image=img)
+    print(f"wrote {OUT_SMOOTH}: mean {img.mean() / st.samples_per_launch:.4f}")
 
 
 if __name__ == "__main__":

@@ -69,8 +69,10 @@ def synthetic(builder=None):
     tri32 = rng.integers(0, 12, 9).astype(np.uint32)
     strip = np.array([0, 1, 2, 3, 4, 5, 6], np.uint16)
     fan = np.array([7, 8, 9, 10, 11], np.uint32)
+    normals = rng.normal(size=(12, 3)).astype(np.float32)
+    normals /= np.linalg.norm(normals, axis=1, keepdims=True)
     mesh_a = b.mesh([
-        {"attributes": {"POSITION": p_grid}, "indices": b.accessor(tri8), "material": 0},
+        {"attributes": {"POSITION": p_grid, "NORMAL": b.accessor(normals)}, "indices": b.accessor(tri8), "material": 0},
         {"attributes": {"POSITION": p_grid_strided}, "indices": b.accessor(tri16, stride=4), "material": 1},
         {"attributes": {"POSITION": p_grid}, "indices": b.accessor(tri32)},  # no material
         {"attributes": {"POSITION": p_grid}, "indices": b.accessor(strip), "mode": 5, "material": 2},
@@ -110,6 +112,11 @@ def _compare(path):
     assert got.positions.shape == want["positions"].shape
     scale = 1.0 + np.abs(want["positions"])
     assert np.all(np.abs(got.positions - want["positions"]) <= 2e-6 * scale)
+    if want["normals"] is None:
+        assert got.vertex_normals is None
+    else:
+        assert got.vertex_normals.shape == want["normals"].shape
+        assert np.all(np.abs(got.vertex_normals - want["normals"]) <= 2e-6)
     expected = M.pack_many(want["materials"])
     assert got.principled.shape == expected.shape
     # material records are bit-identical (same float conversions and clamps)
@@ -133,6 +140,10 @@ def test_synthetic_scene_matches_oracle(tmp_path, container):
     assert got.principled.shape[0] == len(MATERIALS) + 1
     assert set(np.unique(got.material_of_triangle)) == set(range(len(MATERIALS) + 1))
     assert got.camera["yfov"] == pytest.approx(0.5) and got.camera["aspect_ratio"] == pytest.approx(1.5)
+    # normals: unit length where the primitive has them (the first primitive of each mesh A
+    # instance), zero elsewhere
+    ln = np.linalg.norm(got.vertex_normals, axis=1)
+    assert np.all((np.abs(ln - 1) < 1e-6) | (ln == 0)) and 0 < np.count_nonzero(ln) < len(ln)
 
 
 def test_containers_agree(tmp_path):
@@ -181,6 +192,21 @@ def test_transforms_and_winding(tmp_path):
     n = [np.cross(p[t[1]] - p[t[0]], p[t[2]] - p[t[0]]) for t in got.indices]
     assert n[0][2] > 0 and n[1][2] > 0
     np.testing.assert_array_equal(p[3:], tri * [-1, 1, 1] + [5, 0, 0])
+
+
+def test_normals_follow_the_inverse_transpose(tmp_path):
+    """A non-uniform scale tilts normals the other way than positions: the loaded normal of a
+    slanted face stays perpendicular to the scaled face."""
+    b = GltfBuilder()
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 1]], np.float32)
+    n = np.cross(tri[1] - tri[0], tri[2] - tri[0])
+    n = np.tile((n / np.linalg.norm(n)).astype(np.float32), (3, 1))
+    b.node(mesh=b.mesh([{"attributes": {"POSITION": b.accessor(tri), "NORMAL": b.accessor(n)}}]), scale=[1, 3, 0.5])
+    got = gbpt.load_gltf(b.save(str(tmp_path / "n"), "file"))
+    p = got.positions
+    face = np.cross(p[1] - p[0], p[2] - p[0])
+    face /= np.linalg.norm(face)
+    np.testing.assert_allclose(got.vertex_normals, np.tile(face, (3, 1)), atol=1e-6)
 
 
 @pytest.mark.parametrize("name", ["cornell_pbr.gltf", "nested-dielectrics.gltf", "nested-dielectrics-complex.gltf",
