@@ -252,6 +252,7 @@ gbpt::TraceConfig from_c(const gbpt_trace_config& c)
     t.refill_below = c.refill_below;
     t.postpone_below = c.postpone_below;
     t.blocks_per_sm = c.blocks_per_sm;
+    t.shared_stack = c.shared_stack;
     return t;
 }
 
@@ -264,6 +265,7 @@ gbpt_trace_config to_c(const gbpt::TraceConfig& t)
     c.refill_below = t.refill_below;
     c.postpone_below = t.postpone_below;
     c.blocks_per_sm = t.blocks_per_sm;
+    c.shared_stack = t.shared_stack;
     return c;
 }
 
@@ -355,19 +357,22 @@ gbpt_status gbpt_trace_autotune(gbpt_bvh* bvh, const float* origin_tmin, const f
     const int refills[] = {4, 8, 12, 16, 20, 24};
     const int postpones[] = {0, 4, 8, 12, 16, 24};
     const int per_sm[] = {2, 4, 8, 12, 16};
+    const int shared[] = {0, 8, 16};
     for (int pass = 0; pass < 2 && e == cudaSuccess; pass++)
     {
-        for (int coord = 0; coord < 5 && e == cudaSuccess; coord++)
+        // coordinates: kernel, block, shared-stack depth, refill, postpone, blocks per SM
+        for (int coord = 0; coord < 6 && e == cudaSuccess; coord++)
         {
-            if (best.kernel == gbpt::kTraceKernelPerRay && coord >= 2) break;
-            if (best.kernel == gbpt::kTraceKernelFetch && (coord == 2 || coord == 3)) continue;
-            const int* vals = coord == 0 ? kernels : coord == 1 ? blocks : coord == 2 ? refills : coord == 3 ? postpones : per_sm;
-            const int nv = coord == 0 ? 3 : coord == 1 ? 3 : coord == 4 ? 5 : 6;
+            if (best.kernel == gbpt::kTraceKernelPerRay && coord >= 3) break;
+            if (best.kernel == gbpt::kTraceKernelFetch && (coord == 3 || coord == 4)) continue;
+            const int* vals = coord == 0 ? kernels : coord == 1 ? blocks : coord == 2 ? shared : coord == 3 ? refills
+                            : coord == 4 ? postpones : per_sm;
+            const int nv = coord <= 2 ? 3 : coord == 5 ? 5 : 6;
             for (int k = 0; k < nv && e == cudaSuccess; k++)
             {
                 gbpt::TraceConfig c = best;
-                int* field = coord == 0 ? &c.kernel : coord == 1 ? &c.block : coord == 2 ? &c.refill_below
-                                                                  : coord == 3 ? &c.postpone_below : &c.blocks_per_sm;
+                int* field = coord == 0 ? &c.kernel : coord == 1 ? &c.block : coord == 2 ? &c.shared_stack
+                           : coord == 3 ? &c.refill_below : coord == 4 ? &c.postpone_below : &c.blocks_per_sm;
                 if (*field == vals[k]) continue;
                 *field = vals[k];
                 float ms = 0.0f;

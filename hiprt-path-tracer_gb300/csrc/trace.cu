@@ -33,7 +33,10 @@ __device__ __forceinline__ int64_t warp_ray(int64_t v, int64_t warp, int64_t n_w
 
 // refill_below: refill the warp when fewer lanes than this are tracing; postpone_below: run
 // triangle steps only when at least this many lanes have them (else postpone)
-template <bool ANY_HIT>
+// dynamic shared memory of the traversal kernels: SH stack entries per thread, entry-major
+extern __shared__ uint2 trace_sh_stack[];
+
+template <bool ANY_HIT, int SH>
 __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict__ nodes,
                                                              const float4* __restrict__ tris,
                                                              const float4* __restrict__ origin_tmin,
@@ -55,7 +58,9 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
     int32_t skip = -1;
     float t_best = 0, u_best = 0, v_best = 0;
     int32_t prim_best = -1;
-    uint2 stack[kTraversalStack];
+    core::TraversalStack<SH> stack;
+    uint2* const sh_col = trace_sh_stack + threadIdx.x;
+    const int sh_stride = blockDim.x;
     int sp = 0, n_post = 0;
     uint2 ngroup = make_uint2(0u, 0u), tgroup = make_uint2(0u, 0u);
 
@@ -110,7 +115,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
             {
                 if (n_post < post_cap)
                 {
-                    stack[sp++] = tgroup;  // postponed triangle group (bits 24-31 clear)
+                    stack.push(sp, tgroup, sh_col, sh_stride);  // postponed triangle group (bits 24-31 clear)
                     n_post++;
                     tgroup.y = 0u;
                 }
@@ -153,7 +158,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
                 const uint32_t hits_imask = ngroup.y;
                 const uint32_t bit = 31u - __clz(hits_imask & 0xFF000000u);
                 ngroup.y &= ~(1u << bit);
-                if (ngroup.y & 0xFF000000u) stack[sp++] = ngroup;
+                if (ngroup.y & 0xFF000000u) stack.push(sp, ngroup, sh_col, sh_stride);
                 const uint32_t slot = (bit - 24u) ^ oct_inv;
                 const uint32_t rel = __popc(hits_imask & ~(0xFFFFFFFFu << slot));
                 const uint4* np = nodes + 5 * (size_t)(ngroup.x + rel);
@@ -168,7 +173,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
             {
                 if (sp > 0)
                 {
-                    const uint2 g = stack[--sp];
+                    const uint2 g = stack.pop(sp, sh_col, sh_stride);
                     if (g.y & 0xFF000000u)
                         ngroup = g;
                     else
@@ -200,7 +205,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
 // Per-lane fetch: the per-ray loop (a node, then all triangles of its hit leaves, then a pop), and
 // a lane whose ray finished takes the next ray of its warp's chunk at once (a shared-memory
 // counter per warp), so lanes do not wait for the warp's longest ray.
-template <bool ANY_HIT>
+template <bool ANY_HIT, int SH>
 __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                                    const float4* __restrict__ origin_tmin,
                                                    const float4* __restrict__ dir_tmax,
@@ -220,8 +225,9 @@ __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nod
         const int64_t ray = warp_ray(v, warp, n_warps);
         if (v >= rays_per_warp || ray >= n_rays) break;
         uint32_t cn = 0, ct = 0;
-        const float4 h = core::trace_ray<ANY_HIT, false>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
-                                                         last_prim ? last_prim[ray] : -1, cn, ct);
+        const float4 h = core::trace_ray<ANY_HIT, false, SH>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
+                                                             last_prim ? last_prim[ray] : -1, cn, ct,
+                                                             trace_sh_stack + threadIdx.x, blockDim.x);
         if (ANY_HIT)
         {
             if (occluded) occluded[ray] = __float_as_int(h.w) >= 0 ? 1 : 0;
@@ -232,7 +238,7 @@ __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nod
 }
 
 // per-ray traversal, one thread per ray; COUNT adds node / triangle counters (statistics)
-template <bool ANY_HIT, bool COUNT>
+template <bool ANY_HIT, bool COUNT, int SH>
 __global__ void __launch_bounds__(256) trace_ray_kernel(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                                                const float4* __restrict__ origin_tmin,
                                                                const float4* __restrict__ dir_tmax,
@@ -243,8 +249,9 @@ __global__ void __launch_bounds__(256) trace_ray_kernel(const uint4* __restrict_
     const int64_t ray = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ray >= n_rays) return;
     uint32_t n_nodes = 0, n_tris = 0;
-    const float4 h = core::trace_ray<ANY_HIT, COUNT>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
-                                                     last_prim ? last_prim[ray] : -1, n_nodes, n_tris);
+    const float4 h = core::trace_ray<ANY_HIT, COUNT, SH>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
+                                                         last_prim ? last_prim[ray] : -1, n_nodes, n_tris,
+                                                         trace_sh_stack + threadIdx.x, blockDim.x);
     if (ANY_HIT)
     {
         if (occluded) occluded[ray] = __float_as_int(h.w) >= 0 ? 1 : 0;
@@ -285,6 +292,7 @@ TraceConfig default_trace_config(bool any_hit)
     c.refill_below = 12;
     c.postpone_below = 8;
     c.blocks_per_sm = 8;
+    c.shared_stack = 0;
     return c;
 }
 
@@ -294,15 +302,17 @@ bool valid_trace_config(const TraceConfig& c)
     return (c.kernel == kTraceKernelPerRay || c.kernel == kTraceKernelPersistent || c.kernel == kTraceKernelFetch) &&
            block_ok && c.refill_below >= 1 &&
            c.refill_below <= 32 && c.postpone_below >= 0 && c.postpone_below <= 32 && c.blocks_per_sm >= 1 &&
-           c.blocks_per_sm <= 64;
+           c.blocks_per_sm <= 64 && (c.shared_stack == 0 || c.shared_stack == 8 || c.shared_stack == 16);
 }
 
-cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const float* dir_tmax,
-                         const int32_t* last_prim, int64_t n_rays, float* hits, uint8_t* occluded, bool any_hit,
-                         unsigned long long* counters, cudaStream_t stream, const TraceConfig* cfg_in)
+namespace {
+
+// the launches of one shared-stack depth SH (dynamic shared memory: SH entries per thread)
+template <int SH>
+cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, const float* dir_tmax,
+                            const int32_t* last_prim, int64_t n_rays, float* hits, uint8_t* occluded, bool any_hit,
+                            unsigned long long* counters, cudaStream_t stream, const TraceConfig& cfg)
 {
-    if (n_rays <= 0) return cudaSuccess;
-    const TraceConfig cfg = cfg_in ? *cfg_in : default_trace_config(any_hit);
     const uint4* nodes = reinterpret_cast<const uint4*>(bvh.nodes);
     const float4* tris = reinterpret_cast<const float4*>(bvh.tris);
     const float4* o = reinterpret_cast<const float4*>(origin_tmin);
@@ -312,25 +322,27 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
     {
         const int threads = counters ? kThreads : cfg.block;
         const int64_t blocks = (n_rays + threads - 1) / threads;
+        const size_t smem = (size_t)SH * threads * sizeof(uint2);
         if (counters)
         {
             if (any_hit)
-                trace_ray_kernel<true, true><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+                trace_ray_kernel<true, true, 0><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
                                                                                      h, occluded, counters);
             else
-                trace_ray_kernel<false, true><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim,
+                trace_ray_kernel<false, true, 0><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim,
                                                                                       n_rays, h, occluded, counters);
         }
         else if (any_hit)
-            trace_ray_kernel<true, false><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+            trace_ray_kernel<true, false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
                                                                                   h, occluded, nullptr);
         else
-            trace_ray_kernel<false, false><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+            trace_ray_kernel<false, false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
                                                                                    h, occluded, nullptr);
         return cudaGetLastError();
     }
     // persistent grids: blocks_per_sm blocks per SM, each warp owning a contiguous chunk of rays
     const int threads = cfg.block;
+    const size_t smem = (size_t)SH * threads * sizeof(uint2);
     if (cfg.kernel == kTraceKernelFetch)
     {
         const int64_t max_blocks = (int64_t)sm_count() * cfg.blocks_per_sm;
@@ -339,10 +351,10 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
         const int64_t warps = blocks * (threads / 32);
         const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
         if (any_hit)
-            trace_fetch<true><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+            trace_fetch<true, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
                                                                         occluded);
         else
-            trace_fetch<false><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+            trace_fetch<false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
                                                                          occluded);
         return cudaGetLastError();
     }
@@ -353,14 +365,33 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
     const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
     const int post_cap = kTraversalStack - bvh.depth - 1 > 0 ? kTraversalStack - bvh.depth - 1 : 0;
     if (any_hit)
-        trace_persistent<true><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
+        trace_persistent<true, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
                                                                          post_cap, cfg.refill_below, cfg.postpone_below, h,
                                                                          occluded);
     else
-        trace_persistent<false><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
+        trace_persistent<false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
                                                                           post_cap, cfg.refill_below, cfg.postpone_below,
                                                                           h, occluded);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const float* dir_tmax,
+                         const int32_t* last_prim, int64_t n_rays, float* hits, uint8_t* occluded, bool any_hit,
+                         unsigned long long* counters, cudaStream_t stream, const TraceConfig* cfg_in)
+{
+    if (n_rays <= 0) return cudaSuccess;
+    const TraceConfig cfg = cfg_in ? *cfg_in : default_trace_config(any_hit);
+    switch (counters ? 0 : cfg.shared_stack)
+    {
+    case 8: return launch_trace_sh<8>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits, occluded, any_hit, counters,
+                                      stream, cfg);
+    case 16: return launch_trace_sh<16>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits, occluded, any_hit, counters,
+                                        stream, cfg);
+    default: return launch_trace_sh<0>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits, occluded, any_hit, counters,
+                                       stream, cfg);
+    }
 }
 
 }  // namespace gbpt

@@ -191,12 +191,49 @@ GBPT_HD uint32_t intersect_children(const uint4 w0, const uint4 w1, const uint4 
     return hitmask;
 }
 
+// A thread's traversal stack: its first SH entries in shared memory (a column of the block's
+// array, entry k at col[k * stride] with stride = threads per block, so the 32 lanes of a warp
+// touch 32 different bank pairs whatever their depths), the deeper ones in local memory. An
+// 8-wide BVH rarely holds more than a handful of entries, so with SH >= 4 nearly every push and
+// pop stays in shared memory instead of going through L1 as local-memory traffic.
+template <int SH>
+struct TraversalStack
+{
+    uint2 local[kTraversalStack - SH];
+    // col / stride stay in the caller's registers (members here would live in local memory)
+    GBPT_HD void push(int& sp, uint2 v, uint2* col, int stride)
+    {
+        if constexpr (SH > 0)
+        {
+            if (sp < SH)
+            {
+                col[sp * stride] = v;
+                ++sp;
+                return;
+            }
+        }
+        local[sp - SH] = v;
+        ++sp;
+    }
+    GBPT_HD uint2 pop(int& sp, const uint2* col, int stride)
+    {
+        --sp;
+        if constexpr (SH > 0)
+        {
+            if (sp < SH) return col[sp * stride];
+        }
+        return local[sp - SH];
+    }
+};
+
 // Traces one ray. Closest hit: returns the hit as (t, u, v, prim bits), prim = -1 and t = -1 on a
 // miss. Any hit: returns prim >= 0 iff some accepted hit has t < tmax. Counts visited nodes and
-// tested triangles when COUNT is set.
-template <bool ANY_HIT, bool COUNT>
+// tested triangles when COUNT is set. SH > 0: the bottom SH stack entries live in the shared
+// column sh_col (stride sh_stride).
+template <bool ANY_HIT, bool COUNT, int SH = 0>
 GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const float4 ot,
-                         const float4 dt, const int32_t skip_prim, uint32_t& n_nodes, uint32_t& n_tris)
+                         const float4 dt, const int32_t skip_prim, uint32_t& n_nodes, uint32_t& n_tris,
+                         uint2* sh_col = nullptr, int sh_stride = 0)
 {
     const float ox = ot.x, oy = ot.y, oz = ot.z, ray_tmin = ot.w;
     const float dx = dt.x, dy = dt.y, dz = dt.z;
@@ -207,7 +244,7 @@ GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restri
     float u_best = 0.0f, v_best = 0.0f;
     int32_t prim_best = -1;
 
-    uint2 stack[kTraversalStack];
+    TraversalStack<SH> stack;
     int sp = 0;
     uint2 ngroup = make_uint2(0u, 0x80000000u);
     uint2 tgroup = make_uint2(0u, 0u);
@@ -219,7 +256,7 @@ GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restri
             const uint32_t hits_imask = ngroup.y;
             const uint32_t bit = 31u - __clz(hits_imask & 0xFF000000u);
             ngroup.y &= ~(1u << bit);
-            if (ngroup.y & 0xFF000000u) stack[sp++] = ngroup;
+            if (ngroup.y & 0xFF000000u) stack.push(sp, ngroup, sh_col, sh_stride);
             const uint32_t slot = (bit - 24u) ^ oct_inv;
             const uint32_t rel = __popc(hits_imask & ~(0xFFFFFFFFu << slot));
             const uint32_t ni = ngroup.x + rel;
@@ -260,7 +297,7 @@ GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restri
         if (!(ngroup.y & 0xFF000000u))
         {
             if (sp == 0) break;
-            ngroup = stack[--sp];
+            ngroup = stack.pop(sp, sh_col, sh_stride);
         }
     }
     return prim_best >= 0 ? make_float4(t_best, u_best, v_best, __int_as_float(prim_best))

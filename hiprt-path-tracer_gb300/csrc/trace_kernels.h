@@ -26,6 +26,7 @@ struct TraceConfig
     int32_t refill_below;    // persistent: refill when fewer lanes than this trace
     int32_t postpone_below;  // persistent: triangle steps need at least this many lanes
     int32_t blocks_per_sm;   // persistent grid
+    int32_t shared_stack;    // traversal-stack entries per thread in shared memory (0, 8 or 16)
 };
 
 TraceConfig default_trace_config(bool any_hit);

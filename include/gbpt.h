@@ -130,7 +130,9 @@ typedef struct gbpt_trace_config {
     int32_t refill_below;    /* PERSISTENT: refill a warp when fewer lanes than this trace (1..32) */
     int32_t postpone_below;  /* PERSISTENT: triangle steps need this many lanes, else postponed (0..32) */
     int32_t blocks_per_sm;   /* PERSISTENT and FETCH: blocks per SM of the grid (1..64) */
-    int32_t reserved[3];
+    int32_t shared_stack;    /* traversal-stack entries per thread kept in shared memory (0, 8 or 16;
+                                deeper entries in local memory); 0 in configurations written before */
+    int32_t reserved[2];
 } gbpt_trace_config;
 
 /* The configuration gbpt_trace_closest (any_hit = 0) / gbpt_trace_any (any_hit = 1) and their
@@ -144,8 +146,8 @@ GBPT_API gbpt_status gbpt_trace_closest_cfg(const gbpt_bvh* bvh, const float* or
 GBPT_API gbpt_status gbpt_trace_any_cfg(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
                                         const int32_t* last_prim, int64_t n_rays, uint8_t* occluded,
                                         const gbpt_trace_config* cfg, void* stream);
-/* Autotuner: times candidate configurations (kernel, block size, refill and postpone thresholds,
- * resident blocks) on the given device ray batch with CUDA events, coordinate by coordinate from
+/* Autotuner: times candidate configurations (kernel, block size, shared-memory stack depth, refill
+ * and postpone thresholds, resident blocks) on the given device ray batch with CUDA events, coordinate by coordinate from
  * the current best, each candidate run twice and its faster run kept; writes the fastest to *best
  * and its time per launch to *best_ms (either may be NULL). Results go to scratch memory. Stores
  * the result as the BVH's configuration for the class when store != 0. Synchronous. */

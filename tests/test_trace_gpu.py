@@ -125,8 +125,8 @@ def test_full_size_scene_sampled(cuda, oracle):
 
 @pytest.mark.parametrize("any_hit", [False, True])
 def test_every_launch_configuration_gives_identical_results(cuda, any_hit):
-    """Per-ray and persistent kernels over block sizes and refill / postpone thresholds return the
-    same hits bit for bit (the closest hit does not depend on the visiting order), and the
+    """Per-ray and persistent kernels over block sizes, refill / postpone thresholds and shared-memory
+    stack depths return the same hits bit for bit (the closest hit does not depend on the visiting order), and the
     autotuner returns a valid configuration whose results are again identical."""
     mesh, closest, _, shadow, _, _ = load_golden("terrain")
     bvh = gbpt.BVH(mesh.indices, mesh.positions)
@@ -134,10 +134,12 @@ def test_every_launch_configuration_gives_identical_results(cuda, any_hit):
     o, d, lp = _dev(rays, cuda)
     run = bvh.occluded_cfg if any_hit else bvh.closest_cfg
     base = run(o, d, lp, kernel=1, block=128).cpu().numpy()
-    configs = [dict(kernel=1, block=b) for b in (32, 64, 256)]
-    configs += [dict(kernel=2, block=b, refill_below=r, postpone_below=p, blocks_per_sm=s)
-                for b, r, p, s in [(128, 12, 8, 8), (64, 1, 0, 2), (256, 32, 32, 16), (128, 4, 24, 1), (32, 20, 4, 64)]]
-    configs += [dict(kernel=3, block=b, blocks_per_sm=s) for b, s in [(128, 8), (256, 4), (32, 64), (64, 1)]]
+    configs = [dict(kernel=1, block=b, shared_stack=sh) for b in (32, 64, 256) for sh in (0, 8, 16)]
+    configs += [dict(kernel=2, block=b, refill_below=r, postpone_below=p, blocks_per_sm=s, shared_stack=sh)
+                for b, r, p, s in [(128, 12, 8, 8), (64, 1, 0, 2), (256, 32, 32, 16), (128, 4, 24, 1), (32, 20, 4, 64)]
+                for sh in (0, 8, 16)]
+    configs += [dict(kernel=3, block=b, blocks_per_sm=s, shared_stack=sh)
+                for b, s in [(128, 8), (256, 4), (32, 64), (64, 1)] for sh in (0, 8, 16)]
     for cfg in configs:
         got = run(o, d, lp, **cfg).cpu().numpy()
         assert np.array_equal(got.view(np.uint8), base.view(np.uint8)), cfg
@@ -151,6 +153,7 @@ def test_trace_config_validation(cuda):
     from gbpt import GbptError
     mesh, *_ = load_golden("cornell")
     bvh = gbpt.BVH(mesh.indices, mesh.positions)
-    for bad in (dict(kernel=4), dict(block=96), dict(refill_below=0), dict(postpone_below=33), dict(blocks_per_sm=0)):
+    for bad in (dict(kernel=4), dict(block=96), dict(refill_below=0), dict(postpone_below=33), dict(blocks_per_sm=0),
+                dict(shared_stack=4), dict(shared_stack=-8)):
         with pytest.raises(GbptError):
             bvh.set_trace_config(False, **bad)
