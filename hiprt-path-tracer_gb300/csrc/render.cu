@@ -1312,6 +1312,17 @@ cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Qu
     return cudaGetLastError();
 }
 
+cudaError_t launch_trace_queue(const SceneView& s, const Queue& q, bool any_hit, int64_t capacity, int n_sm,
+                               cudaStream_t st)
+{
+    const int tgrid = grid_for(capacity, 128, n_sm * 16);
+    if (any_hit)
+        trace_queue_kernel<true><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, q, nullptr, nullptr);
+    else
+        trace_queue_kernel<false><<<tgrid, 128, 0, st>>>(s.bvh_nodes, s.bvh_tris, q, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next, const Queue& shadow,
                           const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st, const BatchJob* jobs,
                           const int32_t* job_of_slot)

@@ -98,6 +98,7 @@ struct gbpt_renderer
     int gb_cur = 0;
     gbpt::ReservoirBuf res[5];  // initial, temporal, spatial ping, spatial pong, previous
     float4* presampled = nullptr;  // light presampling records (null: off)
+    gbpt::InitialState initial_state{};  // per-pixel state between the initial-candidates phases
     int res_final = 0;
     bool has_prev = false;
     float prev_inverse_view[16];
@@ -963,6 +964,8 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
     r->presampled = k->do_light_presampling
                         ? M.alloc<float4>(2 * (size_t)k->presampling_subsets * k->presampling_subset_size)
                         : nullptr;
+    r->initial_state.cand = M.alloc<float4>(npix);
+    r->initial_state.meta = M.alloc<int4>(npix);
     cudaError_t e = M.err;
     for (int b = 0; b < 5 && e == cudaSuccess; b++)
     {
@@ -1003,7 +1006,10 @@ gbpt_status gbpt_pass_restir_di_initial(gbpt_renderer* r, void* stream)
     cudaError_t e = gbpt::launch_restir_gbuffer(r->scene->view, r->q[r->cur], gb, npix, r->n_sm, cs);
     if (e == cudaSuccess && r->presampled)
         e = gbpt::launch_restir_presample(r->scene->view, r->rc, k, r->presampled, r->n_sm, cs);
-    if (e == cudaSuccess) e = gbpt::launch_restir_initial(r->scene->view, r->rc, k, gb, r->res[0], r->n_sm, cs);
+    // its BSDF-candidate and visibility rays go through the bounce's free queues (left empty after)
+    if (e == cudaSuccess)
+        e = gbpt::launch_restir_initial(r->scene->view, r->rc, k, gb, r->res[0], r->initial_state, r->bsdfq,
+                                        r->q[r->cur ^ 1], r->shadow, r->capacity, r->n_sm, cs);
     r->res_final = 0;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI initial candidates");
 }

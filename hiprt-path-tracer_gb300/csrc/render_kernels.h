@@ -58,6 +58,10 @@ cudaError_t launch_camera(const RenderConst& rc, const PathBuffers& pb, const Qu
 // traversal + resolve). 'restir' (null buffers when ReSTIR DI is off) holds the final reservoirs
 // that replace next-event estimation at bounce 0.
 // jobs / job_of_slot (batched rendering, else null): each ray traverses its slot's job's BVH.
+// Closest-hit (any_hit = false: hits) or any-hit (occluded) traversal of a device-counted queue of
+// at most 'capacity' rays.
+cudaError_t launch_trace_queue(const SceneView& s, const Queue& q, bool any_hit, int64_t capacity, int n_sm,
+                               cudaStream_t st);
 cudaError_t launch_extend(const SceneView& s, const Queue& in, const Queue& next, const Queue& shadow,
                           const Queue& bsdfq, int64_t capacity, int n_sm, cudaStream_t st,
                           const BatchJob* jobs = nullptr, const int32_t* job_of_slot = nullptr);
@@ -85,7 +89,8 @@ cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuf
 cudaError_t launch_restir_presample(const SceneView& s, const RenderConst& rc, const RestirConst& k, float4* out,
                                     int n_sm, cudaStream_t st);
 cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
-                                  const ReservoirBuf& out, int n_sm, cudaStream_t st);
+                                  const ReservoirBuf& out, const InitialState& st, const Queue& qa, const Queue& qb,
+                                  const Queue& vis, int64_t queue_capacity, int n_sm, cudaStream_t stream);
 cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                    const GBuffer& gb_prev, const ReservoirBuf& initial, const ReservoirBuf& prev,
                                    const ReservoirBuf& out, int n_sm, cudaStream_t st);

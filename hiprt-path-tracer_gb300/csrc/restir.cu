@@ -9,8 +9,9 @@
 // default options: light candidates from the emissive triangles only (no envmap, no light
 // presampling), visibility reuse on, bias correction with visibility, no visibility in the
 // spatial target function, geometric-normal and plane-distance neighbour heuristics.
-// One thread per pixel; the few rays a pixel needs (BSDF candidate, visibility, bias correction)
-// are traced inline with the shared traversal core. Each pass draws from its own PCG stream per
+// One thread per pixel. The initial candidates' rays (BSDF candidates, visibility of the kept
+// sample) go through device queues traced by the traversal kernels between phases; the reuse
+// passes' rays (bias correction, visibility) are traced inline with the shared traversal core. Each pass draws from its own PCG stream per
 // pixel; spatial neighbour offsets come from one per-frame Xorshift32 stream shared by all pixels
 // (the reference's coalesced spatial reuse), regenerated for the counting and the reuse loops.
 #include <cuda_runtime.h>
@@ -266,112 +267,238 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuf
 }
 
 // ---------------------------------------------------------------------------------------------
-// initial candidates (InitialCandidates.h:180-538)
+// initial candidates (InitialCandidates.h:180-538) as wavefront phases: the light candidates and
+// the first BSDF candidate's direction (its ray appended to a queue), the queue traced by the
+// traversal kernels, the BSDF candidate resolved (and the next one's ray appended), and so on per
+// BSDF candidate; then the visibility rays of the kept samples, traced as one any-hit queue, and
+// the kill. Tracing inside this kernel ran at its occupancy (168 registers, three CTAs per SM):
+// the two rays of a 1080p frame cost 11.7 of its 17.8 ms. Random numbers are drawn in the
+// reference's order: the pixel's PCG state travels between the phases.
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) initial_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
-                                                      ReservoirBuf out)
+
+// the shared start of a pixel's phase: surface, material and medium
+struct InitialPixel
+{
+    Surface su;
+    bsdf::Material m;
+    bsdf::Medium md;
+};
+
+// draws BSDF candidate 'round' of a pixel: the direction and its ray (appended to 'rays'), or no
+// ray when its pdf is zero; the PCG state after the draw goes to the pixel state
+__device__ __forceinline__ void initial_bsdf_draw(const InitialPixel& px, bool hc, Pcg32& rng, const Queue& rays,
+                                                  const InitialState& st, int pixel)
+{
+    bsdf::Xorshift32 xr = bsdf_rng(rng);
+    V3 dir;
+    int lobe;
+    float pdf;
+    bsdf::sample(px.m, px.md, hc, px.su.view, px.su.ns, px.su.ng, xr, dir, lobe, pdf);
+    const bool want = pdf > 0.0f;
+    const int slot = warp_append(rays.count, want);
+    if (want)
+    {
+        rays.origin_tmin[slot] = f4(px.su.P, 0.0f);
+        rays.dir_tmax[slot] = f4(dir, 1.0e35f - 1.0e-4f);
+        rays.last_prim[slot] = px.su.prim;
+        rays.slot[slot] = pixel;
+    }
+    st.cand[pixel] = f4(dir, pdf);
+    st.meta[pixel] = make_int4((int)(uint32_t)rng.state, (int)(uint32_t)(rng.state >> 32), lobe, want ? slot : -1);
+}
+
+// the end of the candidates: normalisation, M = 1, and the visibility ray of the kept sample
+// (ReSTIR_DI_visibility_test_kill_reservoir, src/Device/includes/ReSTIR/Utils.h:25-64) appended to
+// 'vis' when visibility reuse is on and the sample needs one; else the reservoir is final
+__device__ __forceinline__ void initial_finish(const RestirConst& k, const Surface& su, Reservoir& r,
+                                               const ReservoirBuf& out, const InitialState& st, const Queue& vis,
+                                               int pixel)
+{
+    end_reservoir(r);
+    r.M = 1;
+    const bool test = k.visibility_reuse && !(r.ucw <= 0.0f && r.w_sum <= 0.0f) && !(r.flags & kRestirFlagUnoccluded);
+    const int slot = warp_append(vis.count, test);
+    if (test)
+    {
+        V3 dir = r.point - su.P;
+        const float dist = length(dir);
+        dir = dir / dist;
+        vis.origin_tmin[slot] = f4(su.P, 0.0f);
+        vis.dir_tmax[slot] = f4(dir, dist - 1.0e-4f);
+        vis.last_prim[slot] = su.prim;
+        vis.slot[slot] = pixel;
+    }
+    store_reservoir(out, pixel, r);
+    st.meta[pixel] = make_int4(0, 0, kInitialVisibility, test ? slot : -1);
+}
+
+__device__ __forceinline__ bool initial_load(const SceneView& s, const RestirConst& k, const GBuffer& gb, int pixel,
+                                             InitialPixel& px)
+{
+    px.su = load_surface(gb, pixel, k.camera_pos);
+    if (px.su.prim < 0 || s.n_emissive == 0) return false;
+    px.m = bsdf::load_material(s.pmats[px.su.mat]);
+    px.md = medium_of(px.su, px.m);
+    return true;
+}
+
+// phase 1: the light candidates, then BSDF candidate 0's direction (or the end when there is none)
+__global__ void __launch_bounds__(128, 3) initial_lights_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                                ReservoirBuf out, InitialState st, Queue rays,
+                                                                Queue vis)
 {
     const int n_pix = rc.width * rc.height;
     const bool hc = rc.ggx_height_correlated != 0;
     for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
     {
         Reservoir r = empty_reservoir();
-        const Surface su = load_surface(gb, pixel, k.camera_pos);
-        if (su.prim < 0 || s.n_emissive == 0)
+        InitialPixel px;
+        const bool live = initial_load(s, k, gb, pixel, px);
+        Pcg32 rng = pass_stream(k, pixel, 1);
+        if (live)
+        {
+            const Surface& su = px.su;
+            const float nl = (float)k.light_candidates, nb = (float)k.bsdf_candidates;
+            const int subset = k.presampled ? presampled_subset(k, pixel % rc.width, pixel / rc.width) : 0;
+            for (int c = 0; c < k.light_candidates; c++)
+            {
+                LightSample ls;
+                if (k.presampled)
+                {
+                    // a light of the tile's presampled subset, with the pdf it was drawn with
+                    const int e = subset * k.presample_size + rng.index(k.presample_size);
+                    const float4 a = __ldg(k.presampled + 2 * e), b = __ldg(k.presampled + 2 * e + 1);
+                    ls.point = xyz(a);
+                    ls.triangle = __float_as_int(a.w);
+                    ls.normal = xyz(b);
+                    ls.pdf_area = b.w;
+                    ls.emission = emission_of(s, ls.triangle);
+                }
+                else
+                    ls = sample_light(s, rc, rng);
+                V3 wi = ls.point - su.P;
+                const float dist = length(wi);
+                wi = wi / dist;
+                const float cosine = fmaxf(0.0f, dot(su.ns, wi));
+                float weight = 0.0f, p_hat = 0.0f;
+                if (cosine > 0.0f && ls.pdf_area > 0.0f)
+                {
+                    bsdf::Query q;
+                    q.view = su.view;
+                    q.ns = su.ns;
+                    q.ng = su.ng;
+                    q.light = wi;
+                    float bsdf_pdf;
+                    const V3 f = bsdf::eval(px.m, px.md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
+                    if (bsdf_pdf > 0.0f)
+                    {
+                        const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
+                        p_hat = luminance(f * ls.emission * dot(su.ns, wi) * (cos_l / (dist * dist)));
+                        const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
+                        const float mis = light_pdf == 0.0f ? 0.0f : light_pdf / (nl * light_pdf + nb * bsdf_pdf);
+                        weight = mis * p_hat / ls.pdf_area;
+                    }
+                }
+                add_candidate(r, ls.point, ls.triangle, 0, p_hat, weight, rng.next());
+            }
+        }
+        if (!live)
         {
             store_reservoir(out, pixel, r);
-            continue;
+            st.meta[pixel] = make_int4(0, 0, kInitialDone, -1);
         }
-        Pcg32 rng = pass_stream(k, pixel, 1);
-        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
-        const bsdf::Medium md = medium_of(su, m);
-        const float nl = (float)k.light_candidates, nb = (float)k.bsdf_candidates;
-        const int subset = k.presampled ? presampled_subset(k, pixel % rc.width, pixel / rc.width) : 0;
-
-        for (int c = 0; c < k.light_candidates; c++)
+        else if (k.bsdf_candidates > 0)
         {
-            LightSample ls;
-            if (k.presampled)
+            store_reservoir(out, pixel, r);
+            initial_bsdf_draw(px, hc, rng, rays, st, pixel);
+        }
+        else
+            initial_finish(k, px.su, r, out, st, vis, pixel);
+    }
+}
+
+// phase 2 (one launch per BSDF candidate): the traced candidate joins the reservoir; then the next
+// candidate's direction, or the end
+__global__ void __launch_bounds__(128, 3) initial_bsdf_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                              ReservoirBuf out, InitialState st, Queue traced,
+                                                              Queue rays, Queue vis, int round)
+{
+    const int n_pix = rc.width * rc.height;
+    const bool hc = rc.ggx_height_correlated != 0;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        const int4 meta = st.meta[pixel];
+        const bool live = meta.z >= 0;  // a lobe: the pixel still draws BSDF candidates
+        if (!live) continue;
+        InitialPixel px;
+        Reservoir r = empty_reservoir();
+        Pcg32 rng = pass_stream(k, pixel, 1);
+        {
+            initial_load(s, k, gb, pixel, px);
+            r = load_reservoir(out, pixel);
+            rng.state = (uint64_t)(uint32_t)meta.x | ((uint64_t)(uint32_t)meta.y << 32);
+            if (meta.w >= 0)
             {
-                // a light of the tile's presampled subset, with the pdf it was drawn with
-                const int e = subset * k.presample_size + rng.index(k.presample_size);
-                const float4 a = __ldg(k.presampled + 2 * e), b = __ldg(k.presampled + 2 * e + 1);
-                ls.point = xyz(a);
-                ls.triangle = __float_as_int(a.w);
-                ls.normal = xyz(b);
-                ls.pdf_area = b.w;
-                ls.emission = emission_of(s, ls.triangle);
-            }
-            else
-                ls = sample_light(s, rc, rng);
-            V3 wi = ls.point - su.P;
-            const float dist = length(wi);
-            wi = wi / dist;
-            const float cosine = fmaxf(0.0f, dot(su.ns, wi));
-            float weight = 0.0f, p_hat = 0.0f;
-            if (cosine > 0.0f && ls.pdf_area > 0.0f)
-            {
-                bsdf::Query q;
-                q.view = su.view;
-                q.ns = su.ns;
-                q.ng = su.ng;
-                q.light = wi;
-                float bsdf_pdf;
-                const V3 f = bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
-                if (bsdf_pdf > 0.0f)
+                const Surface& su = px.su;
+                const float nl = (float)k.light_candidates, nb = (float)k.bsdf_candidates;
+                const float4 cd = st.cand[pixel];
+                const V3 dir = xyz(cd);
+                const float pdf = cd.w;
+                const int lobe = meta.z;
+                const float4 h = traced.hits[meta.w];
+                const int lt = __float_as_int(h.w);
+                const V3 Le = lt >= 0 ? emission_of(s, lt) : v3(0.0f);
+                if (lt >= 0 && !is_black(Le))
                 {
-                    const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
-                    p_hat = luminance(f * ls.emission * dot(su.ns, wi) * (cos_l / (dist * dist)));
-                    const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
-                    const float mis = light_pdf == 0.0f ? 0.0f : light_pdf / (nl * light_pdf + nb * bsdf_pdf);
-                    weight = mis * p_hat / ls.pdf_area;
+                    const V3 point = su.P + dir * h.x;
+                    const int flags = kRestirFlagUnoccluded | (lobe & kRestirLobeMask);
+                    const float p_hat = target_function(s, hc, su, px.m, point, lt, flags, false);
+                    const V3 nlt = triangle_unit_normal(s, lt);
+                    const float cos_l = fmaxf(0.0f, dot(nlt, -dir));
+                    float light_pdf = 0.0f;
+                    if (!(dot(dir, su.ns) < 0.0f))
+                    {
+                        V3 a, b, cc;
+                        load_triangle(s, lt, a, b, cc);
+                        const float area = 0.5f * length(cross(b - a, cc - a));
+                        float pa = 1.0f / area;
+                        if (rc.light_sampling == GBPT_LIGHT_POWER)
+                            pa *= (luminance(Le) * area) / s.power_sum;
+                        else
+                            pa /= (float)s.n_emissive;
+                        light_pdf = area_to_solid_angle_pdf(pa, h.x, cos_l);
+                    }
+                    const float mis = pdf / (nb * pdf + nl * light_pdf);
+                    const float pdf_area = pdf / (h.x * h.x) * cos_l;
+                    // the back of a one-sided emitter: zero area pdf (the reference's weight would be 0/0)
+                    if (pdf_area > 0.0f) add_candidate(r, point, lt, flags, p_hat, mis * p_hat / pdf_area, rng.next());
                 }
             }
-            add_candidate(r, ls.point, ls.triangle, 0, p_hat, weight, rng.next());
         }
-
-        for (int c = 0; c < k.bsdf_candidates; c++)
+        if (round + 1 < k.bsdf_candidates)
         {
-            bsdf::Xorshift32 xr = bsdf_rng(rng);
-            V3 dir;
-            int lobe;
-            float pdf;
-            bsdf::sample(m, md, hc, su.view, su.ns, su.ng, xr, dir, lobe, pdf);
-            if (!(pdf > 0.0f)) continue;
-            uint32_t cn = 0, ct = 0;
-            const float4 h = core::trace_ray<false, false>(s.bvh_nodes, s.bvh_tris, f4(su.P, 0.0f),
-                                                           f4(dir, 1.0e35f - 1.0e-4f), su.prim, cn, ct);
-            const int lt = __float_as_int(h.w);
-            if (lt < 0) continue;
-            const V3 Le = emission_of(s, lt);
-            if (is_black(Le)) continue;
-            const V3 point = su.P + dir * h.x;
-            const int flags = kRestirFlagUnoccluded | (lobe & kRestirLobeMask);
-            const float p_hat = target_function(s, hc, su, m, point, lt, flags, false);
-            const V3 nlt = triangle_unit_normal(s, lt);
-            const float cos_l = fmaxf(0.0f, dot(nlt, -dir));
-            float light_pdf = 0.0f;
-            if (!(dot(dir, su.ns) < 0.0f))
-            {
-                V3 a, b, cc;
-                load_triangle(s, lt, a, b, cc);
-                const float area = 0.5f * length(cross(b - a, cc - a));
-                float pa = 1.0f / area;
-                if (rc.light_sampling == GBPT_LIGHT_POWER)
-                    pa *= (luminance(Le) * area) / s.power_sum;
-                else
-                    pa /= (float)s.n_emissive;
-                light_pdf = area_to_solid_angle_pdf(pa, h.x, cos_l);
-            }
-            const float mis = pdf / (nb * pdf + nl * light_pdf);
-            const float pdf_area = pdf / (h.x * h.x) * cos_l;
-            // the back of a one-sided emitter: zero area pdf (the reference's weight would be 0/0)
-            if (!(pdf_area > 0.0f)) continue;
-            add_candidate(r, point, lt, flags, p_hat, mis * p_hat / pdf_area, rng.next());
+            store_reservoir(out, pixel, r);
+            initial_bsdf_draw(px, hc, rng, rays, st, pixel);
         }
-        end_reservoir(r);
-        r.M = 1;
-        if (k.visibility_reuse) visibility_kill(s, r, su);
+        else
+            initial_finish(k, px.su, r, out, st, vis, pixel);
+    }
+}
+
+// phase 3: the visibility results of the kept samples
+__global__ void __launch_bounds__(256) initial_visibility_kernel(RenderConst rc, ReservoirBuf out, InitialState st,
+                                                                 Queue vis)
+{
+    const int n_pix = rc.width * rc.height;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        const int4 meta = st.meta[pixel];
+        if (meta.z != kInitialVisibility || meta.w < 0) continue;
+        Reservoir r = load_reservoir(out, pixel);
+        if (vis.occluded[meta.w])
+            r.ucw = -1.0f;
+        else
+            r.flags |= kRestirFlagUnoccluded;
         store_reservoir(out, pixel, r);
     }
 }
@@ -379,7 +506,7 @@ __global__ void __launch_bounds__(128) initial_kernel(SceneView s, RenderConst r
 // ---------------------------------------------------------------------------------------------
 // temporal reuse (TemporalReuse.h:50-298, pairwise MIS TemporalMISWeight.h:164-250)
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) temporal_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+__global__ void __launch_bounds__(128, 3) temporal_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
                                                        GBuffer gb_prev, ReservoirBuf initial, ReservoirBuf prev,
                                                        ReservoirBuf out)
 {
@@ -726,11 +853,38 @@ cudaError_t launch_restir_presample(const SceneView& s, const RenderConst& rc, c
 }
 
 cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
-                                  const ReservoirBuf& out, int n_sm, cudaStream_t st)
+                                  const ReservoirBuf& out, const InitialState& st, const Queue& qa, const Queue& qb,
+                                  const Queue& vis, int64_t queue_capacity, int n_sm, cudaStream_t stream)
 {
     const int64_t n = (int64_t)rc.width * rc.height;
-    initial_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, out);
-    return cudaGetLastError();
+    if (n > queue_capacity) return cudaErrorInvalidValue;
+    const int grid = grid_for(n, 128, n_sm * 16);
+    cudaError_t e = cudaSuccess;
+    for (const Queue* q : {&qa, &qb, &vis})
+        if (e == cudaSuccess) e = cudaMemsetAsync(q->count, 0, sizeof(int32_t), stream);
+    if (e != cudaSuccess) return e;
+    initial_lights_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, out, st, qa, vis);
+    // BSDF candidate c traces queue c % 2 and appends candidate c + 1's rays to the other one
+    for (int c = 0; c < k.bsdf_candidates && e == cudaSuccess; c++)
+    {
+        const Queue& traced = (c & 1) ? qb : qa;
+        const Queue& next = (c & 1) ? qa : qb;
+        e = launch_trace_queue(s, traced, false, n, n_sm, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(next.count, 0, sizeof(int32_t), stream);
+        if (e == cudaSuccess)
+            initial_bsdf_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, out, st, traced, next, vis, c);
+    }
+    if (e == cudaSuccess && k.visibility_reuse)
+    {
+        e = launch_trace_queue(s, vis, true, n, n_sm, stream);
+        if (e == cudaSuccess)
+            initial_visibility_kernel<<<grid_for(n, 256, n_sm * 8), 256, 0, stream>>>(rc, out, st, vis);
+    }
+    // the queues belong to the bounce's shading: leave them empty
+    for (const Queue* q : {&qa, &qb, &vis})
+        if (e == cudaSuccess) e = cudaMemsetAsync(q->count, 0, sizeof(int32_t), stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,

@@ -31,6 +31,16 @@ struct ReservoirBuf
     int4* w;
 };
 
+// Per-pixel state of the initial-candidates phases: the pending BSDF candidate (direction, pdf)
+// and (PCG state low, high, lobe or a status below, queue index of the pixel's ray or -1).
+struct InitialState
+{
+    float4* cand;
+    int4* meta;
+};
+constexpr int kInitialDone = -1;        // no candidates (no surface or no emitter): reservoir final
+constexpr int kInitialVisibility = -2;  // candidates done; meta.w = index in the visibility queue
+
 struct RestirConst
 {
     int32_t light_candidates, bsdf_candidates;
