@@ -99,6 +99,8 @@ struct gbpt_renderer
     gbpt::ReservoirBuf res[5];  // initial, temporal, spatial ping, spatial pong, previous
     float4* presampled = nullptr;  // light presampling records (null: off)
     gbpt::InitialState initial_state{};  // per-pixel state between the initial-candidates phases
+    int32_t* spatial_ray_of = nullptr;   // spatial reuse: bias-correction ray per pixel and neighbour
+    gbpt::Queue spatial_rays{};          // their any-hit queue (pixels x spatial neighbours)
     int res_final = 0;
     bool has_prev = false;
     float prev_inverse_view[16];
@@ -966,6 +968,14 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
                         : nullptr;
     r->initial_state.cand = M.alloc<float4>(npix);
     r->initial_state.meta = M.alloc<int4>(npix);
+    r->spatial_ray_of = nullptr;
+    std::memset(&r->spatial_rays, 0, sizeof(r->spatial_rays));
+    if (k->do_spatial || k->do_fused_spatiotemporal)
+    {
+        const int64_t n_rays = npix * (int64_t)k->spatial_neighbors;
+        r->spatial_ray_of = M.alloc<int32_t>(n_rays);
+        r->spatial_rays = make_queue(M, n_rays, false, true);
+    }
     cudaError_t e = M.err;
     for (int b = 0; b < 5 && e == cudaSuccess; b++)
     {
@@ -1048,10 +1058,13 @@ gbpt_status gbpt_pass_restir_di_spatial(gbpt_renderer* r, int32_t pass_index, vo
         return set_error(GBPT_ERROR_INVALID_ARG, "pass_index out of range");
     const int in = r->res_final;
     const int out = in == 2 ? 3 : 2;
+    if (!r->spatial_ray_of) return set_error(GBPT_ERROR_INVALID_ARG, "spatial reuse is not enabled on this renderer");
+    // its final visibility rays go through the bounce's shadow queue (left empty after)
     cudaError_t e = gbpt::launch_restir_spatial(r->scene->view, r->rc, restir_const(r), r->gb[r->gb_cur], r->res[in],
                                                 r->res[out], pass_index,
-                                                spatial_seed((uint32_t)r->iteration, pass_index, r->rc.seed), r->n_sm,
-                                                (cudaStream_t)stream);
+                                                spatial_seed((uint32_t)r->iteration, pass_index, r->rc.seed),
+                                                r->spatial_ray_of, r->spatial_rays, r->initial_state, r->shadow,
+                                                r->n_sm, (cudaStream_t)stream);
     r->res_final = out;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI spatial reuse");
 }

@@ -100,7 +100,8 @@ cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& 
                                          const ReservoirBuf& prev, const ReservoirBuf& out, int n_sm, cudaStream_t st);
 cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                   const ReservoirBuf& in, const ReservoirBuf& out, int pass, uint32_t neighbor_seed,
-                                  int n_sm, cudaStream_t st);
+                                  int32_t* ray_of, const Queue& rays, const InitialState& st, const Queue& vis,
+                                  int n_sm, cudaStream_t stream);
 cudaError_t launch_accumulate(const RenderConst& rc, const PathBuffers& pb, float* acc32, double* acc64, int n_sm,
                               cudaStream_t st);
 // Batched rendering (jobs: device table of n_jobs; iteration: device index of the iteration):

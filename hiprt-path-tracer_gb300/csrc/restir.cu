@@ -485,8 +485,9 @@ __global__ void __launch_bounds__(128, 3) initial_bsdf_kernel(SceneView s, Rende
     }
 }
 
-// phase 3: the visibility results of the kept samples
-__global__ void __launch_bounds__(256) initial_visibility_kernel(RenderConst rc, ReservoirBuf out, InitialState st,
+// the visibility results of the kept samples (initial candidates, spatial reuse): killed when
+// occluded, marked unoccluded otherwise
+__global__ void __launch_bounds__(256) visibility_apply_kernel(RenderConst rc, ReservoirBuf out, InitialState st,
                                                                  Queue vis)
 {
     const int n_pix = rc.width * rc.height;
@@ -593,9 +594,59 @@ __global__ void __launch_bounds__(128, 3) temporal_kernel(SceneView s, RenderCon
 // ---------------------------------------------------------------------------------------------
 // spatial reuse (SpatialReuse.h:43-322, pairwise MIS SpatialMISWeight.h:100-160)
 // ---------------------------------------------------------------------------------------------
+// spatial reuse, phase 1: the bias-correction rays. Each valid neighbour evaluates the centre's
+// sample with visibility (the MIS weight's c_at_n); the rays, from the neighbour's surface to the
+// sample, depend only on the input reservoirs and the G-buffer, so they are appended here (one
+// slot per pixel and neighbour in 'ray_of', -1 without a ray) and traced as one any-hit queue.
+__global__ void __launch_bounds__(128) spatial_rays_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                           ReservoirBuf in, uint32_t neighbor_seed, int32_t* ray_of,
+                                                           Queue rays)
+{
+    const int W = rc.width, H = rc.height, n_pix = W * H;
+    const bool hc = rc.ggx_height_correlated != 0;
+    const int K = k.spatial_neighbors;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        int32_t* slots = ray_of + (int64_t)pixel * K;
+        for (int j = 0; j < K; j++) slots[j] = -1;
+        const Surface su = load_surface(gb, pixel, k.camera_pos);
+        const Reservoir center = load_reservoir(in, pixel);
+        if (su.prim < 0 || !(center.M > 0 && center.ucw > 0.0f)) continue;
+        const int cx = pixel % W, cy = pixel / W;
+        bsdf::Xorshift32 nrng{neighbor_seed};
+        for (int j = 0; j < K; j++)
+        {
+            const int idx = spatial_neighbor(j, K, cx, cy, W, H, k.spatial_radius, nrng);
+            bool want = idx >= 0 && center.tri >= 0 && similar(gb, gb, idx, pixel, su.P, su.ng, k);
+            Surface ns_;
+            if (want)
+            {
+                ns_ = load_surface(gb, idx, k.camera_pos);
+                const bsdf::Material nm = bsdf::load_material(s.pmats[ns_.mat]);
+                // the target function without visibility; a ray only where it is positive
+                want = target_function(s, hc, ns_, nm, center.point, center.tri, center.flags, false) > 0.0f;
+            }
+            const int slot = warp_append(rays.count, want);
+            if (!want) continue;
+            V3 dir = center.point - ns_.P;
+            const float dist = length(dir);
+            dir = dir / dist;
+            rays.origin_tmin[slot] = f4(ns_.P, 0.0f);
+            rays.dir_tmax[slot] = f4(dir, dist - 1.0e-4f);
+            rays.last_prim[slot] = ns_.prim;
+            rays.slot[slot] = pixel;
+            slots[j] = slot;
+        }
+    }
+}
+
+// spatial reuse, phase 2 (SpatialReuse.h:43-322): the resampling with the traced bias-correction
+// visibility; the final visibility ray of the result goes to 'vis' (applied by
+// visibility_apply_kernel), the reservoir is stored here
 __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
                                                       ReservoirBuf in, ReservoirBuf out, int pass, int last_pass,
-                                                      uint32_t neighbor_seed)
+                                                      uint32_t neighbor_seed, const int32_t* __restrict__ ray_of,
+                                                      Queue traced, InitialState st, Queue visq)
 {
     const int W = rc.width, H = rc.height, n_pix = W * H;
     const bool hc = rc.ggx_height_correlated != 0;
@@ -607,6 +658,7 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
         if (su.prim < 0)
         {
             store_reservoir(out, pixel, center);
+            st.meta[pixel] = make_int4(0, 0, kInitialDone, -1);
             continue;
         }
         Pcg32 rng = pass_stream(k, pixel, 3 + pass);
@@ -657,7 +709,12 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
                 {
                     const Surface ns_ = load_surface(gb, idx, k.camera_pos);
                     const bsdf::Material nm = bsdf::load_material(s.pmats[ns_.mat]);
-                    const float c_at_n = target_function(s, hc, ns_, nm, center.point, center.tri, center.flags, vis);
+                    float c_at_n = target_function(s, hc, ns_, nm, center.point, center.tri, center.flags, false);
+                    if (vis && c_at_n > 0.0f)
+                    {
+                        const int32_t ray = ray_of[(int64_t)pixel * K + j];
+                        if (ray >= 0 && traced.occluded[ray]) c_at_n = 0.0f;
+                    }
                     const float nume_mc = center.p_hat / div * cM;
                     const float denom_mc = c_at_n * nsum + center.p_hat / div * cM;
                     const float conf = k.confidence_weights ? (nsum == 0.0f ? 0.0f : rM / nsum) : 1.0f;
@@ -676,7 +733,21 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
             }
         }
         end_with_normalization(o, 1.0f, 1.0f);
-        if (k.visibility_reuse && vis && (k.do_temporal || pass != last_pass)) visibility_kill(s, o, su);
+        // visibility reuse of the result (visibility_kill) through the any-hit queue
+        const bool test = k.visibility_reuse && vis && (k.do_temporal || pass != last_pass) &&
+                          !(o.ucw <= 0.0f && o.w_sum <= 0.0f) && !(o.flags & kRestirFlagUnoccluded);
+        const int slot = warp_append(visq.count, test);
+        if (test)
+        {
+            V3 dir = o.point - su.P;
+            const float dist = length(dir);
+            dir = dir / dist;
+            visq.origin_tmin[slot] = f4(su.P, 0.0f);
+            visq.dir_tmax[slot] = f4(dir, dist - 1.0e-4f);
+            visq.last_prim[slot] = su.prim;
+            visq.slot[slot] = pixel;
+        }
+        st.meta[pixel] = make_int4(0, 0, kInitialVisibility, slot);
         store_reservoir(out, pixel, o);
     }
 }
@@ -878,7 +949,7 @@ cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, con
     {
         e = launch_trace_queue(s, vis, true, n, n_sm, stream);
         if (e == cudaSuccess)
-            initial_visibility_kernel<<<grid_for(n, 256, n_sm * 8), 256, 0, stream>>>(rc, out, st, vis);
+            visibility_apply_kernel<<<grid_for(n, 256, n_sm * 8), 256, 0, stream>>>(rc, out, st, vis);
     }
     // the queues belong to the bounce's shading: leave them empty
     for (const Queue* q : {&qa, &qb, &vis})
@@ -907,12 +978,27 @@ cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& 
 
 cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                   const ReservoirBuf& in, const ReservoirBuf& out, int pass, uint32_t neighbor_seed,
-                                  int n_sm, cudaStream_t st)
+                                  int32_t* ray_of, const Queue& rays, const InitialState& st, const Queue& vis,
+                                  int n_sm, cudaStream_t stream)
 {
     const int64_t n = (int64_t)rc.width * rc.height;
-    spatial_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, in, out, pass, k.spatial_passes - 1,
-                                                                 neighbor_seed);
-    return cudaGetLastError();
+    const int grid = grid_for(n, 128, n_sm * 16);
+    cudaError_t e = cudaMemsetAsync(rays.count, 0, sizeof(int32_t), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(vis.count, 0, sizeof(int32_t), stream);
+    if (e != cudaSuccess) return e;
+    if (k.bias_correction_visibility)
+    {
+        spatial_rays_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, in, neighbor_seed, ray_of, rays);
+        e = launch_trace_queue(s, rays, true, n * k.spatial_neighbors, n_sm, stream);
+    }
+    if (e == cudaSuccess)
+        spatial_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, in, out, pass, k.spatial_passes - 1, neighbor_seed,
+                                                 ray_of, rays, st, vis);
+    if (e == cudaSuccess) e = launch_trace_queue(s, vis, true, n, n_sm, stream);
+    if (e == cudaSuccess) visibility_apply_kernel<<<grid_for(n, 256, n_sm * 8), 256, 0, stream>>>(rc, out, st, vis);
+    if (e == cudaSuccess) e = cudaMemsetAsync(vis.count, 0, sizeof(int32_t), stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
 }
 
 }  // namespace gbpt
