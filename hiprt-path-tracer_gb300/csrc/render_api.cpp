@@ -101,6 +101,8 @@ struct gbpt_renderer
     gbpt::InitialState initial_state{};  // per-pixel state between the initial-candidates phases
     int32_t* spatial_ray_of = nullptr;   // spatial reuse: bias-correction ray per pixel and neighbour
     gbpt::Queue spatial_rays{};          // their any-hit queue (pixels x spatial neighbours)
+    int2* temporal_ray_of = nullptr;     // temporal reuse: its two bias-correction rays per pixel
+    gbpt::Queue temporal_rays{};         // their any-hit queue (2 x pixels)
     int res_final = 0;
     bool has_prev = false;
     float prev_inverse_view[16];
@@ -970,6 +972,13 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
     r->initial_state.meta = M.alloc<int4>(npix);
     r->spatial_ray_of = nullptr;
     std::memset(&r->spatial_rays, 0, sizeof(r->spatial_rays));
+    r->temporal_ray_of = nullptr;
+    std::memset(&r->temporal_rays, 0, sizeof(r->temporal_rays));
+    if (k->do_temporal)
+    {
+        r->temporal_ray_of = M.alloc<int2>(npix);
+        r->temporal_rays = make_queue(M, 2 * npix, false, true);
+    }
     if (k->do_spatial || k->do_fused_spatiotemporal)
     {
         const int64_t n_rays = npix * (int64_t)k->spatial_neighbors;
@@ -1031,8 +1040,10 @@ gbpt_status gbpt_pass_restir_di_temporal(gbpt_renderer* r, void* stream)
     gbpt::RestirConst k = restir_const(r);
     if (!view_projection(r->prev_inverse_view, r->rc.inverse_projection, k.prev_view_projection))
         return set_error(GBPT_ERROR_INVALID_ARG, "the previous camera matrices are singular");
+    if (!r->temporal_ray_of) return set_error(GBPT_ERROR_INVALID_ARG, "temporal reuse is not enabled on this renderer");
     cudaError_t e = gbpt::launch_restir_temporal(r->scene->view, r->rc, k, r->gb[r->gb_cur], r->gb[r->gb_cur ^ 1],
-                                                 r->res[0], r->res[4], r->res[1], r->n_sm, (cudaStream_t)stream);
+                                                 r->res[0], r->res[4], r->res[1], r->temporal_ray_of, r->temporal_rays,
+                                                 r->n_sm, (cudaStream_t)stream);
     r->res_final = 1;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI temporal reuse");
 }

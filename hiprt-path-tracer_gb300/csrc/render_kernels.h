@@ -93,7 +93,7 @@ cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, con
                                   const Queue& vis, int64_t queue_capacity, int n_sm, cudaStream_t stream);
 cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                    const GBuffer& gb_prev, const ReservoirBuf& initial, const ReservoirBuf& prev,
-                                   const ReservoirBuf& out, int n_sm, cudaStream_t st);
+                                   const ReservoirBuf& out, int2* ray_of, const Queue& rays, int n_sm, cudaStream_t st);
 // Fused spatiotemporal reuse: initial + previous final reservoirs (and G-buffers) -> out
 cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& rc, const RestirConst& k,
                                          const GBuffer& gb, const GBuffer& gb_prev, const ReservoirBuf& initial,

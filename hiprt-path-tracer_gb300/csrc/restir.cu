@@ -507,9 +507,83 @@ __global__ void __launch_bounds__(256) visibility_apply_kernel(RenderConst rc, R
 // ---------------------------------------------------------------------------------------------
 // temporal reuse (TemporalReuse.h:50-298, pairwise MIS TemporalMISWeight.h:164-250)
 // ---------------------------------------------------------------------------------------------
+// The temporal neighbour of a pixel (UtilsTemporal.h:27-98): backprojection into the previous
+// frame, then up to 'temporal_search_count' jittered tries; -1 when none is similar. Draws from
+// 'rng' in the reference's order.
+__device__ __forceinline__ int temporal_neighbor(const RestirConst& k, const GBuffer& gb, const GBuffer& gb_prev, int W,
+                                                 int H, int pixel, const Surface& su, Pcg32& rng)
+{
+    const V3 ndc = mat_x_point(k.prev_view_projection, su.P);
+    const float px = (ndc.x + 1.0f) * 0.5f * (float)W - 0.5f;
+    const float py = (ndc.y + 1.0f) * 0.5f * (float)H - 0.5f;
+    for (int i = 0; i < k.temporal_search_count + 1; i++)
+    {
+        float ox = 0.0f, oy = 0.0f;
+        if (i > 0)
+        {
+            ox = (rng.next() - 0.5f) * k.temporal_search_radius;
+            oy = (rng.next() - 0.5f) * k.temporal_search_radius;
+        }
+        const int tx = (int)roundf(px + ox), ty = (int)roundf(py + oy);
+        if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
+        const int t_idx = tx + ty * W;
+        if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, k)) return t_idx;
+    }
+    return -1;
+}
+
+// appends the shadow ray of a target-function evaluation (from P to the sample) when 'want'
+__device__ __forceinline__ int append_sample_ray(const Queue& q, bool want, V3 P, V3 point, int skip, int pixel)
+{
+    const int slot = warp_append(q.count, want);
+    if (want)
+    {
+        V3 dir = point - P;
+        const float dist = length(dir);
+        dir = dir / dist;
+        q.origin_tmin[slot] = f4(P, 0.0f);
+        q.dir_tmax[slot] = f4(dir, dist - 1.0e-4f);
+        q.last_prim[slot] = skip;
+        q.slot[slot] = pixel;
+    }
+    return slot;
+}
+
+// temporal reuse, phase 1: the two bias-correction rays of a pixel (the temporal sample seen from
+// the pixel, the pixel's initial sample seen from the temporal neighbour), appended where their
+// target functions without visibility are positive; slots in 'ray_of' (-1: no ray)
+__global__ void __launch_bounds__(128, 3) temporal_rays_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
+                                                               GBuffer gb_prev, ReservoirBuf initial, ReservoirBuf prev,
+                                                               int2* ray_of, Queue rays)
+{
+    const int W = rc.width, H = rc.height, n_pix = W * H;
+    const bool hc = rc.ggx_height_correlated != 0;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        ray_of[pixel] = make_int2(-1, -1);
+        const Reservoir init = load_reservoir(initial, pixel);
+        const Surface su = load_surface(gb, pixel, k.camera_pos);
+        if (su.prim < 0 || !k.has_prev) continue;
+        Pcg32 rng = pass_stream(k, pixel, 2);
+        const int t_idx = temporal_neighbor(k, gb, gb_prev, W, H, pixel, su, rng);
+        if (t_idx < 0) continue;
+        const Reservoir tn = load_reservoir(prev, t_idx);
+        const Surface ts = load_surface(gb_prev, t_idx, k.prev_camera_pos);
+        if (tn.M == 0 || ts.prim < 0 || !is_black(xyz(s.materials[ts.mat].emission))) continue;
+        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bsdf::Material tm = bsdf::load_material(s.pmats[ts.mat]);
+        const bool a = tn.ucw > 0.0f && target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, false) > 0.0f;
+        const bool b = target_function(s, hc, ts, tm, init.point, init.tri, init.flags, false) > 0.0f;
+        const int sa = append_sample_ray(rays, a, su.P, tn.point, su.prim, pixel);
+        const int sb = append_sample_ray(rays, b, ts.P, init.point, ts.prim, pixel);
+        ray_of[pixel] = make_int2(a ? sa : -1, b ? sb : -1);
+    }
+}
+
+// temporal reuse, phase 2 (TemporalReuse.h:50-298): the resampling with the traced visibility
 __global__ void __launch_bounds__(128, 3) temporal_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
                                                        GBuffer gb_prev, ReservoirBuf initial, ReservoirBuf prev,
-                                                       ReservoirBuf out)
+                                                       ReservoirBuf out, const int2* __restrict__ ray_of, Queue traced)
 {
     const int W = rc.width, H = rc.height, n_pix = W * H;
     const bool hc = rc.ggx_height_correlated != 0;
@@ -523,25 +597,7 @@ __global__ void __launch_bounds__(128, 3) temporal_kernel(SceneView s, RenderCon
             continue;
         }
         Pcg32 rng = pass_stream(k, pixel, 2);
-        // backprojection into the previous frame, then up to 'temporal_search_count' jittered tries
-        const V3 ndc = mat_x_point(k.prev_view_projection, su.P);
-        const float px = (ndc.x + 1.0f) * 0.5f * (float)W - 0.5f;
-        const float py = (ndc.y + 1.0f) * 0.5f * (float)H - 0.5f;
-        int t_idx = -1;
-        for (int i = 0; i < k.temporal_search_count + 1; i++)
-        {
-            float ox = 0.0f, oy = 0.0f;
-            if (i > 0)
-            {
-                ox = (rng.next() - 0.5f) * k.temporal_search_radius;
-                oy = (rng.next() - 0.5f) * k.temporal_search_radius;
-            }
-            const int tx = (int)roundf(px + ox), ty = (int)roundf(py + oy);
-            if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
-            t_idx = tx + ty * W;
-            if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, k)) break;
-            t_idx = -1;
-        }
+        const int t_idx = temporal_neighbor(k, gb, gb_prev, W, H, pixel, su, rng);
         if (t_idx < 0)
         {
             store_reservoir(out, pixel, init);
@@ -557,16 +613,19 @@ __global__ void __launch_bounds__(128, 3) temporal_kernel(SceneView s, RenderCon
         const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
         const bsdf::Material tm = bsdf::load_material(s.pmats[ts.mat]);
         const bool vis = k.bias_correction_visibility != 0;
+        const int2 rays = vis ? ray_of[pixel] : make_int2(-1, -1);
         Reservoir o = empty_reservoir();
 
         // temporal neighbour, pairwise MIS weight against the canonical (initial) reservoir
-        const float t_at_center = tn.ucw > 0.0f ? target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, vis) : 0.0f;
+        float t_at_center = tn.ucw > 0.0f ? target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, false) : 0.0f;
+        if (vis && t_at_center > 0.0f && rays.x >= 0 && traced.occluded[rays.x]) t_at_center = 0.0f;
         const float tM = k.confidence_weights ? (float)tn.M : 1.0f;
         const float cM = k.confidence_weights ? (float)init.M : 1.0f;
         const float nsum = k.confidence_weights ? (float)tn.M : 1.0f;
         const float denom = tn.p_hat * nsum + t_at_center * cM;
         const float mi = denom == 0.0f ? 0.0f : tn.p_hat * tM / denom;
-        const float c_at_neighbor = target_function(s, hc, ts, tm, init.point, init.tri, init.flags, vis);
+        float c_at_neighbor = target_function(s, hc, ts, tm, init.point, init.tri, init.flags, false);
+        if (vis && c_at_neighbor > 0.0f && rays.y >= 0 && traced.occluded[rays.y]) c_at_neighbor = 0.0f;
         const float denom_mc = c_at_neighbor * nsum + init.p_hat * cM;
         float mc = 0.0f;
         if (denom_mc != 0.0f) mc += init.p_hat * cM / denom_mc * (k.confidence_weights ? tM / nsum : 1.0f);
@@ -960,11 +1019,23 @@ cudaError_t launch_restir_initial(const SceneView& s, const RenderConst& rc, con
 
 cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                    const GBuffer& gb_prev, const ReservoirBuf& initial, const ReservoirBuf& prev,
-                                   const ReservoirBuf& out, int n_sm, cudaStream_t st)
+                                   const ReservoirBuf& out, int2* ray_of, const Queue& rays, int n_sm, cudaStream_t st)
 {
     const int64_t n = (int64_t)rc.width * rc.height;
-    temporal_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, gb_prev, initial, prev, out);
-    return cudaGetLastError();
+    const int grid = grid_for(n, 128, n_sm * 16);
+    cudaError_t e = cudaSuccess;
+    if (k.bias_correction_visibility && k.has_prev)
+    {
+        e = cudaMemsetAsync(rays.count, 0, sizeof(int32_t), st);
+        if (e == cudaSuccess)
+        {
+            temporal_rays_kernel<<<grid, 128, 0, st>>>(s, rc, k, gb, gb_prev, initial, prev, ray_of, rays);
+            e = launch_trace_queue(s, rays, true, 2 * n, n_sm, st);
+        }
+    }
+    if (e == cudaSuccess) temporal_kernel<<<grid, 128, 0, st>>>(s, rc, k, gb, gb_prev, initial, prev, out, ray_of, rays);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& rc, const RestirConst& k,
