@@ -202,7 +202,10 @@ def _relmse(img, ref):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
+RENDER_WORKLOADS = ("cornell", "envmap", "restir", "guided", "guided_indirect_cornell", "batch")
+
+
+def render_workloads(log, guided_res=(480, 270), cpu_baseline=True, only=RENDER_WORKLOADS):
     """Path-tracing workloads (one GPU, inputs resident; timed with CUDA events on the current stream):
 
     cornell     the Cornell box, 256 x 256, 64 launches x 1 spp, 4 bounces, RR from bounce 3, uniform
@@ -243,6 +246,27 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
     # ---- Cornell box ----
     cb = scenes.cornell_box()
     cscene = gbpt.Scene.from_cornell(cb)
+    if "cornell" in only:
+        cornell_workload(out, cb, cscene, timed, cpu_baseline)
+    # ---- the Cornell box under an importance-sampled environment map ----
+    if "envmap" in only:
+        out["envmap"] = envmap_workload(timed, cscene)
+    del cscene
+    if "restir" in only or "guided" in only:
+        many_light_workloads(out, log, timed, guided_res, only)
+    # ---- guided against plain on the indirectly lit Cornell box ----
+    if "guided_indirect_cornell" in only:
+        out["guided_indirect_cornell"] = guided_indirect_cornell(timed)
+    torch.cuda.empty_cache()
+    # ---- batched jobs ----
+    if "batch" in only:
+        out["batch"] = batch_workload(timed, log)
+    return out
+
+
+def cornell_workload(out, cb, cscene, timed, cpu_baseline):
+    import torch
+    import gbpt
     ref = gbpt.Renderer(cscene, gbpt.cornell_settings(256, 256, samples_per_launch=256, seed=1000))
     ref.render(64)
     torch.cuda.synchronize()
@@ -272,10 +296,15 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
         dt = time.perf_counter() - t0
         out["cornell"]["cpu_baseline"] = {"value": 256 * 256 * spp / dt, "unit": "samples/s", "cores": cores,
                                           "kind": "port", "sample": f"256x256 x {spp} spp, {dt:.2f}s"}
-    # ---- the Cornell box under an importance-sampled environment map ----
-    out["envmap"] = envmap_workload(timed, cscene)
-    del cscene
 
+
+def many_light_workloads(out, log, timed, guided_res, only):
+    import numpy as np
+    import torch
+    import gbpt
+    from gbpt import guide, scenes
+    from gbpt.render import (BSDF_PRINCIPLED, LIGHT_POWER, RenderSettings, guide_render_settings, look_at_camera,
+                             restir_di_settings)
     # ---- many-light principled scene ----
     t0 = time.time()
     S = scenes.many_light_scene()
@@ -303,6 +332,14 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
         del r
         return frame_ms, st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
 
+    if "restir" in only:
+        restir_workload(out, restir_frames)
+    if "guided" in only:
+        guided_workload(out, scene, S, settings, timed, guided_res, log)
+    del scene
+
+
+def restir_workload(out, restir_frames):
     frame_ms, rays = restir_frames()
     tot = sum(frame_ms)
     fused_ms, _ = restir_frames(do_fused_spatiotemporal=1)
@@ -315,6 +352,14 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
                      "fused_and_light_presampling_ms_per_frame": sum(fused_ps_ms) / 8,
                      "light_presampling": "128 subsets x 1024 lights, 8x8-pixel tiles"}
 
+
+
+def guided_workload(out, scene, S, settings, timed, guided_res, log):
+    import numpy as np
+    import torch
+    import gbpt
+    from gbpt import guide
+    from gbpt.render import guide_render_settings, restir_di_settings
     # ---- guided against plain, both with ReSTIR DI at the primary vertex (configs[2]'s plain
     # method; the guide acts on the continuations and on later bounces' BSDF technique) ----
     W, H = guided_res
@@ -363,13 +408,6 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True):
                      "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg), "guide_error_flag": gd.error_flag(),
                      "primary_direct_only_relmse": float(np.mean([b for _, b in direct])),
                      "primary_direct_share_of_relmse": float(np.mean([b for _, b in direct])) / ep}
-    # ---- guided against plain on the indirectly lit Cornell box ----
-    out["guided_indirect_cornell"] = guided_indirect_cornell(timed)
-    del scene
-    torch.cuda.empty_cache()
-    # ---- batched jobs ----
-    out["batch"] = batch_workload(timed, log)
-    return out
 
 
 def envmap_workload(timed, cscene, res=512, launches=32):
@@ -596,6 +634,8 @@ def main():
     ap.add_argument("--ref-fraction", type=float, default=1.0 / 256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the path-tracing workloads")
+    ap.add_argument("--workloads", default=",".join(RENDER_WORKLOADS),
+                    help="comma-separated path-tracing workloads to run (default: all)")
     ap.add_argument("--configs", default=None,
                     help="JSON {primary, bounce, shadow} launch configurations to use instead of autotuning")
     ap.add_argument("--small", action="store_true",
@@ -793,7 +833,11 @@ def main():
     if rank == 0 and not args.no_render:
         del bvh
         torch.cuda.empty_cache()
-        line["render"] = render_workloads(log, cpu_baseline=not args.no_cpu_baseline)
+        only = tuple(w for w in args.workloads.split(",") if w)
+        unknown = [w for w in only if w not in RENDER_WORKLOADS]
+        if unknown:
+            raise SystemExit(f"unknown workloads {unknown}; choose from {RENDER_WORKLOADS}")
+        line["render"] = render_workloads(log, cpu_baseline=not args.no_cpu_baseline, only=only)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
