@@ -981,7 +981,7 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
     }
     if (k->do_spatial || k->do_fused_spatiotemporal)
     {
-        const int64_t n_rays = npix * (int64_t)k->spatial_neighbors;
+        const int64_t n_rays = npix * (int64_t)(k->spatial_neighbors + 2);  // fused: + 2 temporal rays
         r->spatial_ray_of = M.alloc<int32_t>(n_rays);
         r->spatial_rays = make_queue(M, n_rays, false, true);
     }
@@ -1055,8 +1055,11 @@ gbpt_status gbpt_pass_restir_di_spatiotemporal(gbpt_renderer* r, void* stream)
     gbpt::RestirConst k = restir_const(r);
     if (!view_projection(r->prev_inverse_view, r->rc.inverse_projection, k.prev_view_projection))
         return set_error(GBPT_ERROR_INVALID_ARG, "the previous camera matrices are singular");
+    if (!r->spatial_ray_of) return set_error(GBPT_ERROR_INVALID_ARG, "spatial reuse is not enabled on this renderer");
     cudaError_t e = gbpt::launch_restir_spatiotemporal(r->scene->view, r->rc, k, r->gb[r->gb_cur], r->gb[r->gb_cur ^ 1],
-                                                       r->res[0], r->res[4], r->res[2], r->n_sm, (cudaStream_t)stream);
+                                                       r->res[0], r->res[4], r->res[2], r->spatial_ray_of,
+                                                       r->spatial_rays, r->initial_state, r->shadow, r->n_sm,
+                                                       (cudaStream_t)stream);
     r->res_final = 2;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "ReSTIR DI spatiotemporal reuse");
 }

@@ -97,7 +97,9 @@ cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, co
 // Fused spatiotemporal reuse: initial + previous final reservoirs (and G-buffers) -> out
 cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& rc, const RestirConst& k,
                                          const GBuffer& gb, const GBuffer& gb_prev, const ReservoirBuf& initial,
-                                         const ReservoirBuf& prev, const ReservoirBuf& out, int n_sm, cudaStream_t st);
+                                         const ReservoirBuf& prev, const ReservoirBuf& out, int32_t* ray_of,
+                                         const Queue& rays, const InitialState& st, const Queue& vis, int n_sm,
+                                         cudaStream_t stream);
 cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
                                   const ReservoirBuf& in, const ReservoirBuf& out, int pass, uint32_t neighbor_seed,
                                   int32_t* ray_of, const Queue& rays, const InitialState& st, const Queue& vis,

@@ -820,9 +820,93 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
 // seeded per pixel by one draw of the pixel's stream. As in the reference's fused kernel, an
 // emissive temporal neighbour is resampled.
 // ---------------------------------------------------------------------------------------------
+// fused spatiotemporal reuse, phase 1: the bias-correction rays, replaying the pixel's neighbour
+// seed, temporal search and neighbour offsets from its PCG stream. Slots per pixel (K + 2): the
+// temporal sample seen from the pixel, the pixel's initial sample seen from the temporal
+// neighbour, then from each spatial neighbour; -1 without a ray.
+__global__ void __launch_bounds__(128, 3) spatiotemporal_rays_kernel(SceneView s, RenderConst rc, RestirConst k,
+                                                                     GBuffer gb, GBuffer gb_prev, ReservoirBuf initial,
+                                                                     ReservoirBuf prev, int32_t* ray_of, Queue rays)
+{
+    const int W = rc.width, H = rc.height, n_pix = W * H;
+    const bool hc = rc.ggx_height_correlated != 0;
+    const int K = k.spatial_neighbors;
+    for (int pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < n_pix; pixel += gridDim.x * blockDim.x)
+    {
+        int32_t* slots = ray_of + (int64_t)pixel * (K + 2);
+        for (int j = 0; j < K + 2; j++) slots[j] = -1;
+        const Reservoir init = load_reservoir(initial, pixel);
+        const Surface su = load_surface(gb, pixel, k.camera_pos);
+        if (su.prim < 0 || !k.has_prev) continue;
+        Pcg32 rng = pass_stream(k, pixel, 2);
+        uint32_t nseed = rng.next_u32();
+        if (nseed == 0u) nseed = 0x9E3779B9u;
+        const V3 ndc = mat_x_point(k.prev_view_projection, su.P);
+        const float px = (ndc.x + 1.0f) * 0.5f * (float)W - 0.5f;
+        const float py = (ndc.y + 1.0f) * 0.5f * (float)H - 0.5f;
+        const int tx0 = (int)roundf(px), ty0 = (int)roundf(py);
+        const int t_idx = temporal_neighbor(k, gb, gb_prev, W, H, pixel, su, rng);
+        const Reservoir tn = t_idx >= 0 ? load_reservoir(prev, t_idx) : empty_reservoir();
+        const bool t_ok = t_idx >= 0 && tn.M > 0;
+        bsdf::Xorshift32 nrng{nseed};
+        int m_sum = t_ok ? tn.M : 0;
+        uint32_t cache = 0;
+        for (int j = 0; j < K; j++)
+        {
+            const int idx = spatial_neighbor(j, K, tx0, ty0, W, H, k.spatial_radius, nrng);
+            if (idx < 0 || !similar(gb_prev, gb, idx, pixel, su.P, su.ng, k)) continue;
+            m_sum += load_reservoir(prev, idx).M;
+            cache |= 1u << j;
+        }
+        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bool update_mc = init.M > 0 && init.ucw > 0.0f;
+        if (t_ok)
+        {
+            const bool a = tn.ucw > 0.0f && target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, false) > 0.0f;
+            slots[0] = append_sample_ray(rays, a, su.P, tn.point, su.prim, pixel);
+            bool b = false;
+            Surface nsu = su;  // replaced by the neighbour's surface when it is evaluated
+            if (update_mc)
+            {
+                nsu = load_surface(gb_prev, t_idx, k.prev_camera_pos);
+                const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
+                b = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, false) > 0.0f;
+            }
+            slots[1] = append_sample_ray(rays, b, nsu.P, init.point, nsu.prim, pixel);
+            if (!a) slots[0] = -1;
+            if (!b) slots[1] = -1;
+        }
+        if (!update_mc || m_sum == 0) continue;  // the spatial neighbours are not visited
+        nrng = bsdf::Xorshift32{nseed};
+        for (int j = 0; j < K; j++)
+        {
+            bool want = false;
+            Surface nsu = su;  // replaced by the neighbour's surface when it is evaluated
+            if (!(cache & (1u << j)))
+            {
+                nrng();
+                nrng();
+            }
+            else
+            {
+                const int idx = spatial_neighbor(j, K, tx0, ty0, W, H, k.spatial_radius, nrng);
+                if (idx >= 0)
+                {
+                    nsu = load_surface(gb_prev, idx, k.prev_camera_pos);
+                    const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
+                    want = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, false) > 0.0f;
+                }
+            }
+            const int slot = append_sample_ray(rays, want, nsu.P, init.point, nsu.prim, pixel);
+            if (want) slots[2 + j] = slot;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
                                                              GBuffer gb_prev, ReservoirBuf initial, ReservoirBuf prev,
-                                                             ReservoirBuf out)
+                                                             ReservoirBuf out, const int32_t* __restrict__ ray_of,
+                                                             Queue traced, InitialState st, Queue visq)
 {
     const int W = rc.width, H = rc.height, n_pix = W * H;
     const bool hc = rc.ggx_height_correlated != 0;
@@ -834,8 +918,10 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
         if (su.prim < 0 || !k.has_prev)
         {
             store_reservoir(out, pixel, init);
+            st.meta[pixel] = make_int4(0, 0, kInitialDone, -1);
             continue;
         }
+        const int32_t* slots = ray_of + (int64_t)pixel * (K + 2);
         Pcg32 rng = pass_stream(k, pixel, 2);
         uint32_t nseed = rng.next_u32();
         if (nseed == 0u) nseed = 0x9E3779B9u;
@@ -843,21 +929,7 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
         const float px = (ndc.x + 1.0f) * 0.5f * (float)W - 0.5f;
         const float py = (ndc.y + 1.0f) * 0.5f * (float)H - 0.5f;
         const int tx0 = (int)roundf(px), ty0 = (int)roundf(py);
-        int t_idx = -1;
-        for (int i = 0; i < k.temporal_search_count + 1; i++)
-        {
-            float ox = 0.0f, oy = 0.0f;
-            if (i > 0)
-            {
-                ox = (rng.next() - 0.5f) * k.temporal_search_radius;
-                oy = (rng.next() - 0.5f) * k.temporal_search_radius;
-            }
-            const int tx = (int)roundf(px + ox), ty = (int)roundf(py + oy);
-            if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
-            t_idx = tx + ty * W;
-            if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, k)) break;
-            t_idx = -1;
-        }
+        const int t_idx = temporal_neighbor(k, gb, gb_prev, W, H, pixel, su, rng);
         const Reservoir tn = t_idx >= 0 ? load_reservoir(prev, t_idx) : empty_reservoir();
         const bool t_ok = t_idx >= 0 && tn.M > 0;
         // valid spatial neighbours and their confidence (count_valid_spatiotemporal_neighbors)
@@ -911,8 +983,8 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
             const Reservoir nb = j < 0 ? tn : (j == K ? init : load_reservoir(prev, idx));
             float t_at_center = 0.0f;
             if (nb.ucw > 0.0f)
-                t_at_center = j == K ? nb.p_hat
-                                     : target_function(s, hc, su, m, nb.point, nb.tri, nb.flags, j < 0 && vis);
+                t_at_center = j == K ? nb.p_hat : target_function(s, hc, su, m, nb.point, nb.tri, nb.flags, false);
+            if (j < 0 && vis && t_at_center > 0.0f && slots[0] >= 0 && traced.occluded[slots[0]]) t_at_center = 0.0f;
             float mis;
             if (j < K)
             {
@@ -924,7 +996,9 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
                 {
                     const Surface nsu = load_surface(gb_prev, idx, k.prev_camera_pos);
                     const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
-                    const float c_at_n = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, vis);
+                    float c_at_n = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, false);
+                    const int32_t ray = slots[j < 0 ? 1 : 2 + j];
+                    if (vis && c_at_n > 0.0f && ray >= 0 && traced.occluded[ray]) c_at_n = 0.0f;
                     const float nume_mc = init.p_hat / div * cM;
                     const float denom_mc = c_at_n * nsum + init.p_hat / div * cM;
                     const float conf = k.confidence_weights ? (nsum == 0.0f ? 0.0f : rM / nsum) : 1.0f;
@@ -950,8 +1024,12 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
             }
         }
         end_with_normalization(o, 1.0f, 1.0f);
-        if (k.visibility_reuse && vis) visibility_kill(s, o, su);
         if (k.m_cap > 0) o.M = min(o.M, k.m_cap);
+        // visibility reuse of the result (visibility_kill) through the any-hit queue
+        const bool test = k.visibility_reuse && vis && !(o.ucw <= 0.0f && o.w_sum <= 0.0f) &&
+                          !(o.flags & kRestirFlagUnoccluded);
+        const int slot = append_sample_ray(visq, test, su.P, o.point, su.prim, pixel);
+        st.meta[pixel] = make_int4(0, 0, kInitialVisibility, test ? slot : -1);
         store_reservoir(out, pixel, o);
     }
 }
@@ -1040,11 +1118,27 @@ cudaError_t launch_restir_temporal(const SceneView& s, const RenderConst& rc, co
 
 cudaError_t launch_restir_spatiotemporal(const SceneView& s, const RenderConst& rc, const RestirConst& k,
                                          const GBuffer& gb, const GBuffer& gb_prev, const ReservoirBuf& initial,
-                                         const ReservoirBuf& prev, const ReservoirBuf& out, int n_sm, cudaStream_t st)
+                                         const ReservoirBuf& prev, const ReservoirBuf& out, int32_t* ray_of,
+                                         const Queue& rays, const InitialState& st, const Queue& vis, int n_sm,
+                                         cudaStream_t stream)
 {
     const int64_t n = (int64_t)rc.width * rc.height;
-    spatiotemporal_kernel<<<grid_for(n, 128, n_sm * 16), 128, 0, st>>>(s, rc, k, gb, gb_prev, initial, prev, out);
-    return cudaGetLastError();
+    const int grid = grid_for(n, 128, n_sm * 16);
+    cudaError_t e = cudaMemsetAsync(rays.count, 0, sizeof(int32_t), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(vis.count, 0, sizeof(int32_t), stream);
+    if (e != cudaSuccess) return e;
+    if (k.bias_correction_visibility && k.has_prev)
+    {
+        spatiotemporal_rays_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, gb_prev, initial, prev, ray_of, rays);
+        e = launch_trace_queue(s, rays, true, n * (k.spatial_neighbors + 2), n_sm, stream);
+    }
+    if (e == cudaSuccess)
+        spatiotemporal_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, gb_prev, initial, prev, out, ray_of, rays, st, vis);
+    if (e == cudaSuccess) e = launch_trace_queue(s, vis, true, n, n_sm, stream);
+    if (e == cudaSuccess) visibility_apply_kernel<<<grid_for(n, 256, n_sm * 8), 256, 0, stream>>>(rc, out, st, vis);
+    if (e == cudaSuccess) e = cudaMemsetAsync(vis.count, 0, sizeof(int32_t), stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, const RestirConst& k, const GBuffer& gb,
