@@ -644,10 +644,28 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
     return color;
 }
 
+#ifdef __CUDACC__
+// The same evaluation as one out-of-line function per translation unit. Kernels that evaluate the
+// BSDF from several call sites (shading: the light sample, RIS candidates, BSDF-sampled light
+// hits; ReSTIR reuse: the target functions) share one copy of its code instead of one inlined
+// copy per site, which their instruction caches could not hold (ncu: "no instruction" was the
+// shade kernel's top stall). Measured on the 1080p many-light ReSTIR frame: spatial reuse 5.23 ->
+// 3.66 ms, temporal 4.17 -> 3.51, shading 11.9 -> 10.4. The initial candidates' light loop keeps
+// the inlined eval (13.3 ms outlined against 10.4 inlined).
+static __device__ __noinline__ V3 eval_outlined(const Material& m, const Medium& md, bool height_correlated,
+                                                const Query& q, int lobe, float& pdf)
+{
+    return eval(m, md, height_correlated, q, lobe, pdf);
+}
+#define GBPT_BSDF_EVAL_CALL eval_outlined
+#else
+#define GBPT_BSDF_EVAL_CALL eval
+#endif
+
 // Samples a light direction (returned in world space, 'lobe' = where it came from), then
 // evaluates f and pdf for it. A reflection lobe that sampled below the geometric surface
 // returns f = 0, pdf = 0.
-template <typename Rng>
+template <typename Rng, bool INLINE_EVAL = false>
 GBPT_HD V3 sample(const Material& m, const Medium& md, bool height_correlated, V3 view, V3 ns, V3 ng, Rng& rng, V3& dir,
                   int& lobe, float& pdf)
 {
@@ -711,7 +729,12 @@ GBPT_HD V3 sample(const Material& m, const Medium& md, bool height_correlated, V
     q.ns = ns;
     q.ng = ng;
     q.light = dir;
-    return eval(m, md, height_correlated, q, lobe, pdf);
+    // sampling's evaluation through the out-of-line copy on the device (one copy of the code per
+    // translation unit) unless the caller asks for the inlined one
+    if constexpr (INLINE_EVAL)
+        return eval(m, md, height_correlated, q, lobe, pdf);
+    else
+        return GBPT_BSDF_EVAL_CALL(m, md, height_correlated, q, lobe, pdf);
 }
 
 }  // namespace bsdf

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0,
                         q.ns = ns;
                         q.ng = ng;
                         q.light = wi;
-                        return bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, pdf);
+                        return bsdf::eval_outlined(m, md, hc, q, GBPT_LOBE_NONE, pdf);
                     },
                     [&](V3& wi, float& pdf) {
                         bsdf::Xorshift32 xr = bsdf_rng(rng);
@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                         q.ng = ng;
                         q.light = wi;
                         float bsdf_pdf;
-                        const V3 f = bsdf::eval(m, md, hc, q, R.flags & kRestirLobeMask, bsdf_pdf);
+                        const V3 f = bsdf::eval_outlined(m, md, hc, q, R.flags & kRestirLobeMask, bsdf_pdf);
                         float cosine = dot(ns, wi);
                         if (R.flags & GBPT_LOBE_GLASS_REFRACT) cosine = fabsf(cosine);
                         if (cosine > 0.0f)
@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                             q.ns = ns;
                             q.ng = ng;
                             q.light = wi;
-                            return bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, pdf);
+                            return bsdf::eval_outlined(m, md, hc, q, GBPT_LOBE_NONE, pdf);
                         });
                         if (pk.kept)
                         {
@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                             q.ng = ng;
                             q.light = wi;
                             float bsdf_pdf;
-                            const V3 f = bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
+                            const V3 f = bsdf::eval_outlined(m, md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
                             if (bsdf_pdf > 0.0f)
                             {
                                 const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
@@ -671,7 +671,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                             q.ng = ng;
                             q.light = wi;
                             // directions below the geometric surface carry no BSDF value, as in BSDF sampling
-                            f = dot(wi, ng) < 0.0f ? v3(0.0f) : bsdf::eval(m, md, hc, q, GBPT_LOBE_NONE, p_bsdf);
+                            f = dot(wi, ng) < 0.0f ? v3(0.0f) : bsdf::eval_outlined(m, md, hc, q, GBPT_LOBE_NONE, p_bsdf);
                             if (dot(wi, ng) < 0.0f) p_bsdf = 0.0f;
                         }
                         else

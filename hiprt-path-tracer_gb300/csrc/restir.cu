@@ -144,7 +144,7 @@ __device__ float target_function(const SceneView& s, bool hc, const Surface& su,
     q.ng = su.ng;
     q.light = dir;
     float pdf;
-    const V3 f = bsdf::eval(m, medium_of(su, m), hc, q, flags & kRestirLobeMask, pdf);
+    const V3 f = bsdf::eval_outlined(m, medium_of(su, m), hc, q, flags & kRestirLobeMask, pdf);
     const float G = fmaxf(0.0f, dot(triangle_unit_normal(s, tri), -dir)) / (dist * dist);
     const float p = luminance(f * emission_of(s, tri) * cosine * G);
     if (p == 0.0f) return 0.0f;
@@ -293,7 +293,8 @@ __device__ __forceinline__ void initial_bsdf_draw(const InitialPixel& px, bool h
     V3 dir;
     int lobe;
     float pdf;
-    bsdf::sample(px.m, px.md, hc, px.su.view, px.su.ns, px.su.ng, xr, dir, lobe, pdf);
+    // the inlined evaluation: this kernel's light loop inlines it already
+    bsdf::sample<bsdf::Xorshift32, true>(px.m, px.md, hc, px.su.view, px.su.ns, px.su.ng, xr, dir, lobe, pdf);
     const bool want = pdf > 0.0f;
     const int slot = warp_append(rays.count, want);
     if (want)
