@@ -205,7 +205,7 @@ def _relmse(img, ref):
 RENDER_WORKLOADS = ("cornell", "envmap", "restir", "guided", "guided_indirect_cornell", "batch")
 
 
-def render_workloads(log, guided_res=(480, 270), cpu_baseline=True, only=RENDER_WORKLOADS):
+def render_workloads(log, guided_res=(480, 270), cpu_baseline=True, only=RENDER_WORKLOADS, restir_res=(1920, 1080)):
     """Path-tracing workloads (one GPU, inputs resident; timed with CUDA events on the current stream):
 
     cornell     the Cornell box, 256 x 256, 64 launches x 1 spp, 4 bounces, RR from bounce 3, uniform
@@ -253,7 +253,7 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True, only=RENDER_
         out["envmap"] = envmap_workload(timed, cscene)
     del cscene
     if "restir" in only or "guided" in only:
-        many_light_workloads(out, log, timed, guided_res, only)
+        many_light_workloads(out, log, timed, guided_res, only, restir_res)
     # ---- guided against plain on the indirectly lit Cornell box ----
     if "guided_indirect_cornell" in only:
         out["guided_indirect_cornell"] = guided_indirect_cornell(timed)
@@ -298,7 +298,8 @@ def cornell_workload(out, cb, cscene, timed, cpu_baseline):
                                           "kind": "port", "sample": f"256x256 x {spp} spp, {dt:.2f}s"}
 
 
-def many_light_workloads(out, log, timed, guided_res, only):
+def many_light_workloads(out, log, timed, guided_res, only, restir_res=(1920, 1080)):
+    RW, RH = restir_res
     import numpy as np
     import torch
     import gbpt
@@ -318,14 +319,14 @@ def many_light_workloads(out, log, timed, guided_res, only):
                               bsdf=BSDF_PRINCIPLED, seed=seed, inverse_view=iv, inverse_projection=ip)
 
     def restir_frames(**extra):
-        r = gbpt.Renderer(scene, settings(1920, 1080, 1, 3, 1))
+        r = gbpt.Renderer(scene, settings(RW, RH, 1, 3, 1))
         r.set_restir_di(restir_di_settings(light_candidates=32, bsdf_candidates=1, m_cap=20, spatial_passes=1,
                                            spatial_neighbors=5, spatial_radius=30, **extra))
         r.render(3)
         r.reset()
         frame_ms = []
         for f in range(8):
-            iv, ip = look_at_camera(_orbit(S.eye, S.target, 0.5 * f), S.target, vfov_deg=S.vfov_deg, aspect=1920 / 1080)
+            iv, ip = look_at_camera(_orbit(S.eye, S.target, 0.5 * f), S.target, vfov_deg=S.vfov_deg, aspect=RW / RH)
             r.set_camera(iv, ip)
             frame_ms.append(timed(lambda: r.render(1)))
         st = r.stats()
@@ -333,20 +334,20 @@ def many_light_workloads(out, log, timed, guided_res, only):
         return frame_ms, st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
 
     if "restir" in only:
-        restir_workload(out, restir_frames)
+        restir_workload(out, restir_frames, RW, RH)
     if "guided" in only:
         guided_workload(out, scene, S, settings, timed, guided_res, log)
     del scene
 
 
-def restir_workload(out, restir_frames):
+def restir_workload(out, restir_frames, RW=1920, RH=1080):
     frame_ms, rays = restir_frames()
     tot = sum(frame_ms)
     fused_ms, _ = restir_frames(do_fused_spatiotemporal=1)
     fused_ps_ms, _ = restir_frames(do_fused_spatiotemporal=1, do_light_presampling=1)
-    out["restir"] = {"config": "many-light scene 16.8M + 10k emissive tris, 1920x1080, 8 frames orbiting 0.5 deg, 3 bounces, "
+    out["restir"] = {"config": f"many-light scene 16.8M + 10k emissive tris, {RW}x{RH}, 8 frames orbiting 0.5 deg, 3 bounces, "
                                "ReSTIR DI 32+1 candidates, visibility reuse, M-cap 20, 1 spatial pass 5 neighbours 30 px",
-                     "ms_per_frame": tot / 8, "frame_ms": frame_ms, "samples_per_s": 1920 * 1080 * 8 / (tot * 1e-3),
+                     "ms_per_frame": tot / 8, "frame_ms": frame_ms, "samples_per_s": RW * RH * 8 / (tot * 1e-3), "resolution": [RW, RH],
                      "mrays_per_s_traced": rays / (tot * 1e-3) / 1e6,
                      "fused_spatiotemporal_ms_per_frame": sum(fused_ms) / 8,
                      "fused_and_light_presampling_ms_per_frame": sum(fused_ps_ms) / 8,
@@ -638,6 +639,8 @@ def main():
     ap.add_argument("--ref-fraction", type=float, default=1.0 / 256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the path-tracing workloads")
+    ap.add_argument("--restir-res", default="1920x1080",
+                    help="WxH of the ReSTIR workload (a smaller one for ncu captures of its kernels)")
     ap.add_argument("--workloads", default=",".join(RENDER_WORKLOADS),
                     help="comma-separated path-tracing workloads to run (default: all)")
     ap.add_argument("--configs", default=None,
@@ -841,7 +844,8 @@ def main():
         unknown = [w for w in only if w not in RENDER_WORKLOADS]
         if unknown:
             raise SystemExit(f"unknown workloads {unknown}; choose from {RENDER_WORKLOADS}")
-        line["render"] = render_workloads(log, cpu_baseline=not args.no_cpu_baseline, only=only)
+        rw, rh = (int(v) for v in args.restir_res.split("x"))
+        line["render"] = render_workloads(log, cpu_baseline=not args.no_cpu_baseline, only=only, restir_res=(rw, rh))
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
