@@ -29,13 +29,19 @@ namespace {
 __device__ __forceinline__ void camera_ray(const RenderConst& rc, int pixel, int sample, V3& origin, V3& dir, Pcg32& rng)
 {
     const int x = pixel % rc.width, y = pixel / rc.width;
-    rng = pcg_seed((uint32_t)pixel, (uint32_t)sample, rc.seed);
+    const bool ref_rng = rc.rng_mode == GBPT_RNG_REFERENCE;
+    rng = ref_rng ? reference_seed((uint32_t)pixel, (uint32_t)sample, rc.random_number)
+                  : pcg_seed((uint32_t)pixel, (uint32_t)sample, rc.seed);
+    const uint64_t seed0 = rng.state;
     float px = x + 0.5f, py = y + 0.5f;
     if (rc.do_jittering)
     {
         px += rng.next() - 0.5f;
         py += rng.next() - 0.5f;
     }
+    // the reference's MegaKernel seeds its generator as CameraRays did: its first draws at the
+    // camera hit repeat the jitter's (Megakernel.h:52-57)
+    if (ref_rng) rng.state = seed0;
     const float xn = px / rc.width * 2.0f - 1.0f;
     const float yn = py / rc.height * 2.0f - 1.0f;
     origin = mat_x_point(rc.inverse_view, v3(0.0f, 0.0f, 0.0f));
@@ -159,9 +165,7 @@ __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0,
         V3 P = v3(0.0f);
         if (valid && prim >= 0 && env_sampled(s.env))
         {
-            Pcg32 rng;
-            rng.inc = pcg_inc(rc.seed);
-            rng.state = pb.rng[slot];
+            Pcg32 rng = load_rng(rc, pb.rng[slot]);
             const V3 d = xyz(in.dir_tmax[i]);
             P = xyz(in.origin_tmin[i]) + hit.x * d;
             V3 a, b, c;
@@ -208,7 +212,9 @@ __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0,
                     [&](V3& wi, float& pdf) {
                         bsdf::Xorshift32 xr = bsdf_rng(rng);
                         int lobe;
-                        return bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                        const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                        bsdf_rng_done(rng, xr);
+                        return f;
                     });
             }
             store_rng(pb.rng + slot, rng);
@@ -299,9 +305,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
         float4 bsdf_pending = make_float4(0, 0, 0, 0);
         float guide_pdf_out = 0.0f;  // MIS pdf of this vertex's continuation when it is guided
         int next_medium = -1;
-        Pcg32 rng;
-        rng.inc = pcg_inc(rc.seed);
-        rng.state = 0;
+        Pcg32 rng = load_rng(rc, 0);
         if (alive)
         {
             rng.state = pb.rng[slot];
@@ -313,8 +317,9 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             const V3 ng_raw = normalize(cross(b - a, c - a));
             V3 ng = ng_raw;
             V3 ns = shading_normal(s, prim, hit.y, hit.z, ng_raw);
-            const V3 view = -d;
+            V3 view = -d;
             fix_backfacing(view, ng, ns);
+            if (rc.rng_mode == GBPT_RNG_REFERENCE && bounce == 0) reference_gbuffer_vertex(rc.inverse_view, P, ng, ns, view);
             const int mat = __ldg(s.material_of + prim);
             tp = xyz(pb.throughput[slot]);
             V3 L = v3(0, 0, 0);
@@ -491,7 +496,10 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             }
             else
             {
-                const bsdf::Material m = bsdf::load_material(s.pmats[mat]);
+                // under GBPT_RNG_REFERENCE the camera hit shades with the material as the
+                // reference's G-buffer re-packed it (CameraRays.h:183, Megakernel.h:72)
+                const bsdf::Material m = bsdf::load_material(
+                    (rc.rng_mode == GBPT_RNG_REFERENCE && bounce == 0 && s.pmats_camera) ? s.pmats_camera[mat] : s.pmats[mat]);
                 const bool hc = rc.ggx_height_correlated != 0;
                 // volume state: inside a transmissive (non thin-walled) object when its back face is
                 // hit; the incident medium is then the object, else the volume the path is in
@@ -583,6 +591,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                             int lobe;
                             float pdf;
                             const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                            bsdf_rng_done(rng, xr);
                             if (pdf > 0.0f)
                             {
                                 want_bsdf = true;
@@ -641,6 +650,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                         int lobe;
                         float pdf;
                         const V3 f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                        bsdf_rng_done(rng, xr);
                         if (pdf > 0.0f && s.n_emissive > 0)
                         {
                             const V3 w = tp * (f * fabsf(dot(ns, wi)) / pdf);
@@ -678,6 +688,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                         {
                             bsdf::Xorshift32 xr = bsdf_rng(rng);
                             f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, p_bsdf);
+                            bsdf_rng_done(rng, xr);
                         }
                         pdf = is_black(f) ? 0.0f : alpha * guide::mixture_pdf_at(GL, wi) + (1.0f - alpha) * p_bsdf;
                         rec_pb = p_bsdf;
@@ -689,6 +700,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                     {
                         bsdf::Xorshift32 xr = bsdf_rng(rng);
                         f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
+                        bsdf_rng_done(rng, xr);
                     }
                     if (pdf > 0.0f)
                     {
@@ -881,9 +893,7 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst 
                 if (N > 0)
                 {
                     wsum += w_b;
-                    Pcg32 prng;
-                    prng.inc = pcg_inc(rc.seed);
-                    prng.state = pb.rng[slot];
+                    Pcg32 prng = load_rng(rc, pb.rng[slot]);
                     take_bsdf = prng.next() < w_b / wsum;
                     store_rng(pb.rng + slot, prng);
                 }
@@ -1239,7 +1249,8 @@ __global__ void normalize_f64_kernel(const float* __restrict__ power, int n, con
 
 // Vose's alias method with the reference's queue discipline (src/Utils/Utils.cpp:63-131):
 // smalls/larges are FIFO queues filled in index order; a large that falls to <= 1 moves to the
-// smalls. Runs on one thread (O(n)); the queues are ring buffers of n entries each.
+// smalls; an entry never paired keeps probability 1 and alias 0 (the reference's value-initialised
+// alias vector). Runs on one thread (O(n)); the queues are ring buffers of n entries each.
 __global__ void alias_vose_kernel(double* __restrict__ q, int n, float* __restrict__ prob, int32_t* __restrict__ alias,
                                   int32_t* __restrict__ smalls, int32_t* __restrict__ larges)
 {
@@ -1247,7 +1258,7 @@ __global__ void alias_vose_kernel(double* __restrict__ q, int n, float* __restri
     int s_head = 0, s_tail = 0, l_head = 0, l_tail = 0;  // tail - head = size; indices mod n
     for (int i = 0; i < n; i++)
     {
-        alias[i] = i;
+        alias[i] = 0;
         if (q[i] < 1.0)
             smalls[(s_tail++) % n] = i;
         else

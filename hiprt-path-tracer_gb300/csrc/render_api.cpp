@@ -79,6 +79,8 @@ struct gbpt_renderer
 {
     const gbpt_scene* scene = nullptr;
     gbpt::RenderConst rc;
+    // GBPT_RNG_REFERENCE: the host generator of the per-launch random numbers (CPURenderer::m_rng)
+    uint32_t rng_seed = 42u, host_rng = 42u;
     DevMem mem;
     gbpt::PathBuffers pb;
     gbpt::Queue q[2], shadow, bsdfq;
@@ -219,9 +221,78 @@ gbpt_principled_material effective_material(gbpt_principled_material m)
     return m;
 }
 
+// The reference's 8-bit material fields (DevicePackedEffectiveMaterial,
+// src/HostDeviceCommon/Material/MaterialPacked.h:16-520, with the accessors of
+// src/HostDeviceCommon/Packing.h:16-200): a value in [0, 1] is stored as the byte (unsigned
+// char)(x * 255) and read back as byte * (1 / 255); the green channel of a packed colour is read
+// as (byte << 8) * (1 / 65280). Values outside [0, 1] are clamped to the byte range first.
+uint32_t byte_of(float x)
+{
+    const float v = x * 255.0f;
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 255.0f) return 255u;
+    return (uint32_t)v;
+}
+float unpack_byte(float x) { return (float)byte_of(x) * (1.0f / 255.0f); }
+void unpack_color(float* c)
+{
+    const uint32_t r = byte_of(c[0]), g = byte_of(c[1]), b = byte_of(c[2]);
+    c[0] = (float)r * (1.0f / 255.0f);
+    c[1] = (float)(g << 8) * (1.0f / 65280.0f);
+    c[2] = (float)b * (1.0f / 255.0f);
+}
+
+// A material as the reference's kernels read it back from its packed record
+// (CPUMaterial::pack_to_GPU then DevicePackedEffectiveMaterial::unpack)
+gbpt_principled_material packed_material(gbpt_principled_material m)
+{
+    unpack_color(m.base_color);
+    m.roughness = unpack_byte(m.roughness);
+    m.metallic = unpack_byte(m.metallic);
+    unpack_color(m.metallic_F82);
+    unpack_color(m.metallic_F90);
+    m.diffuse_transmission = unpack_byte(m.diffuse_transmission);
+    m.anisotropy = unpack_byte(m.anisotropy);
+    m.anisotropy_rotation = unpack_byte(m.anisotropy_rotation);
+    m.second_roughness_weight = unpack_byte(m.second_roughness_weight);
+    m.second_roughness = unpack_byte(m.second_roughness);
+    unpack_color(m.specular_color);
+    m.specular_tint = unpack_byte(m.specular_tint);
+    m.specular = unpack_byte(m.specular);
+    m.specular_darkening = unpack_byte(m.specular_darkening);
+    m.coat_roughness = unpack_byte(m.coat_roughness);
+    m.coat = unpack_byte(m.coat);
+    unpack_color(m.coat_medium_absorption);
+    m.coat_roughening = unpack_byte(m.coat_roughening);
+    m.coat_darkening = unpack_byte(m.coat_darkening);
+    m.coat_anisotropy = unpack_byte(m.coat_anisotropy);
+    m.coat_anisotropy_rotation = unpack_byte(m.coat_anisotropy_rotation);
+    m.sheen = unpack_byte(m.sheen);
+    unpack_color(m.absorption_color);
+    m.specular_transmission = unpack_byte(m.specular_transmission);
+    return m;
+}
+
+uint32_t xorshift32_step(uint32_t& state)
+{
+    uint32_t x = state;
+    x ^= x << 13;
+    x ^= x >> 17;
+    x ^= x << 5;
+    state = x;
+    return x;
+}
+
 }  // namespace
 
 extern "C" {
+
+gbpt_status gbpt_material_pack_8bit(const gbpt_principled_material* in, int32_t n, gbpt_principled_material* out)
+{
+    if (n < 0 || (n > 0 && (!in || !out))) return set_error(GBPT_ERROR_INVALID_ARG, "NULL material array or negative count");
+    for (int32_t m = 0; m < n; m++) out[m] = packed_material(in[m]);
+    return GBPT_OK;
+}
 
 gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* bvh_params, gbpt_scene** out,
                               void* stream)
@@ -235,6 +306,9 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
         return set_error(GBPT_ERROR_INVALID_ARG, "geometry buffers are NULL");
     if (d->n_materials > 0 && !d->materials && !d->principled_materials)
         return set_error(GBPT_ERROR_INVALID_ARG, "materials and principled_materials are both NULL");
+    if (d->material_packing != GBPT_MATERIALS_FLOAT && d->material_packing != GBPT_MATERIALS_PACKED)
+        return set_error(GBPT_ERROR_INVALID_ARG, "unknown material_packing");
+    const bool packed = d->material_packing == GBPT_MATERIALS_PACKED;
     // the emission/base colour view used by light sampling: the plain materials, else the
     // principled ones
     std::vector<gbpt_material> plain;
@@ -299,7 +373,9 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     for (int32_t m = 0; m < d->n_materials; m++)
     {
         const gbpt_material& src = materials[m];
-        mats[m].base_color = make_float4(src.base_color[0], src.base_color[1], src.base_color[2], 0.0f);
+        float base[3] = {src.base_color[0], src.base_color[1], src.base_color[2]};
+        if (packed) unpack_color(base);
+        mats[m].base_color = make_float4(base[0], base[1], base[2], 0.0f);
         mats[m].emission = make_float4(src.emission[0], src.emission[1], src.emission[2], 0.0f);
     }
     std::vector<int32_t> emissive;
@@ -324,15 +400,28 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     int32_t* dlarge = M.alloc<int32_t>(ne);
     float4* dn = normals.empty() ? nullptr : M.alloc<float4>(normals.size());
     gbpt_principled_material* dpm = nullptr;
-    std::vector<gbpt_principled_material> pmats;
+    gbpt_principled_material* dpm_camera = nullptr;
+    std::vector<gbpt_principled_material> pmats, pmats_camera;
     if (d->principled_materials)
     {
-        for (int32_t m = 0; m < d->n_materials; m++) pmats.push_back(effective_material(d->principled_materials[m]));
+        // packed: quantised, then coat-roughened as the reference's material fetch does on the
+        // unpacked record (Material.h:122-146); the camera-hit table packs that result again, as
+        // the reference's G-buffer stores it (CameraRays.h:183)
+        for (int32_t m = 0; m < d->n_materials; m++)
+        {
+            const gbpt_principled_material& raw = d->principled_materials[m];
+            pmats.push_back(effective_material(packed ? packed_material(raw) : raw));
+            if (packed) pmats_camera.push_back(packed_material(pmats.back()));
+        }
         dpm = M.alloc<gbpt_principled_material>(pmats.size());
+        if (packed) dpm_camera = M.alloc<gbpt_principled_material>(pmats_camera.size());
     }
     cudaError_t e = M.err;
     if (e == cudaSuccess && dpm)
         e = cudaMemcpyAsync(dpm, pmats.data(), pmats.size() * sizeof(gbpt_principled_material), cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess && dpm_camera)
+        e = cudaMemcpyAsync(dpm_camera, pmats_camera.data(), pmats_camera.size() * sizeof(gbpt_principled_material),
+                            cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dv, verts.data(), verts.size() * sizeof(float4), cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess && dn)
         e = cudaMemcpyAsync(dn, normals.data(), normals.size() * sizeof(float4), cudaMemcpyHostToDevice, cs);
@@ -358,6 +447,7 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
     v.bvh_nodes = static_cast<const uint4*>(s->bvh->dev.nodes);
     v.bvh_tris = static_cast<const float4*>(s->bvh->dev.tris);
     v.pmats = dpm;
+    v.pmats_camera = dpm_camera;
     v.normals = dn;
     s->principled = dpm != nullptr;
     s->n_emissive = ne;
@@ -419,19 +509,19 @@ bool scene_env_sampled(const gbpt_scene* s)
 bool finite_nonneg(float x) { return std::isfinite(x) && x >= 0.0f; }
 
 // Vose's alias method over q (texel luminances scaled to mean 1) with FIFO small/large queues
-// filled in index order: the partition of Utils::compute_alias_table (src/Utils/Utils.cpp:63-131).
+// filled in index order: the partition of Utils::compute_alias_table (src/Utils/Utils.cpp:63-131);
+// an entry never paired keeps probability 1 and alias 0, as in the reference's zero-filled vector.
 // Runs on the host: it is one sequential O(n) pass, and on one GPU thread each of its steps would
 // wait on a dependent memory access. Output: (probability as float bits, alias index) per texel.
 void vose_host(std::vector<double>& q, std::vector<uint2>& out)
 {
     const size_t n = q.size();
     std::vector<float> prob(n, 0.0f);
-    std::vector<int32_t> alias(n), smalls, larges;
+    std::vector<int32_t> alias(n, 0), smalls, larges;
     smalls.reserve(n);
     larges.reserve(n);
     for (size_t i = 0; i < n; i++)
     {
-        alias[i] = (int32_t)i;
         (q[i] < 1.0 ? smalls : larges).push_back((int32_t)i);
     }
     size_t sh = 0, lh = 0;
@@ -619,6 +709,8 @@ gbpt_status check_settings(const gbpt_scene* scene, const gbpt_render_settings* 
         return set_error(GBPT_ERROR_INVALID_ARG, "GBPT_BSDF_PRINCIPLED needs a scene created with principled_materials");
     if (st->direct_lighting != GBPT_DIRECT_MIS && st->direct_lighting != GBPT_DIRECT_RIS)
         return set_error(GBPT_ERROR_INVALID_ARG, "unknown direct_lighting");
+    if (st->rng_mode != GBPT_RNG_PCG && st->rng_mode != GBPT_RNG_REFERENCE)
+        return set_error(GBPT_ERROR_INVALID_ARG, "unknown rng_mode");
     if (st->direct_lighting == GBPT_DIRECT_RIS &&
         (st->ris_light_candidates < 0 || st->ris_light_candidates > 64 || st->ris_bsdf_candidates < 0 ||
          st->ris_bsdf_candidates > 1 || st->ris_light_candidates + st->ris_bsdf_candidates == 0))
@@ -645,6 +737,7 @@ gbpt::RenderConst render_const(const gbpt_render_settings* st, int32_t spp)
     rc.direct_ris = st->direct_lighting == GBPT_DIRECT_RIS ? 1 : 0;
     rc.ris_light = st->ris_light_candidates;
     rc.ris_bsdf = st->ris_bsdf_candidates;
+    rc.rng_mode = st->rng_mode;
     std::memcpy(rc.inverse_view, st->inverse_view, sizeof(rc.inverse_view));
     std::memcpy(rc.inverse_projection, st->inverse_projection, sizeof(rc.inverse_projection));
     return rc;
@@ -720,6 +813,7 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
     r->capacity = cap;
     r->n_sm = sm_count();
     r->rc = render_const(st, st->samples_per_launch);
+    r->rng_seed = r->host_rng = st->random_number != 0u ? st->random_number : 42u;
 
     DevMem& M = r->mem;
     alloc_paths(M, cap, st->bsdf == GBPT_BSDF_PRINCIPLED, false, r->pb, r->q, r->shadow, r->bsdfq);
@@ -762,6 +856,7 @@ gbpt_status gbpt_renderer_reset(gbpt_renderer* r, void* stream)
     if (e == cudaSuccess) e = cudaMemsetAsync(r->stats, 0, 4 * sizeof(unsigned long long), cs);
     r->iteration = 0;
     r->samples = 0;
+    r->host_rng = r->rng_seed;
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "reset");
 }
 
@@ -777,6 +872,8 @@ gbpt_status gbpt_pass_camera_rays(gbpt_renderer* r, void* stream)
 {
     if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
     r->cur = 0;
+    // the reference's camera pass draws the frame's random number first (CPURenderer.cpp:698-705)
+    if (r->rc.rng_mode == GBPT_RNG_REFERENCE) r->rc.random_number = xorshift32_step(r->host_rng);
     cudaError_t e = gbpt::launch_camera(r->rc, r->pb, r->q[0], (int32_t)r->iteration, r->stats, r->n_sm,
                                         (cudaStream_t)stream);
     if (e == cudaSuccess && r->gv.rec_count) e = cudaMemsetAsync(r->gv.rec_count, 0, sizeof(int32_t), (cudaStream_t)stream);
@@ -1126,6 +1223,8 @@ gbpt_status gbpt_pass_accumulate(gbpt_renderer* r, void* stream)
     }
     r->iteration += r->rc.spp;
     r->samples += r->rc.spp;
+    // ... and post_sample_update draws one more (CPURenderer.cpp:586-598)
+    if (r->rc.rng_mode == GBPT_RNG_REFERENCE) xorshift32_step(r->host_rng);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "accumulate");
 }
 
@@ -1455,6 +1554,8 @@ gbpt_status gbpt_batch_create(const gbpt_batch_job* jobs, int32_t n_jobs, const 
         gbpt_status chk = check_settings(jobs[j].scene, st);
         if (chk == GBPT_OK && st->bsdf != jobs[0].settings.bsdf)
             chk = set_error(GBPT_ERROR_INVALID_ARG, "all jobs of a batch must use the same bsdf mode");
+        if (chk == GBPT_OK && st->rng_mode != GBPT_RNG_PCG)
+            chk = set_error(GBPT_ERROR_INVALID_ARG, "batched jobs draw PCG streams (rng_mode must be GBPT_RNG_PCG)");
         if (chk != GBPT_OK)
         {
             delete b;

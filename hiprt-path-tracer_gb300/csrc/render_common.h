@@ -64,6 +64,9 @@ struct SceneView
     const uint4* bvh_nodes;
     const float4* bvh_tris;
     const gbpt_principled_material* pmats;  // effective principled materials (NULL: Lambertian scene)
+    // packed materials (GBPT_MATERIALS_PACKED): the effective materials packed again, as the
+    // reference's G-buffer stores the camera hit's material (NULL otherwise)
+    const gbpt_principled_material* pmats_camera;
     EnvView env;
     const float4* normals;        // per vertex: smooth-shading normal, w = 1 when present (NULL: none)
 };
@@ -152,7 +155,12 @@ __device__ __forceinline__ V3 xyz(float4 f) { return v3(f.x, f.y, f.z); }
 __device__ __forceinline__ float4 f4(V3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
 
 // ---------------------------------------------------------------------------------------------
-// PCG32 (O'Neill 2014): one 64-bit state per path, stream selected by the render seed.
+// Random numbers of a path: one 64-bit state per path slot, two generators behind one interface.
+//  - inc != 0: PCG32 (O'Neill 2014), stream selected by the render seed (the default);
+//  - inc == 0: the reference's Xorshift32Generator (src/HostDeviceCommon/Xorshift.h:18-66) on the
+//    low 32 bits of 'state' (GBPT_RNG_REFERENCE): xorshift 13/17/5, floats x / 2^32 clamped to
+//    1 - 1e-7, random_index(n) = floor(x / 2^32 * n) clamped to n - 1. (float)x rounds to nearest
+//    as the reference's conversion does, and x * 2^-32 equals its division by float(0xffffffff).
 // ---------------------------------------------------------------------------------------------
 struct Pcg32
 {
@@ -161,6 +169,15 @@ struct Pcg32
 
     __device__ __forceinline__ uint32_t next_u32()
     {
+        if (inc == 0)
+        {
+            uint32_t x = (uint32_t)state;
+            x ^= x << 13;
+            x ^= x >> 17;
+            x ^= x << 5;
+            state = x;
+            return x;
+        }
         const uint64_t old = state;
         state = old * 6364136223846793005ULL + inc;
         const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
@@ -168,14 +185,45 @@ struct Pcg32
         return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
     }
     // uniform float in [0, 1)
-    __device__ __forceinline__ float next() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+    __device__ __forceinline__ float next()
+    {
+        if (inc == 0) return fminf((float)next_u32() * (1.0f / 4294967296.0f), 1.0f - 1.0e-7f);
+        return (float)(next_u32() >> 8) * (1.0f / 16777216.0f);
+    }
     __device__ __forceinline__ float operator()() { return next(); }
     __device__ __forceinline__ int index(int n)
     {
+        if (inc == 0)
+        {
+            const int i = (int)(__fmul_rn((float)next_u32() * (1.0f / 4294967296.0f), (float)n));
+            return i < n - 1 ? i : n - 1;
+        }
         int i = (int)(next() * (float)n);
         return i < n - 1 ? i : n - 1;
     }
 };
+
+// wang_hash (src/Device/includes/Hash.h:11-19)
+__device__ __forceinline__ uint32_t wang_hash(uint32_t s)
+{
+    s = (s ^ 61u) ^ (s >> 16);
+    s *= 9u;
+    s = s ^ (s >> 4);
+    s *= 0x27d4eb2du;
+    s = s ^ (s >> 15);
+    return s;
+}
+
+// The reference's generator of one pixel sample: Xorshift32 seeded by
+// wang_hash((pixel + 1) * (sample_number + 1) * random_number), 32-bit wrap-around products
+// (CameraRays.h:155-160, Megakernel.h:52-57).
+__device__ __forceinline__ Pcg32 reference_seed(uint32_t pixel, uint32_t sample_number, uint32_t random_number)
+{
+    Pcg32 r;
+    r.state = wang_hash((pixel + 1u) * (sample_number + 1u) * random_number);
+    r.inc = 0;
+    return r;
+}
 
 __device__ __forceinline__ uint64_t pcg_inc(uint32_t seed) { return ((uint64_t)seed << 1u) | 1u; }
 
@@ -210,6 +258,51 @@ __device__ __forceinline__ V3 mat_x_point(const float* m, V3 p)
     float inv_w = 1.0f;
     if (!(w < 1.0e-10f && w > -1.0e-10f)) inv_w = 1.0f / w;
     return v3(x * inv_w, y * inv_w, z * inv_w);
+}
+
+// Octahedral24BitNormalPadded32b pack then unpack (src/HostDeviceCommon/Packing.h:237-367; the
+// octahedral map of Cigolle et al. 2014): the reference's G-buffer stores its camera-hit normals
+// as two 12-bit snorms in three bytes. Every step is exact or a single rounding (no contraction
+// changes a result), so the round trip matches the reference's bit for bit up to the final
+// normalisation.
+__device__ __forceinline__ float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
+__device__ __forceinline__ V3 oct24_roundtrip(V3 n)
+{
+    const float l1 = __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(fabsf(n.x), fabsf(n.y)), fabsf(n.z)));
+    float ex = __fmul_rn(n.x, l1), ey = __fmul_rn(n.y, l1);
+    if (n.z < 0.0f)
+    {
+        const float ax = fabsf(ey), ay = fabsf(ex);
+        ex = (1.0f - ax) * sign_nz(ex);
+        ey = (1.0f - ay) * sign_nz(ey);
+    }
+    const float sx = roundf(__fmul_rn(fminf(fmaxf(ex + 1.0f, 0.0f), 2.0f), 2047.0f));
+    const float sy = roundf(__fmul_rn(fminf(fmaxf(ey + 1.0f, 0.0f), 2.0f), 2047.0f));
+    // the two 12-bit values round-trip through the three bytes unchanged (integer arithmetic)
+    const float px = sx, py = sy;
+    const float dx = fminf(fmaxf(__fdiv_rn(px, 2047.0f) - 1.0f, -1.0f), 1.0f);
+    const float dy = fminf(fmaxf(__fdiv_rn(py, 2047.0f) - 1.0f, -1.0f), 1.0f);
+    V3 v = v3(dx, dy, 1.0f - fabsf(dx) - fabsf(dy));
+    if (v.z < 0.0f)
+    {
+        const float tx = v.x, ty = v.y;
+        v.x = (1.0f - fabsf(ty)) * sign_nz(tx);
+        v.y = (1.0f - fabsf(tx)) * sign_nz(ty);
+    }
+    return normalize(v);
+}
+
+// GBPT_RNG_REFERENCE, camera hit: the vertex as the reference's MegaKernel rebuilds it from its
+// packed G-buffer (Megakernel.h:59-70): octahedral-24 normals written after the backface fix
+// (CameraRays.h:178-181) and renormalised on read, and the view direction from the camera
+// position (the translation column of the inverse view, Camera::to_hiprt) to the stored hit
+// point (GBufferDevice::get_view_direction), negated into a ray direction, normalised and negated.
+__device__ __forceinline__ void reference_gbuffer_vertex(const float* inverse_view, V3 P, V3& ng, V3& ns, V3& view)
+{
+    ng = normalize(oct24_roundtrip(ng));
+    ns = normalize(oct24_roundtrip(ns));
+    const V3 cam = v3(inverse_view[3], inverse_view[7], inverse_view[11]);
+    view = -normalize(-normalize(cam - P));
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -36,6 +36,16 @@ __device__ __forceinline__ void warp_count(unsigned long long* counter, bool c)
 
 __device__ __forceinline__ void store_rng(uint64_t* p, const Pcg32& r) { *p = r.state; }
 
+// A path's generator from its stored state: the PCG stream of the render seed, or under
+// GBPT_RNG_REFERENCE the reference's Xorshift32 (inc = 0).
+__device__ __forceinline__ Pcg32 load_rng(const RenderConst& rc, uint64_t state)
+{
+    Pcg32 r;
+    r.state = state;
+    r.inc = rc.rng_mode == GBPT_RNG_REFERENCE ? 0ULL : pcg_inc(rc.seed);
+    return r;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Lambertian BSDF (src/Device/includes/BSDFs/Lambertian.h:14-58)
 // ---------------------------------------------------------------------------------------------
@@ -195,12 +205,18 @@ __device__ __forceinline__ RisPick ris_light_candidates(const SceneView& s, cons
 }
 
 // A BSDF sample draws its random numbers from a Xorshift32 generator (the reference's generator,
-// src/HostDeviceCommon/Xorshift.h) seeded by the path's PCG stream, so the same numbers can be
-// replayed through the reference's own BSDF.
+// src/HostDeviceCommon/Xorshift.h): with PCG paths one seeded by the path's stream, so the same
+// numbers can be replayed through the reference's own BSDF; under GBPT_RNG_REFERENCE the path's own
+// generator, as the reference's BSDF samplers take it, continued by bsdf_rng_done afterwards.
 __device__ __forceinline__ bsdf::Xorshift32 bsdf_rng(Pcg32& rng)
 {
+    if (rng.inc == 0) return bsdf::Xorshift32{(uint32_t)rng.state};
     uint32_t seed = rng.next_u32();
     return bsdf::Xorshift32{seed != 0u ? seed : 0x9E3779B9u};
+}
+__device__ __forceinline__ void bsdf_rng_done(Pcg32& rng, const bsdf::Xorshift32& xr)
+{
+    if (rng.inc == 0) rng.state = xr.state;
 }
 
 // MaterialUtils::can_do_light_sampling (MaterialUtils.h:71-93): a material whose every lobe is a

@@ -29,6 +29,8 @@ struct RenderConst
     int32_t restir_final_visibility;  // ReSTIR DI final shading traces a shadow ray unless known unoccluded
     int32_t direct_ris;               // GBPT_DIRECT_RIS
     int32_t ris_light, ris_bsdf;      // RIS candidates
+    int32_t rng_mode;                 // GBPT_RNG_*
+    uint32_t random_number;           // GBPT_RNG_REFERENCE: this launch's HIPRTRenderData::random_number
     float inverse_view[16];
     float inverse_projection[16];
 };

@@ -56,6 +56,19 @@ def pack(**kw) -> np.ndarray:
     return rec
 
 
+def unpack(rec: np.ndarray) -> dict:
+    """The fields of one material record as a dict (the inverse of pack)."""
+    out = {}
+    for name, (off, cnt) in OFFSETS.items():
+        if name == "thin_walled":
+            out[name] = int(rec[off:off + 1].view(np.int32)[0])
+        elif cnt == 1:
+            out[name] = float(rec[off])
+        else:
+            out[name] = tuple(float(v) for v in rec[off:off + cnt])
+    return out
+
+
 def pack_many(dicts) -> np.ndarray:
     return np.stack([pack(**d) for d in dicts]) if dicts else np.zeros((0, WORDS), np.float32)
 

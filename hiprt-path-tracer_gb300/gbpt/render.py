@@ -23,6 +23,8 @@ LIGHT_POWER = 1
 BSDF_LAMBERTIAN = 1
 BSDF_PRINCIPLED = 3
 DIRECT_MIS, DIRECT_RIS = 0, 1
+RNG_PCG, RNG_REFERENCE = 0, 1
+MATERIALS_FLOAT, MATERIALS_PACKED = 0, 1
 GBPT_ALIAS_NOALLOC_MAX_EMITTERS = 131072  # include/gbpt_render.h
 
 
@@ -33,7 +35,7 @@ class Material(ctypes.Structure):
 class SceneDesc(ctypes.Structure):
     _fields_ = [("positions", c_vp), ("n_vertices", i64), ("indices", c_vp), ("n_triangles", i64),
                 ("material_indices", c_vp), ("materials", c_vp), ("n_materials", i32),
-                ("principled_materials", c_vp), ("vertex_normals", c_vp)]
+                ("principled_materials", c_vp), ("vertex_normals", c_vp), ("material_packing", i32)]
 
 
 class RenderSettingsC(ctypes.Structure):
@@ -42,8 +44,9 @@ class RenderSettingsC(ctypes.Structure):
                 ("russian_roulette_throughput_clamp", ctypes.c_float), ("light_sampling", i32), ("bsdf", i32),
                 ("seed", ctypes.c_uint32), ("do_jittering", i32), ("ggx_height_correlated", i32),
                 ("direct_lighting", i32), ("ris_light_candidates", i32), ("ris_bsdf_candidates", i32),
-                ("reserved_settings", i32),
-                ("inverse_view", ctypes.c_float * 16), ("inverse_projection", ctypes.c_float * 16)]
+                ("rng_mode", i32),
+                ("inverse_view", ctypes.c_float * 16), ("inverse_projection", ctypes.c_float * 16),
+                ("random_number", ctypes.c_uint32)]
 
 
 class RenderStatsC(ctypes.Structure):
@@ -82,6 +85,7 @@ class GltfCameraC(ctypes.Structure):
 
 
 RENDER_SIGNATURES = [
+    ("gbpt_material_pack_8bit", ctypes.c_int, [c_vp, i32, c_vp]),
     ("gbpt_gltf_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(c_vp)]),
     ("gbpt_gltf_scene_desc", ctypes.c_int, [c_vp, ctypes.POINTER(SceneDesc)]),
     ("gbpt_gltf_get_camera", ctypes.c_int, [c_vp, ctypes.POINTER(GltfCameraC)]),
@@ -211,14 +215,18 @@ class RenderSettings:
     direct_lighting: int = 0  # DIRECT_MIS
     ris_light_candidates: int = 4
     ris_bsdf_candidates: int = 1
+    rng_mode: int = RNG_PCG  # RNG_REFERENCE: the reference's generator and draw order (gbpt_render.h)
+    random_number: int = 0   # RNG_REFERENCE: seed of the per-launch random numbers (0: 42)
     inverse_view: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
     inverse_projection: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
 
     def to_c(self) -> RenderSettingsC:
         c = RenderSettingsC()
         for k in ("width", "height", "samples_per_launch", "nb_bounces", "russian_roulette_min_depth",
-                  "light_sampling", "bsdf", "seed", "direct_lighting", "ris_light_candidates", "ris_bsdf_candidates"):
+                  "light_sampling", "bsdf", "seed", "direct_lighting", "ris_light_candidates", "ris_bsdf_candidates",
+                  "rng_mode"):
             setattr(c, k, int(getattr(self, k)))
+        c.random_number = int(self.random_number) & 0xFFFFFFFF
         c.do_russian_roulette = 1 if self.do_russian_roulette else 0
         c.do_jittering = 1 if self.do_jittering else 0
         c.ggx_height_correlated = 1 if self.ggx_height_correlated else 0
@@ -237,6 +245,15 @@ def _load():
             fn.argtypes = args
         lib._render_sigs = True
     return lib
+
+
+def material_pack_8bit(materials: np.ndarray) -> np.ndarray:
+    """(M, 64) material records as the reference's packed records read them back
+    (gbpt_material_pack_8bit; host code, no device needed)."""
+    lib = _load()
+    m = np.ascontiguousarray(materials, np.float32).reshape(-1, 64).copy()
+    _lib.check(lib.gbpt_material_pack_8bit(m.ctypes.data, m.shape[0], m.ctypes.data))
+    return m
 
 
 class World:
@@ -279,10 +296,12 @@ class World:
 
 class Scene:
     def __init__(self, positions, indices, material_of_triangle, albedo=None, emission=None, stream=None, sah_bins=32,
-                 max_leaf_size=3, principled=None, vertex_normals=None):
+                 max_leaf_size=3, principled=None, vertex_normals=None, material_packing=MATERIALS_FLOAT):
         """albedo/emission: (M, 3) plain materials; principled: (M, 64) gbpt.materials records (the
         reference's CPUMaterial parameters; base colour and emission come from them when albedo is
-        None); vertex_normals: (V, 3) smooth-shading normals (a zero row: none at that vertex)."""
+        None); vertex_normals: (V, 3) smooth-shading normals (a zero row: none at that vertex);
+        material_packing: MATERIALS_PACKED stores the materials as the reference's 8-bit packed
+        records."""
         lib = _load()
         self._pm = None
         if principled is not None:
@@ -307,7 +326,7 @@ class Scene:
         desc = SceneDesc(self._pos.ctypes.data, self._pos.shape[0], self._idx.ctypes.data, self._idx.shape[0],
                          self._mat_of.ctypes.data, ctypes.addressof(self._mats), len(alb),
                          self._pm.ctypes.data if self._pm is not None else None,
-                         self._nrm.ctypes.data if self._nrm is not None else None)
+                         self._nrm.ctypes.data if self._nrm is not None else None, int(material_packing))
         params = _lib.BvhParams(sah_bins, max_leaf_size, 0)
         h = c_vp()
         _lib.check(lib.gbpt_scene_create(ctypes.byref(desc), ctypes.byref(params), ctypes.byref(h), _stream(stream)))

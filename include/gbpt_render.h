@@ -50,7 +50,26 @@ typedef struct gbpt_scene_desc {
      * normal is normalize(n_b u + n_c v + n_a (1 - u - v)) at the hit's barycentrics, then the
      * backface fix. Normal maps are not built. */
     const float* vertex_normals;
+    /* GBPT_MATERIALS_* [GBPT_MATERIALS_FLOAT]. GBPT_MATERIALS_PACKED stores every material as the
+     * reference does (DevicePackedEffectiveMaterial / DevicePackedTexturedMaterialSoA,
+     * src/HostDeviceCommon/Material/MaterialPacked.h:16-520): colours and the [0, 1] parameters
+     * truncated to 8 bits (base colour and roughness, metallic, F82, F90, diffuse transmission,
+     * anisotropy and its rotation, second roughness and its weight, specular, its colour, tint and
+     * darkening, coat, its roughness, roughening, darkening, anisotropy, rotation and medium
+     * absorption, sheen, specular transmission, absorption colour), every other field in float. */
+    int32_t material_packing;
 } gbpt_scene_desc;
+
+enum {
+    GBPT_MATERIALS_FLOAT = 0,  /* material parameters kept in float */
+    GBPT_MATERIALS_PACKED = 1  /* the reference's 8-bit packed material records */
+};
+
+/* The reference's packed material record read back, on the host: n materials through
+ * CPUMaterial::pack_to_GPU and DevicePackedEffectiveMaterial::unpack
+ * (src/HostDeviceCommon/Material/MaterialCPU.h:31-118, MaterialPacked.h:16-520) — what
+ * GBPT_MATERIALS_PACKED stores before the coat roughening. in and out may alias. */
+GBPT_API gbpt_status gbpt_material_pack_8bit(const gbpt_principled_material* in, int32_t n, gbpt_principled_material* out);
 
 /* Uploads the scene, builds its BVH (gbpt_bvh_build), the emissive-triangle list (triangles
  * whose material has non-black emission, in triangle order, as the reference's scene parser
@@ -195,6 +214,23 @@ enum {
  * Vertices guided by the learned proposal and the ReSTIR DI bounce keep their own estimators. */
 enum { GBPT_DIRECT_MIS = 0, GBPT_DIRECT_RIS = 1 };
 
+/* Random numbers of the paths (gbpt_render_settings.rng_mode):
+ *   GBPT_RNG_PCG: one PCG32 stream per pixel sample, keyed on (pixel, sample index, seed);
+ *   GBPT_RNG_REFERENCE: the reference's generator and draw order, for sample-by-sample comparison
+ *     with its own kernels: Xorshift32 (src/HostDeviceCommon/Xorshift.h:18-66) seeded by
+ *     wang_hash((pixel + 1) * (sample index + 1) * random_number) (src/Device/kernels/CameraRays.h:155-160),
+ *     the camera pass's jitter draws repeated by the first bounce (Megakernel.h:52-57), BSDF samples
+ *     drawing from the path's own generator, and the camera hit shaded from the packed G-buffer
+ *     (octahedral 24-bit normals, the view direction from the camera position, the material
+ *     re-packed after its coat roughening; CameraRays.h:178-201, Megakernel.h:59-72). Each launch
+ *     is one frame of the reference's CPU renderer: its random_number is the next output of a
+ *     host Xorshift32 generator seeded with gbpt_render_settings.random_number (42 when 0, the
+ *     reference's default), which the renderer advances once before each camera pass and once
+ *     after each launch (CPURenderer::camera_rays_pass / post_sample_update,
+ *     src/Renderer/CPURenderer.cpp:698-705 and 586-598). The environment map's direct lighting keeps its own
+ *     draw position (before the emissive light sample) in both modes. */
+enum { GBPT_RNG_PCG = 0, GBPT_RNG_REFERENCE = 1 };
+
 typedef struct gbpt_render_settings {
     int32_t width, height;
     int32_t samples_per_launch;      /* spp traced together in one wavefront (>= 1) */
@@ -210,9 +246,10 @@ typedef struct gbpt_render_settings {
     int32_t direct_lighting;         /* GBPT_DIRECT_* (DirectLightSamplingBaseStrategy) */
     int32_t ris_light_candidates;    /* RISSettings::number_of_light_candidates [4] */
     int32_t ris_bsdf_candidates;     /* RISSettings::number_of_bsdf_candidates, 0 or 1 [1] */
-    int32_t reserved_settings;
+    int32_t rng_mode;                /* GBPT_RNG_* [GBPT_RNG_PCG] */
     float inverse_view[16];          /* row-major, points multiplied on the right */
     float inverse_projection[16];
+    uint32_t random_number;          /* GBPT_RNG_REFERENCE: seed of the per-launch random numbers (0: 42) */
 } gbpt_render_settings;
 
 typedef struct gbpt_render_stats {

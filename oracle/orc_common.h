@@ -30,24 +30,69 @@ inline V nrm(V a) { return a / std::sqrt(dot(a, a)); }
 inline bool black(V a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
 inline float lum(V c) { return 0.3086f * c.x + 0.6094f * c.y + 0.0820f * c.z; }
 
+// Random numbers of a path. Two generators behind one interface:
+//  - inc != 0: PCG32 (O'Neill 2014), the library's default streams;
+//  - inc == 0: the reference's Xorshift32Generator (src/HostDeviceCommon/Xorshift.h:18-66), the
+//    32-bit state in 'state': floats are x / 2^32 clamped to 1 - 1e-7, random_index(n) is
+//    floor(x / 2^32 * n) clamped to n - 1.
 struct Pcg
 {
     uint64_t state, inc;
     uint32_t u32()
     {
+        if (inc == 0)
+        {
+            uint32_t x = (uint32_t)state;
+            x ^= x << 13;
+            x ^= x >> 17;
+            x ^= x << 5;
+            state = x;
+            return x;
+        }
         uint64_t old = state;
         state = old * 6364136223846793005ULL + inc;
         uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
         uint32_t rot = (uint32_t)(old >> 59u);
         return (xs >> rot) | (xs << ((32u - rot) & 31u));
     }
-    float next() { return (float)(u32() >> 8) * (1.0f / 16777216.0f); }
+    float next()
+    {
+        if (inc == 0) return std::min((float)u32() / 4294967296.0f, 1.0f - 1.0e-7f);
+        return (float)(u32() >> 8) * (1.0f / 16777216.0f);
+    }
     int index(int n)
     {
+        if (inc == 0)
+        {
+            int i = (int)((float)u32() / 4294967296.0f * (float)n);
+            return std::min(i, n - 1);
+        }
         int i = (int)(next() * (float)n);
         return i < n - 1 ? i : n - 1;
     }
 };
+
+// wang_hash (src/Device/includes/Hash.h:11-19)
+uint32_t wang_hash(uint32_t s)
+{
+    s = (s ^ 61u) ^ (s >> 16);
+    s *= 9u;
+    s = s ^ (s >> 4);
+    s *= 0x27d4eb2du;
+    s = s ^ (s >> 15);
+    return s;
+}
+
+// The reference's per-pixel generator of a frame: Xorshift32 seeded by
+// wang_hash((pixel + 1) * (sample_number + 1) * random_number) (CameraRays.h:155-160,
+// Megakernel.h:52-57), 32-bit wrap-around products.
+Pcg parity_seed(uint32_t pixel, uint32_t sample_number, uint32_t random_number)
+{
+    Pcg r;
+    r.state = wang_hash((pixel + 1u) * (sample_number + 1u) * random_number);
+    r.inc = 0;
+    return r;
+}
 
 uint64_t mix64(uint64_t z)
 {
@@ -216,6 +261,9 @@ struct Settings
     int direct = 0;             // 0: one light + one BSDF sample with MIS, 1: RIS
     int ris_m = 4, ris_n = 1;   // RIS light / BSDF candidates
     const OrcEnv* env = nullptr;  // ambient light / envmap (null: none)
+    int rng_mode = 0;             // 0: PCG streams, 1: the reference's Xorshift32 + packed G-buffer
+    uint32_t random_number = 0;   // rng_mode 1: HIPRTRenderData::random_number of the frame
+    int gbuffer_materials = 0;    // rng_mode 1, principled: offset of the camera-hit material table in pmats
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -260,8 +308,54 @@ void make_query(float* q, V view, V ns, V ng, V l, float eta_i, float eta_o, boo
 
 uint32_t bsdf_seed(Pcg& rng)
 {
+    if (rng.inc == 0) return (uint32_t)rng.state;
     uint32_t s = rng.u32();
     return s != 0u ? s : 0x9E3779B9u;
+}
+
+// After a BSDF sample through the callback: with the reference's generator, the path continues
+// from the sampler's final state (returned in out8[7]); a PCG path already advanced in bsdf_seed.
+void bsdf_seed_done(Pcg& rng, const float* out8)
+{
+    if (rng.inc != 0) return;
+    uint32_t st;
+    std::memcpy(&st, out8 + 7, 4);
+    rng.state = st;
+}
+
+// Octahedral24BitNormalPadded32b pack + unpack (src/HostDeviceCommon/Packing.h:237-367; Cigolle et
+// al. 2014): octahedral projection, two 12-bit snorms in three bytes, decode and normalise.
+float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }
+V oct24(V n)
+{
+    const float l1 = 1.0f / (std::fabs(n.x) + std::fabs(n.y) + std::fabs(n.z));
+    float ex = n.x * l1, ey = n.y * l1;
+    if (n.z < 0.0f)
+    {
+        const float ax = std::fabs(ey), ay = std::fabs(ex);
+        ex = (1.0f - ax) * sign_nz(ex);
+        ey = (1.0f - ay) * sign_nz(ey);
+    }
+    const float sx = std::round(std::min(std::max(ex + 1.0f, 0.0f), 2.0f) * 2047.0f);
+    const float sy = std::round(std::min(std::max(ey + 1.0f, 0.0f), 2.0f) * 2047.0f);
+    const float ux = sx / 16.0f;
+    const float t = std::floor(sy / 256.0f);
+    const unsigned char bx = (unsigned char)ux;
+    const unsigned char by = (unsigned char)((ux - std::floor(ux)) * 256.0f + t);
+    const unsigned char bz = (unsigned char)(sy - t * 256.0f);
+    const float tmp = by / 16.0f;
+    const float px = bx * 16.0f + std::floor(tmp);
+    const float py = (tmp - std::floor(tmp)) * 256.0f * 16.0f + bz;
+    const float dx = std::min(std::max(px / 2047.0f - 1.0f, -1.0f), 1.0f);
+    const float dy = std::min(std::max(py / 2047.0f - 1.0f, -1.0f), 1.0f);
+    V v = mk(dx, dy, 1.0f - std::fabs(dx) - std::fabs(dy));
+    if (v.z < 0.0f)
+    {
+        const float tx = v.x, ty = v.y;
+        v.x = (1.0f - std::fabs(ty)) * sign_nz(tx);
+        v.y = (1.0f - std::fabs(tx)) * sign_nz(ty);
+    }
+    return nrm(v);
 }
 
 }  // namespace

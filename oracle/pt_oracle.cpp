@@ -409,16 +409,34 @@ EnvDirectO env_direct(const OrcEnv& e, const Scene& s, Pcg& rng, V P, int prim, 
     return r;
 }
 
+// rng_mode 1, camera hit: the vertex as the reference's MegaKernel rebuilds it from the packed
+// G-buffer (Megakernel.h:59-70): octahedral-24 normals written after the backface fix
+// (CameraRays.h:178-181), renormalised on read, and the view direction from the camera position
+// (the translation column of the inverse view, Camera::to_hiprt) to the stored hit point
+// (GBufferDevice::get_view_direction), negated into a ray direction, normalised and negated back.
+void gbuffer_vertex(const Settings& st, V P, V& ng, V& ns, V& view)
+{
+    ng = nrm(oct24(ng));
+    ns = nrm(oct24(ns));
+    const V cam = mk(st.iv[3], st.iv[7], st.iv[11]);
+    view = neg(nrm(neg(nrm(cam - P))));
+}
+
 V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
 {
     const int x = pixel % st.width, y = pixel / st.width;
-    Pcg rng = pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
+    Pcg rng = st.rng_mode ? parity_seed((uint32_t)pixel, (uint32_t)iteration, st.random_number)
+                          : pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
+    const uint64_t seed0 = rng.state;
     float px = x + 0.5f, py = y + 0.5f;
     if (st.jitter)
     {
         px += rng.next() - 0.5f;
         py += rng.next() - 0.5f;
     }
+    // the reference's MegaKernel seeds its generator exactly as CameraRays did, so its first
+    // draws repeat the jitter's (Megakernel.h:52-57)
+    if (st.rng_mode) rng.state = seed0;
     float xn = px / st.width * 2.0f - 1.0f, yn = py / st.height * 2.0f - 1.0f;
     V o = mat_point(st.iv, mk(0, 0, 0));
     V pv = mat_point(st.ip, mk(xn, yn, -1.0f));
@@ -447,6 +465,7 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
             refl = refl - nrm(ng * (dot(refl, ng) - 0.01f));
             ns = nrm(view + refl);
         }
+        if (st.rng_mode && bounce == 0) gbuffer_vertex(st, P, ng, ns, view);
         V albedo = s.alb(prim);
         if (bounce == 0) L = L + s.emi(prim);
         // envmap direct lighting: its draws come first at a vertex (the GPU's envmap pass runs
@@ -582,13 +601,18 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
 V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, int pixel, int iteration)
 {
     const int x = pixel % st.width, y = pixel / st.width;
-    Pcg rng = pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
+    Pcg rng = st.rng_mode ? parity_seed((uint32_t)pixel, (uint32_t)iteration, st.random_number)
+                          : pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
+    const uint64_t seed0 = rng.state;
     float px = x + 0.5f, py = y + 0.5f;
     if (st.jitter)
     {
         px += rng.next() - 0.5f;
         py += rng.next() - 0.5f;
     }
+    // the reference's MegaKernel seeds its generator exactly as CameraRays did, so its first
+    // draws repeat the jitter's (Megakernel.h:52-57)
+    if (st.rng_mode) rng.state = seed0;
     float xn = px / st.width * 2.0f - 1.0f, yn = py / st.height * 2.0f - 1.0f;
     V o = mat_point(st.iv, mk(0, 0, 0));
     V pv = mat_point(st.ip, mk(xn, yn, -1.0f));
@@ -618,8 +642,11 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
             refl = refl - nrm(ng * (dot(refl, ng) - 0.01f));
             ns = nrm(view + refl);
         }
+        if (st.rng_mode && bounce == 0) gbuffer_vertex(st, P, ng, ns, view);
         const int mi = s.mat_of[prim];
-        const float* m = ps.mat(mi);
+        // rng_mode 1: the camera hit shades with the material as the G-buffer re-packed it after
+        // the fetch's coat roughening (CameraRays.h:183, Megakernel.h:72)
+        const float* m = (st.rng_mode && bounce == 0 && st.gbuffer_materials) ? ps.mat(mi + st.gbuffer_materials) : ps.mat(mi);
         if (bounce == 0) L = L + s.emi(prim);
         int32_t thin;
         std::memcpy(&thin, m + 44, 4);
@@ -645,6 +672,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                     make_query(qq, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
                     int32_t lobe;
                     ps.sample(m, qq, bsdf_seed(rng), oo, &lobe);
+                    bsdf_seed_done(rng, oo);
                     wi = mk(oo[0], oo[1], oo[2]);
                     pdf = oo[6];
                     return mk(oo[3], oo[4], oo[5]);
@@ -668,6 +696,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                 make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
                 int32_t lobe;
                 ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+            bsdf_seed_done(rng, out);
                 ris_bsdf(s, st, P, ns, prim, mk(out[0], out[1], out[2]), mk(out[3], out[4], out[5]), out[6], st.ris_n, ris);
             }
         }
@@ -721,6 +750,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
             make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
             int32_t lobe;
             ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+            bsdf_seed_done(rng, out);
             const float pdf = out[6];
             V wi = mk(out[0], out[1], out[2]);
             if (pdf > 0.0f && s.ne > 0)
@@ -753,6 +783,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
             make_query(q, view, ns, ng, mk(0, 0, 0), eta_i, eta_o, inside, 0);
             int32_t lobe;
             ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+            bsdf_seed_done(rng, out);
             const float pdf = out[6];
             if (pdf <= 0.0f) return false;
             V wi = mk(out[0], out[1], out[2]);
@@ -787,7 +818,9 @@ extern "C" {
 
 /* settings_i: width, height, nb_bounces, do_rr, rr_min_depth, light_sampling (0 uniform, 1 power),
  * seed, do_jittering, spp, iteration_base, direct lighting (0 MIS, 1 RIS), RIS light candidates,
- * RIS BSDF candidates. env: the world (NULL: none). tri_normals: corner normals, 9 floats per
+ * RIS BSDF candidates, rng mode (0 PCG, 1 the reference's Xorshift32 + packed G-buffer), the
+ * frame's random number (rng mode 1), the offset of the camera-hit material table in pmats (rng
+ * mode 1, principled; 0: none). env: the world (NULL: none). tri_normals: corner normals, 9 floats per
  * triangle (NULL: flat shading). Adds the samples of iterations
  * [iteration_base, iteration_base + spp) to out_rgb (W*H*3 doubles). */
 void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const float* albedo, const float* emission,
@@ -798,7 +831,7 @@ void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const 
     Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum, tri_normals};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
-                settings_i[10], settings_i[11], settings_i[12], env};
+                settings_i[10], settings_i[11], settings_i[12], env, settings_i[13], (uint32_t)settings_i[14], settings_i[15]};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};
@@ -856,7 +889,7 @@ void orc_pt_render_principled(const float* tri_verts, int n_tris, const int* mat
     PScene ps{pmats, (bsdf_eval_fn)eval_fn, (bsdf_sample_fn)sample_fn};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
-                settings_i[10], settings_i[11], settings_i[12], env};
+                settings_i[10], settings_i[11], settings_i[12], env, settings_i[13], (uint32_t)settings_i[14], settings_i[15]};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};
@@ -883,6 +916,18 @@ void orc_pt_render_principled(const float* tri_verts, int n_tris, const int* mat
     for (auto& t : pool) t.join();
 }
 
+/* The octahedral-24 normal round trip of the G-buffer restated (oct24 in orc_common.h). */
+void orc_oct24(const float* in, int n, float* out)
+{
+    for (int i = 0; i < n; i++)
+    {
+        V u = oct24(mk(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+        out[3 * i] = u.x;
+        out[3 * i + 1] = u.y;
+        out[3 * i + 2] = u.z;
+    }
+}
+
 /* Vose alias table exactly as src/Utils/Utils.cpp:63-131: elements normalised in double by
  * 'total_sum' (as given) and scaled by n; FIFO small/large queues in index order. */
 void orc_vose_alias(const float* input, int n, double total_sum, float* out_prob, int* out_alias)
@@ -892,7 +937,7 @@ void orc_vose_alias(const float* input, int n, double total_sum, float* out_prob
     std::deque<int> smalls, larges;
     for (int i = 0; i < n; i++)
     {
-        out_alias[i] = i;
+        out_alias[i] = 0;  // the reference's out_alias.resize(n) value-initialises
         if (q[i] < 1.0f)
             smalls.push_back(i);
         else

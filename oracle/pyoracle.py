@@ -286,7 +286,9 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
     si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0, s.russian_roulette_min_depth,
                    s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base,
                    getattr(s, "direct_lighting", 0), getattr(s, "ris_light_candidates", 4),
-                   getattr(s, "ris_bsdf_candidates", 1)], np.int32)
+                   getattr(s, "ris_bsdf_candidates", 1), getattr(s, "rng_mode", 0),
+                   int(getattr(s, "random_number", 0)) & 0xFFFFFFFF, getattr(s, "gbuffer_materials", 0)],
+                  np.uint32).view(np.int32)
     iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
     ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
     out = np.zeros((s.height, s.width, 3), np.float64)
@@ -328,7 +330,9 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
     si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0, s.russian_roulette_min_depth,
                    s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base,
                    getattr(s, "direct_lighting", 0), getattr(s, "ris_light_candidates", 4),
-                   getattr(s, "ris_bsdf_candidates", 1)], np.int32)
+                   getattr(s, "ris_bsdf_candidates", 1), getattr(s, "rng_mode", 0),
+                   int(getattr(s, "random_number", 0)) & 0xFFFFFFFF, getattr(s, "gbuffer_materials", 0)],
+                  np.uint32).view(np.int32)
     iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
     ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
     out = np.zeros((s.height, s.width, 3), np.float64)
@@ -601,9 +605,151 @@ def vose_alias(power: np.ndarray, total_sum: float):
     return prob, alias
 
 
+def oct24(normals: np.ndarray) -> np.ndarray:
+    """The restated octahedral-24 normal round trip of the reference's G-buffer."""
+    lib = _pt_lib()
+    n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+    out = np.zeros_like(n)
+    lib.orc_oct24(_ptr(n, _c_f), n.shape[0], _ptr(out, _c_f))
+    return out
+
+
 def alias_distribution(prob: np.ndarray, alias: np.ndarray) -> np.ndarray:
     """Probability of each index under the alias sampler (pick uniform i, keep it with prob[i])."""
     n = len(prob)
     d = prob.astype(np.float64).copy()
     np.add.at(d, alias, 1.0 - prob.astype(np.float64))
     return d / n
+
+
+# ---- the reference's own render kernels (oracle/ref_render.cpp): CameraRays + MegaKernel ----
+REF_RENDER_SO = {
+    ("lambert", "uniform"): os.path.join(HERE, "_ref", "libref_render_lambert_uniform.so"),
+    ("lambert", "power"): os.path.join(HERE, "_ref", "libref_render_lambert_power.so"),
+    ("principled", "power"): os.path.join(HERE, "_ref", "libref_render_principled_power.so"),
+}
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+
+def ref_render_available(bsdf: str = "lambert", light: str = "uniform") -> bool:
+    return os.path.exists(REF_RENDER_SO[(bsdf, light)])
+
+
+def _ref_render_lib(bsdf: str, light: str):
+    path = REF_RENDER_SO[(bsdf, light)]
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built: it needs the reference tree (GBPT_REFERENCE_ROOT)")
+    lib = ctypes.CDLL(path)
+    if not getattr(lib, "_sig", False):
+        lib.refr_scene_create.restype = ctypes.c_void_p
+        lib.refr_scene_create.argtypes = [_c_f, _i64, _c_i, _i64, _c_i, _c_f, ctypes.c_int32, _c_f]
+        lib.refr_scene_free.argtypes = [ctypes.c_void_p]
+        lib.refr_scene_light_table.argtypes = [ctypes.c_void_p, _c_i, _c_i, _c_f, _c_i, _c_f]
+        lib.refr_alias_table.argtypes = [_c_f, ctypes.c_int32, ctypes.c_float, _c_f, _c_i]
+        lib.refr_render.argtypes = [ctypes.c_void_p, _c_i, _c_f, _c_f, _c_f, ctypes.c_uint32, ctypes.c_uint32, _c_f,
+                                    _c_i, _c_f]
+        lib.refr_pack_unpack_material.argtypes = [_c_f, _c_f]
+        lib.refr_oct24.argtypes = [_c_f, _i64, _c_f, _u32p]
+        lib._sig = True
+    return lib
+
+
+class RefRender:
+    """A scene in the reference's own CPU renderer (CameraRays + MegaKernel compiled from the
+    reference's sources, one build per BSDF override 'lambert' / 'principled' and light sampling
+    'uniform' / 'power'). materials: (M, 64) gbpt_principled_material records (for 'lambert' only
+    base colour and emission matter)."""
+
+    def __init__(self, bsdf, light, positions, indices, material_of, materials, vertex_normals=None):
+        self._lib = _ref_render_lib(bsdf, light)
+        self._pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        self._idx = np.ascontiguousarray(indices, np.int32).reshape(-1, 3)
+        self._mo = np.ascontiguousarray(material_of, np.int32)
+        self._mats = np.ascontiguousarray(materials, np.float32).reshape(-1, 64)
+        self._nrm = None if vertex_normals is None else np.ascontiguousarray(vertex_normals, np.float32).reshape(-1, 3)
+        self._h = self._lib.refr_scene_create(_ptr(self._pos, _c_f), self._pos.shape[0], _ptr(self._idx, _c_i),
+                                              self._idx.shape[0], _ptr(self._mo, _c_i), _ptr(self._mats, _c_f),
+                                              self._mats.shape[0], _ptr(self._nrm, _c_f))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.refr_scene_free(h)
+            self._h = None
+
+    def light_table(self):
+        n = ctypes.c_int32(0)
+        self._lib.refr_scene_light_table(self._h, ctypes.byref(n), None, None, None, None)
+        e = np.zeros(n.value, np.int32)
+        p = np.zeros(n.value, np.float32)
+        a = np.zeros(n.value, np.int32)
+        s = ctypes.c_float(0.0)
+        self._lib.refr_scene_light_table(self._h, None, _ptr(e, _c_i), _ptr(p, _c_f), _ptr(a, _c_i), ctypes.byref(s))
+        return dict(emissive=e, probas=p, alias=a, power_sum=s.value)
+
+    def render(self, settings, sample_number: int, random_number: int, gbuffer: bool = False):
+        """One frame (one sample per pixel) -> (H, W, 3) float32; with gbuffer, also the camera
+        pass's first-hit primitives (H, W) and positions (H, W, 3)."""
+        s = settings
+        si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0,
+                       s.russian_roulette_min_depth, 1 if s.do_jittering else 0], np.int32)
+        sf = np.array([s.russian_roulette_throughput_clamp], np.float32)
+        iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
+        ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
+        out = np.zeros((s.height, s.width, 3), np.float32)
+        prim = np.zeros((s.height, s.width), np.int32) if gbuffer else None
+        pos = np.zeros((s.height, s.width, 3), np.float32) if gbuffer else None
+        self._lib.refr_render(self._h, _ptr(si, _c_i), _ptr(sf, _c_f), _ptr(iv, _c_f), _ptr(ip, _c_f),
+                              int(sample_number) & 0xFFFFFFFF, int(random_number) & 0xFFFFFFFF, _ptr(out, _c_f),
+                              _ptr(prim, _c_i), _ptr(pos, _c_f))
+        return (out, prim, pos) if gbuffer else out
+
+
+def ref_pack_unpack_material(materials: np.ndarray) -> np.ndarray:
+    """The reference's 8-bit material packing then unpacking (CPUMaterial::pack_to_GPU,
+    DevicePackedEffectiveMaterial::unpack) of (M, 64) records."""
+    lib = _ref_render_lib("lambert", "uniform")
+    m = np.ascontiguousarray(materials, np.float32).reshape(-1, 64)
+    out = np.zeros_like(m)
+    for i in range(m.shape[0]):
+        lib.refr_pack_unpack_material(_ptr(m[i], _c_f), _ptr(out[i], _c_f))
+    return out
+
+
+def ref_oct24(normals: np.ndarray):
+    """Octahedral24BitNormalPadded32b pack + unpack of (N, 3) normals -> (unpacked (N, 3), packed (N,))."""
+    lib = _ref_render_lib("lambert", "uniform")
+    n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+    out = np.zeros_like(n)
+    packed = np.zeros(n.shape[0], np.uint32)
+    lib.refr_oct24(_ptr(n, _c_f), n.shape[0], _ptr(out, _c_f), _ptr(packed, _u32p))
+    return out, packed
+
+
+def ref_alias_table(power: np.ndarray, total_sum: float):
+    """The reference's own Utils::compute_alias_table (extracted from src/Utils/Utils.cpp)."""
+    lib = _ref_render_lib("lambert", "uniform")
+    p = np.ascontiguousarray(power, np.float32)
+    prob = np.zeros(len(p), np.float32)
+    alias = np.zeros(len(p), np.int32)
+    lib.refr_alias_table(_ptr(p, _c_f), len(p), float(total_sum), _ptr(prob, _c_f), _ptr(alias, _c_i))
+    return prob, alias
+
+
+def wang_hash(x: int) -> int:
+    """wang_hash (src/Device/includes/Hash.h:11-19) on uint32."""
+    x &= 0xFFFFFFFF
+    x = ((x ^ 61) ^ (x >> 16)) & 0xFFFFFFFF
+    x = (x * 9) & 0xFFFFFFFF
+    x ^= x >> 4
+    x = (x * 0x27D4EB2D) & 0xFFFFFFFF
+    x ^= x >> 15
+    return x
+
+
+def xorshift32(x: int) -> int:
+    """One step of the reference's Xorshift32Generator (src/HostDeviceCommon/Xorshift.h:55-62)."""
+    x ^= (x << 13) & 0xFFFFFFFF
+    x ^= x >> 17
+    x ^= (x << 5) & 0xFFFFFFFF
+    return x & 0xFFFFFFFF

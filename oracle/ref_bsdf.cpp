@@ -176,13 +176,15 @@ void ref_principled_sample(const float* mats, const int32_t* mat_index, const fl
 }
 
 /* Single-query forms with the same layouts, handed to the path-tracing oracle (pt_oracle.cpp) as
- * function pointers so that it shades with the reference's own BSDF. */
+ * function pointers so that it shades with the reference's own BSDF. The sample form returns in
+ * out[7] the bits of the Xorshift32 state after sampling. */
 void ref_principled_eval_one(const float* mat, const float* q, float* out) { eval_query(mat, q, out); }
 
 void ref_principled_sample_one(const float* mat, const float* q, uint32_t seed, float* out, int32_t* lobe)
 {
     uint32_t rng_after;
     sample_query(mat, q, seed, out, lobe, &rng_after);
+    std::memcpy(out + 7, &rng_after, 4);  // the generator's state after sampling, bit for bit
 }
 
 }  // extern "C"

@@ -1,0 +1,434 @@
+/*
+ * TEST INFRASTRUCTURE ONLY — C entry points into the reference's OWN render kernels, compiled
+ * from the reference's sources where they lie (oracle/Makefile, target 'ref'), behind the
+ * clean-room shim headers in oracle/shim/. Output goes to oracle/_ref/ (git-ignored). Used by
+ * tests/golden/make_ref_render_golden.py to write golden images that pin this project's
+ * wavefront path tracer sample by sample.
+ *
+ * Calls, unmodified, one frame per call over every pixel (OpenMP rows, as
+ * CPURenderer::debug_render_pass, src/Renderer/CPURenderer.cpp:613-686, walks them):
+ *   - CameraRays(render_data, x, y)  (src/Device/kernels/CameraRays.h:83-213): jittered camera
+ *     ray, closest hit through the CPU BVH (BVH::intersect, src/Renderer/BVH.h:132-223), the
+ *     packed G-buffer (8-bit material, octahedral-24 normals);
+ *   - MegaKernel(render_data, x, y)  (src/Device/kernels/Megakernel.h:23-144): the bounce loop
+ *     with next-event estimation, BSDF continuation, Russian roulette and accumulation.
+ * Scene set-up follows CPURenderer::set_scene (src/Renderer/CPURenderer.cpp:297-420): materials
+ * packed by CPUMaterial::pack_to_GPU (src/HostDeviceCommon/Material/MaterialCPU.h:31-118) into
+ * the CPU material SoA, triangle areas as ThreadFunctions::load_scene_compute_triangle_areas
+ * (src/Threads/ThreadFunctions.cpp:221-243), the emissive list in triangle order, and for power
+ * sampling the float power list + float running sum + Utils::compute_alias_table
+ * (CPURenderer::compute_emissives_power_alias_table, src/Renderer/CPURenderer.cpp:426-465;
+ * the alias function is the reference's own, extracted from src/Utils/Utils.cpp by the Makefile).
+ *
+ * Compile-time options (-D on the command line, applied after the reference's option headers):
+ *   REF_BSDF = BSDF_LAMBERTIAN (1) or BSDF_PRINCIPLED (3) -> BSDFOverride
+ *   REF_LIGHT_BASE = LSS_BASE_UNIFORM (0) or LSS_BASE_POWER (1) -> DirectLightSamplingBaseStrategy
+ * and always: DirectLightSamplingStrategy = LSS_MIS_LIGHT_BSDF (one light sample + one BSDF
+ * sample, balance heuristic), energy compensation and microfacet regularization off (as the BSDF
+ * harness builds them), alpha testing off (render_settings.do_alpha_testing = false: untextured
+ * materials would otherwise draw a random number per candidate hit), adaptive sampling and the
+ * pixel noise threshold off, no envmap (ambient light NONE).
+ *
+ * Material records: the 64-word gbpt_principled_material layout (include/gbpt_bsdf.h), emission
+ * already multiplied by strength and global factor.
+ */
+#include "HostDeviceCommon/KernelOptions/KernelOptions.h"
+
+#undef DirectLightSamplingStrategy
+#define DirectLightSamplingStrategy LSS_MIS_LIGHT_BSDF
+#undef DirectLightSamplingBaseStrategy
+#define DirectLightSamplingBaseStrategy REF_LIGHT_BASE
+#undef BSDFOverride
+#define BSDFOverride REF_BSDF
+#undef PrincipledBSDFDoEnergyCompensation
+#define PrincipledBSDFDoEnergyCompensation KERNEL_OPTION_FALSE
+#undef PrincipledBSDFDoMicrofacetRegularization
+#define PrincipledBSDFDoMicrofacetRegularization KERNEL_OPTION_FALSE
+
+#include "Device/kernels/CameraRays.h"
+#include "Device/kernels/Megakernel.h"
+#include "HostDeviceCommon/Material/MaterialCPU.h"
+#include "Renderer/BVH.h"
+#include "Renderer/CPUDataStructures/MaterialPackedSoACPUData.h"
+#include "Utils/Utils.h"
+
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+CPUMaterial cpu_material(const float* w)
+{
+    CPUMaterial m;
+    m.base_color = ColorRGB32F(w[0], w[1], w[2]);
+    m.roughness = w[3];
+    m.emission = ColorRGB32F(w[4], w[5], w[6]);
+    m.metallic = w[7];
+    m.metallic_F82 = ColorRGB32F(w[8], w[9], w[10]);
+    m.metallic_F90_falloff_exponent = w[11];
+    m.metallic_F90 = ColorRGB32F(w[12], w[13], w[14]);
+    m.anisotropy = w[15];
+    m.anisotropy_rotation = w[16];
+    m.second_roughness_weight = w[17];
+    m.second_roughness = w[18];
+    m.specular = w[19];
+    m.specular_color = ColorRGB32F(w[20], w[21], w[22]);
+    m.specular_tint = w[23];
+    m.specular_darkening = w[24];
+    m.coat = w[25];
+    m.coat_roughness = w[26];
+    m.coat_roughening = w[27];
+    m.coat_medium_absorption = ColorRGB32F(w[28], w[29], w[30]);
+    m.coat_medium_thickness = w[31];
+    m.coat_darkening = w[32];
+    m.coat_anisotropy = w[33];
+    m.coat_anisotropy_rotation = w[34];
+    m.coat_ior = w[35];
+    m.sheen = w[36];
+    m.ior = w[37];
+    m.specular_transmission = w[38];
+    m.diffuse_transmission = w[39];
+    m.absorption_color = ColorRGB32F(w[40], w[41], w[42]);
+    m.absorption_at_distance = w[43];
+    int32_t thin;
+    std::memcpy(&thin, w + 44, 4);
+    m.thin_walled = thin != 0;
+    // the reference's scene parser calls make_safe on every material
+    // (src/Scene/SceneParser.cpp:391-438); its clamps only touch fields this layout does not
+    // carry, except the dielectric priority of non-transmissive materials
+    m.make_safe();
+    return m;
+}
+
+struct RefRenderScene
+{
+    std::vector<int> indices;
+    std::vector<float3> positions;
+    std::vector<float3> normals;
+    std::vector<float2> texcoords;  // zeros: the path reads them, nothing textured uses them
+    std::vector<unsigned char> has_normals;
+    std::vector<int> material_of;
+    std::vector<float> areas;
+    std::vector<int> emissive;
+    std::vector<unsigned char> opaque;
+    std::vector<float> alias_probas;
+    std::vector<int> alias_alias;
+    float power_sum = 0.0f;
+    DevicePackedTexturedMaterialSoACPUData materials;
+    std::vector<Triangle> tris, emissive_tris;
+    BVH* bvh = nullptr;
+    BVH* light_bvh = nullptr;
+};
+
+}  // namespace
+
+#define REF_EXPORT extern "C" __attribute__((visibility("default")))
+
+REF_EXPORT void* refr_scene_create(const float* positions, int64_t n_vertices, const int32_t* indices, int64_t n_triangles,
+                        const int32_t* material_indices, const float* materials, int32_t n_materials,
+                        const float* vertex_normals)
+{
+    RefRenderScene* s = new RefRenderScene();
+    s->indices.assign(indices, indices + 3 * n_triangles);
+    s->positions.resize(n_vertices);
+    s->normals.resize(n_vertices);
+    s->has_normals.resize(n_vertices);
+    s->texcoords.assign(n_vertices, make_float2(0.0f, 0.0f));
+    for (int64_t v = 0; v < n_vertices; v++)
+    {
+        s->positions[v] = make_float3(positions[3 * v], positions[3 * v + 1], positions[3 * v + 2]);
+        float3 n = vertex_normals ? make_float3(vertex_normals[3 * v], vertex_normals[3 * v + 1], vertex_normals[3 * v + 2])
+                                  : make_float3(0.0f, 0.0f, 0.0f);
+        s->normals[v] = n;
+        s->has_normals[v] = (n.x != 0.0f || n.y != 0.0f || n.z != 0.0f) ? 1 : 0;
+    }
+    s->material_of.assign(material_indices, material_indices + n_triangles);
+
+    std::vector<CPUMaterial> cpu(n_materials);
+    std::vector<DevicePackedTexturedMaterial> packed(n_materials);
+    for (int m = 0; m < n_materials; m++)
+    {
+        cpu[m] = cpu_material(materials + 64 * (int64_t)m);
+        packed[m] = cpu[m].pack_to_GPU();
+    }
+    s->materials.upload_data(packed);
+    s->opaque.assign(n_materials, 0);
+
+    s->areas.resize(n_triangles);
+    for (int64_t t = 0; t < n_triangles; t++)
+    {
+        float3 A = s->positions[s->indices[3 * t]], B = s->positions[s->indices[3 * t + 1]], C = s->positions[s->indices[3 * t + 2]];
+        float3 normal = hippt::cross(B - A, C - A);
+        s->areas[t] = hippt::length(normal) * 0.5f;
+        if (cpu[s->material_of[t]].is_emissive()) s->emissive.push_back((int)t);
+    }
+
+    // power list in float, float running sum (CPURenderer.cpp:437-456)
+    std::vector<float> power(s->emissive.size());
+    float sum = 0.0f;
+    for (size_t i = 0; i < s->emissive.size(); i++)
+    {
+        int t = s->emissive[i];
+        float3 A = s->positions[s->indices[3 * t]], B = s->positions[s->indices[3 * t + 1]], C = s->positions[s->indices[3 * t + 2]];
+        float3 normal = hippt::cross(B - A, C - A);
+        float area = 0.5f * hippt::length(normal);
+        const CPUMaterial& m = cpu[s->material_of[t]];
+        float lum = m.emission.luminance() * m.emission_strength * m.global_emissive_factor;
+        power[i] = lum * area;
+        sum += power[i];
+    }
+    s->power_sum = sum;
+    if (!power.empty()) Utils::compute_alias_table(power, sum, s->alias_probas, s->alias_alias);
+
+    s->tris.resize(n_triangles);
+    for (int64_t t = 0; t < n_triangles; t++)
+        s->tris[t] = Triangle(s->positions[s->indices[3 * t]], s->positions[s->indices[3 * t + 1]], s->positions[s->indices[3 * t + 2]]);
+    for (int t : s->emissive) s->emissive_tris.push_back(s->tris[t]);
+    s->bvh = new BVH(&s->tris);
+    s->light_bvh = new BVH(&s->emissive_tris);
+    return s;
+}
+
+REF_EXPORT void refr_scene_free(void* h)
+{
+    RefRenderScene* s = static_cast<RefRenderScene*>(h);
+    delete s->bvh;
+    delete s->light_bvh;
+    delete s;
+}
+
+/* The emissive list and the power alias table the reference builds (float sum). Arrays of
+ * n_emissive entries; any pointer may be NULL. */
+REF_EXPORT void refr_scene_light_table(void* h, int32_t* n_emissive, int32_t* emissive, float* probas, int32_t* alias, float* power_sum)
+{
+    RefRenderScene* s = static_cast<RefRenderScene*>(h);
+    if (n_emissive) *n_emissive = (int32_t)s->emissive.size();
+    for (size_t i = 0; i < s->emissive.size(); i++)
+    {
+        if (emissive) emissive[i] = s->emissive[i];
+        if (probas && !s->alias_probas.empty()) probas[i] = s->alias_probas[i];
+        if (alias && !s->alias_alias.empty()) alias[i] = s->alias_alias[i];
+    }
+    if (power_sum) *power_sum = s->power_sum;
+}
+
+/* Utils::compute_alias_table(input, in_input_total_sum, ...) on a caller's power list and sum. */
+REF_EXPORT void refr_alias_table(const float* power, int32_t n, float sum, float* probas, int32_t* alias)
+{
+    std::vector<float> in(power, power + n), p;
+    std::vector<int> a;
+    Utils::compute_alias_table(in, sum, p, a);
+    for (int32_t i = 0; i < n; i++)
+    {
+        probas[i] = p[i];
+        alias[i] = a[i];
+    }
+}
+
+/* One frame: CameraRays then MegaKernel over every pixel. settings_i = {width, height,
+ * nb_bounces, do_russian_roulette, russian_roulette_min_depth, do_jittering}, settings_f =
+ * {russian_roulette_throughput_clamp}; inverse_view / inverse_projection row-major as
+ * HIPRTCamera holds them; the camera position is the translation column of inverse_view
+ * (what Camera::to_hiprt's row-vector product with it gives, src/Scene/Camera.cpp:24-25).
+ * out_rgb (W*H*3): the frame's sample of every pixel. Also returns, when not NULL, the packed
+ * G-buffer the camera pass wrote: gbuf_prim (W*H), gbuf_pos (W*H*3). */
+namespace {
+
+// The buffers of one frame and the render data pointing at them (CPURenderer's per-frame state).
+struct Frame
+{
+    int W, H;
+    std::vector<ColorRGB32F> accum;
+    std::vector<unsigned char> pixel_active;
+    std::vector<float3> den_normals;
+    std::vector<ColorRGB32F> den_albedo;
+    std::vector<DevicePackedEffectiveMaterial> gb_mat;
+    std::vector<Octahedral24BitNormalPadded32b> gb_gn, gb_sn;
+    std::vector<float3> gb_pos;
+    std::vector<int> gb_prim;
+    unsigned char still_active = 0;
+    AtomicType<unsigned int> converged{0};
+    HIPRTRenderData rd;
+
+    Frame(RefRenderScene* s, const int32_t* settings_i, const float* settings_f, const float* inverse_view,
+          const float* inverse_projection, uint32_t sample_number, uint32_t random_number)
+        : W(settings_i[0]), H(settings_i[1])
+    {
+        const int n_pix = W * H;
+        accum.assign(n_pix, ColorRGB32F(0.0f));
+        pixel_active.assign(n_pix, 0);
+        den_normals.resize(n_pix);
+        den_albedo.resize(n_pix);
+        gb_mat.resize(n_pix);
+        gb_gn.resize(n_pix);
+        gb_sn.resize(n_pix);
+        gb_pos.resize(n_pix);
+        gb_prim.assign(n_pix, -1);
+
+        rd.random_number = random_number;
+        rd.buffers.accumulated_ray_colors = accum.data();
+        rd.buffers.triangles_indices = s->indices.data();
+        rd.buffers.vertices_positions = s->positions.data();
+        rd.buffers.has_vertex_normals = s->has_normals.data();
+        rd.buffers.vertex_normals = s->normals.data();
+        rd.buffers.texcoords = s->texcoords.data();
+        rd.buffers.triangles_areas = s->areas.data();
+        rd.buffers.material_indices = s->material_of.data();
+        rd.buffers.materials_buffer = s->materials.get_device_SoA_struct();
+        rd.buffers.material_opaque = s->opaque.data();
+        rd.buffers.emissive_triangles_count = (int)s->emissive.size();
+        rd.buffers.emissive_triangles_primitive_indices = s->emissive.data();
+        rd.buffers.emissive_triangles_primitive_indices_and_emissive_textures = s->emissive.data();
+        rd.buffers.emissives_power_alias_table.alias_table_probas = s->alias_probas.data();
+        rd.buffers.emissives_power_alias_table.alias_table_alias = s->alias_alias.data();
+        rd.buffers.emissives_power_alias_table.sum_elements = s->power_sum;
+        rd.buffers.emissives_power_alias_table.size = (int)s->emissive.size();
+
+        rd.aux_buffers.pixel_active = pixel_active.data();
+        rd.aux_buffers.denoiser_normals = den_normals.data();
+        rd.aux_buffers.denoiser_albedo = den_albedo.data();
+        rd.aux_buffers.still_one_ray_active = &still_active;
+        rd.aux_buffers.pixel_count_converged_so_far = &converged;
+
+        rd.g_buffer.materials = gb_mat.data();
+        rd.g_buffer.geometric_normals = gb_gn.data();
+        rd.g_buffer.shading_normals = gb_sn.data();
+        rd.g_buffer.primary_hit_position = gb_pos.data();
+        rd.g_buffer.first_hit_prim_index = gb_prim.data();
+
+        HIPRTRenderSettings& rs = rd.render_settings;
+        rs.render_resolution = make_int2(W, H);
+        rs.need_to_reset = true;
+        rs.sample_number = sample_number;
+        rs.nb_bounces = settings_i[2];
+        rs.do_russian_roulette = settings_i[3] != 0;
+        rs.russian_roulette_min_depth = settings_i[4];
+        rs.russian_roulette_throughput_clamp = settings_f[0];
+        rs.do_alpha_testing = false;
+        rs.enable_adaptive_sampling = false;
+        rs.stop_pixel_noise_threshold = 0.0f;
+        rs.do_update_status_buffers = false;
+
+        rd.world_settings.ambient_light_type = AmbientLightType::NONE;
+
+        HIPRTCamera cam;
+        std::memcpy(&cam.inverse_view, inverse_view, 16 * sizeof(float));
+        std::memcpy(&cam.inverse_projection, inverse_projection, 16 * sizeof(float));
+        cam.position = make_float3(inverse_view[3], inverse_view[7], inverse_view[11]);
+        cam.do_jittering = settings_i[5] != 0;
+        cam.sensor_width = W;
+        cam.sensor_height = H;
+        rd.current_camera = cam;
+        rd.prev_camera = cam;
+
+        rd.cpu_only.bvh = s->bvh;
+        rd.cpu_only.light_bvh = s->light_bvh;
+    }
+};
+
+}  // namespace
+
+/* One frame: CameraRays then MegaKernel over every pixel. settings_i = {width, height,
+ * nb_bounces, do_russian_roulette, russian_roulette_min_depth, do_jittering}, settings_f =
+ * {russian_roulette_throughput_clamp}; inverse_view / inverse_projection row-major as
+ * HIPRTCamera holds them; the camera position is the translation column of inverse_view
+ * (what Camera::to_hiprt's row-vector product with it gives, src/Scene/Camera.cpp:24-25).
+ * out_rgb (W*H*3): the frame's sample of every pixel. Also returns, when not NULL, the packed
+ * G-buffer the camera pass wrote: gbuf_prim (W*H), gbuf_pos (W*H*3). */
+REF_EXPORT void refr_render(void* h, const int32_t* settings_i, const float* settings_f, const float* inverse_view,
+                            const float* inverse_projection, uint32_t sample_number, uint32_t random_number, float* out_rgb,
+                            int32_t* gbuf_prim, float* gbuf_pos)
+{
+    RefRenderScene* s = static_cast<RefRenderScene*>(h);
+    Frame f(s, settings_i, settings_f, inverse_view, inverse_projection, sample_number, random_number);
+    const int W = f.W, H = f.H;
+    HIPRTRenderData& rd = f.rd;
+
+#pragma omp parallel for schedule(dynamic)
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) CameraRays(rd, x, y);
+#pragma omp parallel for schedule(dynamic)
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) MegaKernel(rd, x, y);
+
+    for (int i = 0; i < W * H; i++)
+    {
+        out_rgb[3 * i] = f.accum[i].r;
+        out_rgb[3 * i + 1] = f.accum[i].g;
+        out_rgb[3 * i + 2] = f.accum[i].b;
+        if (gbuf_prim) gbuf_prim[i] = f.gb_prim[i];
+        if (gbuf_pos)
+        {
+            gbuf_pos[3 * i] = f.gb_pos[i].x;
+            gbuf_pos[3 * i + 1] = f.gb_pos[i].y;
+            gbuf_pos[3 * i + 2] = f.gb_pos[i].z;
+        }
+    }
+}
+
+/* The material the reference's kernels see after packing (pack_to_GPU, the 8-bit fields of
+ * DevicePackedEffectiveMaterial, src/HostDeviceCommon/Material/MaterialPacked.h) and unpacking,
+ * written back in the 64-word layout (words 45..63 zero). */
+REF_EXPORT void refr_pack_unpack_material(const float* in, float* out)
+{
+    CPUMaterial c = cpu_material(in);
+    DevicePackedEffectiveMaterial p = c.pack_to_GPU();
+    DeviceUnpackedEffectiveMaterial m = p.unpack();
+    float w[64] = {};
+    w[0] = m.base_color.r; w[1] = m.base_color.g; w[2] = m.base_color.b;
+    w[3] = m.roughness;
+    w[4] = m.emission.r; w[5] = m.emission.g; w[6] = m.emission.b;
+    w[7] = m.metallic;
+    w[8] = m.metallic_F82.r; w[9] = m.metallic_F82.g; w[10] = m.metallic_F82.b;
+    w[11] = m.metallic_F90_falloff_exponent;
+    w[12] = m.metallic_F90.r; w[13] = m.metallic_F90.g; w[14] = m.metallic_F90.b;
+    w[15] = m.anisotropy;
+    w[16] = m.anisotropy_rotation;
+    w[17] = m.second_roughness_weight;
+    w[18] = m.second_roughness;
+    w[19] = m.specular;
+    w[20] = m.specular_color.r; w[21] = m.specular_color.g; w[22] = m.specular_color.b;
+    w[23] = m.specular_tint;
+    w[24] = m.specular_darkening;
+    w[25] = m.coat;
+    w[26] = m.coat_roughness;
+    w[27] = m.coat_roughening;
+    w[28] = m.coat_medium_absorption.r; w[29] = m.coat_medium_absorption.g; w[30] = m.coat_medium_absorption.b;
+    w[31] = m.coat_medium_thickness;
+    w[32] = m.coat_darkening;
+    w[33] = m.coat_anisotropy;
+    w[34] = m.coat_anisotropy_rotation;
+    w[35] = m.coat_ior;
+    w[36] = m.sheen;
+    w[37] = m.ior;
+    w[38] = m.specular_transmission;
+    w[39] = m.diffuse_transmission;
+    w[40] = m.absorption_color.r; w[41] = m.absorption_color.g; w[42] = m.absorption_color.b;
+    w[43] = m.absorption_at_distance;
+    int32_t thin = m.thin_walled ? 1 : 0;
+    std::memcpy(w + 44, &thin, 4);
+    std::memcpy(out, w, sizeof(w));
+}
+
+/* Octahedral24BitNormalPadded32b pack then unpack (src/HostDeviceCommon/Packing.h:237-367) of n
+ * normals; packed (may be NULL) gets the three bytes x | y << 8 | z << 16. */
+REF_EXPORT void refr_oct24(const float* in, int64_t n, float* out, uint32_t* packed)
+{
+    for (int64_t i = 0; i < n; i++)
+    {
+        Octahedral24BitNormalPadded32b p = Octahedral24BitNormalPadded32b::pack_static(make_float3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+        float3 u = p.unpack();
+        out[3 * i] = u.x;
+        out[3 * i + 1] = u.y;
+        out[3 * i + 2] = u.z;
+        if (packed)
+        {
+            unsigned char b[4];
+            std::memcpy(b, &p, 4);
+            packed[i] = (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16);
+        }
+    }
+}
+

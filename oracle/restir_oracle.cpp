@@ -343,6 +343,7 @@ Res initial_pixel(const Ctx& c, const float* gb, int pixel)
         make_query(q, su.view, su.ns, su.ng, mk(0, 0, 0), eta_in(su, m), eta_out(su, m), su.inside, 0);
         int32_t lobe;
         c.ps.sample(m, q, bsdf_seed(rng), out, &lobe);
+        bsdf_seed_done(rng, out);
         float pdf = out[6];
         if (!(pdf > 0.0f)) continue;
         V dir = mk(out[0], out[1], out[2]);
