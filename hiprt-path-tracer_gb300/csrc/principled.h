@@ -105,11 +105,16 @@ GBPT_HD Material load_material(const gbpt_principled_material& s)
 
 // Media on both sides of the interface: IOR of the medium the ray travels in (1 = air) and of
 // the medium behind the surface, and whether the ray is inside the object (RayVolumeState).
+// 'beer' is the Beer-Lambert attenuation of the volume the ray leaves (absorbing: not white),
+// which the reference's glass and diffuse-transmission lobes apply to refracted directions
+// (principled_glass_eval, Principled.h:540-546; principled_diffuse_transmission_eval, :844-851).
 struct Medium
 {
     float eta_incident;
     float eta_outgoing;
     bool inside;
+    bool absorbing = false;
+    V3 beer = V3{1.0f, 1.0f, 1.0f};
 };
 
 enum class Delta
@@ -641,6 +646,9 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
             pdf += fabsf(l.z * kInvPi) * p.diffuse_transmission;
         }
     }
+    // a refracted direction crosses out of the volume the ray travelled in: only the glass and
+    // diffuse-transmission lobes contribute there, both attenuated by its absorption
+    if (md.absorbing && !(v.z * l.z > 0.0f)) color = color * md.beer;
     return color;
 }
 

@@ -17,6 +17,7 @@
 #include "render_kernels.h"
 #include "restir.h"
 #include "trace_core.h"
+#include "volume.h"
 
 namespace gbpt {
 namespace {
@@ -92,7 +93,12 @@ __global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers
         q.slot[i] = (int32_t)slot;
         pb.throughput[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         pb.radiance[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (pb.medium) pb.medium[slot] = -1;
+        if (pb.vol_stack)
+        {
+            VolumeStack v;
+            v.reset();
+            v.store(pb.vol_stack, pb.vol_state, slot);
+        }
         store_rng(pb.rng + slot, rng);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -192,13 +198,11 @@ __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0,
             {
                 const bsdf::Material m = bsdf::load_material(s.pmats[mat]);
                 const bool hc = rc.ggx_height_correlated != 0;
-                // the vertex's volume state, as shade derives it
-                const int cur_medium = pb.medium[slot];
-                const bool transmissive = (m.transmission > 0.0f || m.diffuse_transmission > 0.0f) && !m.thin_walled;
-                bsdf::Medium md;
-                md.inside = transmissive && dot(view, ng_raw) < 0.0f;
-                md.eta_incident = md.inside ? m.ior : (cur_medium >= 0 ? s.pmats[cur_medium].ior : 1.0f);
-                md.eta_outgoing = md.inside ? 1.0f : m.ior;
+                // the vertex's volume state, as shade derives it (the hit pushed on the path's stack)
+                VolumeStack vol;
+                vol.load(pb.vol_stack, pb.vol_state, slot);
+                volume_hit(vol, s.pmats[mat], mat, hit.x);
+                const bsdf::Medium md = volume_medium(s, vol);
                 ed = env_direct(
                     s.env, rng, ns, tp, can_light_sample(m),
                     [&](V3 wi, float& pdf) {
@@ -245,9 +249,9 @@ __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0,
 }
 
 // ---------------------------------------------------------------------------------------------
-// shade: one path vertex per active path. PRINCIPLED selects the layered principled BSDF with
-// volume tracking (a path refracting into a non-thin transmissive material is inside it until it
-// refracts out), else the Lambertian BSDF override.
+// shade: one path vertex per active path. PRINCIPLED selects the layered principled BSDF with the
+// reference's nested-dielectric volume tracking (volume.h: each hit pushes its material, the
+// continuation pops what it leaves), else the Lambertian BSDF override.
 // ---------------------------------------------------------------------------------------------
 template <bool PRINCIPLED>
 __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc0, PathBuffers pb, Queue in, Queue next,
@@ -304,7 +308,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
         float light_target = 0.0f;  // RIS: target function of the kept light candidate
         float4 bsdf_pending = make_float4(0, 0, 0, 0);
         float guide_pdf_out = 0.0f;  // MIS pdf of this vertex's continuation when it is guided
-        int next_medium = -1;
+        VolumeStack vol;  // principled paths: the volume state after this vertex
         Pcg32 rng = load_rng(rc, 0);
         if (alive)
         {
@@ -501,15 +505,11 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                 const bsdf::Material m = bsdf::load_material(
                     (rc.rng_mode == GBPT_RNG_REFERENCE && bounce == 0 && s.pmats_camera) ? s.pmats_camera[mat] : s.pmats[mat]);
                 const bool hc = rc.ggx_height_correlated != 0;
-                // volume state: inside a transmissive (non thin-walled) object when its back face is
-                // hit; the incident medium is then the object, else the volume the path is in
-                const int cur_medium = pb.medium[slot];
-                const bool transmissive = (m.transmission > 0.0f || m.diffuse_transmission > 0.0f) && !m.thin_walled;
-                bsdf::Medium md;
-                md.inside = transmissive && dot(view, ng_raw) < 0.0f;
-                md.eta_incident = md.inside ? m.ior : (cur_medium >= 0 ? s.pmats[cur_medium].ior : 1.0f);
-                md.eta_outgoing = md.inside ? 1.0f : m.ior;
-                next_medium = cur_medium;
+                // volume state: the hit pushes its material on the path's nested-dielectric stack
+                // (at the camera hit the stack holds only the air, as reconstruct_first_hit rebuilds it)
+                vol.load(pb.vol_stack, pb.vol_state, slot);
+                volume_hit(vol, s.pmats[mat], mat, hit.x);
+                const bsdf::Medium md = volume_medium(s, vol);
                 // guided vertex (materials without delta lobes or transmission): the continuation is
                 // drawn from the learned mixture / the BSDF and, outside ReSTIR's bounce 0, doubles as
                 // the BSDF technique of next-event estimation (MIS pdf alpha q + (1 - alpha) p)
@@ -702,6 +702,9 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                         f = bsdf::sample(m, md, hc, view, ns, ng, xr, wi, lobe, pdf);
                         bsdf_rng_done(rng, xr);
                     }
+                    // the continuation leaves the vertex's volume entries behind (a guided direction
+                    // reflects off an opaque material: lobe NONE pops like a reflection lobe)
+                    volume_after_sample(s, vol, m, view, ns, ng, wi, lobe);
                     if (pdf > 0.0f)
                     {
                         const V3 atten = f * fabsf(dot(wi, ns)) / pdf;
@@ -729,8 +732,6 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                             tp = t2;
                             want_next = true;
                             nx_d = f4(wi, INFINITY);
-                            if (transmissive && (lobe == GBPT_LOBE_GLASS_REFRACT || lobe == GBPT_LOBE_DIFFUSE_TRANSMISSION))
-                                next_medium = md.inside ? -1 : mat;
                         }
                     }
                 }
@@ -771,7 +772,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             next.last_prim[ni] = prim;
             next.slot[ni] = slot;
             pb.throughput[slot] = f4(tp, 0.0f);
-            if (PRINCIPLED) pb.medium[slot] = next_medium;
+            if (PRINCIPLED) vol.store(pb.vol_stack, pb.vol_state, slot);
             if (pb.guide_pdf) pb.guide_pdf[slot] = guide_pdf_out;
         }
         if (gv.train_entry)  // uniform: every lane of the warp takes the branch
@@ -1104,7 +1105,12 @@ __global__ void __launch_bounds__(256) camera_batch_kernel(const BatchJob* __res
             q.slot[qi] = (int32_t)slot;
             pb.throughput[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
             pb.radiance[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (pb.medium) pb.medium[slot] = -1;
+            if (pb.vol_stack)
+        {
+            VolumeStack v;
+            v.reset();
+            v.store(pb.vol_stack, pb.vol_state, slot);
+        }
             pb.job[slot] = job;
             store_rng(pb.rng + slot, rng);
         }

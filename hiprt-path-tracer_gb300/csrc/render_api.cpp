@@ -755,7 +755,8 @@ void alloc_paths(DevMem& M, int64_t cap, bool principled, bool batched, gbpt::Pa
     pb.pending_bsdf = M.alloc<float4>(cap);
     pb.shadow_entry = M.alloc<int32_t>(cap);
     pb.bsdf_entry = M.alloc<int32_t>(cap);
-    pb.medium = principled ? M.alloc<int32_t>(cap) : nullptr;
+    pb.vol_stack = principled ? M.alloc<uint4>(cap) : nullptr;
+    pb.vol_state = principled ? M.alloc<int4>(cap) : nullptr;
     pb.job = batched ? M.alloc<int32_t>(cap) : nullptr;
     pb.ris = M.alloc<float4>(cap);
     q[0] = make_queue(M, cap, true, false);

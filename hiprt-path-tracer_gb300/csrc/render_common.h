@@ -91,7 +91,8 @@ struct PathBuffers
     float4* pending_bsdf;   // rgb = throughput * f * cos / pdf, w = BSDF pdf
     int32_t* shadow_entry;  // queue index of the slot's shadow ray this bounce, -1 if none
     int32_t* bsdf_entry;    // queue index of the slot's BSDF-light ray this bounce, -1 if none
-    int32_t* medium;        // material index of the volume the path travels in, -1 = air
+    uint4* vol_stack;       // principled paths: the nested-dielectric stack (volume.h), 4 entries
+    int4* vol_state;        // its incident / outgoing materials, position | inside << 8, distance
     int32_t* job;           // batched rendering: the job of each slot (null for a single renderer)
     float4* ris;            // RIS vertex: throughput before the continuation (rgb) and the light
                             // candidates' weight sum (w); w = -0.5: RIS without light candidates,

@@ -256,10 +256,10 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuf
         const V3 view = -d;
         fix_backfacing(view, ng, ns);
         const int mat = __ldg(s.material_of + prim);
-        const gbpt_principled_material& pm = s.pmats[mat];
-        const bool transmissive =
-            (pm.specular_transmission > 0.0f || pm.diffuse_transmission > 0.0f) && pm.thin_walled == 0;
-        const bool inside = transmissive && dot(view, ng_raw) < 0.0f;
+        // the camera hit's volume state as the reference rebuilds it from the G-buffer
+        // (RayVolumeState::reconstruct_first_hit, ReSTIR/Surface.h:31): the material pushed on a
+        // stack holding only the air, so the ray enters it (camera in the air)
+        const bool inside = false;
         gb.pos[pixel] = f4(P, __int_as_float(prim));
         gb.ns[pixel] = f4(ns, __int_as_float(mat));
         gb.ng[pixel] = f4(ng, __int_as_float(inside ? 1 : 0));

@@ -323,6 +323,162 @@ void bsdf_seed_done(Pcg& rng, const float* out8)
     rng.state = st;
 }
 
+// The reference's nested-dielectric volume state (RayVolumeState, src/Device/includes/RayVolumeState.h:20-80,
+// with the NestedDielectricsInteriorStack of src/Device/includes/NestedDielectrics.h:119-258, Schmidt
+// 2002): 4 stack entries packed as priority (4 bits) | topmost << 4 | odd parity << 5 | material << 6,
+// entry 0 being the air (material 0x3FFFFFF, priority 0); a push per hit finds the last entered
+// material and whether the hit enters or leaves its own material (parity), the BSDF pops it again.
+struct VolState
+{
+    static constexpr int kSize = 4;
+    static constexpr uint32_t kMaxMat = 0x3FFFFFFu;
+    uint32_t e[kSize];
+    int pos = 0;
+    int incident = -1, outgoing = -1;
+    bool inside = false;
+    float distance = 0.0f;
+    VolState()
+    {
+        for (int i = 0; i < kSize; i++) e[i] = (kMaxMat << 6) | (1u << 5) | (1u << 4);
+    }
+    static int mat(uint32_t x) { return (int)((x >> 6) & kMaxMat); }
+    static bool topmost(uint32_t x) { return (x >> 4) & 1u; }
+    static bool odd(uint32_t x) { return (x >> 5) & 1u; }
+    static int prio(uint32_t x) { return (int)(x & 15u); }
+    // returns true when the boundary is skipped (a lower-priority material inside a higher one)
+    bool push(int m, int priority)
+    {
+        if (pos == kSize - 1) return false;
+        int last;
+        for (last = pos; last >= 0; last--)
+            if (mat(e[last]) != m && topmost(e[last]) && odd(e[last])) break;
+        bool par = true;
+        for (int prev = pos; prev >= 0; prev--)
+            if (mat(e[prev]) == m)
+            {
+                e[prev] &= ~(1u << 4);
+                par = !odd(e[prev]);
+                break;
+            }
+        inside = !par;
+        if (pos < kSize - 1) pos++;
+        e[pos] = ((uint32_t)(m & (int)kMaxMat) << 6) | ((par ? 1u : 0u) << 5) | (1u << 4) | ((uint32_t)priority & 15u);
+        if (priority < prio(e[last])) return true;
+        if (par)
+        {
+            incident = mat(e[last]);
+            outgoing = m;
+        }
+        else
+        {
+            incident = m;
+            outgoing = mat(e[last]);
+        }
+        return false;
+    }
+    void pop(bool in)
+    {
+        const int top = mat(e[pos]);
+        if (pos > 0) pos--;
+        if (in)
+        {
+            int prev;
+            for (prev = pos; prev >= 0; prev--)
+                if (mat(e[prev]) == top) break;
+            if (prev >= 0)
+                for (int i = prev + 1; i <= pos; i++) e[i - 1] = e[i];
+            if (pos > 0) pos--;
+        }
+        for (int i = pos; i >= 0; i--)
+            if (mat(e[i]) == top)
+            {
+                e[i] |= 1u << 4;
+                break;
+            }
+    }
+};
+
+// The dielectric priority the reference's material packing gives (CPUMaterial::make_safe,
+// MaterialCPU.h:200-212, then the unsigned-char field): 255 (stored as 15 in a stack entry) for a
+// material without transmission, else the material's own priority (0 by default).
+int dielectric_priority(const float* m) { return (m[38] == 0.0f && m[39] == 0.0f) ? 255 : 0; }
+
+// IOR of a stack entry's material (1 for the air entry)
+float vol_ior(const PScene& ps, int mat) { return (mat < 0 || mat == (int)VolState::kMaxMat) ? 1.0f : ps.mat(mat)[37]; }
+
+// principled_beer_absorption (Principled.h:332-357): attenuation over the distance travelled in the
+// volume being left (the incident entry), 1 when its absorption colour is white
+V vol_beer(const PScene& ps, const VolState& vs)
+{
+    if (vs.incident < 0 || vs.incident == (int)VolState::kMaxMat) return mk(1, 1, 1);
+    const float* m = ps.mat(vs.incident);
+    if (m[40] == 1.0f && m[41] == 1.0f && m[42] == 1.0f) return mk(1, 1, 1);
+    const float d = std::max(vs.distance, 1.0e-6f);
+    return mk(std::exp(std::log(m[40]) / m[43] * d), std::exp(std::log(m[41]) / m[43] * d),
+              std::exp(std::log(m[42]) / m[43] * d));
+}
+
+// MaterialUtils::get_thin_walled_roughness
+float thin_rough(bool thin, float r, float eta)
+{
+    if (!thin) return r;
+    const float x = r * std::sqrt(3.7f * (eta - 1.0f) * (eta - 0.5f) * (eta - 0.5f) / (eta * eta * eta));
+    return std::min(std::max(x / 1.39f, 0.0f), 1.0f);
+}
+
+// The volume-stack updates of a continuation sample (the BSDF sample with update_ray_volume_state):
+// a reflective lobe pops (principled_bsdf_sample, Principled.h:1851-1857), so does a glass
+// reflection or a thin-walled refraction (principled_glass_sample, :793, :821); then the evaluation
+// of the sampled direction pops when it refracts out of a volume through the glass lobe
+// (principled_glass_eval, :536-556, past its early exits) or the diffuse transmission lobe
+// (:844-860), and restarts the travelled distance. Returns false when the sample was rejected
+// below the surface before its evaluation.
+bool vol_after_sample(const PScene& ps, VolState& vs, const float* m, V view, V ns, V ng, V wi, int lobe)
+{
+    int32_t thin_i;
+    std::memcpy(&thin_i, m + 44, 4);
+    const bool thin = thin_i != 0;
+    const bool through = lobe == 32 || lobe == 64 || lobe == 256;
+    if (!through) vs.pop(false);
+    if (lobe == 32 || (lobe == 64 && thin)) vs.pop(false);
+    if (dot(wi, ng) < 0.0f && !through) return false;
+    const bool outside = !vs.inside;
+    const float metallic = m[7], trans = m[38], dt = m[39];
+    const float w_glass = outside ? (1.0f - metallic) * (1.0f - dt) * trans : (1.0f - dt);
+    const float w_dt = outside ? (1.0f - metallic) * dt : dt;
+    const float nov = dot(view, ns), nol = dot(wi, ns);
+    if (w_glass > 0.0f && std::fabs(nol) >= 1.0e-8f && !(nol * nov > 0.0f))
+    {
+        float eta = vol_ior(ps, vs.outgoing) / vol_ior(ps, vs.incident);
+        if (std::fabs(eta - 1.0f) < 1.0e-5f) eta = 1.0f + 1.0e-5f;
+        const float rough = thin_rough(thin, m[3], eta);
+        V h;
+        if (rough <= 1.0e-4f)
+            h = ns;
+        else if (thin)
+            h = nrm((wi - ns * (2.0f * nol)) + view);
+        else
+            h = nrm(wi * eta + view);
+        if (dot(h, ns) < 0.0f) h = neg(h);
+        if (!(dot(wi, h) * nol < 0.0f || dot(view, h) * nov < 0.0f))
+        {
+            if (thin)
+                vs.pop(vs.inside);
+            else if (vs.incident != (int)VolState::kMaxMat)
+            {
+                vs.distance = 0.0f;
+                if (vs.inside) vs.pop(vs.inside);
+            }
+        }
+    }
+    if (w_dt > 0.0f && nol < 0.0f && !(nov * nol > 0.0f) && vs.incident != (int)VolState::kMaxMat)
+    {
+        vs.distance = 0.0f;
+        if (vs.inside) vs.pop(vs.inside);
+    }
+    return true;
+}
+
 // Octahedral24BitNormalPadded32b pack + unpack (src/HostDeviceCommon/Packing.h:237-367; Cigolle et
 // al. 2014): octahedral projection, two 12-bit snorms in three bytes, decode and normalise.
 float sign_nz(float k) { return k >= 0.0f ? 1.0f : -1.0f; }

@@ -619,12 +619,33 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
     V pw = mat_point(st.iv, pv);
     V d = nrm(pw - o);
     int skip = -1;
-    int medium = -1;
+    VolState vs;
     V tp = mk(1, 1, 1), L = mk(0, 0, 0);
     for (int bounce = 0; bounce <= st.nb_bounces; bounce++)
     {
         float t;
-        int prim = closest(s, o, d, skip, t);
+        int prim;
+        // trace_main_path_ray (Intersect.h:200-270): every hit pushes its material on the volume
+        // stack (distance travelled inside a volume accumulated), a skipped boundary (a lower
+        // priority material inside a higher one) is passed through; at the camera hit the stack
+        // restarts from the air (RayVolumeState::reconstruct_first_hit, Megakernel.h:78-82)
+        for (;;)
+        {
+            prim = closest(s, o, d, skip, t);
+            if (prim < 0) break;
+            const int pm = s.mat_of[prim];
+            if (bounce == 0)
+            {
+                vs = VolState();
+                vs.push(pm, dielectric_priority(ps.mat(pm)));
+                break;
+            }
+            const bool skipped = vs.push(pm, dielectric_priority(ps.mat(pm)));
+            if (vs.inside) vs.distance += t;
+            if (!skipped) break;
+            o = o + d * t;
+            vs.distance += t;
+        }
         if (prim < 0)
         {
             L = L + env_miss(st.env, d, bounce, tp);
@@ -648,12 +669,13 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
         // the fetch's coat roughening (CameraRays.h:183, Megakernel.h:72)
         const float* m = (st.rng_mode && bounce == 0 && st.gbuffer_materials) ? ps.mat(mi + st.gbuffer_materials) : ps.mat(mi);
         if (bounce == 0) L = L + s.emi(prim);
-        int32_t thin;
-        std::memcpy(&thin, m + 44, 4);
-        const bool transmissive = (m[38] > 0.0f || m[39] > 0.0f) && thin == 0;
-        const bool inside = transmissive && dot(view, ng_raw) < 0.0f;
-        const float eta_i = inside ? m[37] : (medium >= 0 ? ps.mat(medium)[37] : 1.0f);
-        const float eta_o = inside ? 1.0f : m[37];
+        const bool inside = vs.inside;
+        const float eta_i = vol_ior(ps, vs.incident), eta_o = vol_ior(ps, vs.outgoing);
+        // Beer-Lambert attenuation of a refraction out of a volume (principled_glass_eval and
+        // principled_diffuse_transmission_eval apply it to refracted directions)
+        const V beer = vol_beer(ps, vs);
+        const float nov_b = dot(view, ns);
+        auto refr = [&](V wi, V f) { return (nov_b * dot(wi, ns) <= 0.0f) ? f * beer : f; };
         float q[16], out[8];
         // envmap direct lighting first, as on the GPU
         EnvDirectO ed;
@@ -665,7 +687,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                     make_query(qq, view, ns, ng, wi, eta_i, eta_o, inside, 0);
                     ps.eval(m, qq, oo);
                     pb = oo[3];
-                    return mk(oo[0], oo[1], oo[2]);
+                    return refr(wi, mk(oo[0], oo[1], oo[2]));
                 },
                 [&](V& wi, float& pdf) {
                     float qq[16], oo[8];
@@ -675,7 +697,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                     bsdf_seed_done(rng, oo);
                     wi = mk(oo[0], oo[1], oo[2]);
                     pdf = oo[6];
-                    return mk(oo[3], oo[4], oo[5]);
+                    return refr(wi, mk(oo[3], oo[4], oo[5]));
                 });
         Ris ris;
         const V tp0 = tp;
@@ -688,7 +710,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                            make_query(qq, view, ns, ng, wi, eta_i, eta_o, inside, 0);
                            ps.eval(m, qq, oo);
                            pb = oo[3];
-                           return mk(oo[0], oo[1], oo[2]);
+                           return refr(wi, mk(oo[0], oo[1], oo[2]));
                        },
                        ris);
             if (st.ris_n > 0)
@@ -697,7 +719,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                 int32_t lobe;
                 ps.sample(m, q, bsdf_seed(rng), out, &lobe);
             bsdf_seed_done(rng, out);
-                ris_bsdf(s, st, P, ns, prim, mk(out[0], out[1], out[2]), mk(out[3], out[4], out[5]), out[6], st.ris_n, ris);
+                ris_bsdf(s, st, P, ns, prim, mk(out[0], out[1], out[2]), refr(mk(out[0], out[1], out[2]), mk(out[3], out[4], out[5])), out[6], st.ris_n, ris);
             }
         }
         else if (s.ne > 0 && can_light_sample(m))
@@ -737,7 +759,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                     {
                         float lpdf = a2s(pa, dist, cl);
                         float mis = balance(lpdf, bp);
-                        V f = mk(out[0], out[1], out[2]);
+                        V f = refr(wi, mk(out[0], out[1], out[2]));
                         V c = tp * (f * std::fabs(dot(ns, wi)) * Le * mis / lpdf);
                         if (!black(c) && !occluded(s, P, wi, prim, dist - 1.0e-4f)) L = L + c;
                     }
@@ -755,7 +777,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
             V wi = mk(out[0], out[1], out[2]);
             if (pdf > 0.0f && s.ne > 0)
             {
-                V f = mk(out[3], out[4], out[5]);
+                V f = refr(wi, mk(out[3], out[4], out[5]));
                 V w = tp * (f * std::fabs(dot(ns, wi)) / pdf);
                 float th;
                 int lp = closest(s, P, wi, prim, th);
@@ -787,7 +809,8 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
             const float pdf = out[6];
             if (pdf <= 0.0f) return false;
             V wi = mk(out[0], out[1], out[2]);
-            V f = mk(out[3], out[4], out[5]);
+            V f = refr(wi, mk(out[3], out[4], out[5]));
+            if (!vol_after_sample(ps, vs, m, view, ns, ng, wi, lobe)) return false;
             V att = f * std::fabs(dot(wi, ns)) / pdf;
             if (st.do_rr && bounce >= st.rr_min)
             {
@@ -799,7 +822,6 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
             }
             tp = tp * att;
             tp = mk(std::max(tp.x, 1.0e-5f), std::max(tp.y, 1.0e-5f), std::max(tp.z, 1.0e-5f));
-            if (transmissive && (lobe == 64 || lobe == 256)) medium = inside ? -1 : mi;
             o = P;
             d = wi;
             skip = prim;

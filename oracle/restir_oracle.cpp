@@ -746,11 +746,9 @@ void orc_restir_gbuffer(const float* tri_verts, int n_tris, const int* mat_of, c
             ns = nrm(view + refl);
         }
         const int mi = mat_of[prim];
-        const float* m = pmats + 64 * (size_t)mi;
-        int32_t thin;
-        std::memcpy(&thin, m + 44, 4);
-        const bool transmissive = (m[38] > 0.0f || m[39] > 0.0f) && thin == 0;
-        int32_t inside = transmissive && dot(view, ng_raw) < 0.0f ? 1 : 0;
+        // the camera hit enters its material from the air: the reference rebuilds the surface's
+        // volume state by pushing the hit material on a fresh stack (ReSTIR/Surface.h:31)
+        int32_t inside = 0;
         g[0] = P.x; g[1] = P.y; g[2] = P.z;
         g[4] = ns.x; g[5] = ns.y; g[6] = ns.z;
         int32_t mb = mi;

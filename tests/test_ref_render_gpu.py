@@ -65,16 +65,18 @@ def test_lambert_cornell_matches_reference_megakernel(cuda):
     assert abs(gpu.mean() - ref.mean()) <= 2e-3 * ref.mean(), (gpu.mean(), ref.mean())
 
 
-def test_principled_cornell_matches_reference_megakernel(cuda):
-    """Coated, glossy dielectric, anisotropic metal, metallic-blend and mirror materials, power
-    light sampling, against the reference's MegaKernel with its own principled BSDF."""
+@pytest.mark.parametrize("name", ["principled", "principled_glass"])
+def test_principled_cornell_matches_reference_megakernel(cuda, name):
+    """Coated, glossy dielectric, anisotropic metal, metallic-blend and mirror materials (and a
+    rough glass box entered and left through the nested-dielectric volume stack), power light
+    sampling, against the reference's MegaKernel with its own principled BSDF."""
     g = np.load(GOLDEN)
-    scene = gbpt.Scene(g["positions"], g["indices"], g["principled_material_of"], principled=g["principled_materials"],
+    scene = gbpt.Scene(g["positions"], g["indices"], g[f"{name}_material_of"], principled=g[f"{name}_materials"],
                        material_packing=MATERIALS_PACKED)
     lt = scene.light_table()
-    assert abs(lt["power_sum"] - float(g["principled_power_sum"])) <= 1e-6 * lt["power_sum"]
+    assert abs(lt["power_sum"] - float(g[f"{name}_power_sum"])) <= 1e-6 * lt["power_sum"]
     gpu = _frames(scene, _settings(g, BSDF_PRINCIPLED, LIGHT_POWER), int(g["frames"]))
-    ref = g["principled"]
+    ref = g[name]
     frac = _agreement(gpu, ref)
     assert frac.min() >= 0.97, frac
     assert abs(gpu.mean() - ref.mean()) <= 5e-3 * ref.mean(), (gpu.mean(), ref.mean())

@@ -122,16 +122,19 @@ def test_alias_restatement_matches_reference_utils():
 
 
 @REF
-def test_principled_oracle_matches_reference_megakernel_frames():
+@pytest.mark.parametrize("name", ["principled", "principled_glass"])
+def test_principled_oracle_matches_reference_megakernel_frames(name):
     """The restated estimator with the reference's own BSDF (through callbacks that hand back the
-    generator's state) on the principled Cornell box without transmissive objects."""
+    generator's state) on the principled Cornell box, with and without a rough glass box whose
+    faces wind inwards: only the restated nested-dielectric stack (volume parity, not face
+    orientation) enters and leaves it as the reference does."""
     g = _golden()
-    raw = g["principled_materials"]
+    raw = g[f"{name}_materials"]
     q = pyoracle.ref_pack_unpack_material(raw)
     eff = M.pack_many([M.coat_roughened(M.unpack(q[i])) for i in range(len(q))])
     pm = np.concatenate([eff, pyoracle.ref_pack_unpack_material(eff)])
     emission = raw[:, 4:7]
-    mo = g["principled_material_of"]
+    mo = g[f"{name}_material_of"]
     emissive = np.nonzero(np.any(emission[mo] != 0, axis=1))[0].astype(np.int32)
     r = pyoracle.RefRender("principled", "power", g["positions"], g["indices"], mo, raw)
     lt = r.light_table()
@@ -141,6 +144,6 @@ def test_principled_oracle_matches_reference_megakernel_frames():
         st.random_number = int(rn)
         img = pyoracle.pt_render_principled(_soup(g), mo, pm, emission, emissive, lt["probas"], lt["alias"],
                                             lt["power_sum"], st, 1, iteration_base=k)
-        ref = g["principled"][k]
+        ref = g[name][k]
         rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3)
         assert (rel.max(axis=-1) < 1e-4).mean() > 0.995, k
