@@ -139,16 +139,35 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def kernel_source_hash():
+    """SHA-256 (16 hex digits) of the CUDA and C++ sources of libgbpt, in file-name order."""
+    import hashlib
+    csrc = os.path.join(REPO, "hiprt-path-tracer_gb300", "csrc")
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(csrc)):
+        if name.endswith((".cu", ".h", ".cpp")):
+            h.update(name.encode())
+            with open(os.path.join(csrc, name), "rb") as f:
+                h.update(f.read())
+    return h.hexdigest()[:16]
+
+
 def ncu_traffic():
-    """DRAM bytes per closest-hit ray from the committed ncu summary, if present."""
+    """DRAM bytes per closest-hit ray from the committed ncu summary of the closest-hit kernels,
+    used only when that capture was taken of these very sources (its source_hash line matches),
+    else None: a capture of another build says nothing about this one."""
     path = os.path.join(REPO, "profiles", "trace_closest_traffic.txt")
+    vals = {}
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_ray="):
-                return float(line.split("=")[1])
+            if "=" in line and not line.startswith("#"):
+                k, v = line.strip().split("=", 1)
+                vals[k] = v
     except OSError:
-        pass
-    return None
+        return None
+    if vals.get("source_hash") != kernel_source_hash() or "dram_bytes_per_ray" not in vals:
+        return None
+    return float(vals["dram_bytes_per_ray"])
 
 
 def make_cpu_impl(mesh, log=print):
@@ -605,10 +624,9 @@ def run_reference(args, rank, world):
         return
     mesh, primary = build_workload(log=lambda *a: print(*a, file=sys.stderr))
     impl = make_cpu_impl(mesh, log=lambda *a: print(*a, file=sys.stderr))
-    # primary hits for the secondary rays come from the CPU structure itself on this arm
-    sl = slice(0, None, 8)
-    sub = primary.slice(sl)
-    bounce, shadow = secondary_rays(mesh, sub, impl[0](sub))
+    # the secondary rays are derived as on the GPU arm, from the hits of every primary ray (here
+    # found by the CPU traversal itself: the same hits, bit for bit, but for exact ties)
+    bounce, shadow = secondary_rays(mesh, primary, impl[0](primary))
     frac = args.ref_fraction
     for _ in range(args.warmup):
         cpu_baseline_sample(impl, primary, bounce, shadow, frac / 4)
@@ -636,7 +654,8 @@ def main():
     ap.add_argument("--impl", default="gbpt", choices=["gbpt", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-fraction", type=float, default=0.5)
-    ap.add_argument("--ref-fraction", type=float, default=1.0 / 256)
+    ap.add_argument("--ref-fraction", type=float, default=1.0 / 16,
+                    help="reference arm: fraction of each ray class timed per step (1/16: 1,048,576 rays)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the path-tracing workloads")
     ap.add_argument("--restir-res", default="1920x1080",

@@ -155,6 +155,11 @@ gbpt_status gbpt_bvh_get_stats(const gbpt_bvh* bvh, gbpt_bvh_stats* out)
 gbpt_status gbpt_bvh_destroy(gbpt_bvh* bvh)
 {
     if (!bvh) return GBPT_OK;
+    HostTraceStaging& h = bvh->staging;
+    if (h.buf) cudaFree(h.buf);
+    if (h.side) cudaStreamDestroy(h.side);
+    if (h.start) cudaEventDestroy(h.start);
+    if (h.side_done) cudaEventDestroy(h.side_done);
     cudaError_t e1 = cudaFree(const_cast<void*>(bvh->dev.nodes));
     cudaError_t e2 = cudaFree(const_cast<void*>(bvh->dev.tris));
     delete bvh;
@@ -198,6 +203,11 @@ gbpt_status gbpt_trace_count(const gbpt_bvh* bvh, const float* origin_tmin, cons
     return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "counting launch");
 }
 
+// Host-buffer trace: the batch is cut into chunks issued alternately on the caller's stream and a
+// side stream; each chunk copies its rays in, traces and copies its results out, so that one
+// chunk's copies overlap the other stream's traversal (the copy engines run beside the SMs; with
+// pinned host buffers the copies are asynchronous). The device staging is kept with the BVH and
+// reused. Results do not depend on the chunking: every ray is traced on its own.
 static gbpt_status trace_host(const gbpt_bvh* bvh, const float* origin_tmin, const float* dir_tmax,
                               const int32_t* last_prim, int64_t n, void* out, bool any_hit, cudaStream_t st)
 {
@@ -206,25 +216,59 @@ static gbpt_status trace_host(const gbpt_bvh* bvh, const float* origin_tmin, con
     if (n > 0 && !out) return fail(GBPT_ERROR_INVALID_ARG, "output is NULL");
     if (n == 0) return GBPT_OK;
     const size_t ray_bytes = (size_t)n * 16;
-    const size_t out_bytes = any_hit ? (size_t)n : (size_t)n * 16;
-    char* buf = nullptr;
+    const size_t out_stride = any_hit ? 1 : 16;
     const size_t lp_off = 2 * ray_bytes;
     const size_t out_off = lp_off + (((size_t)n * 4 + 255) & ~(size_t)255);
-    cudaError_t e = cudaMallocAsync((void**)&buf, out_off + out_bytes, st);
-    if (e != cudaSuccess) return cuda_fail(e, "scratch allocation");
-    float* d_o = (float*)buf;
-    float* d_d = (float*)(buf + ray_bytes);
-    int32_t* d_lp = last_prim ? (int32_t*)(buf + lp_off) : nullptr;
-    void* d_out = buf + out_off;
-    e = cudaMemcpyAsync(d_o, origin_tmin, ray_bytes, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_d, dir_tmax, ray_bytes, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && d_lp) e = cudaMemcpyAsync(d_lp, last_prim, (size_t)n * 4, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-        e = gbpt::launch_trace(bvh->dev, d_o, d_d, d_lp, n, any_hit ? nullptr : (float*)d_out,
-                               any_hit ? (uint8_t*)d_out : nullptr, any_hit, nullptr, st, &bvh->cfg[any_hit ? 1 : 0]);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, st);
-    cudaError_t ef = cudaFreeAsync(buf, st);
-    if (e == cudaSuccess) e = ef;
+    const size_t need = out_off + (size_t)n * out_stride;
+
+    HostTraceStaging& h = bvh->staging;
+    std::lock_guard<std::mutex> lock(h.mu);
+    cudaError_t e = cudaSuccess;
+    if (!h.side) e = cudaStreamCreateWithFlags(&h.side, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !h.start) e = cudaEventCreateWithFlags(&h.start, cudaEventDisableTiming);
+    if (e == cudaSuccess && !h.side_done) e = cudaEventCreateWithFlags(&h.side_done, cudaEventDisableTiming);
+    if (e == cudaSuccess && h.cap < need)
+    {
+        // the previous staging may still be read by work queued on the caller's stream
+        if (h.buf) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess && h.buf) e = cudaFree(h.buf);
+        h.buf = nullptr;
+        h.cap = 0;
+        if (e == cudaSuccess) e = cudaMalloc((void**)&h.buf, need);
+        if (e == cudaSuccess) h.cap = need;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "host-buffer trace staging");
+    float* d_o = (float*)h.buf;
+    float* d_d = (float*)(h.buf + ray_bytes);
+    int32_t* d_lp = last_prim ? (int32_t*)(h.buf + lp_off) : nullptr;
+    char* d_out = h.buf + out_off;
+
+    // the side stream starts after the caller's earlier work
+    e = cudaEventRecord(h.start, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h.side, h.start, 0);
+    const int64_t chunk = std::max<int64_t>((int64_t)1 << 20, (n + 7) / 8);
+    int c = 0;
+    for (int64_t b = 0; e == cudaSuccess && b < n; b += chunk, c++)
+    {
+        const int64_t m = std::min(chunk, n - b);
+        cudaStream_t cs = (c & 1) ? h.side : st;
+        e = cudaMemcpyAsync(d_o + 4 * b, origin_tmin + 4 * b, (size_t)m * 16, cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_d + 4 * b, dir_tmax + 4 * b, (size_t)m * 16, cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess && d_lp)
+            e = cudaMemcpyAsync(d_lp + b, last_prim + b, (size_t)m * 4, cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess)
+            e = gbpt::launch_trace(bvh->dev, d_o + 4 * b, d_d + 4 * b, d_lp ? d_lp + b : nullptr, m,
+                                   any_hit ? nullptr : (float*)(d_out + b * 16),
+                                   any_hit ? (uint8_t*)(d_out + b) : nullptr, any_hit, nullptr, cs,
+                                   &bvh->cfg[any_hit ? 1 : 0]);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync((char*)out + b * out_stride, d_out + b * out_stride, (size_t)m * out_stride,
+                                cudaMemcpyDeviceToHost, cs);
+    }
+    // the caller's stream ends after the side stream's chunks
+    cudaError_t er = cudaEventRecord(h.side_done, h.side);
+    if (er == cudaSuccess) er = cudaStreamWaitEvent(st, h.side_done, 0);
+    if (e == cudaSuccess) e = er;
     cudaError_t es = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = es;
     return e == cudaSuccess ? GBPT_OK : cuda_fail(e, "host-buffer trace");

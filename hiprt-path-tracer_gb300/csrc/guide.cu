@@ -104,10 +104,14 @@ __device__ __forceinline__ void publish_smem()
     umma::fence_after();
 }
 
-// all threads: wait for the MMAs committed to the mbarrier; false (on every thread) if it gave up
-__device__ __forceinline__ bool wait_mma(uint64_t* mbar, uint32_t& phase)
+// all threads: wait (at most 'limit' polls) for the MMAs committed to the mbarrier; false (on every
+// thread) if a thread gave up. A thread that gave up still waits, bounded by kWaitLimit, for that
+// phase to complete: the kernel then stops with no tensor-core work of its own in flight, so that
+// it can free the TMEM those MMAs write.
+__device__ __forceinline__ bool wait_mma(uint64_t* mbar, uint32_t& phase, int limit)
 {
-    const bool ok = umma::mbar_wait(mbar, phase, kWaitLimit);
+    const bool ok = umma::mbar_wait(mbar, phase, limit);
+    if (!ok) umma::mbar_wait(mbar, phase, kWaitLimit);
     phase ^= 1u;
     umma::fence_after();
     return __syncthreads_and(ok ? 1 : 0) != 0;
@@ -115,10 +119,10 @@ __device__ __forceinline__ bool wait_mma(uint64_t* mbar, uint32_t& phase)
 
 // issue (thread 0) + wait (all) one forward GEMM into F
 __device__ __forceinline__ bool run_gemm(uint64_t* mbar, uint32_t tmem, const bf16* A, const bf16* B, int N, int K,
-                                         uint32_t& phase)
+                                         uint32_t& phase, int limit)
 {
     if (threadIdx.x == 0) umma::gemm_commit(tmem + kColF, A, B, N, K, mbar);
-    return wait_mma(mbar, phase);
+    return wait_mma(mbar, phase, limit);
 }
 
 __device__ __forceinline__ void load_cols(uint32_t tmem, uint32_t col, int count, float* out)
@@ -194,14 +198,14 @@ __device__ bool forward_tile(uint64_t* mbar, uint32_t tmem, const bf16* w, bf16*
     float h[kHid];
     for (int l = 0; l < 3; l++)
     {
-        if (!run_gemm(mbar, tmem, act[l & 1], w + wf[l], kHid, kHid, phase)) return false;
+        if (!run_gemm(mbar, tmem, act[l & 1], w + wf[l], kHid, kHid, phase, net.wait_limit)) return false;
         load_cols(tmem, kColF, kHid, h);
         uint32_t scratch[2];
         relu(h, masks ? masks[l] : scratch);
         store_row(act[(l + 1) & 1], tr ? tr[l + 1] : nullptr, h, kHid);
         publish_smem();
     }
-    if (!run_gemm(mbar, tmem, act[1], w + kW4f, kOut, kHid, phase)) return false;
+    if (!run_gemm(mbar, tmem, act[1], w + kW4f, kOut, kHid, phase, net.wait_limit)) return false;
     load_cols(tmem, kColF, kOut, raw);
     return true;
 }
@@ -271,7 +275,7 @@ __global__ void __launch_bounds__(kTile) train_kernel(Net net, Batch b, const fl
                 umma::gemm_issue(tmem + col_dw(l), sm.tr[l], sm.gt[cur], n_out, kTile, !first);
                 umma::commit(&sm.mbar);
             }
-            ok = wait_mma(&sm.mbar, phase);
+            ok = wait_mma(&sm.mbar, phase, net.wait_limit);
             if (!ok) break;
             if (l > 0)
             {

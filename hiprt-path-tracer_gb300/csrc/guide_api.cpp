@@ -38,6 +38,7 @@ G::Net net_of(const gbpt_guide* g)
     n.params = g->params;
     n.packed = g->packed;
     n.grid_bf16 = g->grid_bf16;
+    n.wait_limit = g->p.wait_limit > 0 ? g->p.wait_limit : (g->p.wait_limit == 0 ? (1 << 24) : 0);
     for (int a = 0; a < 3; a++)
     {
         n.lo[a] = g->p.scene_min[a];

@@ -29,6 +29,7 @@ struct Net
     const uint16_t* packed;     // BF16 kernel copies of the weights (kPackedWeights)
     const uint32_t* grid_bf16;  // BF16 copy of the grid, both features of an entry in one word
     float lo[3], inv_ext[3];    // hash-grid domain
+    int wait_limit;             // polls of each tensor-core wait before it gives up (<= 0: none)
 };
 
 // A batch of rows: SoA position / normal / view / direction (3 floats per row), weight and BSDF

@@ -27,7 +27,7 @@ WEIGHTS = 3 * HIDDEN * HIDDEN + HIDDEN * OUT
 class GuideParams(ctypes.Structure):
     _fields_ = [("scene_min", ctypes.c_float * 3), ("scene_max", ctypes.c_float * 3), ("learning_rate", ctypes.c_float),
                 ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("epsilon", ctypes.c_float), ("seed", u32),
-                ("max_batch", i32), ("reserved", i32 * 6)]
+                ("max_batch", i32), ("wait_limit", i32), ("reserved", i32 * 5)]
 
 
 GUIDE_SIGNATURES = [

@@ -49,7 +49,13 @@ typedef struct gbpt_guide_params {
     float beta1, beta2, epsilon;      /* default 0.9, 0.99, 1e-8 */
     uint32_t seed;                    /* initialisation */
     int32_t max_batch;                /* largest training batch, default 1 << 18 */
-    int32_t reserved[6];
+    /* Polls of each bounded tensor-core completion wait before it gives up: > 0 that many, 0 the
+     * default (2^24), < 0 none at all. A wait that gives up lets the kernel's issued tensor-core
+     * work finish (a second bounded wait), frees its TMEM, stops the kernel early and raises the
+     * error flag (the call returns GBPT_ERROR_TIMEOUT); the device context stays usable. A
+     * negative value makes every wait give up at once: the test of that path. */
+    int32_t wait_limit;
+    int32_t reserved[5];
 } gbpt_guide_params;
 
 GBPT_API gbpt_status gbpt_guide_default_params(gbpt_guide_params* p);

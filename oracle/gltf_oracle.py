@@ -18,8 +18,8 @@ COLOR_EMISSIVE, the KHR_materials_* extensions -> their keys, present only when 
 is). Triangles are kept in node traversal order (depth first, children in file order); ASSIMP's
 pre-transform step regroups meshes by material, which changes triangle order but no triangle.
 
-Parity pinned against: the reference's own sample scenes (data/GLTFs/*.gltf, parsed here from
-/root/reference when it exists) and synthetic files exercising every branch.
+Parity pinned against: the reference's own sample scenes (data/GLTFs/*.gltf of the reference tree
+named by GBPT_REFERENCE_ROOT, when it is set) and synthetic files exercising every branch.
 """
 from __future__ import annotations
 

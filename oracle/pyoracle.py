@@ -29,13 +29,25 @@ _c_u8 = ctypes.POINTER(ctypes.c_uint8)
 _i64 = ctypes.c_int64
 
 
+def reference_root() -> str | None:
+    """The reference tree, from the GBPT_REFERENCE_ROOT environment variable (None when unset or
+    not a reference tree). The only place the test infrastructure learns where it lies."""
+    root = os.environ.get("GBPT_REFERENCE_ROOT")
+    if root and os.path.isdir(os.path.join(root, "src", "Renderer")):
+        return root
+    return None
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile the restatement (always) and the reference build (when its sources exist)."""
+    """Compile the restatement (always) and the reference build (when the reference tree is given
+    by GBPT_REFERENCE_ROOT; otherwise reference libraries built earlier in oracle/_ref stay)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    ref_root = os.environ.get("GBPT_REFERENCE_ROOT", "/root/reference")
+    ref_root = reference_root()
     if ref is None:
-        ref = os.path.isdir(os.path.join(ref_root, "src", "Renderer"))
+        ref = ref_root is not None
     if ref:
+        if ref_root is None:
+            raise RuntimeError("the reference build needs GBPT_REFERENCE_ROOT to name the reference tree")
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={ref_root}"])
 
 

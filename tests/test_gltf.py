@@ -22,7 +22,9 @@ sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 import gltf_oracle  # noqa: E402
 from gltf_writer import GltfBuilder  # noqa: E402
 
-REFERENCE_SCENES = "/root/reference/data/GLTFs"
+import pyoracle  # noqa: E402
+
+REFERENCE_SCENES = os.path.join(pyoracle.reference_root() or "", "data", "GLTFs")
 
 
 def _quat(axis, deg):

@@ -195,3 +195,25 @@ def test_empty_batch_and_bad_arguments(cuda):
     with pytest.raises(GbptError):
         g.train(_t(P), _t(N), _t(V), _t(D), _t(wt))  # above max_batch
     assert g.error_flag() == 0
+
+
+def test_bounded_wait_gives_up_reports_and_leaves_the_device_usable(cuda):
+    """Failure detection without a GPU fault: a guide whose tensor-core waits are told to give up
+    at once (wait_limit < 0) stops its kernels early after letting their issued MMAs finish and
+    freeing their TMEM, raises the error flag, and its calls return GBPT_ERROR_TIMEOUT instead of
+    hanging; the same process then trains and infers normally with a default guide."""
+    from gbpt import GbptError
+    P, N, V, D, wt, pb = G.random_batch(1024, 3)
+    bad = _guide(seed=5, wait_limit=-1)
+    with pytest.raises(GbptError) as e:
+        bad.gradients(_t(P), _t(N), _t(V), _t(D), _t(wt), _t(pb))
+    assert e.value.status == 4  # GBPT_ERROR_TIMEOUT
+    assert bad.error_flag() == 1
+    with pytest.raises(GbptError):
+        bad.train(_t(P), _t(N), _t(V), _t(D), _t(wt), _t(pb))
+    bad.close()
+    good = _guide(seed=5)
+    loss = good.train(_t(P), _t(N), _t(V), _t(D), _t(wt), _t(pb))
+    rows = good.infer(_t(P), _t(N), _t(V)).cpu().numpy()
+    assert np.isfinite(loss) and np.isfinite(rows).all()
+    assert good.error_flag() == 0
