@@ -793,6 +793,38 @@ def main():
     value = world * n_rays / (ms_step * 1e-3) / 1e6
     clocks = sampler.summary(t_wall0, t_wall1)
 
+    # the production (watertight) triangle test on the same batch and launch configurations: its
+    # throughput (outside the timed region, a few steps) and how its closest hits differ from the
+    # parity test's, classified (gbpt.trace.classify_hit_differences)
+    wcfg = [dict(c, triangle_test=1) for c in (cfg_p, cfg_b, cfg_s)]
+    hits_pw = torch.empty_like(hits_p)
+    hits_bw = torch.empty_like(hits_b)
+    occ_sw = torch.empty_like(occ_s)
+
+    def wt_step():
+        bvh.closest_cfg(*P, out=hits_pw, **wcfg[0])
+        bvh.closest_cfg(*B, out=hits_bw, **wcfg[1])
+        bvh.occluded_cfg(*S, out=occ_sw, **wcfg[2])
+
+    for _ in range(2):
+        wt_step()
+    w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0.record(stream)
+    for _ in range(5):
+        wt_step()
+    w1.record(stream)
+    torch.cuda.synchronize()
+    wt_ms = w0.elapsed_time(w1) / 5
+    from gbpt.trace import classify_hit_differences
+    hp_np, hb_np = hits_p.cpu().numpy(), hits_b.cpu().numpy()
+    dif_p = classify_hit_differences(mesh, hp_np, hits_pw.cpu().numpy())
+    dif_b = classify_hit_differences(mesh, hb_np, hits_bw.cpu().numpy())
+    occ_diff = int((occ_s != occ_sw).sum().item())
+    watertight = {"mrays_s": world * n_rays / (wt_ms * 1e-3) / 1e6, "ms_per_step": wt_ms,
+                  "vs_moller_trumbore_primary": dict(zip(("agree", "edge", "tie", "other"), dif_p)),
+                  "vs_moller_trumbore_bounce": dict(zip(("agree", "edge", "tie", "other"), dif_b)),
+                  "shadow_decisions_differing": occ_diff}
+
     # end to end through the host-buffer C entry points (pinned host memory, copies in the call)
     hp = [torch.from_numpy(x).pin_memory() for x in (primary.origin_tmin, primary.dir_tmax, primary.last_prim)]
     hb = [torch.from_numpy(x).pin_memory() for x in (bounce.origin_tmin, bounce.dir_tmax, bounce.last_prim)]
@@ -848,6 +880,7 @@ def main():
         "e2e": {"value": world * n_rays / e2e_s / 1e6, "unit": UNIT,
                 "h2d_bytes_per_step": n_rays * RAY_IN_BYTES,
                 "d2h_bytes_per_step": (len(primary) + len(bounce)) * CLOSEST_OUT_BYTES + len(shadow) * ANY_OUT_BYTES},
+        "watertight": watertight,
         "gpu_launches": 3 * args.steps,
         "trace_configs": {"primary": cfg_p, "bounce": cfg_b, "shadow": cfg_s},
         "clocks": clocks,

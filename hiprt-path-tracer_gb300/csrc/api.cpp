@@ -297,6 +297,7 @@ gbpt::TraceConfig from_c(const gbpt_trace_config& c)
     t.postpone_below = c.postpone_below;
     t.blocks_per_sm = c.blocks_per_sm;
     t.shared_stack = c.shared_stack;
+    t.triangle_test = c.triangle_test;
     return t;
 }
 
@@ -310,6 +311,7 @@ gbpt_trace_config to_c(const gbpt::TraceConfig& t)
     c.postpone_below = t.postpone_below;
     c.blocks_per_sm = t.blocks_per_sm;
     c.shared_stack = t.shared_stack;
+    c.triangle_test = t.triangle_test;
     return c;
 }
 

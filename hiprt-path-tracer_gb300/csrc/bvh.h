@@ -28,9 +28,10 @@ struct alignas(16) WideNode
 };
 static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
 
-// Stored triangle: three float4 (vertex a + primitive index bits, edge b-a, edge c-a) = 48 bytes.
-// Edges are precomputed in float exactly as the reference's Moller-Trumbore computes them at
-// run time, so the test's results are unchanged bit for bit.
+// Stored triangle: three float4 (vertex a + primitive index bits, vertex b, vertex c) = 48 bytes.
+// The vertices themselves, not edges: the watertight test needs a shared vertex to be the same
+// value in every triangle that uses it, and Moller-Trumbore forms its edges b - a, c - a at run
+// time exactly as the reference does.
 constexpr int kTriangleWords = 3;
 constexpr int kMaxLeafTriangles = 3;
 constexpr int kTraversalStack = 48;  // >= maximum wide depth accepted at build

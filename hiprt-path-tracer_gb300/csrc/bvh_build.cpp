@@ -425,14 +425,10 @@ std::string build_wide_bvh(const int32_t* indices, const float* positions, int64
         r[1] = va[1];
         r[2] = va[2];
         std::memcpy(&r[3], &t, 4);
-        // volatile stores keep the compiler from contracting or reassociating the edge subtraction
-        volatile float e;
         for (int a = 0; a < 3; a++)
         {
-            e = vb[a] - va[a];
-            r[4 + a] = e;
-            e = vc[a] - va[a];
-            r[8 + a] = e;
+            r[4 + a] = vb[a];
+            r[8 + a] = vc[a];
         }
         r[7] = 0.0f;
         r[11] = 0.0f;

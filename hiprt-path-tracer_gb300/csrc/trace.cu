@@ -36,7 +36,7 @@ __device__ __forceinline__ int64_t warp_ray(int64_t v, int64_t warp, int64_t n_w
 // dynamic shared memory of the traversal kernels: SH stack entries per thread, entry-major
 extern __shared__ uint2 trace_sh_stack[];
 
-template <bool ANY_HIT, int SH>
+template <bool ANY_HIT, int SH, int TRI>
 __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict__ nodes,
                                                              const float4* __restrict__ tris,
                                                              const float4* __restrict__ origin_tmin,
@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
     int32_t skip = -1;
     float t_best = 0, u_best = 0, v_best = 0;
     int32_t prim_best = -1;
+    core::WatertightRay wr = {0, 1, 2, 0.0f, 0.0f, 0.0f};
     core::TraversalStack<SH> stack;
     uint2* const sh_col = trace_sh_stack + threadIdx.x;
     const int sh_stride = blockDim.x;
@@ -90,6 +91,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
                     idy = core::safe_rcp(dy);
                     idz = core::safe_rcp(dz);
                     oct_inv = (dx >= 0.0f ? 4u : 0u) | (dy >= 0.0f ? 2u : 0u) | (dz >= 0.0f ? 1u : 0u);
+                    if constexpr (TRI == core::kTriWatertight) wr = core::watertight_ray(dx, dy, dz);
                     skip = last_prim ? last_prim[r] : -1;
                     t_best = tmax;
                     prim_best = -1;
@@ -128,9 +130,9 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
                 const int b = __ffs(tgroup.y) - 1;
                 tgroup.y &= tgroup.y - 1u;
                 const size_t ti = (size_t)(tgroup.x + (uint32_t)b);
-                const float4 a = __ldg(tris + 3 * ti), e1 = __ldg(tris + 3 * ti + 1), e2 = __ldg(tris + 3 * ti + 2);
+                const float4 a = __ldg(tris + 3 * ti), b3 = __ldg(tris + 3 * ti + 1), c3 = __ldg(tris + 3 * ti + 2);
                 float t, u, v;
-                if (core::mt_test(a, e1, e2, ox, oy, oz, dx, dy, dz, t, u, v))
+                if (core::tri_test<TRI>(wr, a, b3, c3, ox, oy, oz, dx, dy, dz, t, u, v))
                 {
                     const int32_t prim = __float_as_int(a.w);
                     if (t >= tmin && prim != skip)
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
 // Per-lane fetch: the per-ray loop (a node, then all triangles of its hit leaves, then a pop), and
 // a lane whose ray finished takes the next ray of its warp's chunk at once (a shared-memory
 // counter per warp), so lanes do not wait for the warp's longest ray.
-template <bool ANY_HIT, int SH>
+template <bool ANY_HIT, int SH, int TRI>
 __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                                    const float4* __restrict__ origin_tmin,
                                                    const float4* __restrict__ dir_tmax,
@@ -225,9 +227,9 @@ __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nod
         const int64_t ray = warp_ray(v, warp, n_warps);
         if (v >= rays_per_warp || ray >= n_rays) break;
         uint32_t cn = 0, ct = 0;
-        const float4 h = core::trace_ray<ANY_HIT, false, SH>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
-                                                             last_prim ? last_prim[ray] : -1, cn, ct,
-                                                             trace_sh_stack + threadIdx.x, blockDim.x);
+        const float4 h = core::trace_ray<ANY_HIT, false, SH, TRI>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
+                                                                  last_prim ? last_prim[ray] : -1, cn, ct,
+                                                                  trace_sh_stack + threadIdx.x, blockDim.x);
         if (ANY_HIT)
         {
             if (occluded) occluded[ray] = __float_as_int(h.w) >= 0 ? 1 : 0;
@@ -238,7 +240,7 @@ __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nod
 }
 
 // per-ray traversal, one thread per ray; COUNT adds node / triangle counters (statistics)
-template <bool ANY_HIT, bool COUNT, int SH>
+template <bool ANY_HIT, bool COUNT, int SH, int TRI>
 __global__ void __launch_bounds__(256) trace_ray_kernel(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                                                const float4* __restrict__ origin_tmin,
                                                                const float4* __restrict__ dir_tmax,
@@ -249,9 +251,9 @@ __global__ void __launch_bounds__(256) trace_ray_kernel(const uint4* __restrict_
     const int64_t ray = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ray >= n_rays) return;
     uint32_t n_nodes = 0, n_tris = 0;
-    const float4 h = core::trace_ray<ANY_HIT, COUNT, SH>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
-                                                         last_prim ? last_prim[ray] : -1, n_nodes, n_tris,
-                                                         trace_sh_stack + threadIdx.x, blockDim.x);
+    const float4 h = core::trace_ray<ANY_HIT, COUNT, SH, TRI>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
+                                                              last_prim ? last_prim[ray] : -1, n_nodes, n_tris,
+                                                              trace_sh_stack + threadIdx.x, blockDim.x);
     if (ANY_HIT)
     {
         if (occluded) occluded[ray] = __float_as_int(h.w) >= 0 ? 1 : 0;
@@ -293,6 +295,7 @@ TraceConfig default_trace_config(bool any_hit)
     c.postpone_below = 8;
     c.blocks_per_sm = 8;
     c.shared_stack = 0;
+    c.triangle_test = core::kTriMollerTrumbore;
     return c;
 }
 
@@ -302,13 +305,14 @@ bool valid_trace_config(const TraceConfig& c)
     return (c.kernel == kTraceKernelPerRay || c.kernel == kTraceKernelPersistent || c.kernel == kTraceKernelFetch) &&
            block_ok && c.refill_below >= 1 &&
            c.refill_below <= 32 && c.postpone_below >= 0 && c.postpone_below <= 32 && c.blocks_per_sm >= 1 &&
-           c.blocks_per_sm <= 64 && (c.shared_stack == 0 || c.shared_stack == 8 || c.shared_stack == 16);
+           c.blocks_per_sm <= 64 && (c.shared_stack == 0 || c.shared_stack == 8 || c.shared_stack == 16) &&
+           (c.triangle_test == core::kTriMollerTrumbore || c.triangle_test == core::kTriWatertight);
 }
 
 namespace {
 
 // the launches of one shared-stack depth SH (dynamic shared memory: SH entries per thread)
-template <int SH>
+template <int SH, int TRI>
 cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, const float* dir_tmax,
                             const int32_t* last_prim, int64_t n_rays, float* hits, uint8_t* occluded, bool any_hit,
                             unsigned long long* counters, cudaStream_t stream, const TraceConfig& cfg)
@@ -326,17 +330,17 @@ cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, cons
         if (counters)
         {
             if (any_hit)
-                trace_ray_kernel<true, true, 0><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+                trace_ray_kernel<true, true, 0, TRI><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
                                                                                      h, occluded, counters);
             else
-                trace_ray_kernel<false, true, 0><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim,
+                trace_ray_kernel<false, true, 0, TRI><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim,
                                                                                       n_rays, h, occluded, counters);
         }
         else if (any_hit)
-            trace_ray_kernel<true, false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+            trace_ray_kernel<true, false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
                                                                                   h, occluded, nullptr);
         else
-            trace_ray_kernel<false, false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+            trace_ray_kernel<false, false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
                                                                                    h, occluded, nullptr);
         return cudaGetLastError();
     }
@@ -351,10 +355,10 @@ cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, cons
         const int64_t warps = blocks * (threads / 32);
         const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
         if (any_hit)
-            trace_fetch<true, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+            trace_fetch<true, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
                                                                         occluded);
         else
-            trace_fetch<false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+            trace_fetch<false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
                                                                          occluded);
         return cudaGetLastError();
     }
@@ -365,11 +369,11 @@ cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, cons
     const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
     const int post_cap = kTraversalStack - bvh.depth - 1 > 0 ? kTraversalStack - bvh.depth - 1 : 0;
     if (any_hit)
-        trace_persistent<true, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
+        trace_persistent<true, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
                                                                          post_cap, cfg.refill_below, cfg.postpone_below, h,
                                                                          occluded);
     else
-        trace_persistent<false, SH><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
+        trace_persistent<false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
                                                                           post_cap, cfg.refill_below, cfg.postpone_below,
                                                                           h, occluded);
     return cudaGetLastError();
@@ -383,14 +387,27 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
 {
     if (n_rays <= 0) return cudaSuccess;
     const TraceConfig cfg = cfg_in ? *cfg_in : default_trace_config(any_hit);
+    // the counting build traces with the parity triangle test (node and triangle counts)
+    if (cfg.triangle_test == core::kTriWatertight && !counters)
+    {
+        switch (cfg.shared_stack)
+        {
+        case 8: return launch_trace_sh<8, core::kTriWatertight>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                occluded, any_hit, counters, stream, cfg);
+        case 16: return launch_trace_sh<16, core::kTriWatertight>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                  occluded, any_hit, counters, stream, cfg);
+        default: return launch_trace_sh<0, core::kTriWatertight>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                 occluded, any_hit, counters, stream, cfg);
+        }
+    }
     switch (counters ? 0 : cfg.shared_stack)
     {
-    case 8: return launch_trace_sh<8>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits, occluded, any_hit, counters,
-                                      stream, cfg);
-    case 16: return launch_trace_sh<16>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits, occluded, any_hit, counters,
-                                        stream, cfg);
-    default: return launch_trace_sh<0>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits, occluded, any_hit, counters,
-                                       stream, cfg);
+    case 8: return launch_trace_sh<8, core::kTriMollerTrumbore>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                occluded, any_hit, counters, stream, cfg);
+    case 16: return launch_trace_sh<16, core::kTriMollerTrumbore>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                  occluded, any_hit, counters, stream, cfg);
+    default: return launch_trace_sh<0, core::kTriMollerTrumbore>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                 occluded, any_hit, counters, stream, cfg);
     }
 }
 

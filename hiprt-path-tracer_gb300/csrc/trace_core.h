@@ -9,9 +9,20 @@
 // (HPG 2017): node groups (child base + 8 hit bits + internal-child mask) on a per-thread stack,
 // children visited nearest-first through the octant slot order, triangle hits from a 24-bit mask.
 //
-// The triangle test is the reference's Moller-Trumbore (src/Renderer/Triangle.h:20-63) written
-// with explicitly rounded operations (__fmul_rn/__fadd_rn/__fsub_rn/__fdiv_rn), which the compiler
-// never contracts into FMAs, so t/u/v match the reference's CPU results bit for bit. Box tests only
+// Two triangle tests (template parameter TRI):
+//  - kTriMollerTrumbore, the parity mode: the reference's Moller-Trumbore
+//    (src/Renderer/Triangle.h:20-63) written with explicitly rounded operations
+//    (__fmul_rn/__fadd_rn/__fsub_rn/__fdiv_rn), which the compiler never contracts into FMAs, so
+//    t/u/v match the reference's CPU results bit for bit. It is not watertight: a ray through an
+//    edge shared by two triangles can miss both (or hit both) by a rounding.
+//  - kTriWatertight, the production mode: Woop, Benthin and Wald, "Watertight Ray/Triangle
+//    Intersection" (JCGT 2013): the vertices are moved into a ray-aligned space by a shear that
+//    depends on the ray only, and the three edge functions are evaluated there; a shared edge
+//    gives the two triangles edge functions of exactly opposite sign (rounded products and
+//    differences are antisymmetric), so no ray passes between them; exactly zero edge functions
+//    are evaluated again in double. Barycentrics are returned as u = weight of b, v = weight of c,
+//    as Moller-Trumbore defines them.
+// Box tests only
 // prune, so their rounding cannot change a result as long as they stay conservative: each node
 // widens its children's slab intervals by an absolute slack that bounds every rounding of the test
 // (derivation at intersect_children).
@@ -41,6 +52,8 @@ inline float __fadd_rn(float a, float b) { return a + b; }
 inline float __fsub_rn(float a, float b) { return a - b; }
 inline float __fdiv_rn(float a, float b) { return a / b; }
 inline float __frcp_rn(float a) { return 1.0f / a; }
+inline double __dmul_rn(double a, double b) { return a * b; }
+inline double __dsub_rn(double a, double b) { return a - b; }
 inline float __uint_as_float(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline float __int_as_float(int32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline int32_t __float_as_int(float f) { int32_t u; std::memcpy(&u, &f, 4); return u; }
@@ -79,10 +92,16 @@ GBPT_HD void cross_rn(float ax, float ay, float az, float bx, float by, float bz
     cz = __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
 }
 
-// Moller-Trumbore in the reference's operation order. Returns true with t/u/v on a hit.
-GBPT_HD bool mt_test(const float4 a, const float4 e1, const float4 e2, float ox, float oy, float oz,
+constexpr int kTriMollerTrumbore = 0;
+constexpr int kTriWatertight = 1;
+
+// Moller-Trumbore in the reference's operation order, from the vertices a, b, c (edges formed
+// here as the reference forms them). Returns true with t/u/v on a hit.
+GBPT_HD bool mt_test(const float4 a, const float4 b, const float4 c, float ox, float oy, float oz,
                                         float dx, float dy, float dz, float& t, float& u, float& v)
 {
+    const float4 e1 = make_float4(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z), 0.0f);
+    const float4 e2 = make_float4(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z), 0.0f);
     float hx, hy, hz;
     cross_rn(dx, dy, dz, e2.x, e2.y, e2.z, hx, hy, hz);
     const float det = dot_rn(e1.x, e1.y, e1.z, hx, hy, hz);
@@ -97,6 +116,90 @@ GBPT_HD bool mt_test(const float4 a, const float4 e1, const float4 e2, float ox,
     if (v < 0.0f || __fadd_rn(u, v) > 1.0f) return false;
     t = __fmul_rn(f, dot_rn(e2.x, e2.y, e2.z, qx, qy, qz));
     return t > kMtEps;
+}
+
+// The per-ray shear of the watertight test: kz the axis of the direction's largest magnitude, kx
+// and ky the two others (swapped when d[kz] < 0, which keeps the edge functions' winding), and
+// the shear constants sx = d[kx] / d[kz], sy = d[ky] / d[kz], sz = 1 / d[kz].
+struct WatertightRay
+{
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+GBPT_HD float axis_of(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+GBPT_HD WatertightRay watertight_ray(float dx, float dy, float dz)
+{
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    WatertightRay r;
+    r.kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    r.kx = r.kz == 2 ? 0 : r.kz + 1;
+    r.ky = r.kx == 2 ? 0 : r.kx + 1;
+    const float dkz = axis_of(dx, dy, dz, r.kz);
+    if (dkz < 0.0f)
+    {
+        const int k = r.kx;
+        r.kx = r.ky;
+        r.ky = k;
+    }
+    r.sx = __fdiv_rn(axis_of(dx, dy, dz, r.kx), dkz);
+    r.sy = __fdiv_rn(axis_of(dx, dy, dz, r.ky), dkz);
+    r.sz = __fdiv_rn(1.0f, dkz);
+    return r;
+}
+
+// Watertight ray/triangle test (Woop et al. 2013, algorithm of section 3, no backface culling).
+// Returns true with t (> 1e-7, the parity mode's minimum), u, v on a hit.
+GBPT_HD bool wt_test(const WatertightRay& w, const float4 a, const float4 b, const float4 c, float ox, float oy,
+                     float oz, float& t, float& u, float& v)
+{
+    const float Ax = __fsub_rn(axis_of(a.x, a.y, a.z, w.kx), axis_of(ox, oy, oz, w.kx));
+    const float Ay = __fsub_rn(axis_of(a.x, a.y, a.z, w.ky), axis_of(ox, oy, oz, w.ky));
+    const float Az = __fsub_rn(axis_of(a.x, a.y, a.z, w.kz), axis_of(ox, oy, oz, w.kz));
+    const float Bx = __fsub_rn(axis_of(b.x, b.y, b.z, w.kx), axis_of(ox, oy, oz, w.kx));
+    const float By = __fsub_rn(axis_of(b.x, b.y, b.z, w.ky), axis_of(ox, oy, oz, w.ky));
+    const float Bz = __fsub_rn(axis_of(b.x, b.y, b.z, w.kz), axis_of(ox, oy, oz, w.kz));
+    const float Cx = __fsub_rn(axis_of(c.x, c.y, c.z, w.kx), axis_of(ox, oy, oz, w.kx));
+    const float Cy = __fsub_rn(axis_of(c.x, c.y, c.z, w.ky), axis_of(ox, oy, oz, w.ky));
+    const float Cz = __fsub_rn(axis_of(c.x, c.y, c.z, w.kz), axis_of(ox, oy, oz, w.kz));
+    // shear into ray space
+    const float ax = __fsub_rn(Ax, __fmul_rn(w.sx, Az)), ay = __fsub_rn(Ay, __fmul_rn(w.sy, Az));
+    const float bx = __fsub_rn(Bx, __fmul_rn(w.sx, Bz)), by = __fsub_rn(By, __fmul_rn(w.sy, Bz));
+    const float cx = __fsub_rn(Cx, __fmul_rn(w.sx, Cz)), cy = __fsub_rn(Cy, __fmul_rn(w.sy, Cz));
+    // edge functions: U for edge (b, c), V for (c, a), W for (a, b)
+    float U = __fsub_rn(__fmul_rn(cx, by), __fmul_rn(cy, bx));
+    float V = __fsub_rn(__fmul_rn(ax, cy), __fmul_rn(ay, cx));
+    float W = __fsub_rn(__fmul_rn(bx, ay), __fmul_rn(by, ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f)
+    {
+        U = (float)__dsub_rn(__dmul_rn((double)cx, (double)by), __dmul_rn((double)cy, (double)bx));
+        V = (float)__dsub_rn(__dmul_rn((double)ax, (double)cy), __dmul_rn((double)ay, (double)cx));
+        W = (float)__dsub_rn(__dmul_rn((double)bx, (double)ay), __dmul_rn((double)by, (double)ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float az = __fmul_rn(w.sz, Az), bz = __fmul_rn(w.sz, Bz), cz = __fmul_rn(w.sz, Cz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, az), __fmul_rn(V, bz)), __fmul_rn(W, cz));
+    // t = T / det must be positive: T and det of the same sign
+    if ((__float_as_int(T) ^ __float_as_int(det)) < 0) return false;
+    const float rcp = __fdiv_rn(1.0f, det);
+    t = __fmul_rn(T, rcp);
+    u = __fmul_rn(V, rcp);
+    v = __fmul_rn(W, rcp);
+    return t > kMtEps;
+}
+
+// The triangle test of mode TRI (w is only read by the watertight test)
+template <int TRI>
+GBPT_HD bool tri_test(const WatertightRay& w, const float4 a, const float4 b, const float4 c, float ox, float oy,
+                      float oz, float dx, float dy, float dz, float& t, float& u, float& v)
+{
+    if constexpr (TRI == kTriWatertight)
+        return wt_test(w, a, b, c, ox, oy, oz, t, u, v);
+    else
+        return mt_test(a, b, c, ox, oy, oz, dx, dy, dz, t, u, v);
 }
 
 GBPT_HD float safe_rcp(float d)
@@ -230,13 +333,15 @@ struct TraversalStack
 // miss. Any hit: returns prim >= 0 iff some accepted hit has t < tmax. Counts visited nodes and
 // tested triangles when COUNT is set. SH > 0: the bottom SH stack entries live in the shared
 // column sh_col (stride sh_stride).
-template <bool ANY_HIT, bool COUNT, int SH = 0>
+template <bool ANY_HIT, bool COUNT, int SH = 0, int TRI = kTriMollerTrumbore>
 GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const float4 ot,
                          const float4 dt, const int32_t skip_prim, uint32_t& n_nodes, uint32_t& n_tris,
                          uint2* sh_col = nullptr, int sh_stride = 0)
 {
     const float ox = ot.x, oy = ot.y, oz = ot.z, ray_tmin = ot.w;
     const float dx = dt.x, dy = dt.y, dz = dt.z;
+    WatertightRay wr = {0, 1, 2, 0.0f, 0.0f, 0.0f};
+    if constexpr (TRI == kTriWatertight) wr = watertight_ray(dx, dy, dz);
     const float idx = safe_rcp(dx), idy = safe_rcp(dy), idz = safe_rcp(dz);
     const uint32_t oct_inv = (dx >= 0.0f ? 4u : 0u) | (dy >= 0.0f ? 2u : 0u) | (dz >= 0.0f ? 1u : 0u);
 
@@ -275,10 +380,10 @@ GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restri
             const int b = __ffs(tgroup.y) - 1;
             tgroup.y &= tgroup.y - 1u;
             const size_t ti = (size_t)(tgroup.x + (uint32_t)b);
-            const float4 a = GBPT_LDG(tris + 3 * ti), e1 = GBPT_LDG(tris + 3 * ti + 1), e2 = GBPT_LDG(tris + 3 * ti + 2);
+            const float4 a = GBPT_LDG(tris + 3 * ti), vb = GBPT_LDG(tris + 3 * ti + 1), vc = GBPT_LDG(tris + 3 * ti + 2);
             if (COUNT) n_tris++;
             float t, u, v;
-            if (!mt_test(a, e1, e2, ox, oy, oz, dx, dy, dz, t, u, v)) continue;
+            if (!tri_test<TRI>(wr, a, vb, vc, ox, oy, oz, dx, dy, dz, t, u, v)) continue;
             const int32_t prim = __float_as_int(a.w);
             if (t < ray_tmin || prim == skip_prim) continue;
             if (ANY_HIT)

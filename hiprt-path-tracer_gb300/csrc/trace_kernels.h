@@ -27,6 +27,7 @@ struct TraceConfig
     int32_t postpone_below;  // persistent: triangle steps need at least this many lanes
     int32_t blocks_per_sm;   // persistent grid
     int32_t shared_stack;    // traversal-stack entries per thread in shared memory (0, 8 or 16)
+    int32_t triangle_test;   // core::kTriMollerTrumbore (parity) or core::kTriWatertight
 };
 
 TraceConfig default_trace_config(bool any_hit);

@@ -172,3 +172,39 @@ def _host_ptr(a) -> int:
         return int(a.ctypes.data)
     assert a.is_contiguous() and a.device.type == "cpu"
     return int(a.data_ptr())
+
+
+def classify_hit_differences(mesh, a, b, edge_eps=1e-4):
+    """Compares two closest-hit records of the same rays (e.g. the Moller-Trumbore and the
+    watertight triangle tests) -> (agree, edge, tie, other) counts.
+    agree: both miss, or the same triangle with t within 1e-5 relative and the points their (u, v)
+      address on it within 2e-5 t (barycentrics of a small triangle seen from afar are conditioned
+      by t over its size, differently in the two tests);
+    edge: a different outcome where a hit lies within edge_eps (barycentric) of its triangle's edge;
+    tie: two different triangles hit at the same t (1e-6 relative);
+    other: anything else."""
+    pa, pb = a[:, 3].view(np.int32), b[:, 3].view(np.int32)
+    same = pa == pb
+    both = np.nonzero(same & (pa >= 0))[0]
+    tri = mesh.triangle_soup().reshape(-1, 3, 3).astype(np.float64)[pa[both]]
+    e1, e2 = tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]
+
+    def at(h):
+        return tri[:, 0] + h[both, 1:2].astype(np.float64) * e1 + h[both, 2:3].astype(np.float64) * e2
+
+    t = a[both, 0].astype(np.float64)
+    ok = (np.abs(t - b[both, 0]) <= 1e-5 * t) & (np.linalg.norm(at(a) - at(b), axis=1) <= 2e-5 * t)
+    agree = int((same & (pa < 0)).sum() + ok.sum())
+
+    def near_edge(h):
+        return min(h[1], h[2], 1.0 - h[1] - h[2]) < edge_eps
+
+    edge = tie = other = 0
+    for i in np.nonzero(~same)[0]:
+        if (pa[i] >= 0 and near_edge(a[i])) or (pb[i] >= 0 and near_edge(b[i])):
+            edge += 1
+        elif pa[i] >= 0 and pb[i] >= 0 and abs(float(a[i, 0]) - float(b[i, 0])) <= 1e-6 * max(1.0, abs(float(a[i, 0]))):
+            tie += 1
+        else:
+            other += 1
+    return agree, edge, tie, other + int((~ok).sum())

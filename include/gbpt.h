@@ -132,8 +132,18 @@ typedef struct gbpt_trace_config {
     int32_t blocks_per_sm;   /* PERSISTENT and FETCH: blocks per SM of the grid (1..64) */
     int32_t shared_stack;    /* traversal-stack entries per thread kept in shared memory (0, 8 or 16;
                                 deeper entries in local memory); 0 in configurations written before */
-    int32_t reserved[2];
+    int32_t triangle_test;   /* GBPT_TRIANGLE_* [GBPT_TRIANGLE_MOLLER_TRUMBORE]; the autotuner keeps it */
+    int32_t reserved;
 } gbpt_trace_config;
+
+/* Ray/triangle test of a traversal (gbpt_trace_config.triangle_test):
+ *   GBPT_TRIANGLE_MOLLER_TRUMBORE: the reference's Moller-Trumbore (src/Renderer/Triangle.h:20-63)
+ *     in its operation order, rounded step by step: hits bit-identical to the reference's CPU
+ *     traversal (the parity mode); not watertight at shared edges;
+ *   GBPT_TRIANGLE_WATERTIGHT: Woop, Benthin and Wald 2013 (JCGT 2:1): no ray passes between two
+ *     triangles that share an edge (the production mode). t, u, v agree with Moller-Trumbore to
+ *     float rounding away from edges. */
+enum { GBPT_TRIANGLE_MOLLER_TRUMBORE = 0, GBPT_TRIANGLE_WATERTIGHT = 1 };
 
 /* The configuration gbpt_trace_closest (any_hit = 0) / gbpt_trace_any (any_hit = 1) and their
  * host variants use for this BVH (defaults: persistent closest-hit, per-ray any-hit). */

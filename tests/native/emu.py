@@ -50,12 +50,12 @@ class EmuBVH:
         lib().emu_export(self.h, nodes.ctypes.data, tris.ctypes.data)
         return nodes.reshape(-1, 80), tris
 
-    def trace(self, rays, any_hit=False):
+    def trace(self, rays, any_hit=False, watertight=False):
         o = np.ascontiguousarray(rays.origin_tmin, np.float32)
         d = np.ascontiguousarray(rays.dir_tmax, np.float32)
         lp = np.ascontiguousarray(rays.last_prim, np.int32)
         out = np.zeros((len(o), 4), np.float32)
         cnt = np.zeros(2, np.int64)
-        lib().emu_trace(self.h, o.ctypes.data, d.ctypes.data, lp.ctypes.data, len(o), 1 if any_hit else 0,
+        lib().emu_trace(self.h, o.ctypes.data, d.ctypes.data, lp.ctypes.data, len(o), (1 if any_hit else 0) | (2 if watertight else 0),
                         out.ctypes.data, cnt.ctypes.data)
         return out, cnt

@@ -61,9 +61,12 @@ void emu_export(void* h, void* nodes, void* tris)
     std::memcpy(tris, e->bvh.tris.data(), e->bvh.tris.size() * sizeof(float));
 }
 
+/* any_hit bit 0: any-hit traversal; bit 1: the watertight triangle test (else Moller-Trumbore) */
 void emu_trace(void* h, const float* origin_tmin, const float* dir_tmax, const int32_t* last_prim, int64_t n, int any_hit,
                float* hits, int64_t* counters)
 {
+    const bool wt = (any_hit & 2) != 0;
+    any_hit &= 1;
     Emu* e = static_cast<Emu*>(h);
     const uint4* nodes = reinterpret_cast<const uint4*>(e->bvh.nodes.data());
     const float4* tris = reinterpret_cast<const float4*>(e->bvh.tris.data());
@@ -74,8 +77,13 @@ void emu_trace(void* h, const float* origin_tmin, const float* dir_tmax, const i
         float4 dt{dir_tmax[4 * i], dir_tmax[4 * i + 1], dir_tmax[4 * i + 2], dir_tmax[4 * i + 3]};
         int32_t lp = last_prim ? last_prim[i] : -1;
         uint32_t nn = 0, nt = 0;
-        float4 r = any_hit ? gbpt::core::trace_ray<true, true>(nodes, tris, ot, dt, lp, nn, nt)
-                           : gbpt::core::trace_ray<false, true>(nodes, tris, ot, dt, lp, nn, nt);
+        float4 r;
+        if (wt)
+            r = any_hit ? gbpt::core::trace_ray<true, true, 0, gbpt::core::kTriWatertight>(nodes, tris, ot, dt, lp, nn, nt)
+                        : gbpt::core::trace_ray<false, true, 0, gbpt::core::kTriWatertight>(nodes, tris, ot, dt, lp, nn, nt);
+        else
+            r = any_hit ? gbpt::core::trace_ray<true, true>(nodes, tris, ot, dt, lp, nn, nt)
+                        : gbpt::core::trace_ray<false, true>(nodes, tris, ot, dt, lp, nn, nt);
         cn += nn;
         ct += nt;
         std::memcpy(hits + 4 * i, &r, 16);

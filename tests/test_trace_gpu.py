@@ -157,3 +157,59 @@ def test_trace_config_validation(cuda):
                 dict(shared_stack=4), dict(shared_stack=-8)):
         with pytest.raises(GbptError):
             bvh.set_trace_config(False, **bad)
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_watertight_kernels_match_host_build_and_autotune(cuda, any_hit):
+    """The watertight triangle test in every kernel variant returns, bit for bit, what the host build
+    of the same traversal core returns; the autotuner keeps the triangle test it is given."""
+    import sys
+    sys.path.insert(0, __file__.rsplit("/", 1)[0])
+    from native.emu import EmuBVH
+    mesh = scenes.traversal_scene(cells=96, n_random=3000, seed=4)
+    rays = scenes.pinhole_rays(256, 128, eye=(0.0, 1.5, -2.5), target=(0.0, 0.0, 0.0), vfov_deg=30.0)
+    if any_hit:
+        pts, _, prim = scenes.hit_points_normals(mesh, rays, EmuBVH(mesh).trace(rays)[0])
+        m = prim >= 0
+        rays, _ = scenes.shadow_rays(pts[m], prim[m], seed=6)
+    want, _ = EmuBVH(mesh).trace(rays, any_hit=any_hit, watertight=True)
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    o, d, lp = _dev(rays, cuda)
+    run = bvh.occluded_cfg if any_hit else bvh.closest_cfg
+    for cfg in (dict(kernel=1, block=128), dict(kernel=1, block=64, shared_stack=8),
+                dict(kernel=2, block=128, refill_below=12, postpone_below=8, blocks_per_sm=8, shared_stack=16),
+                dict(kernel=3, block=256, blocks_per_sm=4)):
+        got = run(o, d, lp, triangle_test=1, **cfg).cpu().numpy()
+        if any_hit:
+            assert np.array_equal(got, (want[:, 3].view(np.int32) >= 0).astype(np.uint8)), cfg
+        else:
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), cfg
+    bvh.set_trace_config(any_hit, triangle_test=1)
+    best, _ = bvh.autotune(o, d, lp, any_hit=any_hit)
+    assert best["triangle_test"] == 1
+
+
+def test_watertight_against_moller_trumbore_on_benchmark_scene(cuda):
+    """The traversal benchmark scene (2,297,152 triangles): Moller-Trumbore (parity) and watertight
+    closest hits of 2M primary rays and of bounce rays; every disagreement is a ray within a
+    rounding of an edge or an exact tie (classified as in tests/test_watertight.py)."""
+    import sys
+    sys.path.insert(0, __file__.rsplit("/", 1)[0])
+    from test_watertight import classify
+    mesh = scenes.traversal_scene()
+    bvh = gbpt.BVH(mesh.indices, mesh.positions)
+    rays = scenes.pinhole_rays(2048, 1024, vfov_deg=30)
+    o, d, lp = _dev(rays, cuda)
+    mt = bvh.closest_cfg(o, d, lp, kernel=1, block=128).cpu().numpy()
+    wt = bvh.closest_cfg(o, d, lp, kernel=1, block=128, triangle_test=1).cpu().numpy()
+    agree, edge, tie, other = classify(mesh, rays, mt, wt)
+    assert other == 0, (agree, edge, tie, other)
+    assert agree >= 0.999 * len(rays), (agree, edge, tie)
+    pts, nrm, prim = scenes.hit_points_normals(mesh, rays, mt)
+    m = np.nonzero(prim >= 0)[0][::4]
+    b = scenes.bounce_rays(pts[m], nrm[m], prim[m], seed=9)
+    o, d, lp = _dev(b, cuda)
+    mt = bvh.closest_cfg(o, d, lp, kernel=1, block=128).cpu().numpy()
+    wt = bvh.closest_cfg(o, d, lp, kernel=1, block=128, triangle_test=1).cpu().numpy()
+    agree, edge, tie, other = classify(mesh, b, mt, wt)
+    assert other == 0, (agree, edge, tie, other)
