@@ -646,6 +646,31 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def guide_kernels_case(n, data_seed=1, guide_seed=3):
+    """The guide's training and inference kernels on n seeded random samples (positions in the unit
+    box, random unit normals / view / incident directions, exponential weights with a fifth zero,
+    cosine BSDF pdfs): the case the guide's ncu captures run."""
+    import numpy as np
+    import torch
+    from gbpt import guide
+    rng = np.random.default_rng(data_seed)
+    P = rng.uniform(0.0, 1.0, (n, 3))
+    N, V, D = (rng.normal(size=(n, 3)) for _ in range(3))
+    for a in (N, V, D):
+        a /= np.linalg.norm(a, axis=1, keepdims=True)
+    w = rng.exponential(1.0, n) * (rng.random(n) < 0.8)
+    pb = np.maximum((N * D).sum(1), 0.0) / np.pi
+    t = [torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda() for a in (P, N, V, D, w, pb)]
+    g = guide.Guide(seed=guide_seed)
+    for _ in range(2):
+        loss = g.train(*t)
+        rows = g.infer(t[0], t[1], t[2])
+    torch.cuda.synchronize()
+    if g.error_flag() != 0:
+        raise SystemExit(f"guide kernels reported error flag {g.error_flag()}")
+    print(json.dumps({"guide_kernels": n, "loss": float(loss), "rows": list(rows.shape)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -666,7 +691,13 @@ def main():
                     help="JSON {primary, bounce, shadow} launch configurations to use instead of autotuning")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 2048x1024 primary + 1M bounce + 1M shadow rays, no e2e/CPU legs")
+    ap.add_argument("--guide-kernels", type=int, default=0, metavar="N",
+                    help="profiling case: two training steps and two queries of the guide on N seeded random "
+                         "samples, then exit")
     args = ap.parse_args()
+    if args.guide_kernels:
+        guide_kernels_case(args.guide_kernels)
+        return
     if args.warmup < 3:
         args.warmup = 3
     global WIDTH, HEIGHT, N_BOUNCE, N_SHADOW
