@@ -848,12 +848,11 @@ def main():
     wt_ms = w0.elapsed_time(w1) / 5
     from gbpt.trace import classify_hit_differences
     hp_np, hb_np = hits_p.cpu().numpy(), hits_b.cpu().numpy()
-    dif_p = classify_hit_differences(mesh, hp_np, hits_pw.cpu().numpy())
-    dif_b = classify_hit_differences(mesh, hb_np, hits_bw.cpu().numpy())
+    dif_p = classify_hit_differences(mesh, primary, hp_np, hits_pw.cpu().numpy())
+    dif_b = classify_hit_differences(mesh, bounce, hb_np, hits_bw.cpu().numpy())
     occ_diff = int((occ_s != occ_sw).sum().item())
     watertight = {"mrays_s": world * n_rays / (wt_ms * 1e-3) / 1e6, "ms_per_step": wt_ms,
-                  "vs_moller_trumbore_primary": dict(zip(("agree", "edge", "tie", "other"), dif_p)),
-                  "vs_moller_trumbore_bounce": dict(zip(("agree", "edge", "tie", "other"), dif_b)),
+                  "vs_moller_trumbore_primary": dif_p, "vs_moller_trumbore_bounce": dif_b,
                   "shadow_decisions_differing": occ_diff}
 
     # end to end through the host-buffer C entry points (pinned host memory, copies in the call)

@@ -31,18 +31,17 @@ __device__ __forceinline__ void camera_ray(const RenderConst& rc, int pixel, int
 {
     const int x = pixel % rc.width, y = pixel / rc.width;
     const bool ref_rng = rc.rng_mode == GBPT_RNG_REFERENCE;
-    rng = ref_rng ? reference_seed((uint32_t)pixel, (uint32_t)sample, rc.random_number)
+    rng = ref_rng ? reference_seed((uint32_t)pixel, (uint32_t)sample, rc.random_number_camera)
                   : pcg_seed((uint32_t)pixel, (uint32_t)sample, rc.seed);
-    const uint64_t seed0 = rng.state;
     float px = x + 0.5f, py = y + 0.5f;
     if (rc.do_jittering)
     {
         px += rng.next() - 0.5f;
         py += rng.next() - 0.5f;
     }
-    // the reference's MegaKernel seeds its generator as CameraRays did: its first draws at the
-    // camera hit repeat the jitter's (Megakernel.h:52-57)
-    if (ref_rng) rng.state = seed0;
+    // the reference's MegaKernel seeds a new generator from its own pass's random number
+    // (Megakernel.h:52-57): the path continues with that one
+    if (ref_rng) rng = reference_seed((uint32_t)pixel, (uint32_t)sample, rc.random_number);
     const float xn = px / rc.width * 2.0f - 1.0f;
     const float yn = py / rc.height * 2.0f - 1.0f;
     origin = mat_x_point(rc.inverse_view, v3(0.0f, 0.0f, 0.0f));

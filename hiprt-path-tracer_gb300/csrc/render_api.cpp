@@ -873,8 +873,13 @@ gbpt_status gbpt_pass_camera_rays(gbpt_renderer* r, void* stream)
 {
     if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
     r->cur = 0;
-    // the reference's camera pass draws the frame's random number first (CPURenderer.cpp:698-705)
-    if (r->rc.rng_mode == GBPT_RNG_REFERENCE) r->rc.random_number = xorshift32_step(r->host_rng);
+    // the reference's GPU renderer draws one random number per pass from its generator: the
+    // G-buffer pass, then the MegaKernel pass (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53)
+    if (r->rc.rng_mode == GBPT_RNG_REFERENCE)
+    {
+        r->rc.random_number_camera = xorshift32_step(r->host_rng);
+        r->rc.random_number = xorshift32_step(r->host_rng);
+    }
     cudaError_t e = gbpt::launch_camera(r->rc, r->pb, r->q[0], (int32_t)r->iteration, r->stats, r->n_sm,
                                         (cudaStream_t)stream);
     if (e == cudaSuccess && r->gv.rec_count) e = cudaMemsetAsync(r->gv.rec_count, 0, sizeof(int32_t), (cudaStream_t)stream);
@@ -1224,8 +1229,6 @@ gbpt_status gbpt_pass_accumulate(gbpt_renderer* r, void* stream)
     }
     r->iteration += r->rc.spp;
     r->samples += r->rc.spp;
-    // ... and post_sample_update draws one more (CPURenderer.cpp:586-598)
-    if (r->rc.rng_mode == GBPT_RNG_REFERENCE) xorshift32_step(r->host_rng);
     return e == cudaSuccess ? GBPT_OK : cuda_error(e, "accumulate");
 }
 

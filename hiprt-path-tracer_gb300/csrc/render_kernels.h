@@ -30,7 +30,8 @@ struct RenderConst
     int32_t direct_ris;               // GBPT_DIRECT_RIS
     int32_t ris_light, ris_bsdf;      // RIS candidates
     int32_t rng_mode;                 // GBPT_RNG_*
-    uint32_t random_number;           // GBPT_RNG_REFERENCE: this launch's HIPRTRenderData::random_number
+    uint32_t random_number;           // GBPT_RNG_REFERENCE: HIPRTRenderData::random_number of the MegaKernel pass
+    uint32_t random_number_camera;    // GBPT_RNG_REFERENCE: HIPRTRenderData::random_number of the G-buffer pass
     float inverse_view[16];
     float inverse_projection[16];
 };

@@ -174,37 +174,77 @@ def _host_ptr(a) -> int:
     return int(a.data_ptr())
 
 
-def classify_hit_differences(mesh, a, b, edge_eps=1e-4):
-    """Compares two closest-hit records of the same rays (e.g. the Moller-Trumbore and the
-    watertight triangle tests) -> (agree, edge, tie, other) counts.
-    agree: both miss, or the same triangle with t within 1e-5 relative and the points their (u, v)
-      address on it within 2e-5 t (barycentrics of a small triangle seen from afar are conditioned
-      by t over its size, differently in the two tests);
-    edge: a different outcome where a hit lies within edge_eps (barycentric) of its triangle's edge;
-    tie: two different triangles hit at the same t (1e-6 relative);
-    other: anything else."""
+def classify_hit_differences(mesh, rays, a, b, edge_rel=2.5e-7, mt_epsilon=1e-7):
+    """Compares the closest-hit records a (Moller-Trumbore, the parity test) and b (watertight) of
+    the same rays -> dict of counts {agree, edge, parallel, tie, other}:
+      agree: both miss, or the same triangle at the same point: |t_a - t_b| cos(theta) <= 4e-6 s
+        and the points their (u, v) address within 4e-6 s / cos(theta), with s = max(t, |origin|)
+        the magnitude of the coordinates both tests round (a bounce ray's t can be far below its
+        origin's) and theta the angle between the ray and the triangle's normal (the position of a
+        grazing intersection along the ray is conditioned by 1 / cos(theta));
+      edge: a different outcome where a hit lies within edge_rel s of an edge of its triangle,
+        measured in the plane perpendicular to the ray (the plane both tests decide in: a
+        coordinate rounding decides which side of the edge the ray passes);
+      parallel: b hits a triangle whose Moller-Trumbore determinant e1 . (d x e2), in float as the
+        reference computes it, is within +-mt_epsilon: the reference's test treats such a ray as
+        parallel to the triangle and never reports it (src/Renderer/Triangle.h:22-31) - grazing
+        hits on small triangles that only the watertight test keeps;
+      tie: two different triangles hit at the same t (1e-6 relative);
+      other: anything else."""
     pa, pb = a[:, 3].view(np.int32), b[:, 3].view(np.int32)
+    soup = np.asarray(mesh.triangle_soup(), np.float32).reshape(-1, 3, 3)
+    tri = soup.astype(np.float64)
+    origin = np.asarray(rays.origin_tmin)[:, :3].astype(np.float64)
+    direction = np.asarray(rays.dir_tmax)[:, :3].astype(np.float64)
     same = pa == pb
     both = np.nonzero(same & (pa >= 0))[0]
-    tri = mesh.triangle_soup().reshape(-1, 3, 3).astype(np.float64)[pa[both]]
-    e1, e2 = tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]
+    T = tri[pa[both]]
+    e1, e2 = T[:, 1] - T[:, 0], T[:, 2] - T[:, 0]
+    n = np.cross(e1, e2)
+    dn = direction[both] / np.linalg.norm(direction[both], axis=1, keepdims=True)
+    cos = np.abs(np.einsum("ij,ij->i", n, dn)) / np.maximum(np.linalg.norm(n, axis=1), 1e-300)
+    cos = np.maximum(cos, 1e-6)
 
     def at(h):
-        return tri[:, 0] + h[both, 1:2].astype(np.float64) * e1 + h[both, 2:3].astype(np.float64) * e2
+        return T[:, 0] + h[both, 1:2].astype(np.float64) * e1 + h[both, 2:3].astype(np.float64) * e2
 
     t = a[both, 0].astype(np.float64)
-    ok = (np.abs(t - b[both, 0]) <= 1e-5 * t) & (np.linalg.norm(at(a) - at(b), axis=1) <= 2e-5 * t)
-    agree = int((same & (pa < 0)).sum() + ok.sum())
+    scale = np.maximum(t, np.linalg.norm(origin[both], axis=1))
+    ok = (np.abs(t - b[both, 0]) * cos <= 4e-6 * scale) & (np.linalg.norm(at(a) - at(b), axis=1) * cos <= 4e-6 * scale)
+    counts = dict(agree=int((same & (pa < 0)).sum() + ok.sum()), edge=0, parallel=0, tie=0, other=int((~ok).sum()))
 
-    def near_edge(h):
-        return min(h[1], h[2], 1.0 - h[1] - h[2]) < edge_eps
+    def edge_distance(i, h):
+        o, d = origin[i], direction[i] / np.linalg.norm(direction[i])
+        v0, v1, v2 = tri[int(h[3:4].view(np.int32)[0])]
+        p = v0 + float(h[1]) * (v1 - v0) + float(h[2]) * (v2 - v0)
 
-    edge = tie = other = 0
+        def perp(x):
+            return x - np.dot(x - o, d) * d
+
+        q, w = perp(p), [perp(v) for v in (v0, v1, v2)]
+        best = np.inf
+        for k in range(3):
+            s0, s1 = w[k], w[(k + 1) % 3]
+            e = s1 - s0
+            s = np.clip(np.dot(q - s0, e) / max(np.dot(e, e), 1e-300), 0.0, 1.0)
+            best = min(best, float(np.linalg.norm(q - (s0 + s * e))))
+        return best
+
+    def mt_determinant(i, prim):
+        v0, v1, v2 = soup[prim]
+        d = np.asarray(rays.dir_tmax)[i, :3].astype(np.float32)
+        return float(np.dot(v1 - v0, np.cross(d, v2 - v0)))
+
     for i in np.nonzero(~same)[0]:
-        if (pa[i] >= 0 and near_edge(a[i])) or (pb[i] >= 0 and near_edge(b[i])):
-            edge += 1
+        o_len = float(np.linalg.norm(origin[i]))
+        near = [1 for h, p in ((a, pa), (b, pb))
+                if p[i] >= 0 and edge_distance(i, h[i]) <= edge_rel * max(float(h[i, 0]), o_len)]
+        if near:
+            counts["edge"] += 1
+        elif pb[i] >= 0 and abs(mt_determinant(i, pb[i])) < mt_epsilon:
+            counts["parallel"] += 1
         elif pa[i] >= 0 and pb[i] >= 0 and abs(float(a[i, 0]) - float(b[i, 0])) <= 1e-6 * max(1.0, abs(float(a[i, 0]))):
-            tie += 1
+            counts["tie"] += 1
         else:
-            other += 1
-    return agree, edge, tie, other + int((~ok).sum())
+            counts["other"] += 1
+    return counts

@@ -219,16 +219,17 @@ enum { GBPT_DIRECT_MIS = 0, GBPT_DIRECT_RIS = 1 };
  *   GBPT_RNG_REFERENCE: the reference's generator and draw order, for sample-by-sample comparison
  *     with its own kernels: Xorshift32 (src/HostDeviceCommon/Xorshift.h:18-66) seeded by
  *     wang_hash((pixel + 1) * (sample index + 1) * random_number) (src/Device/kernels/CameraRays.h:155-160),
- *     the camera pass's jitter draws repeated by the first bounce (Megakernel.h:52-57), BSDF samples
- *     drawing from the path's own generator, and the camera hit shaded from the packed G-buffer
- *     (octahedral 24-bit normals, the view direction from the camera position, the material
- *     re-packed after its coat roughening; CameraRays.h:178-201, Megakernel.h:59-72). Each launch
- *     is one frame of the reference's CPU renderer: its random_number is the next output of a
- *     host Xorshift32 generator seeded with gbpt_render_settings.random_number (42 when 0, the
- *     reference's default), which the renderer advances once before each camera pass and once
- *     after each launch (CPURenderer::camera_rays_pass / post_sample_update,
- *     src/Renderer/CPURenderer.cpp:698-705 and 586-598). The environment map's direct lighting keeps its own
- *     draw position (before the emissive light sample) in both modes. */
+ *     the camera pass and the bounce loop each seeding their own generator from their own pass's
+ *     random_number (Megakernel.h:52-57), BSDF samples drawing from the path's generator, and the
+ *     camera hit shaded from the packed G-buffer (octahedral 24-bit normals, the view direction
+ *     from the camera position, the material re-packed after its coat roughening;
+ *     CameraRays.h:178-201, Megakernel.h:59-72). Each launch is one sample of the reference's GPU
+ *     renderer: a host Xorshift32 generator seeded with gbpt_render_settings.random_number (42
+ *     when 0, GPURenderer.cpp:750-751) gives one number to each pass in launch order, the G-buffer
+ *     pass first and the MegaKernel pass last (FillGBufferRenderPass.cpp:91,
+ *     MegaKernelRenderPass.cpp:53; with ReSTIR DI its passes draw theirs in between,
+ *     ReSTIRDIRenderPass.cpp:449-578). The environment map's direct lighting keeps its own draw
+ *     position (before the emissive light sample) in both modes. */
 enum { GBPT_RNG_PCG = 0, GBPT_RNG_REFERENCE = 1 };
 
 typedef struct gbpt_render_settings {

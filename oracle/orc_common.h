@@ -262,8 +262,9 @@ struct Settings
     int ris_m = 4, ris_n = 1;   // RIS light / BSDF candidates
     const OrcEnv* env = nullptr;  // ambient light / envmap (null: none)
     int rng_mode = 0;             // 0: PCG streams, 1: the reference's Xorshift32 + packed G-buffer
-    uint32_t random_number = 0;   // rng_mode 1: HIPRTRenderData::random_number of the frame
+    uint32_t random_number = 0;   // rng_mode 1: HIPRTRenderData::random_number of the camera pass
     int gbuffer_materials = 0;    // rng_mode 1, principled: offset of the camera-hit material table in pmats
+    uint32_t random_number_shade = 0;  // rng_mode 1: HIPRTRenderData::random_number of the MegaKernel pass
 };
 
 // ---------------------------------------------------------------------------------------------

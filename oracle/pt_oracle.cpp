@@ -427,16 +427,15 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
     const int x = pixel % st.width, y = pixel / st.width;
     Pcg rng = st.rng_mode ? parity_seed((uint32_t)pixel, (uint32_t)iteration, st.random_number)
                           : pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
-    const uint64_t seed0 = rng.state;
     float px = x + 0.5f, py = y + 0.5f;
     if (st.jitter)
     {
         px += rng.next() - 0.5f;
         py += rng.next() - 0.5f;
     }
-    // the reference's MegaKernel seeds its generator exactly as CameraRays did, so its first
-    // draws repeat the jitter's (Megakernel.h:52-57)
-    if (st.rng_mode) rng.state = seed0;
+    // the reference's MegaKernel seeds a new generator from its own pass's random number
+    // (Megakernel.h:52-57; MegaKernelRenderPass::launch_async draws it after the camera pass's)
+    if (st.rng_mode) rng = parity_seed((uint32_t)pixel, (uint32_t)iteration, st.random_number_shade);
     float xn = px / st.width * 2.0f - 1.0f, yn = py / st.height * 2.0f - 1.0f;
     V o = mat_point(st.iv, mk(0, 0, 0));
     V pv = mat_point(st.ip, mk(xn, yn, -1.0f));
@@ -603,16 +602,15 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
     const int x = pixel % st.width, y = pixel / st.width;
     Pcg rng = st.rng_mode ? parity_seed((uint32_t)pixel, (uint32_t)iteration, st.random_number)
                           : pcg_seed((uint32_t)pixel, (uint32_t)iteration, (uint32_t)st.seed);
-    const uint64_t seed0 = rng.state;
     float px = x + 0.5f, py = y + 0.5f;
     if (st.jitter)
     {
         px += rng.next() - 0.5f;
         py += rng.next() - 0.5f;
     }
-    // the reference's MegaKernel seeds its generator exactly as CameraRays did, so its first
-    // draws repeat the jitter's (Megakernel.h:52-57)
-    if (st.rng_mode) rng.state = seed0;
+    // the reference's MegaKernel seeds a new generator from its own pass's random number
+    // (Megakernel.h:52-57; MegaKernelRenderPass::launch_async draws it after the camera pass's)
+    if (st.rng_mode) rng = parity_seed((uint32_t)pixel, (uint32_t)iteration, st.random_number_shade);
     float xn = px / st.width * 2.0f - 1.0f, yn = py / st.height * 2.0f - 1.0f;
     V o = mat_point(st.iv, mk(0, 0, 0));
     V pv = mat_point(st.ip, mk(xn, yn, -1.0f));
@@ -853,7 +851,7 @@ void orc_pt_render(const float* tri_verts, int n_tris, const int* mat_of, const 
     Scene s{tri_verts, n_tris, mat_of, albedo, emission, emissive, n_emissive, alias_prob, alias_idx, power_sum, tri_normals};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
-                settings_i[10], settings_i[11], settings_i[12], env, settings_i[13], (uint32_t)settings_i[14], settings_i[15]};
+                settings_i[10], settings_i[11], settings_i[12], env, settings_i[13], (uint32_t)settings_i[14], settings_i[15], (uint32_t)settings_i[16]};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};
@@ -911,7 +909,7 @@ void orc_pt_render_principled(const float* tri_verts, int n_tris, const int* mat
     PScene ps{pmats, (bsdf_eval_fn)eval_fn, (bsdf_sample_fn)sample_fn};
     Settings st{settings_i[0], settings_i[1], settings_i[2], settings_i[3], settings_i[4], settings_i[5],
                 settings_i[6], settings_i[7], settings_i[8], settings_i[9], rr_clamp, inv_view, inv_proj,
-                settings_i[10], settings_i[11], settings_i[12], env, settings_i[13], (uint32_t)settings_i[14], settings_i[15]};
+                settings_i[10], settings_i[11], settings_i[12], env, settings_i[13], (uint32_t)settings_i[14], settings_i[15], (uint32_t)settings_i[16]};
     const int npix = st.width * st.height;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next{0};

@@ -299,7 +299,8 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
                    s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base,
                    getattr(s, "direct_lighting", 0), getattr(s, "ris_light_candidates", 4),
                    getattr(s, "ris_bsdf_candidates", 1), getattr(s, "rng_mode", 0),
-                   int(getattr(s, "random_number", 0)) & 0xFFFFFFFF, getattr(s, "gbuffer_materials", 0)],
+                   int(getattr(s, "random_number", 0)) & 0xFFFFFFFF, getattr(s, "gbuffer_materials", 0),
+                   int(getattr(s, "random_number_shade", 0)) & 0xFFFFFFFF],
                   np.uint32).view(np.int32)
     iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
     ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
@@ -343,7 +344,8 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
                    s.light_sampling, s.seed, 1 if s.do_jittering else 0, spp, iteration_base,
                    getattr(s, "direct_lighting", 0), getattr(s, "ris_light_candidates", 4),
                    getattr(s, "ris_bsdf_candidates", 1), getattr(s, "rng_mode", 0),
-                   int(getattr(s, "random_number", 0)) & 0xFFFFFFFF, getattr(s, "gbuffer_materials", 0)],
+                   int(getattr(s, "random_number", 0)) & 0xFFFFFFFF, getattr(s, "gbuffer_materials", 0),
+                   int(getattr(s, "random_number_shade", 0)) & 0xFFFFFFFF],
                   np.uint32).view(np.int32)
     iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
     ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
@@ -658,7 +660,8 @@ def _ref_render_lib(bsdf: str, light: str):
         lib.refr_scene_free.argtypes = [ctypes.c_void_p]
         lib.refr_scene_light_table.argtypes = [ctypes.c_void_p, _c_i, _c_i, _c_f, _c_i, _c_f]
         lib.refr_alias_table.argtypes = [_c_f, ctypes.c_int32, ctypes.c_float, _c_f, _c_i]
-        lib.refr_render.argtypes = [ctypes.c_void_p, _c_i, _c_f, _c_f, _c_f, ctypes.c_uint32, ctypes.c_uint32, _c_f,
+        lib.refr_render.argtypes = [ctypes.c_void_p, _c_i, _c_f, _c_f, _c_f, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, _c_f,
                                     _c_i, _c_f]
         lib.refr_pack_unpack_material.argtypes = [_c_f, _c_f]
         lib.refr_oct24.argtypes = [_c_f, _i64, _c_f, _u32p]
@@ -699,9 +702,11 @@ class RefRender:
         self._lib.refr_scene_light_table(self._h, None, _ptr(e, _c_i), _ptr(p, _c_f), _ptr(a, _c_i), ctypes.byref(s))
         return dict(emissive=e, probas=p, alias=a, power_sum=s.value)
 
-    def render(self, settings, sample_number: int, random_number: int, gbuffer: bool = False):
-        """One frame (one sample per pixel) -> (H, W, 3) float32; with gbuffer, also the camera
-        pass's first-hit primitives (H, W) and positions (H, W, 3)."""
+    def render(self, settings, sample_number: int, random_numbers, gbuffer: bool = False):
+        """One frame (one sample per pixel) -> (H, W, 3) float32; random_numbers = the camera
+        pass's and the MegaKernel pass's HIPRTRenderData::random_number. With gbuffer, also the
+        camera pass's first-hit primitives (H, W) and positions (H, W, 3)."""
+        rn_cam, rn_mk = (int(v) & 0xFFFFFFFF for v in random_numbers)
         s = settings
         si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0,
                        s.russian_roulette_min_depth, 1 if s.do_jittering else 0], np.int32)
@@ -712,7 +717,7 @@ class RefRender:
         prim = np.zeros((s.height, s.width), np.int32) if gbuffer else None
         pos = np.zeros((s.height, s.width, 3), np.float32) if gbuffer else None
         self._lib.refr_render(self._h, _ptr(si, _c_i), _ptr(sf, _c_f), _ptr(iv, _c_f), _ptr(ip, _c_f),
-                              int(sample_number) & 0xFFFFFFFF, int(random_number) & 0xFFFFFFFF, _ptr(out, _c_f),
+                              int(sample_number) & 0xFFFFFFFF, rn_cam, rn_mk, _ptr(out, _c_f),
                               _ptr(prim, _c_i), _ptr(pos, _c_f))
         return (out, prim, pos) if gbuffer else out
 

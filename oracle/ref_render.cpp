@@ -335,20 +335,24 @@ struct Frame
  * {russian_roulette_throughput_clamp}; inverse_view / inverse_projection row-major as
  * HIPRTCamera holds them; the camera position is the translation column of inverse_view
  * (what Camera::to_hiprt's row-vector product with it gives, src/Scene/Camera.cpp:24-25).
- * out_rgb (W*H*3): the frame's sample of every pixel. Also returns, when not NULL, the packed
- * G-buffer the camera pass wrote: gbuf_prim (W*H), gbuf_pos (W*H*3). */
+ * random_number_camera / random_number_megakernel: HIPRTRenderData::random_number of the two
+ * launches. out_rgb (W*H*3): the frame's sample of every pixel. Also returns, when not NULL, the
+ * packed G-buffer the camera pass wrote: gbuf_prim (W*H), gbuf_pos (W*H*3). */
 REF_EXPORT void refr_render(void* h, const int32_t* settings_i, const float* settings_f, const float* inverse_view,
-                            const float* inverse_projection, uint32_t sample_number, uint32_t random_number, float* out_rgb,
-                            int32_t* gbuf_prim, float* gbuf_pos)
+                            const float* inverse_projection, uint32_t sample_number, uint32_t random_number_camera,
+                            uint32_t random_number_megakernel, float* out_rgb, int32_t* gbuf_prim, float* gbuf_pos)
 {
     RefRenderScene* s = static_cast<RefRenderScene*>(h);
-    Frame f(s, settings_i, settings_f, inverse_view, inverse_projection, sample_number, random_number);
+    Frame f(s, settings_i, settings_f, inverse_view, inverse_projection, sample_number, random_number_camera);
     const int W = f.W, H = f.H;
     HIPRTRenderData& rd = f.rd;
 
 #pragma omp parallel for schedule(dynamic)
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) CameraRays(rd, x, y);
+    // each render pass sets its own random number before its launch (FillGBufferRenderPass and
+    // MegaKernelRenderPass::launch_async draw one each from the renderer's generator)
+    rd.random_number = random_number_megakernel;
 #pragma omp parallel for schedule(dynamic)
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) MegaKernel(rd, x, y);

@@ -4,8 +4,9 @@ render kernels — CameraRays + MegaKernel compiled from the reference's sources
 GBPT_RNG_REFERENCE mode sample by sample.
 
 Three scenes, each rendered for FRAMES frames of one sample per pixel with the reference's
-per-frame random numbers (the CPU renderer's Xorshift32 seeded with 42 draws one number before
-each camera pass and one after each sample, src/Renderer/CPURenderer.cpp:586-598, 698-705):
+per-pass random numbers as its GPU renderer draws them: the renderer's Xorshift32, seeded with 42
+(GPURenderer.cpp:750-751), gives one number to the G-buffer pass and one to the MegaKernel pass of
+every sample (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53):
   * lambert: the Cornell box (36 triangles, albedos 0.73 / red / green, light (17, 12, 4)),
     Lambertian BSDF override, uniform light sampling, 4 bounces, Russian roulette from bounce 3 —
     the configuration the path-tracing benchmark names (at 64 x 64 instead of 256 x 256);
@@ -49,12 +50,12 @@ GLASS = OPAQUE[:4] + [
 
 
 def frame_random_numbers(n, seed=42):
-    """The random number of each of the reference's first n frames."""
+    """(camera pass, MegaKernel pass) random numbers of each of the reference's first n frames."""
     x, out = seed, []
     for _ in range(n):
-        x = pyoracle.xorshift32(x)  # camera_rays_pass
-        out.append(x)
-        x = pyoracle.xorshift32(x)  # post_sample_update
+        cam = x = pyoracle.xorshift32(x)
+        mk = x = pyoracle.xorshift32(x)
+        out.append((cam, mk))
     return out
 
 

@@ -40,8 +40,8 @@ def test_lambert_oracle_matches_reference_megakernel_frames(oracle):
     emission = lam[:, 4:7]
     emissive = np.nonzero(np.any(emission[g["lambert_material_of"]] != 0, axis=1))[0].astype(np.int32)
     st = _settings(g, LIGHT_UNIFORM)
-    for k, rn in enumerate(g["random_numbers"]):
-        st.random_number = int(rn)
+    for k, (rn_cam, rn_mk) in enumerate(g["random_numbers"]):
+        st.random_number, st.random_number_shade = int(rn_cam), int(rn_mk)
         img = pyoracle.pt_render(_soup(g), g["lambert_material_of"], albedo, emission, emissive, None, None, 1.0, st, 1,
                                  iteration_base=k)
         ref = g["lambert"][k]
@@ -140,8 +140,8 @@ def test_principled_oracle_matches_reference_megakernel_frames(name):
     lt = r.light_table()
     st = _settings(g, LIGHT_POWER)
     st.gbuffer_materials = len(raw)
-    for k, rn in enumerate(g["random_numbers"]):
-        st.random_number = int(rn)
+    for k, (rn_cam, rn_mk) in enumerate(g["random_numbers"]):
+        st.random_number, st.random_number_shade = int(rn_cam), int(rn_mk)
         img = pyoracle.pt_render_principled(_soup(g), mo, pm, emission, emissive, lt["probas"], lt["alias"],
                                             lt["power_sum"], st, 1, iteration_base=k)
         ref = g[name][k]

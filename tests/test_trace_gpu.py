@@ -202,8 +202,8 @@ def test_watertight_against_moller_trumbore_on_benchmark_scene(cuda):
     o, d, lp = _dev(rays, cuda)
     mt = bvh.closest_cfg(o, d, lp, kernel=1, block=128).cpu().numpy()
     wt = bvh.closest_cfg(o, d, lp, kernel=1, block=128, triangle_test=1).cpu().numpy()
-    agree, edge, tie, other = classify(mesh, rays, mt, wt)
-    assert other == 0, (agree, edge, tie, other)
+    agree, edge, parallel, tie, other = classify(mesh, rays, mt, wt)
+    assert other == 0, (agree, edge, parallel, tie, other)
     assert agree >= 0.999 * len(rays), (agree, edge, tie)
     pts, nrm, prim = scenes.hit_points_normals(mesh, rays, mt)
     m = np.nonzero(prim >= 0)[0][::4]
@@ -211,5 +211,5 @@ def test_watertight_against_moller_trumbore_on_benchmark_scene(cuda):
     o, d, lp = _dev(b, cuda)
     mt = bvh.closest_cfg(o, d, lp, kernel=1, block=128).cpu().numpy()
     wt = bvh.closest_cfg(o, d, lp, kernel=1, block=128, triangle_test=1).cpu().numpy()
-    agree, edge, tie, other = classify(mesh, b, mt, wt)
-    assert other == 0, (agree, edge, tie, other)
+    agree, edge, parallel, tie, other = classify(mesh, b, mt, wt)
+    assert other == 0, (agree, edge, parallel, tie, other)
