@@ -378,6 +378,9 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                             bs_d = f4(wi, 1.0e35f - 1.0e-4f);
                             bsdf_pending = f4(f * fabsf(dot(ns, wi)), pdf);
                         }
+                        // the reference adds the BSDF candidate to the reservoir here, one draw
+                        // (RISReservoir::add_one_candidate, RIS_Reservoir.h:35-42)
+                        if (pb.ris_u) pb.ris_u[slot] = rng.next();
                     }
                 }
                 // ---- next-event estimation: light sample (sample_one_light_MIS, Lights.h:123-185) ----
@@ -597,6 +600,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                                 bs_d = f4(wi, 1.0e35f - 1.0e-4f);
                                 bsdf_pending = f4(f * fabsf(dot(ns, wi)), pdf);
                             }
+                            if (pb.ris_u) pb.ris_u[slot] = rng.next();
                         }
                     }
                     // ---- next-event estimation: light sample ----
@@ -893,9 +897,14 @@ __global__ void __launch_bounds__(128) resolve_kernel(SceneView s0, RenderConst 
                 if (N > 0)
                 {
                     wsum += w_b;
-                    Pcg32 prng = load_rng(rc, pb.rng[slot]);
-                    take_bsdf = prng.next() < w_b / wsum;
-                    store_rng(pb.rng + slot, prng);
+                    if (pb.ris_u)
+                        take_bsdf = pb.ris_u[slot] < w_b / wsum;
+                    else
+                    {
+                        Pcg32 prng = load_rng(rc, pb.rng[slot]);
+                        take_bsdf = prng.next() < w_b / wsum;
+                        store_rng(pb.rng + slot, prng);
+                    }
                 }
                 V3 add = v3(0.0f);
                 if (take_bsdf)

@@ -818,6 +818,7 @@ gbpt_status gbpt_renderer_create(const gbpt_scene* scene, const gbpt_render_sett
 
     DevMem& M = r->mem;
     alloc_paths(M, cap, st->bsdf == GBPT_BSDF_PRINCIPLED, false, r->pb, r->q, r->shadow, r->bsdfq);
+    if (st->rng_mode == GBPT_RNG_REFERENCE) r->pb.ris_u = M.alloc<float>(cap);
     const int64_t npix = (int64_t)st->width * st->height;
     r->acc32 = M.alloc<float>(3 * npix);
     r->acc64 = M.alloc<double>(3 * npix);

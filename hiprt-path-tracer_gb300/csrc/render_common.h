@@ -97,6 +97,8 @@ struct PathBuffers
     float4* ris;            // RIS vertex: throughput before the continuation (rgb) and the light
                             // candidates' weight sum (w); w = -0.5: RIS without light candidates,
                             // w = -1: not a RIS vertex
+    float* ris_u;           // GBPT_RNG_REFERENCE (null otherwise): the BSDF candidate's reservoir
+                            // draw, taken where the reference draws it (before the continuation)
     // guided rendering (null otherwise): the one-sample MIS pdf of each path's last continuation
     // when it was a guided continuation (which doubles as next-event estimation's BSDF technique),
     // else 0; emission found by the next extension ray is weighted against light sampling with it

@@ -52,9 +52,10 @@ namespace {
 // UCW = w_sum / p^ of the kept sample; a kept light sample is shaded through a shadow ray, a
 // kept BSDF sample without one. The balance heuristic leaves the count out of the numerator as
 // the reference's does (src/Device/includes/Sampling.h:103-116).
-// Random numbers (the GPU kernels' order): per light candidate the light sample's draws then the
-// reservoir draw; the BSDF candidate's sample draws; then the vertex's continuation draws; then
-// (in the GPU's resolve pass) the BSDF candidate's reservoir draw.
+// Random numbers: per light candidate the light sample's draws then the reservoir draw; the BSDF
+// candidate's sample draws; then, with the reference's generator (rng_mode 1), the BSDF
+// candidate's reservoir draw as the reference makes it; then the vertex's continuation draws; with
+// PCG streams the BSDF candidate's reservoir draw comes last (the GPU's resolve pass draws it).
 // ---------------------------------------------------------------------------------------------
 float bal(float a, float na, float b, float nb) { return a == 0.0f ? 0.0f : a / (na * a + nb * b); }
 
@@ -95,6 +96,7 @@ struct Ris
     V lp = mk(0, 0, 0), dir = mk(0, 0, 0), c_l = mk(0, 0, 0), c_b = mk(0, 0, 0);
     float dist = 0, t_l = 0, t_b = 0, w_l = 0, w_b = 0;
     int M = 0;
+    float u_b = -1.0f;  // the BSDF candidate's reservoir draw when drawn in the reference's place
 };
 
 // light candidates; eval(wi, pdf) -> f
@@ -164,7 +166,7 @@ V ris_finish(const Scene& s, const Settings& st, Pcg& rng, V P, int prim, V tp, 
     if (st.ris_n > 0)
     {
         wsum += r.w_b;
-        take_bsdf = rng.next() < r.w_b / wsum;
+        take_bsdf = (r.u_b >= 0.0f ? r.u_b : rng.next()) < r.w_b / wsum;
     }
     if (take_bsdf) return tp * r.c_b * (wsum / r.t_b);
     if (r.kept && r.t_l > 0.0f && !occluded(s, P, r.dir, prim, r.dist - 1.0e-4f)) return tp * r.c_l * (wsum / r.t_l);
@@ -491,6 +493,7 @@ V trace_path(const Scene& s, const Settings& st, int pixel, int iteration)
                 float pdf;
                 V f = lambert(albedo, dot(ns, wi), pdf);
                 ris_bsdf(s, st, P, ns, prim, wi, f, pdf, st.ris_n, ris);
+                if (st.rng_mode) ris.u_b = rng.next();
             }
         }
         else if (s.ne > 0)
@@ -718,6 +721,7 @@ V trace_path_principled(const Scene& s, const PScene& ps, const Settings& st, in
                 ps.sample(m, q, bsdf_seed(rng), out, &lobe);
             bsdf_seed_done(rng, out);
                 ris_bsdf(s, st, P, ns, prim, mk(out[0], out[1], out[2]), refr(mk(out[0], out[1], out[2]), mk(out[3], out[4], out[5])), out[6], st.ris_n, ris);
+                if (st.rng_mode) ris.u_b = rng.next();
             }
         }
         else if (s.ne > 0 && can_light_sample(m))

@@ -641,6 +641,7 @@ REF_RENDER_SO = {
     ("lambert", "uniform"): os.path.join(HERE, "_ref", "libref_render_lambert_uniform.so"),
     ("lambert", "power"): os.path.join(HERE, "_ref", "libref_render_lambert_power.so"),
     ("principled", "power"): os.path.join(HERE, "_ref", "libref_render_principled_power.so"),
+    ("principled", "power_ris"): os.path.join(HERE, "_ref", "libref_render_principled_power_ris.so"),
 }
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 
@@ -672,7 +673,7 @@ def _ref_render_lib(bsdf: str, light: str):
 class RefRender:
     """A scene in the reference's own CPU renderer (CameraRays + MegaKernel compiled from the
     reference's sources, one build per BSDF override 'lambert' / 'principled' and light sampling
-    'uniform' / 'power'). materials: (M, 64) gbpt_principled_material records (for 'lambert' only
+    'uniform' / 'power' / 'power_ris' (RIS direct lighting over light and BSDF candidates)). materials: (M, 64) gbpt_principled_material records (for 'lambert' only
     base colour and emission matter)."""
 
     def __init__(self, bsdf, light, positions, indices, material_of, materials, vertex_normals=None):
@@ -709,7 +710,8 @@ class RefRender:
         rn_cam, rn_mk = (int(v) & 0xFFFFFFFF for v in random_numbers)
         s = settings
         si = np.array([s.width, s.height, s.nb_bounces, 1 if s.do_russian_roulette else 0,
-                       s.russian_roulette_min_depth, 1 if s.do_jittering else 0], np.int32)
+                       s.russian_roulette_min_depth, 1 if s.do_jittering else 0,
+                       getattr(s, "ris_light_candidates", 4), getattr(s, "ris_bsdf_candidates", 1)], np.int32)
         sf = np.array([s.russian_roulette_throughput_clamp], np.float32)
         iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
         ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)

@@ -23,8 +23,10 @@
  * Compile-time options (-D on the command line, applied after the reference's option headers):
  *   REF_BSDF = BSDF_LAMBERTIAN (1) or BSDF_PRINCIPLED (3) -> BSDFOverride
  *   REF_LIGHT_BASE = LSS_BASE_UNIFORM (0) or LSS_BASE_POWER (1) -> DirectLightSamplingBaseStrategy
- * and always: DirectLightSamplingStrategy = LSS_MIS_LIGHT_BSDF (one light sample + one BSDF
- * sample, balance heuristic), energy compensation and microfacet regularization off (as the BSDF
+ *   REF_DIRECT = the DirectLightSamplingStrategy, LSS_MIS_LIGHT_BSDF (one light sample + one
+ *     BSDF sample, balance heuristic; the default here) or LSS_RIS_BSDF_AND_LIGHT (RIS over
+ *     light and BSDF candidates, src/Device/includes/RIS/RIS.h:83-255)
+ * and always: energy compensation and microfacet regularization off (as the BSDF
  * harness builds them), alpha testing off (render_settings.do_alpha_testing = false: untextured
  * materials would otherwise draw a random number per candidate hit), adaptive sampling and the
  * pixel noise threshold off, no envmap (ambient light NONE).
@@ -34,8 +36,11 @@
  */
 #include "HostDeviceCommon/KernelOptions/KernelOptions.h"
 
+#ifndef REF_DIRECT
+#define REF_DIRECT LSS_MIS_LIGHT_BSDF
+#endif
 #undef DirectLightSamplingStrategy
-#define DirectLightSamplingStrategy LSS_MIS_LIGHT_BSDF
+#define DirectLightSamplingStrategy REF_DIRECT
 #undef DirectLightSamplingBaseStrategy
 #define DirectLightSamplingBaseStrategy REF_LIGHT_BASE
 #undef BSDFOverride
@@ -227,13 +232,6 @@ REF_EXPORT void refr_alias_table(const float* power, int32_t n, float sum, float
     }
 }
 
-/* One frame: CameraRays then MegaKernel over every pixel. settings_i = {width, height,
- * nb_bounces, do_russian_roulette, russian_roulette_min_depth, do_jittering}, settings_f =
- * {russian_roulette_throughput_clamp}; inverse_view / inverse_projection row-major as
- * HIPRTCamera holds them; the camera position is the translation column of inverse_view
- * (what Camera::to_hiprt's row-vector product with it gives, src/Scene/Camera.cpp:24-25).
- * out_rgb (W*H*3): the frame's sample of every pixel. Also returns, when not NULL, the packed
- * G-buffer the camera pass wrote: gbuf_prim (W*H), gbuf_pos (W*H*3). */
 namespace {
 
 // The buffers of one frame and the render data pointing at them (CPURenderer's per-frame state).
@@ -310,6 +308,8 @@ struct Frame
         rs.enable_adaptive_sampling = false;
         rs.stop_pixel_noise_threshold = 0.0f;
         rs.do_update_status_buffers = false;
+        rs.ris_settings.number_of_light_candidates = settings_i[6];
+        rs.ris_settings.number_of_bsdf_candidates = settings_i[7];
 
         rd.world_settings.ambient_light_type = AmbientLightType::NONE;
 
@@ -331,7 +331,8 @@ struct Frame
 }  // namespace
 
 /* One frame: CameraRays then MegaKernel over every pixel. settings_i = {width, height,
- * nb_bounces, do_russian_roulette, russian_roulette_min_depth, do_jittering}, settings_f =
+ * nb_bounces, do_russian_roulette, russian_roulette_min_depth, do_jittering, RIS light
+ * candidates, RIS BSDF candidates}, settings_f =
  * {russian_roulette_throughput_clamp}; inverse_view / inverse_projection row-major as
  * HIPRTCamera holds them; the camera position is the translation column of inverse_view
  * (what Camera::to_hiprt's row-vector product with it gives, src/Scene/Camera.cpp:24-25).

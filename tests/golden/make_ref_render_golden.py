@@ -12,7 +12,9 @@ every sample (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53):
     the configuration the path-tracing benchmark names (at 64 x 64 instead of 256 x 256);
   * principled: the Cornell box with coated, glossy, anisotropic metal and mirror materials
     (no transmissive object), power light sampling;
-  * principled_glass: the same with a rough glass short box (nested-dielectric volume tracking).
+  * principled_glass: the same with a rough glass short box (nested-dielectric volume tracking);
+  * principled_ris: the principled scene with direct lighting by RIS over 4 light and 1 BSDF
+    candidates (LSS_RIS_BSDF_AND_LIGHT, the reference's default strategy, RIS.h:83-255).
 Each frame image is the frame's sample (float32 H x W x 3); the scene arrays and settings are stored
 with it, so the GPU test needs nothing else.
 Usage (where the reference tree is present):  python tests/golden/make_ref_render_golden.py
@@ -68,13 +70,13 @@ class Settings:
         self.russian_roulette_throughput_clamp = 0.0
         self.do_jittering = True
         self.light_sampling = light
+        self.ris_light_candidates, self.ris_bsdf_candidates = 4, 1
         self.inverse_view, self.inverse_projection = look_at_camera((2.75, 2.75, -8.0), (2.75, 2.75, 0.0),
                                                                     vfov_deg=40.0, aspect=1.0)
 
 
 def render(bsdf, light, mesh, mat_of, mats, st):
-    r = pyoracle.RefRender(bsdf, "uniform" if light == LIGHT_UNIFORM else "power", mesh.positions, mesh.indices,
-                           mat_of, mats)
+    r = pyoracle.RefRender(bsdf, light, mesh.positions, mesh.indices, mat_of, mats)
     frames = np.stack([r.render(st, k, rn) for k, rn in enumerate(frame_random_numbers(FRAMES))])
     return frames, r.light_table()
 
@@ -87,15 +89,16 @@ def main():
     st = Settings(LIGHT_UNIFORM)
     out["inverse_view"], out["inverse_projection"] = st.inverse_view, st.inverse_projection
     lam = np.stack([M.pack(base_color=tuple(cb.albedo[i]), emission=tuple(cb.emission[i])) for i in range(4)])
-    img, _ = render("lambert", LIGHT_UNIFORM, cb.mesh, cb.material_of_triangle, lam, st)
+    img, _ = render("lambert", "uniform", cb.mesh, cb.material_of_triangle, lam, st)
     out.update(lambert_materials=lam, lambert_material_of=cb.material_of_triangle, lambert=img)
     print(f"lambert: mean {img.mean():.5f}")
     mat_of = cb.material_of_triangle.copy()
     mat_of[10:22] = 4
     mat_of[22:34] = 5
-    for name, mats in (("principled", OPAQUE), ("principled_glass", GLASS)):
+    for name, mats, light in (("principled", OPAQUE, "power"), ("principled_glass", GLASS, "power"),
+                              ("principled_ris", OPAQUE, "power_ris")):
         raw = M.pack_many(mats)
-        img, lt = render("principled", LIGHT_POWER, cb.mesh, mat_of, raw, Settings(LIGHT_POWER))
+        img, lt = render("principled", light, cb.mesh, mat_of, raw, Settings(LIGHT_POWER))
         out.update({f"{name}_materials": raw, f"{name}_material_of": mat_of, name: img,
                     f"{name}_power_sum": np.float32(lt["power_sum"])})
         print(f"{name}: mean {img.mean():.5f}")

@@ -3,10 +3,10 @@ REFERENCE's own CPU kernels (CameraRays + MegaKernel compiled from the reference
 tests/golden/ref_render_cornell.npz, made by tests/golden/make_ref_render_golden.py).
 
 In that mode every path draws the reference's random numbers in the reference's order (Xorshift32
-seeded by wang_hash((pixel + 1)(sample + 1) random_number), the camera jitter's draws repeated at
-the camera hit, BSDF samples continuing the path's generator), the camera hit is shaded from the
-reference's packed G-buffer, and the scene stores the reference's 8-bit packed materials, so the
-GPU reproduces each of the reference's frames pixel by pixel. The tolerance is 1e-3 relative per
+seeded by wang_hash((pixel + 1)(sample + 1) random_number) with one random_number per pass as the
+reference's GPU renderer draws them, BSDF samples continuing the path's generator), the camera hit
+is shaded from the reference's packed G-buffer, and the scene stores the reference's 8-bit packed
+materials, so the GPU reproduces each of the reference's frames pixel by pixel. The tolerance is 1e-3 relative per
 pixel: the GPU contracts multiply-adds (and uses its own sqrt/sin/cos), so a path that crosses a
 branch threshold (a lobe choice, Russian roulette, a grazing hit) on one side only diverges; the
 test requires 97% of the pixels of every frame to agree."""
@@ -17,8 +17,8 @@ import pytest
 import torch
 
 import gbpt
-from gbpt.render import (BSDF_LAMBERTIAN, BSDF_PRINCIPLED, LIGHT_POWER, LIGHT_UNIFORM, MATERIALS_PACKED,
-                         RNG_REFERENCE, RenderSettings)
+from gbpt.render import (BSDF_LAMBERTIAN, BSDF_PRINCIPLED, DIRECT_RIS, LIGHT_POWER, LIGHT_UNIFORM,
+                         MATERIALS_PACKED, RNG_REFERENCE, RenderSettings)
 
 pytestmark = pytest.mark.gpu
 
@@ -65,17 +65,22 @@ def test_lambert_cornell_matches_reference_megakernel(cuda):
     assert abs(gpu.mean() - ref.mean()) <= 2e-3 * ref.mean(), (gpu.mean(), ref.mean())
 
 
-@pytest.mark.parametrize("name", ["principled", "principled_glass"])
+@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris"])
 def test_principled_cornell_matches_reference_megakernel(cuda, name):
     """Coated, glossy dielectric, anisotropic metal, metallic-blend and mirror materials (and a
     rough glass box entered and left through the nested-dielectric volume stack), power light
-    sampling, against the reference's MegaKernel with its own principled BSDF."""
+    sampling, against the reference's MegaKernel with its own principled BSDF; principled_ris
+    with RIS direct lighting over 4 light and 1 BSDF candidates (LSS_RIS_BSDF_AND_LIGHT)."""
     g = np.load(GOLDEN)
     scene = gbpt.Scene(g["positions"], g["indices"], g[f"{name}_material_of"], principled=g[f"{name}_materials"],
                        material_packing=MATERIALS_PACKED)
     lt = scene.light_table()
     assert abs(lt["power_sum"] - float(g[f"{name}_power_sum"])) <= 1e-6 * lt["power_sum"]
-    gpu = _frames(scene, _settings(g, BSDF_PRINCIPLED, LIGHT_POWER), int(g["frames"]))
+    st = _settings(g, BSDF_PRINCIPLED, LIGHT_POWER)
+    if name.endswith("_ris"):
+        st = RenderSettings(**{**st.__dict__, "direct_lighting": DIRECT_RIS, "ris_light_candidates": 4,
+                               "ris_bsdf_candidates": 1})
+    gpu = _frames(scene, st, int(g["frames"]))
     ref = g[name]
     frac = _agreement(gpu, ref)
     assert frac.min() >= 0.97, frac

@@ -122,12 +122,13 @@ def test_alias_restatement_matches_reference_utils():
 
 
 @REF
-@pytest.mark.parametrize("name", ["principled", "principled_glass"])
+@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris"])
 def test_principled_oracle_matches_reference_megakernel_frames(name):
     """The restated estimator with the reference's own BSDF (through callbacks that hand back the
     generator's state) on the principled Cornell box, with and without a rough glass box whose
     faces wind inwards: only the restated nested-dielectric stack (volume parity, not face
-    orientation) enters and leaves it as the reference does."""
+    orientation) enters and leaves it as the reference does; and with RIS direct lighting over
+    4 light and 1 BSDF candidates (the reference's default strategy)."""
     g = _golden()
     raw = g[f"{name}_materials"]
     q = pyoracle.ref_pack_unpack_material(raw)
@@ -140,6 +141,8 @@ def test_principled_oracle_matches_reference_megakernel_frames(name):
     lt = r.light_table()
     st = _settings(g, LIGHT_POWER)
     st.gbuffer_materials = len(raw)
+    st.direct_lighting = 1 if name.endswith("_ris") else 0
+    st.ris_light_candidates, st.ris_bsdf_candidates = 4, 1
     for k, (rn_cam, rn_mk) in enumerate(g["random_numbers"]):
         st.random_number, st.random_number_shade = int(rn_cam), int(rn_mk)
         img = pyoracle.pt_render_principled(_soup(g), mo, pm, emission, emissive, lt["probas"], lt["alias"],
