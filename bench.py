@@ -139,16 +139,19 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+TRAVERSAL_SOURCES = ("bvh.h", "bvh_build.cpp", "trace.cu", "trace_core.h", "trace_kernels.h")
+
+
 def kernel_source_hash():
-    """SHA-256 (16 hex digits) of the CUDA and C++ sources of libgbpt, in file-name order."""
+    """SHA-256 (16 hex digits) of the sources that make the traversal kernels and the BVH they
+    walk (trace.cu and the headers it includes, the BVH builder), in file-name order."""
     import hashlib
     csrc = os.path.join(REPO, "hiprt-path-tracer_gb300", "csrc")
     h = hashlib.sha256()
-    for name in sorted(os.listdir(csrc)):
-        if name.endswith((".cu", ".h", ".cpp")):
-            h.update(name.encode())
-            with open(os.path.join(csrc, name), "rb") as f:
-                h.update(f.read())
+    for name in TRAVERSAL_SOURCES:
+        h.update(name.encode())
+        with open(os.path.join(csrc, name), "rb") as f:
+            h.update(f.read())
     return h.hexdigest()[:16]
 
 

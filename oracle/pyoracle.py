@@ -642,6 +642,7 @@ REF_RENDER_SO = {
     ("lambert", "power"): os.path.join(HERE, "_ref", "libref_render_lambert_power.so"),
     ("principled", "power"): os.path.join(HERE, "_ref", "libref_render_principled_power.so"),
     ("principled", "power_ris"): os.path.join(HERE, "_ref", "libref_render_principled_power_ris.so"),
+    ("principled", "power_restir"): os.path.join(HERE, "_ref", "libref_render_principled_power_restir.so"),
 }
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 
@@ -722,6 +723,65 @@ class RefRender:
                               int(sample_number) & 0xFFFFFFFF, rn_cam, rn_mk, _ptr(out, _c_f),
                               _ptr(prim, _c_i), _ptr(pos, _c_f))
         return (out, prim, pos) if gbuffer else out
+
+
+class RefRestir(RefRender):
+    """ReSTIR DI frames of the reference's own kernels (build 'power_restir': CameraRays,
+    ReSTIR_DI_InitialCandidates / TemporalReuse / SpatialReuse and the MegaKernel's ReSTIR DI
+    final shading, in the GPU renderer's pass order). Keeps the reference's per-frame state (both
+    G-buffers, the reservoir buffers and which one was last frame's output) across frames."""
+
+    def __init__(self, width, height, positions, indices, material_of, materials, vertex_normals=None):
+        super().__init__("principled", "power_restir", positions, indices, material_of, materials, vertex_normals)
+        lib = self._lib
+        if not getattr(lib, "_restir_sig", False):
+            lib.refr_restir_create.restype = ctypes.c_void_p
+            lib.refr_restir_create.argtypes = [ctypes.c_int32, ctypes.c_int32]
+            lib.refr_restir_free.argtypes = [ctypes.c_void_p]
+            lib.refr_restir_frame.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _c_i, _c_f, _c_f, _c_f, _c_f, _c_f,
+                                              ctypes.c_uint32, _u32p, _c_f, _c_f, _c_f, _c_f, _c_i, _c_f]
+            lib._restir_sig = True
+        self.width, self.height = int(width), int(height)
+        self._st = lib.refr_restir_create(self.width, self.height)
+
+    def __del__(self):
+        st = getattr(self, "_st", None)
+        if st:
+            self._lib.refr_restir_free(st)
+            self._st = None
+        super().__del__()
+
+    def frame(self, settings, restir, sample_number, random_numbers, prev_inverse_view, prev_view_projection):
+        """One frame -> dict(image (H, W, 3), initial / temporal / final reservoirs (H*W, 8) float32
+        records, prim (H, W), pos (H, W, 3)). restir: dict with light_candidates, bsdf_candidates,
+        do_temporal, temporal_search_count, temporal_search_radius, do_spatial, spatial_passes,
+        spatial_neighbors, spatial_radius, m_cap, use_confidence_weights, normal_similarity_cos,
+        plane_distance_threshold. random_numbers: the passes' random numbers in launch order."""
+        s, r = settings, restir
+        W, H = self.width, self.height
+        si = np.array([W, H, s.nb_bounces, 1 if s.do_russian_roulette else 0, s.russian_roulette_min_depth,
+                       1 if s.do_jittering else 0, getattr(s, "ris_light_candidates", 4),
+                       getattr(s, "ris_bsdf_candidates", 1), r["light_candidates"], r["bsdf_candidates"],
+                       r["do_temporal"], r["temporal_search_count"], r["temporal_search_radius"], r["do_spatial"],
+                       r["spatial_passes"], r["spatial_neighbors"], r["spatial_radius"], r["m_cap"],
+                       r["use_confidence_weights"]], np.int32)
+        sf = np.array([s.russian_roulette_throughput_clamp, r["normal_similarity_cos"],
+                       r["plane_distance_threshold"]], np.float32)
+        iv = np.ascontiguousarray(s.inverse_view, np.float32).reshape(16)
+        ip = np.ascontiguousarray(s.inverse_projection, np.float32).reshape(16)
+        piv = np.ascontiguousarray(prev_inverse_view, np.float32).reshape(16)
+        pvp = np.ascontiguousarray(prev_view_projection, np.float32).reshape(16)
+        rn = np.ascontiguousarray(np.asarray(random_numbers, np.uint64) & 0xFFFFFFFF, np.uint32)
+        out = dict(image=np.zeros((H, W, 3), np.float32), prim=np.zeros((H, W), np.int32),
+                   pos=np.zeros((H, W, 3), np.float32))
+        for k in ("initial", "temporal", "final"):
+            out[k] = np.zeros((H * W, 8), np.float32)
+        self._lib.refr_restir_frame(self._h, self._st, _ptr(si, _c_i), _ptr(sf, _c_f), _ptr(iv, _c_f), _ptr(ip, _c_f),
+                                    _ptr(piv, _c_f), _ptr(pvp, _c_f), int(sample_number) & 0xFFFFFFFF,
+                                    _ptr(rn, _u32p), _ptr(out["image"], _c_f), _ptr(out["initial"], _c_f),
+                                    _ptr(out["temporal"], _c_f), _ptr(out["final"], _c_f), _ptr(out["prim"], _c_i),
+                                    _ptr(out["pos"], _c_f))
+        return out
 
 
 def ref_pack_unpack_material(materials: np.ndarray) -> np.ndarray:

@@ -52,6 +52,11 @@
 
 #include "Device/kernels/CameraRays.h"
 #include "Device/kernels/Megakernel.h"
+#if REF_RESTIR
+#include "Device/kernels/ReSTIR/DI/InitialCandidates.h"
+#include "Device/kernels/ReSTIR/DI/SpatialReuse.h"
+#include "Device/kernels/ReSTIR/DI/TemporalReuse.h"
+#endif
 #include "HostDeviceCommon/Material/MaterialCPU.h"
 #include "Renderer/BVH.h"
 #include "Renderer/CPUDataStructures/MaterialPackedSoACPUData.h"
@@ -437,3 +442,215 @@ REF_EXPORT void refr_oct24(const float* in, int64_t n, float* out, uint32_t* pac
     }
 }
 
+
+#if REF_RESTIR
+/* ReSTIR DI frames (build with REF_DIRECT = LSS_RESTIR_DI): the reference's GPU renderer's pass
+ * sequence per frame (FillGBufferRenderPass, ReSTIRDIRenderPass::launch_async and its configure_*
+ * functions, src/Renderer/RenderPasses/ReSTIRDIRenderPass.cpp:440-600, MegaKernelRenderPass),
+ * run on the CPU kernels pixel by pixel:
+ *   CameraRays (G-buffer; the previous frame's kept in g_buffer_prev_frame),
+ *   ReSTIR_DI_InitialCandidates -> initial reservoirs,
+ *   ReSTIR_DI_TemporalReuse (input: last frame's output; output: the initial buffer when spatial
+ *     reuse follows, else the spatial buffer of the frame's parity),
+ *   ReSTIR_DI_SpatialReuse per pass (pass 0: temporal/initial output -> spatial 1, then ping-pong),
+ *   MegaKernel (ReSTIR DI final shading at the camera hit; RIS at later bounces, the reference's
+ *     ReSTIR_DI_LaterBouncesSamplingStrategy default).
+ * The camera moves (render_settings.accumulate = false): the temporal pass backprojects through
+ * prev_camera.view_projection. Reservoirs are exported as 8 words per pixel: point xyz, target
+ * function, triangle, (M << 9) | flags, weight sum, UCW. */
+namespace {
+
+struct RefRestirState
+{
+    int W = 0, H = 0;
+    bool first = true, odd_frame = false;
+    std::vector<DevicePackedEffectiveMaterial> mat, pmat;
+    std::vector<Octahedral24BitNormalPadded32b> gn, sn, pgn, psn;
+    std::vector<float3> pos, ppos;
+    std::vector<int> prim, pprim;
+    std::vector<ReSTIRDIReservoir> initial, spatial1, spatial2;
+    ReSTIRDIReservoir* last_output = nullptr;
+};
+
+void export_reservoirs(const std::vector<ReSTIRDIReservoir>& in, const ReSTIRDIReservoir* src, float* out)
+{
+    if (!out || !src) return;
+    for (size_t i = 0; i < in.size(); i++)
+    {
+        const ReSTIRDIReservoir& r = src[i];
+        float* o = out + 8 * i;
+        o[0] = r.sample.point_on_light_source.x;
+        o[1] = r.sample.point_on_light_source.y;
+        o[2] = r.sample.point_on_light_source.z;
+        o[3] = r.sample.target_function;
+        int32_t t = r.sample.emissive_triangle_index, mf = (r.M << 9) | (int32_t)(r.sample.flags & 0x1FF);
+        std::memcpy(o + 4, &t, 4);
+        std::memcpy(o + 5, &mf, 4);
+        o[6] = r.weight_sum;
+        o[7] = r.UCW;
+    }
+}
+
+}  // namespace
+
+REF_EXPORT void* refr_restir_create(int32_t W, int32_t H)
+{
+    RefRestirState* st = new RefRestirState();
+    const size_t n = (size_t)W * H;
+    st->W = W;
+    st->H = H;
+    st->mat.resize(n);
+    st->pmat.resize(n);
+    st->gn.resize(n);
+    st->sn.resize(n);
+    st->pgn.resize(n);
+    st->psn.resize(n);
+    st->pos.assign(n, make_float3(0.0f, 0.0f, 0.0f));
+    st->ppos.assign(n, make_float3(0.0f, 0.0f, 0.0f));
+    st->prim.assign(n, -1);
+    st->pprim.assign(n, -1);
+    st->initial.resize(n);
+    st->spatial1.resize(n);
+    st->spatial2.resize(n);
+    return st;
+}
+
+REF_EXPORT void refr_restir_free(void* h) { delete static_cast<RefRestirState*>(h); }
+
+/* One frame. settings_i: refr_render's eight, then {light candidates, BSDF candidates, temporal
+ * reuse on, temporal search count, temporal search radius, spatial reuse on, spatial passes,
+ * spatial neighbours, spatial radius, M-cap, confidence weights}; settings_f: {RR throughput
+ * clamp, normal similarity cosine, plane distance threshold}. prev_inverse_view / prev_vp: the
+ * previous frame's camera (position from the translation column; view-projection row-major).
+ * random_numbers: the passes' HIPRTRenderData::random_number in launch order: camera, initial,
+ * [temporal, permutation bits], spatial pass 0..P-1, MegaKernel. Any output may be NULL:
+ * out_rgb (W*H*3), reservoirs after the initial / temporal / last spatial pass (W*H*8), the final
+ * (shaded) reservoirs, the G-buffer's primitives and positions. */
+REF_EXPORT void refr_restir_frame(void* scene, void* state, const int32_t* settings_i, const float* settings_f,
+                                  const float* inverse_view, const float* inverse_projection,
+                                  const float* prev_inverse_view, const float* prev_vp, uint32_t sample_number,
+                                  const uint32_t* random_numbers, float* out_rgb, float* res_initial, float* res_temporal,
+                                  float* res_final, int32_t* gbuf_prim, float* gbuf_pos)
+{
+    RefRenderScene* s = static_cast<RefRenderScene*>(scene);
+    RefRestirState* st = static_cast<RefRestirState*>(state);
+    Frame f(s, settings_i, settings_f, inverse_view, inverse_projection, sample_number, random_numbers[0]);
+    const int W = f.W, H = f.H;
+    HIPRTRenderData& rd = f.rd;
+    HIPRTRenderSettings& rs = rd.render_settings;
+    rs.need_to_reset = st->first;
+    rs.accumulate = false;
+
+    rd.g_buffer.materials = st->mat.data();
+    rd.g_buffer.geometric_normals = st->gn.data();
+    rd.g_buffer.shading_normals = st->sn.data();
+    rd.g_buffer.primary_hit_position = st->pos.data();
+    rd.g_buffer.first_hit_prim_index = st->prim.data();
+    rd.g_buffer_prev_frame.materials = st->pmat.data();
+    rd.g_buffer_prev_frame.geometric_normals = st->pgn.data();
+    rd.g_buffer_prev_frame.shading_normals = st->psn.data();
+    rd.g_buffer_prev_frame.primary_hit_position = st->ppos.data();
+    rd.g_buffer_prev_frame.first_hit_prim_index = st->pprim.data();
+
+    HIPRTCamera prev = rd.current_camera;
+    prev.position = make_float3(prev_inverse_view[3], prev_inverse_view[7], prev_inverse_view[11]);
+    std::memcpy(&prev.inverse_view, prev_inverse_view, 16 * sizeof(float));
+    std::memcpy(&prev.view_projection, prev_vp, 16 * sizeof(float));
+    rd.prev_camera = prev;
+
+    ReSTIRDISettings& rds = rs.restir_di_settings;
+    rds.initial_candidates.number_of_initial_light_candidates = settings_i[8];
+    rds.initial_candidates.number_of_initial_bsdf_candidates = settings_i[9];
+    rds.common_temporal_pass.do_temporal_reuse_pass = settings_i[10] != 0;
+    rds.common_temporal_pass.max_neighbor_search_count = settings_i[11];
+    rds.common_temporal_pass.neighbor_search_radius = settings_i[12];
+    rds.common_spatial_pass.do_spatial_reuse_pass = settings_i[13] != 0;
+    rds.common_spatial_pass.number_of_passes = settings_i[14];
+    rds.common_spatial_pass.reuse_neighbor_count = settings_i[15];
+    rds.common_spatial_pass.neighbor_visibility_count = settings_i[15];
+    rds.common_spatial_pass.reuse_radius = settings_i[16];
+    rds.common_spatial_pass.auto_reuse_radius = false;
+    rds.m_cap = settings_i[17];
+    rds.use_confidence_weights = settings_i[18] != 0;
+    rds.neighbor_similarity_settings.normal_similarity_angle_precomp = settings_f[1];
+    rds.neighbor_similarity_settings.plane_distance_threshold = settings_f[2];
+    rds.light_presampling.light_samples = nullptr;
+    const int passes = rds.common_spatial_pass.do_spatial_reuse_pass ? rds.common_spatial_pass.number_of_passes : 0;
+    const bool temporal = rds.common_temporal_pass.do_temporal_reuse_pass;
+    if (!st->last_output) st->last_output = st->spatial2.data();
+
+    auto each_pixel = [&](auto&& fn) {
+#pragma omp parallel for schedule(dynamic)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) fn(x, y);
+    };
+    int k = 0;
+    rd.random_number = random_numbers[k++];
+    each_pixel([&](int x, int y) { CameraRays(rd, x, y); });
+
+    rd.random_number = random_numbers[k++];
+    rds.initial_candidates.output_reservoirs = st->initial.data();
+    each_pixel([&](int x, int y) { ReSTIR_DI_InitialCandidates(rd, x, y); });
+    export_reservoirs(st->initial, st->initial.data(), res_initial);
+
+    ReSTIRDIReservoir* out = st->initial.data();
+    if (temporal)
+    {
+        rd.random_number = random_numbers[k++];
+        rds.common_temporal_pass.permutation_sampling_random_bits = random_numbers[k++];
+        rds.temporal_pass.input_reservoirs = st->last_output;
+        rds.temporal_pass.output_reservoirs =
+            passes > 0 ? st->initial.data() : (st->odd_frame ? st->spatial1.data() : st->spatial2.data());
+        each_pixel([&](int x, int y) { ReSTIR_DI_TemporalReuse(rd, x, y); });
+        out = rds.temporal_pass.output_reservoirs;
+        export_reservoirs(st->initial, out, res_temporal);
+    }
+    for (int p = 0; p < passes; p++)
+    {
+        rd.random_number = random_numbers[k++];
+        rds.common_spatial_pass.spatial_pass_index = p;
+        if (p == 0)
+        {
+            rds.spatial_pass.input_reservoirs = out;
+            rds.spatial_pass.output_reservoirs = st->spatial1.data();
+        }
+        else if ((p & 1) == 0)
+        {
+            rds.spatial_pass.input_reservoirs = st->spatial2.data();
+            rds.spatial_pass.output_reservoirs = st->spatial1.data();
+        }
+        else
+        {
+            rds.spatial_pass.input_reservoirs = st->spatial1.data();
+            rds.spatial_pass.output_reservoirs = st->spatial2.data();
+        }
+        each_pixel([&](int x, int y) { ReSTIR_DI_SpatialReuse(rd, x, y); });
+        out = rds.spatial_pass.output_reservoirs;
+    }
+    rds.restir_output_reservoirs = out;
+    st->last_output = out;
+    st->odd_frame = !st->odd_frame;
+
+    rd.random_number = random_numbers[k++];
+    each_pixel([&](int x, int y) { MegaKernel(rd, x, y); });
+    export_reservoirs(st->initial, out, res_final);
+    st->first = false;
+
+    for (int i = 0; i < W * H; i++)
+    {
+        if (out_rgb)
+        {
+            out_rgb[3 * i] = f.accum[i].r;
+            out_rgb[3 * i + 1] = f.accum[i].g;
+            out_rgb[3 * i + 2] = f.accum[i].b;
+        }
+        if (gbuf_prim) gbuf_prim[i] = st->prim[i];
+        if (gbuf_pos)
+        {
+            gbuf_pos[3 * i] = st->pos[i].x;
+            gbuf_pos[3 * i + 1] = st->pos[i].y;
+            gbuf_pos[3 * i + 2] = st->pos[i].z;
+        }
+    }
+}
+#endif
