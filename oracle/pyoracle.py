@@ -511,7 +511,8 @@ def _restir_lib():
     lib = _pt_lib()
     if not getattr(lib, "_restir_sigs", False):
         lib.orc_restir_gbuffer.argtypes = [_c_f, ctypes.c_int, _c_i, _c_f, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                           ctypes.c_int, ctypes.c_int, _c_f, _c_f, _c_f, ctypes.c_int]
+                                           ctypes.c_int, ctypes.c_int, _c_f, _c_f, _c_f, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_uint32]
         lib.orc_restir_pass.argtypes = [ctypes.c_int, _c_f, ctypes.c_int, _c_i, _c_f, _c_i, ctypes.c_int, _c_f, _c_i,
                                         ctypes.c_float, _c_f, ctypes.c_void_p, ctypes.c_void_p, _c_i, _c_f, _c_f,
                                         _c_f, _c_f, _c_f, _c_f, _c_f, ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
@@ -524,8 +525,10 @@ def _restir_lib():
 
 
 def restir_gbuffer(soup, material_of, pmats, width, height, seed, frame, jitter, inverse_view, inverse_projection,
-                   nthreads=0) -> np.ndarray:
-    """G-buffer of the camera hits, (W*H, 12) float32 (int fields as bit patterns)."""
+                   nthreads=0, random_number=None) -> np.ndarray:
+    """G-buffer of the camera hits, (W*H, 12) float32 (int fields as bit patterns). random_number:
+    the reference's camera pass instead of the PCG jitter (frame = its sample number), with the
+    reference's packed normals."""
     lib = _restir_lib()
     soup = np.ascontiguousarray(soup, np.float32)
     mo = np.ascontiguousarray(material_of, np.int32)
@@ -534,7 +537,8 @@ def restir_gbuffer(soup, material_of, pmats, width, height, seed, frame, jitter,
     ip = np.ascontiguousarray(inverse_projection, np.float32).reshape(16)
     gb = np.zeros((width * height, 12), np.float32)
     lib.orc_restir_gbuffer(_ptr(soup, _c_f), soup.shape[0], _ptr(mo, _c_i), _ptr(pm, _c_f), width, height, seed, frame,
-                           1 if jitter else 0, _ptr(iv, _c_f), _ptr(ip, _c_f), _ptr(gb, _c_f), nthreads)
+                           1 if jitter else 0, _ptr(iv, _c_f), _ptr(ip, _c_f), _ptr(gb, _c_f), nthreads,
+                           0 if random_number is None else 1, 0 if random_number is None else int(random_number) & 0xFFFFFFFF)
     return gb
 
 
@@ -576,7 +580,9 @@ def restir_pass(pass_kind, scene, pmats, settings_i, settings_f, prev_vp, gb, gb
     ap = np.ascontiguousarray(scene["alias_prob"], np.float32)
     ai = np.ascontiguousarray(scene["alias_idx"], np.int32)
     pm = np.ascontiguousarray(pmats, np.float32)
-    si = np.ascontiguousarray(settings_i, np.int32)
+    si = np.zeros(25, np.int32)
+    si_in = np.array([int(v) & 0xFFFFFFFF for v in settings_i], np.uint32).view(np.int32)
+    si[:len(si_in)] = si_in
     sf = np.ascontiguousarray(settings_f, np.float32)
     vp = np.ascontiguousarray(prev_vp if prev_vp is not None else np.eye(4), np.float32).reshape(16)
     n = int(si[0]) * int(si[1])

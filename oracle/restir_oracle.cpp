@@ -16,11 +16,22 @@
  *   - spatial reuse with pairwise MIS and confidence weights (SpatialReuse.h:43-322,
  *     SpatialMISWeight.h:100-160, UtilsSpatial.h:77-220, NeighborSimilarity.h:34-84);
  *   - final shading of the reservoir (src/Device/includes/ReSTIR/DI/FinalShading.h:13-85).
- * Random numbers: one PCG32 stream per pixel and pass, pcg_seed(pixel, frame * 16 + pass, seed)
- * with pass 1 = initial, 2 = temporal, 3 + p = spatial pass p; each BSDF sample is seeded with one
- * 32-bit draw; spatial neighbour offsets from a Xorshift32 seeded per frame and pass for all
- * pixels. These are the GPU kernels' streams (hiprt-path-tracer_gb300/csrc/restir.cu), so the
- * oracle and the kernels select the same samples.
+ * Random numbers, rng_mode 0: one PCG32 stream per pixel and pass, pcg_seed(pixel, frame * 16 +
+ * pass, seed) with pass 1 = initial, 2 = temporal, 3 + p = spatial pass p; each BSDF sample is
+ * seeded with one 32-bit draw; spatial neighbour offsets from a Xorshift32 seeded per frame and
+ * pass for all pixels. These are the GPU kernels' streams (hiprt-path-tracer_gb300/csrc/
+ * restir.cu), so the oracle and the kernels select the same samples.
+ * rng_mode 1 (the reference's generator and draw order): each pass seeds a Xorshift32 per pixel
+ * with wang_hash((pixel + 1) (sample + 1) random_number) from its own random number
+ * (InitialCandidates.h:500-505, TemporalReuse.h:69-74, SpatialReuse.h:62-69); a light candidate
+ * first draws the envmap-or-light choice (sample_fresh_light_candidate, InitialCandidates.h:100);
+ * BSDF samples draw from the pixel's generator; a spatial pass seeds each pixel's neighbour
+ * generator with one draw of the pixel's (setup_adaptive_directional_spatial_reuse,
+ * UtilsSpatial.h:17-22); the G-buffer holds octahedral 24-bit normals and the packed camera-hit
+ * materials (offset 'gbuffer_materials' in the material table); the temporal heuristics compare
+ * against the centre's shading normal (TemporalReuse.h:81-82) and a previous-frame surface's view
+ * direction runs from the previous camera to the CURRENT frame's hit point of that pixel
+ * (get_pixel_surface_previous_frame, src/Device/includes/ReSTIR/Surface.h:52).
  * Reservoir record: 8 words per pixel (point xyz, p_hat, triangle, (M << 9) | flags, w_sum, UCW).
  */
 #include <atomic>
@@ -103,6 +114,10 @@ struct RSettings
     const float* presampled = nullptr;
     int subsets = 0, size = 0, tile = 8;
     uint32_t presample_seed = 0;
+    // rng_mode 1: the reference's per-pass random numbers (HIPRTRenderData::random_number)
+    int rng_mode = 0;
+    uint32_t sample_number = 0, rn_initial = 0, rn_temporal = 0, rn_spatial[4] = {0, 0, 0, 0};
+    int gbuffer_materials = 0;  // offset of the packed camera-hit materials in the material table
 };
 
 struct Surf
@@ -140,9 +155,11 @@ V tri_normal(const Scene& s, int t) { return nrm(cross(s.b(t) - s.a(t), s.c(t) -
 float eta_in(const Surf& su, const float* m) { return su.inside ? m[37] : 1.0f; }
 float eta_out(const Surf& su, const float* m) { return su.inside ? 1.0f : m[37]; }
 
+const float* surf_mat(const Ctx& c, const Surf& su) { return c.ps.mat(su.mat + c.st.gbuffer_materials); }
+
 V bsdf_eval(const Ctx& c, const Surf& su, V l, int lobe, float& pdf)
 {
-    const float* m = c.ps.mat(su.mat);
+    const float* m = surf_mat(c, su);
     float q[16], out[4];
     make_query(q, su.view, su.ns, su.ng, l, eta_in(su, m), eta_out(su, m), su.inside, lobe);
     c.ps.eval(m, q, out);
@@ -225,6 +242,11 @@ void visibility_kill(const Ctx& c, Res& r, const Surf& su)
 
 Pcg stream(const RSettings& st, int pixel, int pass)
 {
+    if (st.rng_mode)
+    {
+        const uint32_t rn = pass == 1 ? st.rn_initial : pass == 2 ? st.rn_temporal : st.rn_spatial[(pass - 3) & 3];
+        return parity_seed((uint32_t)pixel, st.sample_number, rn);
+    }
     return pcg_seed((uint32_t)pixel, (uint32_t)st.frame * 16u + (uint32_t)pass, (uint32_t)st.seed);
 }
 
@@ -299,7 +321,7 @@ Res initial_pixel(const Ctx& c, const float* gb, int pixel)
     const Surf su = load_surf(gb, pixel, c.st.cam);
     if (su.prim < 0 || c.s.ne == 0) return r;
     Pcg rng = stream(c.st, pixel, 1);
-    const float* m = c.ps.mat(su.mat);
+    const float* m = surf_mat(c, su);
     const float nl = (float)c.st.n_light, nb = (float)c.st.n_bsdf;
     const int subset = c.st.presampled ? presampled_subset(c.st, pixel % c.st.width, pixel / c.st.width) : 0;
     for (int k = 0; k < c.st.n_light; k++)
@@ -316,7 +338,10 @@ Res initial_pixel(const Ctx& c, const float* gb, int pixel)
             ls.emission = c.s.emi(ls.tri);
         }
         else
+        {
+            if (c.st.rng_mode) rng.next();  // the envmap-or-light draw (no envmap: a light)
             ls = sample_light(c.s, c.st.light_strategy, rng);
+        }
         V wi = ls.point - su.P;
         float dist = len(wi);
         wi = wi / dist;
@@ -329,7 +354,9 @@ Res initial_pixel(const Ctx& c, const float* gb, int pixel)
             if (bpdf > 0.0f)
             {
                 float cl = std::max(0.0f, dot(ls.normal, neg(wi)));
-                p_hat = lum(f * ls.emission * dot(su.ns, wi) * (cl / (dist * dist)));
+                // the reference's candidate carries ReSTIR_DI_evaluate_target_function's value
+                p_hat = c.st.rng_mode ? target(c, su, ls.point, ls.tri, 0, false)
+                                      : lum(f * ls.emission * dot(su.ns, wi) * (cl / (dist * dist)));
                 float lpdf = a2s(ls.pdf_area, dist, cl);
                 float mis = lpdf == 0.0f ? 0.0f : lpdf / (nl * lpdf + nb * bpdf);
                 weight = mis * p_hat / ls.pdf_area;
@@ -407,12 +434,17 @@ Res temporal_pixel(const Ctx& c, const float* gb, const float* gb_prev, const fl
         int tx = (int)std::round(px + ox), ty = (int)std::round(py + oy);
         if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
         t_idx = tx + ty * W;
-        if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, c.st)) break;
+        if (similar(gb_prev, gb, t_idx, pixel, su.P, c.st.rng_mode ? su.ns : su.ng, c.st)) break;
         t_idx = -1;
     }
     if (t_idx < 0) return init;
     const Res tn = load_res(prev, t_idx);
-    const Surf ts = load_surf(gb_prev, t_idx, c.st.prev_cam);
+    Surf ts = load_surf(gb_prev, t_idx, c.st.prev_cam);
+    if (c.st.rng_mode)
+    {
+        const float* pc = gb + 12 * (size_t)t_idx;
+        ts.view = nrm(mk(c.st.prev_cam[0], c.st.prev_cam[1], c.st.prev_cam[2]) - mk(pc[0], pc[1], pc[2]));
+    }
     if (tn.M == 0 || ts.prim < 0 || !black(mk(c.s.emission[3 * ts.mat], c.s.emission[3 * ts.mat + 1], c.s.emission[3 * ts.mat + 2])))
         return init;
     const bool vis = c.st.bias_vis != 0;
@@ -464,6 +496,7 @@ Res spatial_pixel(const Ctx& c, const float* gb, const float* in, int pixel, int
     const Res center = load_res(in, pixel);
     if (su.prim < 0) return center;
     Pcg rng = stream(c.st, pixel, 3 + pass);
+    if (c.st.rng_mode) seed = rng.u32();  // the pixel's neighbour generator seed
     const int W = c.st.width, H = c.st.height, K = c.st.spatial_neighbors;
     const int cx = pixel % W, cy = pixel / W;
     Xor32 nr{seed};
@@ -528,6 +561,7 @@ Res spatial_pixel(const Ctx& c, const float* gb, const float* in, int pixel, int
     }
     end_norm(o);
     if (c.st.visibility_reuse && vis && (c.st.do_temporal || pass != last_pass)) visibility_kill(c, o, su);
+    if (c.st.m_cap > 0) o.M = std::min(o.M, c.st.m_cap);  // SpatialReuse.h:317-319
     return o;
 }
 
@@ -700,6 +734,14 @@ RSettings settings_from(const int* si, const float* sf, const float* prev_vp)
         st.prev_cam[k] = sf[7 + k];
     }
     st.prev_vp = prev_vp;
+    // settings_i[16..24]: rng mode, sample number, the initial / temporal / spatial passes' random
+    // numbers (rng mode 1), the offset of the packed camera-hit materials
+    st.rng_mode = si[16];
+    st.sample_number = (uint32_t)si[17];
+    st.rn_initial = (uint32_t)si[18];
+    st.rn_temporal = (uint32_t)si[19];
+    for (int k = 0; k < 4; k++) st.rn_spatial[k] = (uint32_t)si[20 + k];
+    st.gbuffer_materials = si[24];
     return st;
 }
 
@@ -708,14 +750,19 @@ RSettings settings_from(const int* si, const float* sf, const float* prev_vp)
 extern "C" {
 
 /* G-buffer of the camera hits (12 floats per pixel: P, prim bits, ns, material bits, ng, inside
- * bits), with the GPU camera's jitter stream: pcg_seed(pixel, frame, seed). */
+ * bits), with the GPU camera's jitter stream pcg_seed(pixel, frame, seed); with rng_mode 1, the
+ * reference's camera pass instead (Xorshift32 seeded by wang_hash((pixel + 1) (frame + 1)
+ * random_number), CameraRays.h:155-170) and its packed normals (octahedral 24 bits, written at
+ * CameraRays.h:178-201). */
 void orc_restir_gbuffer(const float* tri_verts, int n_tris, const int* mat_of, const float* pmats, int width, int height,
-                        int seed, int frame, int jitter, const float* inv_view, const float* inv_proj, float* gb, int nthreads)
+                        int seed, int frame, int jitter, const float* inv_view, const float* inv_proj, float* gb, int nthreads,
+                        int rng_mode, uint32_t random_number)
 {
     Scene s{tri_verts, n_tris, mat_of, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0.0f};
     parallel_pixels(width * height, nthreads, [&](int pixel) {
         const int x = pixel % width, y = pixel / width;
-        Pcg rng = pcg_seed((uint32_t)pixel, (uint32_t)frame, (uint32_t)seed);
+        Pcg rng = rng_mode ? parity_seed((uint32_t)pixel, (uint32_t)frame, random_number)
+                           : pcg_seed((uint32_t)pixel, (uint32_t)frame, (uint32_t)seed);
         float px = x + 0.5f, py = y + 0.5f;
         if (jitter)
         {
@@ -745,6 +792,11 @@ void orc_restir_gbuffer(const float* tri_verts, int n_tris, const int* mat_of, c
             refl = refl - nrm(ng * (dot(refl, ng) - 0.01f));
             ns = nrm(view + refl);
         }
+        if (rng_mode)
+        {
+            ns = oct24(ns);
+            ng = oct24(ng);
+        }
         const int mi = mat_of[prim];
         // the camera hit enters its material from the air: the reference rebuilds the surface's
         // volume state by pushing the hit material on a fresh stack (ReSTIR/Surface.h:31)
@@ -764,9 +816,11 @@ void orc_restir_gbuffer(const float* tri_verts, int n_tris, const int* mat_of, c
  * initial, prev = previous final reservoirs, gb_prev = previous G-buffer).
  * presampled (NULL: off): light presampling records (orc_restir_presample) with presample_i =
  * subsets, subset size, tile size, the frame's subset seed (bits).
- * settings_i: width, height, seed, frame, has_prev, light strategy (0 uniform, 1 power), light
+ * settings_i (25): width, height, seed, frame, has_prev, light strategy (0 uniform, 1 power), light
  *   candidates, bsdf candidates, visibility reuse, do temporal, temporal search count, spatial
- *   passes, spatial neighbours, m cap, confidence weights, bias-correction visibility.
+ *   passes, spatial neighbours, m cap, confidence weights, bias-correction visibility, rng mode,
+ *   sample number, random numbers of the initial / temporal / spatial passes 0..3, offset of the
+ *   packed camera-hit materials.
  * settings_f: temporal radius, spatial radius, normal cos, plane distance, camera pos xyz,
  *   previous camera pos xyz. */
 void orc_restir_pass(int pass, const float* tri_verts, int n_tris, const int* mat_of, const float* emission,

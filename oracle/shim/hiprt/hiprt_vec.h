@@ -46,13 +46,28 @@ struct hiprtInt3 { int x, y, z; };
 struct hiprtInt4 { int x, y, z, w; };
 struct hiprtUint2 { unsigned int x, y; };
 
-inline hiprtFloat2 make_hiprtFloat2(float x, float y) { return {x, y}; }
-inline hiprtFloat2 make_hiprtFloat2(float s) { return {s, s}; }
-inline hiprtFloat3 make_hiprtFloat3(float x, float y, float z) { return {x, y, z}; }
-inline hiprtFloat3 make_hiprtFloat3(float s) { return {s, s, s}; }
-inline hiprtFloat3 make_hiprtFloat3(const hiprtFloat4& a) { return {a.x, a.y, a.z}; }
 inline hiprtFloat4 make_hiprtFloat4(float x, float y, float z, float w) { return {x, y, z, w}; }
 inline hiprtFloat4 make_hiprtFloat4(const hiprtFloat3& a, float w) { return {a.x, a.y, a.z, w}; }
+// The reference's device compilers evaluate a call's arguments left to right, and some of its
+// kernels draw random numbers inside one call (make_float2(rng() - 0.5f, rng() - 0.5f),
+// src/Device/includes/ReSTIR/UtilsTemporal.h:65, UtilsSpatial.h:155,199). A host compiler may
+// evaluate them in another order (g++ on x86-64 goes right to left), so the float vector
+// constructors are macros over braced lists, whose elements C++ evaluates left to right.
+struct hiprtFloat2Args
+{
+    hiprtFloat2 v;
+    hiprtFloat2Args(float x, float y) : v{x, y} {}
+    explicit hiprtFloat2Args(float s) : v{s, s} {}
+};
+struct hiprtFloat3Args
+{
+    hiprtFloat3 v;
+    hiprtFloat3Args(float x, float y, float z) : v{x, y, z} {}
+    explicit hiprtFloat3Args(float s) : v{s, s, s} {}
+    explicit hiprtFloat3Args(const hiprtFloat4& a) : v{a.x, a.y, a.z} {}
+};
+#define make_hiprtFloat2(...) (hiprtFloat2Args{__VA_ARGS__}.v)
+#define make_hiprtFloat3(...) (hiprtFloat3Args{__VA_ARGS__}.v)
 inline hiprtInt2 make_hiprtInt2(int x, int y) { return {x, y}; }
 inline hiprtInt3 make_hiprtInt3(int x, int y, int z) { return {x, y, z}; }
 inline hiprtInt4 make_hiprtInt4(int x, int y, int z, int w) { return {x, y, z, w}; }

@@ -122,7 +122,7 @@ def main():
                                                      "spatial_passes", "spatial_neighbors", "spatial_radius", "m_cap",
                                                      "use_confidence_weights")], np.int32),
                restir_f=np.array([RESTIR["normal_similarity_cos"], RESTIR["plane_distance_threshold"]], np.float32))
-    keys = ("image", "initial", "temporal", "final", "prim")
+    keys = ("image", "initial", "temporal", "final", "prim", "pos")
     acc = {k: [] for k in keys}
     ivs, ips = [], []
     prev_iv = None
