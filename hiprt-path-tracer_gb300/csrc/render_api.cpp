@@ -81,6 +81,8 @@ struct gbpt_renderer
     gbpt::RenderConst rc;
     // GBPT_RNG_REFERENCE: the host generator of the per-launch random numbers (CPURenderer::m_rng)
     uint32_t rng_seed = 42u, host_rng = 42u;
+    // ... and the ReSTIR DI passes' numbers of the current sample: initial, temporal, spatial 0..3
+    uint32_t rn_initial = 0u, rn_temporal = 0u, rn_spatial[4] = {0u, 0u, 0u, 0u};
     DevMem mem;
     gbpt::PathBuffers pb;
     gbpt::Queue q[2], shadow, bsdfq;
@@ -874,11 +876,24 @@ gbpt_status gbpt_pass_camera_rays(gbpt_renderer* r, void* stream)
 {
     if (!r) return set_error(GBPT_ERROR_INVALID_ARG, "renderer is NULL");
     r->cur = 0;
-    // the reference's GPU renderer draws one random number per pass from its generator: the
-    // G-buffer pass, then the MegaKernel pass (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53)
+    // the reference's GPU renderer draws one random number per pass from its generator, in launch
+    // order: the G-buffer pass (FillGBufferRenderPass.cpp:91), the ReSTIR DI passes (initial
+    // candidates; temporal reuse and its permutation-sampling bits; each spatial pass;
+    // ReSTIRDIRenderPass.cpp:449-578), then the MegaKernel pass (MegaKernelRenderPass.cpp:53)
     if (r->rc.rng_mode == GBPT_RNG_REFERENCE)
     {
         r->rc.random_number_camera = xorshift32_step(r->host_rng);
+        if (r->restir)
+        {
+            const gbpt_restir_di_settings& k = r->restir_settings;
+            r->rn_initial = xorshift32_step(r->host_rng);
+            if (k.do_temporal)
+            {
+                r->rn_temporal = xorshift32_step(r->host_rng);
+                xorshift32_step(r->host_rng);  // permutation-sampling bits (permutation sampling off)
+            }
+            for (int p = 0; k.do_spatial && p < k.spatial_passes; p++) r->rn_spatial[p] = xorshift32_step(r->host_rng);
+        }
         r->rc.random_number = xorshift32_step(r->host_rng);
     }
     cudaError_t e = gbpt::launch_camera(r->rc, r->pb, r->q[0], (int32_t)r->iteration, r->stats, r->n_sm,
@@ -967,6 +982,11 @@ gbpt::RestirConst restir_const(const gbpt_renderer* r)
     c.frame = (uint32_t)r->iteration;
     c.seed = r->rc.seed;
     c.has_prev = r->has_prev ? 1 : 0;
+    c.rng_mode = r->rc.rng_mode;
+    c.sample_number = (uint32_t)r->iteration;
+    c.rn_initial = r->rn_initial;
+    c.rn_temporal = r->rn_temporal;
+    for (int p = 0; p < 4; p++) c.rn_spatial[p] = r->rn_spatial[p];
     camera_position(r->rc.inverse_view, c.camera_pos);
     camera_position(r->prev_inverse_view, c.prev_camera_pos);
     if (r->presampled)
@@ -1056,6 +1076,11 @@ gbpt_status gbpt_renderer_set_restir_di(gbpt_renderer* r, const gbpt_restir_di_s
         (k->presampling_subsets < 1 || k->presampling_subset_size < 1 || k->presampling_tile_size < 1 ||
          (int64_t)k->presampling_subsets * k->presampling_subset_size > ((int64_t)1 << 24)))
         return set_error(GBPT_ERROR_INVALID_ARG, "light presampling sizes out of range (at most 2^24 records)");
+    if (r->rc.rng_mode == GBPT_RNG_REFERENCE &&
+        (k->do_fused_spatiotemporal || k->do_light_presampling || (k->do_spatial && k->spatial_passes > 4)))
+        return set_error(GBPT_ERROR_INVALID_ARG,
+                         "GBPT_RNG_REFERENCE covers the separate temporal and spatial passes (at most 4), "
+                         "without light presampling");
     const int64_t npix = (int64_t)r->rc.width * r->rc.height;
     DevMem& M = r->restir_mem;
     for (int g = 0; g < 2; g++)
@@ -1126,7 +1151,8 @@ gbpt_status gbpt_pass_restir_di_initial(gbpt_renderer* r, void* stream)
     const int64_t npix = (int64_t)r->rc.width * r->rc.height;
     const gbpt::GBuffer& gb = r->gb[r->gb_cur];
     const gbpt::RestirConst k = restir_const(r);
-    cudaError_t e = gbpt::launch_restir_gbuffer(r->scene->view, r->q[r->cur], gb, npix, r->n_sm, cs);
+    cudaError_t e = gbpt::launch_restir_gbuffer(r->scene->view, r->q[r->cur], gb, npix,
+                                                r->rc.rng_mode == GBPT_RNG_REFERENCE ? 1 : 0, r->n_sm, cs);
     if (e == cudaSuccess && r->presampled)
         e = gbpt::launch_restir_presample(r->scene->view, r->rc, k, r->presampled, r->n_sm, cs);
     // its BSDF-candidate and visibility rays go through the bounce's free queues (left empty after)

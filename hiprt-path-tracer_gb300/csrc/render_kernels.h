@@ -86,8 +86,8 @@ cudaError_t launch_guide_inputs(const SceneView& s, const Queue& in, const Guide
                                 cudaStream_t st);
 // Training-record weights from the final path radiance (after the launch's last bounce)
 cudaError_t launch_guide_weights(const PathBuffers& pb, const GuideView& gv, int n_sm, cudaStream_t st);
-cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int n_sm,
-                                  cudaStream_t st);
+cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int packed_normals,
+                                  int n_sm, cudaStream_t st);
 // Light presampling of the frame into out (2 float4 per record, k.presample_subsets * size records)
 cudaError_t launch_restir_presample(const SceneView& s, const RenderConst& rc, const RestirConst& k, float4* out,
                                     int n_sm, cudaStream_t st);

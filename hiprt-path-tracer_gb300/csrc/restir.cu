@@ -168,7 +168,29 @@ __device__ void visibility_kill(const SceneView& s, Reservoir& r, const Surface&
 
 __device__ __forceinline__ Pcg32 pass_stream(const RestirConst& k, int pixel, int pass)
 {
+    if (k.rng_mode == GBPT_RNG_REFERENCE)
+    {
+        const uint32_t rn = pass == 1 ? k.rn_initial : pass == 2 ? k.rn_temporal : k.rn_spatial[(pass - 3) & 3];
+        return reference_seed((uint32_t)pixel, k.sample_number, rn);
+    }
     return pcg_seed((uint32_t)pixel, k.frame * 16u + (uint32_t)pass, k.seed);
+}
+
+// The material a G-buffer surface is shaded with: with the reference's generator, the packed
+// camera-hit material the reference's G-buffer stores (DevicePackedEffectiveMaterial,
+// CameraRays.h:178-201); else the scene's
+__device__ __forceinline__ const gbpt_principled_material& surface_material(const SceneView& s, const RestirConst& k,
+                                                                           int mat)
+{
+    return (k.rng_mode == GBPT_RNG_REFERENCE && s.pmats_camera) ? s.pmats_camera[mat] : s.pmats[mat];
+}
+
+// The spatial neighbours' generator of a pixel: with the reference's generator, seeded by one draw
+// of the pixel's own (setup_adaptive_directional_spatial_reuse, UtilsSpatial.h:17-22); else the
+// pass's seed shared by all pixels
+__device__ __forceinline__ uint32_t neighbor_seed_of(const RestirConst& k, Pcg32& rng, uint32_t shared_seed)
+{
+    return k.rng_mode == GBPT_RNG_REFERENCE ? rng.next_u32() : shared_seed;
 }
 
 // neighbour heuristics (NeighborSimilarity.h:34-84): plane distance and geometric-normal angle;
@@ -234,7 +256,7 @@ __device__ __forceinline__ int presampled_subset(const RestirConst& k, int x, in
 // ---------------------------------------------------------------------------------------------
 // G-buffer from the camera hits (CameraRays, src/Device/kernels/CameraRays.h:178-201)
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuffer gb)
+__global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuffer gb, int packed_normals)
 {
     const int n = *q.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -255,6 +277,13 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(SceneView s, Queue q, GBuf
         V3 ng = ng_raw, ns = shading_normal(s, prim, hit.y, hit.z, ng_raw);
         const V3 view = -d;
         fix_backfacing(view, ng, ns);
+        if (packed_normals)
+        {
+            // the reference's G-buffer stores octahedral 24-bit normals, read back unpacked as
+            // they are by its ReSTIR surfaces (get_pixel_surface, ReSTIR/Surface.h:26-40)
+            ns = oct24_roundtrip(ns);
+            ng = oct24_roundtrip(ng);
+        }
         const int mat = __ldg(s.material_of + prim);
         // the camera hit's volume state as the reference rebuilds it from the G-buffer
         // (RayVolumeState::reconstruct_first_hit, ReSTIR/Surface.h:31): the material pushed on a
@@ -338,7 +367,7 @@ __device__ __forceinline__ bool initial_load(const SceneView& s, const RestirCon
 {
     px.su = load_surface(gb, pixel, k.camera_pos);
     if (px.su.prim < 0 || s.n_emissive == 0) return false;
-    px.m = bsdf::load_material(s.pmats[px.su.mat]);
+    px.m = bsdf::load_material(surface_material(s, k, px.su.mat));
     px.md = medium_of(px.su, px.m);
     return true;
 }
@@ -376,7 +405,12 @@ __global__ void __launch_bounds__(128, 3) initial_lights_kernel(SceneView s, Ren
                     ls.emission = emission_of(s, ls.triangle);
                 }
                 else
+                {
+                    // the reference first draws the envmap-or-light choice (sample_fresh_light_candidate,
+                    // InitialCandidates.h:100; without an envmap always a light)
+                    if (k.rng_mode == GBPT_RNG_REFERENCE) rng.next();
                     ls = sample_light(s, rc, rng);
+                }
                 V3 wi = ls.point - su.P;
                 const float dist = length(wi);
                 wi = wi / dist;
@@ -394,7 +428,10 @@ __global__ void __launch_bounds__(128, 3) initial_lights_kernel(SceneView s, Ren
                     if (bsdf_pdf > 0.0f)
                     {
                         const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
-                        p_hat = luminance(f * ls.emission * dot(su.ns, wi) * (cos_l / (dist * dist)));
+                        // the reference's candidate carries ReSTIR_DI_evaluate_target_function's value
+                        p_hat = k.rng_mode == GBPT_RNG_REFERENCE
+                                    ? target_function(s, hc, su, px.m, ls.point, ls.triangle, 0, false)
+                                    : luminance(f * ls.emission * dot(su.ns, wi) * (cos_l / (dist * dist)));
                         const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
                         const float mis = light_pdf == 0.0f ? 0.0f : light_pdf / (nl * light_pdf + nb * bsdf_pdf);
                         weight = mis * p_hat / ls.pdf_area;
@@ -528,9 +565,22 @@ __device__ __forceinline__ int temporal_neighbor(const RestirConst& k, const GBu
         const int tx = (int)roundf(px + ox), ty = (int)roundf(py + oy);
         if (tx < 0 || tx >= W || ty < 0 || ty >= H) continue;
         const int t_idx = tx + ty * W;
-        if (similar(gb_prev, gb, t_idx, pixel, su.P, su.ng, k)) return t_idx;
+        // the reference's temporal pass compares against the centre's shading normal
+        // (TemporalReuse.h:81-82); the other heuristics use the geometric one
+        if (similar(gb_prev, gb, t_idx, pixel, su.P, k.rng_mode == GBPT_RNG_REFERENCE ? su.ns : su.ng, k)) return t_idx;
     }
     return -1;
+}
+
+// A previous-frame G-buffer surface. With the reference's generator its view direction runs from
+// the previous camera to the CURRENT frame's hit point of that pixel, as the reference builds it
+// (get_pixel_surface_previous_frame, ReSTIR/Surface.h:52)
+__device__ __forceinline__ Surface previous_surface(const GBuffer& gb, const GBuffer& gb_prev, int idx, const RestirConst& k)
+{
+    Surface su = load_surface(gb_prev, idx, k.prev_camera_pos);
+    if (k.rng_mode == GBPT_RNG_REFERENCE)
+        su.view = normalize(v3(k.prev_camera_pos[0], k.prev_camera_pos[1], k.prev_camera_pos[2]) - xyz(gb.pos[idx]));
+    return su;
 }
 
 // appends the shadow ray of a target-function evaluation (from P to the sample) when 'want'
@@ -569,10 +619,10 @@ __global__ void __launch_bounds__(128, 3) temporal_rays_kernel(SceneView s, Rend
         const int t_idx = temporal_neighbor(k, gb, gb_prev, W, H, pixel, su, rng);
         if (t_idx < 0) continue;
         const Reservoir tn = load_reservoir(prev, t_idx);
-        const Surface ts = load_surface(gb_prev, t_idx, k.prev_camera_pos);
+        const Surface ts = previous_surface(gb, gb_prev, t_idx, k);
         if (tn.M == 0 || ts.prim < 0 || !is_black(xyz(s.materials[ts.mat].emission))) continue;
-        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
-        const bsdf::Material tm = bsdf::load_material(s.pmats[ts.mat]);
+        const bsdf::Material m = bsdf::load_material(surface_material(s, k, su.mat));
+        const bsdf::Material tm = bsdf::load_material(surface_material(s, k, ts.mat));
         const bool a = tn.ucw > 0.0f && target_function(s, hc, su, m, tn.point, tn.tri, tn.flags, false) > 0.0f;
         const bool b = target_function(s, hc, ts, tm, init.point, init.tri, init.flags, false) > 0.0f;
         const int sa = append_sample_ray(rays, a, su.P, tn.point, su.prim, pixel);
@@ -605,14 +655,14 @@ __global__ void __launch_bounds__(128, 3) temporal_kernel(SceneView s, RenderCon
             continue;
         }
         const Reservoir tn = load_reservoir(prev, t_idx);
-        const Surface ts = load_surface(gb_prev, t_idx, k.prev_camera_pos);
+        const Surface ts = previous_surface(gb, gb_prev, t_idx, k);
         if (tn.M == 0 || ts.prim < 0 || !is_black(xyz(s.materials[ts.mat].emission)))
         {
             store_reservoir(out, pixel, init);
             continue;
         }
-        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
-        const bsdf::Material tm = bsdf::load_material(s.pmats[ts.mat]);
+        const bsdf::Material m = bsdf::load_material(surface_material(s, k, su.mat));
+        const bsdf::Material tm = bsdf::load_material(surface_material(s, k, ts.mat));
         const bool vis = k.bias_correction_visibility != 0;
         const int2 rays = vis ? ray_of[pixel] : make_int2(-1, -1);
         Reservoir o = empty_reservoir();
@@ -659,8 +709,8 @@ __global__ void __launch_bounds__(128, 3) temporal_kernel(SceneView s, RenderCon
 // sample, depend only on the input reservoirs and the G-buffer, so they are appended here (one
 // slot per pixel and neighbour in 'ray_of', -1 without a ray) and traced as one any-hit queue.
 __global__ void __launch_bounds__(128) spatial_rays_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
-                                                           ReservoirBuf in, uint32_t neighbor_seed, int32_t* ray_of,
-                                                           Queue rays)
+                                                           ReservoirBuf in, int pass, uint32_t neighbor_seed,
+                                                           int32_t* ray_of, Queue rays)
 {
     const int W = rc.width, H = rc.height, n_pix = W * H;
     const bool hc = rc.ggx_height_correlated != 0;
@@ -673,7 +723,8 @@ __global__ void __launch_bounds__(128) spatial_rays_kernel(SceneView s, RenderCo
         const Reservoir center = load_reservoir(in, pixel);
         if (su.prim < 0 || !(center.M > 0 && center.ucw > 0.0f)) continue;
         const int cx = pixel % W, cy = pixel / W;
-        bsdf::Xorshift32 nrng{neighbor_seed};
+        Pcg32 rng = pass_stream(k, pixel, 3 + pass);
+        bsdf::Xorshift32 nrng{neighbor_seed_of(k, rng, neighbor_seed)};
         for (int j = 0; j < K; j++)
         {
             const int idx = spatial_neighbor(j, K, cx, cy, W, H, k.spatial_radius, nrng);
@@ -682,7 +733,7 @@ __global__ void __launch_bounds__(128) spatial_rays_kernel(SceneView s, RenderCo
             if (want)
             {
                 ns_ = load_surface(gb, idx, k.camera_pos);
-                const bsdf::Material nm = bsdf::load_material(s.pmats[ns_.mat]);
+                const bsdf::Material nm = bsdf::load_material(surface_material(s, k, ns_.mat));
                 // the target function without visibility; a ray only where it is positive
                 want = target_function(s, hc, ns_, nm, center.point, center.tri, center.flags, false) > 0.0f;
             }
@@ -723,8 +774,9 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
         }
         Pcg32 rng = pass_stream(k, pixel, 3 + pass);
         const int cx = pixel % W, cy = pixel / W;
+        const uint32_t nseed = neighbor_seed_of(k, rng, neighbor_seed);
         // count the valid neighbours and their confidence (count_valid_spatial_neighbors)
-        bsdf::Xorshift32 nrng{neighbor_seed};
+        bsdf::Xorshift32 nrng{nseed};
         int valid = 0, m_sum = 0;
         uint32_t cache = 0;
         for (int j = 0; j < K; j++)
@@ -736,7 +788,7 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
             valid++;
             cache |= 1u << j;
         }
-        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bsdf::Material m = bsdf::load_material(surface_material(s, k, su.mat));
         const bool vis = k.bias_correction_visibility != 0;
         const bool update_mc = center.M > 0 && center.ucw > 0.0f;
         const float cM = k.confidence_weights ? (float)center.M : 1.0f;
@@ -744,7 +796,7 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
         const float div = k.confidence_weights ? 1.0f : (float)valid;
         float mc = 0.0f;
         Reservoir o = empty_reservoir();
-        nrng = bsdf::Xorshift32{neighbor_seed};
+        nrng = bsdf::Xorshift32{nseed};
         for (int j = m_sum == 0 ? K : 0; j < K + 1; j++)
         {
             if (j < K && !(cache & (1u << j)))
@@ -768,7 +820,7 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
                 if (update_mc)
                 {
                     const Surface ns_ = load_surface(gb, idx, k.camera_pos);
-                    const bsdf::Material nm = bsdf::load_material(s.pmats[ns_.mat]);
+                    const bsdf::Material nm = bsdf::load_material(surface_material(s, k, ns_.mat));
                     float c_at_n = target_function(s, hc, ns_, nm, center.point, center.tri, center.flags, false);
                     if (vis && c_at_n > 0.0f)
                     {
@@ -793,6 +845,7 @@ __global__ void __launch_bounds__(128) spatial_kernel(SceneView s, RenderConst r
             }
         }
         end_with_normalization(o, 1.0f, 1.0f);
+        if (k.m_cap > 0) o.M = min(o.M, k.m_cap);  // SpatialReuse.h:317-319
         // visibility reuse of the result (visibility_kill) through the any-hit queue
         const bool test = k.visibility_reuse && vis && (k.do_temporal || pass != last_pass) &&
                           !(o.ucw <= 0.0f && o.w_sum <= 0.0f) && !(o.flags & kRestirFlagUnoccluded);
@@ -859,7 +912,7 @@ __global__ void __launch_bounds__(128, 3) spatiotemporal_rays_kernel(SceneView s
             m_sum += load_reservoir(prev, idx).M;
             cache |= 1u << j;
         }
-        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bsdf::Material m = bsdf::load_material(surface_material(s, k, su.mat));
         const bool update_mc = init.M > 0 && init.ucw > 0.0f;
         if (t_ok)
         {
@@ -870,7 +923,7 @@ __global__ void __launch_bounds__(128, 3) spatiotemporal_rays_kernel(SceneView s
             if (update_mc)
             {
                 nsu = load_surface(gb_prev, t_idx, k.prev_camera_pos);
-                const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
+                const bsdf::Material nm = bsdf::load_material(surface_material(s, k, nsu.mat));
                 b = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, false) > 0.0f;
             }
             slots[1] = append_sample_ray(rays, b, nsu.P, init.point, nsu.prim, pixel);
@@ -894,7 +947,7 @@ __global__ void __launch_bounds__(128, 3) spatiotemporal_rays_kernel(SceneView s
                 if (idx >= 0)
                 {
                     nsu = load_surface(gb_prev, idx, k.prev_camera_pos);
-                    const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
+                    const bsdf::Material nm = bsdf::load_material(surface_material(s, k, nsu.mat));
                     want = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, false) > 0.0f;
                 }
             }
@@ -951,7 +1004,7 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
             valid++;
             m_sum += tn.M;
         }
-        const bsdf::Material m = bsdf::load_material(s.pmats[su.mat]);
+        const bsdf::Material m = bsdf::load_material(surface_material(s, k, su.mat));
         const bool vis = k.bias_correction_visibility != 0;
         const bool update_mc = init.M > 0 && init.ucw > 0.0f;
         const float cM = k.confidence_weights ? (float)init.M : 1.0f;
@@ -996,7 +1049,7 @@ __global__ void __launch_bounds__(128) spatiotemporal_kernel(SceneView s, Render
                 if (update_mc)
                 {
                     const Surface nsu = load_surface(gb_prev, idx, k.prev_camera_pos);
-                    const bsdf::Material nm = bsdf::load_material(s.pmats[nsu.mat]);
+                    const bsdf::Material nm = bsdf::load_material(surface_material(s, k, nsu.mat));
                     float c_at_n = target_function(s, hc, nsu, nm, init.point, init.tri, init.flags, false);
                     const int32_t ray = slots[j < 0 ? 1 : 2 + j];
                     if (vis && c_at_n > 0.0f && ray >= 0 && traced.occluded[ray]) c_at_n = 0.0f;
@@ -1045,10 +1098,10 @@ inline int grid_for(int64_t n, int threads, int max_blocks)
 
 }  // namespace
 
-cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int n_sm,
-                                  cudaStream_t st)
+cudaError_t launch_restir_gbuffer(const SceneView& s, const Queue& q, const GBuffer& gb, int64_t n_pix, int packed_normals,
+                                  int n_sm, cudaStream_t st)
 {
-    gbuffer_kernel<<<grid_for(n_pix, 256, n_sm * 8), 256, 0, st>>>(s, q, gb);
+    gbuffer_kernel<<<grid_for(n_pix, 256, n_sm * 8), 256, 0, st>>>(s, q, gb, packed_normals);
     return cudaGetLastError();
 }
 
@@ -1154,7 +1207,7 @@ cudaError_t launch_restir_spatial(const SceneView& s, const RenderConst& rc, con
     if (e != cudaSuccess) return e;
     if (k.bias_correction_visibility)
     {
-        spatial_rays_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, in, neighbor_seed, ray_of, rays);
+        spatial_rays_kernel<<<grid, 128, 0, stream>>>(s, rc, k, gb, in, pass, neighbor_seed, ray_of, rays);
         e = launch_trace_queue(s, rays, true, n * k.spatial_neighbors, n_sm, stream);
     }
     if (e == cudaSuccess)

@@ -62,6 +62,12 @@ struct RestirConst
     const float4* presampled;
     int32_t presample_subsets, presample_size, presample_tile;
     uint32_t presample_seed;
+    // GBPT_RNG_REFERENCE: each pass seeds a Xorshift32 per pixel from its own random number and the
+    // sample number, as the reference's passes do (InitialCandidates.h:500-505,
+    // TemporalReuse.h:69-74, SpatialReuse.h:62-69); the G-buffer holds the reference's packed
+    // normals and the surfaces read the packed camera-hit materials
+    int32_t rng_mode;
+    uint32_t sample_number, rn_initial, rn_temporal, rn_spatial[4];
 };
 
 #ifdef __CUDACC__
