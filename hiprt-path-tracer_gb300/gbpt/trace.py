@@ -178,17 +178,20 @@ def classify_hit_differences(mesh, rays, a, b, edge_rel=2.5e-7, mt_epsilon=1e-7)
     """Compares the closest-hit records a (Moller-Trumbore, the parity test) and b (watertight) of
     the same rays -> dict of counts {agree, edge, parallel, tie, other}:
       agree: both miss, or the same triangle at the same point: |t_a - t_b| cos(theta) <= 4e-6 s
-        and the points their (u, v) address within 4e-6 s / cos(theta), with s = max(t, |origin|)
+        and the points their (u, v) address within 4e-6 s k / cos(theta), with s = max(t, |origin|)
         the magnitude of the coordinates both tests round (a bounce ray's t can be far below its
-        origin's) and theta the angle between the ray and the triangle's normal (the position of a
-        grazing intersection along the ray is conditioned by 1 / cos(theta));
-      edge: a different outcome where a hit lies within edge_rel s of an edge of its triangle,
-        measured in the plane perpendicular to the ray (the plane both tests decide in: a
-        coordinate rounding decides which side of the edge the ray passes);
-      parallel: b hits a triangle whose Moller-Trumbore determinant e1 . (d x e2), in float as the
-        reference computes it, is within +-mt_epsilon: the reference's test treats such a ray as
-        parallel to the triangle and never reports it (src/Renderer/Triangle.h:22-31) - grazing
-        hits on small triangles that only the watertight test keeps;
+        origin's), theta the angle between the ray and the triangle's normal (the position of a
+        grazing intersection along the ray is conditioned by 1 / cos(theta)) and k = max(1,
+        longest edge^2 / (2 area)) the triangle's aspect (a sliver's barycentrics are conditioned
+        by it: both tests divide edge functions of size ~area by the determinant);
+      parallel (checked first): b hits a triangle whose Moller-Trumbore determinant e1 . (d x e2),
+        in float as the reference computes it, is within +-mt_epsilon: the reference's test treats
+        such a ray as parallel to the triangle and never reports it (src/Renderer/Triangle.h:22-31)
+        - grazing hits on small triangles that only the watertight test keeps;
+      edge: a different outcome where a hit lies within edge_rel s / max(cos(theta), 1e-3) of an
+        edge of its triangle, measured in the plane perpendicular to the ray (the plane both tests
+        decide in: a coordinate rounding decides which side of the edge the ray passes, and a
+        grazing incidence stretches that rounding by 1 / cos(theta));
       tie: two different triangles hit at the same t (1e-6 relative);
       other: anything else."""
     pa, pb = a[:, 3].view(np.int32), b[:, 3].view(np.int32)
@@ -210,12 +213,21 @@ def classify_hit_differences(mesh, rays, a, b, edge_rel=2.5e-7, mt_epsilon=1e-7)
 
     t = a[both, 0].astype(np.float64)
     scale = np.maximum(t, np.linalg.norm(origin[both], axis=1))
-    ok = (np.abs(t - b[both, 0]) * cos <= 4e-6 * scale) & (np.linalg.norm(at(a) - at(b), axis=1) * cos <= 4e-6 * scale)
+    e3 = T[:, 0] - T[:, 2]
+    longest2 = np.maximum(np.maximum((e1 * e1).sum(1), (e2 * e2).sum(1)), ((T[:, 2] - T[:, 1]) ** 2).sum(1))
+    longest2 = np.maximum(longest2, (e3 * e3).sum(1))
+    aspect = np.maximum(1.0, longest2 / np.maximum(np.linalg.norm(n, axis=1), 1e-300))
+    ok = (np.abs(t - b[both, 0]) * cos <= 4e-6 * scale) & \
+         (np.linalg.norm(at(a) - at(b), axis=1) * cos <= 4e-6 * scale * aspect)
     counts = dict(agree=int((same & (pa < 0)).sum() + ok.sum()), edge=0, parallel=0, tie=0, other=int((~ok).sum()))
 
     def edge_distance(i, h):
+        """(distance of the hit from its triangle's nearest edge, perpendicular to the ray;
+        |cos| of the incidence)"""
         o, d = origin[i], direction[i] / np.linalg.norm(direction[i])
         v0, v1, v2 = tri[int(h[3:4].view(np.int32)[0])]
+        nv = np.cross(v1 - v0, v2 - v0)
+        c = abs(float(np.dot(nv, d))) / max(float(np.linalg.norm(nv)), 1e-300)
         p = v0 + float(h[1]) * (v1 - v0) + float(h[2]) * (v2 - v0)
 
         def perp(x):
@@ -228,7 +240,7 @@ def classify_hit_differences(mesh, rays, a, b, edge_rel=2.5e-7, mt_epsilon=1e-7)
             e = s1 - s0
             s = np.clip(np.dot(q - s0, e) / max(np.dot(e, e), 1e-300), 0.0, 1.0)
             best = min(best, float(np.linalg.norm(q - (s0 + s * e))))
-        return best
+        return best, c
 
     def mt_determinant(i, prim):
         v0, v1, v2 = soup[prim]
@@ -236,13 +248,17 @@ def classify_hit_differences(mesh, rays, a, b, edge_rel=2.5e-7, mt_epsilon=1e-7)
         return float(np.dot(v1 - v0, np.cross(d, v2 - v0)))
 
     for i in np.nonzero(~same)[0]:
+        if pb[i] >= 0 and abs(mt_determinant(i, pb[i])) < mt_epsilon:
+            counts["parallel"] += 1
+            continue
         o_len = float(np.linalg.norm(origin[i]))
-        near = [1 for h, p in ((a, pa), (b, pb))
-                if p[i] >= 0 and edge_distance(i, h[i]) <= edge_rel * max(float(h[i, 0]), o_len)]
+        near = False
+        for h, p in ((a, pa), (b, pb)):
+            if p[i] >= 0:
+                dist, c = edge_distance(i, h[i])
+                near = near or dist <= edge_rel * max(float(h[i, 0]), o_len) / max(c, 1e-3)
         if near:
             counts["edge"] += 1
-        elif pb[i] >= 0 and abs(mt_determinant(i, pb[i])) < mt_epsilon:
-            counts["parallel"] += 1
         elif pa[i] >= 0 and pb[i] >= 0 and abs(float(a[i, 0]) - float(b[i, 0])) <= 1e-6 * max(1.0, abs(float(a[i, 0]))):
             counts["tie"] += 1
         else:
