@@ -155,10 +155,10 @@ def kernel_source_hash():
     return h.hexdigest()[:16]
 
 
-def ncu_traffic():
-    """DRAM bytes per closest-hit ray from the committed ncu summary of the closest-hit kernels,
-    used only when that capture was taken of these very sources (its source_hash line matches),
-    else None: a capture of another build says nothing about this one."""
+def ncu_traffic(key="dram_bytes_per_ray"):
+    """DRAM (or, key l2_bytes_per_ray, L2) bytes per closest-hit ray from the committed ncu summary
+    of the closest-hit kernels, used only when that capture was taken of these very sources (its
+    source_hash line matches), else None: a capture of another build says nothing about this one."""
     path = os.path.join(REPO, "profiles", "trace_closest_traffic.txt")
     vals = {}
     try:
@@ -168,9 +168,32 @@ def ncu_traffic():
                 vals[k] = v
     except OSError:
         return None
-    if vals.get("source_hash") != kernel_source_hash() or "dram_bytes_per_ray" not in vals:
+    if vals.get("source_hash") != kernel_source_hash() or key not in vals:
         return None
-    return float(vals["dram_bytes_per_ray"])
+    return float(vals[key])
+
+
+def l2_copy_peak(dev, sizes_mb=(8, 16, 32, 48), reps=200):
+    """Measured L2 bandwidth of this GPU: a device-to-device copy of a buffer pair that fits in the
+    129 MB L2 (read + write bytes per second, CUDA events, best over the buffer sizes), the L2
+    counterpart of the measured HBM copy peak. Returns (GB/s, {size MB: GB/s})."""
+    import torch
+    by_size = {}
+    for mb in sizes_mb:
+        n = mb * (1 << 20) // 4
+        a = torch.rand(n, device=dev)
+        b = torch.empty_like(a)
+        for _ in range(10):
+            b.copy_(a)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        by_size[mb] = 2 * n * 4 / (e0.elapsed_time(e1) / reps * 1e-3) / 1e9
+        del a, b
+    return max(by_size.values()), by_size
 
 
 def make_cpu_impl(mesh, log=print):
@@ -893,6 +916,17 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = alg_closest / (closest_ms * 1e-3) / 1e9
     traffic_per_ray = ncu_traffic()
+    l2_per_ray = ncu_traffic("l2_bytes_per_ray")
+    l2_peak, l2_by_size = l2_copy_peak(dev)
+    l2_roofline = None
+    if l2_per_ray:
+        l2_achieved = l2_per_ray * (len(primary) + len(bounce)) / (closest_ms * 1e-3) / 1e9
+        l2_roofline = {"bound": "l2", "achieved": l2_achieved, "peak": l2_peak, "unit": "GB/s",
+                       "frac": l2_achieved / l2_peak,
+                       "peak_source": "measured here: L2-resident device copy, best of " +
+                                      ", ".join(f"{k} MB {v:.0f}" for k, v in l2_by_size.items()),
+                       "bytes_per_ray": l2_per_ray,
+                       "bytes_source": "ncu lts__t_sectors x 32 B per closest-hit ray (profiles/trace_closest_traffic.txt)"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -909,7 +943,8 @@ def main():
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "algorithmic_bytes_per_launch": alg_closest / 2,
-                     "traffic": (traffic_per_ray * (len(primary) + len(bounce)) / 2) if traffic_per_ray else None},
+                     "traffic": (traffic_per_ray * (len(primary) + len(bounce)) / 2) if traffic_per_ray else None,
+                     "l2": l2_roofline},
         "e2e": {"value": world * n_rays / e2e_s / 1e6, "unit": UNIT,
                 "h2d_bytes_per_step": n_rays * RAY_IN_BYTES,
                 "d2h_bytes_per_step": (len(primary) + len(bounce)) * CLOSEST_OUT_BYTES + len(shadow) * ANY_OUT_BYTES},

@@ -298,6 +298,7 @@ gbpt::TraceConfig from_c(const gbpt_trace_config& c)
     t.blocks_per_sm = c.blocks_per_sm;
     t.shared_stack = c.shared_stack;
     t.triangle_test = c.triangle_test;
+    t.top_levels = c.top_levels;
     return t;
 }
 
@@ -312,6 +313,7 @@ gbpt_trace_config to_c(const gbpt::TraceConfig& t)
     c.blocks_per_sm = t.blocks_per_sm;
     c.shared_stack = t.shared_stack;
     c.triangle_test = t.triangle_test;
+    c.top_levels = t.top_levels;
     return c;
 }
 
@@ -404,23 +406,34 @@ gbpt_status gbpt_trace_autotune(gbpt_bvh* bvh, const float* origin_tmin, const f
     const int postpones[] = {0, 4, 8, 12, 16, 24};
     const int per_sm[] = {2, 4, 8, 12, 16};
     const int shared[] = {0, 8, 16};
+    const int binary[] = {0, 1};
     for (int pass = 0; pass < 2 && e == cudaSuccess; pass++)
     {
-        // coordinates: kernel, block, shared-stack depth, refill, postpone, blocks per SM
-        for (int coord = 0; coord < 6 && e == cudaSuccess; coord++)
+        // coordinates: kernel, block, shared-stack depth, top levels in shared memory, refill,
+        // postpone, blocks per SM
+        for (int coord = 0; coord < 7 && e == cudaSuccess; coord++)
         {
-            if (best.kernel == gbpt::kTraceKernelPerRay && coord >= 3) break;
-            if (best.kernel == gbpt::kTraceKernelFetch && (coord == 3 || coord == 4)) continue;
-            const int* vals = coord == 0 ? kernels : coord == 1 ? blocks : coord == 2 ? shared : coord == 3 ? refills
-                            : coord == 4 ? postpones : per_sm;
-            const int nv = coord <= 2 ? 3 : coord == 5 ? 5 : 6;
+            if (best.kernel == gbpt::kTraceKernelPerRay && coord >= 4) break;
+            if (best.kernel == gbpt::kTraceKernelFetch && (coord == 4 || coord == 5)) continue;
+            const int* vals = coord == 0 ? kernels : coord == 1 ? blocks : coord == 2 ? shared
+                            : coord == 3 ? binary : coord == 4 ? refills : coord == 5 ? postpones : per_sm;
+            const int nv = coord <= 2 ? 3 : coord == 3 ? 2 : coord == 6 ? 5 : 6;
             for (int k = 0; k < nv && e == cudaSuccess; k++)
             {
                 gbpt::TraceConfig c = best;
                 int* field = coord == 0 ? &c.kernel : coord == 1 ? &c.block : coord == 2 ? &c.shared_stack
-                           : coord == 3 ? &c.refill_below : coord == 4 ? &c.postpone_below : &c.blocks_per_sm;
+                           : coord == 3 ? &c.top_levels : coord == 4 ? &c.refill_below
+                           : coord == 5 ? &c.postpone_below : &c.blocks_per_sm;
                 if (*field == vals[k]) continue;
                 *field = vals[k];
+                // the top levels in shared memory come with the local-memory stack only
+                if (c.top_levels && c.shared_stack != 0)
+                {
+                    if (coord == 2)
+                        c.top_levels = 0;
+                    else
+                        c.shared_stack = 0;
+                }
                 float ms = 0.0f;
                 e = timed(c, ms);
                 if (e == cudaSuccess && ms < best_ms)

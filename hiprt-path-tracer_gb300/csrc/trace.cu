@@ -12,6 +12,7 @@
 // core::trace_ray: the closest hit does not depend on the visiting order (ties go to the lowest
 // primitive index), the any-hit result is the occlusion bit.
 // The counting variant (statistics for the roofline) runs the per-ray traversal of trace_core.h.
+#include <algorithm>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -22,6 +23,7 @@ namespace gbpt {
 namespace {
 
 constexpr int kThreads = 128;
+constexpr int64_t kTopNodes = 1 + 8 + 64;  // staged nodes with top_levels: a full 8-wide tree's top three levels
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
 // v-th ray of a warp: its (v / 32)-th group of 32 consecutive rays, the groups being dealt
@@ -36,7 +38,21 @@ __device__ __forceinline__ int64_t warp_ray(int64_t v, int64_t warp, int64_t n_w
 // dynamic shared memory of the traversal kernels: SH stack entries per thread, entry-major
 extern __shared__ uint2 trace_sh_stack[];
 
-template <bool ANY_HIT, int SH, int TRI>
+// The n_top nodes nearest the root (breadth-first order: the root, its children, theirs) copied
+// from global memory into dynamic shared memory after the SH-deep stacks of the block, by all its
+// threads; returns their shared copy (nullptr when n_top is 0). Every thread of the block must call
+// it before any returns.
+template <int SH>
+__device__ __forceinline__ const uint4* stage_top_nodes(const uint4* __restrict__ nodes, uint32_t n_top)
+{
+    if (n_top == 0u) return nullptr;
+    uint4* top = reinterpret_cast<uint4*>(trace_sh_stack + SH * blockDim.x);
+    for (uint32_t i = threadIdx.x; i < 5u * n_top; i += blockDim.x) top[i] = __ldg(nodes + i);
+    __syncthreads();
+    return top;
+}
+
+template <bool ANY_HIT, int SH, int TRI, bool TOP>
 __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict__ nodes,
                                                              const float4* __restrict__ tris,
                                                              const float4* __restrict__ origin_tmin,
@@ -44,8 +60,9 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
                                                              const int32_t* __restrict__ last_prim, int64_t n_rays,
                                                              int64_t rays_per_warp, int post_cap, int refill_below,
                                                              int postpone_below, float4* __restrict__ hits,
-                                                             uint8_t* __restrict__ occluded)
+                                                             uint8_t* __restrict__ occluded, uint32_t n_top)
 {
+    const uint4* top = TOP ? stage_top_nodes<SH>(nodes, n_top) : nullptr;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -163,9 +180,26 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
                 if (ngroup.y & 0xFF000000u) stack.push(sp, ngroup, sh_col, sh_stride);
                 const uint32_t slot = (bit - 24u) ^ oct_inv;
                 const uint32_t rel = __popc(hits_imask & ~(0xFFFFFFFFu << slot));
-                const uint4* np = nodes + 5 * (size_t)(ngroup.x + rel);
-                const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
-                            w4 = __ldg(np + 4);
+                const uint32_t ni = ngroup.x + rel;
+                uint4 w0, w1, w2, w3, w4;
+                if (TOP && ni < n_top)
+                {
+                    const uint4* tp = top + 5 * ni;
+                    w0 = tp[0];
+                    w1 = tp[1];
+                    w2 = tp[2];
+                    w3 = tp[3];
+                    w4 = tp[4];
+                }
+                else
+                {
+                    const uint4* np = nodes + 5 * (size_t)ni;
+                    w0 = __ldg(np + 0);
+                    w1 = __ldg(np + 1);
+                    w2 = __ldg(np + 2);
+                    w3 = __ldg(np + 3);
+                    w4 = __ldg(np + 4);
+                }
                 const uint32_t hm = core::intersect_children(w0, w1, w2, w3, w4, ox, oy, oz, idx, idy, idz, tmin,
                                                              ANY_HIT ? tmax : t_best, oct_inv);
                 ngroup = make_uint2(w1.x, (hm & 0xFF000000u) | (w0.w >> 24));
@@ -207,15 +241,16 @@ __global__ void __launch_bounds__(256) trace_persistent(const uint4* __restrict_
 // Per-lane fetch: the per-ray loop (a node, then all triangles of its hit leaves, then a pop), and
 // a lane whose ray finished takes the next ray of its warp's chunk at once (a shared-memory
 // counter per warp), so lanes do not wait for the warp's longest ray.
-template <bool ANY_HIT, int SH, int TRI>
+template <bool ANY_HIT, int SH, int TRI, bool TOP>
 __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                                    const float4* __restrict__ origin_tmin,
                                                    const float4* __restrict__ dir_tmax,
                                                    const int32_t* __restrict__ last_prim, int64_t n_rays,
                                                    int64_t rays_per_warp, float4* __restrict__ hits,
-                                                   uint8_t* __restrict__ occluded)
+                                                   uint8_t* __restrict__ occluded, uint32_t n_top)
 {
     __shared__ unsigned int next_ray[8];  // per warp of the block (<= 256 threads)
+    const uint4* top = TOP ? stage_top_nodes<SH>(nodes, n_top) : nullptr;
     const int wib = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) next_ray[wib] = 0u;
     __syncwarp();
@@ -227,9 +262,10 @@ __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nod
         const int64_t ray = warp_ray(v, warp, n_warps);
         if (v >= rays_per_warp || ray >= n_rays) break;
         uint32_t cn = 0, ct = 0;
-        const float4 h = core::trace_ray<ANY_HIT, false, SH, TRI>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
-                                                                  last_prim ? last_prim[ray] : -1, cn, ct,
-                                                                  trace_sh_stack + threadIdx.x, blockDim.x);
+        const float4 h = core::trace_ray<ANY_HIT, false, SH, TRI, TOP>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
+                                                                       last_prim ? last_prim[ray] : -1, cn, ct,
+                                                                       trace_sh_stack + threadIdx.x, blockDim.x, top,
+                                                                       n_top);
         if (ANY_HIT)
         {
             if (occluded) occluded[ray] = __float_as_int(h.w) >= 0 ? 1 : 0;
@@ -240,20 +276,21 @@ __global__ void __launch_bounds__(256) trace_fetch(const uint4* __restrict__ nod
 }
 
 // per-ray traversal, one thread per ray; COUNT adds node / triangle counters (statistics)
-template <bool ANY_HIT, bool COUNT, int SH, int TRI>
+template <bool ANY_HIT, bool COUNT, int SH, int TRI, bool TOP>
 __global__ void __launch_bounds__(256) trace_ray_kernel(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                                                const float4* __restrict__ origin_tmin,
                                                                const float4* __restrict__ dir_tmax,
                                                                const int32_t* __restrict__ last_prim, int64_t n_rays,
                                                                float4* __restrict__ hits, uint8_t* __restrict__ occluded,
-                                                               unsigned long long* __restrict__ counters)
+                                                               unsigned long long* __restrict__ counters, uint32_t n_top)
 {
+    const uint4* top = TOP ? stage_top_nodes<SH>(nodes, n_top) : nullptr;
     const int64_t ray = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ray >= n_rays) return;
     uint32_t n_nodes = 0, n_tris = 0;
-    const float4 h = core::trace_ray<ANY_HIT, COUNT, SH, TRI>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
-                                                              last_prim ? last_prim[ray] : -1, n_nodes, n_tris,
-                                                              trace_sh_stack + threadIdx.x, blockDim.x);
+    const float4 h = core::trace_ray<ANY_HIT, COUNT, SH, TRI, TOP>(nodes, tris, origin_tmin[ray], dir_tmax[ray],
+                                                                   last_prim ? last_prim[ray] : -1, n_nodes, n_tris,
+                                                                   trace_sh_stack + threadIdx.x, blockDim.x, top, n_top);
     if (ANY_HIT)
     {
         if (occluded) occluded[ray] = __float_as_int(h.w) >= 0 ? 1 : 0;
@@ -296,6 +333,7 @@ TraceConfig default_trace_config(bool any_hit)
     c.blocks_per_sm = 8;
     c.shared_stack = 0;
     c.triangle_test = core::kTriMollerTrumbore;
+    c.top_levels = 0;
     return c;
 }
 
@@ -306,13 +344,14 @@ bool valid_trace_config(const TraceConfig& c)
            block_ok && c.refill_below >= 1 &&
            c.refill_below <= 32 && c.postpone_below >= 0 && c.postpone_below <= 32 && c.blocks_per_sm >= 1 &&
            c.blocks_per_sm <= 64 && (c.shared_stack == 0 || c.shared_stack == 8 || c.shared_stack == 16) &&
-           (c.triangle_test == core::kTriMollerTrumbore || c.triangle_test == core::kTriWatertight);
+           (c.triangle_test == core::kTriMollerTrumbore || c.triangle_test == core::kTriWatertight) &&
+           (c.top_levels == 0 || (c.top_levels == 1 && c.shared_stack == 0));
 }
 
 namespace {
 
 // the launches of one shared-stack depth SH (dynamic shared memory: SH entries per thread)
-template <int SH, int TRI>
+template <int SH, int TRI, bool TOP>
 cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, const float* dir_tmax,
                             const int32_t* last_prim, int64_t n_rays, float* hits, uint8_t* occluded, bool any_hit,
                             unsigned long long* counters, cudaStream_t stream, const TraceConfig& cfg)
@@ -322,31 +361,34 @@ cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, cons
     const float4* o = reinterpret_cast<const float4*>(origin_tmin);
     const float4* d = reinterpret_cast<const float4*>(dir_tmax);
     float4* h = reinterpret_cast<float4*>(hits);
+    // the nodes nearest the root staged in shared memory (top_levels): the root's three levels
+    const uint32_t n_top = (TOP && !counters) ? (uint32_t)std::min<int64_t>(kTopNodes, bvh.n_nodes) : 0u;
+    const size_t top_bytes = (size_t)n_top * 5 * sizeof(uint4);
     if (counters || cfg.kernel == kTraceKernelPerRay)
     {
         const int threads = counters ? kThreads : cfg.block;
         const int64_t blocks = (n_rays + threads - 1) / threads;
-        const size_t smem = (size_t)SH * threads * sizeof(uint2);
+        const size_t smem = (size_t)SH * threads * sizeof(uint2) + top_bytes;
         if (counters)
         {
             if (any_hit)
-                trace_ray_kernel<true, true, 0, TRI><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
-                                                                                     h, occluded, counters);
+                trace_ray_kernel<true, true, 0, TRI, false><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+                                                                                     h, occluded, counters, 0u);
             else
-                trace_ray_kernel<false, true, 0, TRI><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim,
-                                                                                      n_rays, h, occluded, counters);
+                trace_ray_kernel<false, true, 0, TRI, false><<<(unsigned)blocks, threads, 0, stream>>>(nodes, tris, o, d, last_prim,
+                                                                                      n_rays, h, occluded, counters, 0u);
         }
         else if (any_hit)
-            trace_ray_kernel<true, false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
-                                                                                  h, occluded, nullptr);
+            trace_ray_kernel<true, false, SH, TRI, TOP><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+                                                                                  h, occluded, nullptr, n_top);
         else
-            trace_ray_kernel<false, false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
-                                                                                   h, occluded, nullptr);
+            trace_ray_kernel<false, false, SH, TRI, TOP><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays,
+                                                                                   h, occluded, nullptr, n_top);
         return cudaGetLastError();
     }
     // persistent grids: blocks_per_sm blocks per SM, each warp owning a contiguous chunk of rays
     const int threads = cfg.block;
-    const size_t smem = (size_t)SH * threads * sizeof(uint2);
+    const size_t smem = (size_t)SH * threads * sizeof(uint2) + top_bytes;
     if (cfg.kernel == kTraceKernelFetch)
     {
         const int64_t max_blocks = (int64_t)sm_count() * cfg.blocks_per_sm;
@@ -355,11 +397,11 @@ cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, cons
         const int64_t warps = blocks * (threads / 32);
         const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
         if (any_hit)
-            trace_fetch<true, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
-                                                                        occluded);
+            trace_fetch<true, SH, TRI, TOP><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+                                                                        occluded, n_top);
         else
-            trace_fetch<false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
-                                                                         occluded);
+            trace_fetch<false, SH, TRI, TOP><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp, h,
+                                                                         occluded, n_top);
         return cudaGetLastError();
     }
     const int64_t max_blocks = (int64_t)sm_count() * cfg.blocks_per_sm;
@@ -369,13 +411,13 @@ cudaError_t launch_trace_sh(const DeviceBVH& bvh, const float* origin_tmin, cons
     const int64_t per_warp = ((n_rays + 31) / 32 + warps - 1) / warps * 32;  // whole groups of 32
     const int post_cap = kTraversalStack - bvh.depth - 1 > 0 ? kTraversalStack - bvh.depth - 1 : 0;
     if (any_hit)
-        trace_persistent<true, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
+        trace_persistent<true, SH, TRI, TOP><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
                                                                          post_cap, cfg.refill_below, cfg.postpone_below, h,
-                                                                         occluded);
+                                                                         occluded, n_top);
     else
-        trace_persistent<false, SH, TRI><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
+        trace_persistent<false, SH, TRI, TOP><<<(unsigned)blocks, threads, smem, stream>>>(nodes, tris, o, d, last_prim, n_rays, per_warp,
                                                                           post_cap, cfg.refill_below, cfg.postpone_below,
-                                                                          h, occluded);
+                                                                          h, occluded, n_top);
     return cudaGetLastError();
 }
 
@@ -387,27 +429,34 @@ cudaError_t launch_trace(const DeviceBVH& bvh, const float* origin_tmin, const f
 {
     if (n_rays <= 0) return cudaSuccess;
     const TraceConfig cfg = cfg_in ? *cfg_in : default_trace_config(any_hit);
-    // the counting build traces with the parity triangle test (node and triangle counts)
+    // the counting build traces with the parity triangle test (node and triangle counts); the top
+    // levels in shared memory come with the local-memory stack only (shared_stack 0)
     if (cfg.triangle_test == core::kTriWatertight && !counters)
     {
+        if (cfg.top_levels)
+            return launch_trace_sh<0, core::kTriWatertight, true>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                  occluded, any_hit, counters, stream, cfg);
         switch (cfg.shared_stack)
         {
-        case 8: return launch_trace_sh<8, core::kTriWatertight>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
-                                                                occluded, any_hit, counters, stream, cfg);
-        case 16: return launch_trace_sh<16, core::kTriWatertight>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
-                                                                  occluded, any_hit, counters, stream, cfg);
-        default: return launch_trace_sh<0, core::kTriWatertight>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
-                                                                 occluded, any_hit, counters, stream, cfg);
+        case 8: return launch_trace_sh<8, core::kTriWatertight, false>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                       occluded, any_hit, counters, stream, cfg);
+        case 16: return launch_trace_sh<16, core::kTriWatertight, false>(bvh, origin_tmin, dir_tmax, last_prim, n_rays,
+                                                                         hits, occluded, any_hit, counters, stream, cfg);
+        default: return launch_trace_sh<0, core::kTriWatertight, false>(bvh, origin_tmin, dir_tmax, last_prim, n_rays,
+                                                                        hits, occluded, any_hit, counters, stream, cfg);
         }
     }
+    if (cfg.top_levels && !counters)
+        return launch_trace_sh<0, core::kTriMollerTrumbore, true>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                  occluded, any_hit, counters, stream, cfg);
     switch (counters ? 0 : cfg.shared_stack)
     {
-    case 8: return launch_trace_sh<8, core::kTriMollerTrumbore>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
-                                                                occluded, any_hit, counters, stream, cfg);
-    case 16: return launch_trace_sh<16, core::kTriMollerTrumbore>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
-                                                                  occluded, any_hit, counters, stream, cfg);
-    default: return launch_trace_sh<0, core::kTriMollerTrumbore>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
-                                                                 occluded, any_hit, counters, stream, cfg);
+    case 8: return launch_trace_sh<8, core::kTriMollerTrumbore, false>(bvh, origin_tmin, dir_tmax, last_prim, n_rays, hits,
+                                                                       occluded, any_hit, counters, stream, cfg);
+    case 16: return launch_trace_sh<16, core::kTriMollerTrumbore, false>(bvh, origin_tmin, dir_tmax, last_prim, n_rays,
+                                                                         hits, occluded, any_hit, counters, stream, cfg);
+    default: return launch_trace_sh<0, core::kTriMollerTrumbore, false>(bvh, origin_tmin, dir_tmax, last_prim, n_rays,
+                                                                        hits, occluded, any_hit, counters, stream, cfg);
     }
 }
 

@@ -332,11 +332,12 @@ struct TraversalStack
 // Traces one ray. Closest hit: returns the hit as (t, u, v, prim bits), prim = -1 and t = -1 on a
 // miss. Any hit: returns prim >= 0 iff some accepted hit has t < tmax. Counts visited nodes and
 // tested triangles when COUNT is set. SH > 0: the bottom SH stack entries live in the shared
-// column sh_col (stride sh_stride).
-template <bool ANY_HIT, bool COUNT, int SH = 0, int TRI = kTriMollerTrumbore>
+// column sh_col (stride sh_stride). TOP: the n_top nodes nearest the root are read from 'top'
+// (shared memory) instead of 'nodes'.
+template <bool ANY_HIT, bool COUNT, int SH = 0, int TRI = kTriMollerTrumbore, bool TOP = false>
 GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const float4 ot,
                          const float4 dt, const int32_t skip_prim, uint32_t& n_nodes, uint32_t& n_tris,
-                         uint2* sh_col = nullptr, int sh_stride = 0)
+                         uint2* sh_col = nullptr, int sh_stride = 0, const uint4* top = nullptr, uint32_t n_top = 0)
 {
     const float ox = ot.x, oy = ot.y, oz = ot.z, ray_tmin = ot.w;
     const float dx = dt.x, dy = dt.y, dz = dt.z;
@@ -365,9 +366,26 @@ GBPT_HD float4 trace_ray(const uint4* __restrict__ nodes, const float4* __restri
             const uint32_t slot = (bit - 24u) ^ oct_inv;
             const uint32_t rel = __popc(hits_imask & ~(0xFFFFFFFFu << slot));
             const uint32_t ni = ngroup.x + rel;
-            const uint4* np = nodes + 5 * (size_t)ni;
-            const uint4 w0 = GBPT_LDG(np + 0), w1 = GBPT_LDG(np + 1), w2 = GBPT_LDG(np + 2), w3 = GBPT_LDG(np + 3),
-                        w4 = GBPT_LDG(np + 4);
+            uint4 w0, w1, w2, w3, w4;
+            if (TOP && ni < n_top)
+            {
+                // one of the nodes nearest the root, staged in shared memory by the kernel
+                const uint4* tp = top + 5 * ni;
+                w0 = tp[0];
+                w1 = tp[1];
+                w2 = tp[2];
+                w3 = tp[3];
+                w4 = tp[4];
+            }
+            else
+            {
+                const uint4* np = nodes + 5 * (size_t)ni;
+                w0 = GBPT_LDG(np + 0);
+                w1 = GBPT_LDG(np + 1);
+                w2 = GBPT_LDG(np + 2);
+                w3 = GBPT_LDG(np + 3);
+                w4 = GBPT_LDG(np + 4);
+            }
             if (COUNT) n_nodes++;
             const uint32_t hm = intersect_children(w0, w1, w2, w3, w4, ox, oy, oz, idx, idy, idz, ray_tmin,
                                                    ANY_HIT ? dt.w : t_best, oct_inv);

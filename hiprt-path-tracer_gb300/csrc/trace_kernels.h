@@ -28,6 +28,7 @@ struct TraceConfig
     int32_t blocks_per_sm;   // persistent grid
     int32_t shared_stack;    // traversal-stack entries per thread in shared memory (0, 8 or 16)
     int32_t triangle_test;   // core::kTriMollerTrumbore (parity) or core::kTriWatertight
+    int32_t top_levels;      // 1: the 73 nodes nearest the root staged in shared memory per block
 };
 
 TraceConfig default_trace_config(bool any_hit);

@@ -32,7 +32,8 @@ class BvhStats(ctypes.Structure):
 
 class TraceConfig(ctypes.Structure):
     _fields_ = [("kernel", i32), ("block", i32), ("refill_below", i32), ("postpone_below", i32),
-                ("blocks_per_sm", i32), ("shared_stack", i32), ("triangle_test", i32), ("reserved", i32)]
+                ("blocks_per_sm", i32), ("shared_stack", i32), ("triangle_test", i32), ("top_levels", i32),
+                ("reserved", i32 * 4)]
 
 
 class GbptError(RuntimeError):

@@ -133,8 +133,12 @@ typedef struct gbpt_trace_config {
     int32_t shared_stack;    /* traversal-stack entries per thread kept in shared memory (0, 8 or 16;
                                 deeper entries in local memory); 0 in configurations written before */
     int32_t triangle_test;   /* GBPT_TRIANGLE_* [GBPT_TRIANGLE_MOLLER_TRUMBORE]; the autotuner keeps it */
-    int32_t reserved;
+    int32_t top_levels;      /* 1: each block first copies the 73 nodes nearest the root (the top three
+                                levels of the 8-wide BVH, 5.8 KB) into shared memory and fetches them
+                                from there; needs shared_stack 0 [0] */
+    int32_t reserved[4];
 } gbpt_trace_config;
+
 
 /* Ray/triangle test of a traversal (gbpt_trace_config.triangle_test):
  *   GBPT_TRIANGLE_MOLLER_TRUMBORE: the reference's Moller-Trumbore (src/Renderer/Triangle.h:20-63)

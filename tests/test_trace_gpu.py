@@ -125,9 +125,10 @@ def test_full_size_scene_sampled(cuda, oracle):
 
 @pytest.mark.parametrize("any_hit", [False, True])
 def test_every_launch_configuration_gives_identical_results(cuda, any_hit):
-    """Per-ray and persistent kernels over block sizes, refill / postpone thresholds and shared-memory
-    stack depths return the same hits bit for bit (the closest hit does not depend on the visiting order), and the
-    autotuner returns a valid configuration whose results are again identical."""
+    """Per-ray and persistent kernels over block sizes, refill / postpone thresholds, shared-memory
+    stack depths and the top BVH levels in shared memory return the same hits bit for bit
+    (the closest hit does not depend on the visiting order), and the autotuner returns a valid
+    configuration whose results are again identical."""
     mesh, closest, _, shadow, _, _ = load_golden("terrain")
     bvh = gbpt.BVH(mesh.indices, mesh.positions)
     rays = shadow if any_hit else closest
@@ -140,6 +141,8 @@ def test_every_launch_configuration_gives_identical_results(cuda, any_hit):
                 for sh in (0, 8, 16)]
     configs += [dict(kernel=3, block=b, blocks_per_sm=s, shared_stack=sh)
                 for b, s in [(128, 8), (256, 4), (32, 64), (64, 1)] for sh in (0, 8, 16)]
+    # the top levels of the BVH staged in shared memory, in every kernel
+    configs += [dict(c, top_levels=1) for c in configs if c.get("shared_stack", 0) == 0]
     for cfg in configs:
         got = run(o, d, lp, **cfg).cpu().numpy()
         assert np.array_equal(got.view(np.uint8), base.view(np.uint8)), cfg
@@ -154,7 +157,7 @@ def test_trace_config_validation(cuda):
     mesh, *_ = load_golden("cornell")
     bvh = gbpt.BVH(mesh.indices, mesh.positions)
     for bad in (dict(kernel=4), dict(block=96), dict(refill_below=0), dict(postpone_below=33), dict(blocks_per_sm=0),
-                dict(shared_stack=4), dict(shared_stack=-8)):
+                dict(shared_stack=4), dict(shared_stack=-8), dict(top_levels=2), dict(top_levels=1, shared_stack=8)):
         with pytest.raises(GbptError):
             bvh.set_trace_config(False, **bad)
 
