@@ -248,13 +248,14 @@ def _relmse(img, ref):
 
 
 RENDER_WORKLOADS = ("cornell", "envmap", "restir", "guided", "guided_indirect_cornell", "batch")
+OPTIONAL_WORKLOADS = ("guided_spec",)  # run only when named in --workloads
 
 
 def render_workloads(log, guided_res=(480, 270), cpu_baseline=True, only=RENDER_WORKLOADS, restir_res=(1920, 1080)):
     """Path-tracing workloads (one GPU, inputs resident; timed with CUDA events on the current stream):
 
     cornell     the Cornell box, 256 x 256, 64 launches x 1 spp, 4 bounces, RR from bounce 3, uniform
-                light sampling NEE + BSDF MIS, Lambertian; relMSE against a 16384-spp FP64 image;
+                light sampling NEE + BSDF MIS, Lambertian; relMSE against a 65536-spp FP64 image;
                 cpu_baseline = the oracle's restatement of the reference's CPU estimator on all host
                 cores over a bounded sample.
     envmap      the Cornell box under a 2048 x 1024 sky, 512 x 512: envmap table build time and samples/s
@@ -297,25 +298,25 @@ def render_workloads(log, guided_res=(480, 270), cpu_baseline=True, only=RENDER_
     if "envmap" in only:
         out["envmap"] = envmap_workload(timed, cscene)
     del cscene
-    if "restir" in only or "guided" in only:
-        many_light_workloads(out, log, timed, guided_res, only, restir_res)
+    if "restir" in only or "guided" in only or "guided_spec" in only:
+        many_light_workloads(out, log, timed, guided_res, only, restir_res, cpu_baseline)
     # ---- guided against plain on the indirectly lit Cornell box ----
     if "guided_indirect_cornell" in only:
         out["guided_indirect_cornell"] = guided_indirect_cornell(timed)
     torch.cuda.empty_cache()
     # ---- batched jobs ----
     if "batch" in only:
-        out["batch"] = batch_workload(timed, log)
+        out["batch"] = batch_workload(timed, log, cpu_baseline=cpu_baseline)
     return out
 
 
 def cornell_workload(out, cb, cscene, timed, cpu_baseline):
     import torch
     import gbpt
+    # the FP64-accumulated 65,536-spp reference image (256 launches of 256 spp, independent seed)
     ref = gbpt.Renderer(cscene, gbpt.cornell_settings(256, 256, samples_per_launch=256, seed=1000))
-    ref.render(64)
-    torch.cuda.synchronize()
-    cref = ref.image_sums()[1] / (256 * 64)
+    t_ref = timed(lambda: ref.render(256))
+    cref = ref.image_sums()[1] / (256 * 256)
     del ref
     r = gbpt.Renderer(cscene, gbpt.cornell_settings(256, 256, samples_per_launch=1, seed=1))
     r.render(3)
@@ -325,7 +326,8 @@ def cornell_workload(out, cb, cscene, timed, cpu_baseline):
     rays = st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
     out["cornell"] = {"config": "256x256, 64 launches x 1 spp, 4 bounces, RR from 3, uniform NEE + BSDF MIS, Lambert",
                       "ms": ms, "samples_per_s": 256 * 256 * 64 / (ms * 1e-3), "mrays_per_s": rays / (ms * 1e-3) / 1e6,
-                      "relmse_vs_16384spp_fp64": _relmse(r.image_sums()[1] / 64, cref)}
+                      "relmse_vs_65536spp_fp64": _relmse(r.image_sums()[1] / 64, cref),
+                      "reference_ms": t_ref}
     del r
     if cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -343,7 +345,7 @@ def cornell_workload(out, cb, cscene, timed, cpu_baseline):
                                           "kind": "port", "sample": f"256x256 x {spp} spp, {dt:.2f}s"}
 
 
-def many_light_workloads(out, log, timed, guided_res, only, restir_res=(1920, 1080)):
+def many_light_workloads(out, log, timed, guided_res, only, restir_res=(1920, 1080), cpu_baseline=True):
     RW, RH = restir_res
     import numpy as np
     import torch
@@ -382,7 +384,84 @@ def many_light_workloads(out, log, timed, guided_res, only, restir_res=(1920, 10
         restir_workload(out, restir_frames, RW, RH)
     if "guided" in only:
         guided_workload(out, scene, S, settings, timed, guided_res, log)
+    if cpu_baseline and ("restir" in out or "guided" in out):
+        many_light_cpu_baselines(out, scene, S, settings, log)
+    if "guided_spec" in only:
+        guided_spec_workload(out, scene, S, settings, timed, log)
     del scene
+
+
+def oracle_principled_scene(mesh, material_of, materials, light_table, log, cores):
+    """The oracles' view of a principled scene for a CPU baseline: the triangle soup, the
+    coat-roughened material records, the light table, and an octree over the triangles set as
+    the oracles' scene accelerator (the exhaustive test would not finish on these scenes).
+    Returns (pyoracle, scene dict, effective materials, octree, build seconds)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    from gbpt import materials as M
+    soup = np.ascontiguousarray(mesh.triangle_soup(), np.float32)
+    eff = M.pack_many([M.coat_roughened(M.unpack(materials[i])) for i in range(len(materials))])
+    t0 = time.time()
+    oc = pyoracle.Oracle().octree(soup)
+    build_s = time.time() - t0
+    pyoracle.set_scene_accel(oc)
+    sc = dict(soup=soup, material_of=np.ascontiguousarray(material_of, np.int32),
+              emission=np.ascontiguousarray(materials[:, 4:7], np.float32), emissive=light_table["emissive"],
+              alias_prob=light_table["probas"], alias_idx=light_table["alias"], power_sum=light_table["power_sum"])
+    log(f"CPU baseline: octree over {len(soup)} triangles in {build_s:.1f}s ({cores} threads)")
+    return pyoracle, sc, eff, oc, build_s
+
+
+def many_light_cpu_baselines(out, scene, S, settings, log, W=480, H=270):
+    """CPU baselines of the many-light workloads: the oracles (the reference's estimator restated,
+    tracing through an octree restating the reference's CPU BVH, shading with the library's
+    principled BSDF compiled for the host: the reference's own BSDF needs the reference tree) on
+    all host cores, on a W x H rendering of the same camera:
+      restir: one frame's ReSTIR DI passes (G-buffer, 32 + 1 initial candidates with visibility
+        reuse, spatial reuse of 5 neighbours) plus the path's 3 bounces of MIS next-event
+        estimation, in samples (pixels) per second;
+      guided: plain path tracing with 8 bounces, 1 spp (the reference has no guiding), in samples
+        per second."""
+    cores = os.cpu_count() or 1
+    pyoracle, sc, eff, oc, build_s = oracle_principled_scene(S.mesh, S.material_of_triangle, S.materials,
+                                                               scene.light_table(), log, cores)
+    try:
+        from gbpt.render import look_at_camera
+        iv, ip = look_at_camera(S.eye, S.target, vfov_deg=S.vfov_deg, aspect=W / H)
+        ivm = np.asarray(iv, np.float32).reshape(4, 4)
+        cam = [float(ivm[0, 3]), float(ivm[1, 3]), float(ivm[2, 3])]
+        if "restir" in out:
+            si = [W, H, 1, 0, 0, 1, 32, 1, 1, 0, 8, 1, 5, 20, 1, 1]
+            sf = [4.0, 30.0, 0.906307787, 0.1, *cam, *cam]
+            t0 = time.perf_counter()
+            gb = pyoracle.restir_gbuffer(sc["soup"], sc["material_of"], eff, W, H, 1, 0, True, iv, ip, nthreads=cores)
+            init = pyoracle.restir_pass(0, sc, eff, si, sf, None, gb, nthreads=cores, bsdf="host")
+            pyoracle.restir_pass(2, sc, eff, si, sf, None, gb, inp=init, spatial_index=0, spatial_seed=1,
+                                 nthreads=cores, bsdf="host")
+            t_restir = time.perf_counter() - t0
+            st = settings(W, H, 1, 3, 1)
+            t0 = time.perf_counter()
+            pyoracle.pt_render_principled(sc["soup"], sc["material_of"], eff, sc["emission"], sc["emissive"],
+                                          sc["alias_prob"], sc["alias_idx"], sc["power_sum"], st, 1, nthreads=cores,
+                                          bsdf="host")
+            t_pt = time.perf_counter() - t0
+            dt = t_restir + t_pt
+            out["restir"]["cpu_baseline"] = {
+                "value": W * H / dt, "unit": "samples/s", "cores": cores, "kind": "port",
+                "sample": f"{W}x{H}, 1 frame: ReSTIR DI passes {t_restir:.2f}s + 3-bounce path tracing {t_pt:.2f}s "
+                          f"(octree built in {build_s:.1f}s, not timed)"}
+        if "guided" in out:
+            st = settings(W, H, 1, 8, 2)
+            t0 = time.perf_counter()
+            pyoracle.pt_render_principled(sc["soup"], sc["material_of"], eff, sc["emission"], sc["emissive"],
+                                          sc["alias_prob"], sc["alias_idx"], sc["power_sum"], st, 1, nthreads=cores,
+                                          bsdf="host")
+            dt = time.perf_counter() - t0
+            out["guided"]["cpu_baseline"] = {"value": W * H / dt, "unit": "samples/s", "cores": cores, "kind": "port",
+                                             "sample": f"{W}x{H} x 1 spp, 8 bounces, plain path tracing, {dt:.2f}s"}
+    finally:
+        pyoracle.set_scene_accel(None)
+        del oc
 
 
 def restir_workload(out, restir_frames, RW=1920, RH=1080):
@@ -458,6 +537,46 @@ def guided_workload(out, scene, S, settings, timed, guided_res, log):
                      "guided_relmse_median": float(np.median([b for _, b in guided])),
                      "primary_direct_only_relmse": float(np.mean([b for _, b in direct])),
                      "primary_direct_share_of_relmse": float(np.mean([b for _, b in direct])) / ep}
+
+
+def guided_spec_workload(out, scene, S, settings, timed, log, W=1920, H=1080, spp=256, nb=8, ref_spp=4096):
+    """Guided against plain at the guided-rendering configuration's size: the many-light scene at
+    1920 x 1080, 8 bounces, one 256-spp image per arm (256 launches of 1 spp; ReSTIR DI at the
+    primary vertex in both, the guide trained online from the first launch), relMSE against an
+    FP64-accumulated plain image of ref_spp samples per pixel (64 launches of 64 spp). Not in the
+    default workload list: the reference alone is ~8.5G path samples."""
+    import numpy as np
+    import torch
+    import gbpt
+    from gbpt import guide
+    from gbpt.render import guide_render_settings, restir_di_settings
+    ref = gbpt.Renderer(scene, settings(W, H, 64, nb, 5000))
+    t_ref = timed(lambda: ref.render(ref_spp // 64))
+    gref = ref.image_sums()[1] / ref_spp
+    del ref
+    torch.cuda.empty_cache()
+    rs = restir_di_settings(light_candidates=32, bsdf_candidates=1, m_cap=20, spatial_passes=1, spatial_neighbors=5,
+                            spatial_radius=30)
+    res = {}
+    for name, guided, seed in (("plain", False, 5100), ("guided", True, 5200)):
+        r = gbpt.Renderer(scene, settings(W, H, 1, nb, seed))
+        r.set_restir_di(rs)
+        gd = None
+        if guided:
+            gd = guide.Guide(scene_min=S.box[0], scene_max=S.box[1])
+            r.set_guide(gd, guide_render_settings())
+        t = timed(lambda: r.render(spp))
+        res[name] = (t, _relmse(r.image_sums()[1] / spp, gref), gd.error_flag() if gd else 0)
+        log(f"guided_spec {name}: {t / 1e3:.1f} s, relMSE {res[name][1]:.4f}")
+        del r, gd
+        torch.cuda.empty_cache()
+    (tp, ep, _), (tg, eg, flag) = res["plain"], res["guided"]
+    out["guided_spec"] = {"config": f"many-light scene, {W}x{H}, {nb} bounces, {spp} spp per arm (launches of 1 spp), "
+                                    "ReSTIR DI at the primary vertex in both arms, guide trained online from the first "
+                                    f"launch; relMSE vs a {ref_spp}-spp plain FP64 image",
+                          "plain_ms": tp, "plain_relmse": ep, "guided_ms": tg, "guided_relmse": eg,
+                          "time_to_equal_relmse_speedup": (ep * tp) / (eg * tg), "reference_ms": t_ref,
+                          "guide_error_flag": flag}
 
 
 def envmap_workload(timed, cscene, res=512, launches=32):
@@ -538,22 +657,54 @@ def batch_jobs(n_jobs=48, seed=1):
                             nb_bounces=int(rng.integers(2, 17)), light_sampling=LIGHT_POWER, bsdf=BSDF_PRINCIPLED,
                             seed=int(rng.integers(1, 1 << 30)), inverse_view=iv, inverse_projection=ip)
         jobs.append((scene, st, {"res": res, "triangles": int(mesh.n_triangles), "emitters": n_emit,
-                                 "bounces": st.nb_bounces, "spp": st.samples_per_launch}))
+                                 "bounces": st.nb_bounces, "spp": st.samples_per_launch},
+                     (mesh, np.concatenate(mat_of).astype(np.int32), M.pack_many(mats))))
     return jobs
 
 
-def batch_workload(timed, log, ref_factor=4):
+def batch_cpu_baseline(jobs, picks, log):
+    """CPU baseline of the batch: the path-tracing oracle (the reference's estimator restated,
+    tracing through an octree restating the reference's CPU BVH, shading with the library's
+    principled BSDF compiled for the host) on all host cores, one spp of each picked job at its own
+    settings; samples per second over the picked jobs."""
+    cores = os.cpu_count() or 1
+    total_px, total_s, notes = 0, 0.0, []
+    for j in picks:
+        sc, st, info, (mesh, mat_of, recs) = jobs[j]
+        pyoracle, osc, eff, oc, build_s = oracle_principled_scene(mesh, mat_of, recs, sc.light_table(), log, cores)
+        try:
+            from gbpt.render import RenderSettings
+            one = RenderSettings(**{**st.__dict__, "samples_per_launch": 1})
+            t0 = time.perf_counter()
+            pyoracle.pt_render_principled(osc["soup"], osc["material_of"], eff, osc["emission"], osc["emissive"],
+                                          osc["alias_prob"], osc["alias_idx"], osc["power_sum"], one, 1,
+                                          nthreads=cores, bsdf="host")
+            dt = time.perf_counter() - t0
+        finally:
+            pyoracle.set_scene_accel(None)
+            del oc
+        total_px += st.width * st.height
+        total_s += dt
+        notes.append(f"job {j} ({info['res']}^2, {info['triangles']} tris, {info['bounces']} bounces) {dt:.2f}s")
+    if not picks:
+        return None
+    return {"value": total_px / total_s, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": "1 spp of " + "; ".join(notes)}
+
+
+def batch_workload(timed, log, ref_factor=4, cpu_baseline=True):
     """48 jobs in one batched wavefront (one launch per stage for all jobs, one iteration captured
     as a CUDA graph and replayed). samples_per_iteration is picked by timing candidates on the jobs
     clipped to 8 spp; per-job relMSE against an FP64 image of ref_factor x the job's spp (the same
-    batch machinery, other seeds); job-completion latency from device timer stamps."""
+    batch machinery, other seeds), and for the first four 128 x 128 jobs against FP64 65,536-spp
+    images; job-completion latency from device timer stamps."""
     import torch
     import gbpt
     from gbpt.render import RenderSettings
     t0 = time.time()
     jobs = batch_jobs()
     log(f"batch: {len(jobs)} jobs built in {time.time() - t0:.1f}s")
-    pairs = [(sc, st) for sc, st, _ in jobs]
+    pairs = [(sc, st) for sc, st, _, _ in jobs]
     # autotune samples_per_iteration on the jobs clipped to 8 spp
     clip = [(sc, RenderSettings(**{**st.__dict__, "samples_per_launch": min(8, st.samples_per_launch)})) for sc, st in pairs]
     tune = {}
@@ -579,6 +730,16 @@ def batch_workload(timed, log, ref_factor=4):
         ref = rb.image_sums(j)[1] / ref_pairs[j][1].samples_per_launch
         rel.append(_relmse(imgs[j], ref))
     del rb
+    # FP64 65,536-spp references (64 launches of 1,024 spp, other seeds) for the first four 128 x 128
+    # jobs: a full-set 65,536-spp reference would be ~10^12 samples
+    small = [j for j in range(len(pairs)) if pairs[j][1].width == 128][:4]
+    rel64k, t64k = [], 0.0
+    for j in small:
+        sc, s = pairs[j]
+        rr = gbpt.Renderer(sc, RenderSettings(**{**s.__dict__, "samples_per_launch": 1024, "seed": s.seed + 104729}))
+        t64k += timed(lambda: rr.render(64))
+        rel64k.append(_relmse(imgs[j], rr.image_sums()[1] / 65536))
+        del rr
     samples = st["samples"]
     rays = st["extension_rays"] + st["shadow_rays"] + st["bsdf_light_rays"]
     return {"config": "48 jobs from seed 1: res {128,256,512,1024}^2, heightfield 64^2..512^2 cells + 0..2000 emitters, "
@@ -590,7 +751,11 @@ def batch_workload(timed, log, ref_factor=4):
             "relmse_vs_fp64": {"reference_spp_factor": ref_factor, "reference_ms": t_ref,
                                "median": float(np.median(rel)), "max": float(np.max(rel)),
                                "each": [round(x, 5) for x in rel]},
-            "jobs": [j for _, _, j in jobs]}
+            "relmse_vs_65536spp_fp64": {"jobs": small, "each": [round(x, 5) for x in rel64k],
+                                        "median": float(np.median(rel64k)) if rel64k else None,
+                                        "reference_ms": t64k},
+            "jobs": [j for _, _, j, _ in jobs],
+            "cpu_baseline": batch_cpu_baseline(jobs, small[:2], log) if cpu_baseline else None}
 
 
 def indirect_cornell_scene():
@@ -961,9 +1126,9 @@ def main():
         del bvh
         torch.cuda.empty_cache()
         only = tuple(w for w in args.workloads.split(",") if w)
-        unknown = [w for w in only if w not in RENDER_WORKLOADS]
+        unknown = [w for w in only if w not in RENDER_WORKLOADS + OPTIONAL_WORKLOADS]
         if unknown:
-            raise SystemExit(f"unknown workloads {unknown}; choose from {RENDER_WORKLOADS}")
+            raise SystemExit(f"unknown workloads {unknown}; choose from {RENDER_WORKLOADS + OPTIONAL_WORKLOADS}")
         rw, rh = (int(v) for v in args.restir_res.split("x"))
         line["render"] = render_workloads(log, cpu_baseline=not args.no_cpu_baseline, only=only, restir_res=(rw, rh))
     if rank == 0:

@@ -12,6 +12,11 @@
 #include <cstdint>
 #include <cstring>
 
+// The scene accelerator of the path-tracing and ReSTIR oracles, shared by their translation units
+// (defined in trace_oracle.cpp)
+extern "C" void* orc_scene_accel();
+extern "C" int32_t orc_octree_closest_one(void* h, const float* o, const float* d, int32_t skip, float* t_out);
+
 namespace {
 
 
@@ -192,6 +197,13 @@ V shading_normal(const Scene& s, int t, V o, V d, V ng)
 // closest hit with the self-hit filter; returns prim or -1 (lowest index on exact ties)
 int closest(const Scene& s, V o, V d, int skip, float& t_out)
 {
+    // the scene accelerator (an orc_octree_build handle over the same triangles) when one is set
+    // (orc_set_scene_accel, trace_oracle.cpp); else every triangle is tested
+    if (void* accel = orc_scene_accel())
+    {
+        const float of[3] = {o.x, o.y, o.z}, df[3] = {d.x, d.y, d.z};
+        return orc_octree_closest_one(accel, of, df, skip, &t_out);
+    }
     int best = -1;
     float bt = 0.0f;
     for (int k = 0; k < s.nt; k++)

@@ -20,6 +20,21 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
+HOST_BSDF_SO = os.path.join(HERE, "libhost_bsdf.so")
+
+
+def bsdf_callbacks(bsdf: str = "reference"):
+    """(eval, sample) function pointers of the principled BSDF the oracles shade with: the
+    reference's own (oracle/_ref/libref.so, every parity test) or, with bsdf="host", the library's
+    BSDF compiled for the host (oracle/libhost_bsdf.so; CPU baselines where the reference tree is
+    absent)."""
+    if bsdf == "host":
+        lib = ctypes.CDLL(HOST_BSDF_SO)
+        return (ctypes.cast(lib.host_principled_eval_one, ctypes.c_void_p).value,
+                ctypes.cast(lib.host_principled_sample_one, ctypes.c_void_p).value)
+    ref = ctypes.CDLL(REF_SO)
+    return (ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value,
+            ctypes.cast(ref.ref_principled_sample_one, ctypes.c_void_p).value)
 REF_ENV_SO = os.path.join(HERE, "_ref", "libref_env.so")
 REF_ENV_BILINEAR_SO = os.path.join(HERE, "_ref", "libref_env_bilinear.so")
 
@@ -102,6 +117,15 @@ class Oracle:
         out = np.zeros(3, np.float32)
         ok = self.lib.orc_mt_intersect(_ptr(tri9, _c_f), _ptr(o, _c_f), _ptr(d, _c_f), _ptr(out, _c_f))
         return bool(ok), out
+
+
+def set_scene_accel(octree: "OracleOctree | None") -> None:
+    """Makes the path-tracing and ReSTIR oracles trace through this octree (built over the same
+    triangles their next calls pass) instead of testing every triangle; None switches back. For
+    CPU baselines on large scenes; parity tests keep the exhaustive test."""
+    lib = Oracle().lib
+    lib.orc_set_scene_accel.argtypes = [ctypes.c_void_p]
+    lib.orc_set_scene_accel(octree.h if octree is not None else None)
 
 
 class OracleOctree:
@@ -314,7 +338,8 @@ def pt_render(soup, material_of, albedo, emission, emissive, alias_prob, alias_i
 
 
 def pt_render_principled(soup, material_of, pmats_effective, emission, emissive, alias_prob, alias_idx, power_sum,
-                         settings, spp, iteration_base=0, nthreads=0, env: OracleEnv | None = None, normals=None):
+                         settings, spp, iteration_base=0, nthreads=0, env: OracleEnv | None = None, normals=None,
+                         bsdf: str = "reference"):
     """Path-tracing oracle for principled scenes: the estimator of pt_render with the BSDF
     evaluated and sampled by the REFERENCE's own principled BSDF (oracle/_ref/libref.so, built
     only where the reference tree exists). pmats_effective: (M, 64) records after coat
@@ -328,9 +353,7 @@ def pt_render_principled(soup, material_of, pmats_effective, emission, emissive,
                                                  ctypes.c_float, _c_f, _c_f, ctypes.POINTER(ctypes.c_double),
                                                  ctypes.c_int, ctypes.c_void_p, _c_f]
         lib._ptp_sig = True
-    ref = ctypes.CDLL(REF_SO)
-    eval_fn = ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value
-    sample_fn = ctypes.cast(ref.ref_principled_sample_one, ctypes.c_void_p).value
+    eval_fn, sample_fn = bsdf_callbacks(bsdf)
     soup = np.ascontiguousarray(soup, np.float32)
     mo = np.ascontiguousarray(material_of, np.int32)
     pm = np.ascontiguousarray(pmats_effective, np.float32)
@@ -564,15 +587,14 @@ def restir_presample_seed(frame: int, seed: int) -> int:
 
 
 def restir_pass(pass_kind, scene, pmats, settings_i, settings_f, prev_vp, gb, gb_prev=None, inp=None, prev=None,
-                spatial_index=0, spatial_seed=0, nthreads=0, presampled=None, presample_i=None) -> np.ndarray:
+                spatial_index=0, spatial_seed=0, nthreads=0, presampled=None, presample_i=None,
+                bsdf: str = "reference") -> np.ndarray:
     """One ReSTIR DI pass of the oracle (0 initial, 1 temporal, 2 spatial, 3 fused spatiotemporal)
     shading with the reference's own BSDF; scene = dict(soup, material_of, emission, emissive,
     alias_prob, alias_idx, power_sum). presampled / presample_i (subsets, size, tile, seed): light
     presampling for the initial pass. Returns (W*H, 8) reservoir records."""
     lib = _restir_lib()
-    ref = ctypes.CDLL(REF_SO)
-    eval_fn = ctypes.cast(ref.ref_principled_eval_one, ctypes.c_void_p).value
-    sample_fn = ctypes.cast(ref.ref_principled_sample_one, ctypes.c_void_p).value
+    eval_fn, sample_fn = bsdf_callbacks(bsdf)
     soup = np.ascontiguousarray(scene["soup"], np.float32)
     mo = np.ascontiguousarray(scene["material_of"], np.int32)
     em = np.ascontiguousarray(scene["emission"], np.float32)

@@ -415,6 +415,23 @@ void orc_octree_closest(void* h, const float* origin_tmin, const float* dir_tmax
     });
 }
 
+/* Scene accelerator for the path-tracing and ReSTIR oracles (an orc_octree_build handle over the
+ * triangles their next calls pass; NULL: their exhaustive test). */
+static void* g_scene_accel = nullptr;
+void orc_set_scene_accel(void* octree) { g_scene_accel = octree; }
+void* orc_scene_accel() { return g_scene_accel; }
+
+/* One ray (origin o[3], direction d[3], minimum t 0): the closest hit's triangle (-1: none) and
+ * its t. The path-tracing and ReSTIR oracles trace through this when a scene accelerator is set
+ * (orc_set_scene_accel), e.g. for CPU baselines on scenes too large for their exhaustive test. */
+int32_t orc_octree_closest_one(void* h, const float* o, const float* d, int32_t skip, float* t_out)
+{
+    const Octree* oc = static_cast<const Octree*>(h);
+    Hit r = oc->closest(v3(o[0], o[1], o[2]), v3(d[0], d[1], d[2]), 0.0f, skip);
+    *t_out = r.t;
+    return r.prim;
+}
+
 /* Shadow rays: occluded[i] = 1 iff the closest accepted hit has t < dir_tmax[4*i+3]. */
 void orc_octree_occluded(void* h, const float* origin_tmin, const float* dir_tmax, const int32_t* last_prim,
                          int64_t n, uint8_t* occluded, int nthreads)
