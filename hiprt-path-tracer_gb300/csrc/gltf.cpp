@@ -769,6 +769,8 @@ gbpt_principled_material cpu_material_defaults()
     m.ior = 1.4f;
     rgb(m.absorption_color, 1.0f);
     m.absorption_at_distance = 1.0f;
+    m.diffuse_lobe = GBPT_DIFFUSE_LAMBERTIAN;
+    m.oren_nayar_sigma = 0.34906585039886591538f;  // 20 degrees
     return m;
 }
 

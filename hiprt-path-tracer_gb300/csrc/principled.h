@@ -68,6 +68,8 @@ struct Material
     V3 coat_absorption;
     float sheen, ior, transmission, diffuse_transmission;
     bool thin_walled;
+    bool oren_nayar;           // GBPT_DIFFUSE_OREN_NAYAR diffuse lobe
+    float oren_a, oren_b;      // its A and B terms of the facet-slope deviation
 };
 
 GBPT_HD Material load_material(const gbpt_principled_material& s)
@@ -100,6 +102,12 @@ GBPT_HD Material load_material(const gbpt_principled_material& s)
     m.transmission = s.specular_transmission;
     m.diffuse_transmission = s.diffuse_transmission;
     m.thin_walled = s.thin_walled != 0;
+    // Oren-Nayar A and B from the facet-slope deviation sigma (MaterialUtils::get_oren_nayar_AB,
+    // src/HostDeviceCommon/Material/MaterialUtils.h:18-23)
+    m.oren_nayar = s.diffuse_lobe == GBPT_DIFFUSE_OREN_NAYAR;
+    const float s2 = s.oren_nayar_sigma * s.oren_nayar_sigma;
+    m.oren_a = 1.0f - s2 / (2.0f * (s2 + 0.33f));
+    m.oren_b = 0.45f * s2 / (s2 + 0.09f);
     return m;
 }
 
@@ -464,6 +472,34 @@ GBPT_HD float glass_fresnel(const Material& m, float hov, float eta, float rough
     return F;
 }
 
+// The Oren-Nayar factor A + B max(0, cos(phi_i - phi_o)) sin(alpha) tan(beta) of the diffuse lobe
+// (oren_nayar_brdf_eval, src/Device/includes/BSDFs/OrenNayar.h:14-47), v and l in the unrotated
+// shading frame; the azimuth difference does not depend on the frame's tangent
+GBPT_HD float oren_nayar_shape(const Material& m, V3 v, V3 l)
+{
+    const float sin_i = sqrtf(1.0f - l.z * l.z);
+    const float sin_o = sqrtf(1.0f - v.z * v.z);
+    float max_cos = 0.0f;
+    if (sin_i > 1.0e-4f && sin_o > 1.0e-4f)
+    {
+        const float sp_i = l.y / sin_i, cp_i = l.x / sin_i;
+        const float sp_o = v.y / sin_o, cp_o = v.x / sin_o;
+        max_cos = fmaxf(0.0f, cp_i * cp_o + sp_i * sp_o);
+    }
+    float sin_alpha, tan_beta;
+    if (fabsf(l.z) > fabsf(v.z))
+    {
+        sin_alpha = sin_o;
+        tan_beta = sin_i / fabsf(l.z);
+    }
+    else
+    {
+        sin_alpha = sin_i;
+        tan_beta = sin_o / fabsf(v.z);
+    }
+    return m.oren_a + m.oren_b * max_cos * sin_alpha * tan_beta;
+}
+
 // Glass lobe (Principled.h:359-558): reflection or refraction through a GGX interface.
 GBPT_HD V3 glass_eval(const Material& m, const Medium& md, bool height_correlated, V3 v, V3 l, int lobe, float& pdf)
 {
@@ -632,7 +668,8 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
     const float diffuse_w = w.diffuse * (refracting ? 0.0f : 1.0f);
     if (diffuse_w > 0.0f && v.z > 0.0f && l.z > 0.0f)
     {
-        glossy = glossy + m.base * kInvPi * diffuse_w * throughput;
+        const float shape = m.oren_nayar ? oren_nayar_shape(m, v, l) : 1.0f;
+        glossy = glossy + m.base * kInvPi * shape * diffuse_w * throughput;
         pdf += l.z * kInvPi * p.diffuse;
     }
     color = color + glossy;

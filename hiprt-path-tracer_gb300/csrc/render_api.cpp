@@ -323,6 +323,10 @@ gbpt_status gbpt_scene_create(const gbpt_scene_desc* d, const gbpt_bvh_params* b
                 return set_error(GBPT_ERROR_UNSUPPORTED, "material " + std::to_string(m) + ": the sheen lobe is not built (sheen must be 0)");
             if (!(pm.ior > 0.0f) || !(pm.coat_ior > 0.0f))
                 return set_error(GBPT_ERROR_INVALID_ARG, "material " + std::to_string(m) + " has a non-positive IOR");
+            if (pm.diffuse_lobe != GBPT_DIFFUSE_LAMBERTIAN && pm.diffuse_lobe != GBPT_DIFFUSE_OREN_NAYAR)
+                return set_error(GBPT_ERROR_INVALID_ARG, "material " + std::to_string(m) + ": unknown diffuse_lobe");
+            if (pm.diffuse_lobe == GBPT_DIFFUSE_OREN_NAYAR && !(pm.oren_nayar_sigma >= 0.0f))
+                return set_error(GBPT_ERROR_INVALID_ARG, "material " + std::to_string(m) + ": negative oren_nayar_sigma");
         }
         if (!d->materials)
         {

@@ -23,8 +23,10 @@ FIELDS = [
     ("coat_darkening", 32, 1), ("coat_anisotropy", 33, 1), ("coat_anisotropy_rotation", 34, 1), ("coat_ior", 35, 1),
     ("sheen", 36, 1), ("ior", 37, 1), ("specular_transmission", 38, 1), ("diffuse_transmission", 39, 1),
     ("absorption_color", 40, 3), ("absorption_at_distance", 43, 1),
-    ("thin_walled", 44, 1),
+    ("thin_walled", 44, 1), ("diffuse_lobe", 45, 1), ("oren_nayar_sigma", 46, 1),
 ]
+INT_FIELDS = ("thin_walled", "diffuse_lobe")
+DIFFUSE_LAMBERTIAN, DIFFUSE_OREN_NAYAR = 0, 1  # GBPT_DIFFUSE_*
 OFFSETS = {n: (o, c) for n, o, c in FIELDS}
 
 DEFAULTS = {
@@ -36,6 +38,7 @@ DEFAULTS = {
     "coat_medium_thickness": 5.0, "coat_darkening": 1.0, "coat_anisotropy": 0.0, "coat_anisotropy_rotation": 0.0,
     "coat_ior": 1.5, "sheen": 0.0, "ior": 1.4, "specular_transmission": 0.0, "diffuse_transmission": 0.0,
     "absorption_color": (1.0, 1.0, 1.0), "absorption_at_distance": 1.0, "thin_walled": 0,
+    "diffuse_lobe": DIFFUSE_LAMBERTIAN, "oren_nayar_sigma": 0.34906585039886591538,  # 20 degrees
 }
 
 
@@ -49,8 +52,8 @@ def pack(**kw) -> np.ndarray:
         vals[k] = v
     for name, (off, cnt) in OFFSETS.items():
         v = vals[name]
-        if name == "thin_walled":
-            rec[off:off + 1] = np.array([1 if v else 0], np.int32).view(np.float32)
+        if name in INT_FIELDS:
+            rec[off:off + 1] = np.array([int(v)], np.int32).view(np.float32)
         else:
             rec[off:off + cnt] = np.broadcast_to(np.asarray(v, np.float32), (cnt,))
     return rec
@@ -60,7 +63,7 @@ def unpack(rec: np.ndarray) -> dict:
     """The fields of one material record as a dict (the inverse of pack)."""
     out = {}
     for name, (off, cnt) in OFFSETS.items():
-        if name == "thin_walled":
+        if name in INT_FIELDS:
             out[name] = int(rec[off:off + 1].view(np.int32)[0])
         elif cnt == 1:
             out[name] = float(rec[off])
@@ -75,7 +78,7 @@ def pack_many(dicts) -> np.ndarray:
 
 def get(rec: np.ndarray, name: str):
     off, cnt = OFFSETS[name]
-    if name == "thin_walled":
+    if name in INT_FIELDS:
         return int(rec[off:off + 1].view(np.int32)[0])
     return rec[off] if cnt == 1 else rec[off:off + cnt]
 

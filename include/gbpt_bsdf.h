@@ -54,8 +54,20 @@ typedef struct gbpt_principled_material {
     float absorption_color[3];
     float absorption_at_distance;
     int32_t thin_walled;
-    int32_t reserved[19];
+    int32_t diffuse_lobe;          /* GBPT_DIFFUSE_* [GBPT_DIFFUSE_LAMBERTIAN] */
+    float oren_nayar_sigma;        /* GBPT_DIFFUSE_OREN_NAYAR: roughness, the standard deviation of
+                                      the facet slope angle in radians (the reference's default is
+                                      20 degrees, 0.349066) */
+    int32_t reserved[17];
 } gbpt_principled_material;
+
+/* The diffuse lobe of the principled BSDF's glossy base (gbpt_principled_material.diffuse_lobe):
+ * the reference selects one for all materials at compile time (PrincipledBSDFDiffuseLobe,
+ * src/HostDeviceCommon/KernelOptions/PrincipledBSDFKernelOptions.h:63-72), here per material:
+ *   GBPT_DIFFUSE_LAMBERTIAN: base_color / pi (the reference's default);
+ *   GBPT_DIFFUSE_OREN_NAYAR: the Oren-Nayar qualitative model (src/Device/includes/BSDFs/
+ *     OrenNayar.h:14-63, MaterialUtils::get_oren_nayar_AB), sampled by the cosine distribution. */
+enum { GBPT_DIFFUSE_LAMBERTIAN = 0, GBPT_DIFFUSE_OREN_NAYAR = 1 };
 
 /* Which lobe a direction was sampled from: the reference's BSDFIncidentLightInfo values
  * (src/Device/includes/BSDFs/BSDFIncidentLightInfo.h). */

@@ -27,7 +27,12 @@ def bsdf_callbacks(bsdf: str = "reference"):
     """(eval, sample) function pointers of the principled BSDF the oracles shade with: the
     reference's own (oracle/_ref/libref.so, every parity test) or, with bsdf="host", the library's
     BSDF compiled for the host (oracle/libhost_bsdf.so; CPU baselines where the reference tree is
-    absent)."""
+    absent) or, with bsdf="reference_oren_nayar", the reference's BSDF compiled with its Oren-Nayar
+    diffuse lobe (oracle/_ref/libref_bsdf_oren_nayar.so)."""
+    if bsdf == "reference_oren_nayar":
+        lib = ctypes.CDLL(os.path.join(HERE, "_ref", "libref_bsdf_oren_nayar.so"))
+        return (ctypes.cast(lib.ref_principled_eval_one, ctypes.c_void_p).value,
+                ctypes.cast(lib.ref_principled_sample_one, ctypes.c_void_p).value)
     if bsdf == "host":
         lib = ctypes.CDLL(HOST_BSDF_SO)
         return (ctypes.cast(lib.host_principled_eval_one, ctypes.c_void_p).value,

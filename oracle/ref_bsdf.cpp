@@ -20,6 +20,10 @@
  */
 #include "HostDeviceCommon/KernelOptions/KernelOptions.h"
 
+#ifdef REF_DIFFUSE_LOBE
+#undef PrincipledBSDFDiffuseLobe
+#define PrincipledBSDFDiffuseLobe REF_DIFFUSE_LOBE
+#endif
 #undef PrincipledBSDFDoEnergyCompensation
 #define PrincipledBSDFDoEnergyCompensation KERNEL_OPTION_FALSE
 #undef PrincipledBSDFDoMicrofacetRegularization
@@ -68,6 +72,7 @@ DeviceUnpackedEffectiveMaterial unpack(const float* w)
     int32_t thin;
     std::memcpy(&thin, w + 44, 4);
     m.thin_walled = thin != 0;
+    m.oren_nayar_sigma = w[46];
     m.thin_film = 0.0f;
     m.dispersion_scale = 0.0f;
     return m;
@@ -142,6 +147,9 @@ void sample_query(const float* mat, const float* q, uint32_t seed, float* o, int
 }  // namespace
 
 extern "C" {
+// the entry points stay visible in a build with -fvisibility=hidden (the Oren-Nayar build, whose
+// inline reference functions must not bind to the default build's)
+#pragma GCC visibility push(default)
 
 /* out: 4 floats per query (rgb, pdf) */
 void ref_principled_eval(const float* mats, const int32_t* mat_index, const float* queries, int64_t n, float* out)
@@ -187,4 +195,5 @@ void ref_principled_sample_one(const float* mat, const float* q, uint32_t seed, 
     std::memcpy(out + 7, &rng_after, 4);  // the generator's state after sampling, bit for bit
 }
 
+#pragma GCC visibility pop
 }  // extern "C"

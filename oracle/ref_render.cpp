@@ -105,6 +105,7 @@ CPUMaterial cpu_material(const float* w)
     int32_t thin;
     std::memcpy(&thin, w + 44, 4);
     m.thin_walled = thin != 0;
+    m.oren_nayar_sigma = w[46];
     // the reference's scene parser calls make_safe on every material
     // (src/Scene/SceneParser.cpp:391-438); its clamps only touch fields this layout does not
     // carry, except the dielectric priority of non-transmissive materials
@@ -380,7 +381,7 @@ REF_EXPORT void refr_render(void* h, const int32_t* settings_i, const float* set
 
 /* The material the reference's kernels see after packing (pack_to_GPU, the 8-bit fields of
  * DevicePackedEffectiveMaterial, src/HostDeviceCommon/Material/MaterialPacked.h) and unpacking,
- * written back in the 64-word layout (words 45..63 zero). */
+ * written back in the 64-word layout (word 45, the diffuse-lobe selector, copied; 47..63 zero). */
 REF_EXPORT void refr_pack_unpack_material(const float* in, float* out)
 {
     CPUMaterial c = cpu_material(in);
@@ -419,6 +420,8 @@ REF_EXPORT void refr_pack_unpack_material(const float* in, float* out)
     w[43] = m.absorption_at_distance;
     int32_t thin = m.thin_walled ? 1 : 0;
     std::memcpy(w + 44, &thin, 4);
+    w[45] = in[45];  // the diffuse-lobe selector: a compile-time option of the reference, copied
+    w[46] = m.oren_nayar_sigma;
     std::memcpy(out, w, sizeof(w));
 }
 

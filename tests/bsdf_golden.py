@@ -1,5 +1,6 @@
-"""TEST INFRASTRUCTURE ONLY — the principled-BSDF golden vectors (tests/golden/bsdf_principled.npz,
-written by the reference's own BSDF through tests/golden/make_bsdf_golden.py) and the comparison
+"""TEST INFRASTRUCTURE ONLY — the principled-BSDF golden vectors (tests/golden/bsdf_principled.npz and,
+for the Oren-Nayar diffuse lobe, bsdf_oren_nayar.npz, written by the reference's own BSDF through
+tests/golden/make_bsdf_golden.py) and the comparison
 both the CPU test (host build of the BSDF) and the GPU test (CUDA build) apply.
 
 Tolerance on f, pdf and the sampled direction (relative, with an absolute floor of 1e-6 of the
@@ -17,14 +18,17 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_principled.npz")
+# the same queries' kind against the reference built with its Oren-Nayar diffuse lobe
+GOLDEN_OREN_NAYAR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_oren_nayar.npz")
+SETS = {"lambertian": GOLDEN, "oren_nayar": GOLDEN_OREN_NAYAR}
 RTOL = 1e-5
 RTOL_ALL = 2e-4
 TIGHT_FRACTION = 0.995
 TIGHT_FRACTION_SAMPLE = 0.99
 
 
-def load():
-    d = np.load(GOLDEN)
+def load(which: str = "lambertian"):
+    d = np.load(SETS[which])
     return {k: d[k] for k in d.files}
 
 

@@ -7,7 +7,11 @@ regularization compiled out) on seeded materials and directions, and stores inpu
   pdf:    same inputs -> pdf                                      [principled_bsdf_pdf :1717]
   sample: material, view, normals, Xorshift32 seed -> direction, rgb, pdf, sampled lobe,
           generator state after sampling                         [principled_bsdf_sample :1803]
-Usage (where the reference tree is present):  python tests/golden/make_bsdf_golden.py
+With --oren-nayar, writes tests/golden/bsdf_oren_nayar.npz from oracle/_ref/libref_bsdf_oren_nayar.so
+instead: the same BSDF compiled with the reference's Oren-Nayar diffuse lobe
+(PrincipledBSDFDiffuseLobe = PRINCIPLED_DIFFUSE_LOBE_OREN_NAYAR, src/Device/includes/BSDFs/OrenNayar.h),
+every material carrying diffuse_lobe = Oren-Nayar and a seeded facet-slope deviation sigma.
+Usage (where the reference tree is present):  python tests/golden/make_bsdf_golden.py [--oren-nayar]
 """
 import ctypes
 import os
@@ -24,6 +28,8 @@ from gbpt import materials as M  # noqa: E402
 import pyoracle  # noqa: E402
 
 OUT = os.path.join(HERE, "bsdf_principled.npz")
+OUT_ON = os.path.join(HERE, "bsdf_oren_nayar.npz")
+REF_ON_SO = os.path.join(REPO, "oracle", "_ref", "libref_bsdf_oren_nayar.so")
 
 
 def _unit(rng, n):
@@ -31,8 +37,10 @@ def _unit(rng, n):
     return v / np.linalg.norm(v, axis=1, keepdims=True)
 
 
-def material_set(rng):
-    """Edge cases of every lobe first, then the random principled distribution."""
+def material_set(rng, oren_nayar=False):
+    """Edge cases of every lobe first, then the random principled distribution. With oren_nayar,
+    every material selects the Oren-Nayar diffuse lobe with sigma in [0, 1.2] rad (0 and the
+    default 20 degrees among them)."""
     base = [
         dict(base_color=(0.8, 0.3, 0.2), roughness=0.5, specular=0.0),                     # diffuse only
         dict(base_color=(0.8, 0.3, 0.2), roughness=0.5),                                   # specular over diffuse
@@ -55,6 +63,10 @@ def material_set(rng):
              coat_roughness=0.2, diffuse_transmission=0.2),
     ]
     mats = base + M.random_principled(rng, 50)
+    if oren_nayar:
+        sig = rng.uniform(0.0, 1.2, len(mats))
+        sig[0], sig[1] = 0.0, M.DEFAULTS["oren_nayar_sigma"]
+        mats = [dict(m, diffuse_lobe=M.DIFFUSE_OREN_NAYAR, oren_nayar_sigma=float(s)) for m, s in zip(mats, sig)]
     return M.pack_many([M.coat_roughened(m) for m in mats])
 
 
@@ -94,8 +106,9 @@ def queries(rng, mats, n, sample):
 
 
 def main():
+    oren_nayar = "--oren-nayar" in sys.argv[1:]
     pyoracle.build(ref=True)
-    lib = ctypes.CDLL(pyoracle.REF_SO)
+    lib = ctypes.CDLL(REF_ON_SO if oren_nayar else pyoracle.REF_SO)
     fp = ctypes.POINTER(ctypes.c_float)
     ip = ctypes.POINTER(ctypes.c_int32)
     up = ctypes.POINTER(ctypes.c_uint32)
@@ -103,8 +116,8 @@ def main():
     lib.ref_principled_pdf.argtypes = [fp, ip, fp, ctypes.c_int64, fp]
     lib.ref_principled_sample.argtypes = [fp, ip, fp, up, ctypes.c_int64, fp, ip, up]
 
-    rng = np.random.Generator(np.random.PCG64(20240))
-    mats = np.ascontiguousarray(material_set(rng))
+    rng = np.random.Generator(np.random.PCG64(20241 if oren_nayar else 20240))
+    mats = np.ascontiguousarray(material_set(rng, oren_nayar))
     n_eval, n_sample = 8192, 8192
     emi, eq = queries(rng, mats, n_eval, sample=False)
     eout = np.zeros((n_eval, 4), np.float32)
@@ -121,9 +134,10 @@ def main():
     lib.ref_principled_sample(mats.ctypes.data_as(fp), smi.ctypes.data_as(ip), sq.ctypes.data_as(fp),
                               seeds.ctypes.data_as(up), n_sample, sout.ctypes.data_as(fp), sinfo.ctypes.data_as(ip),
                               srng.ctypes.data_as(up))
-    np.savez_compressed(OUT, materials=mats, eval_mat=emi, eval_q=eq, eval_out=eout, pdf_out=pout,
+    out_path = OUT_ON if oren_nayar else OUT
+    np.savez_compressed(out_path, materials=mats, eval_mat=emi, eval_q=eq, eval_out=eout, pdf_out=pout,
                         sample_mat=smi, sample_q=sq, seeds=seeds, sample_out=sout, sample_info=sinfo, sample_rng=srng)
-    print(f"wrote {OUT}: {len(mats)} materials, {n_eval} eval/pdf + {n_sample} sample queries; "
+    print(f"wrote {out_path}: {len(mats)} materials, {n_eval} eval/pdf + {n_sample} sample queries; "
           f"nonzero eval {np.mean(eout[:, 3] > 0):.2f}, sampled lobes {np.unique(sinfo, return_counts=True)}")
 
 

@@ -8,7 +8,9 @@ to floating-point contraction. Materials: coated diffuse walls, a rough dielectr
 anisotropic metal green wall, a rough glass short box (closed: paths enter and leave it), a mirror
 tall box (a delta BSDF: no light sampling), the area light. The scene and settings are stored with
 the image so the GPU test needs nothing else. A third file renders the smooth-shading scene (two
-coarse spheres shaded with their vertex normals).
+coarse spheres shaded with their vertex normals); a fourth, pt_principled_oren_nayar_cornell.npz,
+the Cornell scene with the Oren-Nayar diffuse lobe, shaded by the reference's BSDF built with that
+lobe (oracle/_ref/libref_bsdf_oren_nayar.so).
 Usage (where the reference tree is present):  python tests/golden/make_pt_principled_golden.py
 """
 import os
@@ -28,6 +30,7 @@ import pyoracle  # noqa: E402
 OUT = os.path.join(HERE, "pt_principled_cornell.npz")
 OUT_RIS = os.path.join(HERE, "pt_principled_ris_cornell.npz")
 OUT_SMOOTH = os.path.join(HERE, "pt_principled_smooth_cornell.npz")
+OUT_ON = os.path.join(HERE, "pt_principled_oren_nayar_cornell.npz")
 
 
 MATERIALS = [
@@ -103,6 +106,20 @@ def main():
                         settings=np.array([st.width, st.height, st.samples_per_launch, st.nb_bounces,
                                            st.russian_roulette_min_depth, st.seed], np.int32), image=img)
     print(f"wrote {OUT_SMOOTH}: mean {img.mean() / st.samples_per_launch:.4f}")
+    # the Cornell scene with the Oren-Nayar diffuse lobe on every material (rough facets on the
+    # walls), shaded by the reference's BSDF built with PrincipledBSDFDiffuseLobe = Oren-Nayar
+    mesh, mat_of, _, _ = scene()
+    on = [dict(m, diffuse_lobe=M.DIFFUSE_OREN_NAYAR, oren_nayar_sigma=s)
+          for m, s in zip(MATERIALS, (0.6, 1.0, 0.3, 0.0, 0.2, 0.4))]
+    raw = M.pack_many(on)
+    eff = M.pack_many([M.coat_roughened(m) for m in on])
+    st = settings()
+    emission = raw[:, 4:7]
+    emissive = np.nonzero(np.any(emission[mat_of] != 0, axis=1))[0].astype(np.int32)
+    img = pyoracle.pt_render_principled(mesh.triangle_soup(), mat_of, eff, emission, emissive, None, None, 0.0, st,
+                                        st.samples_per_launch, bsdf="reference_oren_nayar")
+    np.savez_compressed(OUT_ON, materials=raw, image=img)
+    print(f"wrote {OUT_ON}: mean {img.mean() / st.samples_per_launch:.4f}")
 
 
 if __name__ == "__main__":

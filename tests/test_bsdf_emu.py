@@ -4,6 +4,7 @@ sampling with the same Xorshift32 stream)."""
 import ctypes
 
 import numpy as np
+import pytest
 
 import bsdf_golden as G
 from native import build_emu
@@ -25,8 +26,28 @@ def test_golden_vectors_cover_every_lobe():
     assert np.isfinite(g["eval_out"]).all() and np.isfinite(g["sample_out"]).all()
 
 
-def test_host_build_eval_and_pdf_match_reference():
-    g = G.load()
+def test_oren_nayar_vectors_differ_from_lambertian_where_the_lobe_shows():
+    """The Oren-Nayar set selects the lobe on every material (word 45) and its values differ from
+    what a Lambertian lobe gives: the host build with the selector cleared disagrees on a good share
+    of the diffuse queries, and agrees on the sigma = 0 material, where A = 1 and B = 0."""
+    g = G.load("oren_nayar")
+    mats = np.ascontiguousarray(g["materials"])
+    assert (mats[:, 45].view(np.int32) == 1).all()
+    lamb = mats.copy()
+    lamb[:, 45] = np.zeros(len(mats), np.int32).view(np.float32)
+    lib = _lib()
+    q = G.queries(g["eval_q"])
+    mi = np.ascontiguousarray(g["eval_mat"], np.int32)
+    out = np.zeros((len(q), 4), np.float32)
+    lib.emu_bsdf_eval(lamb.ctypes.data, mi.ctypes.data, q.ctypes.data, len(q), 0, out.ctypes.data)
+    same = G.close(out, g["eval_out"], 1e-5)
+    assert same[mi == 0].all()
+    assert (~same).mean() > 0.2
+
+
+@pytest.mark.parametrize("which", sorted(G.SETS))
+def test_host_build_eval_and_pdf_match_reference(which):
+    g = G.load(which)
     lib = _lib()
     mats = np.ascontiguousarray(g["materials"])
     q = G.queries(g["eval_q"])
@@ -37,8 +58,9 @@ def test_host_build_eval_and_pdf_match_reference():
     assert G.close(out[:, 3:4], g["pdf_out"][:, None], rtol=1e-4).mean() > 0.999
 
 
-def test_host_build_sampling_matches_reference():
-    g = G.load()
+@pytest.mark.parametrize("which", sorted(G.SETS))
+def test_host_build_sampling_matches_reference(which):
+    g = G.load(which)
     lib = _lib()
     mats = np.ascontiguousarray(g["materials"])
     q = G.queries(g["sample_q"])

@@ -17,8 +17,9 @@ def _dev(a, dtype=None):
     return t.cuda() if dtype is None else t.to(dtype).cuda()
 
 
-def test_eval_and_pdf_match_reference_golden(cuda):
-    g = G.load()
+@pytest.mark.parametrize("which", sorted(G.SETS))
+def test_eval_and_pdf_match_reference_golden(cuda, which):
+    g = G.load(which)
     mats = _dev(g["materials"])
     q = _dev(G.queries(g["eval_q"]))
     mi = _dev(g["eval_mat"].astype(np.int32))
@@ -30,8 +31,9 @@ def test_eval_and_pdf_match_reference_golden(cuda):
     print(f"eval: {frac:.4%} within 1e-5, {flips} beyond 2e-4 of {len(out)}")
 
 
-def test_sampling_matches_reference_golden(cuda):
-    g = G.load()
+@pytest.mark.parametrize("which", sorted(G.SETS))
+def test_sampling_matches_reference_golden(cuda, which):
+    g = G.load(which)
     mats = _dev(g["materials"])
     q = _dev(G.queries(g["sample_q"]))
     mi = _dev(g["sample_mat"].astype(np.int32))

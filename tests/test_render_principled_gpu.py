@@ -14,6 +14,7 @@ from gbpt.render import BSDF_PRINCIPLED, LIGHT_UNIFORM, RenderSettings
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pt_principled_cornell.npz")
+GOLDEN_ON = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pt_principled_oren_nayar_cornell.npz")
 
 
 def _load():
@@ -48,6 +49,20 @@ def test_principled_cornell_matches_reference_bsdf_oracle(cuda):
     assert mean_rel_close < 1e-4, mean_rel_close
 
 
+def test_oren_nayar_cornell_matches_reference_lobe(cuda):
+    """Every material on the Oren-Nayar diffuse lobe (per-material sigma), against the oracle image
+    shaded by the reference's BSDF compiled with its Oren-Nayar lobe."""
+    g, st, _ = _load()
+    on = np.load(GOLDEN_ON)
+    scene = gbpt.Scene(g["positions"], g["indices"], g["material_of"], principled=on["materials"])
+    gpu = _render(scene, st)
+    orc = on["image"]
+    rel = np.abs(gpu - orc) / np.maximum(np.abs(orc), 1e-3)
+    close = rel.max(axis=-1) < 1e-3
+    assert close.mean() > 0.93, close.mean()
+    assert abs(gpu[close].mean() - orc[close].mean()) / orc[close].mean() < 1e-4
+
+
 def test_principled_relmse_decreases_and_unbiased_over_seeds(cuda):
     g, st, scene = _load()
     ref_st = RenderSettings(**{**st.__dict__, "samples_per_launch": 512, "seed": 1000})
@@ -78,4 +93,8 @@ def test_principled_needs_principled_scene(cuda):
     bad = g["materials"].copy()
     bad[0, 36] = 0.5  # sheen
     with pytest.raises(gbpt.GbptError):
+        gbpt.Scene(g["positions"], g["indices"], g["material_of"], principled=bad)
+    bad = g["materials"].copy()
+    bad[0, 45] = np.array([7], np.int32).view(np.float32)[0]  # no such diffuse lobe
+    with pytest.raises(gbpt.GbptError, match="diffuse_lobe"):
         gbpt.Scene(g["positions"], g["indices"], g["material_of"], principled=bad)
