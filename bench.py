@@ -337,7 +337,7 @@ def cornell_workload(out, cb, cscene, timed, cpu_baseline):
         cores = os.cpu_count() or 1
         cst = gbpt.cornell_settings(256, 256, samples_per_launch=1, seed=1)
         t0 = time.perf_counter()
-        spp = 4
+        spp = 128
         pyoracle.pt_render(cb.mesh.triangle_soup(), cb.material_of_triangle, cb.albedo, cb.emission, lt["emissive"],
                            lt["probas"], lt["alias"], lt["power_sum"], cst, spp, nthreads=cores)
         dt = time.perf_counter() - t0
@@ -665,9 +665,10 @@ def batch_jobs(n_jobs=48, seed=1):
 def batch_cpu_baseline(jobs, picks, log):
     """CPU baseline of the batch: the path-tracing oracle (the reference's estimator restated,
     tracing through an octree restating the reference's CPU BVH, shading with the library's
-    principled BSDF compiled for the host) on all host cores, one spp of each picked job at its own
-    settings; samples per second over the picked jobs."""
+    principled BSDF compiled for the host) on all host cores, `spp` samples per pixel of each picked
+    job at its own settings; samples per second over the picked jobs."""
     cores = os.cpu_count() or 1
+    spp = 32
     total_px, total_s, notes = 0, 0.0, []
     for j in picks:
         sc, st, info, (mesh, mat_of, recs) = jobs[j]
@@ -677,19 +678,19 @@ def batch_cpu_baseline(jobs, picks, log):
             one = RenderSettings(**{**st.__dict__, "samples_per_launch": 1})
             t0 = time.perf_counter()
             pyoracle.pt_render_principled(osc["soup"], osc["material_of"], eff, osc["emission"], osc["emissive"],
-                                          osc["alias_prob"], osc["alias_idx"], osc["power_sum"], one, 1,
+                                          osc["alias_prob"], osc["alias_idx"], osc["power_sum"], one, spp,
                                           nthreads=cores, bsdf="host")
             dt = time.perf_counter() - t0
         finally:
             pyoracle.set_scene_accel(None)
             del oc
-        total_px += st.width * st.height
+        total_px += st.width * st.height * spp
         total_s += dt
         notes.append(f"job {j} ({info['res']}^2, {info['triangles']} tris, {info['bounces']} bounces) {dt:.2f}s")
     if not picks:
         return None
     return {"value": total_px / total_s, "unit": "samples/s", "cores": cores, "kind": "port",
-            "sample": "1 spp of " + "; ".join(notes)}
+            "sample": f"{spp} spp of " + "; ".join(notes)}
 
 
 def batch_workload(timed, log, ref_factor=4, cpu_baseline=True):

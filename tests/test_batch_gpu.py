@@ -1,7 +1,10 @@
 """GPU: batched rendering. Jobs with different scenes, resolutions, bounce depths, seeds and sample
 counts share every wavefront launch; each job's image must equal, bit for bit, the image of a
 single renderer tracing the same pixel samples (a path depends only on its scene, pixel, sample
-index and seed), with and without the CUDA graph."""
+index and seed), with and without the CUDA graph; and each job's image agrees sample by sample
+with the path-tracing oracle's rendering of that job (same PCG streams; the principled jobs
+shaded by the library's BSDF built for the host, which the BSDF golden vectors pin to the
+reference's), to the tolerance of the single-renderer oracle tests."""
 import os
 
 import numpy as np
@@ -24,15 +27,17 @@ def _single(scene, st):
     return r.image_sums()
 
 
-def _lambert_jobs():
+def _lambert_jobs(with_oracle=False):
     cb = scenes.cornell_box()
     scene = gbpt.Scene.from_cornell(cb)
+    if with_oracle:
+        return cb, _lambert_jobs()
     return [(scene, gbpt.cornell_settings(48, 32, samples_per_launch=9, nb_bounces=4, seed=3)),
             (scene, gbpt.cornell_settings(17, 23, samples_per_launch=4, nb_bounces=2, seed=8)),
             (scene, gbpt.cornell_settings(64, 64, samples_per_launch=13, nb_bounces=7, seed=1))]
 
 
-def _principled_jobs():
+def _principled_jobs(with_oracle=False):
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pt_principled_cornell.npz"))
     w, h, _, nb, rr, _ = (int(v) for v in g["settings"])
     cornell = gbpt.Scene(g["positions"], g["indices"], g["material_of"], principled=g["materials"])
@@ -50,6 +55,10 @@ def _principled_jobs():
     iv, ip = look_at_camera((0.0, 1.2, -2.2), (0.0, 0.1, 0.0), vfov_deg=45.0, aspect=40 / 24)
     jobs.append((hscene, RenderSettings(width=40, height=24, samples_per_launch=11, nb_bounces=5, light_sampling=LIGHT_POWER,
                                         bsdf=BSDF_PRINCIPLED, seed=9, inverse_view=iv, inverse_projection=ip)))
+    if with_oracle:
+        # per job: triangle soup, material per triangle, raw records
+        return [(g["positions"][g["indices"]].reshape(-1, 9), g["material_of"], g["materials"]),
+                (mesh.triangle_soup(), mat_of, mats)], jobs
     return jobs
 
 
@@ -72,6 +81,37 @@ def test_batch_jobs_equal_single_renders(cuda, kind, use_graph):
     b.render()
     torch.cuda.synchronize()
     assert np.array_equal(b.image_sums(0)[0], _single(*jobs[0])[0])
+
+
+def _close_to_oracle(gpu, orc, min_close):
+    rel = np.abs(gpu - orc) / np.maximum(np.abs(orc), 1e-3)
+    close = rel.max(axis=-1) < 1e-3
+    assert close.mean() > min_close, close.mean()
+    assert abs(gpu[close].mean() - orc[close].mean()) / orc[close].mean() < 1e-4
+
+
+def test_batch_jobs_match_oracle(cuda):
+    import pyoracle
+    cb, jobs = _lambert_jobs(with_oracle=True)
+    b = gbpt.Batch(jobs, samples_per_iteration=4)
+    b.render()
+    torch.cuda.synchronize()
+    for k, (scene, st) in enumerate(jobs):
+        lt = scene.light_table()
+        orc = pyoracle.pt_render(cb.mesh.triangle_soup(), cb.material_of_triangle, cb.albedo, cb.emission,
+                                 lt["emissive"], lt["probas"], lt["alias"], lt["power_sum"], st, st.samples_per_launch)
+        _close_to_oracle(b.image_sums(k)[1], orc, 0.97)
+    data, jobs = _principled_jobs(with_oracle=True)
+    b = gbpt.Batch(jobs, samples_per_iteration=4)
+    b.render()
+    torch.cuda.synchronize()
+    for k, ((scene, st), (soup, mat_of, raw)) in enumerate(zip(jobs, data)):
+        lt = scene.light_table()
+        eff = M.pack_many([M.coat_roughened(M.unpack(m)) for m in raw])
+        orc = pyoracle.pt_render_principled(np.ascontiguousarray(soup, np.float32), mat_of, eff, raw[:, 4:7],
+                                            lt["emissive"], lt["probas"], lt["alias"], lt["power_sum"], st,
+                                            st.samples_per_launch, bsdf="host")
+        _close_to_oracle(b.image_sums(k)[1], orc, 0.93)
 
 
 def test_job_completion_times_follow_iterations(cuda):

@@ -103,8 +103,10 @@ def test_empty_and_zero_rays(cuda):
 
 
 def test_full_size_scene_sampled(cuda, oracle):
-    """The benchmark scene at full size (2,297,152 triangles): a strided sample of primary rays
-    against the oracle, plus size-independent properties over the whole batch."""
+    """The benchmark scene at full size (2,297,152 triangles): strided samples of primary, bounce
+    (closest hit) and shadow (any hit) rays against the oracle, the secondary rays generated from
+    the primary hits as the benchmark does (cosine bounces off the hit normal, shadow rays to an
+    area light), plus size-independent properties over the whole batch."""
     mesh = scenes.traversal_scene()
     assert mesh.n_triangles == 2_297_152
     bvh = gbpt.BVH(mesh.indices, mesh.positions)
@@ -121,6 +123,18 @@ def test_full_size_scene_sampled(cuda, oracle):
     assert (got[hit, 0] > 0).all() and (prim < mesh.n_triangles).all()
     # determinism: a second launch returns identical bits
     assert np.array_equal(got.view(np.uint32), _closest(bvh, rays, cuda).view(np.uint32))
+    pts, nrm, prims = scenes.hit_points_normals(mesh, rays, got)
+    m = np.nonzero(prims >= 0)[0]
+    b = scenes.bounce_rays(pts[m], nrm[m], prims[m], seed=3)
+    gb = _closest(bvh, b, cuda)
+    bs = b.slice(slice(0, None, 41))
+    n, ties, other = classify_mismatches(oracle, mesh, bs, gb[::41], oc.closest(bs))
+    assert other == 0, f"bounce: {other} non-tie mismatches of {n}"
+    sh, _ = scenes.shadow_rays(pts[m], prims[m], seed=4)
+    occ = _occluded(bvh, sh, cuda)
+    ss = sh.slice(slice(0, None, 41))
+    assert np.array_equal(occ[::41], oc.occluded(ss))
+    assert 0.05 < occ.mean() < 0.95
 
 
 @pytest.mark.parametrize("any_hit", [False, True])
