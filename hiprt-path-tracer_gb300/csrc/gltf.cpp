@@ -771,6 +771,9 @@ gbpt_principled_material cpu_material_defaults()
     m.absorption_at_distance = 1.0f;
     m.diffuse_lobe = GBPT_DIFFUSE_LAMBERTIAN;
     m.oren_nayar_sigma = 0.34906585039886591538f;  // 20 degrees
+    m.thin_film_ior = 1.3f;
+    m.thin_film_thickness = 500.0f;
+    m.thin_film_base_ior_override = 1.0f;
     return m;
 }
 

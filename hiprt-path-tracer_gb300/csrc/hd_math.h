@@ -10,12 +10,16 @@
 #ifndef GBPT_HD
 #define GBPT_HD __device__ __forceinline__
 #endif
+// a device function kept out of line: rarely taken code whose inlined copy would raise the
+// register count of the kernels that call it
+#define GBPT_HD_OUTLINE static __device__ __noinline__
 #else
 #include <cmath>
 #include <cstring>
 #ifndef GBPT_HD
 #define GBPT_HD inline
 #endif
+#define GBPT_HD_OUTLINE inline
 #endif
 
 namespace gbpt {

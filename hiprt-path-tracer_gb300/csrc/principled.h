@@ -2,7 +2,7 @@
 // that the CPU tests compile (tests/native/bsdf_emu.cpp).
 //
 // Behaviour follows the reference's principled BSDF with energy compensation, microfacet
-// regularization, thin film, dispersion and sheen switched off
+// regularization, dispersion and sheen switched off
 // (src/Device/includes/BSDFs/Principled.h:1515-1941 and the lobes it calls):
 //   - lobe weights and sampling probabilities: Principled.h:1515-1618;
 //   - layering (coat over sheen over metal / glass / glossy base / diffuse transmission, with the
@@ -12,7 +12,9 @@
 //   - GGX: anisotropic D, Smith G1/G2, Heitz 2018 visible-normal sampling, Torrance-Sparrow
 //     reflection and Walter 2007 refraction: src/Device/includes/BSDFs/Microfacet.h:25-502;
 //   - Fresnel: dielectric, Adobe F82-tint, d'Eon's hemispherical-albedo fit:
-//     src/Device/includes/Fresnel.h:41-175;
+//     src/Device/includes/Fresnel.h:41-175; thin-film interference (Belcour and Barla 2017):
+//     src/Device/includes/BSDFs/ThinFilm.h:11-226, blended into the metal (Principled.h:143-146),
+//     specular (:215-240, 1363-1382) and glass (:462-483, 663-684, 758-785) Fresnel terms;
 //   - frames: Frisvad/Max ONB and the rotated ONB of anisotropy: src/Device/includes/ONB.h;
 //   - delta-lobe handling (a perfectly smooth lobe contributes only when the direction was
 //     sampled from a lobe with the same mirror peak): MaterialUtils.h:143-177, Microfacet.h:90-120.
@@ -70,6 +72,9 @@ struct Material
     bool thin_walled;
     bool oren_nayar;           // GBPT_DIFFUSE_OREN_NAYAR diffuse lobe
     float oren_a, oren_b;      // its A and B terms of the facet-slope deviation
+    float thin_film;           // thin-film weight (0: no film, the code below skips it)
+    float tf_ior, tf_thickness, tf_hue;
+    float tf_base_ior, tf_kappa;  // the base under the film: override or the material's IOR, kappa 0
 };
 
 GBPT_HD Material load_material(const gbpt_principled_material& s)
@@ -108,6 +113,12 @@ GBPT_HD Material load_material(const gbpt_principled_material& s)
     const float s2 = s.oren_nayar_sigma * s.oren_nayar_sigma;
     m.oren_a = 1.0f - s2 / (2.0f * (s2 + 0.33f));
     m.oren_b = 0.45f * s2 / (s2 + 0.09f);
+    m.thin_film = s.thin_film;
+    m.tf_ior = s.thin_film_ior;
+    m.tf_thickness = s.thin_film_thickness;
+    m.tf_hue = s.thin_film_hue_shift;
+    m.tf_base_ior = s.thin_film_do_ior_override ? s.thin_film_base_ior_override : s.ior;
+    m.tf_kappa = s.thin_film_do_ior_override ? s.thin_film_kappa_3 : 0.0f;
     return m;
 }
 
@@ -220,6 +231,122 @@ GBPT_HD V3 fresnel_f82_tint(V3 f0, V3 f82, V3 f90, float exponent, float cos_t)
     return clamp3(0.0f, 1.0f, schlick - a * lazanyi);
 }
 
+// ---------------------------------------------------------------------------------------------
+// thin-film interference (Belcour and Barla, "A Practical Extension to Microfacet Theory for the
+// Modeling of Varying Iridescence", 2017, and its supplemental code; ThinFilm.h:11-226): the
+// Airy summation of a film between the ambient medium (eta1) and the base (eta3, kappa3), the
+// first two orders of its phase terms integrated against the CIE XYZ sensitivities (Gaussian fits
+// in Fourier space), both polarisations averaged, converted to CIE RGB, clamped, then rotated in
+// hue about the grey axis.
+// ---------------------------------------------------------------------------------------------
+GBPT_HD V3 film_sensitivity(float opd, float shift)
+{
+    const float phase = 2.0f * kPi * opd * 1.0e-6f;
+    const float val[3] = {5.4856e-13f, 4.4201e-13f, 5.2481e-13f};
+    const float pos[3] = {1.6810e+06f, 1.7953e+06f, 2.2084e+06f};
+    const float var[3] = {4.3278e+09f, 9.3046e+09f, 6.6121e+09f};
+    float xyz[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        xyz[c] = val[c] * sqrtf(2.0f * kPi * var[c]) * cosf(pos[c] * phase + shift) * expf(-1.0f * var[c] * phase * phase);
+    xyz[0] += 9.7470e-14f * sqrtf(2.0f * kPi * 4.5282e+09f) * cosf(2.2399e+06f * phase + shift) *
+              expf(-4.5282e+09f * phase * phase);
+    return v3(xyz[0], xyz[1], xyz[2]) / 1.0685e-7f;
+}
+
+// phase shifts of the parallel and perpendicular components reflected at an interface from eta1
+// onto (eta2, kappa2)
+GBPT_HD void film_phase(float cos_i, float eta1, float eta2, float kappa2, float& phi_par, float& phi_perp)
+{
+    const float sin2 = 1.0f - sq(cos_i);
+    const float A = sq(eta2) * (1.0f - sq(kappa2)) - sq(eta1) * sin2;
+    const float B = sqrtf(sq(A) + sq(2.0f * sq(eta2) * kappa2));
+    const float U = sqrtf((A + B) * 0.5f);
+    const float V = sqrtf((B - A) * 0.5f);
+    phi_perp = atan2f(2.0f * eta1 * V * cos_i, sq(U) + sq(V) - sq(eta1 * cos_i));
+    phi_par = atan2f(2.0f * eta1 * sq(eta2) * cos_i * (2.0f * kappa2 * U - (1.0f - sq(kappa2)) * V),
+                     sq(sq(eta2) * (1.0f + sq(kappa2)) * cos_i) - sq(eta1) * (sq(U) + sq(V)));
+}
+
+// reflectances (parallel, perpendicular) of a conductor of relative IOR eta + i k
+GBPT_HD void film_conductor(float cos_i, float eta, float k, float& rp, float& rs)
+{
+    const float c2 = cos_i * cos_i;
+    const float s2 = 1.0f - c2;
+    const float t1 = eta * eta - k * k - s2;
+    const float a2pb2 = sqrtf(t1 * t1 + 4.0f * k * k * eta * eta);
+    const float a = sqrtf(0.5f * (a2pb2 + t1));
+    const float t2 = a2pb2 + c2;
+    const float t3 = 2.0f * a * cos_i;
+    rs = clampf(0.0f, 1.0f, (t2 - t3) / (t2 + t3));
+    const float t4 = a2pb2 * c2 + s2 * s2;
+    const float t5 = t3 * s2;
+    rp = clampf(0.0f, 1.0f, rs * (t4 - t5) / (t4 + t5));
+}
+
+// rotation of an RGB colour about the grey axis by 'degrees'
+GBPT_HD V3 hue_rotate(V3 c, float degrees)
+{
+    if (degrees == 0.0f) return c;
+    const float ca = cosf(degrees / 180.0f * kPi);
+    const float sa = sinf(degrees / 180.0f * kPi);
+    constexpr float kS = 0.57735026918962576451f;  // sqrt(1/3)
+    constexpr float kT = 1.0f / 3.0f;
+    const float d = ca + (1.0f - ca) / 3.0f;
+    const float p = kT * (1.0f - ca) - kS * sa;
+    const float q = kT * (1.0f - ca) + kS * sa;
+    const float d2 = ca + kT * (1.0f - ca);
+    const V3 r = v3(c.x * d + c.y * p + c.z * q, c.x * q + c.y * d2 + c.z * p, c.x * p + c.y * q + c.z * d2);
+    return clamp3(0.0f, 1.0f, r);
+}
+
+// RGB reflectance of the film seen from a medium of IOR ambient_ior at cosine cos_i (out of line
+// on the device: only film materials take it)
+GBPT_HD_OUTLINE V3 thin_film_fresnel(const Material& m, float ambient_ior, float cos_i)
+{
+    if (m.thin_film == 0.0f) return v3(0.0f);
+    const float eta1 = ambient_ior, eta2 = m.tf_ior, eta3 = m.tf_base_ior, kappa3 = m.tf_kappa;
+    float r12p = 1.0f, r12s = 1.0f, r23p = 0.0f, r23s = 0.0f, t121p = 0.0f, t121s = 0.0f, cos2 = 0.0f;
+    const float cos_t2 = 1.0f - (1.0f - sq(cos_i)) * sq(eta1 / eta2);
+    if (cos_t2 > 0.0f)
+    {
+        cos2 = sqrtf(cos_t2);
+        film_conductor(cos_i, eta2 / eta1, 0.0f, r12p, r12s);
+        film_conductor(cos2, eta3 / eta2, kappa3, r23p, r23s);
+        t121p = 1.0f - r12p;
+        t121s = 1.0f - r12s;
+    }
+    const float D = m.tf_thickness / 1000.0f * cos2;  // optical path difference, micrometres
+    float phi21p, phi21s, phi23p, phi23s;
+    film_phase(cos_i, eta1, eta2, 0.0f, phi21p, phi21s);
+    film_phase(cos2, eta2, eta3, kappa3, phi23p, phi23s);
+    phi21p = kPi - phi21p;
+    phi21s = kPi - phi21s;
+    const float r123[2] = {sqrtf(r12p * r23p), sqrtf(r12s * r23s)};
+    const float r12[2] = {r12p, r12s}, r23[2] = {r23p, r23s}, t121[2] = {t121p, t121s};
+    const float phi[2] = {phi23p + phi21p, phi23s + phi21s};
+    V3 I = v3(0.0f);
+#pragma unroll
+    for (int pol = 0; pol < 2; pol++)
+    {
+        const float Rs = (sq(t121[pol]) * r23[pol]) / (1.0f - r12[pol] * r23[pol]);
+        I = I + v3(r12[pol] + Rs);
+        float Cm = Rs - t121[pol];
+#pragma unroll
+        for (int k = 1; k <= 2; k++)
+        {
+            Cm *= r123[pol];
+            I = I + Cm * (2.0f * film_sensitivity(k * D, k * phi[pol]));
+        }
+    }
+    I = I * 0.5f;
+    // CIE XYZ (1931) to CIE RGB
+    const V3 rgb = v3(2.3646381f * I.x - 0.8965361f * I.y - 0.4680737f * I.z,
+                      -0.5151664f * I.x + 1.4264000f * I.y + 0.0887608f * I.z,
+                      0.0052037f * I.x - 0.0144081f * I.y + 1.0092106f * I.z);
+    return hue_rotate(clamp3(0.0f, 1.0f, rgb), m.tf_hue * 360.0f);
+}
+
 // Hemispherical albedo of a smooth dielectric interface (d'Eon, "A Hitchhiker's Guide to
 // Multiple Scattering", eq. 11.15 fit)
 GBPT_HD float fresnel_hemispherical_albedo(float eta)
@@ -280,16 +407,21 @@ GBPT_HD V3 ggx_reflection(float roughness, float anisotropy, bool height_correla
     return F * D * g2 / (4.0f * nol * nov);
 }
 
-// refract(d) about n (d and n in the same hemisphere, no total internal reflection)
+// refract(d) about n (d and n in the same hemisphere); the zero vector under total internal
+// reflection. Without a film the glass lobe never refracts there (its Fresnel term is 1); with a
+// film the blended Fresnel term can be below 1 at a totally reflecting interface, where the
+// reference's refraction returns NaN directions: sampling returns f = 0, pdf = 0 instead.
 GBPT_HD V3 refract_dir(V3 d, V3 n, float eta)
 {
     const float noi = dot(d, n);
-    const float cos_t = sqrtf(1.0f - (1.0f - noi * noi) / (eta * eta));
+    const float k = 1.0f - (1.0f - noi * noi) / (eta * eta);
+    if (k < 0.0f) return v3(0.0f);
+    const float cos_t = sqrtf(k);
     return -d / eta + (noi / eta - cos_t) * n;
 }
 
 // Walter et al. 2007 microfacet transmission
-GBPT_HD V3 ggx_refraction(const Material& m, float roughness, float eta, float F, V3 v, V3 l, V3 h, int lobe, float& pdf)
+GBPT_HD V3 ggx_refraction(const Material& m, float roughness, float eta, V3 F, V3 v, V3 l, V3 h, int lobe, float& pdf)
 {
     const float nol = l.z, nov = v.z;
     const float hol = dot(l, h), hov = dot(v, h);
@@ -299,7 +431,7 @@ GBPT_HD V3 ggx_refraction(const Material& m, float roughness, float eta, float F
         const bool perfect = dot(refract_dir(v, v3(0.0f, 0.0f, 1.0f), eta), l) > kDeltaAlign;
         if (lobe == GBPT_LOBE_GLASS_REFRACT && perfect)
         {
-            color = v3(kDeltaValue) * (1.0f - v3(F)) * m.base;
+            color = v3(kDeltaValue) * (1.0f - F) * m.base;
             color = color / fabsf(nol);
             pdf = kDeltaValue;
         }
@@ -321,7 +453,7 @@ GBPT_HD V3 ggx_refraction(const Material& m, float roughness, float eta, float F
         const float g2 = g1v * smith_G1(ax, ay, l);
         const float dwm_dwi = fabsf(hol) / dp2;
         pdf = dwm_dwi * (g1v / fabsf(nov) * D * fabsf(hov));
-        color = m.base * D * (1.0f - v3(F)) * g2 * fabsf(hol * hov / denom);
+        color = m.base * D * (1.0f - F) * g2 * fabsf(hol * hov / denom);
     }
     return color / sq(eta);
 }
@@ -464,12 +596,27 @@ GBPT_HD float glass_eta(const Medium& md)
     return eta;
 }
 
-// Fresnel of the glass interface with the thin-walled inter-reflection correction
-GBPT_HD float glass_fresnel(const Material& m, float hov, float eta, float roughness)
+// Fresnel of the glass interface, blended with the film's (seen from the incident medium), with
+// the thin-walled inter-reflection correction when there is no film
+GBPT_HD V3 glass_fresnel(const Material& m, float hov, float eta, float eta_incident, float roughness)
 {
+    if (m.thin_film > 0.0f)
+    {
+        const V3 F_film = thin_film_fresnel(m, eta_incident, hov);
+        return lerp(m.thin_film < 1.0f ? v3(fresnel_dielectric(hov, eta)) : v3(0.0f), F_film, m.thin_film);
+    }
     float F = fresnel_dielectric(hov, eta);
     if (m.thin_walled && F < 1.0f && roughness < 0.1f) F += sq(1.0f - F) * F / (1.0f - sq(F));
-    return F;
+    return v3(F);
+}
+
+// Fresnel of the specular layer (relative IOR eta_s), blended with the film's seen from the layer
+// above it (principled_specular_fresnel)
+GBPT_HD V3 specular_fresnel(const Material& m, float eta_s, float cos_i)
+{
+    const float F = fresnel_dielectric(cos_i, eta_s);
+    if (m.thin_film == 0.0f) return v3(F);
+    return lerp(m.thin_film < 1.0f ? v3(F) : v3(0.0f), thin_film_fresnel(m, m.ior / eta_s, cos_i), m.thin_film);
 }
 
 // The Oren-Nayar factor A + B max(0, cos(phi_i - phi_o)) sin(alpha) tan(beta) of the diffuse lobe
@@ -521,12 +668,12 @@ GBPT_HD V3 glass_eval(const Material& m, const Medium& md, bool height_correlate
     if (h.z < 0.0f) h = -h;
     const float hol = dot(l, h), hov = dot(v, h);
     if (hol * nol < 0.0f || hov * nov < 0.0f) return v3(0.0f);
-    const float F = glass_fresnel(m, hov, eta, rough);
-    const float p_reflect = luminance(v3(F));
+    const V3 F = glass_fresnel(m, hov, eta, md.eta_incident, rough);
+    const float p_reflect = luminance(F);
     if (reflecting)
     {
         const Delta ds = delta_state(m, rough, m.anisotropy, lobe);
-        const V3 c = ggx_reflection(rough, m.anisotropy, height_correlated, v3(F), v, l, h, ds, pdf);
+        const V3 c = ggx_reflection(rough, m.anisotropy, height_correlated, F, v, l, h, ds, pdf);
         pdf *= p_reflect;
         return c;
     }
@@ -544,8 +691,8 @@ GBPT_HD V3 glass_sample(const Material& m, const Medium& md, V3 v, Rng& rng, int
     float ax, ay;
     ggx_alphas(rough, m.anisotropy, ax, ay);
     V3 h = ggx_sample_visible_normal(v, ax, ay, rng);
-    const float F = glass_fresnel(m, dot(v, h), eta, rough);
-    if (rng() < luminance(v3(F)))
+    const V3 F = glass_fresnel(m, dot(v, h), eta, md.eta_incident, rough);
+    if (rng() < luminance(F))
     {
         lobe = GBPT_LOBE_GLASS_REFLECT;
         return reflect(v, h);
@@ -631,7 +778,8 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
         if (ds != Delta::PeakNotSampled)
         {
             const float hol = clampf(1.0e-8f, 1.0f, dot(hr, lr));
-            const V3 F = fresnel_f82_tint(m.base, m.f82, m.f90, m.f90_exponent, hol);
+            V3 F = fresnel_f82_tint(m.base, m.f82, m.f90, m.f90_exponent, hol);
+            if (m.thin_film > 0.0f) F = lerp(F, thin_film_fresnel(m, eta_in, hol), m.thin_film);
             c = ggx_reflection(metal_r[k], m.anisotropy, height_correlated, F, vr, lr, hr, ds, lobe_pdf);
         }
         color = color + c * metal_w[k] * throughput;
@@ -654,13 +802,22 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
         const float eta_s = specular_relative_ior(m, eta_in);
         float lobe_pdf;
         const Delta ds = delta_state(m, m.roughness, m.anisotropy, lobe);
-        V3 c = ggx_reflection(m.roughness, m.anisotropy, height_correlated, v3(fresnel_dielectric(dot(lr, hr), eta_s)), vr,
+        V3 c = ggx_reflection(m.roughness, m.anisotropy, height_correlated, specular_fresnel(m, eta_s, dot(lr, hr)), vr,
                               lr, hr, ds, lobe_pdf);
         c = c * lerp(v3(1.0f), m.specular_tint * m.specular_color, m.specular);
         glossy = glossy + c * w.specular * throughput;
-        const float light_f = fresnel_dielectric(fabsf(lr.z), eta_s) * (1.0f - m.diffuse_transmission);
-        const float view_f = fresnel_dielectric(fabsf(vr.z), eta_s);
-        V3 att = v3((1.0f - light_f) * (1.0f - view_f));
+        V3 att;
+        if (m.thin_film == 0.0f)
+        {
+            const float light_f = fresnel_dielectric(fabsf(lr.z), eta_s) * (1.0f - m.diffuse_transmission);
+            const float view_f = fresnel_dielectric(fabsf(vr.z), eta_s);
+            att = v3((1.0f - light_f) * (1.0f - view_f));
+        }
+        else
+        {
+            const V3 light_f = specular_fresnel(m, eta_s, fabsf(lr.z)) * (1.0f - m.diffuse_transmission);
+            att = (1.0f - light_f) * (1.0f - specular_fresnel(m, eta_s, fabsf(vr.z)));
+        }
         att = att * specular_darkening(m, eta_s);
         throughput = throughput * lerp(v3(1.0f), att, m.specular);
         pdf += lobe_pdf * p.specular;
@@ -766,7 +923,15 @@ GBPT_HD V3 sample(const Material& m, const Medium& md, bool height_correlated, V
         dir = cosine_around(-ns, rng);
     }
     else
-        dir = FR.to_world(glass_sample(m, md, vr, rng, lobe));
+    {
+        const V3 d = glass_sample(m, md, vr, rng, lobe);
+        if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f)
+        {
+            dir = ns;  // refraction under total internal reflection: no direction
+            return v3(0.0f);
+        }
+        dir = FR.to_world(d);
+    }
 
     if (dot(dir, ng) < 0.0f && !through_glass && !through_dt) return v3(0.0f);
     Query q;

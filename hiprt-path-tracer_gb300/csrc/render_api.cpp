@@ -272,6 +272,11 @@ gbpt_principled_material packed_material(gbpt_principled_material m)
     m.sheen = unpack_byte(m.sheen);
     unpack_color(m.absorption_color);
     m.specular_transmission = unpack_byte(m.specular_transmission);
+    m.thin_film = unpack_byte(m.thin_film);
+    m.thin_film_hue_shift = unpack_byte(m.thin_film_hue_shift);
+    // the packed record's setter takes a bool (set_thin_film_base_ior_override,
+    // MaterialPacked.h:347): any non-zero override IOR arrives as 1
+    m.thin_film_base_ior_override = m.thin_film_base_ior_override != 0.0f ? 1.0f : 0.0f;
     return m;
 }
 

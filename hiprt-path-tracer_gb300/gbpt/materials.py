@@ -24,8 +24,10 @@ FIELDS = [
     ("sheen", 36, 1), ("ior", 37, 1), ("specular_transmission", 38, 1), ("diffuse_transmission", 39, 1),
     ("absorption_color", 40, 3), ("absorption_at_distance", 43, 1),
     ("thin_walled", 44, 1), ("diffuse_lobe", 45, 1), ("oren_nayar_sigma", 46, 1),
+    ("thin_film", 47, 1), ("thin_film_ior", 48, 1), ("thin_film_thickness", 49, 1), ("thin_film_kappa_3", 50, 1),
+    ("thin_film_hue_shift", 51, 1), ("thin_film_base_ior_override", 52, 1), ("thin_film_do_ior_override", 53, 1),
 ]
-INT_FIELDS = ("thin_walled", "diffuse_lobe")
+INT_FIELDS = ("thin_walled", "diffuse_lobe", "thin_film_do_ior_override")
 DIFFUSE_LAMBERTIAN, DIFFUSE_OREN_NAYAR = 0, 1  # GBPT_DIFFUSE_*
 OFFSETS = {n: (o, c) for n, o, c in FIELDS}
 
@@ -39,6 +41,8 @@ DEFAULTS = {
     "coat_ior": 1.5, "sheen": 0.0, "ior": 1.4, "specular_transmission": 0.0, "diffuse_transmission": 0.0,
     "absorption_color": (1.0, 1.0, 1.0), "absorption_at_distance": 1.0, "thin_walled": 0,
     "diffuse_lobe": DIFFUSE_LAMBERTIAN, "oren_nayar_sigma": 0.34906585039886591538,  # 20 degrees
+    "thin_film": 0.0, "thin_film_ior": 1.3, "thin_film_thickness": 500.0, "thin_film_kappa_3": 0.0,
+    "thin_film_hue_shift": 0.0, "thin_film_base_ior_override": 1.0, "thin_film_do_ior_override": 0,
 }
 
 

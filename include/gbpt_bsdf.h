@@ -7,7 +7,7 @@
  * sheen, two metal lobes, specular over diffuse, glass and diffuse transmission, blended by the
  * same lobe weights and sampled with the same lobe probabilities.
  * Built without: energy compensation (it needs the reference's precomputed directional-albedo
- * tables), microfacet regularization (biased), thin-film interference, dispersion and the sheen
+ * tables), microfacet regularization (biased), dispersion and the sheen
  * lobe: the entry points below treat 'sheen' as 0, and scene creation rejects materials with
  * sheen > 0 (GBPT_ERROR_UNSUPPORTED). A query whose material index is out of range returns zeros.
  * See gbpt.h for status codes; all pointers below are device pointers.
@@ -58,7 +58,17 @@ typedef struct gbpt_principled_material {
     float oren_nayar_sigma;        /* GBPT_DIFFUSE_OREN_NAYAR: roughness, the standard deviation of
                                       the facet slope angle in radians (the reference's default is
                                       20 degrees, 0.349066) */
-    int32_t reserved[17];
+    /* thin-film interference over the metal, specular and glass interfaces (Belcour and Barla
+     * 2017, the reference's thin_film_fresnel, src/Device/includes/BSDFs/ThinFilm.h:124-226):
+     * each lobe's Fresnel term becomes lerp(its own, the film's RGB reflectance, thin_film) */
+    float thin_film;               /* weight in [0, 1] [0] */
+    float thin_film_ior;           /* the film's IOR [1.3] */
+    float thin_film_thickness;     /* nanometres [500] */
+    float thin_film_kappa_3;       /* extinction of the base under the film, with the override [0] */
+    float thin_film_hue_shift;     /* in turns (degrees / 360, as the reference's unpacked material) [0] */
+    float thin_film_base_ior_override; /* the base's IOR under the film, with the override [1] */
+    int32_t thin_film_do_ior_override; /* 0: the base is the material's own IOR, kappa 0 */
+    int32_t reserved[10];
 } gbpt_principled_material;
 
 /* The diffuse lobe of the principled BSDF's glossy base (gbpt_principled_material.diffuse_lobe):

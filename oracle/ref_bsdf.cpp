@@ -31,6 +31,7 @@
 
 #include "Device/includes/BSDFs/Principled.h"
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -73,7 +74,15 @@ DeviceUnpackedEffectiveMaterial unpack(const float* w)
     std::memcpy(&thin, w + 44, 4);
     m.thin_walled = thin != 0;
     m.oren_nayar_sigma = w[46];
-    m.thin_film = 0.0f;
+    m.thin_film = w[47];
+    m.thin_film_ior = w[48];
+    m.thin_film_thickness = w[49];
+    m.thin_film_kappa_3 = w[50];
+    m.thin_film_hue_shift_degrees = w[51];  // the unpacked material holds turns (degrees / 360)
+    m.thin_film_base_ior_override = w[52];
+    int32_t tf_override;
+    std::memcpy(&tf_override, w + 53, 4);
+    m.thin_film_do_ior_override = tf_override != 0;
     m.dispersion_scale = 0.0f;
     return m;
 }
@@ -103,6 +112,9 @@ struct Ctx
         vs.outgoing_mat_index = q[13] == 1.0f ? NestedDielectricsInteriorStack::MAX_MATERIAL_INDEX : 1;
         vs.inside_material = q[14] != 0.0f;
         vs.sampled_wavelength = 0.0f;
+        // a NaN caught by the BSDF's CPU sanity check is zeroed rather than written to the
+        // (absent) frame buffer
+        rd.render_settings.display_NaNs = false;
     }
 };
 
@@ -192,6 +204,17 @@ void ref_principled_sample_one(const float* mat, const float* q, uint32_t seed, 
 {
     uint32_t rng_after;
     sample_query(mat, q, seed, out, lobe, &rng_after);
+    // With a thin film the glass lobe can pick refraction at a totally reflecting interface, where
+    // the reference's refraction gives a NaN direction (and pdf). The path-tracing oracle needs a
+    // defined outcome there: the sample is reported as no direction, f = 0, pdf = 0 (the path
+    // ends), which is what the library's BSDF returns in that case.
+    if (!std::isfinite(out[0]) || !std::isfinite(out[1]) || !std::isfinite(out[2]))
+    {
+        out[0] = q[3];
+        out[1] = q[4];
+        out[2] = q[5];
+        out[3] = out[4] = out[5] = out[6] = 0.0f;
+    }
     std::memcpy(out + 7, &rng_after, 4);  // the generator's state after sampling, bit for bit
 }
 

@@ -106,9 +106,19 @@ CPUMaterial cpu_material(const float* w)
     std::memcpy(&thin, w + 44, 4);
     m.thin_walled = thin != 0;
     m.oren_nayar_sigma = w[46];
+    m.thin_film = w[47];
+    m.thin_film_ior = w[48];
+    m.thin_film_thickness = w[49];
+    m.thin_film_kappa_3 = w[50];
+    m.thin_film_hue_shift_degrees = w[51] * 360.0f;  // pack_to_GPU stores degrees / 360
+    m.thin_film_base_ior_override = w[52];
+    int32_t tf_override;
+    std::memcpy(&tf_override, w + 53, 4);
+    m.thin_film_do_ior_override = tf_override != 0;
     // the reference's scene parser calls make_safe on every material
     // (src/Scene/SceneParser.cpp:391-438); its clamps only touch fields this layout does not
-    // carry, except the dielectric priority of non-transmissive materials
+    // carry, the thin-film ranges (weight and hue in range, film IOR >= 1.0005) and the dielectric
+    // priority of non-transmissive materials
     m.make_safe();
     return m;
 }
@@ -381,7 +391,7 @@ REF_EXPORT void refr_render(void* h, const int32_t* settings_i, const float* set
 
 /* The material the reference's kernels see after packing (pack_to_GPU, the 8-bit fields of
  * DevicePackedEffectiveMaterial, src/HostDeviceCommon/Material/MaterialPacked.h) and unpacking,
- * written back in the 64-word layout (word 45, the diffuse-lobe selector, copied; 47..63 zero). */
+ * written back in the 64-word layout (word 45, the diffuse-lobe selector, copied; 54..63 zero). */
 REF_EXPORT void refr_pack_unpack_material(const float* in, float* out)
 {
     CPUMaterial c = cpu_material(in);
@@ -422,6 +432,14 @@ REF_EXPORT void refr_pack_unpack_material(const float* in, float* out)
     std::memcpy(w + 44, &thin, 4);
     w[45] = in[45];  // the diffuse-lobe selector: a compile-time option of the reference, copied
     w[46] = m.oren_nayar_sigma;
+    w[47] = m.thin_film;
+    w[48] = m.thin_film_ior;
+    w[49] = m.thin_film_thickness;
+    w[50] = m.thin_film_kappa_3;
+    w[51] = m.thin_film_hue_shift_degrees;
+    w[52] = m.thin_film_base_ior_override;
+    int32_t tf_override = m.thin_film_do_ior_override ? 1 : 0;
+    std::memcpy(w + 53, &tf_override, 4);
     std::memcpy(out, w, sizeof(w));
 }
 

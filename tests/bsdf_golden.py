@@ -1,5 +1,6 @@
-"""TEST INFRASTRUCTURE ONLY — the principled-BSDF golden vectors (tests/golden/bsdf_principled.npz and,
-for the Oren-Nayar diffuse lobe, bsdf_oren_nayar.npz, written by the reference's own BSDF through
+"""TEST INFRASTRUCTURE ONLY — the principled-BSDF golden vectors (tests/golden/bsdf_principled.npz; for
+the Oren-Nayar diffuse lobe, bsdf_oren_nayar.npz; with thin films, bsdf_thin_film.npz; written by the
+reference's own BSDF through
 tests/golden/make_bsdf_golden.py) and the comparison
 both the CPU test (host build of the BSDF) and the GPU test (CUDA build) apply.
 
@@ -20,7 +21,9 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_principled.npz")
 # the same queries' kind against the reference built with its Oren-Nayar diffuse lobe
 GOLDEN_OREN_NAYAR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_oren_nayar.npz")
-SETS = {"lambertian": GOLDEN, "oren_nayar": GOLDEN_OREN_NAYAR}
+# every material with a thin film over its metal, specular and glass interfaces
+GOLDEN_THIN_FILM = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_thin_film.npz")
+SETS = {"lambertian": GOLDEN, "oren_nayar": GOLDEN_OREN_NAYAR, "thin_film": GOLDEN_THIN_FILM}
 RTOL = 1e-5
 RTOL_ALL = 2e-4
 TIGHT_FRACTION = 0.995

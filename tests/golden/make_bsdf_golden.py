@@ -7,11 +7,18 @@ regularization compiled out) on seeded materials and directions, and stores inpu
   pdf:    same inputs -> pdf                                      [principled_bsdf_pdf :1717]
   sample: material, view, normals, Xorshift32 seed -> direction, rgb, pdf, sampled lobe,
           generator state after sampling                         [principled_bsdf_sample :1803]
+With --thin-film, writes tests/golden/bsdf_thin_film.npz from the same library: every material of the
+set carries a thin film (weight, film IOR, thickness, hue shift and, on a third of them, the base IOR
+and extinction override, all seeded; ThinFilm.h). Sampling queries where the glass lobe picks
+refraction at a totally reflecting interface (possible once the film's Fresnel term is blended in)
+are left out: the reference's refraction returns a NaN direction there and its CPU sanity check
+then takes the harness down. They are found beforehand with the library's BSDF built for the host
+(tests/native), which returns f = 0, pdf = 0 for them.
 With --oren-nayar, writes tests/golden/bsdf_oren_nayar.npz from oracle/_ref/libref_bsdf_oren_nayar.so
 instead: the same BSDF compiled with the reference's Oren-Nayar diffuse lobe
 (PrincipledBSDFDiffuseLobe = PRINCIPLED_DIFFUSE_LOBE_OREN_NAYAR, src/Device/includes/BSDFs/OrenNayar.h),
 every material carrying diffuse_lobe = Oren-Nayar and a seeded facet-slope deviation sigma.
-Usage (where the reference tree is present):  python tests/golden/make_bsdf_golden.py [--oren-nayar]
+Usage (where the reference tree is present):  python tests/golden/make_bsdf_golden.py [--oren-nayar | --thin-film]
 """
 import ctypes
 import os
@@ -29,6 +36,7 @@ import pyoracle  # noqa: E402
 
 OUT = os.path.join(HERE, "bsdf_principled.npz")
 OUT_ON = os.path.join(HERE, "bsdf_oren_nayar.npz")
+OUT_TF = os.path.join(HERE, "bsdf_thin_film.npz")
 REF_ON_SO = os.path.join(REPO, "oracle", "_ref", "libref_bsdf_oren_nayar.so")
 
 
@@ -37,7 +45,7 @@ def _unit(rng, n):
     return v / np.linalg.norm(v, axis=1, keepdims=True)
 
 
-def material_set(rng, oren_nayar=False):
+def material_set(rng, oren_nayar=False, thin_film=False):
     """Edge cases of every lobe first, then the random principled distribution. With oren_nayar,
     every material selects the Oren-Nayar diffuse lobe with sigma in [0, 1.2] rad (0 and the
     default 20 degrees among them)."""
@@ -67,6 +75,18 @@ def material_set(rng, oren_nayar=False):
         sig = rng.uniform(0.0, 1.2, len(mats))
         sig[0], sig[1] = 0.0, M.DEFAULTS["oren_nayar_sigma"]
         mats = [dict(m, diffuse_lobe=M.DIFFUSE_OREN_NAYAR, oren_nayar_sigma=float(s)) for m, s in zip(mats, sig)]
+    if thin_film:
+        n = len(mats)
+        weight = rng.uniform(0.2, 1.0, n)
+        weight[:4] = 1.0  # a full film on the first lobes' edge cases
+        override = rng.random(n) < 1.0 / 3.0
+        mats = [dict(m, thin_film=float(weight[i]), thin_film_ior=float(rng.uniform(1.1, 2.2)),
+                     thin_film_thickness=float(rng.uniform(80.0, 1500.0)),
+                     thin_film_hue_shift=float(rng.choice([0.0, rng.uniform(0.0, 1.0)])),
+                     thin_film_do_ior_override=int(override[i]),
+                     thin_film_base_ior_override=float(rng.uniform(1.0, 3.0)),
+                     thin_film_kappa_3=float(rng.uniform(0.0, 3.0)))
+                for i, m in enumerate(mats)]
     return M.pack_many([M.coat_roughened(m) for m in mats])
 
 
@@ -105,8 +125,28 @@ def queries(rng, mats, n, sample):
     return mi, q
 
 
+def refraction_under_tir(mats, smi, sq, seeds):
+    """Sampling queries whose glass refraction meets total internal reflection (host build)."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from native import build_emu
+    import bsdf_golden
+    lib = ctypes.CDLL(build_emu.build())
+    vp = ctypes.c_void_p
+    lib.emu_bsdf_sample.argtypes = [vp, vp, vp, vp, ctypes.c_int64, ctypes.c_int, vp, vp, vp]
+    q = bsdf_golden.queries(sq)
+    mi = np.ascontiguousarray(smi, np.int32)
+    sd = np.ascontiguousarray(seeds, np.uint32)
+    out = np.zeros((len(q), 8), np.float32)
+    lobe = np.zeros(len(q), np.int32)
+    st = np.zeros(len(q), np.uint32)
+    lib.emu_bsdf_sample(mats.ctypes.data, mi.ctypes.data, q.ctypes.data, sd.ctypes.data, len(q), 0, out.ctypes.data,
+                        lobe.ctypes.data, st.ctypes.data)
+    return (lobe == 64) & (out[:, 6] == 0) & np.all(out[:, 0:3] == sq[:, 3:6], axis=1)
+
+
 def main():
     oren_nayar = "--oren-nayar" in sys.argv[1:]
+    thin_film = "--thin-film" in sys.argv[1:]
     pyoracle.build(ref=True)
     lib = ctypes.CDLL(REF_ON_SO if oren_nayar else pyoracle.REF_SO)
     fp = ctypes.POINTER(ctypes.c_float)
@@ -116,8 +156,8 @@ def main():
     lib.ref_principled_pdf.argtypes = [fp, ip, fp, ctypes.c_int64, fp]
     lib.ref_principled_sample.argtypes = [fp, ip, fp, up, ctypes.c_int64, fp, ip, up]
 
-    rng = np.random.Generator(np.random.PCG64(20241 if oren_nayar else 20240))
-    mats = np.ascontiguousarray(material_set(rng, oren_nayar))
+    rng = np.random.Generator(np.random.PCG64(20241 if oren_nayar else 20242 if thin_film else 20240))
+    mats = np.ascontiguousarray(material_set(rng, oren_nayar, thin_film))
     n_eval, n_sample = 8192, 8192
     emi, eq = queries(rng, mats, n_eval, sample=False)
     eout = np.zeros((n_eval, 4), np.float32)
@@ -128,13 +168,17 @@ def main():
                            pout.ctypes.data_as(fp))
     smi, sq = queries(rng, mats, n_sample, sample=True)
     seeds = rng.integers(1, 2**32 - 1, n_sample, dtype=np.uint64).astype(np.uint32)
+    if thin_film:
+        keep = ~refraction_under_tir(mats, smi, sq, seeds)
+        smi, sq, seeds = np.ascontiguousarray(smi[keep]), np.ascontiguousarray(sq[keep]), np.ascontiguousarray(seeds[keep])
+        n_sample = len(smi)
     sout = np.zeros((n_sample, 8), np.float32)
     sinfo = np.zeros(n_sample, np.int32)
     srng = np.zeros(n_sample, np.uint32)
     lib.ref_principled_sample(mats.ctypes.data_as(fp), smi.ctypes.data_as(ip), sq.ctypes.data_as(fp),
                               seeds.ctypes.data_as(up), n_sample, sout.ctypes.data_as(fp), sinfo.ctypes.data_as(ip),
                               srng.ctypes.data_as(up))
-    out_path = OUT_ON if oren_nayar else OUT
+    out_path = OUT_ON if oren_nayar else OUT_TF if thin_film else OUT
     np.savez_compressed(out_path, materials=mats, eval_mat=emi, eval_q=eq, eval_out=eout, pdf_out=pout,
                         sample_mat=smi, sample_q=sq, seeds=seeds, sample_out=sout, sample_info=sinfo, sample_rng=srng)
     print(f"wrote {out_path}: {len(mats)} materials, {n_eval} eval/pdf + {n_sample} sample queries; "

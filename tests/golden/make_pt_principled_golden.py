@@ -10,7 +10,8 @@ tall box (a delta BSDF: no light sampling), the area light. The scene and settin
 the image so the GPU test needs nothing else. A third file renders the smooth-shading scene (two
 coarse spheres shaded with their vertex normals); a fourth, pt_principled_oren_nayar_cornell.npz,
 the Cornell scene with the Oren-Nayar diffuse lobe, shaded by the reference's BSDF built with that
-lobe (oracle/_ref/libref_bsdf_oren_nayar.so).
+lobe (oracle/_ref/libref_bsdf_oren_nayar.so); a fifth, pt_principled_thin_film_cornell.npz, the
+Cornell scene with thin films on the walls, the metal, the glass box and the mirror (reference BSDF).
 Usage (where the reference tree is present):  python tests/golden/make_pt_principled_golden.py
 """
 import os
@@ -31,6 +32,7 @@ OUT = os.path.join(HERE, "pt_principled_cornell.npz")
 OUT_RIS = os.path.join(HERE, "pt_principled_ris_cornell.npz")
 OUT_SMOOTH = os.path.join(HERE, "pt_principled_smooth_cornell.npz")
 OUT_ON = os.path.join(HERE, "pt_principled_oren_nayar_cornell.npz")
+OUT_TF = os.path.join(HERE, "pt_principled_thin_film_cornell.npz")
 
 
 MATERIALS = [
@@ -120,6 +122,22 @@ def main():
                                         st.samples_per_launch, bsdf="reference_oren_nayar")
     np.savez_compressed(OUT_ON, materials=raw, image=img)
     print(f"wrote {OUT_ON}: mean {img.mean() / st.samples_per_launch:.4f}")
+    # the Cornell scene with thin films: iridescent coated walls, a filmed metal green wall, a
+    # filmed rough glass box (base IOR override with extinction), a filmed mirror box
+    films = (dict(thin_film=1.0, thin_film_ior=1.45, thin_film_thickness=420.0),
+             dict(thin_film=0.7, thin_film_ior=1.8, thin_film_thickness=650.0, thin_film_hue_shift=0.25),
+             dict(thin_film=1.0, thin_film_ior=1.33, thin_film_thickness=300.0),
+             dict(),
+             dict(thin_film=0.8, thin_film_ior=1.6, thin_film_thickness=900.0, thin_film_do_ior_override=1,
+                  thin_film_base_ior_override=1.7, thin_film_kappa_3=0.5),
+             dict(thin_film=1.0, thin_film_ior=1.25, thin_film_thickness=520.0))
+    tf = [dict(m, **f) for m, f in zip(MATERIALS, films)]
+    raw = M.pack_many(tf)
+    eff = M.pack_many([M.coat_roughened(m) for m in tf])
+    img = pyoracle.pt_render_principled(mesh.triangle_soup(), mat_of, eff, emission, emissive, None, None, 0.0, st,
+                                        st.samples_per_launch)
+    np.savez_compressed(OUT_TF, materials=raw, image=img)
+    print(f"wrote {OUT_TF}: mean {img.mean() / st.samples_per_launch:.4f}")
 
 
 if __name__ == "__main__":

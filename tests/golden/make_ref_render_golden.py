@@ -3,7 +3,7 @@ render kernels — CameraRays + MegaKernel compiled from the reference's sources
 (oracle/ref_render.cpp, built by `make -C oracle ref`) — which pin the GPU path tracer's
 GBPT_RNG_REFERENCE mode sample by sample.
 
-Three scenes, each rendered for FRAMES frames of one sample per pixel with the reference's
+Five scenes, each rendered for FRAMES frames of one sample per pixel with the reference's
 per-pass random numbers as its GPU renderer draws them: the renderer's Xorshift32, seeded with 42
 (GPURenderer.cpp:750-751), gives one number to the G-buffer pass and one to the MegaKernel pass of
 every sample (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53):
@@ -14,7 +14,9 @@ every sample (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53):
     (no transmissive object), power light sampling;
   * principled_glass: the same with a rough glass short box (nested-dielectric volume tracking);
   * principled_ris: the principled scene with direct lighting by RIS over 4 light and 1 BSDF
-    candidates (LSS_RIS_BSDF_AND_LIGHT, the reference's default strategy, RIS.h:83-255).
+    candidates (LSS_RIS_BSDF_AND_LIGHT, the reference's default strategy, RIS.h:83-255);
+  * principled_thin_film: the principled scene with thin films on the walls, the boxes and the
+    mirror (the packed record's 8-bit film weight and hue, and its boolean base-IOR override).
 Each frame image is the frame's sample (float32 H x W x 3); the scene arrays and settings are stored
 with it, so the GPU test needs nothing else.
 Usage (where the reference tree is present):  python tests/golden/make_ref_render_golden.py
@@ -44,6 +46,17 @@ OPAQUE = [
     dict(base_color=(0.0, 0.0, 0.0), emission=(17.0, 12.0, 4.0)),                            # 3 light
     dict(base_color=(0.8, 0.75, 0.7), roughness=0.25, metallic=0.5),                         # 4 short box
     dict(base_color=(0.9, 0.9, 0.9), roughness=0.0, metallic=1.0),                           # 5 tall box (mirror)
+]
+# thin films (ThinFilm.h) on the coated walls, the red dielectric wall, the metal wall, the half-metal
+# box (with the base IOR override) and the mirror
+FILMS = [
+    dict(OPAQUE[0], thin_film=1.0, thin_film_ior=1.45, thin_film_thickness=420.0),
+    dict(OPAQUE[1], thin_film=0.6, thin_film_ior=1.8, thin_film_thickness=650.0, thin_film_hue_shift=0.25),
+    dict(OPAQUE[2], thin_film=1.0, thin_film_ior=1.33, thin_film_thickness=300.0),
+    OPAQUE[3],
+    dict(OPAQUE[4], thin_film=0.8, thin_film_ior=1.6, thin_film_thickness=900.0, thin_film_do_ior_override=1,
+         thin_film_base_ior_override=1.7, thin_film_kappa_3=0.5),
+    dict(OPAQUE[5], thin_film=1.0, thin_film_ior=1.25, thin_film_thickness=520.0),
 ]
 GLASS = OPAQUE[:4] + [
     dict(base_color=(0.95, 0.95, 0.95), roughness=0.15, specular_transmission=1.0, ior=1.5),  # 4 glass box
@@ -96,7 +109,7 @@ def main():
     mat_of[10:22] = 4
     mat_of[22:34] = 5
     for name, mats, light in (("principled", OPAQUE, "power"), ("principled_glass", GLASS, "power"),
-                              ("principled_ris", OPAQUE, "power_ris")):
+                              ("principled_ris", OPAQUE, "power_ris"), ("principled_thin_film", FILMS, "power")):
         raw = M.pack_many(mats)
         img, lt = render("principled", light, cb.mesh, mat_of, raw, Settings(LIGHT_POWER))
         out.update({f"{name}_materials": raw, f"{name}_material_of": mat_of, name: img,

@@ -65,7 +65,7 @@ def test_lambert_cornell_matches_reference_megakernel(cuda):
     assert abs(gpu.mean() - ref.mean()) <= 2e-3 * ref.mean(), (gpu.mean(), ref.mean())
 
 
-@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris"])
+@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris", "principled_thin_film"])
 def test_principled_cornell_matches_reference_megakernel(cuda, name):
     """Coated, glossy dielectric, anisotropic metal, metallic-blend and mirror materials (and a
     rough glass box entered and left through the nested-dielectric volume stack), power light

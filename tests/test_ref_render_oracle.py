@@ -60,11 +60,12 @@ def test_library_material_packing_matches_reference_layout():
     """gbpt_material_pack_8bit (host code of the library) on the golden materials gives the
     records the reference's kernels read (8-bit fields truncated, green through its << 8 path)."""
     g = _golden()
-    for key in ("lambert_materials", "principled_materials", "principled_glass_materials"):
+    for key in ("lambert_materials", "principled_materials", "principled_glass_materials",
+                "principled_thin_film_materials"):
         got = _packed_host(g[key])
         if pyoracle.ref_render_available():
             want = pyoracle.ref_pack_unpack_material(g[key])
-            assert np.array_equal(got[:, :44].view(np.uint32), want[:, :44].view(np.uint32)), key
+            assert np.array_equal(got[:, :54].view(np.uint32), want[:, :54].view(np.uint32)), key
 
 
 @REF
@@ -77,9 +78,17 @@ def test_material_packing_random_records_bit_exact():
         recs[:, w] = rng.uniform(0, 1, len(recs)).astype(np.float32)
     recs[:, 36] = 0.0
     recs[:5, 0:3] = [[k / 255.0] * 3 for k in (0, 1, 127, 254, 255)]
+    # thin film: weight and hue shift are 8-bit fields, the rest full floats
+    recs[:, 47] = rng.uniform(0, 1, len(recs)).astype(np.float32)
+    recs[:, 48] = rng.uniform(1.1, 2.2, len(recs)).astype(np.float32)
+    recs[:, 49] = rng.uniform(50.0, 1500.0, len(recs)).astype(np.float32)
+    recs[:, 50] = rng.uniform(0.0, 3.0, len(recs)).astype(np.float32)
+    recs[:, 51] = rng.uniform(0, 1, len(recs)).astype(np.float32)
+    recs[:, 52] = rng.uniform(1.0, 3.0, len(recs)).astype(np.float32)
+    recs[:, 53] = (rng.random(len(recs)) < 0.5).astype(np.int32).view(np.float32)
     got = _packed_host(recs)
     want = pyoracle.ref_pack_unpack_material(recs)
-    assert np.array_equal(got[:, :44].view(np.uint32), want[:, :44].view(np.uint32))
+    assert np.array_equal(got[:, :54].view(np.uint32), want[:, :54].view(np.uint32))
 
 
 @REF
@@ -122,7 +131,7 @@ def test_alias_restatement_matches_reference_utils():
 
 
 @REF
-@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris"])
+@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris", "principled_thin_film"])
 def test_principled_oracle_matches_reference_megakernel_frames(name):
     """The restated estimator with the reference's own BSDF (through callbacks that hand back the
     generator's state) on the principled Cornell box, with and without a rough glass box whose

@@ -15,6 +15,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pt_principled_cornell.npz")
 GOLDEN_ON = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pt_principled_oren_nayar_cornell.npz")
+GOLDEN_TF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pt_principled_thin_film_cornell.npz")
 
 
 def _load():
@@ -49,11 +50,13 @@ def test_principled_cornell_matches_reference_bsdf_oracle(cuda):
     assert mean_rel_close < 1e-4, mean_rel_close
 
 
-def test_oren_nayar_cornell_matches_reference_lobe(cuda):
-    """Every material on the Oren-Nayar diffuse lobe (per-material sigma), against the oracle image
-    shaded by the reference's BSDF compiled with its Oren-Nayar lobe."""
+@pytest.mark.parametrize("golden", [GOLDEN_ON, GOLDEN_TF], ids=["oren_nayar", "thin_film"])
+def test_lobe_variant_cornell_matches_reference(cuda, golden):
+    """Every material on the Oren-Nayar diffuse lobe (per-material sigma), or thin films on the
+    walls, the metal, the glass box and the mirror, against the oracle image shaded by the
+    reference's BSDF (compiled with its Oren-Nayar lobe for the first)."""
     g, st, _ = _load()
-    on = np.load(GOLDEN_ON)
+    on = np.load(golden)
     scene = gbpt.Scene(g["positions"], g["indices"], g["material_of"], principled=on["materials"])
     gpu = _render(scene, st)
     orc = on["image"]
