@@ -70,11 +70,11 @@ struct Material
     V3 coat_absorption;
     float sheen, ior, transmission, diffuse_transmission;
     bool thin_walled;
-    bool oren_nayar;           // GBPT_DIFFUSE_OREN_NAYAR diffuse lobe
-    float oren_a, oren_b;      // its A and B terms of the facet-slope deviation
-    float thin_film;           // thin-film weight (0: no film, the code below skips it)
-    float tf_ior, tf_thickness, tf_hue;
-    float tf_base_ior, tf_kappa;  // the base under the film: override or the material's IOR, kappa 0
+    // the record itself when the material uses a lobe beyond the common ones (an Oren-Nayar
+    // diffuse lobe, a thin film), else null: such materials are evaluated by a separate, out-of-line
+    // instantiation that reads those parameters from here, so that the common materials' code and
+    // registers stay as they are without them
+    const gbpt_principled_material* ext;
 };
 
 GBPT_HD Material load_material(const gbpt_principled_material& s)
@@ -107,18 +107,7 @@ GBPT_HD Material load_material(const gbpt_principled_material& s)
     m.transmission = s.specular_transmission;
     m.diffuse_transmission = s.diffuse_transmission;
     m.thin_walled = s.thin_walled != 0;
-    // Oren-Nayar A and B from the facet-slope deviation sigma (MaterialUtils::get_oren_nayar_AB,
-    // src/HostDeviceCommon/Material/MaterialUtils.h:18-23)
-    m.oren_nayar = s.diffuse_lobe == GBPT_DIFFUSE_OREN_NAYAR;
-    const float s2 = s.oren_nayar_sigma * s.oren_nayar_sigma;
-    m.oren_a = 1.0f - s2 / (2.0f * (s2 + 0.33f));
-    m.oren_b = 0.45f * s2 / (s2 + 0.09f);
-    m.thin_film = s.thin_film;
-    m.tf_ior = s.thin_film_ior;
-    m.tf_thickness = s.thin_film_thickness;
-    m.tf_hue = s.thin_film_hue_shift;
-    m.tf_base_ior = s.thin_film_do_ior_override ? s.thin_film_base_ior_override : s.ior;
-    m.tf_kappa = s.thin_film_do_ior_override ? s.thin_film_kappa_3 : 0.0f;
+    m.ext = (s.diffuse_lobe == GBPT_DIFFUSE_OREN_NAYAR || s.thin_film > 0.0f) ? &s : nullptr;
     return m;
 }
 
@@ -302,10 +291,13 @@ GBPT_HD V3 hue_rotate(V3 c, float degrees)
 
 // RGB reflectance of the film seen from a medium of IOR ambient_ior at cosine cos_i (out of line
 // on the device: only film materials take it)
-GBPT_HD_OUTLINE V3 thin_film_fresnel(const Material& m, float ambient_ior, float cos_i)
+GBPT_HD_OUTLINE V3 thin_film_fresnel(const gbpt_principled_material& e, float ambient_ior, float cos_i)
 {
-    if (m.thin_film == 0.0f) return v3(0.0f);
-    const float eta1 = ambient_ior, eta2 = m.tf_ior, eta3 = m.tf_base_ior, kappa3 = m.tf_kappa;
+    if (e.thin_film == 0.0f) return v3(0.0f);
+    // the base under the film: the override, else the material's own IOR with no extinction
+    const float eta1 = ambient_ior, eta2 = e.thin_film_ior;
+    const float eta3 = e.thin_film_do_ior_override ? e.thin_film_base_ior_override : e.ior;
+    const float kappa3 = e.thin_film_do_ior_override ? e.thin_film_kappa_3 : 0.0f;
     float r12p = 1.0f, r12s = 1.0f, r23p = 0.0f, r23s = 0.0f, t121p = 0.0f, t121s = 0.0f, cos2 = 0.0f;
     const float cos_t2 = 1.0f - (1.0f - sq(cos_i)) * sq(eta1 / eta2);
     if (cos_t2 > 0.0f)
@@ -316,7 +308,7 @@ GBPT_HD_OUTLINE V3 thin_film_fresnel(const Material& m, float ambient_ior, float
         t121p = 1.0f - r12p;
         t121s = 1.0f - r12s;
     }
-    const float D = m.tf_thickness / 1000.0f * cos2;  // optical path difference, micrometres
+    const float D = e.thin_film_thickness / 1000.0f * cos2;  // optical path difference, micrometres
     float phi21p, phi21s, phi23p, phi23s;
     film_phase(cos_i, eta1, eta2, 0.0f, phi21p, phi21s);
     film_phase(cos2, eta2, eta3, kappa3, phi23p, phi23s);
@@ -344,7 +336,7 @@ GBPT_HD_OUTLINE V3 thin_film_fresnel(const Material& m, float ambient_ior, float
     const V3 rgb = v3(2.3646381f * I.x - 0.8965361f * I.y - 0.4680737f * I.z,
                       -0.5151664f * I.x + 1.4264000f * I.y + 0.0887608f * I.z,
                       0.0052037f * I.x - 0.0144081f * I.y + 1.0092106f * I.z);
-    return hue_rotate(clamp3(0.0f, 1.0f, rgb), m.tf_hue * 360.0f);
+    return hue_rotate(clamp3(0.0f, 1.0f, rgb), e.thin_film_hue_shift * 360.0f);
 }
 
 // Hemispherical albedo of a smooth dielectric interface (d'Eon, "A Hitchhiker's Guide to
@@ -596,33 +588,38 @@ GBPT_HD float glass_eta(const Medium& md)
     return eta;
 }
 
-// Fresnel of the glass interface, blended with the film's (seen from the incident medium), with
-// the thin-walled inter-reflection correction when there is no film
-GBPT_HD V3 glass_fresnel(const Material& m, float hov, float eta, float eta_incident, float roughness)
+// Fresnel of the glass interface with the thin-walled inter-reflection correction
+GBPT_HD float glass_fresnel(const Material& m, float hov, float eta, float roughness)
 {
-    if (m.thin_film > 0.0f)
-    {
-        const V3 F_film = thin_film_fresnel(m, eta_incident, hov);
-        return lerp(m.thin_film < 1.0f ? v3(fresnel_dielectric(hov, eta)) : v3(0.0f), F_film, m.thin_film);
-    }
     float F = fresnel_dielectric(hov, eta);
     if (m.thin_walled && F < 1.0f && roughness < 0.1f) F += sq(1.0f - F) * F / (1.0f - sq(F));
-    return v3(F);
+    return F;
+}
+
+// The glass Fresnel term blended with the film's, seen from the incident medium (no thin-walled
+// correction with a film)
+GBPT_HD V3 glass_fresnel_film(const gbpt_principled_material& e, float hov, float eta, float eta_incident)
+{
+    const V3 F_film = thin_film_fresnel(e, eta_incident, hov);
+    return lerp(e.thin_film < 1.0f ? v3(fresnel_dielectric(hov, eta)) : v3(0.0f), F_film, e.thin_film);
 }
 
 // Fresnel of the specular layer (relative IOR eta_s), blended with the film's seen from the layer
-// above it (principled_specular_fresnel)
+// above it when the material has one (principled_specular_fresnel)
+template <bool EXT>
 GBPT_HD V3 specular_fresnel(const Material& m, float eta_s, float cos_i)
 {
     const float F = fresnel_dielectric(cos_i, eta_s);
-    if (m.thin_film == 0.0f) return v3(F);
-    return lerp(m.thin_film < 1.0f ? v3(F) : v3(0.0f), thin_film_fresnel(m, m.ior / eta_s, cos_i), m.thin_film);
+    if constexpr (!EXT) return v3(F);
+    else if (m.ext->thin_film == 0.0f) return v3(F);
+    else return lerp(m.ext->thin_film < 1.0f ? v3(F) : v3(0.0f), thin_film_fresnel(*m.ext, m.ior / eta_s, cos_i),
+                     m.ext->thin_film);
 }
 
 // The Oren-Nayar factor A + B max(0, cos(phi_i - phi_o)) sin(alpha) tan(beta) of the diffuse lobe
 // (oren_nayar_brdf_eval, src/Device/includes/BSDFs/OrenNayar.h:14-47), v and l in the unrotated
 // shading frame; the azimuth difference does not depend on the frame's tangent
-GBPT_HD float oren_nayar_shape(const Material& m, V3 v, V3 l)
+GBPT_HD float oren_nayar_shape(float sigma, V3 v, V3 l)
 {
     const float sin_i = sqrtf(1.0f - l.z * l.z);
     const float sin_o = sqrtf(1.0f - v.z * v.z);
@@ -644,10 +641,16 @@ GBPT_HD float oren_nayar_shape(const Material& m, V3 v, V3 l)
         sin_alpha = sin_i;
         tan_beta = sin_o / fabsf(v.z);
     }
-    return m.oren_a + m.oren_b * max_cos * sin_alpha * tan_beta;
+    // A and B from the facet-slope deviation (MaterialUtils::get_oren_nayar_AB,
+    // src/HostDeviceCommon/Material/MaterialUtils.h:18-23)
+    const float s2 = sigma * sigma;
+    const float A = 1.0f - s2 / (2.0f * (s2 + 0.33f));
+    const float B = 0.45f * s2 / (s2 + 0.09f);
+    return A + B * max_cos * sin_alpha * tan_beta;
 }
 
 // Glass lobe (Principled.h:359-558): reflection or refraction through a GGX interface.
+template <bool EXT>
 GBPT_HD V3 glass_eval(const Material& m, const Medium& md, bool height_correlated, V3 v, V3 l, int lobe, float& pdf)
 {
     pdf = 0.0f;
@@ -668,7 +671,9 @@ GBPT_HD V3 glass_eval(const Material& m, const Medium& md, bool height_correlate
     if (h.z < 0.0f) h = -h;
     const float hol = dot(l, h), hov = dot(v, h);
     if (hol * nol < 0.0f || hov * nov < 0.0f) return v3(0.0f);
-    const V3 F = glass_fresnel(m, hov, eta, md.eta_incident, rough);
+    V3 F;
+    if (EXT && m.ext->thin_film > 0.0f) F = glass_fresnel_film(*m.ext, hov, eta, md.eta_incident);
+    else F = v3(glass_fresnel(m, hov, eta, rough));
     const float p_reflect = luminance(F);
     if (reflecting)
     {
@@ -683,6 +688,13 @@ GBPT_HD V3 glass_eval(const Material& m, const Medium& md, bool height_correlate
     return c;
 }
 
+// the glass lobe's reflection probability with a film (out of line on the device)
+GBPT_HD_OUTLINE float glass_reflect_probability_film(const gbpt_principled_material& e, float hov, float eta,
+                                                     float eta_incident)
+{
+    return luminance(glass_fresnel_film(e, hov, eta, eta_incident));
+}
+
 template <typename Rng>
 GBPT_HD V3 glass_sample(const Material& m, const Medium& md, V3 v, Rng& rng, int& lobe)
 {
@@ -691,8 +703,10 @@ GBPT_HD V3 glass_sample(const Material& m, const Medium& md, V3 v, Rng& rng, int
     float ax, ay;
     ggx_alphas(rough, m.anisotropy, ax, ay);
     V3 h = ggx_sample_visible_normal(v, ax, ay, rng);
-    const V3 F = glass_fresnel(m, dot(v, h), eta, md.eta_incident, rough);
-    if (rng() < luminance(F))
+    const float hov = dot(v, h);
+    const float p_reflect = (m.ext && m.ext->thin_film > 0.0f) ? glass_reflect_probability_film(*m.ext, hov, eta, md.eta_incident)
+                                               : luminance(v3(glass_fresnel(m, hov, eta, rough)));
+    if (rng() < p_reflect)
     {
         lobe = GBPT_LOBE_GLASS_REFLECT;
         return reflect(v, h);
@@ -716,8 +730,11 @@ struct Query
     V3 view, ns, ng, light;
 };
 
-// f (without cosine) and pdf for light direction q.light, given the lobe it was sampled from.
-GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, const Query& q, int lobe, float& pdf)
+// f (without cosine) and pdf for light direction q.light, given the lobe it was sampled from;
+// EXT: the material uses an Oren-Nayar diffuse lobe or a thin film (a separate instantiation, so
+// that the common materials run code without those terms)
+template <bool EXT>
+GBPT_HD V3 eval_layers(const Material& m, const Medium& md, bool height_correlated, const Query& q, int lobe, float& pdf)
 {
     pdf = 0.0f;
     const bool outside = !md.inside;
@@ -779,7 +796,8 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
         {
             const float hol = clampf(1.0e-8f, 1.0f, dot(hr, lr));
             V3 F = fresnel_f82_tint(m.base, m.f82, m.f90, m.f90_exponent, hol);
-            if (m.thin_film > 0.0f) F = lerp(F, thin_film_fresnel(m, eta_in, hol), m.thin_film);
+            if constexpr (EXT)
+                if (m.ext->thin_film > 0.0f) F = lerp(F, thin_film_fresnel(*m.ext, eta_in, hol), m.ext->thin_film);
             c = ggx_reflection(metal_r[k], m.anisotropy, height_correlated, F, vr, lr, hr, ds, lobe_pdf);
         }
         color = color + c * metal_w[k] * throughput;
@@ -790,7 +808,7 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
     if (w.glass > 0.0f)
     {
         float lobe_pdf;
-        const V3 c = glass_eval(m, md, height_correlated, vr, lr, lobe, lobe_pdf);
+        const V3 c = glass_eval<EXT>(m, md, height_correlated, vr, lr, lobe, lobe_pdf);
         color = color + c * w.glass * throughput;
         pdf += lobe_pdf * p.glass;
     }
@@ -802,12 +820,12 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
         const float eta_s = specular_relative_ior(m, eta_in);
         float lobe_pdf;
         const Delta ds = delta_state(m, m.roughness, m.anisotropy, lobe);
-        V3 c = ggx_reflection(m.roughness, m.anisotropy, height_correlated, specular_fresnel(m, eta_s, dot(lr, hr)), vr,
-                              lr, hr, ds, lobe_pdf);
+        V3 c = ggx_reflection(m.roughness, m.anisotropy, height_correlated, specular_fresnel<EXT>(m, eta_s, dot(lr, hr)),
+                              vr, lr, hr, ds, lobe_pdf);
         c = c * lerp(v3(1.0f), m.specular_tint * m.specular_color, m.specular);
         glossy = glossy + c * w.specular * throughput;
         V3 att;
-        if (m.thin_film == 0.0f)
+        if (!EXT || m.ext->thin_film == 0.0f)
         {
             const float light_f = fresnel_dielectric(fabsf(lr.z), eta_s) * (1.0f - m.diffuse_transmission);
             const float view_f = fresnel_dielectric(fabsf(vr.z), eta_s);
@@ -815,8 +833,8 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
         }
         else
         {
-            const V3 light_f = specular_fresnel(m, eta_s, fabsf(lr.z)) * (1.0f - m.diffuse_transmission);
-            att = (1.0f - light_f) * (1.0f - specular_fresnel(m, eta_s, fabsf(vr.z)));
+            const V3 light_f = specular_fresnel<true>(m, eta_s, fabsf(lr.z)) * (1.0f - m.diffuse_transmission);
+            att = (1.0f - light_f) * (1.0f - specular_fresnel<true>(m, eta_s, fabsf(vr.z)));
         }
         att = att * specular_darkening(m, eta_s);
         throughput = throughput * lerp(v3(1.0f), att, m.specular);
@@ -825,7 +843,9 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
     const float diffuse_w = w.diffuse * (refracting ? 0.0f : 1.0f);
     if (diffuse_w > 0.0f && v.z > 0.0f && l.z > 0.0f)
     {
-        const float shape = m.oren_nayar ? oren_nayar_shape(m, v, l) : 1.0f;
+        float shape = 1.0f;
+        if constexpr (EXT)
+            if (m.ext->diffuse_lobe == GBPT_DIFFUSE_OREN_NAYAR) shape = oren_nayar_shape(m.ext->oren_nayar_sigma, v, l);
         glossy = glossy + m.base * kInvPi * shape * diffuse_w * throughput;
         pdf += l.z * kInvPi * p.diffuse;
     }
@@ -846,6 +866,19 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
     return color;
 }
 
+// the instantiation for materials with extension lobes, out of line on the device
+GBPT_HD_OUTLINE V3 eval_ext(const Material& m, const Medium& md, bool height_correlated, const Query& q, int lobe,
+                             float& pdf)
+{
+    return eval_layers<true>(m, md, height_correlated, q, lobe, pdf);
+}
+
+GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, const Query& q, int lobe, float& pdf)
+{
+    if (m.ext) return eval_ext(m, md, height_correlated, q, lobe, pdf);
+    return eval_layers<false>(m, md, height_correlated, q, lobe, pdf);
+}
+
 #ifdef __CUDACC__
 // The same evaluation as one out-of-line function per translation unit. Kernels that evaluate the
 // BSDF from several call sites (shading: the light sample, RIS candidates, BSDF-sampled light
@@ -854,10 +887,18 @@ GBPT_HD V3 eval(const Material& m, const Medium& md, bool height_correlated, con
 // shade kernel's top stall). Measured on the 1080p many-light ReSTIR frame: spatial reuse 5.23 ->
 // 3.66 ms, temporal 4.17 -> 3.51, shading 11.9 -> 10.4. The initial candidates' light loop keeps
 // the inlined eval (13.3 ms outlined against 10.4 inlined).
-static __device__ __noinline__ V3 eval_outlined(const Material& m, const Medium& md, bool height_correlated,
-                                                const Query& q, int lobe, float& pdf)
+// Materials with extension lobes go to eval_ext, its own out-of-line function: the choice is made
+// here, at the call site, so that neither copy calls the other (a call inside the evaluation, or
+// inside a kernel's candidate loop, cost 4-5% of a ReSTIR frame through the calling convention).
+static __device__ __noinline__ V3 eval_common(const Material& m, const Medium& md, bool height_correlated,
+                                              const Query& q, int lobe, float& pdf)
 {
-    return eval(m, md, height_correlated, q, lobe, pdf);
+    return eval_layers<false>(m, md, height_correlated, q, lobe, pdf);
+}
+__device__ __forceinline__ V3 eval_outlined(const Material& m, const Medium& md, bool height_correlated,
+                                            const Query& q, int lobe, float& pdf)
+{
+    return m.ext ? eval_ext(m, md, height_correlated, q, lobe, pdf) : eval_common(m, md, height_correlated, q, lobe, pdf);
 }
 #define GBPT_BSDF_EVAL_CALL eval_outlined
 #else

@@ -372,6 +372,68 @@ __device__ __forceinline__ bool initial_load(const SceneView& s, const RestirCon
     return true;
 }
 
+// the light candidates of a pixel; EXT: its material has extension lobes (the evaluation goes out
+// of line, in its own copy of the loop, so that the common materials' loop makes no call)
+template <bool EXT>
+__device__ __forceinline__ void initial_light_candidates(const SceneView& s, const RenderConst& rc, const RestirConst& k,
+                                                         const InitialPixel& px, bool hc, Pcg32& rng, Reservoir& r,
+                                                         int pixel)
+{
+    const Surface& su = px.su;
+    const float nl = (float)k.light_candidates, nb = (float)k.bsdf_candidates;
+    const int subset = k.presampled ? presampled_subset(k, pixel % rc.width, pixel / rc.width) : 0;
+    for (int c = 0; c < k.light_candidates; c++)
+    {
+        LightSample ls;
+        if (k.presampled)
+        {
+            // a light of the tile's presampled subset, with the pdf it was drawn with
+            const int e = subset * k.presample_size + rng.index(k.presample_size);
+            const float4 a = __ldg(k.presampled + 2 * e), b = __ldg(k.presampled + 2 * e + 1);
+            ls.point = xyz(a);
+            ls.triangle = __float_as_int(a.w);
+            ls.normal = xyz(b);
+            ls.pdf_area = b.w;
+            ls.emission = emission_of(s, ls.triangle);
+        }
+        else
+        {
+            // the reference first draws the envmap-or-light choice (sample_fresh_light_candidate,
+            // InitialCandidates.h:100; without an envmap always a light)
+            if (k.rng_mode == GBPT_RNG_REFERENCE) rng.next();
+            ls = sample_light(s, rc, rng);
+        }
+        V3 wi = ls.point - su.P;
+        const float dist = length(wi);
+        wi = wi / dist;
+        const float cosine = fmaxf(0.0f, dot(su.ns, wi));
+        float weight = 0.0f, p_hat = 0.0f;
+        if (cosine > 0.0f && ls.pdf_area > 0.0f)
+        {
+            bsdf::Query q;
+            q.view = su.view;
+            q.ns = su.ns;
+            q.ng = su.ng;
+            q.light = wi;
+            float bsdf_pdf;
+            const V3 f = EXT ? bsdf::eval_outlined(px.m, px.md, hc, q, GBPT_LOBE_NONE, bsdf_pdf)
+                             : bsdf::eval_layers<false>(px.m, px.md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
+            if (bsdf_pdf > 0.0f)
+            {
+                const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
+                // the reference's candidate carries ReSTIR_DI_evaluate_target_function's value
+                p_hat = k.rng_mode == GBPT_RNG_REFERENCE
+                            ? target_function(s, hc, su, px.m, ls.point, ls.triangle, 0, false)
+                            : luminance(f * ls.emission * dot(su.ns, wi) * (cos_l / (dist * dist)));
+                const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
+                const float mis = light_pdf == 0.0f ? 0.0f : light_pdf / (nl * light_pdf + nb * bsdf_pdf);
+                weight = mis * p_hat / ls.pdf_area;
+            }
+        }
+        add_candidate(r, ls.point, ls.triangle, 0, p_hat, weight, rng.next());
+    }
+}
+
 // phase 1: the light candidates, then BSDF candidate 0's direction (or the end when there is none)
 __global__ void __launch_bounds__(128, 3) initial_lights_kernel(SceneView s, RenderConst rc, RestirConst k, GBuffer gb,
                                                                 ReservoirBuf out, InitialState st, Queue rays,
@@ -387,58 +449,10 @@ __global__ void __launch_bounds__(128, 3) initial_lights_kernel(SceneView s, Ren
         Pcg32 rng = pass_stream(k, pixel, 1);
         if (live)
         {
-            const Surface& su = px.su;
-            const float nl = (float)k.light_candidates, nb = (float)k.bsdf_candidates;
-            const int subset = k.presampled ? presampled_subset(k, pixel % rc.width, pixel / rc.width) : 0;
-            for (int c = 0; c < k.light_candidates; c++)
-            {
-                LightSample ls;
-                if (k.presampled)
-                {
-                    // a light of the tile's presampled subset, with the pdf it was drawn with
-                    const int e = subset * k.presample_size + rng.index(k.presample_size);
-                    const float4 a = __ldg(k.presampled + 2 * e), b = __ldg(k.presampled + 2 * e + 1);
-                    ls.point = xyz(a);
-                    ls.triangle = __float_as_int(a.w);
-                    ls.normal = xyz(b);
-                    ls.pdf_area = b.w;
-                    ls.emission = emission_of(s, ls.triangle);
-                }
-                else
-                {
-                    // the reference first draws the envmap-or-light choice (sample_fresh_light_candidate,
-                    // InitialCandidates.h:100; without an envmap always a light)
-                    if (k.rng_mode == GBPT_RNG_REFERENCE) rng.next();
-                    ls = sample_light(s, rc, rng);
-                }
-                V3 wi = ls.point - su.P;
-                const float dist = length(wi);
-                wi = wi / dist;
-                const float cosine = fmaxf(0.0f, dot(su.ns, wi));
-                float weight = 0.0f, p_hat = 0.0f;
-                if (cosine > 0.0f && ls.pdf_area > 0.0f)
-                {
-                    bsdf::Query q;
-                    q.view = su.view;
-                    q.ns = su.ns;
-                    q.ng = su.ng;
-                    q.light = wi;
-                    float bsdf_pdf;
-                    const V3 f = bsdf::eval(px.m, px.md, hc, q, GBPT_LOBE_NONE, bsdf_pdf);
-                    if (bsdf_pdf > 0.0f)
-                    {
-                        const float cos_l = fmaxf(0.0f, dot(ls.normal, -wi));
-                        // the reference's candidate carries ReSTIR_DI_evaluate_target_function's value
-                        p_hat = k.rng_mode == GBPT_RNG_REFERENCE
-                                    ? target_function(s, hc, su, px.m, ls.point, ls.triangle, 0, false)
-                                    : luminance(f * ls.emission * dot(su.ns, wi) * (cos_l / (dist * dist)));
-                        const float light_pdf = area_to_solid_angle_pdf(ls.pdf_area, dist, cos_l);
-                        const float mis = light_pdf == 0.0f ? 0.0f : light_pdf / (nl * light_pdf + nb * bsdf_pdf);
-                        weight = mis * p_hat / ls.pdf_area;
-                    }
-                }
-                add_candidate(r, ls.point, ls.triangle, 0, p_hat, weight, rng.next());
-            }
+            if (px.m.ext)
+                initial_light_candidates<true>(s, rc, k, px, hc, rng, r, pixel);
+            else
+                initial_light_candidates<false>(s, rc, k, px, hc, rng, r, pixel);
         }
         if (!live)
         {

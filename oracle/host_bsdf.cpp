@@ -32,12 +32,14 @@ Medium medium(const float* q)
     return md;
 }
 
-Material material(const float* w)
+// The material keeps a pointer to its record (for its extension lobes): the record lives in the
+// caller's frame for as long as the material is used
+gbpt_principled_material record(const float* w)
 {
     gbpt_principled_material rec;
     static_assert(sizeof(gbpt_principled_material) == 64 * sizeof(float), "64-word material records");
     std::memcpy(&rec, w, sizeof(rec));
-    return load_material(rec);
+    return rec;
 }
 }  // namespace
 
@@ -51,7 +53,8 @@ void host_principled_eval_one(const float* mat, const float* q, float* out)
     qq.ng = v3(q[6], q[7], q[8]);
     qq.light = v3(q[9], q[10], q[11]);
     float pdf = 0.0f;
-    const V3 f = eval(material(mat), medium(q), false, qq, (int)q[15], pdf);
+    const gbpt_principled_material rec = record(mat);
+    const V3 f = eval(load_material(rec), medium(q), false, qq, (int)q[15], pdf);
     out[0] = f.x;
     out[1] = f.y;
     out[2] = f.z;
@@ -64,7 +67,8 @@ void host_principled_sample_one(const float* mat, const float* q, uint32_t seed,
     V3 dir = v3(0.0f, 0.0f, 0.0f);
     int lb = 0;
     float pdf = 0.0f;
-    const V3 f = sample(material(mat), medium(q), false, v3(q[0], q[1], q[2]), v3(q[3], q[4], q[5]),
+    const gbpt_principled_material rec = record(mat);
+    const V3 f = sample(load_material(rec), medium(q), false, v3(q[0], q[1], q[2]), v3(q[3], q[4], q[5]),
                         v3(q[6], q[7], q[8]), rng, dir, lb, pdf);
     out[0] = dir.x;
     out[1] = dir.y;
