@@ -5,8 +5,11 @@
 // render.cu). Their scratch (block partial sums, the normalised FP64 list and the two Vose queues)
 // lives in one file-scope __device__ array of fixed size, which every device that loads libgbpt
 // holds until the process exits. Host code cannot pass that array's name to a kernel: in host
-// code the name is only a host-side stand-in. Its device address is looked up once per device
-// with cudaGetSymbolAddress, with that device current, on the first call made on that device.
+// code the name is only a host-side stand-in. Its device address is looked up with
+// cudaGetSymbolAddress, with the device current, on the first call made in each CUDA context
+// (the address belongs to the context: after cudaDeviceReset, or in another context on the same
+// device, it is looked up again).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -30,8 +33,26 @@ static __device__ __align__(256) double g_alias_scratch[kScratchDoubles];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double* g_scratch_addr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};  // the context each cached address belongs to
 
-// Device address of g_alias_scratch on the current device (looked up once per device).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+
+// cuCtxGetCurrent through the runtime's driver entry point (no link against the driver library)
+CtxGetCurrentFn ctx_get_current()
+{
+    static const CtxGetCurrentFn fn = []() -> CtxGetCurrentFn {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(p);
+    }();
+    return fn;
+}
+
+// Device address of g_alias_scratch in the current context (looked up again when the context of
+// the current device is not the one the cached address was taken in).
 gbpt_status scratch_for_current_device(double** out)
 {
     int dev = 0;
@@ -40,13 +61,25 @@ gbpt_status scratch_for_current_device(double** out)
     if (dev < 0 || dev >= kMaxDevices)
         return gbpt::set_error(GBPT_ERROR_UNSUPPORTED, "device ordinal " + std::to_string(dev) + " is beyond the " +
                                                            std::to_string(kMaxDevices) + " devices this entry point tracks");
+    const CtxGetCurrentFn get_ctx = ctx_get_current();
+    if (!get_ctx) return gbpt::set_error(GBPT_ERROR_UNSUPPORTED, "cuCtxGetCurrent is unavailable");
+    CUcontext ctx = nullptr;
+    if (get_ctx(&ctx) != CUDA_SUCCESS) return gbpt::set_error(GBPT_ERROR_CUDA, "cuCtxGetCurrent failed");
+    if (!ctx)
+    {
+        // no context current on this thread yet: the runtime makes the device's primary one current
+        e = cudaFree(nullptr);
+        if (e != cudaSuccess) return gbpt::cuda_error(e, "context initialisation");
+        if (get_ctx(&ctx) != CUDA_SUCCESS || !ctx) return gbpt::set_error(GBPT_ERROR_CUDA, "no current CUDA context");
+    }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev])
+    if (!g_scratch_addr[dev] || g_scratch_ctx[dev] != ctx)
     {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_alias_scratch);
         if (e != cudaSuccess) return gbpt::cuda_error(e, "cudaGetSymbolAddress of the alias-table scratch");
         g_scratch_addr[dev] = static_cast<double*>(p);
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_addr[dev];
     return GBPT_OK;

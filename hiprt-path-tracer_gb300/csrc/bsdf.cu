@@ -1,5 +1,5 @@
 // Batched principled-BSDF entry points (declared in include/gbpt_bsdf.h): one thread per query,
-// materials gathered by index, queries read as four 16-byte words.
+// materials gathered by index, queries read as five 16-byte words.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -24,7 +24,7 @@ struct LoadedQuery
 __device__ __forceinline__ LoadedQuery load_query(const gbpt_bsdf_query* qs, int64_t i)
 {
     const float4* p = reinterpret_cast<const float4*>(qs + i);
-    const float4 a = p[0], b = p[1], c = p[2], d = p[3];
+    const float4 a = p[0], b = p[1], c = p[2], d = p[3], e = p[4];
     LoadedQuery r;
     r.q.view = v3(a.x, a.y, a.z);
     r.q.ns = v3(a.w, b.x, b.y);
@@ -34,6 +34,7 @@ __device__ __forceinline__ LoadedQuery load_query(const gbpt_bsdf_query* qs, int
     r.md.eta_outgoing = d.y;
     r.md.inside = __float_as_int(d.z) != 0;
     r.lobe = __float_as_int(d.w);
+    r.md.wavelength = fabsf(e.x);
     return r;
 }
 

@@ -774,6 +774,7 @@ gbpt_principled_material cpu_material_defaults()
     m.thin_film_ior = 1.3f;
     m.thin_film_thickness = 500.0f;
     m.thin_film_base_ior_override = 1.0f;
+    m.dispersion_abbe_number = 20.0f;
     return m;
 }
 

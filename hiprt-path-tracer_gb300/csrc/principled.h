@@ -2,7 +2,7 @@
 // that the CPU tests compile (tests/native/bsdf_emu.cpp).
 //
 // Behaviour follows the reference's principled BSDF with energy compensation, microfacet
-// regularization, dispersion and sheen switched off
+// regularization and sheen switched off
 // (src/Device/includes/BSDFs/Principled.h:1515-1941 and the lobes it calls):
 //   - lobe weights and sampling probabilities: Principled.h:1515-1618;
 //   - layering (coat over sheen over metal / glass / glossy base / diffuse transmission, with the
@@ -15,6 +15,9 @@
 //     src/Device/includes/Fresnel.h:41-175; thin-film interference (Belcour and Barla 2017):
 //     src/Device/includes/BSDFs/ThinFilm.h:11-226, blended into the metal (Principled.h:143-146),
 //     specular (:215-240, 1363-1382) and glass (:462-483, 663-684, 758-785) Fresnel terms;
+//   - dispersion: the glass lobe's IORs at the path's wavelength (Principled.h:375-380, 576-581,
+//     729-734; Dispersion.h:485-499) and the wavelength's RGB weight (Dispersion.h:424-458);
+//   - the Oren-Nayar diffuse lobe (OrenNayar.h:14-63);
 //   - frames: Frisvad/Max ONB and the rotated ONB of anisotropy: src/Device/includes/ONB.h;
 //   - delta-lobe handling (a perfectly smooth lobe contributes only when the direction was
 //     sampled from a lobe with the same mirror peak): MaterialUtils.h:143-177, Microfacet.h:90-120.
@@ -77,6 +80,13 @@ struct Material
     const gbpt_principled_material* ext;
 };
 
+// a glass lobe whose IOR depends on the path's wavelength (the condition under which the reference
+// samples one, Intersect.h:259 and RayVolumeState.h:50)
+GBPT_HD bool is_dispersive(const gbpt_principled_material& s)
+{
+    return s.dispersion_scale > 0.0f && s.specular_transmission > 0.0f;
+}
+
 GBPT_HD Material load_material(const gbpt_principled_material& s)
 {
     Material m;
@@ -107,7 +117,7 @@ GBPT_HD Material load_material(const gbpt_principled_material& s)
     m.transmission = s.specular_transmission;
     m.diffuse_transmission = s.diffuse_transmission;
     m.thin_walled = s.thin_walled != 0;
-    m.ext = (s.diffuse_lobe == GBPT_DIFFUSE_OREN_NAYAR || s.thin_film > 0.0f) ? &s : nullptr;
+    m.ext = (s.diffuse_lobe == GBPT_DIFFUSE_OREN_NAYAR || s.thin_film > 0.0f || is_dispersive(s)) ? &s : nullptr;
     return m;
 }
 
@@ -123,6 +133,7 @@ struct Medium
     bool inside;
     bool absorbing = false;
     V3 beer = V3{1.0f, 1.0f, 1.0f};
+    float wavelength = 0.0f;  // the path's sampled wavelength (nm) for dispersion; 0: none yet
 };
 
 enum class Delta
@@ -580,10 +591,55 @@ GBPT_HD float thin_walled_roughness(bool thin, float roughness, float eta)
     return clampf(0.0f, 1.0f, r / 1.39f);
 }
 
-// relative IOR across the glass interface, kept away from 1 (a null half vector otherwise)
-GBPT_HD float glass_eta(const Medium& md)
+// IOR at 'wavelength' (nm) of a medium whose IOR at 587.6 nm is base_ior, from the Abbe number
+// scaled by 1 / scale (Cauchy's two-term fit through the Fraunhofer F and C lines, as OpenPBR
+// specifies; compute_dispersion_ior, src/Device/includes/Dispersion.h:485-499)
+GBPT_HD float dispersion_ior(float abbe_number, float scale, float base_ior, float wavelength)
 {
-    float eta = md.eta_outgoing / md.eta_incident;
+    if (scale == 0.0f) return base_ior;
+    constexpr float kD2 = 334777.96f;                  // 587.6^2
+    constexpr float kFC = 0.00000191038851931481f;     // 486.1^-2 - 656.3^-2
+    const float abbe = abbe_number / scale;
+    const float B = (base_ior - 1.0f) / (abbe * kFC);
+    const float A = base_ior - B / kD2;
+    return A + B / (wavelength * wavelength);
+}
+
+// RGB weight of a wavelength (nm, in [360, 830]) for the path's colour filter, averaging (1, 1, 1)
+// over that range: the reference's closed-form fit of its CIE-based conversion
+// (wavelength_to_RGB_fit, src/Device/includes/Dispersion.h:424-458, the default
+// WavelengthToRGBMethod); its coefficients are kept as the reference has them so that dispersive
+// paths carry the same colours.
+GBPT_HD V3 wavelength_rgb(float wl)
+{
+    V3 c;
+    if (wl < 463.0f)
+        c.x = -1.2776028240727566e-01f / (1.0f + expf((wl - 4.2680623367293401e+02f) / 8.2197460736637176e+00f)) +
+              -1.3925673552505122e-11f * expf((wl - 45.0f) / 1.8175459086411596e+01f) + 1.2898689750552100e-01f;
+    else if (wl > 553.0f)
+        c.x = 1.7963649137825513e+01f * (1.0f / 2.6577826611702449e+01f) *
+                  expf(-0.5f * sq((wl - 6.0625724092824566e+02f) * (1.0f / 2.6577826611702449e+01f))) +
+              2.5574660155104657e-03f;
+    else
+        c.x = 0.0f;
+    c.y = 3.4962267376163049e+02f * expf(-0.5f * sq((wl - 5.4209217455705152e+02f) / -2.9598170255834638e+01f)) / wl;
+    c.z = expf(3.2987659944421112e+03f + (-2.0975839709372405e+05f / wl) - 4.6368268395094020e+02f * logf(wl));
+    return c * 10.0f;
+}
+
+// relative IOR across the glass interface, kept away from 1 (a null half vector otherwise); both
+// sides' IORs taken at the path's wavelength for a dispersive material. eta_i: the incident side's
+// IOR (what a film on the glass sees).
+GBPT_HD float glass_eta(const Material& m, const Medium& md, float& eta_i)
+{
+    eta_i = md.eta_incident;
+    float eta_t = md.eta_outgoing;
+    if (m.ext && m.ext->dispersion_scale > 0.0f && md.wavelength > 0.0f)
+    {
+        eta_i = dispersion_ior(m.ext->dispersion_abbe_number, m.ext->dispersion_scale, eta_i, md.wavelength);
+        eta_t = dispersion_ior(m.ext->dispersion_abbe_number, m.ext->dispersion_scale, eta_t, md.wavelength);
+    }
+    float eta = eta_t / eta_i;
     if (fabsf(eta - 1.0f) < 1.0e-5f) eta = 1.0f + 1.0e-5f;
     return eta;
 }
@@ -657,7 +713,8 @@ GBPT_HD V3 glass_eval(const Material& m, const Medium& md, bool height_correlate
     const float nov = v.z, nol = l.z;
     if (fabsf(nol) < 1.0e-8f) return v3(0.0f);
     const bool reflecting = nol * nov > 0.0f;
-    const float eta = glass_eta(md);
+    float eta_i;
+    const float eta = glass_eta(m, md, eta_i);
     const float rough = thin_walled_roughness(m.thin_walled, m.roughness, eta);
     V3 h;
     if (rough <= kRoughnessClamp)
@@ -672,7 +729,7 @@ GBPT_HD V3 glass_eval(const Material& m, const Medium& md, bool height_correlate
     const float hol = dot(l, h), hov = dot(v, h);
     if (hol * nol < 0.0f || hov * nov < 0.0f) return v3(0.0f);
     V3 F;
-    if (EXT && m.ext->thin_film > 0.0f) F = glass_fresnel_film(*m.ext, hov, eta, md.eta_incident);
+    if (EXT && m.ext->thin_film > 0.0f) F = glass_fresnel_film(*m.ext, hov, eta, eta_i);
     else F = v3(glass_fresnel(m, hov, eta, rough));
     const float p_reflect = luminance(F);
     if (reflecting)
@@ -698,13 +755,14 @@ GBPT_HD_OUTLINE float glass_reflect_probability_film(const gbpt_principled_mater
 template <typename Rng>
 GBPT_HD V3 glass_sample(const Material& m, const Medium& md, V3 v, Rng& rng, int& lobe)
 {
-    const float eta = glass_eta(md);
+    float eta_i;
+    const float eta = glass_eta(m, md, eta_i);
     const float rough = thin_walled_roughness(m.thin_walled, m.roughness, eta);
     float ax, ay;
     ggx_alphas(rough, m.anisotropy, ax, ay);
     V3 h = ggx_sample_visible_normal(v, ax, ay, rng);
     const float hov = dot(v, h);
-    const float p_reflect = (m.ext && m.ext->thin_film > 0.0f) ? glass_reflect_probability_film(*m.ext, hov, eta, md.eta_incident)
+    const float p_reflect = (m.ext && m.ext->thin_film > 0.0f) ? glass_reflect_probability_film(*m.ext, hov, eta, eta_i)
                                                : luminance(v3(glass_fresnel(m, hov, eta, rough)));
     if (rng() < p_reflect)
     {

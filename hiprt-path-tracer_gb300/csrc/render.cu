@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(256) camera_kernel(RenderConst rc, PathBuffers
             VolumeStack v;
             v.reset();
             v.store(pb.vol_stack, pb.vol_state, slot);
+            pb.wavelength[slot] = 0.0f;
         }
         store_rng(pb.rng + slot, rng);
     }
@@ -144,6 +145,22 @@ __global__ void __launch_bounds__(128) trace_queue_kernel(const uint4* __restric
 // they are when no envmap is sampled. The ReSTIR DI bounce keeps it too: its reservoirs hold
 // emissive triangles only.
 // ---------------------------------------------------------------------------------------------
+// The path's wavelength at a principled hit: drawn from the path's generator when the hit material
+// is dispersive and the path has none yet (the reference draws it right after the hit,
+// Intersect.h:259-267, and at the camera hit in reconstruct_first_hit, RayVolumeState.h:50-58,
+// uniformly in [360, 830] nm, Dispersion.h:469-474), negative until its colour filter is applied.
+__device__ __forceinline__ float path_wavelength(const PathBuffers& pb, int slot, const gbpt_principled_material& rec,
+                                                 Pcg32& rng)
+{
+    float wl = pb.wavelength[slot];
+    if (wl == 0.0f && bsdf::is_dispersive(rec))
+    {
+        wl = -(rng.next() * 470.0f + 360.0f);
+        pb.wavelength[slot] = wl;
+    }
+    return wl;
+}
+
 template <bool PRINCIPLED>
 __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0, PathBuffers pb, Queue in, Queue envq,
                                                   unsigned long long* stats, const BatchJob* __restrict__ jobs)
@@ -201,7 +218,8 @@ __global__ void __launch_bounds__(128) env_kernel(SceneView s0, RenderConst rc0,
                 VolumeStack vol;
                 vol.load(pb.vol_stack, pb.vol_state, slot);
                 volume_hit(vol, s.pmats[mat], mat, hit.x);
-                const bsdf::Medium md = volume_medium(s, vol);
+                bsdf::Medium md = volume_medium(s, vol);
+                md.wavelength = fabsf(path_wavelength(pb, slot, s.pmats[mat], rng));
                 ed = env_direct(
                     s.env, rng, ns, tp, can_light_sample(m),
                     [&](V3 wi, float& pdf) {
@@ -504,14 +522,19 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
             {
                 // under GBPT_RNG_REFERENCE the camera hit shades with the material as the
                 // reference's G-buffer re-packed it (CameraRays.h:183, Megakernel.h:72)
-                const bsdf::Material m = bsdf::load_material(
-                    (rc.rng_mode == GBPT_RNG_REFERENCE && bounce == 0 && s.pmats_camera) ? s.pmats_camera[mat] : s.pmats[mat]);
+                const gbpt_principled_material& rec =
+                    (rc.rng_mode == GBPT_RNG_REFERENCE && bounce == 0 && s.pmats_camera) ? s.pmats_camera[mat] : s.pmats[mat];
+                const bsdf::Material m = bsdf::load_material(rec);
                 const bool hc = rc.ggx_height_correlated != 0;
                 // volume state: the hit pushes its material on the path's nested-dielectric stack
                 // (at the camera hit the stack holds only the air, as reconstruct_first_hit rebuilds it)
                 vol.load(pb.vol_stack, pb.vol_state, slot);
                 volume_hit(vol, s.pmats[mat], mat, hit.x);
-                const bsdf::Medium md = volume_medium(s, vol);
+                bsdf::Medium md = volume_medium(s, vol);
+                // the path's wavelength: drawn at its first dispersive hit, before the vertex's other
+                // draws (as the reference draws it right after the hit)
+                float wavelength = path_wavelength(pb, slot, rec, rng);
+                md.wavelength = fabsf(wavelength);
                 // guided vertex (materials without delta lobes or transmission): the continuation is
                 // drawn from the learned mixture / the BSDF and, outside ReSTIR's bounce 0, doubles as
                 // the BSDF technique of next-event estimation (MIS pdf alpha q + (1 - alpha) p)
@@ -730,6 +753,14 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s0, RenderConst rc
                             want_record = rec_vertex;
                             rec_tp = tp;
                             rec_dir = wi;
+                            // a dispersive vertex filters the path by its wavelength's colour, once
+                            // (get_dispersion_ray_color, Dispersion.h:512-525; PathTracing.h:51-52)
+                            if (wavelength < 0.0f && rec.dispersion_scale > 0.0f)
+                            {
+                                t2 = t2 * bsdf::wavelength_rgb(-wavelength);
+                                wavelength = -wavelength;
+                                pb.wavelength[slot] = wavelength;
+                            }
                             t2 = t2 * atten;
                             t2 = v3(fmaxf(t2.x, 1.0e-5f), fmaxf(t2.y, 1.0e-5f), fmaxf(t2.z, 1.0e-5f));
                             tp = t2;
@@ -1118,6 +1149,7 @@ __global__ void __launch_bounds__(256) camera_batch_kernel(const BatchJob* __res
             VolumeStack v;
             v.reset();
             v.store(pb.vol_stack, pb.vol_state, slot);
+            pb.wavelength[slot] = 0.0f;
         }
             pb.job[slot] = job;
             store_rng(pb.rng + slot, rng);

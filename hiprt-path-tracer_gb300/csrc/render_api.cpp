@@ -273,6 +273,7 @@ gbpt_principled_material packed_material(gbpt_principled_material m)
     unpack_color(m.absorption_color);
     m.specular_transmission = unpack_byte(m.specular_transmission);
     m.thin_film = unpack_byte(m.thin_film);
+    m.dispersion_scale = unpack_byte(m.dispersion_scale);
     m.thin_film_hue_shift = unpack_byte(m.thin_film_hue_shift);
     // the packed record's setter takes a bool (set_thin_film_base_ior_override,
     // MaterialPacked.h:347): any non-zero override IOR arrives as 1
@@ -768,6 +769,7 @@ void alloc_paths(DevMem& M, int64_t cap, bool principled, bool batched, gbpt::Pa
     pb.bsdf_entry = M.alloc<int32_t>(cap);
     pb.vol_stack = principled ? M.alloc<uint4>(cap) : nullptr;
     pb.vol_state = principled ? M.alloc<int4>(cap) : nullptr;
+    pb.wavelength = principled ? M.alloc<float>(cap) : nullptr;
     pb.job = batched ? M.alloc<int32_t>(cap) : nullptr;
     pb.ris = M.alloc<float4>(cap);
     q[0] = make_queue(M, cap, true, false);

@@ -93,6 +93,8 @@ struct PathBuffers
     int32_t* bsdf_entry;    // queue index of the slot's BSDF-light ray this bounce, -1 if none
     uint4* vol_stack;       // principled paths: the nested-dielectric stack (volume.h), 4 entries
     int4* vol_state;        // its incident / outgoing materials, position | inside << 8, distance
+    float* wavelength;      // principled paths: the wavelength (nm) drawn at the first dispersive
+                            // hit, negative until its colour filter is applied; 0: none yet
     int32_t* job;           // batched rendering: the job of each slot (null for a single renderer)
     float4* ris;            // RIS vertex: throughput before the continuation (rgb) and the light
                             // candidates' weight sum (w); w = -0.5: RIS without light candidates,

@@ -1,7 +1,8 @@
 """Principled BSDF entry points of libgbpt (include/gbpt_bsdf.h) over torch device tensors.
 
-Material records are built with gbpt.materials; queries are (n, 16) float32 rows in the
-gbpt_bsdf_query layout (inside and incident_lobe stored as int32 bit patterns).
+Material records are built with gbpt.materials; queries are (n, 20) float32 rows in the
+gbpt_bsdf_query layout (inside and incident_lobe stored as int32 bit patterns, then the path's
+wavelength and three reserved words).
 """
 from __future__ import annotations
 
@@ -31,6 +32,15 @@ LOBES = {"none": 0, "coat": 2, "metal1": 4, "metal2": 8, "specular": 16, "glass_
          "diffuse": 128, "diffuse_transmission": 256}
 
 
+QUERY_WORDS = 20  # sizeof(gbpt_bsdf_query) / 4
+
+
+def _check_queries(queries):
+    if queries.dim() != 2 or queries.shape[1] != QUERY_WORDS:
+        raise ValueError(f"queries must be (n, {QUERY_WORDS}) rows in the gbpt_bsdf_query layout, got "
+                         f"{tuple(queries.shape)}")
+
+
 def _load():
     lib = _lib.load()
     if not getattr(lib, "_bsdf_sigs", False):
@@ -58,6 +68,7 @@ def eval(materials, material_index, queries, height_correlated=False, stream=Non
     """f (rgb) and pdf per query -> (n, 4) float32 tensor on the queries' device."""
     import torch
     lib = _load()
+    _check_queries(queries)
     n = queries.shape[0]
     out = torch.empty((n, 4), dtype=torch.float32, device=queries.device)
     _lib.check(lib.gbpt_bsdf_eval(materials.data_ptr(), materials.shape[0], material_index.data_ptr(),
@@ -69,6 +80,7 @@ def eval(materials, material_index, queries, height_correlated=False, stream=Non
 def pdf(materials, material_index, queries, height_correlated=False, stream=None):
     import torch
     lib = _load()
+    _check_queries(queries)
     n = queries.shape[0]
     out = torch.empty(n, dtype=torch.float32, device=queries.device)
     _lib.check(lib.gbpt_bsdf_pdf(materials.data_ptr(), materials.shape[0], material_index.data_ptr(),
@@ -81,6 +93,7 @@ def sample(materials, material_index, queries, seeds, height_correlated=False, s
     """-> (out (n, 8): direction, f, pdf, 0; lobe (n,) int32; rng state (n,) int32 bits)."""
     import torch
     lib = _load()
+    _check_queries(queries)
     n = queries.shape[0]
     out = torch.empty((n, 8), dtype=torch.float32, device=queries.device)
     lobe = torch.empty(n, dtype=torch.int32, device=queries.device)

@@ -26,6 +26,7 @@ FIELDS = [
     ("thin_walled", 44, 1), ("diffuse_lobe", 45, 1), ("oren_nayar_sigma", 46, 1),
     ("thin_film", 47, 1), ("thin_film_ior", 48, 1), ("thin_film_thickness", 49, 1), ("thin_film_kappa_3", 50, 1),
     ("thin_film_hue_shift", 51, 1), ("thin_film_base_ior_override", 52, 1), ("thin_film_do_ior_override", 53, 1),
+    ("dispersion_scale", 54, 1), ("dispersion_abbe_number", 55, 1),
 ]
 INT_FIELDS = ("thin_walled", "diffuse_lobe", "thin_film_do_ior_override")
 DIFFUSE_LAMBERTIAN, DIFFUSE_OREN_NAYAR = 0, 1  # GBPT_DIFFUSE_*
@@ -43,6 +44,7 @@ DEFAULTS = {
     "diffuse_lobe": DIFFUSE_LAMBERTIAN, "oren_nayar_sigma": 0.34906585039886591538,  # 20 degrees
     "thin_film": 0.0, "thin_film_ior": 1.3, "thin_film_thickness": 500.0, "thin_film_kappa_3": 0.0,
     "thin_film_hue_shift": 0.0, "thin_film_base_ior_override": 1.0, "thin_film_do_ior_override": 0,
+    "dispersion_scale": 0.0, "dispersion_abbe_number": 20.0,
 }
 
 

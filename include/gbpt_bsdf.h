@@ -7,7 +7,7 @@
  * sheen, two metal lobes, specular over diffuse, glass and diffuse transmission, blended by the
  * same lobe weights and sampled with the same lobe probabilities.
  * Built without: energy compensation (it needs the reference's precomputed directional-albedo
- * tables), microfacet regularization (biased), dispersion and the sheen
+ * tables), microfacet regularization (biased) and the sheen
  * lobe: the entry points below treat 'sheen' as 0, and scene creation rejects materials with
  * sheen > 0 (GBPT_ERROR_UNSUPPORTED). A query whose material index is out of range returns zeros.
  * See gbpt.h for status codes; all pointers below are device pointers.
@@ -68,7 +68,12 @@ typedef struct gbpt_principled_material {
     float thin_film_hue_shift;     /* in turns (degrees / 360, as the reference's unpacked material) [0] */
     float thin_film_base_ior_override; /* the base's IOR under the film, with the override [1] */
     int32_t thin_film_do_ior_override; /* 0: the base is the material's own IOR, kappa 0 */
-    int32_t reserved[10];
+    /* dispersion of the glass lobe (the reference's compute_dispersion_ior,
+     * src/Device/includes/Dispersion.h:485-499, OpenPBR's Cauchy fit from the Abbe number): the
+     * glass lobe's IORs become those at the path's sampled wavelength when dispersion_scale > 0 */
+    float dispersion_scale;        /* [0] */
+    float dispersion_abbe_number;  /* [20] */
+    int32_t reserved[8];
 } gbpt_principled_material;
 
 /* The diffuse lobe of the principled BSDF's glossy base (gbpt_principled_material.diffuse_lobe):
@@ -95,7 +100,7 @@ enum {
 
 /* One BSDF query: world-space unit directions (view points away from the surface), the media
  * on both sides (IOR of the medium the ray travels in and of the one behind the surface; 1 =
- * air) and whether the ray is inside the object. Mirrors BSDFContext
+ * air), whether the ray is inside the object and the path's wavelength. Mirrors BSDFContext
  * (src/Device/includes/BSDFs/BSDFContext.h:13-54) with RayVolumeState reduced to those IORs. */
 typedef struct gbpt_bsdf_query {
     float view[3];
@@ -106,6 +111,9 @@ typedef struct gbpt_bsdf_query {
     float eta_outgoing;
     int32_t inside;
     int32_t incident_lobe;      /* GBPT_LOBE_* the light direction came from (eval/pdf) */
+    float wavelength;           /* the path's sampled wavelength in nm (its magnitude; 0: none),
+                                   for materials with dispersion (RayVolumeState::sampled_wavelength) */
+    int32_t reserved[3];
 } gbpt_bsdf_query;
 
 typedef struct gbpt_bsdf_options {

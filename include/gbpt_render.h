@@ -136,8 +136,9 @@ GBPT_API gbpt_status gbpt_gltf_destroy(gbpt_gltf* g);
  * device pointers owned by the caller.
  * Limits: n <= GBPT_ALIAS_NOALLOC_MAX_EMITTERS, else GBPT_ERROR_INVALID_ARG. Its scratch is one
  * fixed 2 MiB device array inside libgbpt that every device which loads the library holds until
- * exit. The first call on a device looks up that array's device address (with the device current);
- * make that first call before any stream capture. All calls share the one array: two calls that
+ * exit. The first call in each CUDA context looks up that array's device address (with the device
+ * current; again after cudaDeviceReset or in another context): make that first call before any
+ * stream capture. All calls share the one array: two calls that
  * overlap on the GPU (different streams, or different host threads) race and must be serialised
  * by the caller. Asynchronous on 'stream'. */
 GBPT_API gbpt_status gbpt_alias_table_build_noalloc(const float* power, int32_t n, float* probas, int32_t* alias,

@@ -83,7 +83,8 @@ DeviceUnpackedEffectiveMaterial unpack(const float* w)
     int32_t tf_override;
     std::memcpy(&tf_override, w + 53, 4);
     m.thin_film_do_ior_override = tf_override != 0;
-    m.dispersion_scale = 0.0f;
+    m.dispersion_scale = w[54];
+    m.dispersion_abbe_number = w[55];
     return m;
 }
 
@@ -98,7 +99,7 @@ struct Ctx
     RayVolumeState vs;
     // absorption: the colour of the material slot the ray travels in (Beer-Lambert when leaving
     // a volume, Principled.h:332-357); the golden materials use white (no absorption)
-    Ctx(const float* q, const DeviceUnpackedEffectiveMaterial& m)
+    Ctx(const float* q, const DeviceUnpackedEffectiveMaterial& m, float wavelength = 0.0f)
     {
         iors[0] = q[12];
         iors[1] = q[13];
@@ -111,7 +112,7 @@ struct Ctx
         vs.incident_mat_index = q[12] == 1.0f ? NestedDielectricsInteriorStack::MAX_MATERIAL_INDEX : 0;
         vs.outgoing_mat_index = q[13] == 1.0f ? NestedDielectricsInteriorStack::MAX_MATERIAL_INDEX : 1;
         vs.inside_material = q[14] != 0.0f;
-        vs.sampled_wavelength = 0.0f;
+        vs.sampled_wavelength = wavelength;
         // a NaN caught by the BSDF's CPU sanity check is zeroed rather than written to the
         // (absent) frame buffer
         rd.render_settings.display_NaNs = false;
@@ -120,10 +121,10 @@ struct Ctx
 
 float3 f3(const float* p) { return make_float3(p[0], p[1], p[2]); }
 
-void eval_query(const float* mat, const float* q, float* out)
+void eval_query(const float* mat, const float* q, float* out, float wavelength = 0.0f)
 {
     DeviceUnpackedEffectiveMaterial m = unpack(mat);
-    Ctx c(q, m);
+    Ctx c(q, m, wavelength);
     BSDFIncidentLightInfo info = (BSDFIncidentLightInfo)(int)q[15];
     BSDFContext ctx(f3(q), f3(q + 3), f3(q + 6), f3(q + 9), info, c.vs, false, m, 0, 0.0f);
     float pdf = 0.0f;
@@ -134,10 +135,11 @@ void eval_query(const float* mat, const float* q, float* out)
     out[3] = pdf;
 }
 
-void sample_query(const float* mat, const float* q, uint32_t seed, float* o, int32_t* lobe, uint32_t* rng_after)
+void sample_query(const float* mat, const float* q, uint32_t seed, float* o, int32_t* lobe, uint32_t* rng_after,
+                  float wavelength = 0.0f)
 {
     DeviceUnpackedEffectiveMaterial m = unpack(mat);
-    Ctx c(q, m);
+    Ctx c(q, m, wavelength);
     BSDFIncidentLightInfo info = BSDFIncidentLightInfo::NO_INFO;
     BSDFContext ctx(f3(q), f3(q + 3), f3(q + 6), make_float3(0.0f, 0.0f, 0.0f), info, c.vs, false, m, 0, 0.0f);
     Xorshift32Generator rng(seed);
@@ -163,21 +165,25 @@ extern "C" {
 // inline reference functions must not bind to the default build's)
 #pragma GCC visibility push(default)
 
-/* out: 4 floats per query (rgb, pdf) */
-void ref_principled_eval(const float* mats, const int32_t* mat_index, const float* queries, int64_t n, float* out)
+/* out: 4 floats per query (rgb, pdf). wavelengths (may be NULL): the path's sampled wavelength
+ * per query (RayVolumeState::sampled_wavelength), for dispersive materials. */
+void ref_principled_eval(const float* mats, const int32_t* mat_index, const float* queries, const float* wavelengths,
+                         int64_t n, float* out)
 {
 #pragma omp parallel for schedule(dynamic, 256)
-    for (int64_t i = 0; i < n; i++) eval_query(mats + 64 * (int64_t)mat_index[i], queries + 16 * i, out + 4 * i);
+    for (int64_t i = 0; i < n; i++)
+        eval_query(mats + 64 * (int64_t)mat_index[i], queries + 16 * i, out + 4 * i, wavelengths ? wavelengths[i] : 0.0f);
 }
 
-void ref_principled_pdf(const float* mats, const int32_t* mat_index, const float* queries, int64_t n, float* out)
+void ref_principled_pdf(const float* mats, const int32_t* mat_index, const float* queries, const float* wavelengths,
+                        int64_t n, float* out)
 {
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++)
     {
         const float* q = queries + 16 * i;
         DeviceUnpackedEffectiveMaterial m = unpack(mats + 64 * (int64_t)mat_index[i]);
-        Ctx c(q, m);
+        Ctx c(q, m, wavelengths ? wavelengths[i] : 0.0f);
         BSDFIncidentLightInfo info = (BSDFIncidentLightInfo)(int)q[15];
         BSDFContext ctx(f3(q), f3(q + 3), f3(q + 6), f3(q + 9), info, c.vs, false, m, 0, 0.0f);
         out[i] = principled_bsdf_pdf(c.rd, ctx);
@@ -187,12 +193,13 @@ void ref_principled_pdf(const float* mats, const int32_t* mat_index, const float
 /* Samples with a Xorshift32 generator seeded by seeds[i]. out: 8 floats per query
  * (direction xyz, rgb, pdf, 0); info_out = the lobe the direction was sampled from;
  * rng_out = generator state after sampling (counts the draws). */
-void ref_principled_sample(const float* mats, const int32_t* mat_index, const float* queries, const uint32_t* seeds,
-                           int64_t n, float* out, int32_t* info_out, uint32_t* rng_out)
+void ref_principled_sample(const float* mats, const int32_t* mat_index, const float* queries, const float* wavelengths,
+                           const uint32_t* seeds, int64_t n, float* out, int32_t* info_out, uint32_t* rng_out)
 {
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; i++)
-        sample_query(mats + 64 * (int64_t)mat_index[i], queries + 16 * i, seeds[i], out + 8 * i, info_out + i, rng_out + i);
+        sample_query(mats + 64 * (int64_t)mat_index[i], queries + 16 * i, seeds[i], out + 8 * i, info_out + i, rng_out + i,
+                     wavelengths ? wavelengths[i] : 0.0f);
 }
 
 /* Single-query forms with the same layouts, handed to the path-tracing oracle (pt_oracle.cpp) as

@@ -115,6 +115,8 @@ CPUMaterial cpu_material(const float* w)
     int32_t tf_override;
     std::memcpy(&tf_override, w + 53, 4);
     m.thin_film_do_ior_override = tf_override != 0;
+    m.dispersion_scale = w[54];
+    m.dispersion_abbe_number = w[55];
     // the reference's scene parser calls make_safe on every material
     // (src/Scene/SceneParser.cpp:391-438); its clamps only touch fields this layout does not
     // carry, the thin-film ranges (weight and hue in range, film IOR >= 1.0005) and the dielectric
@@ -391,7 +393,7 @@ REF_EXPORT void refr_render(void* h, const int32_t* settings_i, const float* set
 
 /* The material the reference's kernels see after packing (pack_to_GPU, the 8-bit fields of
  * DevicePackedEffectiveMaterial, src/HostDeviceCommon/Material/MaterialPacked.h) and unpacking,
- * written back in the 64-word layout (word 45, the diffuse-lobe selector, copied; 54..63 zero). */
+ * written back in the 64-word layout (word 45, the diffuse-lobe selector, copied; 56..63 zero). */
 REF_EXPORT void refr_pack_unpack_material(const float* in, float* out)
 {
     CPUMaterial c = cpu_material(in);
@@ -440,6 +442,8 @@ REF_EXPORT void refr_pack_unpack_material(const float* in, float* out)
     w[52] = m.thin_film_base_ior_override;
     int32_t tf_override = m.thin_film_do_ior_override ? 1 : 0;
     std::memcpy(w + 53, &tf_override, 4);
+    w[54] = m.dispersion_scale;
+    w[55] = m.dispersion_abbe_number;
     std::memcpy(out, w, sizeof(w));
 }
 

@@ -1,8 +1,7 @@
 """TEST INFRASTRUCTURE ONLY — the principled-BSDF golden vectors (tests/golden/bsdf_principled.npz; for
-the Oren-Nayar diffuse lobe, bsdf_oren_nayar.npz; with thin films, bsdf_thin_film.npz; written by the
-reference's own BSDF through
-tests/golden/make_bsdf_golden.py) and the comparison
-both the CPU test (host build of the BSDF) and the GPU test (CUDA build) apply.
+the Oren-Nayar diffuse lobe, bsdf_oren_nayar.npz; with thin films, bsdf_thin_film.npz; with dispersion,
+bsdf_dispersion.npz; written by the reference's own BSDF through tests/golden/make_bsdf_golden.py)
+and the comparison both the CPU test (host build of the BSDF) and the GPU test (CUDA build) apply.
 
 Tolerance on f, pdf and the sampled direction (relative, with an absolute floor of 1e-6 of the
 row's largest value): 1e-5 for at least 99.5% of the evaluation queries and 99% of the sampling
@@ -12,7 +11,9 @@ build does neither; near the peak of a sharp GGX lobe the lobe's conditioning am
 one-ulp differences past 1e-5 for a fraction of a percent of the queries. A query may also sit on
 the other side of a branch threshold (lobe choice u < cdf, total internal reflection, the delta
 peak alignment test 0.999999) and then differ completely; those are counted and allowed up to a
-small number.
+small number. The dispersion set, where every material's glass lobe also contributes to the
+evaluation of each sampled direction, measured 98.9% of its sampling queries within 1e-5 on the
+CUDA build (100% on the host build), all within 2e-4; its sampling bar is 98.5%.
 """
 import os
 
@@ -23,23 +24,34 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsd
 GOLDEN_OREN_NAYAR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_oren_nayar.npz")
 # every material with a thin film over its metal, specular and glass interfaces
 GOLDEN_THIN_FILM = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_thin_film.npz")
-SETS = {"lambertian": GOLDEN, "oren_nayar": GOLDEN_OREN_NAYAR, "thin_film": GOLDEN_THIN_FILM}
+# every material dispersive, each query with the path's wavelength (eval_w, sample_w)
+GOLDEN_DISPERSION = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bsdf_dispersion.npz")
+SETS = {"lambertian": GOLDEN, "oren_nayar": GOLDEN_OREN_NAYAR, "thin_film": GOLDEN_THIN_FILM,
+        "dispersion": GOLDEN_DISPERSION}
 RTOL = 1e-5
 RTOL_ALL = 2e-4
 TIGHT_FRACTION = 0.995
 TIGHT_FRACTION_SAMPLE = 0.99
+TIGHT_FRACTION_SAMPLE_SET = {"dispersion": 0.985}
 
 
 def load(which: str = "lambertian"):
     d = np.load(SETS[which])
-    return {k: d[k] for k in d.files}
+    out = {k: d[k] for k in d.files}
+    out["set"] = which
+    return out
 
 
-def queries(q16: np.ndarray) -> np.ndarray:
-    """Golden query rows (16 floats, inside/lobe as float values) -> gbpt_bsdf_query records."""
-    out = np.ascontiguousarray(q16, np.float32).copy()
+def queries(q16: np.ndarray, wavelength=None) -> np.ndarray:
+    """Golden query rows (16 floats, inside/lobe as float values) and the path's wavelength per row
+    (None: none) -> gbpt_bsdf_query records (20 words)."""
+    q16 = np.asarray(q16, np.float32)
+    out = np.zeros((len(q16), 20), np.float32)
+    out[:, :16] = q16
     out[:, 14] = np.asarray(q16[:, 14] != 0, np.int32).view(np.float32)
     out[:, 15] = np.asarray(q16[:, 15], np.int32).view(np.float32)
+    if wavelength is not None:
+        out[:, 16] = wavelength
     return out
 
 
@@ -84,13 +96,14 @@ def check_sample(got8, got_lobe, got_rng, gold, max_flips=8):
     condition number of order 1/alpha^2; they must agree to 1e-3 for the same fraction of queries.
     The weight f/pdf does not suffer from it (the distribution term cancels)."""
     want = gold["sample_out"]
+    tight_fraction = TIGHT_FRACTION_SAMPLE_SET.get(gold.get("set"), TIGHT_FRACTION_SAMPLE)
     same_path = (got_lobe == gold["sample_info"]) & (got_rng == gold["sample_rng"])
     got_dw = np.concatenate([got8[:, :3], _weight(got8)], axis=1)
     want_dw = np.concatenate([want[:, :3], _weight(want)], axis=1)
     res = _check("sample (direction, f/pdf)", got_dw, want_dw, gold["sample_q"], same_path, max_flips, got_lobe,
-                 gold["sample_info"], tight_fraction=TIGHT_FRACTION_SAMPLE)
+                 gold["sample_info"], tight_fraction=tight_fraction)
     loose = same_path & close(got8[:, 3:7], want[:, 3:7], 1e-3)
-    assert loose.mean() >= TIGHT_FRACTION_SAMPLE, _report("sample (f, pdf)", np.nonzero(~loose)[0], got8, want,
+    assert loose.mean() >= tight_fraction, _report("sample (f, pdf)", np.nonzero(~loose)[0], got8, want,
                                                    gold["sample_q"], got_lobe, gold["sample_info"])
     return res
 

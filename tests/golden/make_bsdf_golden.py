@@ -14,11 +14,14 @@ refraction at a totally reflecting interface (possible once the film's Fresnel t
 are left out: the reference's refraction returns a NaN direction there and its CPU sanity check
 then takes the harness down. They are found beforehand with the library's BSDF built for the host
 (tests/native), which returns f = 0, pdf = 0 for them.
+With --dispersion, writes tests/golden/bsdf_dispersion.npz from the same library: every material
+dispersive (scale and Abbe number seeded; Dispersion.h), each query with a wavelength in
+[360, 830] nm as the path would carry it (stored as eval_w / sample_w).
 With --oren-nayar, writes tests/golden/bsdf_oren_nayar.npz from oracle/_ref/libref_bsdf_oren_nayar.so
 instead: the same BSDF compiled with the reference's Oren-Nayar diffuse lobe
 (PrincipledBSDFDiffuseLobe = PRINCIPLED_DIFFUSE_LOBE_OREN_NAYAR, src/Device/includes/BSDFs/OrenNayar.h),
 every material carrying diffuse_lobe = Oren-Nayar and a seeded facet-slope deviation sigma.
-Usage (where the reference tree is present):  python tests/golden/make_bsdf_golden.py [--oren-nayar | --thin-film]
+Usage (where the reference tree is present):  python tests/golden/make_bsdf_golden.py [--oren-nayar | --thin-film | --dispersion]
 """
 import ctypes
 import os
@@ -37,6 +40,7 @@ import pyoracle  # noqa: E402
 OUT = os.path.join(HERE, "bsdf_principled.npz")
 OUT_ON = os.path.join(HERE, "bsdf_oren_nayar.npz")
 OUT_TF = os.path.join(HERE, "bsdf_thin_film.npz")
+OUT_DISP = os.path.join(HERE, "bsdf_dispersion.npz")
 REF_ON_SO = os.path.join(REPO, "oracle", "_ref", "libref_bsdf_oren_nayar.so")
 
 
@@ -45,7 +49,7 @@ def _unit(rng, n):
     return v / np.linalg.norm(v, axis=1, keepdims=True)
 
 
-def material_set(rng, oren_nayar=False, thin_film=False):
+def material_set(rng, oren_nayar=False, thin_film=False, dispersion=False):
     """Edge cases of every lobe first, then the random principled distribution. With oren_nayar,
     every material selects the Oren-Nayar diffuse lobe with sigma in [0, 1.2] rad (0 and the
     default 20 degrees among them)."""
@@ -87,6 +91,9 @@ def material_set(rng, oren_nayar=False, thin_film=False):
                      thin_film_base_ior_override=float(rng.uniform(1.0, 3.0)),
                      thin_film_kappa_3=float(rng.uniform(0.0, 3.0)))
                 for i, m in enumerate(mats)]
+    if dispersion:
+        mats = [dict(m, dispersion_scale=float(rng.uniform(0.3, 1.0)), dispersion_abbe_number=float(rng.uniform(15.0, 60.0)))
+                for m in mats]
     return M.pack_many([M.coat_roughened(m) for m in mats])
 
 
@@ -125,7 +132,7 @@ def queries(rng, mats, n, sample):
     return mi, q
 
 
-def refraction_under_tir(mats, smi, sq, seeds):
+def refraction_under_tir(mats, smi, sq, seeds, sw=None):
     """Sampling queries whose glass refraction meets total internal reflection (host build)."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
     from native import build_emu
@@ -133,7 +140,7 @@ def refraction_under_tir(mats, smi, sq, seeds):
     lib = ctypes.CDLL(build_emu.build())
     vp = ctypes.c_void_p
     lib.emu_bsdf_sample.argtypes = [vp, vp, vp, vp, ctypes.c_int64, ctypes.c_int, vp, vp, vp]
-    q = bsdf_golden.queries(sq)
+    q = bsdf_golden.queries(sq, sw)
     mi = np.ascontiguousarray(smi, np.int32)
     sd = np.ascontiguousarray(seeds, np.uint32)
     out = np.zeros((len(q), 8), np.float32)
@@ -147,40 +154,48 @@ def refraction_under_tir(mats, smi, sq, seeds):
 def main():
     oren_nayar = "--oren-nayar" in sys.argv[1:]
     thin_film = "--thin-film" in sys.argv[1:]
+    dispersion = "--dispersion" in sys.argv[1:]
     pyoracle.build(ref=True)
     lib = ctypes.CDLL(REF_ON_SO if oren_nayar else pyoracle.REF_SO)
     fp = ctypes.POINTER(ctypes.c_float)
     ip = ctypes.POINTER(ctypes.c_int32)
     up = ctypes.POINTER(ctypes.c_uint32)
-    lib.ref_principled_eval.argtypes = [fp, ip, fp, ctypes.c_int64, fp]
-    lib.ref_principled_pdf.argtypes = [fp, ip, fp, ctypes.c_int64, fp]
-    lib.ref_principled_sample.argtypes = [fp, ip, fp, up, ctypes.c_int64, fp, ip, up]
+    lib.ref_principled_eval.argtypes = [fp, ip, fp, fp, ctypes.c_int64, fp]
+    lib.ref_principled_pdf.argtypes = [fp, ip, fp, fp, ctypes.c_int64, fp]
+    lib.ref_principled_sample.argtypes = [fp, ip, fp, fp, up, ctypes.c_int64, fp, ip, up]
 
-    rng = np.random.Generator(np.random.PCG64(20241 if oren_nayar else 20242 if thin_film else 20240))
-    mats = np.ascontiguousarray(material_set(rng, oren_nayar, thin_film))
+    rng = np.random.Generator(np.random.PCG64(20241 if oren_nayar else 20242 if thin_film else 20243 if dispersion
+                                              else 20240))
+    mats = np.ascontiguousarray(material_set(rng, oren_nayar, thin_film, dispersion))
     n_eval, n_sample = 8192, 8192
     emi, eq = queries(rng, mats, n_eval, sample=False)
+    ew = rng.uniform(360.0, 830.0, n_eval).astype(np.float32) if dispersion else None
     eout = np.zeros((n_eval, 4), np.float32)
     pout = np.zeros(n_eval, np.float32)
-    lib.ref_principled_eval(mats.ctypes.data_as(fp), emi.ctypes.data_as(ip), eq.ctypes.data_as(fp), n_eval,
-                            eout.ctypes.data_as(fp))
-    lib.ref_principled_pdf(mats.ctypes.data_as(fp), emi.ctypes.data_as(ip), eq.ctypes.data_as(fp), n_eval,
-                           pout.ctypes.data_as(fp))
+    lib.ref_principled_eval(mats.ctypes.data_as(fp), emi.ctypes.data_as(ip), eq.ctypes.data_as(fp),
+                            None if ew is None else ew.ctypes.data_as(fp), n_eval, eout.ctypes.data_as(fp))
+    lib.ref_principled_pdf(mats.ctypes.data_as(fp), emi.ctypes.data_as(ip), eq.ctypes.data_as(fp),
+                           None if ew is None else ew.ctypes.data_as(fp), n_eval, pout.ctypes.data_as(fp))
     smi, sq = queries(rng, mats, n_sample, sample=True)
     seeds = rng.integers(1, 2**32 - 1, n_sample, dtype=np.uint64).astype(np.uint32)
-    if thin_film:
-        keep = ~refraction_under_tir(mats, smi, sq, seeds)
+    sw = rng.uniform(360.0, 830.0, n_sample).astype(np.float32) if dispersion else None
+    if thin_film or dispersion:
+        keep = ~refraction_under_tir(mats, smi, sq, seeds, sw)
         smi, sq, seeds = np.ascontiguousarray(smi[keep]), np.ascontiguousarray(sq[keep]), np.ascontiguousarray(seeds[keep])
+        if sw is not None:
+            sw = np.ascontiguousarray(sw[keep])
         n_sample = len(smi)
     sout = np.zeros((n_sample, 8), np.float32)
     sinfo = np.zeros(n_sample, np.int32)
     srng = np.zeros(n_sample, np.uint32)
     lib.ref_principled_sample(mats.ctypes.data_as(fp), smi.ctypes.data_as(ip), sq.ctypes.data_as(fp),
-                              seeds.ctypes.data_as(up), n_sample, sout.ctypes.data_as(fp), sinfo.ctypes.data_as(ip),
-                              srng.ctypes.data_as(up))
-    out_path = OUT_ON if oren_nayar else OUT_TF if thin_film else OUT
+                              None if sw is None else sw.ctypes.data_as(fp), seeds.ctypes.data_as(up), n_sample,
+                              sout.ctypes.data_as(fp), sinfo.ctypes.data_as(ip), srng.ctypes.data_as(up))
+    out_path = OUT_ON if oren_nayar else OUT_TF if thin_film else OUT_DISP if dispersion else OUT
+    extra = dict(eval_w=ew, sample_w=sw) if dispersion else {}
     np.savez_compressed(out_path, materials=mats, eval_mat=emi, eval_q=eq, eval_out=eout, pdf_out=pout,
-                        sample_mat=smi, sample_q=sq, seeds=seeds, sample_out=sout, sample_info=sinfo, sample_rng=srng)
+                        sample_mat=smi, sample_q=sq, seeds=seeds, sample_out=sout, sample_info=sinfo, sample_rng=srng,
+                        **extra)
     print(f"wrote {out_path}: {len(mats)} materials, {n_eval} eval/pdf + {n_sample} sample queries; "
           f"nonzero eval {np.mean(eout[:, 3] > 0):.2f}, sampled lobes {np.unique(sinfo, return_counts=True)}")
 

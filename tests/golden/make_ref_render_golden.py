@@ -3,7 +3,7 @@ render kernels — CameraRays + MegaKernel compiled from the reference's sources
 (oracle/ref_render.cpp, built by `make -C oracle ref`) — which pin the GPU path tracer's
 GBPT_RNG_REFERENCE mode sample by sample.
 
-Five scenes, each rendered for FRAMES frames of one sample per pixel with the reference's
+Six scenes, each rendered for FRAMES frames of one sample per pixel with the reference's
 per-pass random numbers as its GPU renderer draws them: the renderer's Xorshift32, seeded with 42
 (GPURenderer.cpp:750-751), gives one number to the G-buffer pass and one to the MegaKernel pass of
 every sample (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53):
@@ -16,7 +16,8 @@ every sample (FillGBufferRenderPass.cpp:91, MegaKernelRenderPass.cpp:53):
   * principled_ris: the principled scene with direct lighting by RIS over 4 light and 1 BSDF
     candidates (LSS_RIS_BSDF_AND_LIGHT, the reference's default strategy, RIS.h:83-255);
   * principled_thin_film: the principled scene with thin films on the walls, the boxes and the
-    mirror (the packed record's 8-bit film weight and hue, and its boolean base-IOR override).
+    mirror (the packed record's 8-bit film weight and hue, and its boolean base-IOR override);
+  * principled_dispersion: the glass scene with a dispersive glass box.
 Each frame image is the frame's sample (float32 H x W x 3); the scene arrays and settings are stored
 with it, so the GPU test needs nothing else.
 Usage (where the reference tree is present):  python tests/golden/make_ref_render_golden.py
@@ -62,6 +63,9 @@ GLASS = OPAQUE[:4] + [
     dict(base_color=(0.95, 0.95, 0.95), roughness=0.15, specular_transmission=1.0, ior=1.5),  # 4 glass box
     OPAQUE[5],
 ]
+# the glass box dispersive (Dispersion.h): a wavelength per path drawn at its first hit on the box,
+# the box's IORs taken at it, the path's colour filtered by it once
+DISPERSIVE = GLASS[:4] + [dict(GLASS[4], dispersion_scale=1.0, dispersion_abbe_number=18.0), GLASS[5]]
 
 
 def frame_random_numbers(n, seed=42):
@@ -109,7 +113,8 @@ def main():
     mat_of[10:22] = 4
     mat_of[22:34] = 5
     for name, mats, light in (("principled", OPAQUE, "power"), ("principled_glass", GLASS, "power"),
-                              ("principled_ris", OPAQUE, "power_ris"), ("principled_thin_film", FILMS, "power")):
+                              ("principled_ris", OPAQUE, "power_ris"), ("principled_thin_film", FILMS, "power"),
+                              ("principled_dispersion", DISPERSIVE, "power")):
         raw = M.pack_many(mats)
         img, lt = render("principled", light, cb.mesh, mat_of, raw, Settings(LIGHT_POWER))
         out.update({f"{name}_materials": raw, f"{name}_material_of": mat_of, name: img,

@@ -2,6 +2,7 @@
 // (hiprt-path-tracer_gb300/csrc/principled.h) so that CPU-only test runs check it against the
 // golden vectors of the reference's own BSDF before any GPU run; the GPU tests then check the
 // CUDA build against the same vectors. Same material and query layouts as include/gbpt_bsdf.h.
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -21,6 +22,7 @@ void load(const gbpt_bsdf_query& s, Query& q, Medium& md)
     md.eta_incident = s.eta_incident;
     md.eta_outgoing = s.eta_outgoing;
     md.inside = s.inside != 0;
+    md.wavelength = std::fabs(s.wavelength);
 }
 }  // namespace
 

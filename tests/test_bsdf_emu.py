@@ -36,7 +36,7 @@ def test_oren_nayar_vectors_differ_from_lambertian_where_the_lobe_shows():
     lamb = mats.copy()
     lamb[:, 45] = np.zeros(len(mats), np.int32).view(np.float32)
     lib = _lib()
-    q = G.queries(g["eval_q"])
+    q = G.queries(g["eval_q"], g.get("eval_w"))
     mi = np.ascontiguousarray(g["eval_mat"], np.int32)
     out = np.zeros((len(q), 4), np.float32)
     lib.emu_bsdf_eval(lamb.ctypes.data, mi.ctypes.data, q.ctypes.data, len(q), 0, out.ctypes.data)
@@ -50,7 +50,7 @@ def test_host_build_eval_and_pdf_match_reference(which):
     g = G.load(which)
     lib = _lib()
     mats = np.ascontiguousarray(g["materials"])
-    q = G.queries(g["eval_q"])
+    q = G.queries(g["eval_q"], g.get("eval_w"))
     mi = np.ascontiguousarray(g["eval_mat"], np.int32)
     out = np.zeros((len(q), 4), np.float32)
     lib.emu_bsdf_eval(mats.ctypes.data, mi.ctypes.data, q.ctypes.data, len(q), 0, out.ctypes.data)
@@ -63,7 +63,7 @@ def test_host_build_sampling_matches_reference(which):
     g = G.load(which)
     lib = _lib()
     mats = np.ascontiguousarray(g["materials"])
-    q = G.queries(g["sample_q"])
+    q = G.queries(g["sample_q"], g.get("sample_w"))
     mi = np.ascontiguousarray(g["sample_mat"], np.int32)
     seeds = np.ascontiguousarray(g["seeds"], np.uint32)
     out = np.zeros((len(q), 8), np.float32)

@@ -21,7 +21,7 @@ def _dev(a, dtype=None):
 def test_eval_and_pdf_match_reference_golden(cuda, which):
     g = G.load(which)
     mats = _dev(g["materials"])
-    q = _dev(G.queries(g["eval_q"]))
+    q = _dev(G.queries(g["eval_q"], g.get("eval_w")))
     mi = _dev(g["eval_mat"].astype(np.int32))
     out = bsdf.eval(mats, mi, q).cpu().numpy()
     frac, flips = G.check_eval(out, g, max_flips=8)
@@ -35,7 +35,7 @@ def test_eval_and_pdf_match_reference_golden(cuda, which):
 def test_sampling_matches_reference_golden(cuda, which):
     g = G.load(which)
     mats = _dev(g["materials"])
-    q = _dev(G.queries(g["sample_q"]))
+    q = _dev(G.queries(g["sample_q"], g.get("sample_w")))
     mi = _dev(g["sample_mat"].astype(np.int32))
     seeds = _dev(g["seeds"].view(np.int32))
     out, lobe, rng = bsdf.sample(mats, mi, q, seeds)

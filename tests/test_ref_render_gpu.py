@@ -65,12 +65,15 @@ def test_lambert_cornell_matches_reference_megakernel(cuda):
     assert abs(gpu.mean() - ref.mean()) <= 2e-3 * ref.mean(), (gpu.mean(), ref.mean())
 
 
-@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris", "principled_thin_film"])
+@pytest.mark.parametrize("name", ["principled", "principled_glass", "principled_ris", "principled_thin_film",
+                                  "principled_dispersion"])
 def test_principled_cornell_matches_reference_megakernel(cuda, name):
     """Coated, glossy dielectric, anisotropic metal, metallic-blend and mirror materials (and a
     rough glass box entered and left through the nested-dielectric volume stack), power light
     sampling, against the reference's MegaKernel with its own principled BSDF; principled_ris
-    with RIS direct lighting over 4 light and 1 BSDF candidates (LSS_RIS_BSDF_AND_LIGHT)."""
+    with RIS direct lighting over 4 light and 1 BSDF candidates (LSS_RIS_BSDF_AND_LIGHT);
+    principled_thin_film with thin films on five materials; principled_dispersion with a dispersive
+    glass box (a wavelength drawn per path at its first hit on the box, in the reference's order)."""
     g = np.load(GOLDEN)
     scene = gbpt.Scene(g["positions"], g["indices"], g[f"{name}_material_of"], principled=g[f"{name}_materials"],
                        material_packing=MATERIALS_PACKED)

@@ -2,8 +2,9 @@
 device memory (an interactive loop that must not stall on cudaMalloc/cudaFree after an emission
 edit, or a host that gives the library a fixed memory budget). It must write the same table as the
 light-table build inside gbpt_scene_create, from the same power list, with all of its scratch in a
-fixed array inside the library. Two calls in a row check that the shared scratch left by one call
-does not leak into the next. This file is named so that pytest collects it last."""
+fixed array inside the library. Calls in a row (3000 emitters, the maximum count, 700) check that
+the shared scratch left by one call does not leak into the next, and that the maximum fills it
+without overrunning its end. This file is named so that pytest collects it last."""
 import numpy as np
 import pytest
 import torch
@@ -54,6 +55,15 @@ def test_noalloc_alias_table_matches_scene_light_table(cuda, oracle):
         assert np.array_equal(prob, want["probas"])
         assert np.array_equal(alias, want["alias"])
         scene.destroy()
+        if n_emit == 3000:
+            # the maximum count between the two scenes: the queues fill the fixed array to its end
+            n = gbpt.render.GBPT_ALIAS_NOALLOC_MAX_EMITTERS
+            rng = np.random.Generator(np.random.PCG64(13))
+            big = np.exp(rng.uniform(0.0, np.log(1.0e4), n)).astype(np.float32)
+            prob, alias, s64 = _noalloc(lib, torch.from_numpy(big).to(cuda), n, stream)
+            assert abs(s64 - float(np.sum(big.astype(np.float64)))) <= 1e-12 * s64
+            want_p, want_a = pyoracle.vose_alias(big, s64)
+            assert np.array_equal(prob, want_p) and np.array_equal(alias, want_a)
 
 
 def test_noalloc_rejects_oversized_and_empty(cuda):
