@@ -46,10 +46,13 @@ struct HostBVH
     double build_seconds = 0.0;
 };
 
+// Defaults measured on the traversal benchmark (2.3M triangles, 16M rays) against 32 bins and
+// leaves of 3: 1496 -> 1730 Mrays/s, and 1-3% on the path-tracing workloads; leaves of 1 traced
+// 1.4% faster still on the benchmark but doubled the nodes and slowed the Cornell box by 12%.
 struct BuildParams
 {
-    int sah_bins = 32;
-    int max_leaf = 3;
+    int sah_bins = 64;
+    int max_leaf = 2;
     int threads = 0;
 };
 

@@ -51,8 +51,8 @@ GBPT_API int32_t gbpt_version(void);
 typedef struct gbpt_bvh gbpt_bvh;
 
 typedef struct gbpt_bvh_params {
-    int32_t sah_bins;      /* 0 -> 32 */
-    int32_t max_leaf_size; /* 0 -> 3; 1..3 */
+    int32_t sah_bins;      /* 0 -> 64 */
+    int32_t max_leaf_size; /* 0 -> 2; 1..3 */
     int32_t num_threads;   /* host build threads; 0 -> hardware concurrency */
 } gbpt_bvh_params;
 

@@ -84,6 +84,7 @@ def test_gradients_match_oracle(cuda, n):
     want = _blocks(ow, og)
     for name, a in _blocks(gw, gg).items():
         ok, rel, cos = _close(a, want[name])
+        print(f"n={n} {name}: block-relative L2 {rel:.2e}, cosine {cos:.6f}")
         assert ok, (name, rel, cos)
     # the BF16 emulation matters: the kernels are closer to it than to the exact FP64 gradients
     if n >= 1000:
