@@ -13,8 +13,9 @@ pytestmark = pytest.mark.gpu
 # normalisation of the lobe directions, by 1 / |raw direction| for the few samples whose raw
 # direction is short. Measured on the oracle by perturbing its inputs at FP32 precision with the
 # conditioned test network below: block-relative L2 error of the gradients up to 1.6e-2, the
-# output rows identical except for a few at 5e-3.
-GRAD_RTOL = 5e-2
+# output rows identical except for a few at 5e-3. On a GB300 the kernels' gradients measured at
+# most 2.3e-2 over the 20 blocks of the four batch sizes below; the bound is 1.5 times that.
+GRAD_RTOL = 3.5e-2
 GRAD_COS = 0.999
 ROW_ATOL, ROW_RTOL, ROW_FRACTION = 1e-3, 1e-2, 0.99
 
