@@ -46,13 +46,15 @@ struct HostBVH
     double build_seconds = 0.0;
 };
 
-// Defaults measured on the traversal benchmark (2.3M triangles, 16M rays) against 32 bins and
-// leaves of 3: 1496 -> 1730 Mrays/s, and 1-3% on the path-tracing workloads; leaves of 1 traced
-// 1.4% faster still on the benchmark but doubled the nodes and slowed the Cornell box by 12%.
+// Defaults measured on the traversal benchmark (2.3M triangles, 16M rays; Mrays/s): 32 bins with
+// binary leaves of 3 and the greedy collapse 1496, 64 bins with leaves of 2 (greedy) 1730, 64 bins
+// with leaves of 1 and the cost-optimal collapse (which merges up to 3 triangles per wide-node
+// leaf) 1805; the last is also the fastest on the path-tracing workloads (Cornell box 6% faster
+// than leaves of 2) and needs the fewest nodes. max_leaf bounds the binary tree's leaves.
 struct BuildParams
 {
     int sah_bins = 64;
-    int max_leaf = 2;
+    int max_leaf = 1;
     int threads = 0;
 };
 

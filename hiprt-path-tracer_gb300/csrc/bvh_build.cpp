@@ -1,4 +1,6 @@
-// Host BVH builder: binned SAH binary tree, collapsed to 8-wide quantised nodes.
+// Host BVH builder: binned SAH binary tree, collapsed to 8-wide quantised nodes by the
+// cost-optimal (dynamic-programming) collapse of the same paper, which also merges subtrees of up
+// to 3 triangles into one leaf where that costs less.
 //
 // Replaces the reference's GPU BVH build through HIPRT (hiprtBuildGeometry in
 // src/HIPRT-Orochi/HIPRTScene.h:87-150 of the reference, whose algorithm lives in the absent HIPRT
@@ -9,6 +11,7 @@
 #include "bvh.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -44,8 +47,9 @@ struct BNode
 {
     Box box;
     int32_t left = -1;  // right child = left + 1; -1 marks a leaf
-    int32_t begin = 0;
-    int32_t count = 0;
+    int32_t begin = 0;  // the subtree's triangles are idx[begin, begin + n_tris)
+    int32_t count = 0;  // triangles of a binary leaf (0 for an internal node)
+    int32_t n_tris = 0;
 };
 
 struct Builder
@@ -74,6 +78,8 @@ struct Builder
         }
         node.box = box;
         const int32_t count = end - begin;
+        node.begin = begin;
+        node.n_tris = count;
         if (count <= params.max_leaf)
         {
             node.begin = begin;
@@ -173,6 +179,12 @@ struct Builder
     }
 };
 
+// SAH weights of the wide collapse: a node visit against one triangle test. Measured on the
+// traversal benchmark (binary leaves of 1 triangle, 64 bins; Mrays/s): 0.3 -> 1784, 0.6 -> 1805,
+// 1.0 -> 1783 (Ylitie et al. use 0.3 with their triangle test).
+constexpr float kNodeCost = 1.0f;
+constexpr float kTriCost = 0.6f;
+
 struct Child
 {
     int32_t bnode;
@@ -249,6 +261,103 @@ std::string build_wide_bvh(const int32_t* indices, const float* positions, int64
     b.build(0, 0, n_valid);
     out.n_binary_nodes = b.next_node.load();
 
+    // ---- cost-optimal collapse to 8-wide nodes (Ylitie, Karras and Laine, HPG 2017, section 3):
+    // cost[n][i-1] is the least SAH cost of the subtree under binary node n spread over at most i
+    // slots of a wide node, where a slot holds a leaf of at most 3 triangles (area x kTriCost per
+    // triangle) or a wide node (area x kNodeCost plus its own 8 slots). Children are allocated
+    // after their parent, so descending index order visits children first.
+    const int32_t nb = (int32_t)out.n_binary_nodes;
+    std::vector<std::array<float, 8>> cost(nb);
+    std::vector<std::array<int8_t, 8>> split(nb);  // i = 1: 1 leaf / 0 wide node; i > 1: k (0: fewer slots)
+    for (int32_t n = nb - 1; n >= 0; n--)
+    {
+        const BNode& bn = b.nodes[n];
+        const float area = bn.box.half_area();
+        const float leaf = bn.n_tris <= kMaxLeafTriangles ? area * kTriCost * (float)bn.n_tris : INFINITY;
+        if (bn.left < 0)
+        {
+            cost[n].fill(leaf);
+            split[n].fill(0);
+            split[n][0] = 1;
+            continue;
+        }
+        const auto& cl = cost[bn.left];
+        const auto& cr = cost[bn.left + 1];
+        float dist[8];
+        int8_t arg[8];
+        for (int i = 2; i <= 8; i++)
+        {
+            dist[i - 1] = INFINITY;
+            arg[i - 1] = 0;
+            for (int k = 1; k < i; k++)
+            {
+                const float c = cl[k - 1] + cr[i - k - 1];
+                if (c < dist[i - 1])
+                {
+                    dist[i - 1] = c;
+                    arg[i - 1] = (int8_t)k;
+                }
+            }
+        }
+        const float wide = area * kNodeCost + dist[7];
+        cost[n][0] = std::min(leaf, wide);
+        split[n][0] = leaf <= wide ? 1 : 0;
+        for (int i = 2; i <= 8; i++)
+        {
+            if (dist[i - 1] < cost[n][i - 2])
+            {
+                cost[n][i - 1] = dist[i - 1];
+                split[n][i - 1] = arg[i - 1];
+            }
+            else
+            {
+                cost[n][i - 1] = cost[n][i - 2];
+                split[n][i - 1] = 0;
+            }
+        }
+    }
+    // the slots of the wide node of binary node n: its subtree spread over at most 8 slots
+    auto gather = [&](int32_t n, Child* kids) {
+        int nk = 0;
+        struct Item
+        {
+            int32_t node;
+            int slots;
+        };
+        Item stack[64];
+        int sp = 0;
+        const BNode& bn = b.nodes[n];
+        // the wide node itself distributes its 8 slots over its two children
+        int best_k = 1;
+        float best = INFINITY;
+        for (int k = 1; k < 8; k++)
+        {
+            const float c = cost[bn.left][k - 1] + cost[bn.left + 1][8 - k - 1];
+            if (c < best)
+            {
+                best = c;
+                best_k = k;
+            }
+        }
+        stack[sp++] = {bn.left + 1, 8 - best_k};
+        stack[sp++] = {bn.left, best_k};
+        while (sp > 0)
+        {
+            Item it = stack[--sp];
+            while (it.slots > 1 && split[it.node][it.slots - 1] == 0) it.slots--;
+            if (it.slots == 1)
+            {
+                kids[nk++] = {it.node, split[it.node][0] == 1};
+                continue;
+            }
+            const int k = split[it.node][it.slots - 1];
+            const int32_t l = b.nodes[it.node].left;
+            stack[sp++] = {l + 1, it.slots - k};
+            stack[sp++] = {l, k};
+        }
+        return nk;
+    };
+
     // ---- collapse to 8-wide, breadth first ----
     struct Pending
     {
@@ -272,34 +381,10 @@ std::string build_wide_bvh(const int32_t* indices, const float* positions, int64
 
         Child kids[8];
         int nk = 0;
-        if (bn.left < 0)
-        {
-            kids[nk++] = {pend.bnode, true};
-        }
+        if (bn.left < 0 || (pend.bnode == 0 && split[0][0] == 1))
+            kids[nk++] = {pend.bnode, true};  // the whole scene is one leaf
         else
-        {
-            kids[nk++] = {bn.left, b.nodes[bn.left].left < 0};
-            kids[nk++] = {bn.left + 1, b.nodes[bn.left + 1].left < 0};
-            while (nk < 8)
-            {
-                int best = -1;
-                float best_area = -1.0f;
-                for (int i = 0; i < nk; i++)
-                {
-                    if (kids[i].leaf) continue;
-                    float area = b.nodes[kids[i].bnode].box.half_area();
-                    if (area > best_area)
-                    {
-                        best_area = area;
-                        best = i;
-                    }
-                }
-                if (best < 0) break;
-                int32_t l = b.nodes[kids[best].bnode].left;
-                kids[best] = {l, b.nodes[l].left < 0};
-                kids[nk++] = {l + 1, b.nodes[l + 1].left < 0};
-            }
-        }
+            nk = gather(pend.bnode, kids);
 
         // Union box and octant slot assignment (greedy on the offset of each child's centre).
         Box ub;
@@ -385,10 +470,10 @@ std::string build_wide_bvh(const int32_t* indices, const float* positions, int64
             }
             if (kids[ci].leaf)
             {
-                uint32_t cnt = (uint32_t)cn.count;
+                uint32_t cnt = (uint32_t)cn.n_tris;
                 static const uint8_t unary[4] = {0, 1, 3, 7};
                 wn.meta[s] = (uint8_t)((unary[cnt] << 5) | tri_off);
-                for (int32_t k = 0; k < cn.count; k++) order_tris.push_back(b.idx[cn.begin + k]);
+                for (int32_t k = 0; k < cn.n_tris; k++) order_tris.push_back(b.idx[cn.begin + k]);
                 tri_off += cnt;
             }
             else

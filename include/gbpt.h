@@ -45,14 +45,17 @@ GBPT_API int32_t gbpt_version(void);
  * hiprtCreateGeometry + hiprtBuildGeometry over a hiprtTriangleMeshPrimitive
  * {indices, vertices} (src/HIPRT-Orochi/HIPRTScene.h:152-155), and its OOM retry path
  * (:118-139) which here becomes GBPT_ERROR_OOM.
- * Build: binned SAH (sah_bins bins, leaves of at most max_leaf_size <= 3 triangles), collapsed
- * to 8-wide nodes with 8-bit quantised child boxes (80 B per node), uploaded to the device.
+ * Build: binned SAH (sah_bins bins, leaves of at most max_leaf_size triangles), collapsed to
+ * 8-wide nodes by a cost-optimal dynamic program (leaves of up to 3 triangles), with 8-bit
+ * quantised child boxes (80 B per node), uploaded to the device.
  * ---------------------------------------------------------------------------------------- */
 typedef struct gbpt_bvh gbpt_bvh;
 
 typedef struct gbpt_bvh_params {
     int32_t sah_bins;      /* 0 -> 64 */
-    int32_t max_leaf_size; /* 0 -> 2; 1..3 */
+    int32_t max_leaf_size; /* 0 -> 1; 1..3: leaves of the binary SAH tree (the collapse to 8-wide
+                              nodes merges subtrees of up to 3 triangles into one leaf where
+                              that lowers the SAH cost) */
     int32_t num_threads;   /* host build threads; 0 -> hardware concurrency */
 } gbpt_bvh_params;
 
