@@ -3,7 +3,7 @@
 Workload (the traversal microbenchmark scene, FP32):
   scene   1024 x 1024-cell fBm heightfield (2,097,152 triangles, amplitude 0.2, 6 octaves, seed 1)
           + 200,000 random triangles (centres U([-1,1]x[0,0.5]x[-1,1]), vertex offsets N(0, 0.01^2))
-          = 2,297,152 triangles; binned SAH (64 bins, binary leaves of 1), cost-optimal collapse (leaves <= 3) collapsed to 8-wide nodes.
+          = 2,297,152 triangles; binned SAH (128 bins, binary leaves of 1), cost-optimal collapse (leaves <= 3) collapsed to 8-wide nodes.
   rays    16,777,216 per step: 8,388,608 primary (4096 x 2048 pinhole at (0,1.5,-2.5) aimed at the
           origin, 30 degree vertical FOV), 4,194,304 cosine-hemisphere bounce rays from primary hits,
           4,194,304 any-hit shadow rays to uniform points on a 0.5 x 0.5 quad at y = 2
@@ -53,7 +53,7 @@ TRI_BYTES = 36  # algorithmic: three float3 vertex records
 def workload_config(n_tris):
     return {"workload": "bvh-traversal-microbench", "triangles": n_tris, "rays_per_step": WIDTH * HEIGHT + N_BOUNCE + N_SHADOW,
             "primary": f"{WIDTH}x{HEIGHT} pinhole, vfov {VFOV} deg, emitted in 4x8-pixel tiles (8-row bands)", "bounce": N_BOUNCE, "shadow_any_hit": N_SHADOW,
-            "bvh": "binned SAH 64 bins, cost-optimal 8-wide collapse (leaves <= 3 tris), quantised (80 B nodes)",
+            "bvh": "binned SAH 128 bins, cost-optimal 8-wide collapse (leaves <= 3 tris), quantised (80 B nodes)",
             "l2": f"inputs larger than L2 ({(WIDTH * HEIGHT + N_BOUNCE + N_SHADOW) * RAY_IN_BYTES / 1e6:.0f} MB of rays per step); no flush"}
 
 

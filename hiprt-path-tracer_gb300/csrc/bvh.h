@@ -49,11 +49,12 @@ struct HostBVH
 // Defaults measured on the traversal benchmark (2.3M triangles, 16M rays; Mrays/s): 32 bins with
 // binary leaves of 3 and the greedy collapse 1496, 64 bins with leaves of 2 (greedy) 1730, 64 bins
 // with leaves of 1 and the cost-optimal collapse (which merges up to 3 triangles per wide-node
-// leaf) 1805; the last is also the fastest on the path-tracing workloads (Cornell box 6% faster
-// than leaves of 2) and needs the fewest nodes. max_leaf bounds the binary tree's leaves.
+// leaf) 1805, 128 bins 1884; the last is also the fastest on the path-tracing workloads (Cornell
+// box 7% faster than greedy leaves of 2) and needs the fewest nodes. max_leaf bounds the binary
+// tree's leaves.
 struct BuildParams
 {
-    int sah_bins = 64;
+    int sah_bins = 128;
     int max_leaf = 1;
     int threads = 0;
 };

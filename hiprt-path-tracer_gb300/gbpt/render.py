@@ -295,7 +295,7 @@ class World:
 
 
 class Scene:
-    def __init__(self, positions, indices, material_of_triangle, albedo=None, emission=None, stream=None, sah_bins=64,
+    def __init__(self, positions, indices, material_of_triangle, albedo=None, emission=None, stream=None, sah_bins=128,
                  max_leaf_size=1, principled=None, vertex_normals=None, material_packing=MATERIALS_FLOAT):
         """albedo/emission: (M, 3) plain materials; principled: (M, 64) gbpt.materials records (the
         reference's CPUMaterial parameters; base colour and emission come from them when albedo is

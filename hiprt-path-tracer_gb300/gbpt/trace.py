@@ -41,7 +41,7 @@ def hit_prim(hits):
 class BVH:
     """8-wide compressed BVH over a triangle mesh, resident on the current CUDA device."""
 
-    def __init__(self, indices: np.ndarray, positions: np.ndarray, sah_bins: int = 64, max_leaf_size: int = 1,
+    def __init__(self, indices: np.ndarray, positions: np.ndarray, sah_bins: int = 128, max_leaf_size: int = 1,
                  num_threads: int = 0):
         lib = _lib.load()
         idx = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1, 3)

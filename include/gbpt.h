@@ -52,7 +52,7 @@ GBPT_API int32_t gbpt_version(void);
 typedef struct gbpt_bvh gbpt_bvh;
 
 typedef struct gbpt_bvh_params {
-    int32_t sah_bins;      /* 0 -> 64 */
+    int32_t sah_bins;      /* 0 -> 128 */
     int32_t max_leaf_size; /* 0 -> 1; 1..3: leaves of the binary SAH tree (the collapse to 8-wide
                               nodes merges subtrees of up to 3 triangles into one leaf where
                               that lowers the SAH cost) */

@@ -26,7 +26,7 @@ def lib():
 
 
 class EmuBVH:
-    def __init__(self, mesh, max_leaf=1, bins=64):  # the library's defaults (csrc/bvh.h BuildParams)
+    def __init__(self, mesh, max_leaf=1, bins=128):  # the library's defaults (csrc/bvh.h BuildParams)
         self.idx = np.ascontiguousarray(mesh.indices, np.int32)
         self.pos = np.ascontiguousarray(mesh.positions, np.float32)
         self.h = lib().emu_build(self.idx.ctypes.data, self.pos.ctypes.data, self.pos.shape[0], self.idx.shape[0],
