@@ -16,6 +16,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <thread>
 
@@ -264,13 +265,11 @@ std::string build_wide_bvh(const int32_t* indices, const float* positions, int64
     // ---- cost-optimal collapse to 8-wide nodes (Ylitie, Karras and Laine, HPG 2017, section 3):
     // cost[n][i-1] is the least SAH cost of the subtree under binary node n spread over at most i
     // slots of a wide node, where a slot holds a leaf of at most 3 triangles (area x kTriCost per
-    // triangle) or a wide node (area x kNodeCost plus its own 8 slots). Children are allocated
-    // after their parent, so descending index order visits children first.
+    // triangle) or a wide node (area x kNodeCost plus its own 8 slots), solved children first.
     const int32_t nb = (int32_t)out.n_binary_nodes;
     std::vector<std::array<float, 8>> cost(nb);
     std::vector<std::array<int8_t, 8>> split(nb);  // i = 1: 1 leaf / 0 wide node; i > 1: k (0: fewer slots)
-    for (int32_t n = nb - 1; n >= 0; n--)
-    {
+    auto eval_node = [&](int32_t n) {
         const BNode& bn = b.nodes[n];
         const float area = bn.box.half_area();
         const float leaf = bn.n_tris <= kMaxLeafTriangles ? area * kTriCost * (float)bn.n_tris : INFINITY;
@@ -279,7 +278,7 @@ std::string build_wide_bvh(const int32_t* indices, const float* positions, int64
             cost[n].fill(leaf);
             split[n].fill(0);
             split[n][0] = 1;
-            continue;
+            return;
         }
         const auto& cl = cost[bn.left];
         const auto& cr = cost[bn.left + 1];
@@ -315,7 +314,33 @@ std::string build_wide_bvh(const int32_t* indices, const float* positions, int64
                 split[n][i - 1] = 0;
             }
         }
-    }
+    };
+    // children before parents; subtrees of more than 65536 triangles solve their two children on
+    // separate threads (as the binary build does)
+    std::atomic<int> dp_threads{1};
+    std::function<void(int32_t)> solve = [&](int32_t n) {
+        const BNode& bn = b.nodes[n];
+        if (bn.left >= 0)
+        {
+            if (bn.n_tris > 65536 && dp_threads.load() < b.max_threads)
+            {
+                dp_threads++;
+                std::thread t([&solve, &dp_threads, l = bn.left]() {
+                    solve(l);
+                    dp_threads--;
+                });
+                solve(bn.left + 1);
+                t.join();
+            }
+            else
+            {
+                solve(bn.left);
+                solve(bn.left + 1);
+            }
+        }
+        eval_node(n);
+    };
+    solve(0);
     // the slots of the wide node of binary node n: its subtree spread over at most 8 slots
     auto gather = [&](int32_t n, Child* kids) {
         int nk = 0;
